@@ -1,0 +1,417 @@
+#!/usr/bin/env python
+"""Benchmark of the MCPNet compute core on GB300.
+
+Metric (one JSON line on rank 0):
+  "MI gene-pairs/s + max-min Gop/s at n=20k: BF16-TC vs FP32 GPU, MI err<=1e-4"
+
+Workload (default): seeded synthetic GRN expression, 20,000 genes x 2,000
+samples, B-spline MI with 10 bins and spline order 3.
+  * ``value``  -- B-spline MI gene pairs per second (n(n-1)/2 per step), one
+    step = scale + weights + tensor-core contraction with the fused entropy
+    epilogue, inputs resident in HBM, timed with CUDA events on the library's
+    stream; W >= 3 untimed warm-up steps.  Working set (X 160 MB, weights
+    1.6 GB, MI 1.6 GB) is larger than the 129 MB L2, so no flush is needed.
+  * ``e2e``    -- the same metric through the host C ABI (mcpg_bspline_mi with
+    pinned host buffers: host->device copy of X and device->host copy of MI
+    inside the timed region).
+  * ``maxmin`` -- the FP32 max-min product A (x) M1 (the second product of
+    MCP3, a full n^3 non-symmetric product) in Gop/s (2 ops per triple), and
+    the MCP2 stage (symmetric A (x) A with the ratio fused) in ms.
+  * ``mi_fp32``-- the plain FP32 CUDA-core MI on the same input, and the
+    tensor-core speed-up over it.
+  * ``cpu_baseline`` -- the CPU oracle (a restatement of the reference's
+    OpenMP loops) on a bounded row slab of the same workload, all host cores.
+
+``--impl reference`` times the reference's CPU implementation of the path (the
+oracle's restatement on this host; the compiled reference where it was built
+for this machine) on bounded samples, and prints the same metric.
+
+Multi-GPU (``torchrun --nproc-per-node N``): the path has no exchange step on
+one node's replicas; every rank runs the same workload on its own GPU
+("replicas only"), and value sums the ranks' work over the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "MI gene-pairs/s + max-min Gop/s at n=20k: BF16-TC vs FP32 GPU, MI err≤1e-4"
+UNIT = "gene-pairs/s"
+
+
+# ---------------------------------------------------------------- helpers
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except FileNotFoundError:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.flush()
+        rows = []
+        for line in Path(self.f.name).read_text().splitlines():
+            p = [x.strip() for x in line.split(",")]
+            if len(p) >= 9:
+                rows.append(p)
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in rows if num(r[1])]
+        mx = [num(r[2]) for r in rows if num(r[2])]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows),
+                "power_w_max": max((num(r[3]) or 0.0) for r in rows)}
+
+
+def reduce_max(x: float, ws: int) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws: int):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+# ---------------------------------------------------------------- CPU legs
+def cpu_mi_sample(n: int, m: int, target_s: float, seed: int):
+    """Time the CPU oracle's MI (the reference's float loops restated, OpenMP
+    over rows) on a row slab of the n x m workload; returns (pairs/s, info)."""
+    from oracle import oracle as O
+    import mcpnet_gb300 as M
+    P = O.port()
+    X = M.synth_grn(n, m, seed=seed)
+    W = P.bspline_weights(X)
+    t0 = time.perf_counter()
+    P.bspline_mi_rows(W, m, 0, 1)
+    t1 = time.perf_counter()
+    per_row = max(t1 - t0, 1e-4)
+    rows = int(max(1, min(n, target_s / per_row)))
+    t0 = time.perf_counter()
+    P.bspline_mi_rows(W, m, 0, rows)
+    dt = time.perf_counter() - t0
+    pairs = rows * n
+    return pairs / dt, {"rows": rows, "pairs": pairs, "seconds": dt, "threads": P.threads()}
+
+
+def reference_arm(args, ws, rank):
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    O.port()
+    kind = "port"
+    vals = []
+    info = {}
+    for i in range(args.warmup + args.steps):
+        v, info = cpu_mi_sample(args.genes, args.samples, args.ref_seconds, args.seed)
+        if i >= args.warmup:
+            vals.append(v)
+    value = float(np.mean(vals))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": workload_config(args, "fp32-cpu"),
+        "ms_per_step": info["seconds"] * 1e3,
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": info["threads"], "kind": kind,
+                         "sample": f"MI of rows 0..{info['rows']} x all {args.genes} genes "
+                                   f"({info['pairs']} pairs) per step, m={args.samples}, float, "
+                                   "OpenMP over rows (reference loops restated in oracle/)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def workload_config(args, precision):
+    return {"workload": f"bspline-mi {args.genes} genes x {args.samples} samples, {args.bins} bins, order "
+                        f"{args.order}, {precision}; max-min products at n={args.genes}",
+            "genes": args.genes, "samples": args.samples, "bins": args.bins, "order": args.order,
+            "precision": precision, "seed": args.seed, "parallelism": "replicas",
+            "l2": "inputs larger than L2 (weights and MI matrices >> 129 MB); no flush"}
+
+
+# ---------------------------------------------------------------- GPU arm
+def gpu_arm(args, ws, rank, local):
+    import torch
+    import mcpnet_gb300 as M
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    n, m = args.genes, args.samples
+    pairs = n * (n - 1) // 2
+    X_host = M.synth_grn(n, m, seed=args.seed)
+    X = torch.from_numpy(X_host).to(dev)
+    MI = torch.empty((n, n), dtype=torch.float32, device=dev)
+    h = M.Handle(local)
+    stream = torch.cuda.current_stream(dev)
+    h.set_stream(stream.cuda_stream)
+
+    def mi_step(prec):
+        h.bspline_mi_dev(X, MI, args.bins, args.order, prec)
+
+    # ---- warm-up ----
+    for _ in range(args.warmup):
+        mi_step(args.precision)
+    torch.cuda.synchronize(dev)
+
+    # ---- timed MI (value) ----
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = h.kernel_launches
+    h.profile(True)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier(ws)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for a, b in evs:
+        a.record(stream)
+        mi_step(args.precision)
+        b.record(stream)
+    torch.cuda.synchronize(dev)
+    barrier(ws)
+    wall = time.perf_counter() - t0
+    prof = h.profile_report()
+    h.profile(False)
+    launches = h.kernel_launches - launches0
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    dev_s = sum(step_ms) / 1e3
+    dev_s_max = reduce_max(dev_s, ws)
+    value = ws * pairs * args.steps / dev_s_max
+    clk = clocks.stop()
+
+    # dominant kernel of the MI step and its roofline
+    kname = "mi_fp32" if args.precision == "fp32" else "mi_tc"
+    kern = prof.get(kname, {"launches": 0, "ms": float("nan")})
+    k_ms = kern["ms"] / max(kern["launches"], 1)
+    flops = 2.0 * args.bins * args.bins * m * pairs  # algorithmic: 2 b^2 m per unordered pair
+    peaks = {}
+    pk = ROOT / "MEASURED_PEAKS.json"
+    if pk.exists():
+        peaks = json.loads(pk.read_text())
+    props = torch.cuda.get_device_properties(dev)
+    sms = props.multi_processor_count
+    f_max = float(peaks.get("sm_max_mhz", 2070.0)) * 1e6
+    if args.precision == "fp32":
+        peak_tf = sms * 128 * 2 * f_max / 1e12
+        peak_src = f"FP32 FMA peak = {sms} SMs x 128 lanes x 2 x {f_max/1e6:.0f} MHz (computed)"
+        bound = "fp32-alu"
+    else:
+        peak_tf = float(peaks.get("bf16_tflops", 1900.0))
+        peak_src = "MEASURED_PEAKS.json bf16_tflops (burst, of measured)" if "bf16_tflops" in peaks \
+            else "fallback 1.9 PFLOP/s"
+        bound = "tensor"
+    achieved_tf = flops / (k_ms / 1e3) / 1e12
+    roofline = {"bound": bound, "kernel": kname, "achieved": achieved_tf, "peak": peak_tf, "unit": "TFLOP/s",
+                "frac": achieved_tf / peak_tf, "traffic": None, "peak_source": peak_src,
+                "kernel_ms": k_ms, "algorithmic_flop_per_launch": flops,
+                "note": "achieved counts 2*b^2*m flops per unordered gene pair; the hi+lo split issues 3x "
+                        "that on the tensor pipe"}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dev_s / args.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16" if args.precision.startswith("bf16") else ("f16" if args.precision.startswith("fp16")
+                                                                   else "f32"),
+        "data": "synthetic (seeded SEM GRN, in-degree ~ Poisson(2), weights +-U(0.5,1.5))",
+        "config": workload_config(args, args.precision),
+        "clocks": clk, "gpu_launches": launches, "roofline": roofline,
+        "kernel_profile": prof, "wall_s": wall, "sms": sms,
+    }
+
+    # ---- plain FP32 GPU MI on the same input ----
+    if args.precision != "fp32" and not args.no_fp32:
+        mi_step("fp32")
+        torch.cuda.synchronize(dev)
+        MI_tc = None
+        ts = []
+        for _ in range(args.fp32_steps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            mi_step("fp32")
+            b.record(stream)
+            b.synchronize()
+            ts.append(a.elapsed_time(b))
+        MI32 = MI.clone()
+        mi_step(args.precision)
+        torch.cuda.synchronize(dev)
+        diff = float((MI - MI32).abs().max().item())
+        f_ms = float(np.mean(ts))
+        line["mi_fp32"] = {"ms": f_ms, "pairs_per_s": pairs / (f_ms / 1e3),
+                           "speedup_tc_vs_fp32": f_ms / (dev_s / args.steps * 1e3),
+                           "max_abs_diff_vs_tc_bits": diff}
+
+    # ---- max-min products ----
+    if not args.no_maxmin:
+        A = MI
+        h.set_diagonal_dev(A, 0.0)
+        M1 = torch.empty_like(A)
+        R = torch.empty_like(A)
+        C = torch.empty_like(A)
+        h.maxmin_dev(A, A, M1)  # symmetric A (x) A
+        torch.cuda.synchronize(dev)
+        # A (x) M1: full non-symmetric product (MCP3's second product)
+        h.profile(True)
+        ts = []
+        for _ in range(args.maxmin_steps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            h.maxmin_dev(A, M1, C)
+            b.record(stream)
+            b.synchronize()
+            ts.append(a.elapsed_time(b))
+        mm_prof = h.profile_report()
+        h.profile(False)
+        mm_ms = float(np.mean(ts))
+        ops = 2.0 * n * n * n
+        gops = ops / (mm_ms / 1e3) / 1e9
+        alu_peak = sms * 128 * f_max / 1e9
+        med = clk.get("sm_mhz") or None
+        line["maxmin"] = {"gops": gops, "ms": mm_ms, "n": n, "product": "A (x) M1, full n^3",
+                          "alu_peak_gops_at_max_clock": alu_peak,
+                          "frac_alu_peak_at_max_clock": gops / alu_peak,
+                          "alu_peak_note": f"{sms} SMs x 128 lanes x {f_max/1e6:.0f} MHz, 1 FP32 op/lane/clk; "
+                                           "algorithmic 2 ops (min, max) per triple",
+                          "kernel_profile": mm_prof}
+        if med:
+            line["maxmin"]["frac_alu_peak_at_median_clock"] = gops / (sms * 128 * med * 1e6 / 1e9)
+        # MCP2 stage: symmetric A (x) A with the ratio fused
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        h.mcp_dev(A, 2, M=None, R=R)
+        b.record(stream)
+        b.synchronize()
+        line["maxmin"]["mcp2_ms"] = a.elapsed_time(b)
+        del M1, R, C
+
+    # ---- end to end through the host C ABI ----
+    if not args.no_e2e:
+        Xp = torch.empty((n, m), dtype=torch.float32, pin_memory=True)
+        Xp.numpy()[:] = X_host
+        MIp = torch.empty((n, n), dtype=torch.float32, pin_memory=True)
+        xa, ma = Xp.numpy(), MIp.numpy()
+        import ctypes as C
+        L = M.lib()
+        pr = M.PRECISIONS[args.precision]
+
+        def host_call():
+            rc = L.mcpg_bspline_mi(h._h, xa.ctypes.data, n, m, m, args.bins, args.order, pr, ma.ctypes.data, n, None)
+            if rc:
+                raise M.MCPGError(rc, L.mcpg_last_error(h._h).decode())
+        host_call()
+        barrier(ws)
+        ts = []
+        for _ in range(args.e2e_steps):
+            t0 = time.perf_counter()
+            host_call()
+            ts.append(time.perf_counter() - t0)
+        e_s = reduce_max(float(np.mean(ts)), ws)
+        line["e2e"] = {"value": ws * pairs / e_s, "unit": UNIT, "h2d_bytes_per_step": n * m * 4,
+                       "d2h_bytes_per_step": n * n * 4, "ms_per_step": e_s * 1e3,
+                       "api": "mcpg_bspline_mi (host buffers, pinned)"}
+
+    # ---- CPU baseline (rank 0, N = 1 only) ----
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        v, info = cpu_mi_sample(n, m, args.cpu_seconds, args.seed)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": info["threads"], "kind": "port",
+                                "sample": f"MI of rows 0..{info['rows']} x all {n} genes ({info['pairs']} pairs), "
+                                          f"m={m}, float, {info['seconds']:.1f} s; reference loops restated "
+                                          "in oracle/ (OpenMP over rows)"}
+    h.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="mcpgpu", choices=["mcpgpu", "reference"])
+    ap.add_argument("--genes", type=int, default=20000)
+    ap.add_argument("--samples", type=int, default=2000)
+    ap.add_argument("--bins", type=int, default=10)
+    ap.add_argument("--order", type=int, default=3)
+    ap.add_argument("--precision", default="bf16x3", choices=["fp32", "bf16", "bf16x3", "fp16", "fp16x3"])
+    ap.add_argument("--seed", type=int, default=20260001)
+    ap.add_argument("--fp32-steps", type=int, default=2)
+    ap.add_argument("--maxmin-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--ref-seconds", type=float, default=10.0)
+    ap.add_argument("--no-fp32", action="store_true")
+    ap.add_argument("--no-maxmin", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args(argv)
+    if args.warmup < 3:
+        args.warmup = 3  # timing rule: at least 3 warm-up steps
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo" if args.impl == "reference" else "nccl")
+    try:
+        if args.impl == "reference":
+            reference_arm(args, ws, rank)
+        else:
+            gpu_arm(args, ws, rank, local)
+    finally:
+        if ws > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,179 @@
+/*
+ * mcpgpu -- GB300 (sm_103a) implementation of MCPNet's compute core behind a
+ * plain C ABI: B-spline mutual information, max-min (maximum-capacity path)
+ * products with the MCP ratio, the DPI filter and the max-capacity closure.
+ *
+ * Conventions
+ *  - Matrices are row-major with an explicit leading dimension (elements), the
+ *    layout of MCPNet's splash::ds::aligned_matrix (rows may be padded).
+ *  - Every call returns an int status (MCPG_OK == 0, negative on error) and
+ *    never aborts; mcpg_last_error() gives the message of the last failure on
+ *    that handle.
+ *  - Host-buffer entry points (no suffix) take HOST pointers, copy in, compute
+ *    and copy out; they return when the results are in the caller's buffers.
+ *  - Device entry points (suffix _dev) take DEVICE pointers and are
+ *    asynchronous on the handle's stream (mcpg_set_stream); call
+ *    mcpg_synchronize() before reading results.  Scalars they return (removed
+ *    counts, iteration counts) are read back synchronously.
+ *  - A handle is not thread-safe: one host thread, one CUDA stream per handle.
+ *    The library owns the device scratch memory of a handle.
+ *  - MI is in bits (log2), as in the reference.
+ *
+ * Reference interfaces replaced (paths relative to the MCPNet source tree):
+ *  each function names the reference functor / helper whose whole-matrix
+ *  application it performs.
+ */
+#ifndef MCPGPU_H
+#define MCPGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define MCPG_API __attribute__((visibility("default")))
+#else
+#define MCPG_API
+#endif
+
+typedef struct mcpg_handle mcpg_handle;
+
+/* ---- status codes ---- */
+#define MCPG_OK 0
+#define MCPG_ERR_ARG (-1)           /* bad argument: null pointer, bad shape, bad enum */
+#define MCPG_ERR_OOM (-2)           /* device or host allocation failed */
+#define MCPG_ERR_CUDA (-3)          /* a CUDA runtime/driver call failed */
+#define MCPG_ERR_NOT_CONVERGED (-4) /* closure still changing after max_iter products */
+#define MCPG_ERR_UNSUPPORTED (-5)   /* feature unavailable on this device / build */
+#define MCPG_ERR_DEVICE_TIMEOUT (-6)/* a bounded device-side wait gave up */
+
+/* ---- MI contraction precision (mcpg_bspline_mi*) ---- */
+#define MCPG_MI_FP32 0   /* FP32 weights, FP32 CUDA-core contraction */
+#define MCPG_MI_BF16 1   /* weights rounded once to BF16, tcgen05 tensor cores, FP32 accumulate */
+#define MCPG_MI_BF16X3 2 /* hi+lo BF16 split: hi*hi' + hi*lo' + lo*hi' on tcgen05 */
+#define MCPG_MI_FP16 3   /* weights rounded once to FP16, tcgen05 */
+#define MCPG_MI_FP16X3 4 /* hi+lo FP16 split on tcgen05 */
+
+/* ---- library / handle ---- */
+MCPG_API int mcpg_version(void);
+MCPG_API const char* mcpg_status_string(int status);
+MCPG_API int mcpg_create(mcpg_handle** out, int device);
+MCPG_API int mcpg_destroy(mcpg_handle* h);
+MCPG_API const char* mcpg_last_error(const mcpg_handle* h);
+MCPG_API int mcpg_set_stream(mcpg_handle* h, void* cuda_stream);
+MCPG_API int mcpg_synchronize(mcpg_handle* h);
+/* Number of kernels this handle has launched since creation (instrumentation). */
+MCPG_API int64_t mcpg_kernel_launches(const mcpg_handle* h);
+/* Per-kernel timing: with profiling on, the handle records CUDA events around
+ * every kernel it launches.  mcpg_profile() (re)starts or stops recording and
+ * clears what was recorded; mcpg_profile_report() synchronizes the stream and
+ * writes {"<kernel>": {"launches": L, "ms": T}, ...} into buf, returning the
+ * bytes needed (including the terminating NUL). */
+MCPG_API int mcpg_profile(mcpg_handle* h, int enable);
+MCPG_API int64_t mcpg_profile_report(mcpg_handle* h, char* buf, int64_t len);
+
+/* ---- B-spline mutual information ----
+ * Replaces compute_mi (apps/pipeline/mcpnet_helper.hpp:56-99): MinMaxScale
+ * (include/mcp/correlation/BSplineMI.hpp:74-116) -> BSplineWeightsKernel
+ * (:119-274) -> InnerProduct<BSplineMIKernel, SYMM=true> (:276-500).
+ * X: n genes x m samples (ldx >= m).  MI: n x n (ldmi >= n), symmetric, bits.
+ * H (nullable): n per-gene marginal entropies in bits, computed in FP64.
+ * bins >= order >= 1, bins <= 32; order in 1..8. */
+MCPG_API int mcpg_bspline_mi(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_t ldx,
+                             int bins, int order, int precision,
+                             float* MI, int64_t ldmi, double* H);
+MCPG_API int mcpg_bspline_mi_dev(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_t ldx,
+                                 int bins, int order, int precision,
+                                 float* MI, int64_t ldmi, double* H);
+
+/* ---- B-spline weights alone (the Transform<BSplineWeightsKernel> step) ----
+ * Whole-matrix BSplineWeightsKernel (BSplineMI.hpp:248-273) after MinMaxScale,
+ * as mcpnet_helper.hpp:58-80.  W: n rows of bins*m+1 floats in the reference's
+ * own row layout W[g][a*m + s], with W[g][bins*m] = H_g (FP64 value rounded to
+ * float).  H (nullable): FP64 marginal entropies.  The weights are bit-identical
+ * to the reference's float weights when the reference is built without FMA
+ * contraction. */
+MCPG_API int mcpg_bspline_weights(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_t ldx,
+                                  int bins, int order, float* W, double* H);
+MCPG_API int mcpg_bspline_weights_dev(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_t ldx,
+                                      int bins, int order, float* W, double* H);
+
+/* ---- max-min product ----
+ * C[i][j] = max_k min(A[i][k], B[j][k]), i < rows, j < cols, k < k_len: the
+ * whole-matrix application of mcp2_maxmin_kernel<float,false,true>
+ * (include/mcp/filter/mcp.hpp:72-93) under splash InnerProduct(A, B).
+ * Bit-exact (every output is one of the inputs).  Empty k range gives -inf. */
+MCPG_API int mcpg_maxmin(mcpg_handle* h, const float* A, int64_t lda, const float* B, int64_t ldb,
+                         int64_t rows, int64_t cols, int64_t k_len, float* C, int64_t ldc);
+MCPG_API int mcpg_maxmin_dev(mcpg_handle* h, const float* A, int64_t lda, const float* B, int64_t ldb,
+                             int64_t rows, int64_t cols, int64_t k_len, float* C, int64_t ldc);
+
+/* ---- MCP ratio ----
+ * R = ratio_kernel<float,float>(A, M) (include/mcp/transform/combine.hpp:210-222):
+ * |a| < FLT_EPSILON -> 0; |m| < FLT_EPSILON -> FLT_MAX; else (float)(a / m). */
+MCPG_API int mcpg_ratio(mcpg_handle* h, const float* A, int64_t lda, const float* M, int64_t ldm,
+                        int64_t rows, int64_t cols, float* R, int64_t ldr);
+MCPG_API int mcpg_ratio_dev(mcpg_handle* h, const float* A, int64_t lda, const float* M, int64_t ldm,
+                            int64_t rows, int64_t cols, float* R, int64_t ldr);
+
+/* ---- diagonal reset (apps/pipeline/mcpnet.cpp:299-308) ----
+ * A[i][i] = value for i < min(rows, cols); a negative value leaves A untouched. */
+MCPG_API int mcpg_set_diagonal_dev(mcpg_handle* h, float* A, int64_t rows, int64_t cols, int64_t lda, float value);
+
+/* ---- MCP scores of path length 2, 3 or 4 ----
+ * A: n x n MI matrix with its diagonal already set (0 in the reference default).
+ * path_len 2: M = A (x) A                       compute_mcp2 (mcpnet_helper.hpp:199-206)
+ * path_len 3: M = A (x) (A (x) A)               compute_mcp3 (mcpnet_helper.hpp:271-278)
+ *             symmetrize != 0 additionally takes max(M, M^T) as the mcp app
+ *             does (apps/filter/mcp.cpp:463-476)
+ * path_len 4: M = (A (x) A) (x) (A (x) A)       compute_mcp4 (mcpnet_helper.hpp:358-365)
+ * maxmin_out (nullable) receives M, ratio_out (nullable) receives ratio(A, M). */
+MCPG_API int mcpg_mcp(mcpg_handle* h, const float* A, int64_t n, int64_t lda, int path_len, int symmetrize,
+                      float* maxmin_out, int64_t ldm, float* ratio_out, int64_t ldr);
+MCPG_API int mcpg_mcp_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, int path_len, int symmetrize,
+                          float* maxmin_out, int64_t ldm, float* ratio_out, int64_t ldr);
+
+/* ---- DPI filter ----
+ * dpi_kernel<float> (include/mcp/filter/dpi.hpp:42-69) over all (x, z), then
+ * mask<float,true> (include/mcp/filter/threshold.hpp:33-54), as apps/filter/dpi.cpp:236-287.
+ * tol is the float tolerance of `dpi --single`; the multiplier 1/(1-tol) is
+ * formed in double.  out = deleted ? 0 : A; mask (nullable, n*n bytes, row-major)
+ * gets 1 for deleted entries; removed (nullable) gets the reference's
+ * "Mask removing N elements" count. */
+MCPG_API int mcpg_dpi(mcpg_handle* h, const float* A, int64_t n, int64_t lda, float tol,
+                      float* out, int64_t ldo, uint8_t* mask, int64_t* removed);
+MCPG_API int mcpg_dpi_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, float tol,
+                          float* out, int64_t ldo, uint8_t* mask, int64_t* removed);
+
+/* ---- maximum-capacity closure (no counterpart routine in the reference) ----
+ * Repeated squaring B <- max(B, B (x) B) from B = A until no entry changes,
+ * with (x) the reference's max_of_pairmin (include/mcp/filter/simd_maxmin.hpp:30-46).
+ * A must be symmetric.  iterations (nullable) gets the number of products.
+ * Returns MCPG_ERR_NOT_CONVERGED (out holds the last iterate) if max_iter
+ * products did not reach the fixed point. */
+MCPG_API int mcpg_closure(mcpg_handle* h, const float* A, int64_t n, int64_t lda, int max_iter,
+                          float* out, int64_t ldo, int* iterations);
+MCPG_API int mcpg_closure_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, int max_iter,
+                              float* out, int64_t ldo, int* iterations);
+
+/* ---- testing hook: make the next `count` device scratch allocations of this
+ * handle fail with MCPG_ERR_OOM (exercises the error path without a GPU fault). */
+MCPG_API int mcpg_test_fail_allocs(mcpg_handle* h, int count);
+
+/* ---- seeded synthetic GRN expression (host only; no device work) ----
+ * Random DAG over a random topological order, in-degree ~ Poisson(2) from
+ * earlier genes, weights +-U(0.5,1.5); x_g = tanh(sum w x_parent) + N(0, 0.3^2),
+ * roots ~ N(0,1); each gene min-max rescaled to [0,1].  X: n x m (ldx >= m).
+ * edges (nullable, capacity max_edges pairs of int32 parent,child) receives the
+ * ground-truth DAG; n_edges (nullable) gets the edge count. */
+MCPG_API int mcpg_synth_grn(int64_t n, int64_t m, uint64_t seed, float* X, int64_t ldx,
+                            int32_t* edges, int64_t max_edges, int64_t* n_edges);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MCPGPU_H */

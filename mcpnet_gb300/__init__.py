@@ -1,0 +1,292 @@
+"""mcpnet_gb300 -- GB300 (sm_103a) implementation of MCPNet's compute core.
+
+Python host mirror of the C ABI in include/mcpgpu.h (libmcpgpu.so, built
+in-tree by ``python -m mcpnet_gb300.build``).  The operations mirror MCPNet's
+helper-level calls (apps/pipeline/mcpnet_helper.hpp):
+
+=====================  =====================================================
+``bspline_mi``          compute_mi           (mcpnet_helper.hpp:56-99)
+``bspline_weights``     Transform<BSplineWeightsKernel> (mcpnet_helper.hpp:67-80)
+``maxmin``              InnerProduct<mcp2_maxmin_kernel> (filter/mcp.hpp:72-93)
+``ratio``               compute_ratio        (mcpnet_helper.hpp:172-184)
+``mcp``                 compute_mcp2/3/4     (mcpnet_helper.hpp:199-365)
+``dpi``                 the dpi app's mask + apply (apps/filter/dpi.cpp:236-287)
+``closure``             max-capacity closure by repeated squaring (no reference routine)
+=====================  =====================================================
+
+Host calls take and return numpy arrays (``float32``, C-contiguous rows);
+``*_dev`` calls take torch CUDA tensors and run asynchronously on the handle's
+stream.  There is no CPU fallback: without the built library or a GPU these
+raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "_lib" / "libmcpgpu.so"
+
+OK, ERR_ARG, ERR_OOM, ERR_CUDA, ERR_NOT_CONVERGED, ERR_UNSUPPORTED, ERR_DEVICE_TIMEOUT = 0, -1, -2, -3, -4, -5, -6
+PRECISIONS = {"fp32": 0, "bf16": 1, "bf16x3": 2, "fp16": 3, "fp16x3": 4}
+
+# (name, restype, argtypes) of every exported symbol -- the full C ABI.
+_i64, _f32p, _f64p, _vp = C.c_int64, C.POINTER(C.c_float), C.POINTER(C.c_double), C.c_void_p
+ABI = [
+    ("mcpg_version", C.c_int, []),
+    ("mcpg_status_string", C.c_char_p, [C.c_int]),
+    ("mcpg_create", C.c_int, [C.POINTER(_vp), C.c_int]),
+    ("mcpg_destroy", C.c_int, [_vp]),
+    ("mcpg_last_error", C.c_char_p, [_vp]),
+    ("mcpg_set_stream", C.c_int, [_vp, _vp]),
+    ("mcpg_synchronize", C.c_int, [_vp]),
+    ("mcpg_kernel_launches", C.c_int64, [_vp]),
+    ("mcpg_test_fail_allocs", C.c_int, [_vp, C.c_int]),
+    ("mcpg_profile", C.c_int, [_vp, C.c_int]),
+    ("mcpg_profile_report", C.c_int64, [_vp, C.c_char_p, C.c_int64]),
+    ("mcpg_bspline_mi", C.c_int, [_vp, _vp, _i64, _i64, _i64, C.c_int, C.c_int, C.c_int, _vp, _i64, _vp]),
+    ("mcpg_bspline_mi_dev", C.c_int, [_vp, _vp, _i64, _i64, _i64, C.c_int, C.c_int, C.c_int, _vp, _i64, _vp]),
+    ("mcpg_bspline_weights", C.c_int, [_vp, _vp, _i64, _i64, _i64, C.c_int, C.c_int, _vp, _vp]),
+    ("mcpg_bspline_weights_dev", C.c_int, [_vp, _vp, _i64, _i64, _i64, C.c_int, C.c_int, _vp, _vp]),
+    ("mcpg_maxmin", C.c_int, [_vp, _vp, _i64, _vp, _i64, _i64, _i64, _i64, _vp, _i64]),
+    ("mcpg_maxmin_dev", C.c_int, [_vp, _vp, _i64, _vp, _i64, _i64, _i64, _i64, _vp, _i64]),
+    ("mcpg_ratio", C.c_int, [_vp, _vp, _i64, _vp, _i64, _i64, _i64, _vp, _i64]),
+    ("mcpg_ratio_dev", C.c_int, [_vp, _vp, _i64, _vp, _i64, _i64, _i64, _vp, _i64]),
+    ("mcpg_set_diagonal_dev", C.c_int, [_vp, _vp, _i64, _i64, _i64, C.c_float]),
+    ("mcpg_mcp", C.c_int, [_vp, _vp, _i64, _i64, C.c_int, C.c_int, _vp, _i64, _vp, _i64]),
+    ("mcpg_mcp_dev", C.c_int, [_vp, _vp, _i64, _i64, C.c_int, C.c_int, _vp, _i64, _vp, _i64]),
+    ("mcpg_dpi", C.c_int, [_vp, _vp, _i64, _i64, C.c_float, _vp, _i64, _vp, C.POINTER(C.c_int64)]),
+    ("mcpg_dpi_dev", C.c_int, [_vp, _vp, _i64, _i64, C.c_float, _vp, _i64, _vp, C.POINTER(C.c_int64)]),
+    ("mcpg_closure", C.c_int, [_vp, _vp, _i64, _i64, C.c_int, _vp, _i64, C.POINTER(C.c_int)]),
+    ("mcpg_closure_dev", C.c_int, [_vp, _vp, _i64, _i64, C.c_int, _vp, _i64, C.POINTER(C.c_int)]),
+    ("mcpg_synth_grn", C.c_int, [_i64, _i64, C.c_uint64, _vp, _i64, _vp, _i64, C.POINTER(C.c_int64)]),
+]
+
+_lib = None
+
+
+class MCPGError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"mcpgpu status {status}: {msg}")
+        self.status = status
+
+
+def lib() -> C.CDLL:
+    """Load libmcpgpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with `python -m mcpnet_gb300.build` "
+                               "(there is no CPU fallback)")
+        L = C.CDLL(str(LIB_PATH))
+        for name, res, args in ABI:
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _ptr(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data
+
+
+def _f32(a) -> np.ndarray:
+    a = np.asarray(a, dtype=np.float32)
+    return a if a.flags.c_contiguous else np.ascontiguousarray(a)
+
+
+def synth_grn(n: int, m: int, seed: int = 20260001, with_edges: bool = False):
+    """Seeded synthetic GRN expression (n genes x m samples, float32 in [0, 1])."""
+    X = np.empty((n, m), dtype=np.float32)
+    ne = C.c_int64(0)
+    rc = lib().mcpg_synth_grn(n, m, seed, _ptr(X), m, None, 0, C.byref(ne))
+    if rc:
+        raise MCPGError(rc, "synth_grn failed")
+    if not with_edges:
+        return X
+    E = np.empty((max(ne.value, 1), 2), dtype=np.int32)
+    rc = lib().mcpg_synth_grn(n, 0, seed, None, 1, _ptr(E), ne.value, C.byref(ne))
+    if rc:
+        raise MCPGError(rc, "synth_grn failed")
+    return X, E[: ne.value]
+
+
+class Handle:
+    """One device, one stream.  Not thread-safe (as the C handle)."""
+
+    def __init__(self, device: int = 0):
+        self._L = lib()
+        h = C.c_void_p()
+        rc = self._L.mcpg_create(C.byref(h), device)
+        if rc:
+            raise MCPGError(rc, f"mcpg_create(device={device}) failed: "
+                            f"{self._L.mcpg_status_string(rc).decode()}")
+        self._h = h
+        self.device = device
+
+    # -- plumbing --
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.mcpg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, rc: int, what: str):
+        if rc:
+            raise MCPGError(rc, f"{what}: {self._L.mcpg_last_error(self._h).decode()}")
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(self._L.mcpg_kernel_launches(self._h))
+
+    def set_stream(self, stream_ptr: int):
+        self._check(self._L.mcpg_set_stream(self._h, stream_ptr), "set_stream")
+
+    def synchronize(self):
+        self._check(self._L.mcpg_synchronize(self._h), "synchronize")
+
+    def profile(self, enable: bool = True):
+        """Start (clearing) or stop per-kernel CUDA-event timing."""
+        self._check(self._L.mcpg_profile(self._h, int(enable)), "profile")
+
+    def profile_report(self) -> dict:
+        import json
+        need = self._L.mcpg_profile_report(self._h, None, 0)
+        if need < 0:
+            self._check(int(need), "profile_report")
+        buf = C.create_string_buffer(int(need))
+        self._L.mcpg_profile_report(self._h, buf, need)
+        return json.loads(buf.value.decode())
+
+    def fail_next_allocs(self, count: int):
+        self._check(self._L.mcpg_test_fail_allocs(self._h, count), "test_fail_allocs")
+
+    # -- host-buffer entry points --
+    def bspline_mi(self, X, bins: int = 10, order: int = 3, precision: str = "fp32", return_H: bool = False):
+        X = _f32(X)
+        n, m = X.shape
+        MI = np.empty((n, n), dtype=np.float32)
+        H = np.empty(n, dtype=np.float64) if return_H else None
+        self._check(self._L.mcpg_bspline_mi(self._h, _ptr(X), n, m, m, bins, order, PRECISIONS[precision],
+                                             _ptr(MI), n, _ptr(H)), "bspline_mi")
+        return (MI, H) if return_H else MI
+
+    def bspline_weights(self, X, bins: int = 10, order: int = 3):
+        X = _f32(X)
+        n, m = X.shape
+        W = np.empty((n, bins * m + 1), dtype=np.float32)
+        H = np.empty(n, dtype=np.float64)
+        self._check(self._L.mcpg_bspline_weights(self._h, _ptr(X), n, m, m, bins, order, _ptr(W), _ptr(H)),
+                    "bspline_weights")
+        return W, H
+
+    def maxmin(self, A, B=None):
+        A = _f32(A)
+        same = B is None
+        B = A if same else _f32(B)
+        rows, k = A.shape
+        cols = B.shape[0]
+        if B.shape[1] != k:
+            raise ValueError("maxmin: A and B need the same number of columns")
+        Cm = np.empty((rows, cols), dtype=np.float32)
+        self._check(self._L.mcpg_maxmin(self._h, _ptr(A), k, _ptr(B), k, rows, cols, k, _ptr(Cm), cols), "maxmin")
+        return Cm
+
+    def ratio(self, A, M):
+        A, M = _f32(A), _f32(M)
+        rows, cols = A.shape
+        R = np.empty((rows, cols), dtype=np.float32)
+        self._check(self._L.mcpg_ratio(self._h, _ptr(A), cols, _ptr(M), cols, rows, cols, _ptr(R), cols), "ratio")
+        return R
+
+    def mcp(self, A, path_len: int, symmetrize: bool = False, want_maxmin: bool = True, want_ratio: bool = True):
+        A = _f32(A)
+        n = A.shape[0]
+        M = np.empty((n, n), dtype=np.float32) if want_maxmin else None
+        R = np.empty((n, n), dtype=np.float32) if want_ratio else None
+        self._check(self._L.mcpg_mcp(self._h, _ptr(A), n, n, path_len, int(symmetrize), _ptr(M), n, _ptr(R), n),
+                    "mcp")
+        return M, R
+
+    def dpi(self, A, tol: float = 0.1, want_mask: bool = False):
+        A = _f32(A)
+        n = A.shape[0]
+        out = np.empty((n, n), dtype=np.float32)
+        mask = np.empty((n, n), dtype=np.uint8) if want_mask else None
+        removed = C.c_int64(0)
+        self._check(self._L.mcpg_dpi(self._h, _ptr(A), n, n, tol, _ptr(out), n, _ptr(mask), C.byref(removed)), "dpi")
+        return out, mask, removed.value
+
+    def closure(self, A, max_iter: int = 64):
+        A = _f32(A)
+        n = A.shape[0]
+        out = np.empty((n, n), dtype=np.float32)
+        it = C.c_int(0)
+        rc = self._L.mcpg_closure(self._h, _ptr(A), n, n, max_iter, _ptr(out), n, C.byref(it))
+        if rc == ERR_NOT_CONVERGED:
+            return out, -1
+        self._check(rc, "closure")
+        return out, it.value
+
+    # -- device entry points (torch CUDA tensors, float32, row-major, stride(1) == 1) --
+    @staticmethod
+    def _dp(t):
+        return None if t is None else t.data_ptr()
+
+    @staticmethod
+    def _ld(t):
+        if t.dim() != 2 or t.stride(1) != 1:
+            raise ValueError("device matrices must be 2-D with unit column stride")
+        return t.stride(0)
+
+    def bspline_mi_dev(self, X, MI, bins=10, order=3, precision="fp32", H=None):
+        n, m = X.shape
+        self._check(self._L.mcpg_bspline_mi_dev(self._h, self._dp(X), n, m, self._ld(X), bins, order,
+                                                 PRECISIONS[precision], self._dp(MI), self._ld(MI), self._dp(H)),
+                    "bspline_mi_dev")
+
+    def maxmin_dev(self, A, B, Cm):
+        rows, k = A.shape
+        self._check(self._L.mcpg_maxmin_dev(self._h, self._dp(A), self._ld(A), self._dp(B), self._ld(B), rows,
+                                             B.shape[0], k, self._dp(Cm), self._ld(Cm)), "maxmin_dev")
+
+    def set_diagonal_dev(self, A, value: float):
+        self._check(self._L.mcpg_set_diagonal_dev(self._h, self._dp(A), A.shape[0], A.shape[1], self._ld(A), value),
+                    "set_diagonal_dev")
+
+    def mcp_dev(self, A, path_len, M=None, R=None, symmetrize=False):
+        n = A.shape[0]
+        self._check(self._L.mcpg_mcp_dev(self._h, self._dp(A), n, self._ld(A), path_len, int(symmetrize),
+                                          self._dp(M), self._ld(M) if M is not None else n,
+                                          self._dp(R), self._ld(R) if R is not None else n), "mcp_dev")
+
+    def dpi_dev(self, A, out, tol=0.1, mask=None):
+        n = A.shape[0]
+        removed = C.c_int64(0)
+        self._check(self._L.mcpg_dpi_dev(self._h, self._dp(A), n, self._ld(A), tol, self._dp(out), self._ld(out),
+                                          self._dp(mask), C.byref(removed)), "dpi_dev")
+        return removed.value
+
+    def closure_dev(self, A, out, max_iter=64):
+        n = A.shape[0]
+        it = C.c_int(0)
+        rc = self._L.mcpg_closure_dev(self._h, self._dp(A), n, self._ld(A), max_iter, self._dp(out), self._ld(out),
+                                      C.byref(it))
+        if rc == ERR_NOT_CONVERGED:
+            return -1
+        self._check(rc, "closure_dev")
+        return it.value

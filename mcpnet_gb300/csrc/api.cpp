@@ -1,0 +1,831 @@
+// C ABI of the mcpgpu library (include/mcpgpu.h): argument checking, device
+// scratch management, host<->device staging and the composition of the
+// kernels into MCPNet's helper-level operations (compute_mi, compute_mcp2/3/4,
+// the DPI filter).  No CPU fallback exists: every operation runs the CUDA
+// kernels or returns an error status.
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/mcpgpu.h"
+#include "internal.h"
+
+namespace mcpg {
+cudaError_t launch_bspline_weights_ref(const float* X, int64_t n, int64_t m, int64_t ldx, int bins, int order,
+                                       float* W, double* H, cudaStream_t stream, int64_t* launches);
+}
+
+namespace {
+
+enum Slot {
+    S_IN0 = 0,   // staged host input / aligned copy of input 0
+    S_IN1,       // staged host input 1
+    S_OUT0,      // staged output 0
+    S_OUT1,      // staged output 1
+    S_W0,        // weights (FP32 sample-major or 16-bit hi)
+    S_W1,        // weights lo
+    S_H,         // marginal entropies (double)
+    S_M1,        // intermediate max-min product
+    S_M2,        // second intermediate
+    S_SMALL,     // flags and counters
+    S_MASK,      // staged mask
+    NSLOTS
+};
+
+}  // namespace
+
+struct mcpg_handle {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::string err;
+    int64_t launches = 0;
+    void* buf[NSLOTS] = {};
+    size_t cap[NSLOTS] = {};
+    int fail_allocs = 0;  // test hook: number of upcoming scratch allocations to fail
+    // optional per-kernel timing (mcpg_profile): CUDA events around each launch
+    bool prof = false;
+    struct Span { const char* name; cudaEvent_t a, b; };
+    std::vector<Span> spans;
+};
+
+namespace {
+
+int fail(mcpg_handle* h, int code, const char* fmt, ...) {
+    char b[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(b, sizeof b, fmt, ap);
+    va_end(ap);
+    if (h) h->err = b;
+    return code;
+}
+
+int cuda_fail(mcpg_handle* h, cudaError_t e, const char* what) {
+    return fail(h, MCPG_ERR_CUDA, "%s: %s (%s)", what, cudaGetErrorString(e), cudaGetErrorName(e));
+}
+
+#define CK(h, expr, what)                                   \
+    do {                                                    \
+        cudaError_t _e = (expr);                            \
+        if (_e != cudaSuccess) return cuda_fail(h, _e, what); \
+    } while (0)
+
+// Grow-only scratch slot.
+int scratch(mcpg_handle* h, int slot, size_t bytes, void** out) {
+    if (bytes == 0) bytes = 16;
+    if (h->cap[slot] < bytes) {
+        if (h->buf[slot]) {
+            cudaStreamSynchronize(h->stream);
+            cudaFree(h->buf[slot]);
+            h->buf[slot] = nullptr;
+            h->cap[slot] = 0;
+        }
+        if (h->fail_allocs > 0) {
+            --h->fail_allocs;
+            return fail(h, MCPG_ERR_OOM, "device scratch allocation of %zu bytes failed (injected)", bytes);
+        }
+        void* p = nullptr;
+        cudaError_t e = cudaMalloc(&p, bytes);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(h, MCPG_ERR_OOM, "device scratch allocation of %zu bytes failed: %s", bytes,
+                        cudaGetErrorString(e));
+        }
+        h->buf[slot] = p;
+        h->cap[slot] = bytes;
+    }
+    *out = h->buf[slot];
+    return MCPG_OK;
+}
+
+inline bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
+inline int64_t round_up(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
+
+// Returns a device view of a rows x cols float matrix whose rows are 16-byte
+// aligned (lda % 4 == 0, base 16-byte aligned), copying into scratch if needed.
+int aligned_view(mcpg_handle* h, const float* A, int64_t lda, int64_t rows, int64_t cols, int slot,
+                 const float** out, int64_t* ld_out) {
+    if (aligned16(A) && (lda % 4) == 0) {
+        *out = A;
+        *ld_out = lda;
+        return MCPG_OK;
+    }
+    const int64_t ld = round_up(cols > 0 ? cols : 1, 4);
+    void* p;
+    int rc = scratch(h, slot, (size_t)(rows * ld) * sizeof(float), &p);
+    if (rc) return rc;
+    CK(h, mcpg::launch_copy2d(A, lda, (float*)p, ld, rows, cols, h->stream), "copy2d");
+    *out = (const float*)p;
+    *ld_out = ld;
+    return MCPG_OK;
+}
+
+// Records CUDA events around one launch when profiling is on.
+struct ProfScope {
+    mcpg_handle* h;
+    const char* name;
+    cudaEvent_t a = nullptr, b = nullptr;
+    ProfScope(mcpg_handle* h_, const char* n) : h(h_), name(n) {
+        if (h->prof && cudaEventCreate(&a) == cudaSuccess && cudaEventCreate(&b) == cudaSuccess)
+            cudaEventRecord(a, h->stream);
+    }
+    ~ProfScope() {
+        if (a && b) {
+            cudaEventRecord(b, h->stream);
+            h->spans.push_back({name, a, b});
+        }
+    }
+};
+#define PROF(h, name) ProfScope _prof_scope(h, name)
+
+int check_handle(mcpg_handle* h) {
+    if (!h) return MCPG_ERR_ARG;
+    cudaError_t e = cudaSetDevice(h->device);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaSetDevice");
+    return MCPG_OK;
+}
+
+// ---------------- staging helpers for the host entry points ----------------
+int stage_in(mcpg_handle* h, int slot, const float* src, int64_t ld_src, int64_t rows, int64_t cols, float** dev,
+             int64_t* ld_dev) {
+    const int64_t ld = round_up(cols > 0 ? cols : 1, 32);  // 128-byte rows
+    void* p;
+    int rc = scratch(h, slot, (size_t)(rows * ld) * sizeof(float), &p);
+    if (rc) return rc;
+    if (rows > 0 && cols > 0)
+        CK(h, cudaMemcpy2DAsync(p, ld * sizeof(float), src, ld_src * sizeof(float), cols * sizeof(float), rows,
+                                cudaMemcpyHostToDevice, h->stream),
+           "host-to-device copy");
+    *dev = (float*)p;
+    *ld_dev = ld;
+    return MCPG_OK;
+}
+
+int stage_out_alloc(mcpg_handle* h, int slot, int64_t rows, int64_t cols, float** dev, int64_t* ld_dev) {
+    const int64_t ld = round_up(cols > 0 ? cols : 1, 32);
+    void* p;
+    int rc = scratch(h, slot, (size_t)(rows * ld) * sizeof(float), &p);
+    if (rc) return rc;
+    *dev = (float*)p;
+    *ld_dev = ld;
+    return MCPG_OK;
+}
+
+int copy_out(mcpg_handle* h, float* dst, int64_t ld_dst, const float* src, int64_t ld_src, int64_t rows,
+             int64_t cols) {
+    if (!dst || rows <= 0 || cols <= 0) return MCPG_OK;
+    CK(h, cudaMemcpy2DAsync(dst, ld_dst * sizeof(float), src, ld_src * sizeof(float), cols * sizeof(float), rows,
+                            cudaMemcpyDeviceToHost, h->stream),
+       "device-to-host copy");
+    return MCPG_OK;
+}
+
+int finish(mcpg_handle* h) {
+    CK(h, cudaStreamSynchronize(h->stream), "stream synchronize");
+    return MCPG_OK;
+}
+
+// ---------------- device implementations ----------------
+int mi_dev(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_t ldx, int bins, int order, int precision,
+           float* MI, int64_t ldmi, double* H) {
+    if (n < 1 || m < 1) return fail(h, MCPG_ERR_ARG, "bspline_mi: need n >= 1 and m >= 1 (got %lld, %lld)",
+                                    (long long)n, (long long)m);
+    if (ldx < m || ldmi < n) return fail(h, MCPG_ERR_ARG, "bspline_mi: leading dimension too small");
+    if (!X || !MI) return fail(h, MCPG_ERR_ARG, "bspline_mi: null pointer");
+    if (bins < 1 || bins > 32 || order < 1 || order > 8 || bins < order)
+        return fail(h, MCPG_ERR_ARG, "bspline_mi: need 1 <= order <= bins <= 32, order <= 8 (got bins=%d order=%d)",
+                    bins, order);
+    if (precision < MCPG_MI_FP32 || precision > MCPG_MI_FP16X3)
+        return fail(h, MCPG_ERR_ARG, "bspline_mi: unknown precision %d", precision);
+    double* Hd = H;
+    if (!Hd) {
+        void* p;
+        int rc = scratch(h, S_H, (size_t)n * sizeof(double), &p);
+        if (rc) return rc;
+        Hd = (double*)p;
+    }
+    if (precision == MCPG_MI_FP32) {
+        if (bins > 12) return fail(h, MCPG_ERR_UNSUPPORTED, "bspline_mi FP32: bins > 12 not supported");
+        const int64_t ldwt = round_up(n, 16) * bins;
+        const int64_t m_pad = round_up(m, 16);
+        void* p;
+        int rc = scratch(h, S_W0, (size_t)(m_pad * ldwt) * sizeof(float), &p);
+        if (rc) return rc;
+        CK(h, cudaMemsetAsync(p, 0, (size_t)(m_pad * ldwt) * sizeof(float), h->stream), "memset weights");
+        {
+            PROF(h, "bspline_weights");
+            CK(h, mcpg::launch_bspline_weights_fp32(X, n, m, ldx, bins, order, (float*)p, ldwt, Hd, h->stream,
+                                                     &h->launches),
+               "bspline weights kernel");
+        }
+        {
+            PROF(h, "mi_fp32");
+            CK(h, mcpg::launch_mi_fp32((const float*)p, ldwt, Hd, n, m, bins, MI, ldmi, h->stream, &h->launches),
+               "MI FP32 kernel");
+        }
+        return MCPG_OK;
+    }
+    const int fmt = (precision == MCPG_MI_FP16 || precision == MCPG_MI_FP16X3) ? 1 : 0;
+    const int split = (precision == MCPG_MI_BF16X3 || precision == MCPG_MI_FP16X3) ? 1 : 0;
+    const int64_t ldw = round_up(m, 64);
+    const int64_t rows = round_up(n * bins, 256) + 256;  // whole tiles stay in bounds
+    void *hi, *lo = nullptr;
+    int rc = scratch(h, S_W0, (size_t)(rows * ldw) * 2, &hi);
+    if (rc) return rc;
+    if (split) {
+        rc = scratch(h, S_W1, (size_t)(rows * ldw) * 2, &lo);
+        if (rc) return rc;
+    }
+    // rows beyond n*bins must be zero (they are read by the last tiles)
+    const size_t tail = (size_t)((rows - n * bins) * ldw) * 2;
+    CK(h, cudaMemsetAsync((char*)hi + (size_t)(n * bins * ldw) * 2, 0, tail, h->stream), "memset weights");
+    if (lo) CK(h, cudaMemsetAsync((char*)lo + (size_t)(n * bins * ldw) * 2, 0, tail, h->stream), "memset weights");
+    {
+        PROF(h, "bspline_weights16");
+        CK(h, mcpg::launch_bspline_weights_16(X, n, m, ldx, bins, order, fmt, (uint16_t*)hi, (uint16_t*)lo, ldw, Hd,
+                                               h->stream, &h->launches),
+           "bspline weights kernel");
+    }
+    void* flag;
+    rc = scratch(h, S_SMALL, 64, &flag);
+    if (rc) return rc;
+    CK(h, cudaMemsetAsync(flag, 0, sizeof(int), h->stream), "memset flag");
+    cudaError_t e;
+    {
+        PROF(h, "mi_tc");
+            e = mcpg::launch_mi_tc((const uint16_t*)hi, (const uint16_t*)lo, ldw, Hd, n, m, bins, fmt, split, MI,
+                                           ldmi, (int*)flag, h->stream, &h->launches);
+    }
+    if (e == cudaErrorNotSupported)
+        return fail(h, MCPG_ERR_UNSUPPORTED, "bspline_mi tensor-core path: unsupported shape or device");
+    CK(h, e, "MI tensor-core kernel");
+    int timed_out = 0;
+    CK(h, cudaMemcpyAsync(&timed_out, flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream), "read flag");
+    CK(h, cudaStreamSynchronize(h->stream), "stream synchronize");
+    if (timed_out) return fail(h, MCPG_ERR_DEVICE_TIMEOUT, "MI tensor-core kernel: a bounded barrier wait gave up");
+    return MCPG_OK;
+}
+
+int maxmin_dev(mcpg_handle* h, const float* A, int64_t lda, const float* B, int64_t ldb, int64_t rows, int64_t cols,
+               int64_t k, float* C, int64_t ldc) {
+    if (rows < 0 || cols < 0 || k < 0) return fail(h, MCPG_ERR_ARG, "maxmin: negative size");
+    if (rows == 0 || cols == 0) return MCPG_OK;
+    if (!A || !B || !C) return fail(h, MCPG_ERR_ARG, "maxmin: null pointer");
+    if (lda < k || ldb < k || ldc < cols) return fail(h, MCPG_ERR_ARG, "maxmin: leading dimension too small");
+    const bool symm = (A == B) && (lda == ldb) && (rows == cols);
+    const float *a, *b;
+    int64_t la, lb;
+    int rc = aligned_view(h, A, lda, rows, k, S_IN0, &a, &la);
+    if (rc) return rc;
+    if (symm) {
+        b = a;
+        lb = la;
+    } else {
+        rc = aligned_view(h, B, ldb, cols, k, S_IN1, &b, &lb);
+        if (rc) return rc;
+    }
+    mcpg::MaxminParams p{};
+    p.A = a; p.lda = la; p.B = b; p.ldb = lb;
+    p.rows = rows; p.cols = cols; p.k_len = k;
+    p.C = C; p.ldc = ldc;
+    {
+        PROF(h, "maxmin");
+        CK(h, mcpg::launch_maxmin(p, mcpg::MM_PLAIN, symm ? 1 : 0, h->stream, &h->launches), "maxmin kernel");
+    }
+    return MCPG_OK;
+}
+
+int mcp_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, int path_len, int symmetrize, float* Mout,
+            int64_t ldm, float* Rout, int64_t ldr) {
+    if (n < 0) return fail(h, MCPG_ERR_ARG, "mcp: negative size");
+    if (n == 0) return MCPG_OK;
+    if (!A) return fail(h, MCPG_ERR_ARG, "mcp: null input");
+    if (path_len < 2 || path_len > 4) return fail(h, MCPG_ERR_ARG, "mcp: path_len must be 2, 3 or 4 (got %d)", path_len);
+    if (!Mout && !Rout) return MCPG_OK;
+    if (lda < n || (Mout && ldm < n) || (Rout && ldr < n)) return fail(h, MCPG_ERR_ARG, "mcp: leading dimension too small");
+    const float* a;
+    int64_t la;
+    int rc = aligned_view(h, A, lda, n, n, S_IN0, &a, &la);
+    if (rc) return rc;
+    const int64_t ldt = round_up(n, 32);
+    mcpg::MaxminParams p{};
+    p.rows = n; p.cols = n; p.k_len = n;
+    if (path_len == 2) {
+        p.A = a; p.lda = la; p.B = a; p.ldb = la;
+        p.C = Mout; p.ldc = ldm; p.E = a; p.lde = la; p.R = Rout; p.ldr = ldr;
+        if (Rout) {
+            {
+                PROF(h, "maxmin");
+                CK(h, mcpg::launch_maxmin(p, mcpg::MM_RATIO, 1, h->stream, &h->launches), "maxmin+ratio kernel");
+            }
+        } else {
+            {
+                PROF(h, "maxmin");
+                CK(h, mcpg::launch_maxmin(p, mcpg::MM_PLAIN, 1, h->stream, &h->launches), "maxmin kernel");
+            }
+        }
+        return MCPG_OK;
+    }
+    // M1 = A (x) A (symmetric)
+    void* m1;
+    rc = scratch(h, S_M1, (size_t)(n * ldt) * sizeof(float), &m1);
+    if (rc) return rc;
+    p.A = a; p.lda = la; p.B = a; p.ldb = la; p.C = (float*)m1; p.ldc = ldt;
+    {
+        PROF(h, "maxmin");
+        CK(h, mcpg::launch_maxmin(p, mcpg::MM_PLAIN, 1, h->stream, &h->launches), "maxmin kernel (M1)");
+    }
+    const float* X1 = (const float*)m1;
+    mcpg::MaxminParams q{};
+    q.rows = n; q.cols = n; q.k_len = n;
+    int sym2;
+    if (path_len == 3) {  // A (x) M1, InnerProduct(A, M1), not assumed symmetric
+        q.A = a; q.lda = la; q.B = X1; q.ldb = ldt; sym2 = 0;
+    } else {              // M1 (x) M1, symmetric
+        q.A = X1; q.lda = ldt; q.B = X1; q.ldb = ldt; sym2 = 1;
+    }
+    if (path_len == 3 && symmetrize) {
+        void* m2;
+        rc = scratch(h, S_M2, (size_t)(n * ldt) * sizeof(float), &m2);
+        if (rc) return rc;
+        q.C = (float*)m2; q.ldc = ldt;
+        {
+            PROF(h, "maxmin");
+            CK(h, mcpg::launch_maxmin(q, mcpg::MM_PLAIN, sym2, h->stream, &h->launches), "maxmin kernel (M2)");
+        }
+        float* sym = Mout;
+        int64_t lds = ldm;
+        if (!sym) {  // reuse M1's slot: M1 is no longer needed
+            sym = (float*)m1;
+            lds = ldt;
+        }
+        {
+            PROF(h, "max_transpose");
+            CK(h, mcpg::launch_max_transpose((const float*)m2, n, ldt, sym, lds, h->stream, &h->launches),
+           "max(M, M^T) kernel");
+        }
+        if (Rout) {
+            PROF(h, "ratio");
+            CK(h, mcpg::launch_ratio(a, la, sym, lds, n, n, Rout, ldr, h->stream, &h->launches), "ratio kernel");
+        }
+        return MCPG_OK;
+    }
+    q.C = Mout; q.ldc = ldm; q.E = a; q.lde = la; q.R = Rout; q.ldr = ldr;
+    if (Rout) {
+        {
+            PROF(h, "maxmin");
+            CK(h, mcpg::launch_maxmin(q, mcpg::MM_RATIO, sym2, h->stream, &h->launches), "maxmin+ratio kernel");
+        }
+    } else {
+        {
+            PROF(h, "maxmin");
+            CK(h, mcpg::launch_maxmin(q, mcpg::MM_PLAIN, sym2, h->stream, &h->launches), "maxmin kernel");
+        }
+    }
+    return MCPG_OK;
+}
+
+int dpi_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, float tol, float* out, int64_t ldo, uint8_t* mask,
+            int64_t* removed) {
+    if (n < 0) return fail(h, MCPG_ERR_ARG, "dpi: negative size");
+    if (removed) *removed = 0;
+    if (n == 0) return MCPG_OK;
+    if (!A || !out) return fail(h, MCPG_ERR_ARG, "dpi: null pointer");
+    if (lda < n || ldo < n) return fail(h, MCPG_ERR_ARG, "dpi: leading dimension too small");
+    if (!(tol >= 0.0f && tol <= 1.0f)) return fail(h, MCPG_ERR_ARG, "dpi: tolerance must be in [0, 1]");
+    const float* a = A;
+    int64_t la = lda;
+    // the output must not alias the input (other tiles still read it)
+    const bool alias = (const void*)out < (const void*)(A + n * lda) && (const void*)A < (const void*)(out + n * ldo);
+    if (alias || !aligned16(A) || (lda % 4) != 0) {
+        const int64_t ld = round_up(n, 32);
+        void* p;
+        int rc = scratch(h, S_IN0, (size_t)(n * ld) * sizeof(float), &p);
+        if (rc) return rc;
+        CK(h, mcpg::launch_copy2d(A, lda, (float*)p, ld, n, n, h->stream), "copy2d");
+        a = (const float*)p;
+        la = ld;
+    }
+    void* cnt;
+    int rc = scratch(h, S_SMALL, 64, &cnt);
+    if (rc) return rc;
+    CK(h, cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), h->stream), "memset counter");
+    mcpg::MaxminParams p{};
+    p.A = a; p.lda = la; p.B = a; p.ldb = la; p.rows = n; p.cols = n; p.k_len = n;
+    p.C = out; p.ldc = ldo; p.E = a; p.lde = la;
+    p.tol_mult = 1.0 / (1.0 - (double)tol);  // dpi_kernel ctor, dpi.hpp:47
+    p.mask = mask; p.ldmask = n;
+    p.removed = (unsigned long long*)cnt;
+    {
+        PROF(h, "maxmin");
+        CK(h, mcpg::launch_maxmin(p, mcpg::MM_DPI, 1, h->stream, &h->launches), "DPI kernel");
+    }
+    if (removed) {
+        unsigned long long r = 0;
+        CK(h, cudaMemcpyAsync(&r, cnt, sizeof r, cudaMemcpyDeviceToHost, h->stream), "read removed");
+        CK(h, cudaStreamSynchronize(h->stream), "stream synchronize");
+        *removed = (int64_t)r;
+    }
+    return MCPG_OK;
+}
+
+int closure_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, int max_iter, float* out, int64_t ldo,
+                int* iterations) {
+    if (iterations) *iterations = 0;
+    if (n < 0 || max_iter < 0) return fail(h, MCPG_ERR_ARG, "closure: negative size or max_iter");
+    if (n == 0) return MCPG_OK;
+    if (!A || !out) return fail(h, MCPG_ERR_ARG, "closure: null pointer");
+    if (lda < n || ldo < n) return fail(h, MCPG_ERR_ARG, "closure: leading dimension too small");
+    const int64_t ldt = round_up(n, 32);
+    void *b0, *b1, *flag;
+    int rc = scratch(h, S_M1, (size_t)(n * ldt) * sizeof(float), &b0);
+    if (rc) return rc;
+    rc = scratch(h, S_M2, (size_t)(n * ldt) * sizeof(float), &b1);
+    if (rc) return rc;
+    rc = scratch(h, S_SMALL, 64, &flag);
+    if (rc) return rc;
+    CK(h, mcpg::launch_copy2d(A, lda, (float*)b0, ldt, n, n, h->stream), "copy2d");
+    float* cur = (float*)b0;
+    float* nxt = (float*)b1;
+    int it = 0, changed = 1;
+    while (changed && it < max_iter) {
+        CK(h, cudaMemsetAsync(flag, 0, sizeof(int), h->stream), "memset flag");
+        mcpg::MaxminParams p{};
+        p.A = cur; p.lda = ldt; p.B = cur; p.ldb = ldt; p.rows = n; p.cols = n; p.k_len = n;
+        p.C = nxt; p.ldc = ldt; p.E = cur; p.lde = ldt; p.changed = (int*)flag;
+        {
+            PROF(h, "maxmin");
+            CK(h, mcpg::launch_maxmin(p, mcpg::MM_CLOSURE, 1, h->stream, &h->launches), "closure kernel");
+        }
+        CK(h, cudaMemcpyAsync(&changed, flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream), "read flag");
+        CK(h, cudaStreamSynchronize(h->stream), "stream synchronize");
+        float* t = cur; cur = nxt; nxt = t;
+        ++it;
+    }
+    CK(h, mcpg::launch_copy2d(cur, ldt, out, ldo, n, n, h->stream), "copy2d");
+    if (iterations) *iterations = it;
+    if (changed) return fail(h, MCPG_ERR_NOT_CONVERGED, "closure: still changing after %d products", it);
+    return MCPG_OK;
+}
+
+}  // namespace
+
+// =====================================================================
+extern "C" {
+
+int mcpg_version(void) { return 100; }
+
+const char* mcpg_status_string(int s) {
+    switch (s) {
+        case MCPG_OK: return "ok";
+        case MCPG_ERR_ARG: return "invalid argument";
+        case MCPG_ERR_OOM: return "out of memory";
+        case MCPG_ERR_CUDA: return "CUDA error";
+        case MCPG_ERR_NOT_CONVERGED: return "not converged";
+        case MCPG_ERR_UNSUPPORTED: return "unsupported";
+        case MCPG_ERR_DEVICE_TIMEOUT: return "device wait timed out";
+        default: return "unknown status";
+    }
+}
+
+int mcpg_create(mcpg_handle** out, int device) {
+    if (!out) return MCPG_ERR_ARG;
+    *out = nullptr;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return MCPG_ERR_CUDA;
+    }
+    if (device < 0 || device >= count) return MCPG_ERR_ARG;
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return MCPG_ERR_CUDA;
+    if (prop.major < 10) return MCPG_ERR_UNSUPPORTED;  // built for sm_103a only
+    if (cudaSetDevice(device) != cudaSuccess) return MCPG_ERR_CUDA;
+    mcpg_handle* h = new (std::nothrow) mcpg_handle;
+    if (!h) return MCPG_ERR_OOM;
+    h->device = device;
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete h;
+        return MCPG_ERR_CUDA;
+    }
+    h->own_stream = true;
+    *out = h;
+    return MCPG_OK;
+}
+
+int mcpg_destroy(mcpg_handle* h) {
+    if (!h) return MCPG_OK;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    mcpg_profile(h, 0);
+    for (int i = 0; i < NSLOTS; ++i)
+        if (h->buf[i]) cudaFree(h->buf[i]);
+    if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return MCPG_OK;
+}
+
+const char* mcpg_last_error(const mcpg_handle* h) { return h ? h->err.c_str() : "null handle"; }
+
+int mcpg_set_stream(mcpg_handle* h, void* s) {
+    if (!h) return MCPG_ERR_ARG;
+    if (h->own_stream && h->stream) {
+        cudaStreamSynchronize(h->stream);
+        cudaStreamDestroy(h->stream);
+    }
+    h->stream = (cudaStream_t)s;
+    h->own_stream = false;
+    return MCPG_OK;
+}
+
+int mcpg_synchronize(mcpg_handle* h) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    return finish(h);
+}
+
+int64_t mcpg_kernel_launches(const mcpg_handle* h) { return h ? h->launches : 0; }
+
+int mcpg_profile(mcpg_handle* h, int enable) {
+    if (!h) return MCPG_ERR_ARG;
+    for (auto& sp : h->spans) {
+        cudaEventDestroy(sp.a);
+        cudaEventDestroy(sp.b);
+    }
+    h->spans.clear();
+    h->prof = enable != 0;
+    return MCPG_OK;
+}
+
+int64_t mcpg_profile_report(mcpg_handle* h, char* buf, int64_t len) {
+    if (!h) return MCPG_ERR_ARG;
+    if (cudaStreamSynchronize(h->stream) != cudaSuccess) return MCPG_ERR_CUDA;
+    std::map<std::string, std::pair<int64_t, double>> agg;
+    for (auto& sp : h->spans) {
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, sp.a, sp.b) == cudaSuccess) {
+            auto& e = agg[sp.name];
+            e.first += 1;
+            e.second += ms;
+        }
+    }
+    std::string js = "{";
+    bool first = true;
+    for (auto& kv : agg) {
+        char tmp[256];
+        snprintf(tmp, sizeof tmp, "%s\"%s\": {\"launches\": %lld, \"ms\": %.6f}", first ? "" : ", ", kv.first.c_str(),
+                 (long long)kv.second.first, kv.second.second);
+        js += tmp;
+        first = false;
+    }
+    js += "}";
+    if (buf && len > 0) {
+        const size_t c = std::min((size_t)(len - 1), js.size());
+        memcpy(buf, js.data(), c);
+        buf[c] = 0;
+    }
+    return (int64_t)js.size() + 1;
+}
+
+int mcpg_test_fail_allocs(mcpg_handle* h, int count) {
+    if (!h) return MCPG_ERR_ARG;
+    h->fail_allocs = count;
+    return MCPG_OK;
+}
+
+// ---- MI ----
+int mcpg_bspline_mi_dev(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_t ldx, int bins, int order,
+                        int precision, float* MI, int64_t ldmi, double* H) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    return mi_dev(h, X, n, m, ldx, bins, order, precision, MI, ldmi, H);
+}
+
+int mcpg_bspline_mi(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_t ldx, int bins, int order,
+                    int precision, float* MI, int64_t ldmi, double* H) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (!X || !MI) return fail(h, MCPG_ERR_ARG, "bspline_mi: null pointer");
+    if (n < 1 || m < 1 || ldx < m || ldmi < n) return fail(h, MCPG_ERR_ARG, "bspline_mi: bad shape");
+    float *dX, *dMI;
+    int64_t lx, lmi;
+    if ((rc = stage_in(h, S_IN0, X, ldx, n, m, &dX, &lx))) return rc;
+    if ((rc = stage_out_alloc(h, S_OUT0, n, n, &dMI, &lmi))) return rc;
+    double* dH = nullptr;
+    if (H) {
+        void* p;
+        if ((rc = scratch(h, S_H, (size_t)n * sizeof(double), &p))) return rc;
+        dH = (double*)p;
+    }
+    if ((rc = mi_dev(h, dX, n, m, lx, bins, order, precision, dMI, lmi, dH))) return rc;
+    if ((rc = copy_out(h, MI, ldmi, dMI, lmi, n, n))) return rc;
+    if (H) CK(h, cudaMemcpyAsync(H, dH, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "copy H");
+    return finish(h);
+}
+
+// Reference-layout weights: W[g*(bins*m+1) + a*m + s], W[g*(bins*m+1) + bins*m] = H_g.
+int mcpg_bspline_weights_dev(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_t ldx, int bins, int order,
+                             float* W, double* H) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (!X || !W || n < 1 || m < 1 || ldx < m) return fail(h, MCPG_ERR_ARG, "bspline_weights: bad arguments");
+    if (bins < 1 || bins > 32 || order < 1 || order > 8 || bins < order)
+        return fail(h, MCPG_ERR_ARG, "bspline_weights: need 1 <= order <= bins <= 32, order <= 8");
+    CK(h, mcpg::launch_bspline_weights_ref(X, n, m, ldx, bins, order, W, H, h->stream, &h->launches),
+       "bspline weights kernel");
+    return MCPG_OK;
+}
+
+int mcpg_bspline_weights(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_t ldx, int bins, int order,
+                         float* W, double* H) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (!X || !W || n < 1 || m < 1 || ldx < m) return fail(h, MCPG_ERR_ARG, "bspline_weights: bad arguments");
+    float* dX;
+    int64_t lx;
+    if ((rc = stage_in(h, S_IN0, X, ldx, n, m, &dX, &lx))) return rc;
+    const int64_t ldw = (int64_t)bins * m + 1;
+    void *dW, *dH = nullptr;
+    if ((rc = scratch(h, S_OUT0, (size_t)(n * ldw) * sizeof(float), &dW))) return rc;
+    if (H && (rc = scratch(h, S_H, (size_t)n * sizeof(double), &dH))) return rc;
+    if ((rc = mcpg_bspline_weights_dev(h, dX, n, m, lx, bins, order, (float*)dW, (double*)dH))) return rc;
+    CK(h, cudaMemcpyAsync(W, dW, (size_t)(n * ldw) * sizeof(float), cudaMemcpyDeviceToHost, h->stream), "copy W");
+    if (H) CK(h, cudaMemcpyAsync(H, dH, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "copy H");
+    return finish(h);
+}
+
+// ---- max-min ----
+int mcpg_maxmin_dev(mcpg_handle* h, const float* A, int64_t lda, const float* B, int64_t ldb, int64_t rows,
+                    int64_t cols, int64_t k, float* C, int64_t ldc) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    return maxmin_dev(h, A, lda, B, ldb, rows, cols, k, C, ldc);
+}
+
+int mcpg_maxmin(mcpg_handle* h, const float* A, int64_t lda, const float* B, int64_t ldb, int64_t rows, int64_t cols,
+                int64_t k, float* C, int64_t ldc) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (rows < 0 || cols < 0 || k < 0) return fail(h, MCPG_ERR_ARG, "maxmin: negative size");
+    if (rows == 0 || cols == 0) return MCPG_OK;
+    if (!A || !B || !C) return fail(h, MCPG_ERR_ARG, "maxmin: null pointer");
+    if (lda < k || ldb < k || ldc < cols) return fail(h, MCPG_ERR_ARG, "maxmin: leading dimension too small");
+    const bool same = (A == B) && (lda == ldb) && (rows == cols);
+    float *dA, *dB, *dC;
+    int64_t la, lb, lc;
+    if ((rc = stage_in(h, S_IN0, A, lda, rows, k, &dA, &la))) return rc;
+    if (same) {
+        dB = dA; lb = la;
+    } else if ((rc = stage_in(h, S_IN1, B, ldb, cols, k, &dB, &lb))) {
+        return rc;
+    }
+    if ((rc = stage_out_alloc(h, S_OUT0, rows, cols, &dC, &lc))) return rc;
+    if ((rc = maxmin_dev(h, dA, la, dB, lb, rows, cols, k, dC, lc))) return rc;
+    if ((rc = copy_out(h, C, ldc, dC, lc, rows, cols))) return rc;
+    return finish(h);
+}
+
+// ---- ratio ----
+int mcpg_ratio_dev(mcpg_handle* h, const float* A, int64_t lda, const float* M, int64_t ldm, int64_t rows,
+                   int64_t cols, float* R, int64_t ldr) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (rows < 0 || cols < 0) return fail(h, MCPG_ERR_ARG, "ratio: negative size");
+    if (rows == 0 || cols == 0) return MCPG_OK;
+    if (!A || !M || !R) return fail(h, MCPG_ERR_ARG, "ratio: null pointer");
+    if (lda < cols || ldm < cols || ldr < cols) return fail(h, MCPG_ERR_ARG, "ratio: leading dimension too small");
+    {
+        PROF(h, "ratio");
+        CK(h, mcpg::launch_ratio(A, lda, M, ldm, rows, cols, R, ldr, h->stream, &h->launches), "ratio kernel");
+    }
+    return MCPG_OK;
+}
+
+int mcpg_ratio(mcpg_handle* h, const float* A, int64_t lda, const float* M, int64_t ldm, int64_t rows, int64_t cols,
+               float* R, int64_t ldr) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (rows < 0 || cols < 0) return fail(h, MCPG_ERR_ARG, "ratio: negative size");
+    if (rows == 0 || cols == 0) return MCPG_OK;
+    if (!A || !M || !R) return fail(h, MCPG_ERR_ARG, "ratio: null pointer");
+    if (lda < cols || ldm < cols || ldr < cols) return fail(h, MCPG_ERR_ARG, "ratio: leading dimension too small");
+    float *dA, *dM, *dR;
+    int64_t la, lm, lr;
+    if ((rc = stage_in(h, S_IN0, A, lda, rows, cols, &dA, &la))) return rc;
+    if ((rc = stage_in(h, S_IN1, M, ldm, rows, cols, &dM, &lm))) return rc;
+    if ((rc = stage_out_alloc(h, S_OUT0, rows, cols, &dR, &lr))) return rc;
+    if ((rc = mcpg_ratio_dev(h, dA, la, dM, lm, rows, cols, dR, lr))) return rc;
+    if ((rc = copy_out(h, R, ldr, dR, lr, rows, cols))) return rc;
+    return finish(h);
+}
+
+int mcpg_set_diagonal_dev(mcpg_handle* h, float* A, int64_t rows, int64_t cols, int64_t lda, float value) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (rows < 0 || cols < 0) return fail(h, MCPG_ERR_ARG, "set_diagonal: negative size");
+    if (rows == 0 || cols == 0) return MCPG_OK;
+    if (!A || lda < cols) return fail(h, MCPG_ERR_ARG, "set_diagonal: bad arguments");
+    CK(h, mcpg::launch_set_diagonal(A, rows, cols, lda, value, h->stream, &h->launches), "set_diagonal kernel");
+    return MCPG_OK;
+}
+
+// ---- MCP ----
+int mcpg_mcp_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, int path_len, int symmetrize, float* Mout,
+                 int64_t ldm, float* Rout, int64_t ldr) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    return mcp_dev(h, A, n, lda, path_len, symmetrize, Mout, ldm, Rout, ldr);
+}
+
+int mcpg_mcp(mcpg_handle* h, const float* A, int64_t n, int64_t lda, int path_len, int symmetrize, float* Mout,
+             int64_t ldm, float* Rout, int64_t ldr) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (n < 0) return fail(h, MCPG_ERR_ARG, "mcp: negative size");
+    if (n == 0) return MCPG_OK;
+    if (!A) return fail(h, MCPG_ERR_ARG, "mcp: null input");
+    if (path_len < 2 || path_len > 4) return fail(h, MCPG_ERR_ARG, "mcp: path_len must be 2, 3 or 4 (got %d)", path_len);
+    if (lda < n || (Mout && ldm < n) || (Rout && ldr < n)) return fail(h, MCPG_ERR_ARG, "mcp: leading dimension too small");
+    float *dA, *dM = nullptr, *dR = nullptr;
+    int64_t la, lm = 0, lr = 0;
+    if ((rc = stage_in(h, S_IN0, A, lda, n, n, &dA, &la))) return rc;
+    if (Mout && (rc = stage_out_alloc(h, S_OUT0, n, n, &dM, &lm))) return rc;
+    if (Rout && (rc = stage_out_alloc(h, S_OUT1, n, n, &dR, &lr))) return rc;
+    if ((rc = mcp_dev(h, dA, n, la, path_len, symmetrize, dM, lm, dR, lr))) return rc;
+    if ((rc = copy_out(h, Mout, ldm, dM, lm, n, n))) return rc;
+    if ((rc = copy_out(h, Rout, ldr, dR, lr, n, n))) return rc;
+    return finish(h);
+}
+
+// ---- DPI ----
+int mcpg_dpi_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, float tol, float* out, int64_t ldo,
+                 uint8_t* mask, int64_t* removed) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    return dpi_dev(h, A, n, lda, tol, out, ldo, mask, removed);
+}
+
+int mcpg_dpi(mcpg_handle* h, const float* A, int64_t n, int64_t lda, float tol, float* out, int64_t ldo, uint8_t* mask,
+             int64_t* removed) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (removed) *removed = 0;
+    if (n < 0) return fail(h, MCPG_ERR_ARG, "dpi: negative size");
+    if (n == 0) return MCPG_OK;
+    if (!A || !out) return fail(h, MCPG_ERR_ARG, "dpi: null pointer");
+    if (lda < n || ldo < n) return fail(h, MCPG_ERR_ARG, "dpi: leading dimension too small");
+    float *dA, *dO;
+    int64_t la, lo;
+    if ((rc = stage_in(h, S_IN0, A, lda, n, n, &dA, &la))) return rc;
+    if ((rc = stage_out_alloc(h, S_OUT0, n, n, &dO, &lo))) return rc;
+    uint8_t* dMask = nullptr;
+    if (mask) {
+        void* p;
+        if ((rc = scratch(h, S_MASK, (size_t)(n * n), &p))) return rc;
+        dMask = (uint8_t*)p;
+    }
+    if ((rc = dpi_dev(h, dA, n, la, tol, dO, lo, dMask, removed))) return rc;
+    if ((rc = copy_out(h, out, ldo, dO, lo, n, n))) return rc;
+    if (mask) CK(h, cudaMemcpyAsync(mask, dMask, (size_t)(n * n), cudaMemcpyDeviceToHost, h->stream), "copy mask");
+    return finish(h);
+}
+
+// ---- closure ----
+int mcpg_closure_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, int max_iter, float* out, int64_t ldo,
+                     int* iterations) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    return closure_dev(h, A, n, lda, max_iter, out, ldo, iterations);
+}
+
+int mcpg_closure(mcpg_handle* h, const float* A, int64_t n, int64_t lda, int max_iter, float* out, int64_t ldo,
+                 int* iterations) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (iterations) *iterations = 0;
+    if (n < 0 || max_iter < 0) return fail(h, MCPG_ERR_ARG, "closure: negative size or max_iter");
+    if (n == 0) return MCPG_OK;
+    if (!A || !out) return fail(h, MCPG_ERR_ARG, "closure: null pointer");
+    if (lda < n || ldo < n) return fail(h, MCPG_ERR_ARG, "closure: leading dimension too small");
+    float *dA, *dO;
+    int64_t la, lo;
+    if ((rc = stage_in(h, S_IN0, A, lda, n, n, &dA, &la))) return rc;
+    if ((rc = stage_out_alloc(h, S_OUT0, n, n, &dO, &lo))) return rc;
+    int crc = closure_dev(h, dA, n, la, max_iter, dO, lo, iterations);
+    if (crc && crc != MCPG_ERR_NOT_CONVERGED) return crc;
+    std::string keep = h->err;
+    if ((rc = copy_out(h, out, ldo, dO, lo, n, n))) return rc;
+    if ((rc = finish(h))) return rc;
+    h->err = keep;
+    return crc;
+}
+
+}  // extern "C"

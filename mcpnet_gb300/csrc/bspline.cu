@@ -1,0 +1,241 @@
+// Per-gene min-max scaling, B-spline weights and FP64 marginal entropy (K1).
+//
+// Restates, one CTA per gene:
+//   MinMaxScale::operator()            include/mcp/correlation/BSplineMI.hpp:81-115
+//   buildKnotVector                     BSplineMI.hpp:35-71   (host, passed in)
+//   BSplineWeightsKernel::basisFunction BSplineMI.hpp:130-164 (Cox-de Boor)
+//   BSplineWeightsKernel::operator()    BSplineMI.hpp:248-273
+//   entropy1d_2                         BSplineMI.hpp:204-224 (here in FP64)
+// The basis recursion is evaluated bottom-up (order 1 .. k) with the same float
+// operations in the same order as the recursive reference, and with explicit
+// round-to-nearest intrinsics so nvcc cannot fuse a multiply and an add into an
+// FMA: the weights are bit-identical to the reference compiled without FMA
+// contraction.
+//
+// Output layouts (one kernel, chosen by template):
+//   OUT_REF   : W[g*(bins*m+1) + a*m + s] and W[g*(bins*m+1) + bins*m] = (float)H_g
+//               -- the reference's own Transform output row.
+//   OUT_T32   : Wt[s*ldwt + g*bins + a] (sample-major FP32, CUDA-core MI)
+//   OUT_BF16/OUT_FP16 : Whi/Wlo[(g*bins + a)*ldw + s] (gene-bin-major, K = samples
+//               contiguous, zero-padded to ldw; tcgen05 MI)
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <math.h>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace mcpg {
+namespace {
+
+constexpr int KMAX_BINS = 32, KMAX_ORDER = 8, KNOTS_MAX = KMAX_BINS + KMAX_ORDER;
+constexpr int WTHREADS = 256;
+
+struct Knots {
+    float v[KNOTS_MAX];
+};
+
+enum OutKind { OUT_REF = 0, OUT_T32 = 1, OUT_BF16 = 2, OUT_FP16 = 3 };
+
+void host_knots(int bins, int order, Knots& k) {
+    // buildKnotVector<float> (BSplineMI.hpp:35-71): norm_factor in double,
+    // v[i] = (float)((float)(i - order + 1) * norm_factor).
+    const int nint = bins - order;
+    const double nf = 1.0 / (double)(nint + 1);
+    for (int i = 0; i < KNOTS_MAX; ++i) k.v[i] = 0.0f;
+    for (int i = 0; i < order; ++i) k.v[i] = 0.0f;
+    for (int i = order; i < order + nint; ++i) k.v[i] = (float)((double)(float)(i - order + 1) * nf);
+    for (int i = order + nint; i < 2 * order + nint; ++i) k.v[i] = 1.0f;
+}
+
+// All bins' basis values at t, bottom-up.  N[i] holds basis(i, p, t) for the
+// current p.  Each value is produced by the same float operations as the
+// recursive reference (divide, multiply, add, clamp), so the results agree bit
+// for bit.
+__device__ __forceinline__ void basis_all(const Knots& kv, int bins, int order, float t, float* out) {
+    float N[KNOTS_MAX];
+    const int n1 = bins + order - 1;  // number of order-1 functions needed
+    for (int i = 0; i < n1; ++i) {
+        const float a = kv.v[i], b = kv.v[i + 1];
+        const bool in = (t >= a && t < b && a < b) ||
+                        (fabs((double)__fsub_rn(t, b)) < 1e-10 && (i + 1 == bins));
+        N[i] = in ? 1.0f : 0.0f;
+    }
+    for (int p = 2; p <= order; ++p) {
+        const int np = bins + order - p;
+        for (int i = 0; i < np; ++i) {
+            const float d1 = __fsub_rn(kv.v[i + p - 1], kv.v[i]);
+            const float n1v = __fsub_rn(t, kv.v[i]);
+            const float d2 = __fsub_rn(kv.v[i + p], kv.v[i + 1]);
+            const float n2v = __fsub_rn(kv.v[i + p], t);
+            float r;
+            if (d1 < 1e-10 && d2 < 1e-10) {
+                r = 0.0f;
+            } else {
+                float e1, e2;
+                if (d1 < 1e-10) {
+                    e1 = 0.0f;
+                    e2 = __fmul_rn(__fdiv_rn(n2v, d2), N[i + 1]);
+                } else if (d2 < 1e-10) {
+                    e2 = 0.0f;
+                    e1 = __fmul_rn(__fdiv_rn(n1v, d1), N[i]);
+                } else {
+                    e1 = __fmul_rn(__fdiv_rn(n1v, d1), N[i]);
+                    e2 = __fmul_rn(__fdiv_rn(n2v, d2), N[i + 1]);
+                }
+                const float s = __fadd_rn(e1, e2);
+                r = (s < 0.0f) ? 0.0f : s;
+            }
+            N[i] = r;  // N[i+1] (still order p-1) is read before it is overwritten
+        }
+    }
+    for (int a = 0; a < bins; ++a) out[a] = N[a];
+}
+
+template <typename T>
+__device__ __forceinline__ T block_reduce(T v, T (*op)(T, T), T* scratch) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = op(v, __shfl_xor_sync(0xffffffffu, v, o));
+    __syncthreads();
+    if (lane == 0) scratch[warp] = v;
+    __syncthreads();
+    T r = scratch[0];
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) r = op(r, scratch[w]);
+    return r;
+}
+__device__ float op_min(float a, float b) { return (b < a) ? b : a; }
+__device__ float op_max(float a, float b) { return (a < b) ? b : a; }
+
+template <int OUT>
+__global__ void __launch_bounds__(WTHREADS) bspline_weights_kernel(const float* __restrict__ X, int64_t n, int64_t m,
+                                                                   int64_t ldx, int bins, int order, const Knots kv,
+                                                                   void* __restrict__ out0, void* __restrict__ out1,
+                                                                   int64_t ldo, double* __restrict__ H) {
+    __shared__ float fscratch[32];
+    __shared__ double psum[KMAX_BINS][WTHREADS / 32];
+    const int64_t g = blockIdx.x;
+    if (g >= n) return;
+    const float* x = X + g * ldx;
+
+    // ---- MinMaxScale (BSplineMI.hpp:86-115) ----
+    float mn = INFINITY, mx = -INFINITY;
+    for (int64_t s = threadIdx.x; s < m; s += blockDim.x) {
+        const float v = x[s];
+        mn = (v < mn) ? v : mn;
+        mx = (mx < v) ? v : mx;
+    }
+    mn = block_reduce<float>(mn, op_min, fscratch);
+    mx = block_reduce<float>(mx, op_max, fscratch);
+    const float scale = (mx > mn) ? (float)(1.0 / (double)__fsub_rn(mx, mn)) : 1.0f;
+    const float offset = (mx > mn) ? mn : 0.0f;
+
+    double acc[KMAX_BINS];
+#pragma unroll
+    for (int a = 0; a < KMAX_BINS; ++a) acc[a] = 0.0;
+
+    float w[KMAX_BINS];
+    for (int64_t s = threadIdx.x; s < m; s += blockDim.x) {
+        const float t = __fmul_rn(scale, __fsub_rn(x[s], offset));
+        basis_all(kv, bins, order, t, w);
+#pragma unroll
+        for (int a = 0; a < KMAX_BINS; ++a)
+            if (a < bins) acc[a] += (double)w[a];
+        if (OUT == OUT_REF) {
+            float* W = static_cast<float*>(out0) + g * ((int64_t)bins * m + 1);
+            for (int a = 0; a < bins; ++a) W[(int64_t)a * m + s] = w[a];
+        } else if (OUT == OUT_T32) {
+            float* W = static_cast<float*>(out0) + s * ldo + g * bins;
+            for (int a = 0; a < bins; ++a) W[a] = w[a];
+        } else {
+            for (int a = 0; a < bins; ++a) {
+                const int64_t o = (g * bins + a) * ldo + s;
+                if (OUT == OUT_BF16) {
+                    const __nv_bfloat16 hi = __float2bfloat16_rn(w[a]);
+                    static_cast<__nv_bfloat16*>(out0)[o] = hi;
+                    if (out1) static_cast<__nv_bfloat16*>(out1)[o] = __float2bfloat16_rn(w[a] - __bfloat162float(hi));
+                } else {
+                    const __half hi = __float2half_rn(w[a]);
+                    static_cast<__half*>(out0)[o] = hi;
+                    if (out1) static_cast<__half*>(out1)[o] = __float2half_rn(w[a] - __half2float(hi));
+                }
+            }
+        }
+    }
+    // zero the K padding of the 16-bit layouts
+    if (OUT == OUT_BF16 || OUT == OUT_FP16) {
+        for (int64_t s = m + threadIdx.x; s < ldo; s += blockDim.x)
+            for (int a = 0; a < bins; ++a) {
+                const int64_t o = (g * bins + a) * ldo + s;
+                static_cast<uint16_t*>(out0)[o] = 0;
+                if (out1) static_cast<uint16_t*>(out1)[o] = 0;
+            }
+    }
+
+    // ---- marginal entropy in FP64 (entropy1d_2, BSplineMI.hpp:204-224) ----
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int a = 0; a < KMAX_BINS; ++a) {
+        if (a >= bins) break;
+        double v = acc[a];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) psum[a][warp] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double Hg = 0.0;
+        const double inv_m = 1.0 / (double)m;
+        for (int a = 0; a < bins; ++a) {
+            double p = 0.0;
+            for (int w2 = 0; w2 < (int)(blockDim.x >> 5); ++w2) p += psum[a][w2];
+            p *= inv_m;
+            if (p > 0.0) Hg += p * log2(p);
+        }
+        Hg = -Hg;
+        if (H) H[g] = Hg;
+        if (OUT == OUT_REF) static_cast<float*>(out0)[g * ((int64_t)bins * m + 1) + (int64_t)bins * m] = (float)Hg;
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_bspline_weights_ref(const float* X, int64_t n, int64_t m, int64_t ldx, int bins, int order,
+                                       float* W, double* H, cudaStream_t stream, int64_t* launches) {
+    if (n <= 0) return cudaSuccess;
+    Knots kv;
+    host_knots(bins, order, kv);
+    if (launches) ++*launches;
+    bspline_weights_kernel<OUT_REF><<<(unsigned)n, WTHREADS, 0, stream>>>(X, n, m, ldx, bins, order, kv, W, nullptr,
+                                                                          0, H);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bspline_weights_fp32(const float* X, int64_t n, int64_t m, int64_t ldx, int bins, int order,
+                                        float* Wt, int64_t ldwt, double* H, cudaStream_t stream, int64_t* launches) {
+    if (n <= 0) return cudaSuccess;
+    Knots kv;
+    host_knots(bins, order, kv);
+    if (launches) ++*launches;
+    bspline_weights_kernel<OUT_T32><<<(unsigned)n, WTHREADS, 0, stream>>>(X, n, m, ldx, bins, order, kv, Wt, nullptr,
+                                                                          ldwt, H);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bspline_weights_16(const float* X, int64_t n, int64_t m, int64_t ldx, int bins, int order,
+                                      int fmt, uint16_t* Whi, uint16_t* Wlo, int64_t ldw, double* H,
+                                      cudaStream_t stream, int64_t* launches) {
+    if (n <= 0) return cudaSuccess;
+    Knots kv;
+    host_knots(bins, order, kv);
+    if (launches) ++*launches;
+    if (fmt == 0)
+        bspline_weights_kernel<OUT_BF16><<<(unsigned)n, WTHREADS, 0, stream>>>(X, n, m, ldx, bins, order, kv, Whi,
+                                                                               Wlo, ldw, H);
+    else
+        bspline_weights_kernel<OUT_FP16><<<(unsigned)n, WTHREADS, 0, stream>>>(X, n, m, ldx, bins, order, kv, Whi,
+                                                                               Wlo, ldw, H);
+    return cudaGetLastError();
+}
+
+}  // namespace mcpg

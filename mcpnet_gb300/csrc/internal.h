@@ -1,0 +1,66 @@
+// Internal launcher interface between the C ABI (api.cpp) and the kernels.
+// Every launcher enqueues work on `stream`, returns the launch status and adds
+// the number of kernels it launched to *launches.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace mcpg {
+
+// ---------------- max-min family (maxmin.cu) ----------------
+enum MaxminMode : int {
+    MM_PLAIN = 0,    // C = A (x) B
+    MM_RATIO = 1,    // R = ratio(E, A (x) B); C (nullable) = A (x) B
+    MM_CLOSURE = 2,  // C = max(E, A (x) B); *changed |= any entry grew
+    MM_DPI = 3,      // C = dpi-mask(E) applied to E; k excluded when k == i or k == j
+};
+
+struct MaxminParams {
+    const float* A; int64_t lda;  // rows x k_len, 16-byte aligned rows
+    const float* B; int64_t ldb;  // cols x k_len, 16-byte aligned rows
+    int64_t rows, cols, k_len;
+    float* C; int64_t ldc;        // product / closure / DPI output (nullable in RATIO mode)
+    const float* E; int64_t lde;  // RATIO numerator, CLOSURE current iterate, DPI input
+    float* R; int64_t ldr;        // RATIO output
+    int* changed;                 // CLOSURE flag (device)
+    double tol_mult;              // DPI 1/(1 - tol)
+    uint8_t* mask; int64_t ldmask;  // DPI mask (nullable)
+    unsigned long long* removed;  // DPI removed count (device, nullable)
+};
+
+// symmetric != 0: A == B (same rows), rows == cols; only tiles on or above the
+// diagonal are computed and mirrored (C is symmetric for any A in that case).
+cudaError_t launch_maxmin(const MaxminParams& p, int mode, int symmetric, cudaStream_t stream, int64_t* launches);
+cudaError_t launch_ratio(const float* A, int64_t lda, const float* M, int64_t ldm, int64_t rows, int64_t cols,
+                         float* R, int64_t ldr, cudaStream_t stream, int64_t* launches);
+cudaError_t launch_set_diagonal(float* A, int64_t rows, int64_t cols, int64_t lda, float value,
+                                cudaStream_t stream, int64_t* launches);
+cudaError_t launch_max_transpose(const float* M, int64_t n, int64_t ldm, float* out, int64_t ldo,
+                                 cudaStream_t stream, int64_t* launches);
+// Copies a rows x cols matrix between arbitrary leading dimensions (device to device).
+cudaError_t launch_copy2d(const float* src, int64_t lds, float* dst, int64_t ldd, int64_t rows, int64_t cols,
+                          cudaStream_t stream);
+
+// ---------------- B-spline weights and MI (bspline.cu, mi_fp32.cu, mi_tc.cu) ----------------
+// Sample-major FP32 weights for the CUDA-core contraction:
+//   Wt[s * ldwt + g * bins + a] = B_a(scaled x_g[s]),  s < m, g < n  (ldwt >= n*bins)
+// H[g] (double) = marginal entropy in bits.
+cudaError_t launch_bspline_weights_fp32(const float* X, int64_t n, int64_t m, int64_t ldx, int bins, int order,
+                                        float* Wt, int64_t ldwt, double* H, cudaStream_t stream, int64_t* launches);
+// Gene-bin-major 16-bit weights for tcgen05 (K = samples contiguous):
+//   Whi[(g*bins + a) * ldw + s] = round16(w), Wlo[...] = round16(w - Whi) (Wlo nullable)
+// fmt: 0 = bf16, 1 = fp16.  Columns s in [m, ldw) are written as zero.
+cudaError_t launch_bspline_weights_16(const float* X, int64_t n, int64_t m, int64_t ldx, int bins, int order,
+                                      int fmt, uint16_t* Whi, uint16_t* Wlo, int64_t ldw, double* H,
+                                      cudaStream_t stream, int64_t* launches);
+// FP32 MI from sample-major weights (CUDA cores), symmetric output.
+cudaError_t launch_mi_fp32(const float* Wt, int64_t ldwt, const double* H, int64_t n, int64_t m, int bins,
+                           float* MI, int64_t ldmi, cudaStream_t stream, int64_t* launches);
+// Tensor-core MI (tcgen05) from 16-bit weights; split != 0 adds the lo terms.
+// Returns cudaErrorNotSupported when the shape/bins is outside the kernel's tiling.
+cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, int64_t ldw, const double* H, int64_t n,
+                         int64_t m, int bins, int fmt, int split, float* MI, int64_t ldmi, int* timeout_flag,
+                         cudaStream_t stream, int64_t* launches);
+
+}  // namespace mcpg

@@ -1,0 +1,339 @@
+// Max-min ("maximum-capacity path") products and their fused epilogues.
+//
+//   C[i][j] = max_k min(A[i][k], B[j][k])
+//
+// is the whole-matrix form of mcp2_maxmin_kernel<float,false,true>
+// (include/mcp/filter/mcp.hpp:72-93) applied by splash InnerProduct(A, B), with
+// max_of_pairmin_scalar (include/mcp/filter/simd_maxmin.hpp:30-46) as the
+// per-pair reduction.  It is a selection semiring: no rounding anywhere, so the
+// result is bit-exact for NaN-free inputs whatever the reduction order.
+//
+// Kernel shape (FP32 ALU bound, no tensor cores):
+//  - CTA tile 128 x 128 outputs, 256 threads, 8 x 8 outputs per thread held in
+//    registers; k staged through shared memory in 16-wide slices by a 4-stage
+//    cp.async pipeline (operand rows are k-contiguous in HBM, so no transpose).
+//  - inner step per thread and k pair: 16 LDS.64 feed 64 x (min, min, max3):
+//    1.5 FP32 min/max instructions per (i, j, k) triple using the sm_100+
+//    3-input max.
+//  - fused epilogues: MCP ratio (combine.hpp:210-222), closure step
+//    B <- max(B, B (x) B) with a changed flag, DPI mask + apply
+//    (dpi.hpp:56-68, threshold.hpp:46-53) with the y in {x, z} exclusion done
+//    on the k slices that overlap the tile's rows or columns.
+//  - symmetric mode (A == B): only tiles on/above the diagonal run; each writes
+//    its tile and the mirrored tile, as InnerProduct<..., SYMM=true> does.
+#include <float.h>
+#include <math.h>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace mcpg {
+namespace {
+
+constexpr int BM = 128, BN = 128, BK = 16, STAGES = 4, THREADS = 256;
+constexpr int LDS = BK + 4;  // row stride in floats: 16B-aligned, 4 consecutive rows -> 4 distinct bank groups
+constexpr int TILE_FLOATS = BM * LDS;
+constexpr size_t SMEM_BYTES = (size_t)STAGES * 2 * TILE_FLOATS * sizeof(float);  // 80 KB
+
+// Per-thread view of the operand rows it stages: each thread copies the 16-byte
+// chunk q of rows r and r + 64 of both operand tiles.
+struct StageLoader {
+    const float* a0; const float* a1; const float* b0; const float* b1;  // row bases at k = 4q
+    int64_t k_rem;   // k_len - 4q
+    uint32_t soff;   // shared offset (floats) of chunk (r, q)
+    bool va0, va1, vb0, vb1;
+
+    __device__ __forceinline__ void init(const MaxminParams& p, int64_t i0, int64_t j0, int tid) {
+        const int r = tid >> 2, q = tid & 3;
+        soff = r * LDS + q * 4;
+        k_rem = p.k_len - 4 * q;
+        va0 = i0 + r < p.rows; va1 = i0 + r + 64 < p.rows;
+        vb0 = j0 + r < p.cols; vb1 = j0 + r + 64 < p.cols;
+        a0 = va0 ? p.A + (i0 + r) * p.lda + 4 * q : p.A;
+        a1 = va1 ? p.A + (i0 + r + 64) * p.lda + 4 * q : p.A;
+        b0 = vb0 ? p.B + (j0 + r) * p.ldb + 4 * q : p.B;
+        b1 = vb1 ? p.B + (j0 + r + 64) * p.ldb + 4 * q : p.B;
+    }
+    __device__ __forceinline__ void load(float* As, float* Bs, int64_t k0) const {
+        const int64_t rem = k_rem - k0;
+        const int kb = rem >= 4 ? 16 : (rem > 0 ? (int)rem * 4 : 0);
+        cp_async16(As + soff, va0 ? a0 + k0 : a0, va0 ? kb : 0);
+        cp_async16(As + soff + 64 * LDS, va1 ? a1 + k0 : a1, va1 ? kb : 0);
+        cp_async16(Bs + soff, vb0 ? b0 + k0 : b0, vb0 ? kb : 0);
+        cp_async16(Bs + soff + 64 * LDS, vb1 ? b1 + k0 : b1, vb1 ? kb : 0);
+    }
+};
+
+__device__ __forceinline__ float ratio_of(float a, float m) {
+    // ratio_kernel<float,float> (combine.hpp:210-222).  The reference divides in
+    // double and rounds to float; for float operands that double rounding is
+    // innocuous (53 >= 2*24+2), so the correctly rounded float quotient is
+    // bit-identical.
+    return (fabsf(a) < FLT_EPSILON) ? 0.0f : (fabsf(m) < FLT_EPSILON) ? FLT_MAX : __fdiv_rn(a, m);
+}
+
+template <int MODE, bool SYMM>
+__global__ void __launch_bounds__(THREADS, 1) maxmin_kernel(const MaxminParams p) {
+    extern __shared__ float4 smem_f4[];
+    float* smem = reinterpret_cast<float*>(smem_f4);
+
+    int64_t ti = blockIdx.y, tj = blockIdx.x;
+    if (SYMM && tj < ti) return;
+    const int64_t i0 = ti * BM, j0 = tj * BN;
+    const bool mirror = SYMM && (tj != ti);
+
+    const int tid = threadIdx.x;
+    const int warp = tid >> 5, lane = tid & 31;
+    const int ty = ((warp >> 1) << 2) + (lane >> 3);  // 0..15
+    const int tx = ((warp & 1) << 3) + (lane & 7);    // 0..15
+
+    // DPI: NaN is the neutral element of the NaN-ignoring max, so an output with
+    // no admissible y stays NaN and compares false (the reference keeps it).
+    const float init = (MODE == MM_DPI) ? __int_as_float(0x7fc00000) : -INFINITY;
+    float acc[8][8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+#pragma unroll
+        for (int r = 0; r < 8; ++r) acc[q][r] = init;
+
+    StageLoader ld;
+    ld.init(p, i0, j0, tid);
+    const int64_t ktiles = ceil_div(p.k_len, BK);
+#pragma unroll
+    for (int s = 0; s < STAGES - 1; ++s) {
+        if (s < ktiles) ld.load(smem + s * 2 * TILE_FLOATS, smem + s * 2 * TILE_FLOATS + TILE_FLOATS, (int64_t)s * BK);
+        cp_async_commit();
+    }
+
+    for (int64_t t = 0; t < ktiles; ++t) {
+        cp_async_wait<STAGES - 2>();
+        __syncthreads();
+        {
+            const int64_t tn = t + STAGES - 1;
+            if (tn < ktiles) {
+                float* st = smem + (tn % STAGES) * 2 * TILE_FLOATS;
+                ld.load(st, st + TILE_FLOATS, tn * BK);
+            }
+            cp_async_commit();
+        }
+        const float* As = smem + (t % STAGES) * 2 * TILE_FLOATS;
+        const float* Bs = As + TILE_FLOATS;
+        const float* a_base = As + ty * LDS;
+        const float* b_base = Bs + tx * LDS;
+        const int64_t k0 = t * BK;
+        const int64_t kmax = min((int64_t)BK, p.k_len - k0);
+        bool excl = false;
+        if (MODE == MM_DPI) {
+            excl = (k0 < i0 + BM && k0 + BK > i0) || (k0 < j0 + BN && k0 + BK > j0);
+        }
+        if (kmax == BK && !excl) {
+#pragma unroll
+            for (int kk = 0; kk < BK; kk += 2) {
+                float2 a[8];
+#pragma unroll
+                for (int q = 0; q < 8; ++q) a[q] = *reinterpret_cast<const float2*>(a_base + q * 16 * LDS + kk);
+#pragma unroll
+                for (int r = 0; r < 8; ++r) {
+                    const float2 b = *reinterpret_cast<const float2*>(b_base + r * 16 * LDS + kk);
+#pragma unroll
+                    for (int q = 0; q < 8; ++q)
+                        acc[q][r] = fmax3(acc[q][r], fmin2(a[q].x, b.x), fmin2(a[q].y, b.y));
+                }
+            }
+        } else {
+            for (int kk = 0; kk < (int)kmax; ++kk) {
+                const int64_t y = k0 + kk;
+                float a[8], b[8];
+#pragma unroll
+                for (int q = 0; q < 8; ++q) a[q] = a_base[q * 16 * LDS + kk];
+#pragma unroll
+                for (int r = 0; r < 8; ++r) b[r] = b_base[r * 16 * LDS + kk];
+#pragma unroll
+                for (int q = 0; q < 8; ++q)
+#pragma unroll
+                    for (int r = 0; r < 8; ++r) {
+                        float v = fmin2(a[q], b[r]);
+                        if (MODE == MM_DPI) {
+                            if (y == i0 + ty + 16 * q || y == j0 + tx + 16 * r) v = __int_as_float(0x7fc00000);
+                        }
+                        acc[q][r] = fmax2(acc[q][r], v);
+                    }
+            }
+        }
+    }
+    cp_async_wait<0>();
+
+    // ---------------- epilogue ----------------
+    int any_changed = 0;
+    unsigned long long removed = 0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const int64_t i = i0 + ty + 16 * q;
+        if (i >= p.rows) continue;
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            const int64_t j = j0 + tx + 16 * r;
+            if (j >= p.cols) continue;
+            const float m = acc[q][r];
+            if (MODE == MM_PLAIN) {
+                p.C[i * p.ldc + j] = m;
+                if (mirror) p.C[j * p.ldc + i] = m;
+            } else if (MODE == MM_RATIO) {
+                p.R[i * p.ldr + j] = ratio_of(p.E[i * p.lde + j], m);
+                if (p.C) p.C[i * p.ldc + j] = m;
+                if (mirror) {
+                    p.R[j * p.ldr + i] = ratio_of(p.E[j * p.lde + i], m);
+                    if (p.C) p.C[j * p.ldc + i] = m;
+                }
+            } else if (MODE == MM_CLOSURE) {
+                const float e = p.E[i * p.lde + j];
+                const float v = (e < m) ? m : e;  // std::max(e, m)
+                p.C[i * p.ldc + j] = v;
+                any_changed |= (v != e);
+                if (mirror) {
+                    const float e2 = p.E[j * p.lde + i];
+                    const float v2 = (e2 < m) ? m : e2;
+                    p.C[j * p.ldc + i] = v2;
+                    any_changed |= (v2 != e2);
+                }
+            } else {  // MM_DPI
+                {
+                    const float e = p.E[i * p.lde + j];
+                    const float ixz = (float)((double)e * p.tol_mult);
+                    const bool del = (i == j) || (m >= ixz);
+                    const float o = del ? 0.0f : e;
+                    p.C[i * p.ldc + j] = o;
+                    removed += (o != e);
+                    if (p.mask) p.mask[i * p.ldmask + j] = del ? 1 : 0;
+                }
+                if (mirror) {
+                    const float e = p.E[j * p.lde + i];
+                    const float ixz = (float)((double)e * p.tol_mult);
+                    const bool del = (m >= ixz);
+                    const float o = del ? 0.0f : e;
+                    p.C[j * p.ldc + i] = o;
+                    removed += (o != e);
+                    if (p.mask) p.mask[j * p.ldmask + i] = del ? 1 : 0;
+                }
+            }
+        }
+    }
+    if (MODE == MM_CLOSURE) {
+        if (__syncthreads_or(any_changed) && tid == 0) atomicOr(p.changed, 1);
+    }
+    if (MODE == MM_DPI && p.removed) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) removed += __shfl_xor_sync(0xffffffffu, removed, o);
+        if (lane == 0 && removed) atomicAdd(p.removed, removed);
+    }
+}
+
+template <int MODE, bool SYMM>
+cudaError_t launch_one(const MaxminParams& p, cudaStream_t stream) {
+    auto kern = maxmin_kernel<MODE, SYMM>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    dim3 grid((unsigned)ceil_div(p.cols, BN), (unsigned)ceil_div(p.rows, BM));
+    kern<<<grid, THREADS, SMEM_BYTES, stream>>>(p);
+    return cudaGetLastError();
+}
+
+// ---------------- element-wise helpers ----------------
+__global__ void ratio_kernel_ew(const float* A, int64_t lda, const float* M, int64_t ldm, int64_t rows, int64_t cols,
+                                float* R, int64_t ldr) {
+    const int64_t total = rows * cols;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = t / cols, j = t - i * cols;
+        R[i * ldr + j] = ratio_of(A[i * lda + j], M[i * ldm + j]);
+    }
+}
+
+__global__ void set_diag_kernel(float* A, int64_t nd, int64_t lda, float v) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < nd) A[i * lda + i] = v;
+}
+
+// out = max(M, M^T) through a 32x32 shared-memory tile (max_kernel, combine.hpp:42-58).
+__global__ void max_transpose_kernel(const float* M, int64_t n, int64_t ldm, float* out, int64_t ldo) {
+    __shared__ float tile[32][33];
+    const int64_t bi = (int64_t)blockIdx.y * 32, bj = (int64_t)blockIdx.x * 32;
+    // load the transposed block M[bj.., bi..]
+    for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+        const int64_t gi = bj + r, gj = bi + threadIdx.x;
+        tile[r][threadIdx.x] = (gi < n && gj < n) ? M[gi * ldm + gj] : 0.0f;
+    }
+    __syncthreads();
+    for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+        const int64_t i = bi + r, j = bj + threadIdx.x;
+        if (i < n && j < n) {
+            const float a = M[i * ldm + j];
+            const float b = tile[threadIdx.x][r];  // = M[j][i]
+            out[i * ldo + j] = (a < b) ? b : a;    // std::max(in, aux)
+        }
+    }
+}
+
+__global__ void copy2d_kernel(const float* src, int64_t lds, float* dst, int64_t ldd, int64_t rows, int64_t cols) {
+    const int64_t total = rows * cols;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = t / cols, j = t - i * cols;
+        dst[i * ldd + j] = src[i * lds + j];
+    }
+}
+
+unsigned ew_blocks(int64_t total) {
+    int64_t b = ceil_div(total, 256);
+    if (b > 152 * 32) b = 152 * 32;
+    if (b < 1) b = 1;
+    return (unsigned)b;
+}
+
+}  // namespace
+
+cudaError_t launch_maxmin(const MaxminParams& p, int mode, int symmetric, cudaStream_t stream, int64_t* launches) {
+    if (p.rows <= 0 || p.cols <= 0) return cudaSuccess;
+    if (launches) ++*launches;
+    const bool s = symmetric != 0;
+    switch (mode) {
+        case MM_PLAIN: return s ? launch_one<MM_PLAIN, true>(p, stream) : launch_one<MM_PLAIN, false>(p, stream);
+        case MM_RATIO: return s ? launch_one<MM_RATIO, true>(p, stream) : launch_one<MM_RATIO, false>(p, stream);
+        case MM_CLOSURE: return s ? launch_one<MM_CLOSURE, true>(p, stream) : launch_one<MM_CLOSURE, false>(p, stream);
+        case MM_DPI: return s ? launch_one<MM_DPI, true>(p, stream) : launch_one<MM_DPI, false>(p, stream);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_ratio(const float* A, int64_t lda, const float* M, int64_t ldm, int64_t rows, int64_t cols,
+                         float* R, int64_t ldr, cudaStream_t stream, int64_t* launches) {
+    if (rows <= 0 || cols <= 0) return cudaSuccess;
+    if (launches) ++*launches;
+    ratio_kernel_ew<<<ew_blocks(rows * cols), 256, 0, stream>>>(A, lda, M, ldm, rows, cols, R, ldr);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_set_diagonal(float* A, int64_t rows, int64_t cols, int64_t lda, float value, cudaStream_t stream,
+                                int64_t* launches) {
+    const int64_t nd = rows < cols ? rows : cols;
+    if (nd <= 0 || value < 0.0f) return cudaSuccess;
+    if (launches) ++*launches;
+    set_diag_kernel<<<(unsigned)ceil_div(nd, 256), 256, 0, stream>>>(A, nd, lda, value);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_max_transpose(const float* M, int64_t n, int64_t ldm, float* out, int64_t ldo, cudaStream_t stream,
+                                 int64_t* launches) {
+    if (n <= 0) return cudaSuccess;
+    if (launches) ++*launches;
+    dim3 grid((unsigned)ceil_div(n, 32), (unsigned)ceil_div(n, 32));
+    max_transpose_kernel<<<grid, dim3(32, 8), 0, stream>>>(M, n, ldm, out, ldo);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_copy2d(const float* src, int64_t lds, float* dst, int64_t ldd, int64_t rows, int64_t cols,
+                          cudaStream_t stream) {
+    if (rows <= 0 || cols <= 0) return cudaSuccess;
+    copy2d_kernel<<<ew_blocks(rows * cols), 256, 0, stream>>>(src, lds, dst, ldd, rows, cols);
+    return cudaGetLastError();
+}
+
+}  // namespace mcpg

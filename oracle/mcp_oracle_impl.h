@@ -1,0 +1,267 @@
+/* CPU restatement of MCPNet's hot-path arithmetic, instantiated once per
+ * precision by mcp_oracle.c (REAL = float or double, SFX = f32 or f64).
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is the oracle: tests, the smoke check and
+ * the CPU-baseline leg of the benchmark call it as the checker; the product
+ * never links or calls it.
+ *
+ * Every routine names the reference lines it restates (paths relative to the
+ * MCPNet source tree).  The reference's mixed-precision details are kept:
+ * where the reference multiplies a float by a double and stores into a float,
+ * so does this code.
+ */
+
+#define CAT2(a, b) a##_##b
+#define CAT(a, b) CAT2(a, b)
+#define FN(name) CAT(name, SFX)
+
+/* MinMaxScale::operator() -- include/mcp/correlation/BSplineMI.hpp:81-115 */
+static void FN(scale_row)(const REAL* in, int64_t m, REAL* out) {
+    REAL mn = m > 0 ? in[0] : (REAL)0;
+    REAL mx = m > 0 ? in[0] : (REAL)0;
+    for (int64_t j = 1; j < m; ++j) {
+        REAL x = in[j];
+        mn = (x < mn) ? x : mn; /* std::min(minX, x) */
+        mx = (mx < x) ? x : mx; /* std::max(maxX, x) */
+    }
+    REAL scale = (mx > mn) ? (REAL)(1.0 / (double)(mx - mn)) : (REAL)1.0;
+    REAL offset = (mx > mn) ? mn : (REAL)0.0;
+    for (int64_t j = 0; j < m; ++j) out[j] = scale * (in[j] - offset);
+}
+
+/* buildKnotVector<KT> -- BSplineMI.hpp:35-71.  knots has bins+order entries. */
+static void FN(knots)(int bins, int order, REAL* kv) {
+    int nint = bins - order;
+    double nf = 1.0 / (double)(nint + 1);
+    int i;
+    for (i = 0; i < order; ++i) kv[i] = (REAL)0;
+    for (i = order; i < order + nint; ++i) kv[i] = (REAL)((double)(REAL)(i - order + 1) * nf);
+    for (i = order + nint; i < 2 * order + nint; ++i) kv[i] = (REAL)1;
+}
+
+/* BSplineWeightsKernel::basisFunction (Cox-de Boor) -- BSplineMI.hpp:130-164 */
+static REAL FN(basis)(const REAL* kv, int bins, int i, int p, REAL t) {
+    REAL d1, n1, d2, n2, e1, e2;
+    if (p == 1) {
+        if ((t >= kv[i] && t < kv[i + 1] && kv[i] < kv[i + 1]) ||
+            (fabs((double)(REAL)(t - kv[i + 1])) < 1e-10 && (i + 1 == bins)))
+            return (REAL)1;
+        return (REAL)0;
+    }
+    d1 = kv[i + p - 1] - kv[i];
+    n1 = t - kv[i];
+    d2 = kv[i + p] - kv[i + 1];
+    n2 = kv[i + p] - t;
+    if (d1 < 1e-10 && d2 < 1e-10) {
+        return (REAL)0;
+    } else if (d1 < 1e-10) {
+        e1 = (REAL)0;
+        e2 = n2 / d2 * FN(basis)(kv, bins, i + 1, p - 1, t);
+    } else if (d2 < 1e-10) {
+        e2 = (REAL)0;
+        e1 = n1 / d1 * FN(basis)(kv, bins, i, p - 1, t);
+    } else {
+        e1 = n1 / d1 * FN(basis)(kv, bins, i, p - 1, t);
+        e2 = n2 / d2 * FN(basis)(kv, bins, i + 1, p - 1, t);
+    }
+    if (e1 + e2 < 0) return (REAL)0;
+    return e1 + e2;
+}
+
+/* BSplineWeightsKernel::operator() + entropy1d_2 -- BSplineMI.hpp:204-224,248-273.
+ * Row layout per gene: w[bin*m + s] (bin-major), then w[bins*m] = H_g in bits. */
+static void FN(weights_row)(const REAL* kv, const REAL* x, int64_t m, int bins, int order, REAL* w) {
+    int64_t nw = (int64_t)bins * m;
+    double nf = 1.0 / (double)m;
+    for (int64_t i = 0; i < nw; ++i) {
+        int64_t b = i / m, s = i - b * m;
+        w[i] = FN(basis)(kv, bins, (int)b, order, x[s]);
+    }
+    REAL H = 0;
+    int64_t idx = 0;
+    for (int b = 0; b < bins; ++b) {
+        REAL ex = 0;
+        for (int64_t s = 0; s < m; ++s) { ex = (REAL)((double)ex + (double)w[idx] * nf); ++idx; }
+        if (ex > 0.0) H = (REAL)((double)H + (double)ex * log2((double)ex));
+    }
+    w[nw] = (REAL)(0.0 - (double)H);
+}
+
+/* compute_mi steps 1-2: scale then weights -- apps/pipeline/mcpnet_helper.hpp:58-80 */
+void FN(orc_bspline_weights)(const REAL* X, int64_t n, int64_t m, int64_t ldx, int bins, int order, REAL* W) {
+    int64_t ldw = (int64_t)bins * m + 1;
+    REAL kv[64];
+    FN(knots)(bins, order, kv);
+#pragma omp parallel
+    {
+        REAL* sc = (REAL*)malloc(sizeof(REAL) * (size_t)(m > 0 ? m : 1));
+#pragma omp for schedule(dynamic, 4)
+        for (int64_t g = 0; g < n; ++g) {
+            FN(scale_row)(X + g * ldx, m, sc);
+            FN(weights_row)(kv, sc, m, bins, order, W + g * ldw);
+        }
+        free(sc);
+    }
+}
+
+/* BSplineEntropyKernel::entropy2d_simd + BSplineMIKernel::operator()
+ * -- BSplineMI.hpp:288-315,492-499.  The splash dot product is restated as a
+ * sequential accumulation in REAL (its real summation order is not in the
+ * reference snapshot).  norm_factor is REAL(1)/REAL(m) (BSplineMI.hpp:321). */
+static REAL FN(pair_mi)(const REAL* wx, const REAL* wy, int64_t m, int bins) {
+    REAL nf = (REAL)1 / (REAL)m;
+    REAL H = 0;
+    for (int bx = 0; bx < bins; ++bx) {
+        for (int by = 0; by < bins; ++by) {
+            const REAL* a = wx + (int64_t)bx * m;
+            const REAL* b = wy + (int64_t)by * m;
+            REAL hx = 0;
+            for (int64_t s = 0; s < m; ++s) hx += a[s] * b[s];
+            hx *= nf;
+            if (hx > 0.0) H = (REAL)((double)H + (double)hx * log2((double)hx));
+        }
+    }
+    REAL e2d = (REAL)(0.0 - (double)H);
+    int64_t e1 = (int64_t)bins * m;
+    return wx[e1] + wy[e1] - e2d;
+}
+
+/* compute_mi step 4: InnerProduct<..., SYMM=true> -- mcpnet_helper.hpp:88-98 */
+void FN(orc_bspline_mi_from_weights)(const REAL* W, int64_t n, int64_t m, int bins, REAL* MI, int64_t ldmi) {
+    int64_t ldw = (int64_t)bins * m + 1;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t i = 0; i < n; ++i)
+        for (int64_t j = i; j < n; ++j) {
+            REAL v = FN(pair_mi)(W + i * ldw, W + j * ldw, m, bins);
+            MI[i * ldmi + j] = v;
+            MI[j * ldmi + i] = v;
+        }
+}
+
+void FN(orc_bspline_mi)(const REAL* X, int64_t n, int64_t m, int64_t ldx, int bins, int order, REAL* MI, int64_t ldmi) {
+    int64_t ldw = (int64_t)bins * m + 1;
+    REAL* W = (REAL*)malloc(sizeof(REAL) * (size_t)(n * ldw > 0 ? n * ldw : 1));
+    FN(orc_bspline_weights)(X, n, m, ldx, bins, order, W);
+    FN(orc_bspline_mi_from_weights)(W, n, m, bins, MI, ldmi);
+    free(W);
+}
+
+/* Mutual information of the gene pairs (i, j) with i in [r0, r1), all j, into
+ * MI rows r0..r1-1 (a row slab, used to time a bounded CPU sample). */
+void FN(orc_bspline_mi_rows)(const REAL* W, int64_t n, int64_t m, int bins, int64_t r0, int64_t r1, REAL* MI, int64_t ldmi) {
+    int64_t ldw = (int64_t)bins * m + 1;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t i = r0; i < r1; ++i)
+        for (int64_t j = 0; j < n; ++j)
+            MI[(i - r0) * ldmi + j] = FN(pair_mi)(W + i * ldw, W + j * ldw, m, bins);
+}
+
+/* max_of_pairmin_scalar -- include/mcp/filter/simd_maxmin.hpp:30-46 (the float
+ * dispatch at :447-450 always takes this scalar form). */
+static REAL FN(max_of_pairmin)(const REAL* xx, const REAL* yy, int64_t count) {
+    REAL val = (REAL)(-DBL_MAX); /* numeric_limits<double>::lowest(), -inf for float */
+    for (int64_t i = 0; i < count; ++i) {
+        REAL a = xx[i], b = yy[i];
+        REAL mn = (b < a) ? b : a;   /* std::min(a, b) */
+        val = (val < mn) ? mn : val; /* std::max(val, mn) */
+    }
+    return val;
+}
+
+/* mcp2_maxmin_kernel<IT,false,true> over all (i, j): C = A (x) B, the
+ * InnerProduct convention C[i][j] = kernel(row A_i, row B_j) -- filter/mcp.hpp:72-93 */
+void FN(orc_maxmin)(const REAL* A, int64_t lda, const REAL* B, int64_t ldb, int64_t rows, int64_t cols,
+                    int64_t k, REAL* C, int64_t ldc) {
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t i = 0; i < rows; ++i)
+        for (int64_t j = 0; j < cols; ++j)
+            C[i * ldc + j] = FN(max_of_pairmin)(A + i * lda, B + j * ldb, k);
+}
+
+/* ratio_kernel<T,T> -- include/mcp/transform/combine.hpp:210-222 */
+void FN(orc_ratio)(const REAL* A, int64_t lda, const REAL* M, int64_t ldm, int64_t rows, int64_t cols,
+                   REAL* R, int64_t ldr) {
+    const REAL eps = (sizeof(REAL) == 4) ? (REAL)FLT_EPSILON : (REAL)DBL_EPSILON;
+    const REAL big = (sizeof(REAL) == 4) ? (REAL)FLT_MAX : (REAL)DBL_MAX;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < rows; ++i)
+        for (int64_t j = 0; j < cols; ++j) {
+            REAL a = A[i * lda + j], mm = M[i * ldm + j];
+            R[i * ldr + j] = (fabs((double)a) < eps) ? (REAL)0
+                           : (fabs((double)mm) < eps) ? big
+                           : (REAL)((double)a / (double)mm);
+        }
+}
+
+/* max_kernel over (M, M^T) -- combine.hpp:42-58 as used by apps/filter/mcp.cpp:463-476 */
+void FN(orc_max_transpose)(const REAL* M, int64_t n, int64_t ldm, REAL* out, int64_t ldo) {
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i)
+        for (int64_t j = 0; j < n; ++j) {
+            REAL a = M[i * ldm + j], b = M[j * ldm + i];
+            out[i * ldo + j] = (a < b) ? b : a;
+        }
+}
+
+/* dpi_kernel<IT,true,true> -- include/mcp/filter/dpi.hpp:42-69, followed by
+ * mask<IT,true> -- include/mcp/filter/threshold.hpp:33-54, as driven by
+ * apps/filter/dpi.cpp:236-287.  Returns the "removed" count (mask.processed). */
+int64_t FN(orc_dpi)(const REAL* A, int64_t n, int64_t lda, double tol, REAL* out, int64_t ldo, uint8_t* mask) {
+    double tm = 1.0 / (1.0 - tol);
+    int64_t removed = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(+:removed)
+    for (int64_t x = 0; x < n; ++x) {
+        const REAL* rx = A + x * lda;
+        for (int64_t z = 0; z < n; ++z) {
+            const REAL* rz = A + z * lda;
+            int del;
+            if (x == z) {
+                del = 1;
+            } else {
+                REAL ixz = (REAL)((double)rx[z] * tm);
+                int64_t y = 0;
+                for (; y < n && (y == x || y == z || rx[y] < ixz || rz[y] < ixz); ++y) {}
+                del = y < n;
+            }
+            if (mask) mask[x * n + z] = (uint8_t)del;
+            REAL in = rx[z];
+            REAL o = del ? (REAL)0 : in;
+            out[x * ldo + z] = o;
+            removed += (o != in);
+        }
+    }
+    return removed;
+}
+
+/* Maximum-capacity closure by repeated squaring: B <- max(B, B (x) B) until no
+ * entry changes.  The reference has no closure routine; this is the oracle of
+ * the max-capacity-path form, built from the reference's max_of_pairmin
+ * (simd_maxmin.hpp:30-46).  Returns the number of products computed, or -1 if
+ * max_iter products left it still changing. */
+int FN(orc_closure)(const REAL* A, int64_t n, int64_t lda, REAL* out, int64_t ldo, int max_iter) {
+    REAL* cur = (REAL*)malloc(sizeof(REAL) * (size_t)(n * n > 0 ? n * n : 1));
+    REAL* nxt = (REAL*)malloc(sizeof(REAL) * (size_t)(n * n > 0 ? n * n : 1));
+    for (int64_t i = 0; i < n; ++i) memcpy(cur + i * n, A + i * lda, sizeof(REAL) * (size_t)n);
+    int it = 0, changed = 1;
+    while (changed && it < max_iter) {
+        changed = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(|:changed)
+        for (int64_t i = 0; i < n; ++i)
+            for (int64_t j = 0; j < n; ++j) {
+                REAL p = FN(max_of_pairmin)(cur + i * n, cur + j * n, n);
+                REAL c = cur[i * n + j];
+                REAL v = (c < p) ? p : c;
+                nxt[i * n + j] = v;
+                changed |= (v != c);
+            }
+        REAL* t = cur; cur = nxt; nxt = t;
+        ++it;
+    }
+    for (int64_t i = 0; i < n; ++i) memcpy(out + i * ldo, cur + i * n, sizeof(REAL) * (size_t)n);
+    free(cur); free(nxt);
+    return changed ? -1 : it;
+}
+
+#undef FN
+#undef CAT
+#undef CAT2

@@ -1,0 +1,263 @@
+"""ctypes access to the CPU oracle.  TEST INFRASTRUCTURE ONLY.
+
+Two libraries:
+  * ``port()``  -- oracle/_build/libmcporacle.so, the C restatement of the
+    reference arithmetic (oracle/mcp_oracle_impl.h); builds anywhere.
+  * ``ref()``   -- oracle/_ref/libmcpref.so, MCPNet's own kernels compiled from
+    the reference headers (oracle/ref/ref_driver.cpp); exists only where the
+    reference sources were present at build time.  ``None`` otherwise.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may use
+this module.  The product (mcpnet_gb300, libmcpgpu.so) never does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+PORT_LIB = HERE / "_build" / "libmcporacle.so"
+REF_LIB = HERE / "_ref" / "libmcpref.so"
+REF_FAST_LIB = HERE / "_ref" / "libmcpref_fastmath.so"
+REF_ROOT = Path(os.environ.get("MCPNET_REF_ROOT", "/root/reference"))
+
+_i64, _vp = C.c_int64, C.c_void_p
+
+
+def build(with_ref: bool | None = None) -> None:
+    """make the oracle (and the reference build when the reference tree exists)."""
+    subprocess.run(["make", "-s", "-C", str(HERE), "all"], check=True)
+    if with_ref is None:
+        with_ref = (REF_ROOT / "include" / "mcp").is_dir()
+    if with_ref:
+        subprocess.run(["make", "-s", "-C", str(HERE), "ref", "ref-fast", f"REF_ROOT={REF_ROOT}"], check=True)
+
+
+def _bind(L, sfx: str, prefix: str):
+    sig = {
+        "bspline_weights": (None, [_vp, _i64, _i64, _i64, C.c_int, C.c_int, _vp]),
+        "bspline_mi": (None, [_vp, _i64, _i64, _i64, C.c_int, C.c_int, _vp, _i64]),
+        "bspline_mi_from_weights": (None, [_vp, _i64, _i64, C.c_int, _vp, _i64]),
+        "bspline_mi_rows": (None, [_vp, _i64, _i64, C.c_int, _i64, _i64, _vp, _i64]),
+        "maxmin": (None, [_vp, _i64, _vp, _i64, _i64, _i64, _i64, _vp, _i64]),
+        "ratio": (None, [_vp, _i64, _vp, _i64, _i64, _i64, _vp, _i64]),
+        "max_transpose": (None, [_vp, _i64, _i64, _vp, _i64]),
+        "dpi": (C.c_int64, [_vp, _i64, _i64, C.c_double, _vp, _i64, _vp]),
+        "closure": (C.c_int, [_vp, _i64, _i64, _vp, _i64, C.c_int]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, f"{prefix}{name}_{sfx}", None)
+        if f is None:
+            continue
+        f.restype = res
+        f.argtypes = args
+
+
+class _Port:
+    """The C restatement (float and double)."""
+
+    def __init__(self, path: Path):
+        self.L = C.CDLL(str(path))
+        for sfx in ("f32", "f64"):
+            _bind(self.L, sfx, "orc_")
+        self.L.orc_num_threads.restype = C.c_int
+
+    @staticmethod
+    def _dt(a):
+        return "f32" if a.dtype == np.float32 else "f64"
+
+    def threads(self) -> int:
+        return int(self.L.orc_num_threads())
+
+    def bspline_weights(self, X, bins=10, order=3):
+        X = np.ascontiguousarray(X)
+        n, m = X.shape
+        W = np.empty((n, bins * m + 1), dtype=X.dtype)
+        getattr(self.L, f"orc_bspline_weights_{self._dt(X)}")(X.ctypes.data, n, m, m, bins, order, W.ctypes.data)
+        return W
+
+    def bspline_mi(self, X, bins=10, order=3):
+        X = np.ascontiguousarray(X)
+        n, m = X.shape
+        MI = np.empty((n, n), dtype=X.dtype)
+        getattr(self.L, f"orc_bspline_mi_{self._dt(X)}")(X.ctypes.data, n, m, m, bins, order, MI.ctypes.data, n)
+        return MI
+
+    def bspline_mi_from_weights(self, W, m, bins=10):
+        W = np.ascontiguousarray(W)
+        n = W.shape[0]
+        MI = np.empty((n, n), dtype=W.dtype)
+        getattr(self.L, f"orc_bspline_mi_from_weights_{self._dt(W)}")(W.ctypes.data, n, m, bins, MI.ctypes.data, n)
+        return MI
+
+    def bspline_mi_rows(self, W, m, r0, r1, bins=10):
+        W = np.ascontiguousarray(W)
+        n = W.shape[0]
+        out = np.empty((r1 - r0, n), dtype=W.dtype)
+        getattr(self.L, f"orc_bspline_mi_rows_{self._dt(W)}")(W.ctypes.data, n, m, bins, r0, r1, out.ctypes.data, n)
+        return out
+
+    def maxmin(self, A, B=None):
+        A = np.ascontiguousarray(A)
+        B = A if B is None else np.ascontiguousarray(B)
+        rows, k = A.shape
+        cols = B.shape[0]
+        Cm = np.empty((rows, cols), dtype=A.dtype)
+        getattr(self.L, f"orc_maxmin_{self._dt(A)}")(A.ctypes.data, k, B.ctypes.data, k, rows, cols, k,
+                                                     Cm.ctypes.data, cols)
+        return Cm
+
+    def ratio(self, A, M):
+        A, M = np.ascontiguousarray(A), np.ascontiguousarray(M)
+        rows, cols = A.shape
+        R = np.empty_like(A)
+        getattr(self.L, f"orc_ratio_{self._dt(A)}")(A.ctypes.data, cols, M.ctypes.data, cols, rows, cols,
+                                                    R.ctypes.data, cols)
+        return R
+
+    def max_transpose(self, M):
+        M = np.ascontiguousarray(M)
+        n = M.shape[0]
+        out = np.empty_like(M)
+        getattr(self.L, f"orc_max_transpose_{self._dt(M)}")(M.ctypes.data, n, n, out.ctypes.data, n)
+        return out
+
+    def dpi(self, A, tol=0.1):
+        """tol is the float tolerance of `dpi --single`; the multiplier uses (double)tol."""
+        A = np.ascontiguousarray(A)
+        n = A.shape[0]
+        out = np.empty_like(A)
+        mask = np.empty((n, n), dtype=np.uint8)
+        t = float(np.float32(tol)) if A.dtype == np.float32 else float(tol)
+        removed = getattr(self.L, f"orc_dpi_{self._dt(A)}")(A.ctypes.data, n, n, t, out.ctypes.data, n,
+                                                            mask.ctypes.data)
+        return out, mask, int(removed)
+
+    def closure(self, A, max_iter=64):
+        A = np.ascontiguousarray(A)
+        n = A.shape[0]
+        out = np.empty_like(A)
+        it = getattr(self.L, f"orc_closure_{self._dt(A)}")(A.ctypes.data, n, n, out.ctypes.data, n, max_iter)
+        return out, int(it)
+
+    # -- the reference's composite helpers, restated on top of the kernels --
+    def mcp(self, A, path_len, symmetrize=False):
+        """compute_mcp2/3/4 (apps/pipeline/mcpnet_helper.hpp:199-365); symmetrize as apps/filter/mcp.cpp:463-476."""
+        M1 = self.maxmin(A)
+        if path_len == 2:
+            M = M1
+        elif path_len == 3:
+            M = self.maxmin(A, M1)
+            if symmetrize:
+                M = self.max_transpose(M)
+        elif path_len == 4:
+            M = self.maxmin(M1)
+        else:
+            raise ValueError(path_len)
+        return M, self.ratio(A, M)
+
+
+class _Ref:
+    """MCPNet's own kernels driven over whole matrices (float, plus f64 MI)."""
+
+    def __init__(self, path: Path):
+        L = C.CDLL(str(path))
+        L.ref_bspline_weights_f32.argtypes = [_vp, _i64, _i64, _i64, C.c_int, C.c_int, _vp]
+        L.ref_bspline_weights_f64.argtypes = [_vp, _i64, _i64, _i64, C.c_int, C.c_int, _vp]
+        L.ref_bspline_mi_f32.argtypes = [_vp, _i64, _i64, _i64, C.c_int, C.c_int, _vp, _i64, _vp]
+        L.ref_bspline_mi_f64.argtypes = [_vp, _i64, _i64, _i64, C.c_int, C.c_int, _vp, _i64, _vp]
+        L.ref_maxmin_f32.argtypes = [_vp, _i64, _vp, _i64, _i64, _i64, _i64, _vp, _i64]
+        L.ref_maxmin_symm_f32.argtypes = [_vp, _i64, _i64, _vp, _i64]
+        L.ref_ratio_f32.argtypes = [_vp, _i64, _vp, _i64, _i64, _i64, _vp, _i64]
+        L.ref_max_transpose_f32.argtypes = [_vp, _i64, _i64, _vp, _i64]
+        L.ref_dpi_f32.argtypes = [_vp, _i64, _i64, C.c_float, _vp, _i64, _vp]
+        L.ref_dpi_f32.restype = C.c_int64
+        self.L = L
+
+    def bspline_weights(self, X, bins=10, order=3):
+        X = np.ascontiguousarray(X)
+        n, m = X.shape
+        W = np.empty((n, bins * m + 1), dtype=X.dtype)
+        f = self.L.ref_bspline_weights_f32 if X.dtype == np.float32 else self.L.ref_bspline_weights_f64
+        f(X.ctypes.data, n, m, m, bins, order, W.ctypes.data)
+        return W
+
+    def bspline_mi(self, X, bins=10, order=3):
+        X = np.ascontiguousarray(X)
+        n, m = X.shape
+        MI = np.empty((n, n), dtype=X.dtype)
+        f = self.L.ref_bspline_mi_f32 if X.dtype == np.float32 else self.L.ref_bspline_mi_f64
+        f(X.ctypes.data, n, m, m, bins, order, MI.ctypes.data, n, None)
+        return MI
+
+    def maxmin(self, A, B=None):
+        A = np.ascontiguousarray(A, dtype=np.float32)
+        rows, k = A.shape
+        if B is None:
+            Cm = np.empty((rows, rows), dtype=np.float32)
+            self.L.ref_maxmin_symm_f32(A.ctypes.data, k, rows, Cm.ctypes.data, rows)
+            return Cm
+        B = np.ascontiguousarray(B, dtype=np.float32)
+        cols = B.shape[0]
+        Cm = np.empty((rows, cols), dtype=np.float32)
+        self.L.ref_maxmin_f32(A.ctypes.data, k, B.ctypes.data, k, rows, cols, k, Cm.ctypes.data, cols)
+        return Cm
+
+    def ratio(self, A, M):
+        A, M = np.ascontiguousarray(A, dtype=np.float32), np.ascontiguousarray(M, dtype=np.float32)
+        rows, cols = A.shape
+        R = np.empty_like(A)
+        self.L.ref_ratio_f32(A.ctypes.data, cols, M.ctypes.data, cols, rows, cols, R.ctypes.data, cols)
+        return R
+
+    def max_transpose(self, M):
+        M = np.ascontiguousarray(M, dtype=np.float32)
+        n = M.shape[0]
+        out = np.empty_like(M)
+        self.L.ref_max_transpose_f32(M.ctypes.data, n, n, out.ctypes.data, n)
+        return out
+
+    def dpi(self, A, tol=0.1):
+        A = np.ascontiguousarray(A, dtype=np.float32)
+        n = A.shape[0]
+        out = np.empty_like(A)
+        mask = np.empty((n, n), dtype=np.uint8)
+        removed = self.L.ref_dpi_f32(A.ctypes.data, n, n, tol, out.ctypes.data, n, mask.ctypes.data)
+        return out, mask, int(removed)
+
+    def mcp(self, A, path_len, symmetrize=False):
+        M1 = self.maxmin(A)
+        if path_len == 2:
+            M = M1
+        elif path_len == 3:
+            M = self.maxmin(A, M1)
+            if symmetrize:
+                M = self.max_transpose(M)
+        else:
+            M = self.maxmin(M1)
+        return M, self.ratio(A, M)
+
+
+_port = None
+_ref = {}
+
+
+def port() -> _Port:
+    global _port
+    if _port is None:
+        if not PORT_LIB.exists():
+            build(with_ref=False)
+        _port = _Port(PORT_LIB)
+    return _port
+
+
+def ref(fast_math: bool = False):
+    """MCPNet's own kernels, or None when they were not built here."""
+    path = REF_FAST_LIB if fast_math else REF_LIB
+    if path not in _ref:
+        _ref[path] = _Ref(path) if path.exists() else None
+    return _ref[path]

@@ -1,0 +1,158 @@
+// Driver that runs MCPNet's OWN hot-path kernels (compiled from the reference
+// headers where they lie, see oracle/Makefile) over whole matrices, standing in
+// for the splash InnerProduct / Transform / BinaryOp patterns that are absent
+// from the reference snapshot.  Output goes to oracle/_ref/libmcpref.so.
+//
+// Test infrastructure only: used to pin the C restatement (oracle/mcp_oracle.c)
+// and to generate the golden fixtures under tests/golden/.  Nothing in the
+// product links it.
+//
+// Loops follow the reference call sites:
+//   compute_mi            apps/pipeline/mcpnet_helper.hpp:56-99
+//   compute_maxmin1/2/3   apps/pipeline/mcpnet_helper.hpp:188-196,247-268,335-355
+//   compute_ratio         apps/pipeline/mcpnet_helper.hpp:172-184
+//   DPI mask + apply      apps/filter/dpi.cpp:236-287
+//   MCP3 symmetrisation   apps/filter/mcp.cpp:463-476
+// The InnerProduct SYMM=true pattern is restated as "compute j >= i, mirror".
+#include <cstdint>
+#include <cstring>
+#include <vector>
+#include <limits>
+#include <algorithm>
+
+#include "mcp/correlation/BSplineMI.hpp"
+#include "mcp/filter/mcp.hpp"
+#include "mcp/filter/dpi.hpp"
+#include "mcp/filter/threshold.hpp"
+#include "mcp/transform/combine.hpp"
+
+namespace {
+
+template <typename T>
+void bspline_weights(T const* X, int64_t n, int64_t m, int64_t ldx, int bins, int order,
+                     T* W /* n x (bins*m+1) */) {
+    mcp::kernel::MinMaxScale<T> scaler;
+    mcp::kernel::BSplineWeightsKernel<T> wk(bins, order, (int)m);
+    std::vector<T> scaled(m);
+    const int64_t ldw = (int64_t)bins * m + 1;
+#pragma omp parallel for firstprivate(scaled) schedule(dynamic, 4)
+    for (int64_t g = 0; g < n; ++g) {
+        scaler(X + g * ldx, (size_t)m, scaled.data());
+        wk(scaled.data(), (size_t)m, W + g * ldw);
+    }
+}
+
+template <typename T>
+void bspline_mi(T const* X, int64_t n, int64_t m, int64_t ldx, int bins, int order,
+                T* MI, int64_t ldmi, T* W_out) {
+    const int64_t ldw = (int64_t)bins * m + 1;
+    std::vector<T> W((size_t)(n * ldw));
+    bspline_weights(X, n, m, ldx, bins, order, W.data());
+    if (W_out) std::memcpy(W_out, W.data(), W.size() * sizeof(T));
+    mcp::kernel::BSplineMIKernel<T> mik(bins, (int)m);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t i = 0; i < n; ++i) {
+        for (int64_t j = i; j < n; ++j) {
+            T v = mik(W.data() + i * ldw, W.data() + j * ldw, (size_t)ldw);
+            MI[i * ldmi + j] = v;
+            MI[j * ldmi + i] = v;
+        }
+    }
+}
+
+template <typename T>
+void maxmin(T const* A, int64_t lda, T const* B, int64_t ldb, int64_t rows, int64_t cols,
+            int64_t k, T* C, int64_t ldc) {
+    mcp::kernel::mcp2_maxmin_kernel<T, false, true> kern;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t i = 0; i < rows; ++i)
+        for (int64_t j = 0; j < cols; ++j)
+            C[i * ldc + j] = kern(A + i * lda, B + j * ldb, (size_t)k);
+}
+
+template <typename T>
+void maxmin_symm(T const* A, int64_t lda, int64_t n, T* C, int64_t ldc) {
+    mcp::kernel::mcp2_maxmin_kernel<T, false, true> kern;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t i = 0; i < n; ++i)
+        for (int64_t j = i; j < n; ++j) {
+            T v = kern(A + i * lda, A + j * lda, (size_t)n);
+            C[i * ldc + j] = v;
+            C[j * ldc + i] = v;
+        }
+}
+
+template <typename T>
+void ratio(T const* A, int64_t lda, T const* M, int64_t ldm, int64_t rows, int64_t cols,
+           T* R, int64_t ldr) {
+    mcp::kernel::ratio_kernel<T, T> kern;
+    for (int64_t i = 0; i < rows; ++i) kern(A + i * lda, M + i * ldm, (size_t)cols, R + i * ldr);
+}
+
+template <typename T>
+void max_transpose(T const* M, int64_t n, int64_t ldm, T* out, int64_t ldo) {
+    mcp::kernel::max_kernel<T> kern;
+    std::vector<T> row(n);
+    for (int64_t i = 0; i < n; ++i) {
+        for (int64_t j = 0; j < n; ++j) row[j] = M[j * ldm + i];
+        kern(M + i * ldm, row.data(), (size_t)n, out + i * ldo);
+    }
+}
+
+template <typename T>
+int64_t dpi(T const* A, int64_t n, int64_t lda, double tol, T* out, int64_t ldo, uint8_t* mask_out) {
+    mcp::kernel::dpi_kernel<T> kern(tol);
+    std::vector<uint8_t> mask((size_t)(n * n));
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t x = 0; x < n; ++x)
+        for (int64_t z = 0; z < n; ++z)
+            mask[x * n + z] = kern((size_t)x, (size_t)z, A + x * lda, A + z * lda, (size_t)n) ? 1 : 0;
+    mcp::kernel::mask<T, true> masker;
+    bool* b = new bool[n];
+    for (int64_t x = 0; x < n; ++x) {
+        for (int64_t z = 0; z < n; ++z) b[z] = mask[x * n + z] != 0;
+        masker(A + x * lda, b, (size_t)n, out + x * ldo);
+    }
+    delete[] b;
+    if (mask_out) std::memcpy(mask_out, mask.data(), mask.size());
+    return (int64_t)masker.processed;
+}
+
+}  // namespace
+
+extern "C" {
+
+void ref_bspline_weights_f32(const float* X, int64_t n, int64_t m, int64_t ldx, int bins, int order, float* W) {
+    bspline_weights<float>(X, n, m, ldx, bins, order, W);
+}
+void ref_bspline_weights_f64(const double* X, int64_t n, int64_t m, int64_t ldx, int bins, int order, double* W) {
+    bspline_weights<double>(X, n, m, ldx, bins, order, W);
+}
+void ref_bspline_mi_f32(const float* X, int64_t n, int64_t m, int64_t ldx, int bins, int order,
+                        float* MI, int64_t ldmi, float* W_out) {
+    bspline_mi<float>(X, n, m, ldx, bins, order, MI, ldmi, W_out);
+}
+void ref_bspline_mi_f64(const double* X, int64_t n, int64_t m, int64_t ldx, int bins, int order,
+                        double* MI, int64_t ldmi, double* W_out) {
+    bspline_mi<double>(X, n, m, ldx, bins, order, MI, ldmi, W_out);
+}
+void ref_maxmin_f32(const float* A, int64_t lda, const float* B, int64_t ldb, int64_t rows, int64_t cols,
+                    int64_t k, float* C, int64_t ldc) {
+    maxmin<float>(A, lda, B, ldb, rows, cols, k, C, ldc);
+}
+void ref_maxmin_symm_f32(const float* A, int64_t lda, int64_t n, float* C, int64_t ldc) {
+    maxmin_symm<float>(A, lda, n, C, ldc);
+}
+void ref_ratio_f32(const float* A, int64_t lda, const float* M, int64_t ldm, int64_t rows, int64_t cols,
+                   float* R, int64_t ldr) {
+    ratio<float>(A, lda, M, ldm, rows, cols, R, ldr);
+}
+void ref_max_transpose_f32(const float* M, int64_t n, int64_t ldm, float* out, int64_t ldo) {
+    max_transpose<float>(M, n, ldm, out, ldo);
+}
+// tol arrives as float, as under `--single` (apps/filter/dpi.cpp:63,69-74).
+int64_t ref_dpi_f32(const float* A, int64_t n, int64_t lda, float tol, float* out, int64_t ldo, uint8_t* mask) {
+    return dpi<float>(A, n, lda, (double)tol, out, ldo, mask);
+}
+
+}  // extern "C"

@@ -1,0 +1,46 @@
+import os
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+GOLDEN = ROOT / "tests" / "golden"
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (sm_103a) and the built libmcpgpu.so")
+
+
+@pytest.fixture(scope="session")
+def golden():
+    def load(name):
+        with np.load(GOLDEN / f"{name}.npz") as z:
+            return {k: z[k] for k in z.files}
+    return load
+
+
+@pytest.fixture(scope="session")
+def port():
+    from oracle import oracle as O
+    return O.port()
+
+
+@pytest.fixture(scope="session")
+def built_lib():
+    """Build libmcpgpu.so in-tree if stale and return the package."""
+    from mcpnet_gb300 import build as B
+    B.build()
+    import mcpnet_gb300 as M
+    return M
+
+
+@pytest.fixture(scope="session")
+def gpu(built_lib):
+    """A library handle on cuda:0; the GPU tests fail (not skip) without one."""
+    h = built_lib.Handle(0)
+    yield h
+    h.close()

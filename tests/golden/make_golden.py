@@ -1,0 +1,94 @@
+"""Generate the golden fixtures in this folder from MCPNet's OWN kernels.
+
+Runs the reference's hot-path headers compiled from the MCPNet source tree
+(oracle/ref/ref_driver.cpp -> oracle/_ref/libmcpref.so; the tree is read from
+$MCPNET_REF_ROOT, default /root/reference) on seeded synthetic inputs and
+stores inputs and outputs together, so the fixtures need neither the
+reference nor this script at test time.
+
+    python tests/golden/make_golden.py
+
+Fixtures (all float32 unless noted):
+  mi_*.npz       X, W (reference weight rows), MI32 (reference --single MI),
+                 MI64 (reference double MI, float64), bins, order
+  mcp_*.npz      A (MI with diagonal 0), M2/M3/M4 (max-min products of
+                 compute_mcp2/3/4), R2/R3/R4 (MCP ratios), M3s/R3s (mcp app's
+                 symmetrised MCP3), DPI_out, DPI_mask (uint8), DPI_removed, tol
+  maxmin_rect.npz  A (33 x 77), B (45 x 77) with negative entries, C = A (x) B
+  dpi_ties.npz   a matrix with repeated values and zeros, DPI outputs at tol 0 and 0.1
+"""
+from __future__ import annotations
+
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent.parent
+sys.path.insert(0, str(ROOT))
+
+from oracle import oracle as O  # noqa: E402
+
+
+def synth(n, m, seed):
+    import mcpnet_gb300 as M
+    return M.synth_grn(n, m, seed=seed)
+
+
+def main():
+    O.build(with_ref=True)
+    R = O.ref()
+    if R is None:
+        raise SystemExit("reference kernels not built (MCPNet sources not found)")
+
+    # ---- MI ----
+    for name, (n, m, seed, bins, order) in {
+        "mi_37x211": (37, 211, 11, 10, 3),
+        "mi_64x500": (64, 500, 12, 10, 3),
+        "mi_3x7": (3, 7, 13, 10, 3),
+        "mi_1x5": (1, 5, 14, 10, 3),
+        "mi_20x64_b8k2": (20, 64, 15, 8, 2),
+    }.items():
+        X = synth(n, m, seed)
+        W = R.bspline_weights(X, bins, order)
+        MI32 = R.bspline_mi(X, bins, order)
+        MI64 = R.bspline_mi(X.astype(np.float64), bins, order)
+        np.savez_compressed(HERE / f"{name}.npz", X=X, W=W, MI32=MI32, MI64=MI64, bins=bins, order=order)
+
+    # ---- MCP / DPI on an MI matrix ----
+    for name, (n, m, seed) in {"mcp_70": (70, 300, 21), "mcp_130": (130, 200, 22)}.items():
+        X = synth(n, m, seed)
+        A = R.bspline_mi(X)
+        np.fill_diagonal(A, 0.0)
+        out = {"A": A}
+        for pl in (2, 3, 4):
+            M, Rt = R.mcp(A, pl)
+            out[f"M{pl}"], out[f"R{pl}"] = M, Rt
+        M3s, R3s = R.mcp(A, 3, symmetrize=True)
+        out["M3s"], out["R3s"] = M3s, R3s
+        tol = np.float32(0.1)
+        o, mask, removed = R.dpi(A, tol)
+        out.update(DPI_out=o, DPI_mask=mask, DPI_removed=np.int64(removed), tol=tol)
+        np.savez_compressed(HERE / f"{name}.npz", **out)
+
+    # ---- rectangular max-min with negative values ----
+    rng = np.random.default_rng(31)
+    A = rng.normal(size=(33, 77)).astype(np.float32)
+    B = rng.normal(size=(45, 77)).astype(np.float32)
+    np.savez_compressed(HERE / "maxmin_rect.npz", A=A, B=B, C=R.maxmin(A, B))
+
+    # ---- DPI with ties and zeros ----
+    v = rng.integers(0, 4, size=(40, 40)).astype(np.float32) * np.float32(0.25)
+    T = np.maximum(v, v.T)
+    np.fill_diagonal(T, 0.0)
+    res = {"A": T}
+    for tag, tol in (("t0", np.float32(0.0)), ("t1", np.float32(0.1))):
+        o, mask, removed = R.dpi(T, tol)
+        res.update({f"out_{tag}": o, f"mask_{tag}": mask, f"removed_{tag}": np.int64(removed), f"tol_{tag}": tol})
+    np.savez_compressed(HERE / "dpi_ties.npz", **res)
+    print("wrote", sorted(p.name for p in HERE.glob("*.npz")))
+
+
+if __name__ == "__main__":
+    main()

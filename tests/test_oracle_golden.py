@@ -1,0 +1,146 @@
+"""Pins the CPU oracle (the C restatement) against fixtures produced by
+MCPNet's own kernels (tests/golden/make_golden.py), and -- where the reference
+build exists in this checkout -- against the reference directly."""
+import numpy as np
+import pytest
+
+MI_CASES = ["mi_37x211", "mi_64x500", "mi_3x7", "mi_1x5", "mi_20x64_b8k2"]
+
+
+@pytest.mark.parametrize("name", MI_CASES)
+def test_weights_bit_exact(port, golden, name):
+    g = golden(name)
+    W = port.bspline_weights(g["X"], int(g["bins"]), int(g["order"]))
+    # the weight block is bit-exact; the trailing H_g slot follows the
+    # reference's SIMD reduction order (entropy1d_2), so only ~1 ulp
+    assert np.array_equal(W[:, :-1], g["W"][:, :-1])
+    np.testing.assert_allclose(W[:, -1], g["W"][:, -1], rtol=0, atol=2e-6)
+
+
+@pytest.mark.parametrize("name", MI_CASES)
+def test_mi_matches_reference(port, golden, name):
+    g = golden(name)
+    bins, order = int(g["bins"]), int(g["order"])
+    mi32 = port.bspline_mi(g["X"], bins, order)
+    np.testing.assert_allclose(mi32, g["MI32"], rtol=0, atol=5e-6)  # bits
+    mi64 = port.bspline_mi(g["X"].astype(np.float64), bins, order)
+    np.testing.assert_allclose(mi64, g["MI64"], rtol=0, atol=1e-12)
+    assert np.array_equal(mi32, mi32.T)
+
+
+@pytest.mark.parametrize("name", ["mcp_70", "mcp_130"])
+def test_mcp_bit_exact(port, golden, name):
+    g = golden(name)
+    A = g["A"]
+    for pl in (2, 3, 4):
+        M, R = port.mcp(A, pl)
+        assert np.array_equal(M.view(np.uint32), g[f"M{pl}"].view(np.uint32)), pl
+        assert np.array_equal(R.view(np.uint32), g[f"R{pl}"].view(np.uint32)), pl
+    M, R = port.mcp(A, 3, symmetrize=True)
+    assert np.array_equal(M, g["M3s"]) and np.array_equal(R, g["R3s"])
+
+
+@pytest.mark.parametrize("name", ["mcp_70", "mcp_130"])
+def test_dpi_bit_exact(port, golden, name):
+    g = golden(name)
+    out, mask, removed = port.dpi(g["A"], float(g["tol"]))
+    assert np.array_equal(out.view(np.uint32), g["DPI_out"].view(np.uint32))
+    assert np.array_equal(mask, g["DPI_mask"])
+    assert removed == int(g["DPI_removed"])
+
+
+def test_dpi_ties(port, golden):
+    g = golden("dpi_ties")
+    for tag in ("t0", "t1"):
+        out, mask, removed = port.dpi(g["A"], float(g[f"tol_{tag}"]))
+        assert np.array_equal(out, g[f"out_{tag}"])
+        assert np.array_equal(mask, g[f"mask_{tag}"])
+        assert removed == int(g[f"removed_{tag}"])
+
+
+def test_maxmin_rect_negative(port, golden):
+    g = golden("maxmin_rect")
+    C = port.maxmin(g["A"], g["B"])
+    assert np.array_equal(C.view(np.uint32), g["C"].view(np.uint32))
+
+
+def test_maxmin_empty_k_is_minus_inf(port):
+    A = np.zeros((3, 0), np.float32)
+    C = port.maxmin(A)
+    assert np.all(np.isneginf(C))
+
+
+def test_ratio_edges(port):
+    A = np.array([[0.0, 1e-8, 0.5, -0.25, 3.0]], np.float32)
+    M = np.array([[0.0, 0.5, 0.0, 0.5, 7.0]], np.float32)
+    R = port.ratio(A, M)
+    assert R[0, 0] == 0 and R[0, 1] == 0
+    assert R[0, 2] == np.finfo(np.float32).max
+    assert R[0, 3] == np.float32(-0.5)
+    assert R[0, 4] == np.float32(np.float64(np.float32(3.0)) / np.float64(np.float32(7.0)))
+
+
+def test_closure_matches_spanning_tree_bottleneck(port):
+    """The squaring closure equals the bottleneck (max-capacity) path value
+    read off a maximum spanning tree, for every off-diagonal pair."""
+    rng = np.random.default_rng(3)
+    n = 40
+    A = rng.random((n, n)).astype(np.float32)
+    A = np.maximum(A, A.T)
+    np.fill_diagonal(A, 0)
+    B, it = port.closure(A)
+    assert it > 0
+    # Prim's maximum spanning tree, then widest path by DFS
+    in_t = np.zeros(n, bool); in_t[0] = True
+    best = A[0].astype(np.float64).copy(); par = np.zeros(n, int)
+    adj = [[] for _ in range(n)]
+    for _ in range(n - 1):
+        c = np.where(~in_t, best, -np.inf).argmax()
+        in_t[c] = True
+        adj[c].append((par[c], A[c, par[c]])); adj[par[c]].append((c, A[c, par[c]]))
+        upd = (~in_t) & (A[c] > best)
+        best[upd] = A[c][upd]; par[upd] = c
+    for s in range(n):
+        cap = np.full(n, np.inf, np.float32); seen = np.zeros(n, bool); st = [s]; seen[s] = True
+        while st:
+            u = st.pop()
+            for v, w in adj[u]:
+                if not seen[v]:
+                    seen[v] = True; cap[v] = min(cap[u], w); st.append(v)
+        off = np.arange(n) != s
+        assert np.array_equal(B[s, off], cap[off])
+
+
+def test_port_against_reference_build(port):
+    """Extra seeded shapes against MCPNet's own kernels (only where the
+    reference sources were available to build them)."""
+    from oracle import oracle as O
+    R = O.ref()
+    if R is None:
+        pytest.skip("reference build not present in this checkout")
+    rng = np.random.default_rng(7)
+    for n, m in ((5, 33), (17, 129), (40, 64)):
+        X = rng.random((n, m)).astype(np.float32)
+        assert np.array_equal(port.bspline_weights(X)[:, :-1], R.bspline_weights(X)[:, :-1])
+        np.testing.assert_allclose(port.bspline_mi(X), R.bspline_mi(X), rtol=0, atol=5e-6)
+        A = port.bspline_mi(X); np.fill_diagonal(A, 0)
+        for pl in (2, 3, 4):
+            a, b = port.mcp(A, pl), R.mcp(A, pl)
+            assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+        a, b = port.dpi(A, 0.1), R.dpi(A, 0.1)
+        assert np.array_equal(a[0], b[0]) and a[2] == b[2]
+
+
+def test_reference_fast_math_same_bytes(port):
+    """The reference's Release flags include -ffast-math; on the max-min / ratio /
+    DPI path that build gives the same bytes as the strict build."""
+    from oracle import oracle as O
+    R, RF = O.ref(), O.ref(fast_math=True)
+    if R is None or RF is None:
+        pytest.skip("reference build not present in this checkout")
+    rng = np.random.default_rng(8)
+    A = rng.random((60, 60)).astype(np.float32); A = np.maximum(A, A.T); np.fill_diagonal(A, 0)
+    for pl in (2, 3, 4):
+        a, b = R.mcp(A, pl), RF.mcp(A, pl)
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    assert np.array_equal(R.dpi(A, 0.1)[0], RF.dpi(A, 0.1)[0])
