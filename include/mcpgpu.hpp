@@ -1,0 +1,181 @@
+// C++ host mirror of MCPNet's helper-level compute calls on top of the mcpgpu
+// C ABI (mcpgpu.h).  Header-only; link against libmcpgpu.so.
+//
+// The function names, argument meaning and output shapes follow the
+// reference's helpers in apps/pipeline/mcpnet_helper.hpp so that a call site
+// switches by changing the namespace:
+//
+//   compute_mi(input, bins, dmi)          mcpnet_helper.hpp:56-99   (B-spline MI)
+//   compute_maxmin1/2/3(g2g, dmaxmin)     mcpnet_helper.hpp:189-196, 248-268, 336-355
+//   compute_ratio(mi, dmaxmin, dmcp)      mcpnet_helper.hpp:172-184
+//   compute_mcp2/3/4(g2g, dmcp)           mcpnet_helper.hpp:199-206, 271-278, 358-365
+//   dpi_filter(input, tol, out)           apps/filter/dpi.cpp:236-287
+//   set_diagonal(m, value)                apps/pipeline/mcpnet.cpp:299-308
+//
+// Matrices are float, row-major with a leading dimension (the layout of
+// splash::ds::aligned_matrix<float> with its padded column_bytes()).  Errors
+// throw mcpgpu::Error carrying the library status and message; there is no
+// CPU fallback.
+#pragma once
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "mcpgpu.h"
+
+namespace mcpgpu {
+
+class Error : public std::runtime_error {
+  public:
+    Error(int status, const std::string& msg) : std::runtime_error(msg), status_(status) {}
+    int status() const { return status_; }
+
+  private:
+    int status_;
+};
+
+// Owning host matrix (row-major, leading dimension >= columns).
+template <typename T>
+class Matrix {
+  public:
+    Matrix() = default;
+    Matrix(int64_t rows, int64_t cols, int64_t ld = -1)
+        : rows_(rows), cols_(cols), ld_(ld < 0 ? cols : ld), data_((size_t)(rows * (ld < 0 ? cols : ld))) {}
+    int64_t rows() const { return rows_; }
+    int64_t columns() const { return cols_; }
+    int64_t ld() const { return ld_; }
+    T* data(int64_t r = 0) { return data_.data() + r * ld_; }
+    const T* data(int64_t r = 0) const { return data_.data() + r * ld_; }
+    T& at(int64_t r, int64_t c) { return data_[(size_t)(r * ld_ + c)]; }
+    const T& at(int64_t r, int64_t c) const { return data_[(size_t)(r * ld_ + c)]; }
+    void resize(int64_t rows, int64_t cols) {
+        rows_ = rows;
+        cols_ = cols;
+        ld_ = cols;
+        data_.assign((size_t)(rows * cols), T());
+    }
+
+  private:
+    int64_t rows_ = 0, cols_ = 0, ld_ = 0;
+    std::vector<T> data_;
+};
+
+// One device, one CUDA stream; not thread-safe (as the C handle).
+class Context {
+  public:
+    explicit Context(int device = 0) {
+        int rc = mcpg_create(&h_, device);
+        if (rc) throw Error(rc, std::string("mcpg_create failed: ") + mcpg_status_string(rc));
+    }
+    ~Context() { mcpg_destroy(h_); }
+    Context(const Context&) = delete;
+    Context& operator=(const Context&) = delete;
+    mcpg_handle* handle() const { return h_; }
+    void check(int rc, const char* what) const {
+        if (rc) throw Error(rc, std::string(what) + ": " + mcpg_last_error(h_));
+    }
+
+  private:
+    mcpg_handle* h_ = nullptr;
+};
+
+enum class MIPrecision : int {
+    FP32 = MCPG_MI_FP32,
+    BF16 = MCPG_MI_BF16,
+    BF16X3 = MCPG_MI_BF16X3,
+    FP16 = MCPG_MI_FP16,
+    FP16X3 = MCPG_MI_FP16X3,
+};
+
+// compute_mi: scale -> B-spline weights (order 3, as the reference hard-codes)
+// -> all-pairs MI in bits.  dmi is resized to n x n.
+inline void compute_mi(Context& ctx, const Matrix<float>& input, int bins, Matrix<float>& dmi,
+                       MIPrecision prec = MIPrecision::BF16X3, int order = 3, std::vector<double>* H = nullptr) {
+    const int64_t n = input.rows(), m = input.columns();
+    dmi.resize(n, n);
+    if (H) H->assign((size_t)n, 0.0);
+    ctx.check(mcpg_bspline_mi(ctx.handle(), input.data(), n, m, input.ld(), bins, order, (int)prec, dmi.data(),
+                              dmi.ld(), H ? H->data() : nullptr),
+              "compute_mi");
+}
+
+inline void set_diagonal(Matrix<float>& mi, float value) {
+    if (value < 0.0f) return;
+    const int64_t mc = mi.rows() < mi.columns() ? mi.rows() : mi.columns();
+    for (int64_t i = 0; i < mc; ++i) mi.at(i, i) = value;
+}
+
+// InnerProduct(a, b) with mcp2_maxmin_kernel: out[i][j] = max_k min(a[i][k], b[j][k]).
+inline void maxmin(Context& ctx, const Matrix<float>& a, const Matrix<float>& b, Matrix<float>& out) {
+    if (a.columns() != b.columns()) throw Error(MCPG_ERR_ARG, "maxmin: operand column counts differ");
+    out.resize(a.rows(), b.rows());
+    ctx.check(mcpg_maxmin(ctx.handle(), a.data(), a.ld(), b.data(), b.ld(), a.rows(), b.rows(), a.columns(),
+                          out.data(), out.ld()),
+              "maxmin");
+}
+
+inline void compute_maxmin1(Context& ctx, const Matrix<float>& g2g, Matrix<float>& dmaxmin) {
+    maxmin(ctx, g2g, g2g, dmaxmin);
+}
+inline void compute_maxmin2(Context& ctx, const Matrix<float>& g2g, Matrix<float>& dmaxmin) {
+    dmaxmin.resize(g2g.rows(), g2g.columns());
+    ctx.check(mcpg_mcp(ctx.handle(), g2g.data(), g2g.rows(), g2g.ld(), 3, 0, dmaxmin.data(), dmaxmin.ld(), nullptr, 0),
+              "compute_maxmin2");
+}
+inline void compute_maxmin3(Context& ctx, const Matrix<float>& g2g, Matrix<float>& dmaxmin) {
+    dmaxmin.resize(g2g.rows(), g2g.columns());
+    ctx.check(mcpg_mcp(ctx.handle(), g2g.data(), g2g.rows(), g2g.ld(), 4, 0, dmaxmin.data(), dmaxmin.ld(), nullptr, 0),
+              "compute_maxmin3");
+}
+
+inline void compute_ratio(Context& ctx, const Matrix<float>& mi, const Matrix<float>& dmaxmin, Matrix<float>& dmcp) {
+    dmcp.resize(dmaxmin.rows(), dmaxmin.columns());
+    ctx.check(mcpg_ratio(ctx.handle(), mi.data(), mi.ld(), dmaxmin.data(), dmaxmin.ld(), dmaxmin.rows(),
+                         dmaxmin.columns(), dmcp.data(), dmcp.ld()),
+              "compute_ratio");
+}
+
+// compute_mcp{2,3,4}: ratio(mi, maxmin of path length L); the max-min matrix
+// is returned through `maxmin_out` when given.  symmetrize reproduces the mcp
+// app's max(M, M^T) step for MCP3.
+inline void compute_mcp(Context& ctx, const Matrix<float>& g2g, int path_len, Matrix<float>& dmcp,
+                        Matrix<float>* maxmin_out = nullptr, bool symmetrize = false) {
+    const int64_t n = g2g.rows();
+    dmcp.resize(n, n);
+    if (maxmin_out) maxmin_out->resize(n, n);
+    ctx.check(mcpg_mcp(ctx.handle(), g2g.data(), n, g2g.ld(), path_len, symmetrize ? 1 : 0,
+                       maxmin_out ? maxmin_out->data() : nullptr, maxmin_out ? maxmin_out->ld() : n, dmcp.data(),
+                       dmcp.ld()),
+              "compute_mcp");
+}
+inline void compute_mcp2(Context& ctx, const Matrix<float>& g2g, Matrix<float>& dmcp) { compute_mcp(ctx, g2g, 2, dmcp); }
+inline void compute_mcp3(Context& ctx, const Matrix<float>& g2g, Matrix<float>& dmcp) { compute_mcp(ctx, g2g, 3, dmcp); }
+inline void compute_mcp4(Context& ctx, const Matrix<float>& g2g, Matrix<float>& dmcp) { compute_mcp(ctx, g2g, 4, dmcp); }
+
+// The dpi app's filter: returns the reference's "Mask removing N elements" count.
+inline int64_t dpi_filter(Context& ctx, const Matrix<float>& input, float tolerance, Matrix<float>& output,
+                          std::vector<uint8_t>* mask = nullptr) {
+    const int64_t n = input.rows();
+    output.resize(n, n);
+    if (mask) mask->assign((size_t)(n * n), 0);
+    int64_t removed = 0;
+    ctx.check(mcpg_dpi(ctx.handle(), input.data(), n, input.ld(), tolerance, output.data(), output.ld(),
+                       mask ? mask->data() : nullptr, &removed),
+              "dpi_filter");
+    return removed;
+}
+
+// Maximum-capacity closure by repeated squaring; returns the number of products.
+inline int max_capacity_closure(Context& ctx, const Matrix<float>& a, Matrix<float>& out, int max_iter = 64) {
+    const int64_t n = a.rows();
+    out.resize(n, n);
+    int it = 0;
+    ctx.check(mcpg_closure(ctx.handle(), a.data(), n, a.ld(), max_iter, out.data(), out.ld(), &it),
+              "max_capacity_closure");
+    return it;
+}
+
+}  // namespace mcpgpu

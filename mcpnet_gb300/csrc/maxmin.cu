@@ -30,37 +30,63 @@
 namespace mcpg {
 namespace {
 
-constexpr int BM = 128, BN = 128, BK = 16, STAGES = 4, THREADS = 256;
+#ifndef MCPG_MM_BK
+#define MCPG_MM_BK 16
+#endif
+#ifndef MCPG_MM_STAGES
+#define MCPG_MM_STAGES 4
+#endif
+#ifndef MCPG_MM_MINB
+#define MCPG_MM_MINB 1
+#endif
+#ifndef MCPG_MM_KSTEP
+#define MCPG_MM_KSTEP 2
+#endif
+constexpr int BM = 128, BN = 128, BK = MCPG_MM_BK, STAGES = MCPG_MM_STAGES, THREADS = 256;
+constexpr int KSTEP = MCPG_MM_KSTEP;  // k values per shared-memory load (2: LDS.64, 4: LDS.128)
 constexpr int LDS = BK + 4;  // row stride in floats: 16B-aligned, 4 consecutive rows -> 4 distinct bank groups
 constexpr int TILE_FLOATS = BM * LDS;
 constexpr size_t SMEM_BYTES = (size_t)STAGES * 2 * TILE_FLOATS * sizeof(float);  // 80 KB
 
-// Per-thread view of the operand rows it stages: each thread copies the 16-byte
-// chunk q of rows r and r + 64 of both operand tiles.
+// Per-thread view of the operand rows it stages: with CPR = BK/4 chunks of 16
+// bytes per row, thread t copies chunk q = t % CPR of rows t / CPR + h * RSTEP
+// (h < CPR/2) of both operand tiles.
+constexpr int CPR = BK / 4;
+constexpr int HPT = CPR / 2;            // rows per thread per operand
+constexpr int RSTEP = THREADS / CPR;    // row step between a thread's rows
+static_assert(HPT * RSTEP * CPR == BM * CPR && BM == BN, "loader covers the tile");
+
 struct StageLoader {
-    const float* a0; const float* a1; const float* b0; const float* b1;  // row bases at k = 4q
+    const float* a[HPT];
+    const float* b[HPT];
     int64_t k_rem;   // k_len - 4q
     uint32_t soff;   // shared offset (floats) of chunk (r, q)
-    bool va0, va1, vb0, vb1;
+    uint32_t va, vb; // validity bit per row
 
     __device__ __forceinline__ void init(const MaxminParams& p, int64_t i0, int64_t j0, int tid) {
-        const int r = tid >> 2, q = tid & 3;
+        const int r = tid / CPR, q = tid % CPR;
         soff = r * LDS + q * 4;
         k_rem = p.k_len - 4 * q;
-        va0 = i0 + r < p.rows; va1 = i0 + r + 64 < p.rows;
-        vb0 = j0 + r < p.cols; vb1 = j0 + r + 64 < p.cols;
-        a0 = va0 ? p.A + (i0 + r) * p.lda + 4 * q : p.A;
-        a1 = va1 ? p.A + (i0 + r + 64) * p.lda + 4 * q : p.A;
-        b0 = vb0 ? p.B + (j0 + r) * p.ldb + 4 * q : p.B;
-        b1 = vb1 ? p.B + (j0 + r + 64) * p.ldb + 4 * q : p.B;
+        va = vb = 0;
+#pragma unroll
+        for (int h = 0; h < HPT; ++h) {
+            const int64_t gi = i0 + r + h * RSTEP, gj = j0 + r + h * RSTEP;
+            const bool oka = gi < p.rows, okb = gj < p.cols;
+            va |= (uint32_t)oka << h;
+            vb |= (uint32_t)okb << h;
+            a[h] = oka ? p.A + gi * p.lda + 4 * q : p.A;
+            b[h] = okb ? p.B + gj * p.ldb + 4 * q : p.B;
+        }
     }
     __device__ __forceinline__ void load(float* As, float* Bs, int64_t k0) const {
         const int64_t rem = k_rem - k0;
         const int kb = rem >= 4 ? 16 : (rem > 0 ? (int)rem * 4 : 0);
-        cp_async16(As + soff, va0 ? a0 + k0 : a0, va0 ? kb : 0);
-        cp_async16(As + soff + 64 * LDS, va1 ? a1 + k0 : a1, va1 ? kb : 0);
-        cp_async16(Bs + soff, vb0 ? b0 + k0 : b0, vb0 ? kb : 0);
-        cp_async16(Bs + soff + 64 * LDS, vb1 ? b1 + k0 : b1, vb1 ? kb : 0);
+#pragma unroll
+        for (int h = 0; h < HPT; ++h) {
+            const bool oka = (va >> h) & 1u, okb = (vb >> h) & 1u;
+            cp_async16(As + soff + h * RSTEP * LDS, oka ? a[h] + k0 : a[h], oka ? kb : 0);
+            cp_async16(Bs + soff + h * RSTEP * LDS, okb ? b[h] + k0 : b[h], okb ? kb : 0);
+        }
     }
 };
 
@@ -73,7 +99,7 @@ __device__ __forceinline__ float ratio_of(float a, float m) {
 }
 
 template <int MODE, bool SYMM>
-__global__ void __launch_bounds__(THREADS, 1) maxmin_kernel(const MaxminParams p) {
+__global__ void __launch_bounds__(THREADS, MCPG_MM_MINB) maxmin_kernel(const MaxminParams p) {
     extern __shared__ float4 smem_f4[];
     float* smem = reinterpret_cast<float*>(smem_f4);
 
@@ -127,17 +153,35 @@ __global__ void __launch_bounds__(THREADS, 1) maxmin_kernel(const MaxminParams p
             excl = (k0 < i0 + BM && k0 + BK > i0) || (k0 < j0 + BN && k0 + BK > j0);
         }
         if (kmax == BK && !excl) {
+            if (KSTEP == 2) {
 #pragma unroll
-            for (int kk = 0; kk < BK; kk += 2) {
-                float2 a[8];
+                for (int kk = 0; kk < BK; kk += 2) {
+                    float2 a[8];
 #pragma unroll
-                for (int q = 0; q < 8; ++q) a[q] = *reinterpret_cast<const float2*>(a_base + q * 16 * LDS + kk);
+                    for (int q = 0; q < 8; ++q) a[q] = *reinterpret_cast<const float2*>(a_base + q * 16 * LDS + kk);
 #pragma unroll
-                for (int r = 0; r < 8; ++r) {
-                    const float2 b = *reinterpret_cast<const float2*>(b_base + r * 16 * LDS + kk);
+                    for (int r = 0; r < 8; ++r) {
+                        const float2 b = *reinterpret_cast<const float2*>(b_base + r * 16 * LDS + kk);
 #pragma unroll
-                    for (int q = 0; q < 8; ++q)
-                        acc[q][r] = fmax3(acc[q][r], fmin2(a[q].x, b.x), fmin2(a[q].y, b.y));
+                        for (int q = 0; q < 8; ++q)
+                            acc[q][r] = fmax3(acc[q][r], fmin2(a[q].x, b.x), fmin2(a[q].y, b.y));
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int kk = 0; kk < BK; kk += 4) {
+                    float4 a[8];
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) a[q] = *reinterpret_cast<const float4*>(a_base + q * 16 * LDS + kk);
+#pragma unroll
+                    for (int r = 0; r < 8; ++r) {
+                        const float4 b = *reinterpret_cast<const float4*>(b_base + r * 16 * LDS + kk);
+#pragma unroll
+                        for (int q = 0; q < 8; ++q) {
+                            acc[q][r] = fmax3(acc[q][r], fmin2(a[q].x, b.x), fmin2(a[q].y, b.y));
+                            acc[q][r] = fmax3(acc[q][r], fmin2(a[q].z, b.z), fmin2(a[q].w, b.w));
+                        }
+                    }
                 }
             }
         } else {

@@ -1,0 +1,50 @@
+"""Tensor-core (tcgen05) B-spline MI against the reference's double-precision
+MI (golden fixtures) and the FP64 oracle.  Tolerances in bits (1 bit = ln 2
+nats); the benchmark spec's bound is 1e-4 nats = 1.44e-4 bits:
+  bf16x3 (hi+lo split) 2e-5 bits   fp16x3 2e-5 bits
+  fp16 (single)        2e-4 bits   bf16 (single) 3e-3 bits (does not meet the bound)
+The single-rounding forms carry one 16-bit rounding per weight, which only
+averages out over many samples: below 200 samples their bound is 10x looser.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"bf16x3": 2e-5, "fp16x3": 2e-5, "fp16": 2e-4, "bf16": 3e-3}
+MI_CASES = ["mi_37x211", "mi_64x500", "mi_3x7", "mi_1x5"]
+
+
+@pytest.mark.parametrize("prec", ["bf16x3", "bf16", "fp16", "fp16x3"])
+@pytest.mark.parametrize("name", MI_CASES)
+def test_mi_tc_golden(gpu, golden, name, prec):
+    g = golden(name)
+    MI = gpu.bspline_mi(g["X"], 10, 3, prec)
+    assert np.array_equal(MI, MI.T)
+    tol = TOL[prec] * (10 if prec in ("fp16", "bf16") and g["X"].shape[1] < 200 else 1)
+    np.testing.assert_allclose(MI, g["MI64"], rtol=0, atol=tol)
+
+
+@pytest.mark.parametrize("n,m", [(13, 64), (25, 65), (37, 300), (130, 1000), (251, 129)])
+def test_mi_bf16x3_vs_oracle(gpu, port, built_lib, n, m):
+    X = built_lib.synth_grn(n, m, seed=1000 + n + m)
+    ref = port.bspline_mi(X.astype(np.float64))
+    for prec in ("bf16x3", "fp16"):
+        MI = gpu.bspline_mi(X, 10, 3, prec)
+        err = np.abs(MI - ref).max()
+        tol = TOL[prec] * (10 if prec in ("fp16", "bf16") and m < 200 else 1)
+        assert err <= tol, (prec, err)
+
+
+def test_mi_tc_matches_fp32_path(gpu, built_lib):
+    X = built_lib.synth_grn(300, 700, seed=77)
+    a = gpu.bspline_mi(X, 10, 3, "fp32")
+    b = gpu.bspline_mi(X, 10, 3, "bf16x3")
+    assert np.abs(a - b).max() < 3e-5
+
+
+def test_mi_tc_unsupported_bins_report(gpu, built_lib):
+    X = built_lib.synth_grn(20, 64, seed=3)
+    with pytest.raises(built_lib.MCPGError) as e:
+        gpu.bspline_mi(X, 8, 3, "bf16x3")
+    assert e.value.status == built_lib.ERR_UNSUPPORTED
