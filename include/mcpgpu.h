@@ -49,6 +49,7 @@ typedef struct mcpg_handle mcpg_handle;
 #define MCPG_ERR_NOT_CONVERGED (-4) /* closure still changing after max_iter products */
 #define MCPG_ERR_UNSUPPORTED (-5)   /* feature unavailable on this device / build */
 #define MCPG_ERR_DEVICE_TIMEOUT (-6)/* a bounded device-side wait gave up */
+#define MCPG_ERR_SCRATCH_LIMIT (-7) /* problem too large for the no-allocation entry point's static scratch */
 
 /* ---- MI contraction precision (mcpg_bspline_mi*) ---- */
 #define MCPG_MI_FP32 0   /* FP32 weights, FP32 CUDA-core contraction */
@@ -158,6 +159,23 @@ MCPG_API int mcpg_closure(mcpg_handle* h, const float* A, int64_t n, int64_t lda
                           float* out, int64_t ldo, int* iterations);
 MCPG_API int mcpg_closure_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, int max_iter,
                               float* out, int64_t ldo, int* iterations);
+
+/* ---- B-spline MI without any device allocation (no counterpart in the reference) ----
+ * For callers that cannot call cudaMalloc -- an application whose device
+ * memory belongs entirely to its own pool allocator, or a latency-critical
+ * loop that cannot take cudaMalloc's implicit synchronisation.  Same result as
+ * mcpg_bspline_mi_dev(..., MCPG_MI_FP32, ...) with device pointers, enqueued on
+ * `cuda_stream` (0 = legacy default stream), no handle.  Its FP32 weight table
+ * lives in a file-scope device array of 32 MiB that every GPU loading this
+ * library holds until exit; problems whose table (ceil(m/16)*16 x
+ * ceil(n/16)*16*bins floats, plus n doubles when H is null) does not fit return
+ * MCPG_ERR_SCRATCH_LIMIT.  The first call on a device looks up the array's
+ * address with that device current: make it before any stream capture.  All
+ * calls share the array and it keeps the last call's contents (the call clears
+ * the padding it needs); calls that overlap on the GPU race on it.
+ * bins <= 12. */
+MCPG_API int mcpg_bspline_mi_fp32_noalloc(const float* X, int64_t n, int64_t m, int64_t ldx, int bins, int order,
+                                          float* MI, int64_t ldmi, double* H, void* cuda_stream);
 
 /* ---- testing hook: make the next `count` device scratch allocations of this
  * handle fail with MCPG_ERR_OOM (exercises the error path without a GPU fault). */

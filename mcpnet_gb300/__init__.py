@@ -30,6 +30,7 @@ _PKG = Path(__file__).resolve().parent
 LIB_PATH = _PKG / "_lib" / "libmcpgpu.so"
 
 OK, ERR_ARG, ERR_OOM, ERR_CUDA, ERR_NOT_CONVERGED, ERR_UNSUPPORTED, ERR_DEVICE_TIMEOUT = 0, -1, -2, -3, -4, -5, -6
+ERR_SCRATCH_LIMIT = -7
 PRECISIONS = {"fp32": 0, "bf16": 1, "bf16x3": 2, "fp16": 3, "fp16x3": 4}
 
 # (name, restype, argtypes) of every exported symbol -- the full C ABI.
@@ -62,6 +63,7 @@ ABI = [
     ("mcpg_closure", C.c_int, [_vp, _vp, _i64, _i64, C.c_int, _vp, _i64, C.POINTER(C.c_int)]),
     ("mcpg_closure_dev", C.c_int, [_vp, _vp, _i64, _i64, C.c_int, _vp, _i64, C.POINTER(C.c_int)]),
     ("mcpg_synth_grn", C.c_int, [_i64, _i64, C.c_uint64, _vp, _i64, _vp, _i64, C.POINTER(C.c_int64)]),
+    ("mcpg_bspline_mi_fp32_noalloc", C.c_int, [_vp, _i64, _i64, _i64, C.c_int, C.c_int, _vp, _i64, _vp, _vp]),
 ]
 
 _lib = None

@@ -491,6 +491,7 @@ const char* mcpg_status_string(int s) {
         case MCPG_ERR_NOT_CONVERGED: return "not converged";
         case MCPG_ERR_UNSUPPORTED: return "unsupported";
         case MCPG_ERR_DEVICE_TIMEOUT: return "device wait timed out";
+        case MCPG_ERR_SCRATCH_LIMIT: return "problem exceeds the 32 MiB static scratch of the no-allocation entry point";
         default: return "unknown status";
     }
 }
