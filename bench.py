@@ -127,36 +127,48 @@ def barrier(ws: int):
 
 
 # ---------------------------------------------------------------- CPU legs
-def cpu_mi_sample(n: int, m: int, target_s: float, seed: int):
-    """Time the CPU oracle's MI (the reference's float loops restated, OpenMP
-    over rows) on a row slab of the n x m workload; returns (pairs/s, info)."""
-    from oracle import oracle as O
-    import mcpnet_gb300 as M
-    P = O.port()
-    X = M.synth_grn(n, m, seed=seed)
-    W = P.bspline_weights(X)
-    t0 = time.perf_counter()
-    P.bspline_mi_rows(W, m, 0, 1)
-    t1 = time.perf_counter()
-    per_row = max(t1 - t0, 1e-4)
-    rows = int(max(1, min(n, target_s / per_row)))
-    t0 = time.perf_counter()
-    P.bspline_mi_rows(W, m, 0, rows)
-    dt = time.perf_counter() - t0
-    pairs = rows * n
-    return pairs / dt, {"rows": rows, "pairs": pairs, "seconds": dt, "threads": P.threads()}
+class CpuMiSampler:
+    """Times the reference's CPU MI (OpenMP over rows, float) on a row slab of
+    the n x m workload.  Uses MCPNet's own kernels where they were compiled for
+    this machine (oracle/_ref), else the oracle's restatement of them."""
+
+    def __init__(self, n: int, m: int, seed: int):
+        from oracle import oracle as O
+        import mcpnet_gb300 as M
+        self.n, self.m = n, m
+        R = O.ref()
+        self.kind = "reference" if R is not None else "port"
+        self.impl = R if R is not None else O.port()
+        X = M.synth_grn(n, m, seed=seed)
+        self.W = self.impl.bspline_weights(X)
+        self.threads = O.port().threads()
+
+    def run(self, target_s: float):
+        t0 = time.perf_counter()
+        self.impl.bspline_mi_rows(self.W, self.m, 0, 1)
+        per_row = max(time.perf_counter() - t0, 1e-4)
+        rows = int(max(1, min(self.n, target_s / per_row)))
+        t0 = time.perf_counter()
+        self.impl.bspline_mi_rows(self.W, self.m, 0, rows)
+        dt = time.perf_counter() - t0
+        pairs = rows * self.n
+        return pairs / dt, {"rows": rows, "pairs": pairs, "seconds": dt, "threads": self.threads}
+
+    def describe(self, info) -> str:
+        src = ("MCPNet's BSplineMIKernel compiled from the reference sources" if self.kind == "reference"
+               else "the reference's loops restated in oracle/")
+        return (f"MI of rows 0..{info['rows']} x all {self.n} genes ({info['pairs']} pairs), m={self.m}, float, "
+                f"{info['seconds']:.1f} s, OpenMP over rows; {src}")
 
 
 def reference_arm(args, ws, rank):
     if rank != 0:
         return
-    from oracle import oracle as O
-    O.port()
-    kind = "port"
+    sampler = CpuMiSampler(args.genes, args.samples, args.seed)
     vals = []
     info = {}
     for i in range(args.warmup + args.steps):
-        v, info = cpu_mi_sample(args.genes, args.samples, args.ref_seconds, args.seed)
+        v, info = sampler.run(args.ref_seconds)
         if i >= args.warmup:
             vals.append(v)
     value = float(np.mean(vals))
@@ -166,10 +178,8 @@ def reference_arm(args, ws, rank):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": workload_config(args, "fp32-cpu"),
         "ms_per_step": info["seconds"] * 1e3,
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": info["threads"], "kind": kind,
-                         "sample": f"MI of rows 0..{info['rows']} x all {args.genes} genes "
-                                   f"({info['pairs']} pairs) per step, m={args.samples}, float, "
-                                   "OpenMP over rows (reference loops restated in oracle/)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": info["threads"], "kind": sampler.kind,
+                         "sample": sampler.describe(info) + " (per step)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -364,11 +374,10 @@ def gpu_arm(args, ws, rank, local):
 
     # ---- CPU baseline (rank 0, N = 1 only) ----
     if rank == 0 and ws == 1 and not args.no_cpu:
-        v, info = cpu_mi_sample(n, m, args.cpu_seconds, args.seed)
-        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": info["threads"], "kind": "port",
-                                "sample": f"MI of rows 0..{info['rows']} x all {n} genes ({info['pairs']} pairs), "
-                                          f"m={m}, float, {info['seconds']:.1f} s; reference loops restated "
-                                          "in oracle/ (OpenMP over rows)"}
+        sampler = CpuMiSampler(n, m, args.seed)
+        v, info = sampler.run(args.cpu_seconds)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": info["threads"], "kind": sampler.kind,
+                                "sample": sampler.describe(info)}
     h.close()
     if rank == 0:
         print(json.dumps(line), flush=True)

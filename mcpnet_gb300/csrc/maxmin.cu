@@ -10,11 +10,12 @@
 //
 // Kernel shape (FP32 ALU bound, no tensor cores):
 //  - CTA tile 128 x 128 outputs, 256 threads, 8 x 8 outputs per thread held in
-//    registers; k staged through shared memory in 16-wide slices by a 4-stage
+//    registers; k staged through shared memory in 32-wide slices by a 3-stage
 //    cp.async pipeline (operand rows are k-contiguous in HBM, so no transpose).
-//  - inner step per thread and k pair: 16 LDS.64 feed 64 x (min, min, max3):
+//  - inner step per thread and 4 k: 16 LDS.128 feed 64 x 2 x (min, min, max3):
 //    1.5 FP32 min/max instructions per (i, j, k) triple using the sm_100+
-//    3-input max.
+//    3-input max.  (BK 32 / 3 stages / LDS.128 measured best of a sweep over
+//    BK 16-32, 3-4 stages, LDS.64/128 on GB300.)
 //  - fused epilogues: MCP ratio (combine.hpp:210-222), closure step
 //    B <- max(B, B (x) B) with a changed flag, DPI mask + apply
 //    (dpi.hpp:56-68, threshold.hpp:46-53) with the y in {x, z} exclusion done
@@ -31,16 +32,16 @@ namespace mcpg {
 namespace {
 
 #ifndef MCPG_MM_BK
-#define MCPG_MM_BK 16
+#define MCPG_MM_BK 32
 #endif
 #ifndef MCPG_MM_STAGES
-#define MCPG_MM_STAGES 4
+#define MCPG_MM_STAGES 3
 #endif
 #ifndef MCPG_MM_MINB
 #define MCPG_MM_MINB 1
 #endif
 #ifndef MCPG_MM_KSTEP
-#define MCPG_MM_KSTEP 2
+#define MCPG_MM_KSTEP 4
 #endif
 constexpr int BM = 128, BN = 128, BK = MCPG_MM_BK, STAGES = MCPG_MM_STAGES, THREADS = 256;
 constexpr int KSTEP = MCPG_MM_KSTEP;  // k values per shared-memory load (2: LDS.64, 4: LDS.128)

@@ -176,7 +176,18 @@ class _Ref:
         L.ref_max_transpose_f32.argtypes = [_vp, _i64, _i64, _vp, _i64]
         L.ref_dpi_f32.argtypes = [_vp, _i64, _i64, C.c_float, _vp, _i64, _vp]
         L.ref_dpi_f32.restype = C.c_int64
+        L.ref_bspline_mi_rows_f32.argtypes = [_vp, _i64, _i64, C.c_int, _i64, _i64, _vp, _i64]
         self.L = L
+
+    def bspline_mi_rows(self, W, m, r0, r1, bins=10):
+        W = np.ascontiguousarray(W, dtype=np.float32)
+        n = W.shape[0]
+        out = np.empty((r1 - r0, n), dtype=np.float32)
+        self.L.ref_bspline_mi_rows_f32(W.ctypes.data, n, m, bins, r0, r1, out.ctypes.data, n)
+        return out
+
+    def threads(self) -> int:
+        return port().threads()
 
     def bspline_weights(self, X, bins=10, order=3):
         X = np.ascontiguousarray(X)
@@ -259,5 +270,8 @@ def ref(fast_math: bool = False):
     """MCPNet's own kernels, or None when they were not built here."""
     path = REF_FAST_LIB if fast_math else REF_LIB
     if path not in _ref:
-        _ref[path] = _Ref(path) if path.exists() else None
+        try:
+            _ref[path] = _Ref(path) if path.exists() else None
+        except OSError:  # built for another machine
+            _ref[path] = None
     return _ref[path]

@@ -136,6 +136,16 @@ void ref_bspline_mi_f64(const double* X, int64_t n, int64_t m, int64_t ldx, int 
                         double* MI, int64_t ldmi, double* W_out) {
     bspline_mi<double>(X, n, m, ldx, bins, order, MI, ldmi, W_out);
 }
+// MI of the pairs (i, j), i in [r0, r1), all j, from reference weight rows
+// (a row slab of the InnerProduct, used to time a bounded CPU sample).
+void ref_bspline_mi_rows_f32(const float* W, int64_t n, int64_t m, int bins, int64_t r0, int64_t r1, float* out,
+                             int64_t ldo) {
+    const int64_t ldw = (int64_t)bins * m + 1;
+    mcp::kernel::BSplineMIKernel<float> mik(bins, (int)m);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t i = r0; i < r1; ++i)
+        for (int64_t j = 0; j < n; ++j) out[(i - r0) * ldo + j] = mik(W + i * ldw, W + j * ldw, (size_t)ldw);
+}
 void ref_maxmin_f32(const float* A, int64_t lda, const float* B, int64_t ldb, int64_t rows, int64_t cols,
                     int64_t k, float* C, int64_t ldc) {
     maxmin<float>(A, lda, B, ldb, rows, cols, k, C, ldc);
