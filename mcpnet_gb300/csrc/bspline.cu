@@ -51,19 +51,30 @@ void host_knots(int bins, int order, Knots& k) {
 // All bins' basis values at t, bottom-up.  N[i] holds basis(i, p, t) for the
 // current p.  Each value is produced by the same float operations as the
 // recursive reference (divide, multiply, add, clamp), so the results agree bit
-// for bit.
-__device__ __forceinline__ void basis_all(const Knots& kv, int bins, int order, float t, float* out) {
-    float N[KNOTS_MAX];
+// for bit.  BT / OT > 0 fix bins / order at compile time (registers only);
+// 0 takes them from the arguments.
+template <int BT, int OT>
+__device__ __forceinline__ void basis_all(const Knots& kv, int bins_rt, int order_rt, float t, float* out) {
+    const int bins = BT ? BT : bins_rt;
+    const int order = OT ? OT : order_rt;
+    constexpr int NMAX = (BT && OT) ? BT + OT : KNOTS_MAX;
+    float N[NMAX];
     const int n1 = bins + order - 1;  // number of order-1 functions needed
-    for (int i = 0; i < n1; ++i) {
+#pragma unroll
+    for (int i = 0; i < NMAX - 1; ++i) {
+        if (i >= n1) break;
         const float a = kv.v[i], b = kv.v[i + 1];
         const bool in = (t >= a && t < b && a < b) ||
                         (fabs((double)__fsub_rn(t, b)) < 1e-10 && (i + 1 == bins));
         N[i] = in ? 1.0f : 0.0f;
     }
-    for (int p = 2; p <= order; ++p) {
+#pragma unroll
+    for (int p = 2; p <= (OT ? OT : KMAX_ORDER); ++p) {
+        if (p > order) break;
         const int np = bins + order - p;
-        for (int i = 0; i < np; ++i) {
+#pragma unroll
+        for (int i = 0; i < NMAX - 1; ++i) {
+            if (i >= np) break;
             const float d1 = __fsub_rn(kv.v[i + p - 1], kv.v[i]);
             const float n1v = __fsub_rn(t, kv.v[i]);
             const float d2 = __fsub_rn(kv.v[i + p], kv.v[i + 1]);
@@ -89,7 +100,9 @@ __device__ __forceinline__ void basis_all(const Knots& kv, int bins, int order, 
             N[i] = r;  // N[i+1] (still order p-1) is read before it is overwritten
         }
     }
-    for (int a = 0; a < bins; ++a) out[a] = N[a];
+#pragma unroll
+    for (int a = 0; a < (BT ? BT : KMAX_BINS); ++a)
+        if (a < bins) out[a] = N[a];
 }
 
 template <typename T>
@@ -107,9 +120,9 @@ __device__ __forceinline__ T block_reduce(T v, T (*op)(T, T), T* scratch) {
 __device__ float op_min(float a, float b) { return (b < a) ? b : a; }
 __device__ float op_max(float a, float b) { return (a < b) ? b : a; }
 
-template <int OUT>
+template <int OUT, int BT, int OT>
 __global__ void __launch_bounds__(WTHREADS) bspline_weights_kernel(const float* __restrict__ X, int64_t n, int64_t m,
-                                                                   int64_t ldx, int bins, int order, const Knots kv,
+                                                                   int64_t ldx, int bins_rt, int order_rt, const Knots kv,
                                                                    void* __restrict__ out0, void* __restrict__ out1,
                                                                    int64_t ldo, double* __restrict__ H) {
     __shared__ float fscratch[32];
@@ -117,6 +130,8 @@ __global__ void __launch_bounds__(WTHREADS) bspline_weights_kernel(const float* 
     const int64_t g = blockIdx.x;
     if (g >= n) return;
     const float* x = X + g * ldx;
+    const int bins = BT ? BT : bins_rt;
+    constexpr int NB = BT ? BT : KMAX_BINS;
 
     // ---- MinMaxScale (BSplineMI.hpp:86-115) ----
     float mn = INFINITY, mx = -INFINITY;
@@ -130,16 +145,16 @@ __global__ void __launch_bounds__(WTHREADS) bspline_weights_kernel(const float* 
     const float scale = (mx > mn) ? (float)(1.0 / (double)__fsub_rn(mx, mn)) : 1.0f;
     const float offset = (mx > mn) ? mn : 0.0f;
 
-    double acc[KMAX_BINS];
+    double acc[NB];
 #pragma unroll
-    for (int a = 0; a < KMAX_BINS; ++a) acc[a] = 0.0;
+    for (int a = 0; a < NB; ++a) acc[a] = 0.0;
 
-    float w[KMAX_BINS];
+    float w[NB];
     for (int64_t s = threadIdx.x; s < m; s += blockDim.x) {
         const float t = __fmul_rn(scale, __fsub_rn(x[s], offset));
-        basis_all(kv, bins, order, t, w);
+        basis_all<BT, OT>(kv, bins_rt, order_rt, t, w);
 #pragma unroll
-        for (int a = 0; a < KMAX_BINS; ++a)
+        for (int a = 0; a < NB; ++a)
             if (a < bins) acc[a] += (double)w[a];
         if (OUT == OUT_REF) {
             float* W = static_cast<float*>(out0) + g * ((int64_t)bins * m + 1);
@@ -175,7 +190,7 @@ __global__ void __launch_bounds__(WTHREADS) bspline_weights_kernel(const float* 
     // ---- marginal entropy in FP64 (entropy1d_2, BSplineMI.hpp:204-224) ----
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
-    for (int a = 0; a < KMAX_BINS; ++a) {
+    for (int a = 0; a < NB; ++a) {
         if (a >= bins) break;
         double v = acc[a];
 #pragma unroll
@@ -206,8 +221,12 @@ cudaError_t launch_bspline_weights_ref(const float* X, int64_t n, int64_t m, int
     Knots kv;
     host_knots(bins, order, kv);
     if (launches) ++*launches;
-    bspline_weights_kernel<OUT_REF><<<(unsigned)n, WTHREADS, 0, stream>>>(X, n, m, ldx, bins, order, kv, W, nullptr,
-                                                                          0, H);
+    if (bins == 10 && order == 3)
+        bspline_weights_kernel<OUT_REF, 10, 3><<<(unsigned)n, WTHREADS, 0, stream>>>(X, n, m, ldx, bins, order, kv, W,
+                                                                                 nullptr, 0, H);
+    else
+        bspline_weights_kernel<OUT_REF, 0, 0><<<(unsigned)n, WTHREADS, 0, stream>>>(X, n, m, ldx, bins, order, kv, W,
+                                                                               nullptr, 0, H);
     return cudaGetLastError();
 }
 
@@ -217,8 +236,12 @@ cudaError_t launch_bspline_weights_fp32(const float* X, int64_t n, int64_t m, in
     Knots kv;
     host_knots(bins, order, kv);
     if (launches) ++*launches;
-    bspline_weights_kernel<OUT_T32><<<(unsigned)n, WTHREADS, 0, stream>>>(X, n, m, ldx, bins, order, kv, Wt, nullptr,
-                                                                          ldwt, H);
+    if (bins == 10 && order == 3)
+        bspline_weights_kernel<OUT_T32, 10, 3><<<(unsigned)n, WTHREADS, 0, stream>>>(X, n, m, ldx, bins, order, kv, Wt,
+                                                                                 nullptr, ldwt, H);
+    else
+        bspline_weights_kernel<OUT_T32, 0, 0><<<(unsigned)n, WTHREADS, 0, stream>>>(X, n, m, ldx, bins, order, kv, Wt,
+                                                                               nullptr, ldwt, H);
     return cudaGetLastError();
 }
 
@@ -229,12 +252,19 @@ cudaError_t launch_bspline_weights_16(const float* X, int64_t n, int64_t m, int6
     Knots kv;
     host_knots(bins, order, kv);
     if (launches) ++*launches;
-    if (fmt == 0)
-        bspline_weights_kernel<OUT_BF16><<<(unsigned)n, WTHREADS, 0, stream>>>(X, n, m, ldx, bins, order, kv, Whi,
-                                                                               Wlo, ldw, H);
+    const bool fast = bins == 10 && order == 3;
+    if (fmt == 0 && fast)
+        bspline_weights_kernel<OUT_BF16, 10, 3><<<(unsigned)n, WTHREADS, 0, stream>>>(X, n, m, ldx, bins, order, kv,
+                                                                                  Whi, Wlo, ldw, H);
+    else if (fmt == 0)
+        bspline_weights_kernel<OUT_BF16, 0, 0><<<(unsigned)n, WTHREADS, 0, stream>>>(X, n, m, ldx, bins, order, kv,
+                                                                                Whi, Wlo, ldw, H);
+    else if (fast)
+        bspline_weights_kernel<OUT_FP16, 10, 3><<<(unsigned)n, WTHREADS, 0, stream>>>(X, n, m, ldx, bins, order, kv,
+                                                                                  Whi, Wlo, ldw, H);
     else
-        bspline_weights_kernel<OUT_FP16><<<(unsigned)n, WTHREADS, 0, stream>>>(X, n, m, ldx, bins, order, kv, Whi,
-                                                                               Wlo, ldw, H);
+        bspline_weights_kernel<OUT_FP16, 0, 0><<<(unsigned)n, WTHREADS, 0, stream>>>(X, n, m, ldx, bins, order, kv,
+                                                                                Whi, Wlo, ldw, H);
     return cudaGetLastError();
 }
 
