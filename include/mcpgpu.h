@@ -149,6 +149,39 @@ MCPG_API int mcpg_dpi(mcpg_handle* h, const float* A, int64_t n, int64_t lda, fl
 MCPG_API int mcpg_dpi_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, float tol,
                           float* out, int64_t ldo, uint8_t* mask, int64_t* removed);
 
+/* ---- TF-restricted variants ----
+ * tfs / mask are HOST arrays of floats.  tfs is the reference's TF vector
+ * (load_tfs, apps/pipeline/mcpnet_helper.hpp:1074-1123): one value per gene,
+ * > 0 marks a transcription factor (the reference stores +max / lowest, which
+ * are +inf / -inf in float).
+ *
+ * mcpg_maxmin_masked: mcp2_maxmin_kernel<float,true,true> (mcp.hpp:72-93) as a
+ * whole-matrix InnerProduct: C[i][j] = max_k min(mask[k], min(A[i][k], B[j][k])),
+ * mask of k_len values.  Bit-exact for any mask. */
+MCPG_API int mcpg_maxmin_masked(mcpg_handle* h, const float* A, int64_t lda, const float* B, int64_t ldb,
+                                int64_t rows, int64_t cols, int64_t k_len, const float* mask, float* C, int64_t ldc);
+MCPG_API int mcpg_maxmin_masked_dev(mcpg_handle* h, const float* A, int64_t lda, const float* B, int64_t ldb,
+                                    int64_t rows, int64_t cols, int64_t k_len, const float* mask, float* C,
+                                    int64_t ldc);
+/* compute_mcp{2,3,4}_tfs (mcpnet_helper.hpp:209-243, 281-333, 367-434) with
+ * tf_gene_transition in 0..1 (path 2), 0..2 (path 3), 0..3 (path 4).  A is the
+ * n x n MI matrix (diagonal already set); outputs are t x n with t = number of
+ * TFs, rows in gene order: maxmin_out gets the max-min matrix, ratio_out the
+ * MCP score ratio(tfs_to_genes, maxmin).  Nothing is written when t == 0. */
+MCPG_API int mcpg_mcp_tf(mcpg_handle* h, const float* A, int64_t n, int64_t lda, const float* tfs, int path_len,
+                         int tf_gene_transition, float* maxmin_out, int64_t ldm, float* ratio_out, int64_t ldr);
+MCPG_API int mcpg_mcp_tf_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, const float* tfs,
+                             int path_len, int tf_gene_transition, float* maxmin_out, int64_t ldm,
+                             float* ratio_out, int64_t ldr);
+/* dpi_tf_kernel (dpi.hpp:74-110) over all (x, z), then mask<float,true>: an
+ * edge between a TF and a non-TF is only deleted through TF intermediates; the
+ * tolerance multiplier is kept in float as the reference's IT member.  out is
+ * n x n (the dpi app then keeps the TF rows); mask / removed as mcpg_dpi. */
+MCPG_API int mcpg_dpi_tf(mcpg_handle* h, const float* A, int64_t n, int64_t lda, float tol, const float* tfs,
+                         float* out, int64_t ldo, uint8_t* mask, int64_t* removed);
+MCPG_API int mcpg_dpi_tf_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, float tol, const float* tfs,
+                             float* out, int64_t ldo, uint8_t* mask, int64_t* removed);
+
 /* ---- maximum-capacity closure (no counterpart routine in the reference) ----
  * Repeated squaring B <- max(B, B (x) B) from B = A until no entry changes,
  * with (x) the reference's max_of_pairmin (include/mcp/filter/simd_maxmin.hpp:30-46).

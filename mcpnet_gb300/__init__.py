@@ -61,6 +61,12 @@ ABI = [
     ("mcpg_dpi", C.c_int, [_vp, _vp, _i64, _i64, C.c_float, _vp, _i64, _vp, C.POINTER(C.c_int64)]),
     ("mcpg_dpi_dev", C.c_int, [_vp, _vp, _i64, _i64, C.c_float, _vp, _i64, _vp, C.POINTER(C.c_int64)]),
     ("mcpg_closure", C.c_int, [_vp, _vp, _i64, _i64, C.c_int, _vp, _i64, C.POINTER(C.c_int)]),
+    ("mcpg_maxmin_masked", C.c_int, [_vp, _vp, _i64, _vp, _i64, _i64, _i64, _i64, _vp, _vp, _i64]),
+    ("mcpg_maxmin_masked_dev", C.c_int, [_vp, _vp, _i64, _vp, _i64, _i64, _i64, _i64, _vp, _vp, _i64]),
+    ("mcpg_mcp_tf", C.c_int, [_vp, _vp, _i64, _i64, _vp, C.c_int, C.c_int, _vp, _i64, _vp, _i64]),
+    ("mcpg_mcp_tf_dev", C.c_int, [_vp, _vp, _i64, _i64, _vp, C.c_int, C.c_int, _vp, _i64, _vp, _i64]),
+    ("mcpg_dpi_tf", C.c_int, [_vp, _vp, _i64, _i64, C.c_float, _vp, _vp, _i64, _vp, C.POINTER(C.c_int64)]),
+    ("mcpg_dpi_tf_dev", C.c_int, [_vp, _vp, _i64, _i64, C.c_float, _vp, _vp, _i64, _vp, C.POINTER(C.c_int64)]),
     ("mcpg_closure_dev", C.c_int, [_vp, _vp, _i64, _i64, C.c_int, _vp, _i64, C.POINTER(C.c_int)]),
     ("mcpg_synth_grn", C.c_int, [_i64, _i64, C.c_uint64, _vp, _i64, _vp, _i64, C.POINTER(C.c_int64)]),
     ("mcpg_bspline_mi_fp32_noalloc", C.c_int, [_vp, _i64, _i64, _i64, C.c_int, C.c_int, _vp, _i64, _vp, _vp]),
@@ -231,6 +237,41 @@ class Handle:
         mask = np.empty((n, n), dtype=np.uint8) if want_mask else None
         removed = C.c_int64(0)
         self._check(self._L.mcpg_dpi(self._h, _ptr(A), n, n, tol, _ptr(out), n, _ptr(mask), C.byref(removed)), "dpi")
+        return out, mask, removed.value
+
+    def maxmin_masked(self, A, B, mask):
+        A = _f32(A)
+        same = B is None
+        B = A if same else _f32(B)
+        mask = _f32(mask)
+        rows, k = A.shape
+        cols = B.shape[0]
+        Cm = np.empty((rows, cols), dtype=np.float32)
+        self._check(self._L.mcpg_maxmin_masked(self._h, _ptr(A), k, _ptr(B), k, rows, cols, k, _ptr(mask),
+                                                _ptr(Cm), cols), "maxmin_masked")
+        return Cm
+
+    def mcp_tf(self, A, tfs, path_len: int, transition: int):
+        """compute_mcp{2,3,4}_tfs: returns (maxmin, ratio), each t x n."""
+        A = _f32(A)
+        tfs = _f32(tfs)
+        n = A.shape[0]
+        t = int((tfs > 0).sum())
+        M = np.empty((t, n), dtype=np.float32)
+        R = np.empty((t, n), dtype=np.float32)
+        self._check(self._L.mcpg_mcp_tf(self._h, _ptr(A), n, n, _ptr(tfs), path_len, transition, _ptr(M), n,
+                                         _ptr(R), n), "mcp_tf")
+        return M, R
+
+    def dpi_tf(self, A, tfs, tol: float = 0.1, want_mask: bool = False):
+        A = _f32(A)
+        tfs = _f32(tfs)
+        n = A.shape[0]
+        out = np.empty((n, n), dtype=np.float32)
+        mask = np.empty((n, n), dtype=np.uint8) if want_mask else None
+        removed = C.c_int64(0)
+        self._check(self._L.mcpg_dpi_tf(self._h, _ptr(A), n, n, tol, _ptr(tfs), _ptr(out), n, _ptr(mask),
+                                         C.byref(removed)), "dpi_tf")
         return out, mask, removed.value
 
     def closure(self, A, max_iter: int = 64):

@@ -8,6 +8,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <map>
 #include <string>
@@ -35,6 +36,13 @@ enum Slot {
     S_M2,        // second intermediate
     S_SMALL,     // flags and counters
     S_MASK,      // staged mask
+    S_TFA,       // TF-compacted / mask-folded operand A
+    S_TFB,       // TF-compacted operand B
+    S_TFIDX,     // TF column indices (int)
+    S_TFEX,      // TF exclusion indices / flags
+    S_TFROWS,    // TF rows of the MI matrix (tfs_to_genes)
+    S_M3,        // third intermediate (TF MCP4)
+    S_IN2,       // staged host input 2
     NSLOTS
 };
 
@@ -475,6 +483,222 @@ int closure_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, int max_
     return MCPG_OK;
 }
 
+
+// ---------------- TF-restricted variants ----------------
+struct TfSet {
+    std::vector<int> idx;  // positions with value > 0 (the reference's TF test)
+    bool pm_inf = true;    // every value is +inf or -inf (a pure TF mask)
+};
+
+TfSet tf_set(const float* v, int64_t n) {
+    TfSet t;
+    for (int64_t i = 0; i < n; ++i) {
+        if (v[i] > 0.0f) t.idx.push_back((int)i);
+        if (!(v[i] == INFINITY || v[i] == -INFINITY)) t.pm_inf = false;
+    }
+    return t;
+}
+
+int upload(mcpg_handle* h, int slot, const void* src, size_t bytes, void** dev) {
+    int rc = scratch(h, slot, bytes, dev);
+    if (rc) return rc;
+    if (bytes) CK(h, cudaMemcpyAsync(*dev, src, bytes, cudaMemcpyHostToDevice, h->stream), "upload");
+    return MCPG_OK;
+}
+
+// mcp2_maxmin_kernel<float,true,true> (mcp.hpp:72-93) as a whole-matrix call:
+// C[i][j] = max_k min(mask[k], min(A[i][k], B[j][k])), mask on the host.
+// A pure TF mask (+-inf) restricts k to the TF columns (gathered, exact); any
+// other mask is folded into A: min(mask, min(a, b)) == min(min(a, mask), b).
+int maxmin_masked_dev(mcpg_handle* h, const float* A, int64_t lda, const float* B, int64_t ldb, int64_t rows,
+                      int64_t cols, int64_t k, const float* mask, float* C, int64_t ldc) {
+    if (rows < 0 || cols < 0 || k < 0) return fail(h, MCPG_ERR_ARG, "maxmin_masked: negative size");
+    if (rows == 0 || cols == 0) return MCPG_OK;
+    if (!A || !B || !C || (k > 0 && !mask)) return fail(h, MCPG_ERR_ARG, "maxmin_masked: null pointer");
+    if (lda < k || ldb < k || ldc < cols) return fail(h, MCPG_ERR_ARG, "maxmin_masked: leading dimension too small");
+    const bool same = (A == B) && (lda == ldb) && (rows == cols);
+    TfSet ts = tf_set(mask, k);
+    mcpg::MaxminParams p{};
+    p.rows = rows; p.cols = cols; p.C = C; p.ldc = ldc;
+    if (ts.pm_inf) {
+        const int64_t t = (int64_t)ts.idx.size();
+        const int64_t ldt = round_up(t > 0 ? t : 1, 4);
+        void *idx, *a, *b;
+        int rc;
+        if ((rc = upload(h, S_TFIDX, ts.idx.data(), ts.idx.size() * sizeof(int), &idx))) return rc;
+        if ((rc = scratch(h, S_TFA, (size_t)(rows * ldt) * sizeof(float), &a))) return rc;
+        CK(h, mcpg::launch_gather(A, lda, nullptr, (const int*)idx, rows, t, (float*)a, ldt, h->stream, &h->launches),
+           "gather kernel");
+        if (same) {
+            b = a;
+        } else {
+            if ((rc = scratch(h, S_TFB, (size_t)(cols * ldt) * sizeof(float), &b))) return rc;
+            CK(h, mcpg::launch_gather(B, ldb, nullptr, (const int*)idx, cols, t, (float*)b, ldt, h->stream,
+                                      &h->launches),
+               "gather kernel");
+        }
+        p.A = (const float*)a; p.lda = ldt; p.B = (const float*)b; p.ldb = ldt; p.k_len = t;
+    } else {
+        const int64_t ldk = round_up(k, 4);
+        void *mk, *a;
+        int rc;
+        if ((rc = upload(h, S_TFIDX, mask, (size_t)k * sizeof(float), &mk))) return rc;
+        if ((rc = scratch(h, S_TFA, (size_t)(rows * ldk) * sizeof(float), &a))) return rc;
+        CK(h, mcpg::launch_fold_mask(A, lda, (const float*)mk, rows, k, (float*)a, ldk, h->stream, &h->launches),
+           "fold_mask kernel");
+        const float* bb;
+        int64_t lb;
+        if ((rc = aligned_view(h, B, ldb, cols, k, S_TFB, &bb, &lb))) return rc;
+        p.A = (const float*)a; p.lda = ldk; p.B = bb; p.ldb = lb; p.k_len = k;
+    }
+    {
+        PROF(h, "maxmin");
+        CK(h, mcpg::launch_maxmin(p, mcpg::MM_PLAIN, (same && ts.pm_inf) ? 1 : 0, h->stream, &h->launches),
+           "maxmin kernel");
+    }
+    return MCPG_OK;
+}
+
+// compute_mcp{2,3,4}_tfs (mcpnet_helper.hpp:209-243, 281-333, 367-434):
+// outputs are t x n (t = number of TFs, rows in gene order).
+int mcp_tf_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, const float* tfs, int path_len,
+               int transition, float* Mout, int64_t ldm, float* Rout, int64_t ldr) {
+    if (n < 0) return fail(h, MCPG_ERR_ARG, "mcp_tf: negative size");
+    if (n == 0) return MCPG_OK;
+    if (!A || !tfs) return fail(h, MCPG_ERR_ARG, "mcp_tf: null pointer");
+    if (path_len < 2 || path_len > 4) return fail(h, MCPG_ERR_ARG, "mcp_tf: path_len must be 2, 3 or 4");
+    const int tmax = path_len == 2 ? 1 : (path_len == 3 ? 2 : 3);
+    if (transition < 0 || transition > tmax)
+        return fail(h, MCPG_ERR_ARG, "mcp_tf: tf_gene_transition %d out of range 0..%d for path length %d",
+                    transition, tmax, path_len);
+    if (lda < n || (Mout && ldm < n) || (Rout && ldr < n)) return fail(h, MCPG_ERR_ARG, "mcp_tf: leading dimension too small");
+    TfSet ts = tf_set(tfs, n);
+    const int64_t t = (int64_t)ts.idx.size();
+    if (t == 0 || (!Mout && !Rout)) return MCPG_OK;
+    const int64_t ldt = round_up(n, 32);
+    int rc;
+    void *idx, *tg;
+    if ((rc = upload(h, S_TFEX, ts.idx.data(), (size_t)t * sizeof(int), &idx))) return rc;
+    if ((rc = scratch(h, S_TFROWS, (size_t)(t * ldt) * sizeof(float), &tg))) return rc;
+    CK(h, mcpg::launch_gather(A, lda, (const int*)idx, nullptr, t, n, (float*)tg, ldt, h->stream, &h->launches),
+       "gather kernel");
+    const float* TG = (const float*)tg;
+    auto prod = [&](const float* X, int64_t ldx, int64_t rx, const float* Y, int64_t ldy, int64_t ry, bool masked,
+                    float* out, int64_t ldo) -> int {
+        if (masked) return maxmin_masked_dev(h, X, ldx, Y, ldy, rx, ry, n, tfs, out, ldo);
+        return maxmin_dev(h, X, ldx, Y, ldy, rx, ry, n, out, ldo);
+    };
+    float* M = Mout;
+    int64_t lm = ldm;
+    void* mbuf = nullptr;
+    if (!M) {
+        if ((rc = scratch(h, S_M3, (size_t)(t * ldt) * sizeof(float), &mbuf))) return rc;
+        M = (float*)mbuf;
+        lm = ldt;
+    }
+    if (path_len == 2) {
+        if ((rc = prod(TG, ldt, t, A, lda, n, transition == 1, M, lm))) return rc;
+    } else {
+        void* m1;
+        if ((rc = scratch(h, S_M1, (size_t)(n * ldt) * sizeof(float), &m1))) return rc;
+        const bool m1_masked = (path_len == 3) ? (transition == 2) : (transition == 3);
+        if ((rc = prod(A, lda, n, A, lda, n, m1_masked, (float*)m1, ldt))) return rc;
+        if (path_len == 3) {
+            if ((rc = prod(TG, ldt, t, (const float*)m1, ldt, n, transition == 1 || transition == 2, M, lm))) return rc;
+        } else {
+            void* m2;
+            if ((rc = scratch(h, S_M2, (size_t)(t * ldt) * sizeof(float), &m2))) return rc;
+            if ((rc = prod(TG, ldt, t, A, lda, n, transition != 0, (float*)m2, ldt))) return rc;
+            if ((rc = prod((const float*)m2, ldt, t, (const float*)m1, ldt, n, transition == 2 || transition == 3, M,
+                           lm)))
+                return rc;
+        }
+    }
+    if (Rout) {
+        PROF(h, "ratio");
+        CK(h, mcpg::launch_ratio(TG, ldt, M, lm, t, n, Rout, ldr, h->stream, &h->launches), "ratio kernel");
+    }
+    return MCPG_OK;
+}
+
+// dpi_tf_kernel (dpi.hpp:74-110) over all (x, z), then mask<float,true>.
+int dpi_tf_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, float tol, const float* tfs, float* out,
+               int64_t ldo, uint8_t* mask, int64_t* removed) {
+    if (n < 0) return fail(h, MCPG_ERR_ARG, "dpi_tf: negative size");
+    if (removed) *removed = 0;
+    if (n == 0) return MCPG_OK;
+    if (!A || !out || !tfs) return fail(h, MCPG_ERR_ARG, "dpi_tf: null pointer");
+    if (lda < n || ldo < n) return fail(h, MCPG_ERR_ARG, "dpi_tf: leading dimension too small");
+    if (!(tol >= 0.0f && tol <= 1.0f)) return fail(h, MCPG_ERR_ARG, "dpi_tf: tolerance must be in [0, 1]");
+    const int64_t ldt = round_up(n, 32);
+    int rc;
+    const float* a = A;
+    int64_t la = lda;
+    const bool alias = (const void*)out < (const void*)(A + n * lda) && (const void*)A < (const void*)(out + n * ldo);
+    if (alias || !aligned16(A) || (lda % 4) != 0) {
+        void* p;
+        if ((rc = scratch(h, S_IN0, (size_t)(n * ldt) * sizeof(float), &p))) return rc;
+        CK(h, mcpg::launch_copy2d(A, lda, (float*)p, ldt, n, n, h->stream), "copy2d");
+        a = (const float*)p;
+        la = ldt;
+    }
+    TfSet ts = tf_set(tfs, n);
+    const int64_t t = (int64_t)ts.idx.size();
+    // all-y value (y not in {x, z})
+    void* call;
+    if ((rc = scratch(h, S_M1, (size_t)(n * ldt) * sizeof(float), &call))) return rc;
+    mcpg::MaxminParams p{};
+    p.A = a; p.lda = la; p.B = a; p.ldb = la; p.rows = n; p.cols = n; p.k_len = n;
+    p.C = (float*)call; p.ldc = ldt;
+    {
+        PROF(h, "maxmin");
+        CK(h, mcpg::launch_maxmin(p, mcpg::MM_EXCL, 1, h->stream, &h->launches), "maxmin kernel (all y)");
+    }
+    // TF-y value: k over the TF columns only, excluding x's and z's own TF column
+    const float* ctf = (const float*)call;
+    if (t > 0) {
+        std::vector<int> ex((size_t)n, -1);
+        for (int64_t c = 0; c < t; ++c) ex[(size_t)ts.idx[(size_t)c]] = (int)c;
+        void *idx, *exd, *atf, *c2;
+        const int64_t ldk = round_up(t, 4);
+        if ((rc = upload(h, S_TFIDX, ts.idx.data(), (size_t)t * sizeof(int), &idx))) return rc;
+        if ((rc = upload(h, S_TFEX, ex.data(), (size_t)n * sizeof(int), &exd))) return rc;
+        if ((rc = scratch(h, S_TFA, (size_t)(n * ldk) * sizeof(float), &atf))) return rc;
+        if ((rc = scratch(h, S_M2, (size_t)(n * ldt) * sizeof(float), &c2))) return rc;
+        CK(h, mcpg::launch_gather(a, la, nullptr, (const int*)idx, n, t, (float*)atf, ldk, h->stream, &h->launches),
+           "gather kernel");
+        mcpg::MaxminParams q{};
+        q.A = (const float*)atf; q.lda = ldk; q.B = (const float*)atf; q.ldb = ldk;
+        q.rows = n; q.cols = n; q.k_len = t; q.C = (float*)c2; q.ldc = ldt;
+        q.excl_row = (const int*)exd; q.excl_col = (const int*)exd;
+        {
+            PROF(h, "maxmin");
+            CK(h, mcpg::launch_maxmin(q, mcpg::MM_EXCL, 1, h->stream, &h->launches), "maxmin kernel (TF y)");
+        }
+        ctf = (const float*)c2;
+    }
+    std::vector<uint8_t> flag((size_t)n, 0);
+    for (int i : ts.idx) flag[(size_t)i] = 1;
+    void *fl, *cnt;
+    if ((rc = upload(h, S_MASK + 0, flag.data(), (size_t)n, &fl))) return rc;
+    if ((rc = scratch(h, S_SMALL, 64, &cnt))) return rc;
+    CK(h, cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), h->stream), "memset counter");
+    const float tm = (float)(1.0 / (1.0 - (double)tol));  // dpi_tf_kernel stores it as IT
+    {
+        PROF(h, "dpi_tf_apply");
+        CK(h, mcpg::launch_dpi_tf_apply(a, la, (const float*)call, ldt, ctf, ldt, (const uint8_t*)fl, n, tm, out, ldo,
+                                        mask, (unsigned long long*)cnt, h->stream, &h->launches),
+           "dpi_tf_apply kernel");
+    }
+    if (removed) {
+        unsigned long long r = 0;
+        CK(h, cudaMemcpyAsync(&r, cnt, sizeof r, cudaMemcpyDeviceToHost, h->stream), "read removed");
+        CK(h, cudaStreamSynchronize(h->stream), "stream synchronize");
+        *removed = (int64_t)r;
+    }
+    return MCPG_OK;
+}
+
 }  // namespace
 
 // =====================================================================
@@ -827,6 +1051,100 @@ int mcpg_closure(mcpg_handle* h, const float* A, int64_t n, int64_t lda, int max
     if ((rc = finish(h))) return rc;
     h->err = keep;
     return crc;
+}
+
+
+// ---- TF-restricted variants ----
+int mcpg_maxmin_masked_dev(mcpg_handle* h, const float* A, int64_t lda, const float* B, int64_t ldb, int64_t rows,
+                           int64_t cols, int64_t k, const float* mask, float* C, int64_t ldc) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    return maxmin_masked_dev(h, A, lda, B, ldb, rows, cols, k, mask, C, ldc);
+}
+
+int mcpg_maxmin_masked(mcpg_handle* h, const float* A, int64_t lda, const float* B, int64_t ldb, int64_t rows,
+                       int64_t cols, int64_t k, const float* mask, float* C, int64_t ldc) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (rows < 0 || cols < 0 || k < 0) return fail(h, MCPG_ERR_ARG, "maxmin_masked: negative size");
+    if (rows == 0 || cols == 0) return MCPG_OK;
+    if (!A || !B || !C || (k > 0 && !mask)) return fail(h, MCPG_ERR_ARG, "maxmin_masked: null pointer");
+    if (lda < k || ldb < k || ldc < cols) return fail(h, MCPG_ERR_ARG, "maxmin_masked: leading dimension too small");
+    const bool same = (A == B) && (lda == ldb) && (rows == cols);
+    float *dA, *dB, *dC;
+    int64_t la, lb, lc;
+    if ((rc = stage_in(h, S_IN0, A, lda, rows, k, &dA, &la))) return rc;
+    if (same) {
+        dB = dA; lb = la;
+    } else if ((rc = stage_in(h, S_IN1, B, ldb, cols, k, &dB, &lb))) {
+        return rc;
+    }
+    if ((rc = stage_out_alloc(h, S_OUT0, rows, cols, &dC, &lc))) return rc;
+    if ((rc = maxmin_masked_dev(h, dA, la, dB, lb, rows, cols, k, mask, dC, lc))) return rc;
+    if ((rc = copy_out(h, C, ldc, dC, lc, rows, cols))) return rc;
+    return finish(h);
+}
+
+int mcpg_mcp_tf_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, const float* tfs, int path_len,
+                    int tf_gene_transition, float* Mout, int64_t ldm, float* Rout, int64_t ldr) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    return mcp_tf_dev(h, A, n, lda, tfs, path_len, tf_gene_transition, Mout, ldm, Rout, ldr);
+}
+
+int mcpg_mcp_tf(mcpg_handle* h, const float* A, int64_t n, int64_t lda, const float* tfs, int path_len,
+                int tf_gene_transition, float* Mout, int64_t ldm, float* Rout, int64_t ldr) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (n < 0) return fail(h, MCPG_ERR_ARG, "mcp_tf: negative size");
+    if (n == 0) return MCPG_OK;
+    if (!A || !tfs) return fail(h, MCPG_ERR_ARG, "mcp_tf: null pointer");
+    if (lda < n || (Mout && ldm < n) || (Rout && ldr < n)) return fail(h, MCPG_ERR_ARG, "mcp_tf: leading dimension too small");
+    int64_t t = 0;
+    for (int64_t i = 0; i < n; ++i) t += tfs[i] > 0.0f;
+    float *dA, *dM = nullptr, *dR = nullptr;
+    int64_t la, lm = 0, lr = 0;
+    if ((rc = stage_in(h, S_IN0, A, lda, n, n, &dA, &la))) return rc;
+    if (Mout && t > 0 && (rc = stage_out_alloc(h, S_OUT0, t, n, &dM, &lm))) return rc;
+    if (Rout && t > 0 && (rc = stage_out_alloc(h, S_OUT1, t, n, &dR, &lr))) return rc;
+    if ((rc = mcp_tf_dev(h, dA, n, la, tfs, path_len, tf_gene_transition, dM, lm, dR, lr))) return rc;
+    if (t > 0) {
+        if ((rc = copy_out(h, Mout, ldm, dM, lm, t, n))) return rc;
+        if ((rc = copy_out(h, Rout, ldr, dR, lr, t, n))) return rc;
+    }
+    return finish(h);
+}
+
+int mcpg_dpi_tf_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, float tol, const float* tfs, float* out,
+                    int64_t ldo, uint8_t* mask, int64_t* removed) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    return dpi_tf_dev(h, A, n, lda, tol, tfs, out, ldo, mask, removed);
+}
+
+int mcpg_dpi_tf(mcpg_handle* h, const float* A, int64_t n, int64_t lda, float tol, const float* tfs, float* out,
+                int64_t ldo, uint8_t* mask, int64_t* removed) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (removed) *removed = 0;
+    if (n < 0) return fail(h, MCPG_ERR_ARG, "dpi_tf: negative size");
+    if (n == 0) return MCPG_OK;
+    if (!A || !out || !tfs) return fail(h, MCPG_ERR_ARG, "dpi_tf: null pointer");
+    if (lda < n || ldo < n) return fail(h, MCPG_ERR_ARG, "dpi_tf: leading dimension too small");
+    float *dA, *dO;
+    int64_t la, lo;
+    if ((rc = stage_in(h, S_IN2, A, lda, n, n, &dA, &la))) return rc;
+    if ((rc = stage_out_alloc(h, S_OUT0, n, n, &dO, &lo))) return rc;
+    uint8_t* dMask = nullptr;
+    if (mask) {
+        void* p;
+        if ((rc = scratch(h, S_OUT1, (size_t)(n * n), &p))) return rc;
+        dMask = (uint8_t*)p;
+    }
+    if ((rc = dpi_tf_dev(h, dA, n, la, tol, tfs, dO, lo, dMask, removed))) return rc;
+    if ((rc = copy_out(h, out, ldo, dO, lo, n, n))) return rc;
+    if (mask) CK(h, cudaMemcpyAsync(mask, dMask, (size_t)(n * n), cudaMemcpyDeviceToHost, h->stream), "copy mask");
+    return finish(h);
 }
 
 }  // extern "C"

@@ -14,6 +14,8 @@ enum MaxminMode : int {
     MM_RATIO = 1,    // R = ratio(E, A (x) B); C (nullable) = A (x) B
     MM_CLOSURE = 2,  // C = max(E, A (x) B); *changed |= any entry grew
     MM_DPI = 3,      // C = dpi-mask(E) applied to E; k excluded when k == i or k == j
+    MM_EXCL = 4,     // C = max over admissible k of min(A[i][k], B[j][k]); k excluded as in
+                     // MM_DPI; an output with no admissible k is NaN
 };
 
 struct MaxminParams {
@@ -27,6 +29,10 @@ struct MaxminParams {
     double tol_mult;              // DPI 1/(1 - tol)
     uint8_t* mask; int64_t ldmask;  // DPI mask (nullable)
     unsigned long long* removed;  // DPI removed count (device, nullable)
+    // MM_DPI / MM_EXCL: the excluded k of output (i, j) are excl_row[i] and
+    // excl_col[j] (device, -1 = none) when given, else i and j.
+    const int* excl_row;
+    const int* excl_col;
 };
 
 // symmetric != 0: A == B (same rows), rows == cols; only tiles on or above the
@@ -38,6 +44,17 @@ cudaError_t launch_set_diagonal(float* A, int64_t rows, int64_t cols, int64_t ld
                                 cudaStream_t stream, int64_t* launches);
 cudaError_t launch_max_transpose(const float* M, int64_t n, int64_t ldm, float* out, int64_t ldo,
                                  cudaStream_t stream, int64_t* launches);
+// dst[r][c] = src[rows_idx ? rows_idx[r] : r][cols_idx ? cols_idx[c] : c]  (device index arrays)
+cudaError_t launch_gather(const float* src, int64_t lds, const int* rows_idx, const int* cols_idx, int64_t rows,
+                          int64_t cols, float* dst, int64_t ldd, cudaStream_t stream, int64_t* launches);
+// dst[r][c] = min(src[r][c], mask[c])  (mask: device, cols floats)
+cudaError_t launch_fold_mask(const float* src, int64_t lds, const float* mask, int64_t rows, int64_t cols, float* dst,
+                             int64_t ldd, cudaStream_t stream, int64_t* launches);
+// dpi_tf_kernel decision (dpi.hpp:74-110) + mask<float,true>: per (x, z) pick the
+// all-y value Call or the TF-y value Ctf by tf[x] xor tf[z].
+cudaError_t launch_dpi_tf_apply(const float* A, int64_t lda, const float* Call, int64_t ld1, const float* Ctf,
+                                int64_t ld2, const uint8_t* tf, int64_t n, float tol_mult, float* out, int64_t ldo,
+                                uint8_t* mask, unsigned long long* removed, cudaStream_t stream, int64_t* launches);
 // Copies a rows x cols matrix between arbitrary leading dimensions (device to device).
 cudaError_t launch_copy2d(const float* src, int64_t lds, float* dst, int64_t ldd, int64_t rows, int64_t cols,
                           cudaStream_t stream);

@@ -116,7 +116,18 @@ __global__ void __launch_bounds__(THREADS, MCPG_MM_MINB) maxmin_kernel(const Max
 
     // DPI: NaN is the neutral element of the NaN-ignoring max, so an output with
     // no admissible y stays NaN and compares false (the reference keeps it).
-    const float init = (MODE == MM_DPI) ? __int_as_float(0x7fc00000) : -INFINITY;
+    constexpr bool EXCL = (MODE == MM_DPI || MODE == MM_EXCL);
+    const float init = EXCL ? __int_as_float(0x7fc00000) : -INFINITY;
+    // excluded k per owned row / column (EXCL modes)
+    int64_t exr[8], exc[8];
+    if (EXCL) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int64_t i = i0 + ty + 16 * q, j = j0 + tx + 16 * q;
+            exr[q] = p.excl_row ? (i < p.rows ? (int64_t)p.excl_row[i] : -1) : i;
+            exc[q] = p.excl_col ? (j < p.cols ? (int64_t)p.excl_col[j] : -1) : j;
+        }
+    }
     float acc[8][8];
 #pragma unroll
     for (int q = 0; q < 8; ++q)
@@ -150,8 +161,9 @@ __global__ void __launch_bounds__(THREADS, MCPG_MM_MINB) maxmin_kernel(const Max
         const int64_t k0 = t * BK;
         const int64_t kmax = min((int64_t)BK, p.k_len - k0);
         bool excl = false;
-        if (MODE == MM_DPI) {
-            excl = (k0 < i0 + BM && k0 + BK > i0) || (k0 < j0 + BN && k0 + BK > j0);
+        if (EXCL) {
+            excl = (p.excl_row || p.excl_col) ||
+                   (k0 < i0 + BM && k0 + BK > i0) || (k0 < j0 + BN && k0 + BK > j0);
         }
         if (kmax == BK && !excl) {
             if (KSTEP == 2) {
@@ -198,8 +210,8 @@ __global__ void __launch_bounds__(THREADS, MCPG_MM_MINB) maxmin_kernel(const Max
 #pragma unroll
                     for (int r = 0; r < 8; ++r) {
                         float v = fmin2(a[q], b[r]);
-                        if (MODE == MM_DPI) {
-                            if (y == i0 + ty + 16 * q || y == j0 + tx + 16 * r) v = __int_as_float(0x7fc00000);
+                        if (EXCL) {
+                            if (y == exr[q] || y == exc[r]) v = __int_as_float(0x7fc00000);
                         }
                         acc[q][r] = fmax2(acc[q][r], v);
                     }
@@ -220,7 +232,7 @@ __global__ void __launch_bounds__(THREADS, MCPG_MM_MINB) maxmin_kernel(const Max
             const int64_t j = j0 + tx + 16 * r;
             if (j >= p.cols) continue;
             const float m = acc[q][r];
-            if (MODE == MM_PLAIN) {
+            if (MODE == MM_PLAIN || MODE == MM_EXCL) {
                 p.C[i * p.ldc + j] = m;
                 if (mirror) p.C[j * p.ldc + i] = m;
             } else if (MODE == MM_RATIO) {
@@ -326,6 +338,51 @@ __global__ void copy2d_kernel(const float* src, int64_t lds, float* dst, int64_t
     }
 }
 
+__global__ void gather_kernel(const float* src, int64_t lds, const int* ri, const int* ci, int64_t rows, int64_t cols,
+                              float* dst, int64_t ldd) {
+    const int64_t total = rows * cols;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = t / cols, c = t - r * cols;
+        const int64_t sr = ri ? ri[r] : r, sc = ci ? ci[c] : c;
+        dst[r * ldd + c] = src[sr * lds + sc];
+    }
+}
+
+__global__ void fold_mask_kernel(const float* src, int64_t lds, const float* mask, int64_t rows, int64_t cols,
+                                 float* dst, int64_t ldd) {
+    const int64_t total = rows * cols;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = t / cols, c = t - r * cols;
+        const float a = src[r * lds + c], mk = mask[c];
+        dst[r * ldd + c] = (mk < a) ? mk : a;  // min(a, mask[c]); min is exact, so folding the mask
+                                               // into one operand equals the reference's 3-way min
+    }
+}
+
+__global__ void dpi_tf_apply_kernel(const float* A, int64_t lda, const float* Call, int64_t ld1, const float* Ctf,
+                                    int64_t ld2, const uint8_t* tf, int64_t n, float tm, float* out, int64_t ldo,
+                                    uint8_t* mask, unsigned long long* removed) {
+    const int64_t total = n * n;
+    unsigned long long cnt = 0;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t x = t / n, z = t - x * n;
+        const float e = A[x * lda + z];
+        const float ixz = __fmul_rn(e, tm);  // dpi_tf_kernel keeps its multiplier in IT (float)
+        const bool tfxz = (tf[x] != 0) != (tf[z] != 0);
+        const float c = tfxz ? Ctf[x * ld2 + z] : Call[x * ld1 + z];
+        const bool del = (x == z) || (c >= ixz);
+        const float o = del ? 0.0f : e;
+        out[x * ldo + z] = o;
+        cnt += (o != e);
+        if (mask) mask[x * n + z] = del ? 1 : 0;
+    }
+    if (removed) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+        if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(removed, cnt);
+    }
+}
+
 unsigned ew_blocks(int64_t total) {
     int64_t b = ceil_div(total, 256);
     if (b > 152 * 32) b = 152 * 32;
@@ -344,6 +401,7 @@ cudaError_t launch_maxmin(const MaxminParams& p, int mode, int symmetric, cudaSt
         case MM_RATIO: return s ? launch_one<MM_RATIO, true>(p, stream) : launch_one<MM_RATIO, false>(p, stream);
         case MM_CLOSURE: return s ? launch_one<MM_CLOSURE, true>(p, stream) : launch_one<MM_CLOSURE, false>(p, stream);
         case MM_DPI: return s ? launch_one<MM_DPI, true>(p, stream) : launch_one<MM_DPI, false>(p, stream);
+        case MM_EXCL: return s ? launch_one<MM_EXCL, true>(p, stream) : launch_one<MM_EXCL, false>(p, stream);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -371,6 +429,32 @@ cudaError_t launch_max_transpose(const float* M, int64_t n, int64_t ldm, float* 
     if (launches) ++*launches;
     dim3 grid((unsigned)ceil_div(n, 32), (unsigned)ceil_div(n, 32));
     max_transpose_kernel<<<grid, dim3(32, 8), 0, stream>>>(M, n, ldm, out, ldo);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather(const float* src, int64_t lds, const int* ri, const int* ci, int64_t rows, int64_t cols,
+                          float* dst, int64_t ldd, cudaStream_t stream, int64_t* launches) {
+    if (rows <= 0 || cols <= 0) return cudaSuccess;
+    if (launches) ++*launches;
+    gather_kernel<<<ew_blocks(rows * cols), 256, 0, stream>>>(src, lds, ri, ci, rows, cols, dst, ldd);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fold_mask(const float* src, int64_t lds, const float* mask, int64_t rows, int64_t cols, float* dst,
+                             int64_t ldd, cudaStream_t stream, int64_t* launches) {
+    if (rows <= 0 || cols <= 0) return cudaSuccess;
+    if (launches) ++*launches;
+    fold_mask_kernel<<<ew_blocks(rows * cols), 256, 0, stream>>>(src, lds, mask, rows, cols, dst, ldd);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dpi_tf_apply(const float* A, int64_t lda, const float* Call, int64_t ld1, const float* Ctf,
+                                int64_t ld2, const uint8_t* tf, int64_t n, float tm, float* out, int64_t ldo,
+                                uint8_t* mask, unsigned long long* removed, cudaStream_t stream, int64_t* launches) {
+    if (n <= 0) return cudaSuccess;
+    if (launches) ++*launches;
+    dpi_tf_apply_kernel<<<ew_blocks(n * n), 256, 0, stream>>>(A, lda, Call, ld1, Ctf, ld2, tf, n, tm, out, ldo, mask,
+                                                             removed);
     return cudaGetLastError();
 }
 

@@ -178,6 +178,29 @@ void FN(orc_maxmin)(const REAL* A, int64_t lda, const REAL* B, int64_t ldb, int6
             C[i * ldc + j] = FN(max_of_pairmin)(A + i * lda, B + j * ldb, k);
 }
 
+/* max_of_pairmin_scalar with a mask -- simd_maxmin.hpp:30-46 (mask branch,
+ * :35-38): val = max(val, min(mask[i], min(xx[i], yy[i]))). */
+static REAL FN(max_of_pairmin_masked)(const REAL* xx, const REAL* yy, const REAL* mask, int64_t count) {
+    REAL val = (REAL)(-DBL_MAX);
+    for (int64_t i = 0; i < count; ++i) {
+        REAL a = xx[i], b = yy[i];
+        REAL mn = (b < a) ? b : a;
+        REAL mk = mask[i];
+        REAL m2 = (mn < mk) ? mn : mk; /* std::min(mask[i], mn) */
+        val = (val < m2) ? m2 : val;
+    }
+    return val;
+}
+
+/* mcp2_maxmin_kernel<IT,true,true> over all (i, j) -- filter/mcp.hpp:72-93 */
+void FN(orc_maxmin_masked)(const REAL* A, int64_t lda, const REAL* B, int64_t ldb, int64_t rows, int64_t cols,
+                           int64_t k, const REAL* mask, REAL* C, int64_t ldc) {
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t i = 0; i < rows; ++i)
+        for (int64_t j = 0; j < cols; ++j)
+            C[i * ldc + j] = FN(max_of_pairmin_masked)(A + i * lda, B + j * ldb, mask, k);
+}
+
 /* ratio_kernel<T,T> -- include/mcp/transform/combine.hpp:210-222 */
 void FN(orc_ratio)(const REAL* A, int64_t lda, const REAL* M, int64_t ldm, int64_t rows, int64_t cols,
                    REAL* R, int64_t ldr) {
@@ -221,6 +244,38 @@ int64_t FN(orc_dpi)(const REAL* A, int64_t n, int64_t lda, double tol, REAL* out
                 REAL ixz = (REAL)((double)rx[z] * tm);
                 int64_t y = 0;
                 for (; y < n && (y == x || y == z || rx[y] < ixz || rz[y] < ixz); ++y) {}
+                del = y < n;
+            }
+            if (mask) mask[x * n + z] = (uint8_t)del;
+            REAL in = rx[z];
+            REAL o = del ? (REAL)0 : in;
+            out[x * ldo + z] = o;
+            removed += (o != in);
+        }
+    }
+    return removed;
+}
+
+/* dpi_tf_kernel<IT,true> -- include/mcp/filter/dpi.hpp:74-110 (note its
+ * multiplier is stored in IT, so i_xz is an IT product), then mask<IT,true>
+ * as apps/filter/dpi.cpp:276-287.  tfs: the reference's TF vector (> 0 = TF). */
+int64_t FN(orc_dpi_tf)(const REAL* A, int64_t n, int64_t lda, REAL tol, const REAL* tfs, REAL* out, int64_t ldo,
+                       uint8_t* mask) {
+    const REAL tm = (REAL)(1.0 / (1.0 - (double)tol));
+    int64_t removed = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(+:removed)
+    for (int64_t x = 0; x < n; ++x) {
+        const REAL* rx = A + x * lda;
+        for (int64_t z = 0; z < n; ++z) {
+            const REAL* rz = A + z * lda;
+            int del;
+            if (x == z) {
+                del = 1;
+            } else {
+                REAL ixz = rx[z] * tm;
+                int tfxz = (tfs[x] > 0) ^ (tfs[z] > 0);
+                int64_t y = 0;
+                for (; y < n && (y == x || y == z || rx[y] < ixz || rz[y] < ixz || ((tfs[y] <= 0) && tfxz)); ++y) {}
                 del = y < n;
             }
             if (mask) mask[x * n + z] = (uint8_t)del;

@@ -48,6 +48,7 @@ def _bind(L, sfx: str, prefix: str):
         "max_transpose": (None, [_vp, _i64, _i64, _vp, _i64]),
         "dpi": (C.c_int64, [_vp, _i64, _i64, C.c_double, _vp, _i64, _vp]),
         "closure": (C.c_int, [_vp, _i64, _i64, _vp, _i64, C.c_int]),
+        "maxmin_masked": (None, [_vp, _i64, _vp, _i64, _i64, _i64, _i64, _vp, _vp, _i64]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, f"{prefix}{name}_{sfx}", None)
@@ -55,9 +56,42 @@ def _bind(L, sfx: str, prefix: str):
             continue
         f.restype = res
         f.argtypes = args
+    f = getattr(L, f"{prefix}dpi_tf_{sfx}", None)
+    if f is not None:
+        f.restype = C.c_int64
+        f.argtypes = [_vp, _i64, _i64, C.c_float if sfx == "f32" else C.c_double, _vp, _vp, _i64, _vp]
 
 
-class _Port:
+class _TfCompositions:
+    """The reference's TF-restricted helpers restated on top of maxmin /
+    maxmin_masked / ratio: compute_mcp{2,3,4}_tfs
+    (apps/pipeline/mcpnet_helper.hpp:209-243, 281-333, 367-434)."""
+
+    @staticmethod
+    def tf_rows(A, tfs):
+        return np.ascontiguousarray(A[np.asarray(tfs) > 0])
+
+    def mcp_tf(self, A, tfs, path_len, transition):
+        A = np.ascontiguousarray(A, dtype=np.float32)
+        tfs = np.ascontiguousarray(tfs, dtype=np.float32)
+        tg = self.tf_rows(A, tfs)
+        mm = lambda X, Y, masked: self.maxmin_masked(X, Y, tfs) if masked else self.maxmin(X, Y)
+        if path_len == 2:      # compute_maxmin1_tfs
+            assert transition in (0, 1)
+            M = mm(tg, A, transition == 1)
+        elif path_len == 3:    # compute_maxmin2_tfs
+            assert transition in (0, 1, 2)
+            M1 = mm(A, A, transition == 2)
+            M = mm(tg, M1, transition in (1, 2))
+        else:                  # compute_maxmin3_tfs
+            assert transition in (0, 1, 2, 3)
+            M1 = mm(A, A, transition == 3)
+            M2 = mm(tg, A, transition != 0)
+            M = mm(M2, M1, transition in (2, 3))
+        return M, self.ratio(tg, M)
+
+
+class _Port(_TfCompositions):
     """The C restatement (float and double)."""
 
     def __init__(self, path: Path):
@@ -137,6 +171,27 @@ class _Port:
                                                             mask.ctypes.data)
         return out, mask, int(removed)
 
+    def maxmin_masked(self, A, B, mask):
+        A = np.ascontiguousarray(A)
+        B = A if B is None else np.ascontiguousarray(B)
+        mask = np.ascontiguousarray(mask, dtype=A.dtype)
+        rows, k = A.shape
+        cols = B.shape[0]
+        Cm = np.empty((rows, cols), dtype=A.dtype)
+        getattr(self.L, f"orc_maxmin_masked_{self._dt(A)}")(A.ctypes.data, k, B.ctypes.data, k, rows, cols, k,
+                                                            mask.ctypes.data, Cm.ctypes.data, cols)
+        return Cm
+
+    def dpi_tf(self, A, tfs, tol=0.1):
+        A = np.ascontiguousarray(A)
+        tfs = np.ascontiguousarray(tfs, dtype=A.dtype)
+        n = A.shape[0]
+        out = np.empty_like(A)
+        mask = np.empty((n, n), dtype=np.uint8)
+        removed = getattr(self.L, f"orc_dpi_tf_{self._dt(A)}")(A.ctypes.data, n, n, tol, tfs.ctypes.data,
+                                                               out.ctypes.data, n, mask.ctypes.data)
+        return out, mask, int(removed)
+
     def closure(self, A, max_iter=64):
         A = np.ascontiguousarray(A)
         n = A.shape[0]
@@ -161,7 +216,7 @@ class _Port:
         return M, self.ratio(A, M)
 
 
-class _Ref:
+class _Ref(_TfCompositions):
     """MCPNet's own kernels driven over whole matrices (float, plus f64 MI)."""
 
     def __init__(self, path: Path):
@@ -177,7 +232,31 @@ class _Ref:
         L.ref_dpi_f32.argtypes = [_vp, _i64, _i64, C.c_float, _vp, _i64, _vp]
         L.ref_dpi_f32.restype = C.c_int64
         L.ref_bspline_mi_rows_f32.argtypes = [_vp, _i64, _i64, C.c_int, _i64, _i64, _vp, _i64]
+        L.ref_maxmin_masked_f32.argtypes = [_vp, _i64, _vp, _i64, _i64, _i64, _i64, _vp, _vp, _i64]
+        L.ref_dpi_tf_f32.argtypes = [_vp, _i64, _i64, C.c_float, _vp, _vp, _i64, _vp]
+        L.ref_dpi_tf_f32.restype = C.c_int64
         self.L = L
+
+    def maxmin_masked(self, A, B, mask):
+        A = np.ascontiguousarray(A, dtype=np.float32)
+        B = A if B is None else np.ascontiguousarray(B, dtype=np.float32)
+        mask = np.ascontiguousarray(mask, dtype=np.float32)
+        rows, k = A.shape
+        cols = B.shape[0]
+        Cm = np.empty((rows, cols), dtype=np.float32)
+        self.L.ref_maxmin_masked_f32(A.ctypes.data, k, B.ctypes.data, k, rows, cols, k, mask.ctypes.data,
+                                     Cm.ctypes.data, cols)
+        return Cm
+
+    def dpi_tf(self, A, tfs, tol=0.1):
+        A = np.ascontiguousarray(A, dtype=np.float32)
+        tfs = np.ascontiguousarray(tfs, dtype=np.float32)
+        n = A.shape[0]
+        out = np.empty_like(A)
+        mask = np.empty((n, n), dtype=np.uint8)
+        removed = self.L.ref_dpi_tf_f32(A.ctypes.data, n, n, tol, tfs.ctypes.data, out.ctypes.data, n,
+                                        mask.ctypes.data)
+        return out, mask, int(removed)
 
     def bspline_mi_rows(self, W, m, r0, r1, bins=10):
         W = np.ascontiguousarray(W, dtype=np.float32)

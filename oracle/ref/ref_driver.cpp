@@ -83,6 +83,37 @@ void maxmin_symm(T const* A, int64_t lda, int64_t n, T* C, int64_t ldc) {
 }
 
 template <typename T>
+void maxmin_masked(T const* A, int64_t lda, T const* B, int64_t ldb, int64_t rows, int64_t cols, int64_t k,
+                   T const* mask, T* C, int64_t ldc) {
+    std::vector<T> tfs(mask, mask + k);
+    mcp::kernel::mcp2_maxmin_kernel<T, true, true> kern(tfs);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t i = 0; i < rows; ++i)
+        for (int64_t j = 0; j < cols; ++j)
+            C[i * ldc + j] = kern(A + i * lda, B + j * ldb, (size_t)k);
+}
+
+template <typename T>
+int64_t dpi_tf(T const* A, int64_t n, int64_t lda, T tol, T const* tfs_in, T* out, int64_t ldo, uint8_t* mask_out) {
+    std::vector<T> tfs(tfs_in, tfs_in + n);
+    mcp::kernel::dpi_tf_kernel<T> kern(tfs, tol);
+    std::vector<uint8_t> mask((size_t)(n * n));
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t x = 0; x < n; ++x)
+        for (int64_t z = 0; z < n; ++z)
+            mask[x * n + z] = kern((size_t)x, (size_t)z, A + x * lda, A + z * lda, (size_t)n) ? 1 : 0;
+    mcp::kernel::mask<T, true> masker;
+    bool* b = new bool[n];
+    for (int64_t x = 0; x < n; ++x) {
+        for (int64_t z = 0; z < n; ++z) b[z] = mask[x * n + z] != 0;
+        masker(A + x * lda, b, (size_t)n, out + x * ldo);
+    }
+    delete[] b;
+    if (mask_out) std::memcpy(mask_out, mask.data(), mask.size());
+    return (int64_t)masker.processed;
+}
+
+template <typename T>
 void ratio(T const* A, int64_t lda, T const* M, int64_t ldm, int64_t rows, int64_t cols,
            T* R, int64_t ldr) {
     mcp::kernel::ratio_kernel<T, T> kern;
@@ -159,6 +190,14 @@ void ref_ratio_f32(const float* A, int64_t lda, const float* M, int64_t ldm, int
 }
 void ref_max_transpose_f32(const float* M, int64_t n, int64_t ldm, float* out, int64_t ldo) {
     max_transpose<float>(M, n, ldm, out, ldo);
+}
+void ref_maxmin_masked_f32(const float* A, int64_t lda, const float* B, int64_t ldb, int64_t rows, int64_t cols,
+                           int64_t k, const float* mask, float* C, int64_t ldc) {
+    maxmin_masked<float>(A, lda, B, ldb, rows, cols, k, mask, C, ldc);
+}
+int64_t ref_dpi_tf_f32(const float* A, int64_t n, int64_t lda, float tol, const float* tfs, float* out, int64_t ldo,
+                       uint8_t* mask) {
+    return dpi_tf<float>(A, n, lda, tol, tfs, out, ldo, mask);
 }
 // tol arrives as float, as under `--single` (apps/filter/dpi.cpp:63,69-74).
 int64_t ref_dpi_f32(const float* A, int64_t n, int64_t lda, float tol, float* out, int64_t ldo, uint8_t* mask) {

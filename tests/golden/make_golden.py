@@ -87,6 +87,23 @@ def main():
         o, mask, removed = R.dpi(T, tol)
         res.update({f"out_{tag}": o, f"mask_{tag}": mask, f"removed_{tag}": np.int64(removed), f"tol_{tag}": tol})
     np.savez_compressed(HERE / "dpi_ties.npz", **res)
+    # ---- TF-restricted variants on an MI matrix ----
+    X = synth(90, 250, 41)
+    A = R.bspline_mi(X)
+    np.fill_diagonal(A, 0.0)
+    tfs = np.where(rng.random(90) < 0.2, np.float32(np.inf), np.float32(-np.inf)).astype(np.float32)
+    tf = {"A": A, "tfs": tfs}
+    for pl, transitions in ((2, (0, 1)), (3, (0, 1, 2)), (4, (0, 1, 2, 3))):
+        for t in transitions:
+            M, Rt = R.mcp_tf(A, tfs, pl, t)
+            tf[f"M{pl}_t{t}"], tf[f"R{pl}_t{t}"] = M, Rt
+    tol = np.float32(0.1)
+    o, mask, removed = R.dpi_tf(A, tfs, tol)
+    tf.update(DPI_out=o, DPI_mask=mask, DPI_removed=np.int64(removed), tol=tol)
+    general = rng.normal(size=90).astype(np.float32)   # a general (non +-inf) mask
+    tf["mask_general"] = general
+    tf["MM_general"] = R.maxmin_masked(A, A, general)
+    np.savez_compressed(HERE / "tf_90.npz", **tf)
     print("wrote", sorted(p.name for p in HERE.glob("*.npz")))
 
 

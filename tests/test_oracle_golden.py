@@ -144,3 +144,19 @@ def test_reference_fast_math_same_bytes(port):
         a, b = R.mcp(A, pl), RF.mcp(A, pl)
         assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
     assert np.array_equal(R.dpi(A, 0.1)[0], RF.dpi(A, 0.1)[0])
+
+
+def test_tf_variants_bit_exact(port, golden):
+    """compute_mcp{2,3,4}_tfs for every tf_gene_transition, dpi_tf_kernel and a
+    general-valued mask, against the reference's own TF kernels."""
+    g = golden("tf_90")
+    A, tfs = g["A"], g["tfs"]
+    for pl, ts in ((2, (0, 1)), (3, (0, 1, 2)), (4, (0, 1, 2, 3))):
+        for t in ts:
+            M, R = port.mcp_tf(A, tfs, pl, t)
+            assert np.array_equal(M.view(np.uint32), g[f"M{pl}_t{t}"].view(np.uint32)), (pl, t)
+            assert np.array_equal(R.view(np.uint32), g[f"R{pl}_t{t}"].view(np.uint32)), (pl, t)
+    out, mask, removed = port.dpi_tf(A, tfs, float(g["tol"]))
+    assert np.array_equal(out, g["DPI_out"]) and np.array_equal(mask, g["DPI_mask"])
+    assert removed == int(g["DPI_removed"])
+    assert np.array_equal(port.maxmin_masked(A, A, g["mask_general"]), g["MM_general"])
