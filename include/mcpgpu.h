@@ -182,6 +182,49 @@ MCPG_API int mcpg_dpi_tf(mcpg_handle* h, const float* A, int64_t n, int64_t lda,
 MCPG_API int mcpg_dpi_tf_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, float tol, const float* tfs,
                              float* out, int64_t ldo, uint8_t* mask, int64_t* removed);
 
+/* ---- adjoints (no counterpart in the reference) ----
+ * Forward/backward pairs for sample-level sensitivity of MCP scores.  Every
+ * backward ACCUMULATES (+=) into its gradient outputs, except
+ * mcpg_bspline_mi_bwd, which writes dX.
+ *
+ * mcpg_maxmin_witness: the product C = A (x) B plus, per output, the witness
+ * K[i][j] = the first k attaining the maximum (-1 where C is -inf).
+ * mcpg_maxmin_bwd: routes dC[i][j] to A[i][k*] when A[i][k*] <= B[j][k*] (the
+ * operand std::min returns on a tie) else to B[j][k*]; k* from K when given
+ * (saved witness), else recomputed from C as the first k with
+ * min(A[i][k], B[j][k]) == C[i][j] (cheap when dC is sparse).  dA and dB may be
+ * the same buffer when A and B are.  Accumulation uses atomics, so the last
+ * bits of a sum can vary between runs. */
+MCPG_API int mcpg_maxmin_witness(mcpg_handle* h, const float* A, int64_t lda, const float* B, int64_t ldb,
+                                 int64_t rows, int64_t cols, int64_t k_len, float* C, int64_t ldc, int32_t* K,
+                                 int64_t ldk);
+MCPG_API int mcpg_maxmin_witness_dev(mcpg_handle* h, const float* A, int64_t lda, const float* B, int64_t ldb,
+                                     int64_t rows, int64_t cols, int64_t k_len, float* C, int64_t ldc, int32_t* K,
+                                     int64_t ldk);
+MCPG_API int mcpg_maxmin_bwd(mcpg_handle* h, const float* A, int64_t lda, const float* B, int64_t ldb,
+                             int64_t rows, int64_t cols, int64_t k_len, const float* C, int64_t ldc,
+                             const float* dC, int64_t lddc, const int32_t* K, int64_t ldk, float* dA, int64_t ldda,
+                             float* dB, int64_t lddb);
+MCPG_API int mcpg_maxmin_bwd_dev(mcpg_handle* h, const float* A, int64_t lda, const float* B, int64_t ldb,
+                                 int64_t rows, int64_t cols, int64_t k_len, const float* C, int64_t ldc,
+                                 const float* dC, int64_t lddc, const int32_t* K, int64_t ldk, float* dA,
+                                 int64_t ldda, float* dB, int64_t lddb);
+/* Adjoint of ratio_kernel: where |A| and |M| are at least FLT_EPSILON,
+ * dA += dR / M and dM -= dR * A / M^2 (elsewhere the ratio is constant). */
+MCPG_API int mcpg_ratio_bwd_dev(mcpg_handle* h, const float* A, int64_t lda, const float* M, int64_t ldm,
+                                int64_t rows, int64_t cols, const float* dR, int64_t lddr, float* dA, int64_t ldda,
+                                float* dM, int64_t lddm);
+/* Adjoint of mcpg_bspline_mi (FP32): given G = dL/dMI (n x n, all ordered
+ * entries; the diagonal is ignored), writes dX = dL/dX (n x m).  Goes through
+ * MI_ij = H_i + H_j - H_ij (cells with p = 0 contribute no gradient), the
+ * B-spline weight derivatives as a contraction of Gs_ij (log2 P_ab + 1/ln 2)
+ * with the weights, and the min-max scaling including its min / max samples.
+ * bins <= 12. */
+MCPG_API int mcpg_bspline_mi_bwd(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_t ldx, int bins,
+                                 int order, const float* G, int64_t ldg, float* dX, int64_t lddx);
+MCPG_API int mcpg_bspline_mi_bwd_dev(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_t ldx, int bins,
+                                     int order, const float* G, int64_t ldg, float* dX, int64_t lddx);
+
 /* ---- maximum-capacity closure (no counterpart routine in the reference) ----
  * Repeated squaring B <- max(B, B (x) B) from B = A until no entry changes,
  * with (x) the reference's max_of_pairmin (include/mcp/filter/simd_maxmin.hpp:30-46).

@@ -68,6 +68,15 @@ ABI = [
     ("mcpg_dpi_tf", C.c_int, [_vp, _vp, _i64, _i64, C.c_float, _vp, _vp, _i64, _vp, C.POINTER(C.c_int64)]),
     ("mcpg_dpi_tf_dev", C.c_int, [_vp, _vp, _i64, _i64, C.c_float, _vp, _vp, _i64, _vp, C.POINTER(C.c_int64)]),
     ("mcpg_closure_dev", C.c_int, [_vp, _vp, _i64, _i64, C.c_int, _vp, _i64, C.POINTER(C.c_int)]),
+    ("mcpg_maxmin_witness", C.c_int, [_vp, _vp, _i64, _vp, _i64, _i64, _i64, _i64, _vp, _i64, _vp, _i64]),
+    ("mcpg_maxmin_witness_dev", C.c_int, [_vp, _vp, _i64, _vp, _i64, _i64, _i64, _i64, _vp, _i64, _vp, _i64]),
+    ("mcpg_maxmin_bwd", C.c_int, [_vp, _vp, _i64, _vp, _i64, _i64, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64,
+                                  _vp, _i64, _vp, _i64]),
+    ("mcpg_maxmin_bwd_dev", C.c_int, [_vp, _vp, _i64, _vp, _i64, _i64, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64,
+                                      _vp, _i64, _vp, _i64]),
+    ("mcpg_ratio_bwd_dev", C.c_int, [_vp, _vp, _i64, _vp, _i64, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64]),
+    ("mcpg_bspline_mi_bwd", C.c_int, [_vp, _vp, _i64, _i64, _i64, C.c_int, C.c_int, _vp, _i64, _vp, _i64]),
+    ("mcpg_bspline_mi_bwd_dev", C.c_int, [_vp, _vp, _i64, _i64, _i64, C.c_int, C.c_int, _vp, _i64, _vp, _i64]),
     ("mcpg_synth_grn", C.c_int, [_i64, _i64, C.c_uint64, _vp, _i64, _vp, _i64, C.POINTER(C.c_int64)]),
     ("mcpg_bspline_mi_fp32_noalloc", C.c_int, [_vp, _i64, _i64, _i64, C.c_int, C.c_int, _vp, _i64, _vp, _vp]),
 ]
@@ -306,6 +315,113 @@ class Handle:
         rows, k = A.shape
         self._check(self._L.mcpg_maxmin_dev(self._h, self._dp(A), self._ld(A), self._dp(B), self._ld(B), rows,
                                              B.shape[0], k, self._dp(Cm), self._ld(Cm)), "maxmin_dev")
+
+    def ratio_dev(self, A, M, R):
+        rows, cols = A.shape
+        self._check(self._L.mcpg_ratio_dev(self._h, self._dp(A), self._ld(A), self._dp(M), self._ld(M), rows, cols,
+                                            self._dp(R), self._ld(R)), "ratio_dev")
+
+    def maxmin_witness_dev(self, A, B, Cm, K):
+        rows, k = A.shape
+        self._check(self._L.mcpg_maxmin_witness_dev(self._h, self._dp(A), self._ld(A), self._dp(B), self._ld(B),
+                                                     rows, B.shape[0], k, self._dp(Cm), self._ld(Cm), self._dp(K),
+                                                     self._ld(K)), "maxmin_witness_dev")
+
+    def maxmin_bwd_dev(self, A, B, Cm, dC, K, dA, dB):
+        """Accumulate the adjoint of Cm = A (x) B into dA, dB (K: saved witness or None)."""
+        rows, k = A.shape
+        self._check(self._L.mcpg_maxmin_bwd_dev(
+            self._h, self._dp(A), self._ld(A), self._dp(B), self._ld(B), rows, B.shape[0], k,
+            self._dp(Cm), self._ld(Cm) if Cm is not None else 0, self._dp(dC), self._ld(dC),
+            self._dp(K), self._ld(K) if K is not None else 0, self._dp(dA), self._ld(dA), self._dp(dB),
+            self._ld(dB)), "maxmin_bwd_dev")
+
+    def ratio_bwd_dev(self, A, M, dR, dA, dM):
+        rows, cols = A.shape
+        self._check(self._L.mcpg_ratio_bwd_dev(self._h, self._dp(A), self._ld(A), self._dp(M), self._ld(M), rows, cols,
+                                                self._dp(dR), self._ld(dR), self._dp(dA), self._ld(dA), self._dp(dM),
+                                                self._ld(dM)), "ratio_bwd_dev")
+
+    def bspline_mi_bwd_dev(self, X, G, dX, bins=10, order=3):
+        n, m = X.shape
+        self._check(self._L.mcpg_bspline_mi_bwd_dev(self._h, self._dp(X), n, m, self._ld(X), bins, order,
+                                                     self._dp(G), self._ld(G), self._dp(dX), self._ld(dX)),
+                    "bspline_mi_bwd_dev")
+
+    def maxmin_witness(self, A, B=None):
+        A = _f32(A)
+        B = A if B is None else _f32(B)
+        rows, k = A.shape
+        cols = B.shape[0]
+        Cm = np.empty((rows, cols), dtype=np.float32)
+        K = np.empty((rows, cols), dtype=np.int32)
+        self._check(self._L.mcpg_maxmin_witness(self._h, _ptr(A), k, _ptr(B), k, rows, cols, k, _ptr(Cm), cols,
+                                                 _ptr(K), cols), "maxmin_witness")
+        return Cm, K
+
+    def bspline_mi_bwd(self, X, G, bins=10, order=3):
+        X, G = _f32(X), _f32(G)
+        n, m = X.shape
+        dX = np.empty((n, m), dtype=np.float32)
+        self._check(self._L.mcpg_bspline_mi_bwd(self._h, _ptr(X), n, m, m, bins, order, _ptr(G), n, _ptr(dX), m),
+                    "bspline_mi_bwd")
+        return dX
+
+    def mcp3_loss_dev(self, X, rows_idx, cols_idx, coef, bins=10, order=3, precision="fp32"):
+        """Forward only: L = sum_e coef[e] * R[rows_idx[e], cols_idx[e]] (FP64 sum of the FP32 scores)."""
+        import torch
+        n, m = X.shape
+        f32 = dict(dtype=torch.float32, device=X.device)
+        A = torch.empty((n, n), **f32)
+        self.bspline_mi_dev(X, A, bins, order, precision)
+        self.set_diagonal_dev(A, 0.0)
+        R = torch.empty((n, n), **f32)
+        self.mcp_dev(A, 3, M=None, R=R)
+        return float((coef.to(torch.float64) * R[rows_idx, cols_idx].to(torch.float64)).sum().item())
+
+    def mcp3_loss_grad_dev(self, X, rows_idx, cols_idx, coef, witness: str = "auto", bins=10, order=3,
+                           return_dA: bool = False):
+        """Differentiation form of the pipeline (torch CUDA tensors): with
+        A = MI(X) (FP32, diagonal 0), M1 = A (x) A, M2 = A (x) M1, R = ratio(A, M2),
+        L = sum_e coef[e] * R[rows_idx[e], cols_idx[e]]; returns (L, dL/dX).
+        witness: "saved" keeps int32 argmax indices of both products, "recompute"
+        finds them again from the products, "auto" saves them when the two
+        n x n int32 arrays take under a quarter of the free device memory."""
+        import torch
+        n, m = X.shape
+        dev = X.device
+        f32 = dict(dtype=torch.float32, device=dev)
+        if witness == "auto":
+            free, _ = torch.cuda.mem_get_info(dev)
+            witness = "saved" if 2 * n * n * 4 < free // 4 else "recompute"
+        MI = torch.empty((n, n), **f32)
+        self.bspline_mi_dev(X, MI, bins, order, "fp32")
+        A = MI
+        self.set_diagonal_dev(A, 0.0)
+        M1, M2, R = (torch.empty((n, n), **f32) for _ in range(3))
+        K1 = K2 = None
+        if witness == "saved":
+            K1 = torch.empty((n, n), dtype=torch.int32, device=dev)
+            K2 = torch.empty((n, n), dtype=torch.int32, device=dev)
+            self.maxmin_witness_dev(A, A, M1, K1)
+            self.maxmin_witness_dev(A, M1, M2, K2)
+        else:
+            self.maxmin_dev(A, A, M1)
+            self.maxmin_dev(A, M1, M2)
+        self.ratio_dev(A, M2, R)
+        L = (coef.to(torch.float64) * R[rows_idx, cols_idx].to(torch.float64)).sum()
+        dR = torch.zeros((n, n), **f32)
+        dR.index_put_((rows_idx, cols_idx), coef.to(torch.float32), accumulate=True)
+        dA, dM2, dM1 = (torch.zeros((n, n), **f32) for _ in range(3))
+        self.ratio_bwd_dev(A, M2, dR, dA, dM2)
+        self.maxmin_bwd_dev(A, M1, M2, dM2, K2, dA, dM1)
+        self.maxmin_bwd_dev(A, A, M1, dM1, K1, dA, dA)
+        dA.fill_diagonal_(0.0)  # the diagonal reset cuts the gradient to MI_ii
+        dX = torch.empty((n, m), **f32)
+        self.bspline_mi_bwd_dev(X, dA, dX, bins, order)
+        if return_dA:
+            return float(L.item()), dX, dA
+        return float(L.item()), dX
 
     def set_diagonal_dev(self, A, value: float):
         self._check(self._L.mcpg_set_diagonal_dev(self._h, self._dp(A), A.shape[0], A.shape[1], self._ld(A), value),

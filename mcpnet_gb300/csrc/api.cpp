@@ -43,6 +43,11 @@ enum Slot {
     S_TFROWS,    // TF rows of the MI matrix (tfs_to_genes)
     S_M3,        // third intermediate (TF MCP4)
     S_IN2,       // staged host input 2
+    S_Q,         // MI adjoint slab Q
+    S_DW,        // MI adjoint dW slab
+    S_GS,        // MI adjoint pair sums
+    S_IN3,       // staged host input 3
+    S_IN4,       // staged host input 4
     NSLOTS
 };
 
@@ -699,6 +704,127 @@ int dpi_tf_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, float tol
     return MCPG_OK;
 }
 
+
+// ---------------- adjoints ----------------
+int maxmin_witness_dev(mcpg_handle* h, const float* A, int64_t lda, const float* B, int64_t ldb, int64_t rows,
+                       int64_t cols, int64_t k, float* C, int64_t ldc, int32_t* K, int64_t ldk) {
+    if (rows < 0 || cols < 0 || k < 0) return fail(h, MCPG_ERR_ARG, "maxmin_witness: negative size");
+    if (rows == 0 || cols == 0) return MCPG_OK;
+    if (!A || !B || !C || !K) return fail(h, MCPG_ERR_ARG, "maxmin_witness: null pointer");
+    if (lda < k || ldb < k || ldc < cols || ldk < cols)
+        return fail(h, MCPG_ERR_ARG, "maxmin_witness: leading dimension too small");
+    const bool symm = (A == B) && (lda == ldb) && (rows == cols);
+    const float *a, *b;
+    int64_t la, lb;
+    int rc = aligned_view(h, A, lda, rows, k, S_IN0, &a, &la);
+    if (rc) return rc;
+    if (symm) {
+        b = a; lb = la;
+    } else if ((rc = aligned_view(h, B, ldb, cols, k, S_IN1, &b, &lb))) {
+        return rc;
+    }
+    mcpg::MaxminParams p{};
+    p.A = a; p.lda = la; p.B = b; p.ldb = lb; p.rows = rows; p.cols = cols; p.k_len = k;
+    p.C = C; p.ldc = ldc; p.K = K; p.ldk = ldk;
+    PROF(h, "maxmin_witness");
+    CK(h, mcpg::launch_maxmin(p, mcpg::MM_WITNESS, symm ? 1 : 0, h->stream, &h->launches), "maxmin witness kernel");
+    return MCPG_OK;
+}
+
+int maxmin_bwd_dev(mcpg_handle* h, const float* A, int64_t lda, const float* B, int64_t ldb, int64_t rows,
+                   int64_t cols, int64_t k, const float* C, int64_t ldc, const float* dC, int64_t lddc,
+                   const int32_t* K, int64_t ldk, float* dA, int64_t ldda, float* dB, int64_t lddb) {
+    if (rows < 0 || cols < 0 || k < 0) return fail(h, MCPG_ERR_ARG, "maxmin_bwd: negative size");
+    if (rows == 0 || cols == 0) return MCPG_OK;
+    if (!A || !B || !dC || !dA || !dB || (!K && !C)) return fail(h, MCPG_ERR_ARG, "maxmin_bwd: null pointer");
+    if (lda < k || ldb < k || lddc < cols || ldda < k || lddb < k || (K && ldk < cols) || (!K && ldc < cols))
+        return fail(h, MCPG_ERR_ARG, "maxmin_bwd: leading dimension too small");
+    PROF(h, "maxmin_route");
+    CK(h, mcpg::launch_maxmin_route(A, lda, B, ldb, rows, cols, k, C, ldc, dC, lddc, K, ldk, dA, ldda, dB, lddb,
+                                    h->stream, &h->launches),
+       "maxmin route kernel");
+    return MCPG_OK;
+}
+
+int ratio_bwd_dev(mcpg_handle* h, const float* A, int64_t lda, const float* M, int64_t ldm, int64_t rows, int64_t cols,
+                  const float* dR, int64_t lddr, float* dA, int64_t ldda, float* dM, int64_t lddm) {
+    if (rows < 0 || cols < 0) return fail(h, MCPG_ERR_ARG, "ratio_bwd: negative size");
+    if (rows == 0 || cols == 0) return MCPG_OK;
+    if (!A || !M || !dR || !dA || !dM) return fail(h, MCPG_ERR_ARG, "ratio_bwd: null pointer");
+    if (lda < cols || ldm < cols || lddr < cols || ldda < cols || lddm < cols)
+        return fail(h, MCPG_ERR_ARG, "ratio_bwd: leading dimension too small");
+    PROF(h, "ratio_bwd");
+    CK(h, mcpg::launch_ratio_bwd(A, lda, M, ldm, rows, cols, dR, lddr, dA, ldda, dM, lddm, h->stream, &h->launches),
+       "ratio_bwd kernel");
+    return MCPG_OK;
+}
+
+// MI adjoint: dX from G = dL/dMI (FP32).  Q = Gs (log2 P + 1/ln 2) is built in
+// slabs of gene tiles that fit the slab budget, contracted with the weights on
+// the plus-times twin of the max-min kernel, then pushed through the B-spline
+// derivative and the min-max scaling per gene.
+int mi_bwd_dev(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_t ldx, int bins, int order,
+               const float* G, int64_t ldg, float* dX, int64_t lddx) {
+    if (n < 1 || m < 1) return fail(h, MCPG_ERR_ARG, "bspline_mi_bwd: need n >= 1 and m >= 1");
+    if (!X || !G || !dX) return fail(h, MCPG_ERR_ARG, "bspline_mi_bwd: null pointer");
+    if (ldx < m || ldg < n || lddx < m) return fail(h, MCPG_ERR_ARG, "bspline_mi_bwd: leading dimension too small");
+    if (bins < 1 || bins > 12 || order < 1 || order > 8 || bins < order)
+        return fail(h, MCPG_ERR_ARG, "bspline_mi_bwd: need 1 <= order <= bins <= 12, order <= 8");
+    int rc;
+    const int64_t ldwt = round_up(n, 16) * bins;
+    const int64_t m_pad = round_up(m, 16);
+    void *wt, *hd, *gs;
+    if ((rc = scratch(h, S_W0, (size_t)(m_pad * ldwt) * sizeof(float), &wt))) return rc;
+    if ((rc = scratch(h, S_H, (size_t)n * sizeof(double), &hd))) return rc;
+    if ((rc = scratch(h, S_GS, (size_t)n * sizeof(float), &gs))) return rc;
+    CK(h, cudaMemsetAsync(wt, 0, (size_t)(m_pad * ldwt) * sizeof(float), h->stream), "memset weights");
+    {
+        PROF(h, "bspline_weights");
+        CK(h, mcpg::launch_bspline_weights_fp32(X, n, m, ldx, bins, order, (float*)wt, ldwt, (double*)hd, h->stream,
+                                                 &h->launches),
+           "bspline weights kernel");
+    }
+    {
+        PROF(h, "pair_sums");
+        CK(h, mcpg::launch_pair_sums(G, ldg, n, (float*)gs, h->stream, &h->launches), "pair sums kernel");
+    }
+    const int64_t T = (n + 15) / 16;
+    const int64_t ldq = ldwt;  // >= n*bins, multiple of 4
+    const size_t budget = (size_t)2 << 30;
+    int64_t tiles_per_slab = (int64_t)(budget / ((size_t)16 * bins * ldq * sizeof(float)));
+    if (tiles_per_slab < 1) tiles_per_slab = 1;
+    if (tiles_per_slab > T) tiles_per_slab = T;
+    const int64_t lddw = round_up(m, 4);
+    void *q, *dw;
+    if ((rc = scratch(h, S_Q, (size_t)(tiles_per_slab * 16 * bins * ldq) * sizeof(float), &q))) return rc;
+    if ((rc = scratch(h, S_DW, (size_t)(tiles_per_slab * 16 * bins * lddw) * sizeof(float), &dw))) return rc;
+    for (int64_t t0 = 0; t0 < T; t0 += tiles_per_slab) {
+        const int64_t nt = (t0 + tiles_per_slab <= T) ? tiles_per_slab : T - t0;
+        const int64_t g0 = t0 * 16, g1 = (g0 + nt * 16 < n) ? g0 + nt * 16 : n;
+        {
+            PROF(h, "mi_q");
+            CK(h, mcpg::launch_mi_q((const float*)wt, ldwt, G, ldg, n, m, bins, t0, nt, (float*)q, ldq, h->stream,
+                                    &h->launches),
+               "MI adjoint Q kernel");
+        }
+        mcpg::MaxminParams p{};
+        p.A = (const float*)q; p.lda = ldq; p.B = (const float*)wt; p.ldb = ldwt;
+        p.rows = (g1 - g0) * bins; p.cols = m; p.k_len = n * bins;
+        p.C = (float*)dw; p.ldc = lddw;
+        {
+            PROF(h, "gemm");
+            CK(h, mcpg::launch_maxmin(p, mcpg::MM_GEMM, 0, h->stream, &h->launches), "adjoint contraction kernel");
+        }
+        {
+            PROF(h, "mi_bwd_x");
+            CK(h, mcpg::launch_mi_bwd_x(X, n, m, ldx, bins, order, g0, g1, (const float*)gs, (const float*)dw, lddw,
+                                        dX, lddx, h->stream, &h->launches),
+               "MI adjoint x kernel");
+        }
+    }
+    return MCPG_OK;
+}
+
 }  // namespace
 
 // =====================================================================
@@ -1144,6 +1270,118 @@ int mcpg_dpi_tf(mcpg_handle* h, const float* A, int64_t n, int64_t lda, float to
     if ((rc = dpi_tf_dev(h, dA, n, la, tol, tfs, dO, lo, dMask, removed))) return rc;
     if ((rc = copy_out(h, out, ldo, dO, lo, n, n))) return rc;
     if (mask) CK(h, cudaMemcpyAsync(mask, dMask, (size_t)(n * n), cudaMemcpyDeviceToHost, h->stream), "copy mask");
+    return finish(h);
+}
+
+
+// ---- adjoints ----
+int mcpg_maxmin_witness_dev(mcpg_handle* h, const float* A, int64_t lda, const float* B, int64_t ldb, int64_t rows,
+                            int64_t cols, int64_t k, float* C, int64_t ldc, int32_t* K, int64_t ldk) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    return maxmin_witness_dev(h, A, lda, B, ldb, rows, cols, k, C, ldc, K, ldk);
+}
+
+int mcpg_maxmin_witness(mcpg_handle* h, const float* A, int64_t lda, const float* B, int64_t ldb, int64_t rows,
+                        int64_t cols, int64_t k, float* C, int64_t ldc, int32_t* K, int64_t ldk) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (rows < 0 || cols < 0 || k < 0) return fail(h, MCPG_ERR_ARG, "maxmin_witness: negative size");
+    if (rows == 0 || cols == 0) return MCPG_OK;
+    if (!A || !B || !C || !K) return fail(h, MCPG_ERR_ARG, "maxmin_witness: null pointer");
+    if (lda < k || ldb < k || ldc < cols || ldk < cols)
+        return fail(h, MCPG_ERR_ARG, "maxmin_witness: leading dimension too small");
+    const bool same = (A == B) && (lda == ldb) && (rows == cols);
+    float *dA, *dB, *dC, *dK;
+    int64_t la, lb, lc, lk;
+    if ((rc = stage_in(h, S_IN0, A, lda, rows, k, &dA, &la))) return rc;
+    if (same) {
+        dB = dA; lb = la;
+    } else if ((rc = stage_in(h, S_IN1, B, ldb, cols, k, &dB, &lb))) {
+        return rc;
+    }
+    if ((rc = stage_out_alloc(h, S_OUT0, rows, cols, &dC, &lc))) return rc;
+    if ((rc = stage_out_alloc(h, S_OUT1, rows, cols, &dK, &lk))) return rc;
+    if ((rc = maxmin_witness_dev(h, dA, la, dB, lb, rows, cols, k, dC, lc, (int32_t*)dK, lk))) return rc;
+    if ((rc = copy_out(h, C, ldc, dC, lc, rows, cols))) return rc;
+    if ((rc = copy_out(h, (float*)K, ldk, dK, lk, rows, cols))) return rc;
+    return finish(h);
+}
+
+int mcpg_maxmin_bwd_dev(mcpg_handle* h, const float* A, int64_t lda, const float* B, int64_t ldb, int64_t rows,
+                        int64_t cols, int64_t k, const float* C, int64_t ldc, const float* dC, int64_t lddc,
+                        const int32_t* K, int64_t ldk, float* dA, int64_t ldda, float* dB, int64_t lddb) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    return maxmin_bwd_dev(h, A, lda, B, ldb, rows, cols, k, C, ldc, dC, lddc, K, ldk, dA, ldda, dB, lddb);
+}
+
+int mcpg_maxmin_bwd(mcpg_handle* h, const float* A, int64_t lda, const float* B, int64_t ldb, int64_t rows,
+                    int64_t cols, int64_t k, const float* C, int64_t ldc, const float* dC, int64_t lddc,
+                    const int32_t* K, int64_t ldk, float* dA, int64_t ldda, float* dB, int64_t lddb) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (rows < 0 || cols < 0 || k < 0) return fail(h, MCPG_ERR_ARG, "maxmin_bwd: negative size");
+    if (rows == 0 || cols == 0) return MCPG_OK;
+    if (!A || !B || !dC || !dA || !dB || (!K && !C)) return fail(h, MCPG_ERR_ARG, "maxmin_bwd: null pointer");
+    if (lda < k || ldb < k || lddc < cols || ldda < k || lddb < k || (K && ldk < cols) || (!K && ldc < cols))
+        return fail(h, MCPG_ERR_ARG, "maxmin_bwd: leading dimension too small");
+    const bool same_in = (A == B) && (lda == ldb) && (rows == cols);
+    const bool same_out = (dA == dB) && (ldda == lddb) && (rows == cols);
+    float *a, *b, *c = nullptr, *g, *ga, *gb, *kk = nullptr;
+    int64_t la, lb, lc = 0, lg, lga, lgb, lk = 0;
+    if ((rc = stage_in(h, S_IN0, A, lda, rows, k, &a, &la))) return rc;
+    if (same_in) {
+        b = a; lb = la;
+    } else if ((rc = stage_in(h, S_IN1, B, ldb, cols, k, &b, &lb))) {
+        return rc;
+    }
+    if (K) {
+        if ((rc = stage_in(h, S_IN2, (const float*)K, ldk, rows, cols, &kk, &lk))) return rc;
+    } else if ((rc = stage_in(h, S_IN2, C, ldc, rows, cols, &c, &lc))) {
+        return rc;
+    }
+    if ((rc = stage_in(h, S_IN3, dC, lddc, rows, cols, &g, &lg))) return rc;
+    if ((rc = stage_in(h, S_OUT0, dA, ldda, rows, k, &ga, &lga))) return rc;
+    if (same_out) {
+        gb = ga; lgb = lga;
+    } else if ((rc = stage_in(h, S_OUT1, dB, lddb, cols, k, &gb, &lgb))) {
+        return rc;
+    }
+    if ((rc = maxmin_bwd_dev(h, a, la, b, lb, rows, cols, k, c, lc, g, lg, (const int32_t*)kk, lk, ga, lga, gb, lgb)))
+        return rc;
+    if ((rc = copy_out(h, dA, ldda, ga, lga, rows, k))) return rc;
+    if (!same_out && (rc = copy_out(h, dB, lddb, gb, lgb, cols, k))) return rc;
+    return finish(h);
+}
+
+int mcpg_ratio_bwd_dev(mcpg_handle* h, const float* A, int64_t lda, const float* M, int64_t ldm, int64_t rows,
+                       int64_t cols, const float* dR, int64_t lddr, float* dA, int64_t ldda, float* dM, int64_t lddm) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    return ratio_bwd_dev(h, A, lda, M, ldm, rows, cols, dR, lddr, dA, ldda, dM, lddm);
+}
+
+int mcpg_bspline_mi_bwd_dev(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_t ldx, int bins, int order,
+                            const float* G, int64_t ldg, float* dX, int64_t lddx) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    return mi_bwd_dev(h, X, n, m, ldx, bins, order, G, ldg, dX, lddx);
+}
+
+int mcpg_bspline_mi_bwd(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_t ldx, int bins, int order,
+                        const float* G, int64_t ldg, float* dX, int64_t lddx) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (n < 1 || m < 1 || !X || !G || !dX || ldx < m || ldg < n || lddx < m)
+        return fail(h, MCPG_ERR_ARG, "bspline_mi_bwd: bad arguments");
+    float *dXin, *dG, *dOut;
+    int64_t lx, lg, lo;
+    if ((rc = stage_in(h, S_IN3, X, ldx, n, m, &dXin, &lx))) return rc;
+    if ((rc = stage_in(h, S_IN4, G, ldg, n, n, &dG, &lg))) return rc;
+    if ((rc = stage_out_alloc(h, S_OUT0, n, m, &dOut, &lo))) return rc;
+    if ((rc = mi_bwd_dev(h, dXin, n, m, lx, bins, order, dG, lg, dOut, lo))) return rc;
+    if ((rc = copy_out(h, dX, lddx, dOut, lo, n, m))) return rc;
     return finish(h);
 }
 

@@ -54,7 +54,8 @@ void host_knots(int bins, int order, Knots& k) {
 // for bit.  BT / OT > 0 fix bins / order at compile time (registers only);
 // 0 takes them from the arguments.
 template <int BT, int OT>
-__device__ __forceinline__ void basis_all(const Knots& kv, int bins_rt, int order_rt, float t, float* out) {
+__device__ __forceinline__ void basis_all(const Knots& kv, int bins_rt, int order_rt, float t, float* out,
+                                          float* prev = nullptr) {
     const int bins = BT ? BT : bins_rt;
     const int order = OT ? OT : order_rt;
     constexpr int NMAX = (BT && OT) ? BT + OT : KNOTS_MAX;
@@ -71,6 +72,11 @@ __device__ __forceinline__ void basis_all(const Knots& kv, int bins_rt, int orde
 #pragma unroll
     for (int p = 2; p <= (OT ? OT : KMAX_ORDER); ++p) {
         if (p > order) break;
+        if (prev && p == order) {  // keep the order-1 level (bins + 1 values) for the derivative
+#pragma unroll
+            for (int i = 0; i < (BT ? BT + 1 : KMAX_BINS + 1); ++i)
+                if (i <= bins) prev[i] = N[i];
+        }
         const int np = bins + order - p;
 #pragma unroll
         for (int i = 0; i < NMAX - 1; ++i) {
@@ -213,7 +219,170 @@ __global__ void __launch_bounds__(WTHREADS) bspline_weights_kernel(const float* 
     }
 }
 
+// ---------------- MI adjoint through the weights and the scaling ----------------
+// Derivative of the basis, from the order-1 level:
+//   N'_{a,p}(t) = (p-1) [ N_{a,p-1}(t)/(t_{a+p-1}-t_a) - N_{a+1,p-1}(t)/(t_{a+p}-t_{a+1}) ]
+// (a term is dropped when its knot span is below 1e-10, the basis's own guard).
+__device__ __forceinline__ float basis_deriv(const Knots& kv, int order, int a, const float* prev) {
+    if (order <= 1) return 0.0f;
+    const float d1 = kv.v[a + order - 1] - kv.v[a], d2 = kv.v[a + order] - kv.v[a + 1];
+    float r = 0.0f;
+    if (!(d1 < 1e-10f)) r += prev[a] / d1;
+    if (!(d2 < 1e-10f)) r -= prev[a + 1] / d2;
+    return (float)(order - 1) * r;
+}
+
+struct ValIdx {
+    float v;
+    int64_t i;
+};
+
+template <int BT, int OT>
+__global__ void __launch_bounds__(WTHREADS) mi_bwd_x_kernel(const float* __restrict__ X, int64_t m, int64_t ldx,
+                                                            int bins_rt, int order_rt, const Knots kv, int64_t g0,
+                                                            const float* __restrict__ gsum,
+                                                            const float* __restrict__ dWq, int64_t lddw,
+                                                            float* __restrict__ dX, int64_t lddx) {
+    __shared__ ValIdx red_min[WTHREADS / 32], red_max[WTHREADS / 32];
+    __shared__ double dred[2][WTHREADS / 32];
+    __shared__ double psum[KMAX_BINS][WTHREADS / 32];
+    __shared__ float hc[KMAX_BINS];
+    const int64_t g = g0 + blockIdx.x;
+    const float* x = X + g * ldx;
+    const int bins = BT ? BT : bins_rt;
+    const int order = OT ? OT : order_rt;
+    constexpr int NB = BT ? BT : KMAX_BINS;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+
+    // first arg-min / arg-max (ties -> lowest sample index)
+    ValIdx mn{INFINITY, INT64_MAX}, mx{-INFINITY, INT64_MAX};
+    for (int64_t s = threadIdx.x; s < m; s += blockDim.x) {
+        const float v = x[s];
+        if (v < mn.v || (v == mn.v && s < mn.i)) mn = {v, s};
+        if (v > mx.v || (v == mx.v && s < mx.i)) mx = {v, s};
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        ValIdx a{__shfl_xor_sync(0xffffffffu, mn.v, o), __shfl_xor_sync(0xffffffffu, mn.i, o)};
+        ValIdx b{__shfl_xor_sync(0xffffffffu, mx.v, o), __shfl_xor_sync(0xffffffffu, mx.i, o)};
+        if (a.v < mn.v || (a.v == mn.v && a.i < mn.i)) mn = a;
+        if (b.v > mx.v || (b.v == mx.v && b.i < mx.i)) mx = b;
+    }
+    if (lane == 0) { red_min[warp] = mn; red_max[warp] = mx; }
+    __syncthreads();
+    mn = red_min[0];
+    mx = red_max[0];
+    for (int w = 1; w < nw; ++w) {
+        const ValIdx a = red_min[w], b = red_max[w];
+        if (a.v < mn.v || (a.v == mn.v && a.i < mn.i)) mn = a;
+        if (b.v > mx.v || (b.v == mx.v && b.i < mx.i)) mx = b;
+    }
+    const bool ranged = mx.v > mn.v;
+    const float scale = ranged ? (float)(1.0 / (double)__fsub_rn(mx.v, mn.v)) : 1.0f;
+    const float offset = ranged ? mn.v : 0.0f;
+
+    // marginals p_a -> log2 p_a + 1/ln 2
+    float w[NB], prev[NB + 1];
+    double acc[NB];
+#pragma unroll
+    for (int a = 0; a < NB; ++a) acc[a] = 0.0;
+    for (int64_t s = threadIdx.x; s < m; s += blockDim.x) {
+        const float t = __fmul_rn(scale, __fsub_rn(x[s], offset));
+        basis_all<BT, OT>(kv, bins_rt, order_rt, t, w);
+#pragma unroll
+        for (int a = 0; a < NB; ++a)
+            if (a < bins) acc[a] += (double)w[a];
+    }
+#pragma unroll
+    for (int a = 0; a < NB; ++a) {
+        if (a >= bins) break;
+        double v = acc[a];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) psum[a][warp] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < bins) {
+        double p = 0.0;
+        for (int w2 = 0; w2 < nw; ++w2) p += psum[threadIdx.x][w2];
+        p /= (double)m;
+        hc[threadIdx.x] = p > 0.0 ? (float)(log2(p) + 1.4426950408889634) : 0.0f;
+    }
+    __syncthreads();
+
+    // dL/dt_s = (1/m) sum_a (-hc_a gsum + dWq[a][s]) N'_a(t_s), then dL/dx
+    const float gs = gsum[g];
+    const float inv_m = 1.0f / (float)m;
+    double s1 = 0.0, s2 = 0.0;
+    const float* dw = dWq + (int64_t)blockIdx.x * bins * lddw;
+    for (int64_t s = threadIdx.x; s < m; s += blockDim.x) {
+        const float t = __fmul_rn(scale, __fsub_rn(x[s], offset));
+        basis_all<BT, OT>(kv, bins_rt, order_rt, t, w, prev);
+        float dt = 0.0f;
+#pragma unroll
+        for (int a = 0; a < NB; ++a) {
+            if (a >= bins) break;
+            const float gw = dw[(int64_t)a * lddw + s] - hc[a] * gs;
+            dt += gw * basis_deriv(kv, order, a, prev);
+        }
+        dt *= inv_m;
+        dX[g * lddx + s] = scale * dt;
+        s1 += (double)dt * ((double)t - 1.0);
+        s2 += (double)dt * (double)t;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+        s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+    }
+    if (lane == 0) { dred[0][warp] = s1; dred[1][warp] = s2; }
+    __syncthreads();
+    if (threadIdx.x == 0 && ranged) {
+        double a1 = 0.0, a2 = 0.0;
+        for (int w2 = 0; w2 < nw; ++w2) { a1 += dred[0][w2]; a2 += dred[1][w2]; }
+        dX[g * lddx + mn.i] += (float)((double)scale * a1);   // d t_s / d min = scale (t_s - 1)
+        dX[g * lddx + mx.i] -= (float)((double)scale * a2);   // d t_s / d max = -scale t_s
+    }
+}
+
+__global__ void pair_sums_kernel(const float* __restrict__ G, int64_t ldg, int64_t n, float* __restrict__ gsum) {
+    // one warp per gene: row sum + column sum, diagonal excluded
+    const int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (i >= n) return;
+    double s = 0.0;
+    for (int64_t j = lane; j < n; j += 32)
+        if (j != i) s += (double)G[i * ldg + j] + (double)G[j * ldg + i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) gsum[i] = (float)s;
+}
+
 }  // namespace
+
+cudaError_t launch_pair_sums(const float* G, int64_t ldg, int64_t n, float* gsum, cudaStream_t stream,
+                             int64_t* launches) {
+    if (n <= 0) return cudaSuccess;
+    if (launches) ++*launches;
+    pair_sums_kernel<<<(unsigned)ceil_div(n, 8), 256, 0, stream>>>(G, ldg, n, gsum);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mi_bwd_x(const float* X, int64_t n, int64_t m, int64_t ldx, int bins, int order, int64_t g0,
+                            int64_t g1, const float* gsum, const float* dWq, int64_t lddw, float* dX, int64_t lddx,
+                            cudaStream_t stream, int64_t* launches) {
+    if (g1 <= g0) return cudaSuccess;
+    Knots kv;
+    host_knots(bins, order, kv);
+    if (launches) ++*launches;
+    if (bins == 10 && order == 3)
+        mi_bwd_x_kernel<10, 3><<<(unsigned)(g1 - g0), WTHREADS, 0, stream>>>(X, m, ldx, bins, order, kv, g0, gsum,
+                                                                            dWq, lddw, dX, lddx);
+    else
+        mi_bwd_x_kernel<0, 0><<<(unsigned)(g1 - g0), WTHREADS, 0, stream>>>(X, m, ldx, bins, order, kv, g0, gsum,
+                                                                          dWq, lddw, dX, lddx);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_bspline_weights_ref(const float* X, int64_t n, int64_t m, int64_t ldx, int bins, int order,
                                        float* W, double* H, cudaStream_t stream, int64_t* launches) {

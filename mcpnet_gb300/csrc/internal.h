@@ -16,6 +16,8 @@ enum MaxminMode : int {
     MM_DPI = 3,      // C = dpi-mask(E) applied to E; k excluded when k == i or k == j
     MM_EXCL = 4,     // C = max over admissible k of min(A[i][k], B[j][k]); k excluded as in
                      // MM_DPI; an output with no admissible k is NaN
+    MM_WITNESS = 5,  // C = A (x) B and K[i][j] = first k attaining it (-1 where C is -inf)
+    MM_GEMM = 6,     // C = A B^T in (+, x): the plus-times twin of the kernel (FP32 FFMA)
 };
 
 struct MaxminParams {
@@ -33,6 +35,7 @@ struct MaxminParams {
     // excl_col[j] (device, -1 = none) when given, else i and j.
     const int* excl_row;
     const int* excl_col;
+    int32_t* K; int64_t ldk;      // MM_WITNESS output
 };
 
 // symmetric != 0: A == B (same rows), rows == cols; only tiles on or above the
@@ -55,6 +58,17 @@ cudaError_t launch_fold_mask(const float* src, int64_t lds, const float* mask, i
 cudaError_t launch_dpi_tf_apply(const float* A, int64_t lda, const float* Call, int64_t ld1, const float* Ctf,
                                 int64_t ld2, const uint8_t* tf, int64_t n, float tol_mult, float* out, int64_t ldo,
                                 uint8_t* mask, unsigned long long* removed, cudaStream_t stream, int64_t* launches);
+// Adjoint of C = A (x) B: for every (i, j) with dC != 0 route dC to A[i][k*]
+// (if A[i][k*] <= B[j][k*]) or B[j][k*], k* = K[i][j] when K is given, else the
+// first k with min(A[i][k], B[j][k]) == C[i][j].  Accumulates with atomics.
+cudaError_t launch_maxmin_route(const float* A, int64_t lda, const float* B, int64_t ldb, int64_t rows, int64_t cols,
+                                int64_t k, const float* C, int64_t ldc, const float* dC, int64_t lddc,
+                                const int32_t* K, int64_t ldk, float* dA, int64_t ldda, float* dB, int64_t lddb,
+                                cudaStream_t stream, int64_t* launches);
+// Adjoint of ratio_kernel: dA += dR / M, dM -= dR A / M^2 where |A|, |M| >= FLT_EPSILON.
+cudaError_t launch_ratio_bwd(const float* A, int64_t lda, const float* M, int64_t ldm, int64_t rows, int64_t cols,
+                             const float* dR, int64_t lddr, float* dA, int64_t ldda, float* dM, int64_t lddm,
+                             cudaStream_t stream, int64_t* launches);
 // Copies a rows x cols matrix between arbitrary leading dimensions (device to device).
 cudaError_t launch_copy2d(const float* src, int64_t lds, float* dst, int64_t ldd, int64_t rows, int64_t cols,
                           cudaStream_t stream);
@@ -74,6 +88,19 @@ cudaError_t launch_bspline_weights_16(const float* X, int64_t n, int64_t m, int6
 // FP32 MI from sample-major weights (CUDA cores), symmetric output.
 cudaError_t launch_mi_fp32(const float* Wt, int64_t ldwt, const double* H, int64_t n, int64_t m, int bins,
                            float* MI, int64_t ldmi, cudaStream_t stream, int64_t* launches);
+// MI adjoint, slab of gene tiles [tile0, tile0 + tiles) (16 genes each) x all genes:
+// Q[(i - 16*tile0)*bins + a][j*bins + b] = Gs_ij (log2 P_ab + 1/ln 2) [P_ab > 0],
+// Gs_ij = G[i][j] + G[j][i] (i != j), recomputing P from the sample-major weights.
+cudaError_t launch_mi_q(const float* Wt, int64_t ldwt, const float* G, int64_t ldg, int64_t n, int64_t m, int bins,
+                        int64_t tile0, int64_t tiles, float* Q, int64_t ldq, cudaStream_t stream, int64_t* launches);
+// gsum[i] = sum_{j != i} (G[i][j] + G[j][i])
+cudaError_t launch_pair_sums(const float* G, int64_t ldg, int64_t n, float* gsum, cudaStream_t stream,
+                             int64_t* launches);
+// dL/dX for genes [g0, g1) from dWq[(g - g0)*bins + a][s] (= sum_j,b Q w_jb(s)), gsum,
+// through the weights (B-spline derivative), the min-max scaling and its min / max.
+cudaError_t launch_mi_bwd_x(const float* X, int64_t n, int64_t m, int64_t ldx, int bins, int order, int64_t g0,
+                            int64_t g1, const float* gsum, const float* dWq, int64_t lddw, float* dX, int64_t lddx,
+                            cudaStream_t stream, int64_t* launches);
 // Tensor-core MI (tcgen05) from 16-bit weights; split != 0 adds the lo terms.
 // Returns cudaErrorNotSupported when the shape/bins is outside the kernel's tiling.
 cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, int64_t ldw, const double* H, int64_t n,

@@ -117,7 +117,16 @@ __global__ void __launch_bounds__(THREADS, MCPG_MM_MINB) maxmin_kernel(const Max
     // DPI: NaN is the neutral element of the NaN-ignoring max, so an output with
     // no admissible y stays NaN and compares false (the reference keeps it).
     constexpr bool EXCL = (MODE == MM_DPI || MODE == MM_EXCL);
-    const float init = EXCL ? __int_as_float(0x7fc00000) : -INFINITY;
+    constexpr bool WIT = (MODE == MM_WITNESS);
+    constexpr bool GEMM = (MODE == MM_GEMM);
+    const float init = EXCL ? __int_as_float(0x7fc00000) : (GEMM ? 0.0f : -INFINITY);
+    int32_t kidx[WIT ? 8 : 1][WIT ? 8 : 1];
+    if (WIT) {
+#pragma unroll
+        for (int q = 0; q < (WIT ? 8 : 1); ++q)
+#pragma unroll
+            for (int r = 0; r < (WIT ? 8 : 1); ++r) kidx[q][r] = -1;
+    }
     // excluded k per owned row / column (EXCL modes)
     int64_t exr[8], exc[8];
     if (EXCL) {
@@ -166,7 +175,36 @@ __global__ void __launch_bounds__(THREADS, MCPG_MM_MINB) maxmin_kernel(const Max
                    (k0 < i0 + BM && k0 + BK > i0) || (k0 < j0 + BN && k0 + BK > j0);
         }
         if (kmax == BK && !excl) {
-            if (KSTEP == 2) {
+            if (WIT || GEMM) {
+#pragma unroll
+                for (int kk = 0; kk < BK; kk += 4) {
+                    float4 a[8];
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) a[q] = *reinterpret_cast<const float4*>(a_base + q * 16 * LDS + kk);
+#pragma unroll
+                    for (int r = 0; r < 8; ++r) {
+                        const float4 b = *reinterpret_cast<const float4*>(b_base + r * 16 * LDS + kk);
+#pragma unroll
+                        for (int q = 0; q < 8; ++q) {
+                            if (GEMM) {
+                                float t = fmaf(a[q].x, b.x, acc[q][r]);
+                                t = fmaf(a[q].y, b.y, t);
+                                t = fmaf(a[q].z, b.z, t);
+                                acc[q][r] = fmaf(a[q].w, b.w, t);
+                            } else {
+                                // first k attaining the running maximum (strict >)
+                                const int32_t y0 = (int32_t)(k0 + kk);
+                                const float v0 = fmin2(a[q].x, b.x), v1 = fmin2(a[q].y, b.y);
+                                const float v2 = fmin2(a[q].z, b.z), v3 = fmin2(a[q].w, b.w);
+                                if (v0 > acc[q][r]) { acc[q][r] = v0; kidx[WIT ? q : 0][WIT ? r : 0] = y0; }
+                                if (v1 > acc[q][r]) { acc[q][r] = v1; kidx[WIT ? q : 0][WIT ? r : 0] = y0 + 1; }
+                                if (v2 > acc[q][r]) { acc[q][r] = v2; kidx[WIT ? q : 0][WIT ? r : 0] = y0 + 2; }
+                                if (v3 > acc[q][r]) { acc[q][r] = v3; kidx[WIT ? q : 0][WIT ? r : 0] = y0 + 3; }
+                            }
+                        }
+                    }
+                }
+            } else if (KSTEP == 2) {
 #pragma unroll
                 for (int kk = 0; kk < BK; kk += 2) {
                     float2 a[8];
@@ -209,7 +247,15 @@ __global__ void __launch_bounds__(THREADS, MCPG_MM_MINB) maxmin_kernel(const Max
                 for (int q = 0; q < 8; ++q)
 #pragma unroll
                     for (int r = 0; r < 8; ++r) {
+                        if (GEMM) {
+                            acc[q][r] = fmaf(a[q], b[r], acc[q][r]);
+                            continue;
+                        }
                         float v = fmin2(a[q], b[r]);
+                        if (WIT) {
+                            if (v > acc[q][r]) { acc[q][r] = v; kidx[WIT ? q : 0][WIT ? r : 0] = (int32_t)y; }
+                            continue;
+                        }
                         if (EXCL) {
                             if (y == exr[q] || y == exc[r]) v = __int_as_float(0x7fc00000);
                         }
@@ -232,9 +278,17 @@ __global__ void __launch_bounds__(THREADS, MCPG_MM_MINB) maxmin_kernel(const Max
             const int64_t j = j0 + tx + 16 * r;
             if (j >= p.cols) continue;
             const float m = acc[q][r];
-            if (MODE == MM_PLAIN || MODE == MM_EXCL) {
+            if (MODE == MM_PLAIN || MODE == MM_EXCL || MODE == MM_GEMM) {
                 p.C[i * p.ldc + j] = m;
                 if (mirror) p.C[j * p.ldc + i] = m;
+            } else if (MODE == MM_WITNESS) {
+                const int32_t kw = kidx[WIT ? q : 0][WIT ? r : 0];
+                p.C[i * p.ldc + j] = m;
+                p.K[i * p.ldk + j] = kw;
+                if (mirror) {
+                    p.C[j * p.ldc + i] = m;
+                    p.K[j * p.ldk + i] = kw;
+                }
             } else if (MODE == MM_RATIO) {
                 p.R[i * p.ldr + j] = ratio_of(p.E[i * p.lde + j], m);
                 if (p.C) p.C[i * p.ldc + j] = m;
@@ -383,6 +437,46 @@ __global__ void dpi_tf_apply_kernel(const float* A, int64_t lda, const float* Ca
     }
 }
 
+__global__ void maxmin_route_kernel(const float* A, int64_t lda, const float* B, int64_t ldb, int64_t rows,
+                                    int64_t cols, int64_t k, const float* C, int64_t ldc, const float* dC,
+                                    int64_t lddc, const int32_t* K, int64_t ldk, float* dA, int64_t ldda, float* dB,
+                                    int64_t lddb) {
+    const int64_t total = rows * cols;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = t / cols, j = t - i * cols;
+        const float g = dC[i * lddc + j];
+        if (g == 0.0f) continue;
+        int64_t ks = -1;
+        if (K) {
+            ks = K[i * ldk + j];
+        } else {
+            const float c = C[i * ldc + j];
+            if (c > -INFINITY)
+                for (int64_t q = 0; q < k; ++q)
+                    if (fmin2(A[i * lda + q], B[j * ldb + q]) == c) {
+                        ks = q;
+                        break;
+                    }
+        }
+        if (ks < 0) continue;
+        const float a = A[i * lda + ks], b = B[j * ldb + ks];
+        if (a <= b) atomicAdd(dA + i * ldda + ks, g);  // std::min(a, b) returns a on a tie
+        else atomicAdd(dB + j * lddb + ks, g);
+    }
+}
+
+__global__ void ratio_bwd_kernel(const float* A, int64_t lda, const float* M, int64_t ldm, int64_t rows, int64_t cols,
+                                 const float* dR, int64_t lddr, float* dA, int64_t ldda, float* dM, int64_t lddm) {
+    const int64_t total = rows * cols;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = t / cols, j = t - i * cols;
+        const float a = A[i * lda + j], m = M[i * ldm + j], g = dR[i * lddr + j];
+        if (g == 0.0f || fabsf(a) < FLT_EPSILON || fabsf(m) < FLT_EPSILON) continue;
+        dA[i * ldda + j] += g / m;
+        dM[i * lddm + j] -= g * a / (m * m);
+    }
+}
+
 unsigned ew_blocks(int64_t total) {
     int64_t b = ceil_div(total, 256);
     if (b > 152 * 32) b = 152 * 32;
@@ -402,6 +496,9 @@ cudaError_t launch_maxmin(const MaxminParams& p, int mode, int symmetric, cudaSt
         case MM_CLOSURE: return s ? launch_one<MM_CLOSURE, true>(p, stream) : launch_one<MM_CLOSURE, false>(p, stream);
         case MM_DPI: return s ? launch_one<MM_DPI, true>(p, stream) : launch_one<MM_DPI, false>(p, stream);
         case MM_EXCL: return s ? launch_one<MM_EXCL, true>(p, stream) : launch_one<MM_EXCL, false>(p, stream);
+        case MM_WITNESS:
+            return s ? launch_one<MM_WITNESS, true>(p, stream) : launch_one<MM_WITNESS, false>(p, stream);
+        case MM_GEMM: return launch_one<MM_GEMM, false>(p, stream);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -455,6 +552,27 @@ cudaError_t launch_dpi_tf_apply(const float* A, int64_t lda, const float* Call, 
     if (launches) ++*launches;
     dpi_tf_apply_kernel<<<ew_blocks(n * n), 256, 0, stream>>>(A, lda, Call, ld1, Ctf, ld2, tf, n, tm, out, ldo, mask,
                                                              removed);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_maxmin_route(const float* A, int64_t lda, const float* B, int64_t ldb, int64_t rows, int64_t cols,
+                                int64_t k, const float* C, int64_t ldc, const float* dC, int64_t lddc,
+                                const int32_t* K, int64_t ldk, float* dA, int64_t ldda, float* dB, int64_t lddb,
+                                cudaStream_t stream, int64_t* launches) {
+    if (rows <= 0 || cols <= 0) return cudaSuccess;
+    if (launches) ++*launches;
+    maxmin_route_kernel<<<ew_blocks(rows * cols), 256, 0, stream>>>(A, lda, B, ldb, rows, cols, k, C, ldc, dC, lddc, K,
+                                                                   ldk, dA, ldda, dB, lddb);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ratio_bwd(const float* A, int64_t lda, const float* M, int64_t ldm, int64_t rows, int64_t cols,
+                             const float* dR, int64_t lddr, float* dA, int64_t ldda, float* dM, int64_t lddm,
+                             cudaStream_t stream, int64_t* launches) {
+    if (rows <= 0 || cols <= 0) return cudaSuccess;
+    if (launches) ++*launches;
+    ratio_bwd_kernel<<<ew_blocks(rows * cols), 256, 0, stream>>>(A, lda, M, ldm, rows, cols, dR, lddr, dA, ldda, dM,
+                                                                lddm);
     return cudaGetLastError();
 }
 

@@ -48,16 +48,30 @@ __device__ __forceinline__ void tri_tile(int64_t b, int64_t T, int64_t& ti, int6
     tj = r + (b - (r * T - r * (r - 1) / 2));
 }
 
-template <int BINS>
+// Adjoint epilogue arguments (EPI == 1): Q[(i - q_gene0) * BINS + a][j * BINS + b]
+// = Gs_ij (log2 P_ab + 1/ln 2) for P_ab > 0 (else 0), Gs_ij = G[i][j] + G[j][i]
+// for i != j and 0 on the diagonal; tiles cover A genes [16*q_tile0, ...) x all genes.
+struct QArgs {
+    const float* G; int64_t ldg;
+    float* Q; int64_t ldq;
+    int64_t q_tile0;
+};
+
+template <int BINS, int EPI>
 __global__ void __launch_bounds__(THREADS, 1)
     mi_fp32_kernel(const float* __restrict__ Wt, int64_t ldwt, const double* __restrict__ H, int64_t n,
-                   int64_t m_pad, float inv_m, float* __restrict__ MI, int64_t ldmi, int64_t T) {
+                   int64_t m_pad, float inv_m, float* __restrict__ MI, int64_t ldmi, int64_t T, const QArgs qa) {
     using C = MiCfg<BINS>;
     extern __shared__ float4 smem_f4[];
     float* smem = reinterpret_cast<float*>(smem_f4);
 
     int64_t ti, tj;
-    tri_tile(blockIdx.x, T, ti, tj);
+    if (EPI == 0) {
+        tri_tile(blockIdx.x, T, ti, tj);
+    } else {
+        ti = qa.q_tile0 + blockIdx.x / T;
+        tj = blockIdx.x % T;
+    }
     const int64_t gi0 = ti * G, gj0 = tj * G;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -126,6 +140,20 @@ __global__ void __launch_bounds__(THREADS, 1)
     cp_async_wait<0>();
 
     const int64_t i = gi0 + il, j = gj0 + jl;
+    if (EPI == 1) {
+        if (i >= n || j >= n) return;
+        const float gs = (i == j) ? 0.0f : qa.G[i * qa.ldg + j] + qa.G[j * qa.ldg + i];
+        const float c = 1.4426950408889634f;  // 1 / ln 2
+        float* Qr = qa.Q + (i - qa.q_tile0 * G) * BINS * qa.ldq + j * BINS;
+#pragma unroll
+        for (int x = 0; x < BINS; ++x)
+#pragma unroll
+            for (int y = 0; y < BINS; ++y) {
+                const float pv = acc[x][y] * inv_m;
+                Qr[x * qa.ldq + y] = (gs != 0.0f && pv > 0.0f) ? gs * (__log2f(pv) + c) : 0.0f;
+            }
+        return;
+    }
     if (i >= n || j >= n || j < i) return;
     double hxy = 0.0;
 #pragma unroll
@@ -147,18 +175,55 @@ template <int BINS>
 cudaError_t launch_bins(const float* Wt, int64_t ldwt, const double* H, int64_t n, int64_t m, float* MI, int64_t ldmi,
                         cudaStream_t stream) {
     using C = MiCfg<BINS>;
-    auto kern = mi_fp32_kernel<BINS>;
+    auto kern = mi_fp32_kernel<BINS, 0>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM);
     if (e != cudaSuccess) return e;
     const int64_t T = ceil_div(n, G);
     const int64_t tiles = T * (T + 1) / 2;
     const int64_t m_pad = ceil_div(m, BKS) * BKS;
     const float inv_m = 1.0f / (float)m;  // norm_factor = FT(1) / FT(m), BSplineMI.hpp:321
-    kern<<<(unsigned)tiles, THREADS, C::SMEM, stream>>>(Wt, ldwt, H, n, m_pad, inv_m, MI, ldmi, T);
+    kern<<<(unsigned)tiles, THREADS, C::SMEM, stream>>>(Wt, ldwt, H, n, m_pad, inv_m, MI, ldmi, T, QArgs{});
+    return cudaGetLastError();
+}
+
+template <int BINS>
+cudaError_t launch_q_bins(const float* Wt, int64_t ldwt, int64_t n, int64_t m, const QArgs& qa, int64_t tiles_a,
+                          cudaStream_t stream) {
+    using C = MiCfg<BINS>;
+    auto kern = mi_fp32_kernel<BINS, 1>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM);
+    if (e != cudaSuccess) return e;
+    const int64_t T = ceil_div(n, G);
+    const int64_t m_pad = ceil_div(m, BKS) * BKS;
+    const float inv_m = 1.0f / (float)m;
+    kern<<<(unsigned)(tiles_a * T), THREADS, C::SMEM, stream>>>(Wt, ldwt, nullptr, n, m_pad, inv_m, nullptr, 0, T,
+                                                                qa);
     return cudaGetLastError();
 }
 
 }  // namespace
+
+// Adjoint slab: Q for A genes [16*tile0, 16*(tile0 + tiles)) x all genes.
+cudaError_t launch_mi_q(const float* Wt, int64_t ldwt, const float* G, int64_t ldg, int64_t n, int64_t m, int bins,
+                        int64_t tile0, int64_t tiles, float* Q, int64_t ldq, cudaStream_t stream, int64_t* launches) {
+    if (n <= 0 || tiles <= 0) return cudaSuccess;
+    if (launches) ++*launches;
+    QArgs qa{G, ldg, Q, ldq, tile0};
+    switch (bins) {
+        case 2: return launch_q_bins<2>(Wt, ldwt, n, m, qa, tiles, stream);
+        case 3: return launch_q_bins<3>(Wt, ldwt, n, m, qa, tiles, stream);
+        case 4: return launch_q_bins<4>(Wt, ldwt, n, m, qa, tiles, stream);
+        case 5: return launch_q_bins<5>(Wt, ldwt, n, m, qa, tiles, stream);
+        case 6: return launch_q_bins<6>(Wt, ldwt, n, m, qa, tiles, stream);
+        case 7: return launch_q_bins<7>(Wt, ldwt, n, m, qa, tiles, stream);
+        case 8: return launch_q_bins<8>(Wt, ldwt, n, m, qa, tiles, stream);
+        case 9: return launch_q_bins<9>(Wt, ldwt, n, m, qa, tiles, stream);
+        case 10: return launch_q_bins<10>(Wt, ldwt, n, m, qa, tiles, stream);
+        case 11: return launch_q_bins<11>(Wt, ldwt, n, m, qa, tiles, stream);
+        case 12: return launch_q_bins<12>(Wt, ldwt, n, m, qa, tiles, stream);
+        default: return cudaErrorNotSupported;
+    }
+}
 
 // Wt must be zero-padded: ldwt >= ceil(n/16)*16*bins (multiple of 4), rows
 // s in [m, ceil(m/16)*16) zero.

@@ -317,6 +317,156 @@ int FN(orc_closure)(const REAL* A, int64_t n, int64_t lda, REAL* out, int64_t ld
     return changed ? -1 : it;
 }
 
+/* ================= adjoints (no reference routine; oracle of this build's
+ * definitions, restated in plain loops) =================
+ *
+ * B-spline basis derivative: d/dt N_{a,p}(t) = (p-1) [ N_{a,p-1}(t) / (t_{a+p-1} - t_a)
+ *   - N_{a+1,p-1}(t) / (t_{a+p} - t_{a+1}) ], a term dropped when its knot span
+ *   is below 1e-10 (the reference basis's own guard, BSplineMI.hpp:146-157). */
+static REAL FN(basis_deriv)(const REAL* kv, int bins, int a, int p, REAL t) {
+    if (p <= 1) return (REAL)0;
+    REAL d1 = kv[a + p - 1] - kv[a], d2 = kv[a + p] - kv[a + 1];
+    REAL r = 0;
+    if (!(d1 < 1e-10)) r += FN(basis)(kv, bins, a, p - 1, t) / d1;
+    if (!(d2 < 1e-10)) r -= FN(basis)(kv, bins, a + 1, p - 1, t) / d2;
+    return (REAL)(p - 1) * r;
+}
+
+/* Gradient of L with respect to the expression X, given G = dL/dMI (n x n,
+ * every ordered entry; the diagonal is ignored because the pipeline resets it).
+ * MI_ij = H_i + H_j - H_ij with p_ia = (1/m) sum_s w_ia(s),
+ * P_ab = (1/m) sum_s w_ia(s) w_jb(s), c = 1/ln 2:
+ *   dMI_ij/dw_ia(s) = (1/m) [ -(log2 p_ia + c) + sum_b (log2 P_ab + c) w_jb(s) ]
+ * (cells with p = 0 contribute 0), then w = N(t), t = (x - min)/(max - min)
+ * including the dependence of min and max (first arg-min / arg-max sample). */
+void FN(orc_mi_bwd)(const REAL* X, int64_t n, int64_t m, int64_t ldx, int bins, int order, const REAL* G,
+                    int64_t ldg, REAL* dX, int64_t lddx) {
+    const double c = 1.0 / log(2.0);
+    REAL kv[64];
+    FN(knots)(bins, order, kv);
+    const int64_t ldw = (int64_t)bins * m;
+    REAL* T = (REAL*)malloc(sizeof(REAL) * (size_t)(n * m));
+    REAL* W = (REAL*)malloc(sizeof(REAL) * (size_t)(n * ldw));
+    REAL* Hc = (REAL*)malloc(sizeof(REAL) * (size_t)(n * bins));
+    REAL* gsum = (REAL*)malloc(sizeof(REAL) * (size_t)n);
+#pragma omp parallel for schedule(static)
+    for (int64_t g = 0; g < n; ++g) {
+        FN(scale_row)(X + g * ldx, m, T + g * m);
+        for (int a = 0; a < bins; ++a) {
+            double p = 0;
+            for (int64_t s = 0; s < m; ++s) {
+                REAL w = FN(basis)(kv, bins, a, order, T[g * m + s]);
+                W[g * ldw + a * m + s] = w;
+                p += w;
+            }
+            p /= (double)m;
+            Hc[g * bins + a] = p > 0 ? (REAL)(log2(p) + c) : (REAL)0;
+        }
+        double gs = 0;
+        for (int64_t j = 0; j < n; ++j)
+            if (j != g) gs += (double)G[g * ldg + j] + (double)G[j * ldg + g];
+        gsum[g] = (REAL)gs;
+    }
+#pragma omp parallel
+    {
+        REAL* dW = (REAL*)malloc(sizeof(REAL) * (size_t)ldw);
+        REAL* Q = (REAL*)malloc(sizeof(REAL) * (size_t)(bins * bins));
+#pragma omp for schedule(dynamic, 1)
+        for (int64_t i = 0; i < n; ++i) {
+            const REAL* wi = W + i * ldw;
+            for (int a = 0; a < bins; ++a)
+                for (int64_t s = 0; s < m; ++s) dW[a * m + s] = -Hc[i * bins + a] * gsum[i];
+            for (int64_t j = 0; j < n; ++j) {
+                if (j == i) continue;
+                const REAL gs = G[i * ldg + j] + G[j * ldg + i];
+                if (gs == 0) continue;
+                const REAL* wj = W + j * ldw;
+                for (int a = 0; a < bins; ++a)
+                    for (int b = 0; b < bins; ++b) {
+                        double P = 0;
+                        for (int64_t s = 0; s < m; ++s) P += (double)wi[a * m + s] * wj[b * m + s];
+                        P /= (double)m;
+                        Q[a * bins + b] = P > 0 ? (REAL)(gs * (log2(P) + c)) : (REAL)0;
+                    }
+                for (int a = 0; a < bins; ++a)
+                    for (int b = 0; b < bins; ++b) {
+                        const REAL q = Q[a * bins + b];
+                        if (q == 0) continue;
+                        for (int64_t s = 0; s < m; ++s) dW[a * m + s] += q * wj[b * m + s];
+                    }
+            }
+            /* through the weights, the scaling and its min / max */
+            const REAL* x = X + i * ldx;
+            int64_t amin = 0, amax = 0;
+            for (int64_t s = 1; s < m; ++s) {
+                if (x[s] < x[amin]) amin = s;
+                if (x[amax] < x[s]) amax = s;
+            }
+            const REAL mn = x[amin], mx = x[amax];
+            const int ranged = mx > mn;
+            const REAL scale = ranged ? (REAL)(1.0 / (double)(mx - mn)) : (REAL)1;
+            double s1 = 0, s2 = 0;
+            for (int64_t s = 0; s < m; ++s) {
+                const REAL t = T[i * m + s];
+                double dt = 0;
+                for (int a = 0; a < bins; ++a) dt += (double)dW[a * m + s] * FN(basis_deriv)(kv, bins, a, order, t);
+                dt /= (double)m;
+                dX[i * lddx + s] = (REAL)(scale * dt);
+                s1 += dt * ((double)t - 1.0);
+                s2 += dt * (double)t;
+            }
+            if (ranged) {
+                dX[i * lddx + amin] += (REAL)(scale * s1);
+                dX[i * lddx + amax] -= (REAL)(scale * s2);
+            }
+        }
+        free(dW);
+        free(Q);
+    }
+    free(T); free(W); free(Hc); free(gsum);
+}
+
+/* Adjoint of C = A (x) B (C[i][j] = max_k min(A[i][k], B[j][k])): for every
+ * (i, j) with dC != 0, the witness k* is the first k with min(A[i][k], B[j][k])
+ * == C[i][j]; the gradient goes to A[i][k*] when A[i][k*] <= B[j][k*] (the
+ * operand std::min returns on a tie), else to B[j][k*].  Accumulates into dA,
+ * dB (which may alias when A and B are the same matrix).  Where C is -inf there
+ * is no witness (-1) and no gradient.  Sequential, so the sums are
+ * deterministic. */
+void FN(orc_maxmin_bwd)(const REAL* A, int64_t lda, const REAL* B, int64_t ldb, int64_t rows, int64_t cols,
+                        int64_t k, const REAL* Cm, int64_t ldc, const REAL* dC, int64_t lddc, REAL* dA, int64_t ldda,
+                        REAL* dB, int64_t lddb, int32_t* witness) {
+    for (int64_t i = 0; i < rows; ++i)
+        for (int64_t j = 0; j < cols; ++j) {
+            const REAL g = dC[i * lddc + j];
+            int64_t ks = -1;
+            /* no witness (and no gradient) where the product is -inf */
+            for (int64_t q = 0; q < k && Cm[i * ldc + j] > (REAL)(-DBL_MAX); ++q) {
+                REAL a = A[i * lda + q], b = B[j * ldb + q];
+                REAL mn = (b < a) ? b : a;
+                if (mn == Cm[i * ldc + j]) { ks = q; break; }
+            }
+            if (witness) witness[i * cols + j] = (int32_t)ks;
+            if (g == 0 || ks < 0) continue;
+            if (A[i * lda + ks] <= B[j * ldb + ks]) dA[i * ldda + ks] += g;
+            else dB[j * lddb + ks] += g;
+        }
+}
+
+/* Adjoint of R = ratio(A, M) (combine.hpp:210-222): where both |a| and |m| are
+ * at least epsilon, dA += dR / m and dM -= dR * a / m^2; elsewhere R is constant. */
+void FN(orc_ratio_bwd)(const REAL* A, int64_t lda, const REAL* M, int64_t ldm, int64_t rows, int64_t cols,
+                       const REAL* dR, int64_t lddr, REAL* dA, int64_t ldda, REAL* dM, int64_t lddm) {
+    const REAL eps = (sizeof(REAL) == 4) ? (REAL)FLT_EPSILON : (REAL)DBL_EPSILON;
+    for (int64_t i = 0; i < rows; ++i)
+        for (int64_t j = 0; j < cols; ++j) {
+            const REAL a = A[i * lda + j], mm = M[i * ldm + j], g = dR[i * lddr + j];
+            if (fabs((double)a) < eps || fabs((double)mm) < eps) continue;
+            dA[i * ldda + j] += g / mm;
+            dM[i * lddm + j] -= g * a / (mm * mm);
+        }
+}
+
 #undef FN
 #undef CAT
 #undef CAT2

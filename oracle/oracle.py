@@ -56,6 +56,16 @@ def _bind(L, sfx: str, prefix: str):
             continue
         f.restype = res
         f.argtypes = args
+    for name, res, args in (
+        ("mi_bwd", None, [_vp, _i64, _i64, _i64, C.c_int, C.c_int, _vp, _i64, _vp, _i64]),
+        ("maxmin_bwd", None, [_vp, _i64, _vp, _i64, _i64, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _i64,
+                              _vp]),
+        ("ratio_bwd", None, [_vp, _i64, _vp, _i64, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64]),
+    ):
+        f = getattr(L, f"{prefix}{name}_{sfx}", None)
+        if f is not None:
+            f.restype = res
+            f.argtypes = args
     f = getattr(L, f"{prefix}dpi_tf_{sfx}", None)
     if f is not None:
         f.restype = C.c_int64
@@ -191,6 +201,34 @@ class _Port(_TfCompositions):
         removed = getattr(self.L, f"orc_dpi_tf_{self._dt(A)}")(A.ctypes.data, n, n, tol, tfs.ctypes.data,
                                                                out.ctypes.data, n, mask.ctypes.data)
         return out, mask, int(removed)
+
+    # -- adjoints (this build's definitions; see mcp_oracle_impl.h) --
+    def mi_bwd(self, X, G, bins=10, order=3):
+        X = np.ascontiguousarray(X)
+        G = np.ascontiguousarray(G, dtype=X.dtype)
+        n, m = X.shape
+        dX = np.zeros_like(X)
+        getattr(self.L, f"orc_mi_bwd_{self._dt(X)}")(X.ctypes.data, n, m, m, bins, order, G.ctypes.data, n,
+                                                     dX.ctypes.data, m)
+        return dX
+
+    def maxmin_bwd(self, A, B, Cm, dC, dA, dB):
+        """Accumulates into dA, dB (may be the same array); returns the witnesses."""
+        A, B, Cm, dC = (np.ascontiguousarray(x) for x in (A, B, Cm, dC))
+        rows, k = A.shape
+        cols = B.shape[0]
+        K = np.empty((rows, cols), dtype=np.int32)
+        getattr(self.L, f"orc_maxmin_bwd_{self._dt(A)}")(A.ctypes.data, k, B.ctypes.data, k, rows, cols, k,
+                                                         Cm.ctypes.data, cols, dC.ctypes.data, cols, dA.ctypes.data,
+                                                         dA.shape[1], dB.ctypes.data, dB.shape[1], K.ctypes.data)
+        return K
+
+    def ratio_bwd(self, A, M, dR, dA, dM):
+        A, M, dR = (np.ascontiguousarray(x) for x in (A, M, dR))
+        rows, cols = A.shape
+        getattr(self.L, f"orc_ratio_bwd_{self._dt(A)}")(A.ctypes.data, cols, M.ctypes.data, cols, rows, cols,
+                                                        dR.ctypes.data, cols, dA.ctypes.data, cols, dM.ctypes.data,
+                                                        cols)
 
     def closure(self, A, max_iter=64):
         A = np.ascontiguousarray(A)
