@@ -171,6 +171,8 @@ class Handle:
         return int(self._L.mcpg_kernel_launches(self._h))
 
     def set_stream(self, stream_ptr: int):
+        """Run this handle's work on an existing CUDA stream (e.g. torch's current
+        stream, so *_dev calls are ordered with torch operations)."""
         self._check(self._L.mcpg_set_stream(self._h, stream_ptr), "set_stream")
 
     def synchronize(self):
@@ -371,6 +373,7 @@ class Handle:
         """Forward only: L = sum_e coef[e] * R[rows_idx[e], cols_idx[e]] (FP64 sum of the FP32 scores)."""
         import torch
         n, m = X.shape
+        self.set_stream(torch.cuda.current_stream(X.device).cuda_stream)  # order with the torch ops below
         f32 = dict(dtype=torch.float32, device=X.device)
         A = torch.empty((n, n), **f32)
         self.bspline_mi_dev(X, A, bins, order, precision)
@@ -390,6 +393,7 @@ class Handle:
         import torch
         n, m = X.shape
         dev = X.device
+        self.set_stream(torch.cuda.current_stream(dev).cuda_stream)  # order with the torch ops below
         f32 = dict(dtype=torch.float32, device=dev)
         if witness == "auto":
             free, _ = torch.cuda.mem_get_info(dev)

@@ -40,7 +40,11 @@ def built_lib():
 
 @pytest.fixture(scope="session")
 def gpu(built_lib):
-    """A library handle on cuda:0; the GPU tests fail (not skip) without one."""
+    """A library handle on cuda:0 on torch's current stream (so tests that mix
+    torch tensors with *_dev calls are ordered); GPU tests fail (not skip)
+    without a GPU."""
     h = built_lib.Handle(0)
+    import torch
+    h.set_stream(torch.cuda.current_stream().cuda_stream)
     yield h
     h.close()
