@@ -16,12 +16,14 @@
 // D = 128 x 240 FP32 in tensor memory (256 columns allocated).
 //   warp 0 / one lane : TMA producer (cp.async.bulk.tensor, 128B swizzle, 64-sample slices)
 //   warp 1 / one lane : tcgen05.mma issuer (kind::f16, M=128, N=240, K=16)
-//   warps 0-3         : epilogue -- tcgen05.ld one row per thread, p*log2(p)
+//   warps 2-5         : epilogue -- tcgen05.ld one row per thread, p*log2(p)
 //                       per (row, B gene) in FP32, cross-bin sums and
 //                       H_i + H_j - H_ij in FP64, symmetric store.
-// Two pipeline stages of 64 samples (92 KB each with the split) are double
-// buffered through mbarriers.  Only gene-tile pairs that contain some j >= i
-// run; tiles are visited in groups of GI A-tiles so that the A and B tiles in
+// Persistent CTAs (one per SM) walk the tile list; a ring of 64-sample stages
+// (2 x 92 KB with the split, 4 x 46 KB without) feeds the MMAs through
+// mbarriers, and two TMEM accumulators let the epilogue of one tile overlap the
+// main loop of the next.  Only gene-tile pairs that contain some j >= i run;
+// tiles are visited in groups of GI A-tiles so that the A and B tiles in
 // flight stay resident in L2.
 //
 // Every mbarrier wait is bounded (2 s of %globaltimer): on expiry the kernel
@@ -43,8 +45,6 @@ constexpr int GBN = 24;                // genes per B tile
 constexpr int MROWS = 128;             // MMA M
 constexpr int NCOLS = GBN * BINS;      // MMA N = 240
 constexpr int BK = 64;                 // samples per stage (128 bytes of 16-bit)
-constexpr int STAGES = 2;
-constexpr int THREADS = 128;
 constexpr int TMEM_COLS = 256;
 constexpr int GI = 8;                  // A tiles per rasterization group
 constexpr uint32_t A_BYTES = MROWS * BK * 2;   // 16 KB
@@ -173,29 +173,61 @@ __device__ __forceinline__ int j_min_for(int I) {
     return v <= 0 ? 0 : (v + 23) / 24;
 }
 
-template <bool SPLIT>
-__global__ void __launch_bounds__(THREADS, 1)
+// Bounded wait that also gives up as soon as another role raised the CTA's
+// abort flag (so one timeout does not cascade into a long chain of timeouts).
+__device__ __forceinline__ bool mbar_wait_abortable(uint32_t bar, uint32_t parity, int* err, volatile int* abort_flag) {
+    if (mbar_try(bar, parity)) return true;
+    const unsigned long long t0 = gtimer();
+    for (;;) {
+        for (int i = 0; i < 64; ++i)
+            if (mbar_try(bar, parity)) return true;
+        if (*abort_flag) return false;
+        if (gtimer() - t0 > WAIT_NS) {
+            atomicExch(err, 1);
+            *abort_flag = 1;
+            return false;
+        }
+    }
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+// Linear tile index -> (I, J): groups of GI A tiles, B tiles outer within a
+// group.  Returns false for rectangle slots outside the upper triangle.
+__device__ __forceinline__ bool tile_of(int64_t L, const TcArgs& a, int& I, int& J) {
+    const int64_t per_group = (int64_t)GI * a.TJ;
+    const int g = (int)(L / per_group);
+    const int r = (int)(L - (int64_t)g * per_group);
+    J = r / GI;
+    I = g * GI + (r - J * GI);
+    return I < a.TI && J >= j_min_for(I);
+}
+
+// Persistent, warp-specialised CTA (one per SM):
+//   warp 0 (one lane)  TMA producer over a STAGES-deep ring of 64-sample slices
+//   warp 1 (one lane)  tcgen05.mma issuer; warp 1 also owns the TMEM allocation
+//   warps 2-5          epilogue, 128 threads = 128 accumulator rows
+// Two TMEM accumulators (2 x 256 columns) let the epilogue of tile t overlap the
+// main loop of tile t+1.
+template <bool SPLIT, int STAGES>
+__global__ void __launch_bounds__(192, 1)
     mi_tc_kernel(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CUtensorMap map_lo,
                  const __grid_constant__ CUtensorMap mapb_hi, const __grid_constant__ CUtensorMap mapb_lo,
-                 const TcArgs args) {
-    // ---- tile of this CTA: grouped rasterization over the TI x TJ rectangle ----
-    const int64_t b = (int64_t)blockIdx.x;
-    const int64_t per_group = (int64_t)GI * args.TJ;
-    const int g = (int)(b / per_group);
-    const int r = (int)(b - (int64_t)g * per_group);
-    const int J = r / GI;
-    const int I = g * GI + (r - J * GI);
-    if (I >= args.TI || J < j_min_for(I)) return;
-
+                 const TcArgs args, const int64_t n_slots) {
     extern __shared__ uint8_t smem_raw[];
     const uint32_t raw = smem_u32(smem_raw);
     const uint32_t base = (raw + 1023u) & ~1023u;
     uint8_t* gbase = smem_raw + (base - raw);
     constexpr uint32_t STAGE_BYTES = (SPLIT ? 2 : 1) * (A_BYTES + B_BYTES);
-    // layout per stage: A_hi, B_hi, [A_lo, B_lo]
-    const uint32_t bar_base = base + STAGES * STAGE_BYTES;  // full[S], empty[S], done
-    const uint32_t full0 = bar_base, empty0 = bar_base + 8 * STAGES, done = bar_base + 16 * STAGES;
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(gbase + STAGES * STAGE_BYTES + 16 * STAGES + 16);
+    constexpr uint32_t PART_BYTES = MROWS * PSTRIDE * 4;
+    float* part = reinterpret_cast<float*>(gbase + STAGES * STAGE_BYTES);
+    const uint32_t bars = base + STAGES * STAGE_BYTES + PART_BYTES;
+    const uint32_t full0 = bars, empty0 = bars + 8 * STAGES;
+    const uint32_t tfull0 = bars + 16 * STAGES, tempty0 = tfull0 + 16;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(gbase + STAGES * STAGE_BYTES + PART_BYTES + 16 * STAGES + 32);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (tid == 0) {
@@ -203,119 +235,157 @@ __global__ void __launch_bounds__(THREADS, 1)
             mbar_init(full0 + 8 * s, 1);
             mbar_init(empty0 + 8 * s, 1);
         }
-        mbar_init(done, 1);
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(tfull0 + 8 * b, 1);
+            mbar_init(tempty0 + 8 * b, 4);
+        }
+        *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
-    if (warp == 0) tmem_alloc(smem_u32(tmem_slot), TMEM_COLS);
+    if (warp == 1) tmem_alloc(smem_u32(tmem_slot), 2 * TMEM_COLS);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(tmem_slot);
-
-    const int rowA = I * GA * BINS;
-    const int rowB = J * GBN * BINS;
     const int KT = args.ktiles;
 
-    if (warp == 0 && lane == 0) {
-        // ---------------- TMA producer ----------------
-        bool ok = true;
-        for (int kt = 0; kt < KT && ok; ++kt) {
-            const int s = kt % STAGES;
-            const int u = kt / STAGES;
-            if (u > 0) ok = mbar_wait(empty0 + 8 * s, (u - 1) & 1, args.err);
-            if (!ok) break;
-            const uint32_t st = base + s * STAGE_BYTES;
-            mbar_expect_tx(full0 + 8 * s, STAGE_BYTES);
-            tma_load_2d(st, &map_hi, kt * BK, rowA, full0 + 8 * s);
-            tma_load_2d(st + A_BYTES, &mapb_hi, kt * BK, rowB, full0 + 8 * s);
-            if (SPLIT) {
-                tma_load_2d(st + A_BYTES + B_BYTES, &map_lo, kt * BK, rowA, full0 + 8 * s);
-                tma_load_2d(st + 2 * A_BYTES + B_BYTES, &mapb_lo, kt * BK, rowB, full0 + 8 * s);
-            }
-        }
-        // drain: the last phase issued on each stage must complete before smem goes away
-        for (int s = 0; s < STAGES && s < KT; ++s) {
-            const int last = ((KT - 1 - s) / STAGES);
-            mbar_wait(full0 + 8 * s, last & 1, args.err);
-        }
-    } else if (warp == 1 && lane == 0) {
-        // ---------------- MMA issuer ----------------
-        bool ok = true;
-        for (int kt = 0; kt < KT && ok; ++kt) {
-            const int s = kt % STAGES;
-            ok = mbar_wait(full0 + 8 * s, (kt / STAGES) & 1, args.err);
-            if (!ok) break;
-            tc_fence_after();
-            const uint32_t st = base + s * STAGE_BYTES;
-#pragma unroll
-            for (int k = 0; k < BK / 16; ++k) {
-                const uint64_t ahi = sdesc_sw128(st + 32 * k);
-                const uint64_t bhi = sdesc_sw128(st + A_BYTES + 32 * k);
-                const uint32_t acc0 = (kt > 0 || k > 0) ? 1u : 0u;
-                mma_f16(tmem, ahi, bhi, args.idesc, acc0);
-                if (SPLIT) {
-                    const uint64_t alo = sdesc_sw128(st + A_BYTES + B_BYTES + 32 * k);
-                    const uint64_t blo = sdesc_sw128(st + 2 * A_BYTES + B_BYTES + 32 * k);
-                    mma_f16(tmem, ahi, blo, args.idesc, 1u);
-                    mma_f16(tmem, alo, bhi, args.idesc, 1u);
+    if (warp == 0) {
+        if (lane == 0) {
+            // ---------------- TMA producer ----------------
+            int64_t g = 0;  // running k-slice counter across this CTA's tiles
+            bool ok = true;
+            for (int64_t L = blockIdx.x; L < n_slots && ok; L += gridDim.x) {
+                int I, J;
+                if (!tile_of(L, args, I, J)) continue;
+                const int rowA = I * GA * BINS, rowB = J * GBN * BINS;
+                for (int kt = 0; kt < KT; ++kt, ++g) {
+                    const int s = (int)(g % STAGES);
+                    const int64_t u = g / STAGES;
+                    if (u > 0 && !(ok = mbar_wait_abortable(empty0 + 8 * s, (uint32_t)((u - 1) & 1), args.err,
+                                                            abort_flag)))
+                        break;
+                    const uint32_t st = base + s * STAGE_BYTES;
+                    mbar_expect_tx(full0 + 8 * s, STAGE_BYTES);
+                    tma_load_2d(st, &map_hi, kt * BK, rowA, full0 + 8 * s);
+                    tma_load_2d(st + A_BYTES, &mapb_hi, kt * BK, rowB, full0 + 8 * s);
+                    if (SPLIT) {
+                        tma_load_2d(st + A_BYTES + B_BYTES, &map_lo, kt * BK, rowA, full0 + 8 * s);
+                        tma_load_2d(st + 2 * A_BYTES + B_BYTES, &mapb_lo, kt * BK, rowB, full0 + 8 * s);
+                    }
                 }
             }
-            mma_commit(empty0 + 8 * s);  // frees the stage once these MMAs have read it
-        }
-        mma_commit(done);  // accumulator complete (or, after an abort, nothing in flight)
-    }
-    __syncwarp();
-
-    // ---------------- epilogue (all 4 warps) ----------------
-    const bool got = mbar_wait(done, 0, args.err);
-    tc_fence_after();
-    float* part = reinterpret_cast<float*>(gbase);  // reuse stage buffers: 128 x PSTRIDE floats
-    // CTA-uniform, so the .sync.aligned tensor-memory loads below never diverge;
-    // also: every thread is past its last smem-stage access
-    const bool have = __syncthreads_and(got) != 0;
-    if (have) {
-        float acc[GBN];
-#pragma unroll
-        for (int q = 0; q < GBN; ++q) acc[q] = 0.0f;
-        const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
-#pragma unroll
-        for (int c = 0; c < NCOLS / 16; ++c) {
-            float v[16];
-            tmem_ld16(trow + c * 16, v);
-            if (args.dbg && I == 0 && J == 0) {
-#pragma unroll
-                for (int e = 0; e < 16; ++e) args.dbg[tid * NCOLS + c * 16 + e] = v[e];
-            }
-#pragma unroll
-            for (int e = 0; e < 16; ++e) {
-                const int col = c * 16 + e;
-                const float p = v[e] * args.inv_m;
-                const float t = (p > 0.0f) ? p * __log2f(p) : 0.0f;
-                acc[col / BINS] += t;
+            // drain: the last phase issued on each stage lands before the CTA exits
+            for (int s = 0; s < STAGES && (int64_t)s < g; ++s) {
+                const int64_t last = (g - 1 - s) / STAGES;
+                mbar_wait_abortable(full0 + 8 * s, (uint32_t)(last & 1), args.err, abort_flag);
             }
         }
+        __syncwarp();
+    } else if (warp == 1) {
+        if (lane == 0) {
+            // ---------------- MMA issuer ----------------
+            int64_t g = 0, t = 0;
+            bool ok = true;
+            for (int64_t L = blockIdx.x; L < n_slots && ok; L += gridDim.x) {
+                int I, J;
+                if (!tile_of(L, args, I, J)) continue;
+                const int ab = (int)(t & 1);
+                const int64_t ua = t >> 1;
+                if (ua > 0 &&
+                    !(ok = mbar_wait_abortable(tempty0 + 8 * ab, (uint32_t)((ua - 1) & 1), args.err, abort_flag)))
+                    break;
+                tc_fence_after();
+                const uint32_t dacc = tmem + (uint32_t)(ab * TMEM_COLS);
+                for (int kt = 0; kt < KT; ++kt, ++g) {
+                    const int s = (int)(g % STAGES);
+                    if (!(ok = mbar_wait_abortable(full0 + 8 * s, (uint32_t)((g / STAGES) & 1), args.err,
+                                                   abort_flag)))
+                        break;
+                    tc_fence_after();
+                    const uint32_t st = base + s * STAGE_BYTES;
 #pragma unroll
-        for (int q = 0; q < GBN; ++q) part[tid * PSTRIDE + q] = acc[q];
+                    for (int k = 0; k < BK / 16; ++k) {
+                        const uint64_t ahi = sdesc_sw128(st + 32 * k);
+                        const uint64_t bhi = sdesc_sw128(st + A_BYTES + 32 * k);
+                        mma_f16(dacc, ahi, bhi, args.idesc, (kt > 0 || k > 0) ? 1u : 0u);
+                        if (SPLIT) {
+                            const uint64_t alo = sdesc_sw128(st + A_BYTES + B_BYTES + 32 * k);
+                            const uint64_t blo = sdesc_sw128(st + 2 * A_BYTES + B_BYTES + 32 * k);
+                            mma_f16(dacc, ahi, blo, args.idesc, 1u);
+                            mma_f16(dacc, alo, bhi, args.idesc, 1u);
+                        }
+                    }
+                    mma_commit(empty0 + 8 * s);  // frees the stage once these MMAs have read it
+                }
+                if (!ok) break;
+                mma_commit(tfull0 + 8 * ab);  // accumulator ab complete
+                ++t;
+            }
+        }
+        __syncwarp();
+    } else {
+        // ---------------- epilogue: warps 2..5, 128 rows ----------------
+        const int row = ((warp & 3) << 5) + lane;  // TMEM lane quarter of this warp
+        const int etid = tid - 64;                  // 0..127
+        int64_t t = 0;
+        for (int64_t L = blockIdx.x; L < n_slots; L += gridDim.x) {
+            int I, J;
+            if (!tile_of(L, args, I, J)) continue;
+            const int ab = (int)(t & 1);
+            const bool got = mbar_wait_abortable(tfull0 + 8 * ab, (uint32_t)((t >> 1) & 1), args.err, abort_flag);
+            tc_fence_after();
+            // uniform across the 128 epilogue threads (.sync.aligned loads below)
+            asm volatile("bar.sync 1, 128;" ::: "memory");
+            if (!got || *abort_flag) break;
+            float acc[GBN];
+#pragma unroll
+            for (int q = 0; q < GBN; ++q) acc[q] = 0.0f;
+            const uint32_t trow = tmem + (uint32_t)(ab * TMEM_COLS) + ((uint32_t)((warp & 3) * 32) << 16);
+#pragma unroll
+            for (int c = 0; c < NCOLS / 16; ++c) {
+                float v[16];
+                tmem_ld16(trow + c * 16, v);
+                if (args.dbg && I == 0 && J == 0) {
+#pragma unroll
+                    for (int e = 0; e < 16; ++e) args.dbg[row * NCOLS + c * 16 + e] = v[e];
+                }
+#pragma unroll
+                for (int e = 0; e < 16; ++e) {
+                    const int col = c * 16 + e;
+                    const float p = v[e] * args.inv_m;
+                    const float tt = (p > 0.0f) ? p * __log2f(p) : 0.0f;
+                    acc[col / BINS] += tt;
+                }
+            }
+            // accumulator ab may be overwritten from here on
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(tempty0 + 8 * ab);
+#pragma unroll
+            for (int q = 0; q < GBN; ++q) part[row * PSTRIDE + q] = acc[q];
+            asm volatile("bar.sync 1, 128;" ::: "memory");
+            const int64_t gi0 = (int64_t)I * GA, gj0 = (int64_t)J * GBN;
+            for (int p = etid; p < GA * GBN; p += 128) {
+                const int il = p / GBN, jl = p - il * GBN;
+                const int64_t i = gi0 + il, j = gj0 + jl;
+                if (i >= args.n || j >= args.n || j < i) continue;
+                double sum = 0.0;
+#pragma unroll
+                for (int a = 0; a < BINS; ++a) sum += (double)part[(il * BINS + a) * PSTRIDE + jl];
+                const float val = (float)(args.H[i] + args.H[j] + sum);  // sum = -H_ij
+                args.MI[i * args.ldmi + j] = val;
+                args.MI[j * args.ldmi + i] = val;
+            }
+            ++t;
+        }
     }
     tc_fence_before();
     __syncthreads();
-    if (have) {
-        const int64_t gi0 = (int64_t)I * GA, gj0 = (int64_t)J * GBN;
-        for (int p = tid; p < GA * GBN; p += THREADS) {
-            const int il = p / GBN, jl = p - il * GBN;
-            const int64_t i = gi0 + il, j = gj0 + jl;
-            if (i >= args.n || j >= args.n || j < i) continue;
-            double s = 0.0;
-#pragma unroll
-            for (int a = 0; a < BINS; ++a) s += (double)part[(il * BINS + a) * PSTRIDE + jl];
-            const float v = (float)(args.H[i] + args.H[j] + s);  // s = -H_ij
-            args.MI[i * args.ldmi + j] = v;
-            args.MI[j * args.ldmi + i] = v;
-        }
+    if (warp == 1) {
+        tc_fence_after();
+        tmem_dealloc(tmem, 2 * TMEM_COLS);
     }
-    __syncthreads();
-    if (warp == 0) tmem_dealloc(tmem, TMEM_COLS);
 }
 
 // ---------------------------------------------------------------- host side
@@ -389,19 +459,23 @@ cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, int64_t ldw, 
     a.err = timeout_flag;
     a.dbg = g_tc_debug_dump;
     const int groups = (a.TI + GI - 1) / GI;
-    const int64_t grid = (int64_t)groups * GI * a.TJ;
+    const int64_t n_slots = (int64_t)groups * GI * a.TJ;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t grid = n_slots < sms ? n_slots : sms;
     const uint32_t stage_bytes = (split ? 2u : 1u) * (A_BYTES + B_BYTES);
-    const size_t smem = 1024 + STAGES * stage_bytes + 16 * STAGES + 16 + 16;
+    const int stages = split ? 2 : 4;
+    const size_t smem = 1024 + stages * stage_bytes + MROWS * PSTRIDE * 4 + 16 * stages + 32 + 16;
     cudaError_t e;
     if (launches) ++*launches;
     if (split) {
-        e = cudaFuncSetAttribute(mi_tc_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        e = cudaFuncSetAttribute(mi_tc_kernel<true, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        mi_tc_kernel<true><<<(unsigned)grid, THREADS, smem, stream>>>(ma_hi, ma_lo, mb_hi, mb_lo, a);
+        mi_tc_kernel<true, 2><<<(unsigned)grid, 192, smem, stream>>>(ma_hi, ma_lo, mb_hi, mb_lo, a, n_slots);
     } else {
-        e = cudaFuncSetAttribute(mi_tc_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        e = cudaFuncSetAttribute(mi_tc_kernel<false, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        mi_tc_kernel<false><<<(unsigned)grid, THREADS, smem, stream>>>(ma_hi, ma_lo, mb_hi, mb_lo, a);
+        mi_tc_kernel<false, 4><<<(unsigned)grid, 192, smem, stream>>>(ma_hi, ma_lo, mb_hi, mb_lo, a, n_slots);
     }
     return cudaGetLastError();
 }
