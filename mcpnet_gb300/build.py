@@ -23,6 +23,8 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIBDIR = PKG / "_lib"
 LIB = LIBDIR / "libmcpgpu.so"
+APPS = PKG / "apps"
+CLI = LIBDIR / "mcpgpu_cli"
 INCLUDE = ROOT / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -88,6 +90,15 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed\n{r.stdout}\n{r.stderr}")
+    cli_src = APPS / "mcpgpu_cli.cpp"
+    if cli_src.exists() and (force or _stale(CLI, [cli_src, LIB, *_headers()])):
+        cmd = ["g++", "-O2", "-std=c++17", f"-I{INCLUDE}", str(cli_src), "-o", str(CLI), f"-L{LIBDIR}", "-lmcpgpu",
+               "-Wl,-rpath,$ORIGIN"]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"CLI build failed\n{r.stdout}\n{r.stderr}")
     return LIB
 
 
