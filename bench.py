@@ -383,6 +383,123 @@ def gpu_arm(args, ws, rank, local):
         print(json.dumps(line), flush=True)
 
 
+def pipeline_arm(args, ws, rank, local):
+    """The whole MCPNet compute core once, stage by stage (the large single-GPU
+    configuration: 32,768 genes x 4,096 samples by default): B-spline MI
+    (tensor cores), diagonal reset, the three max-min products with the
+    MCP2/3/4 ratios fused (M1 shared), the DPI filter and optionally the
+    max-capacity closure.  Prints one JSON line with per-stage times and
+    roofline fractions, and the reference CPU path's time on the host cores
+    extrapolated from timed row slabs."""
+    import torch
+    import mcpnet_gb300 as M
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    n, m, b = args.genes, args.samples, args.bins
+    X = torch.from_numpy(M.synth_grn(n, m, seed=args.seed)).to(dev)
+    h = M.Handle(local)
+    stream = torch.cuda.current_stream(dev)
+    h.set_stream(stream.cuda_stream)
+    f32 = dict(dtype=torch.float32, device=dev)
+    A = torch.empty((n, n), **f32)
+    R2, R3, R4, D = (torch.empty((n, n), **f32) for _ in range(4))
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    fmax = float(peaks.get("sm_max_mhz", 2070.0)) * 1e6
+    tc_peak = float(peaks.get("bf16_tflops", 1900.0)) * 1e12
+    hbm = float(peaks.get("hbm_gbs", 6800.0)) * 1e9
+    alu_peak = sms * 128 * fmax
+
+    def timed(fn):
+        a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        e.record(stream)
+        e.synchronize()
+        return a.elapsed_time(e) / 1e3
+
+    # warm-up on a small problem (module load, workspace)
+    Xs = X[:256].contiguous()
+    As = torch.empty((256, 256), **f32)
+    h.bspline_mi_dev(Xs, As, b, args.order, args.precision)
+    h.set_diagonal_dev(As, 0.0)
+    h.maxmins_dev(As, R2=torch.empty_like(As))
+    torch.cuda.synchronize(dev)
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    h.profile(True)
+    st = {}
+    t_all0 = time.perf_counter()
+    st["mi"] = timed(lambda: h.bspline_mi_dev(X, A, b, args.order, args.precision))
+    st["diagonal"] = timed(lambda: h.set_diagonal_dev(A, 0.0))
+    st["mcp234"] = timed(lambda: h.maxmins_dev(A, R2=R2, R3=R3, R4=R4))
+    removed = [0]
+    st["dpi"] = timed(lambda: removed.__setitem__(0, h.dpi_dev(A, D, 0.1)))
+    iters = None
+    if args.closure:
+        Cl = torch.empty((n, n), **f32)
+        it = [0]
+        st["closure"] = timed(lambda: it.__setitem__(0, h.closure_dev(A, Cl, 64)))
+        iters = it[0]
+        del Cl
+    wall = time.perf_counter() - t_all0
+    prof = h.profile_report()
+    h.profile(False)
+    clk = clocks.stop()
+
+    pairs = n * (n - 1) // 2
+    mi_flops = 2.0 * b * b * m * pairs
+    w_ms = prof.get("bspline_weights16", {}).get("ms", float("nan"))
+    tc_ms = prof.get("mi_tc", {}).get("ms", float("nan"))
+    ldw = -(-m // 64) * 64
+    w_bytes = n * m * 4 + 2 * n * b * ldw * 2
+    mm = prof.get("maxmin", {"launches": 0, "ms": float("nan")})
+    # executed min/max work: M1 and M3 symmetric (n^3 / 2), M2 full (n^3), DPI symmetric (n^3 / 2)
+    mm_ops_exec = 2.0 * (0.5 + 1.0 + 0.5) * n ** 3
+    stages = {
+        "bspline_weights": {"ms": w_ms, "GB/s": w_bytes / (w_ms / 1e3) / 1e9, "frac_hbm": w_bytes / (w_ms / 1e3) / hbm},
+        "mi_tc": {"ms": tc_ms, "TFLOP/s_algorithmic": mi_flops / (tc_ms / 1e3) / 1e12,
+                  "frac_tensor_algorithmic": mi_flops / (tc_ms / 1e3) / tc_peak,
+                  "frac_tensor_issued": 3.0 * mi_flops * (128 / 120) / (tc_ms / 1e3) / tc_peak
+                  if args.precision.endswith("x3") else None},
+        "maxmin_M1_M2_M3": {"ms": mm["ms"], "launches": mm["launches"],
+                            "Gop/s_executed": mm_ops_exec / (mm["ms"] / 1e3) / 1e9,
+                            "frac_alu_peak": mm_ops_exec / (mm["ms"] / 1e3) / alu_peak},
+    }
+    dpi_ms = st["dpi"] * 1e3
+    stages["dpi"] = {"ms": dpi_ms, "removed": removed[0],
+                     "frac_alu_peak": 2.0 * 0.5 * n ** 3 / (dpi_ms / 1e3) / alu_peak}
+    line = {"mode": "pipeline", "genes": n, "samples": m, "precision": args.precision,
+            "stage_s": st, "wall_s": wall, "stages": stages, "closure_iterations": iters, "clocks": clk,
+            "kernel_profile": prof, "sms": sms}
+    if not args.no_cpu:
+        sampler = CpuMiSampler(min(n, args.cpu_genes), m, args.seed)
+        v, info = sampler.run(args.cpu_seconds / 2)
+        from oracle import oracle as O
+        P = O.port()
+        Ah = A.cpu().numpy()
+        t0 = time.perf_counter()
+        P.maxmin(Ah[:1], Ah)
+        per_row = max(time.perf_counter() - t0, 1e-4)
+        rows = int(max(1, min(n, (args.cpu_seconds / 2) / per_row)))
+        t0 = time.perf_counter()
+        P.maxmin(Ah[:rows], Ah)
+        mm_row_s = (time.perf_counter() - t0) / rows
+        cpu_mi_s = pairs / v
+        cpu_mm_s = mm_row_s * n * (0.5 + 1.0 + 0.5 + 0.5)  # M1, M2, M3 as the reference's SYMM patterns + DPI bound
+        line["cpu_baseline"] = {"kind": sampler.kind, "cores": info["threads"],
+                                "mi_s_extrapolated": cpu_mi_s, "maxmin_dpi_s_extrapolated": cpu_mm_s,
+                                "total_s_extrapolated": cpu_mi_s + cpu_mm_s,
+                                "sample": f"MI {sampler.describe(info)}; max-min rows 0..{rows} x {n} x {n} "
+                                          f"({mm_row_s:.3f} s/row); DPI counted as one symmetric product "
+                                          "(an upper bound: the reference's DPI scan exits early)"}
+    h.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -404,7 +521,14 @@ def main(argv=None):
     ap.add_argument("--no-maxmin", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--pipeline", action="store_true",
+                    help="run the whole compute core once, stage by stage (defaults to 32768 x 4096)")
+    ap.add_argument("--closure", action="store_true", help="with --pipeline: add the max-capacity closure")
+    ap.add_argument("--cpu-genes", type=int, default=8192,
+                    help="with --pipeline: genes of the CPU MI sample (its weights are built on the host)")
     args = ap.parse_args(argv)
+    if args.pipeline and "--genes" not in (argv or sys.argv):
+        args.genes, args.samples = 32768, 4096
     if args.warmup < 3:
         args.warmup = 3  # timing rule: at least 3 warm-up steps
     ws, rank, local = dist_env()
@@ -414,6 +538,8 @@ def main(argv=None):
     try:
         if args.impl == "reference":
             reference_arm(args, ws, rank)
+        elif args.pipeline:
+            pipeline_arm(args, ws, rank, local)
         else:
             gpu_arm(args, ws, rank, local)
     finally:

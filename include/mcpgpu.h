@@ -137,6 +137,16 @@ MCPG_API int mcpg_mcp(mcpg_handle* h, const float* A, int64_t n, int64_t lda, in
 MCPG_API int mcpg_mcp_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, int path_len, int symmetrize,
                           float* maxmin_out, int64_t ldm, float* ratio_out, int64_t ldr);
 
+/* ---- the three max-min products at once (compute_maxmins, mcpnet_helper.hpp:437-460) ----
+ * M1 = A (x) A, M2 = A (x) M1, M3 = M1 (x) M1 with M1 computed once, and the
+ * MCP2 / MCP3 / MCP4 scores R2 = ratio(A, M1), R3 = ratio(A, M2),
+ * R4 = ratio(A, M3) fused into the products.  Every output is nullable (M1 is
+ * kept in scratch when not requested); a product whose outputs are all null
+ * is skipped. */
+MCPG_API int mcpg_maxmins_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, float* M1, int64_t ld1,
+                              float* M2, int64_t ld2, float* M3, int64_t ld3, float* R2, int64_t ldr2, float* R3,
+                              int64_t ldr3, float* R4, int64_t ldr4);
+
 /* ---- DPI filter ----
  * dpi_kernel<float> (include/mcp/filter/dpi.hpp:42-69) over all (x, z), then
  * mask<float,true> (include/mcp/filter/threshold.hpp:33-54), as apps/filter/dpi.cpp:236-287.

@@ -58,6 +58,7 @@ ABI = [
     ("mcpg_set_diagonal_dev", C.c_int, [_vp, _vp, _i64, _i64, _i64, C.c_float]),
     ("mcpg_mcp", C.c_int, [_vp, _vp, _i64, _i64, C.c_int, C.c_int, _vp, _i64, _vp, _i64]),
     ("mcpg_mcp_dev", C.c_int, [_vp, _vp, _i64, _i64, C.c_int, C.c_int, _vp, _i64, _vp, _i64]),
+    ("mcpg_maxmins_dev", C.c_int, [_vp, _vp, _i64, _i64] + [_vp, _i64] * 6),
     ("mcpg_dpi", C.c_int, [_vp, _vp, _i64, _i64, C.c_float, _vp, _i64, _vp, C.POINTER(C.c_int64)]),
     ("mcpg_dpi_dev", C.c_int, [_vp, _vp, _i64, _i64, C.c_float, _vp, _i64, _vp, C.POINTER(C.c_int64)]),
     ("mcpg_closure", C.c_int, [_vp, _vp, _i64, _i64, C.c_int, _vp, _i64, C.POINTER(C.c_int)]),
@@ -436,6 +437,14 @@ class Handle:
         self._check(self._L.mcpg_mcp_dev(self._h, self._dp(A), n, self._ld(A), path_len, int(symmetrize),
                                           self._dp(M), self._ld(M) if M is not None else n,
                                           self._dp(R), self._ld(R) if R is not None else n), "mcp_dev")
+
+    def maxmins_dev(self, A, M1=None, M2=None, M3=None, R2=None, R3=None, R4=None):
+        """compute_maxmins with the MCP2/3/4 ratios fused (torch CUDA tensors, all optional)."""
+        n = A.shape[0]
+        args = []
+        for t in (M1, M2, M3, R2, R3, R4):
+            args += [self._dp(t), self._ld(t) if t is not None else n]
+        self._check(self._L.mcpg_maxmins_dev(self._h, self._dp(A), n, self._ld(A), *args), "maxmins_dev")
 
     def dpi_dev(self, A, out, tol=0.1, mask=None):
         n = A.shape[0]

@@ -825,6 +825,60 @@ int mi_bwd_dev(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_t ldx
     return MCPG_OK;
 }
 
+
+// compute_maxmins (mcpnet_helper.hpp:437-460): M1 = A (x) A, M2 = A (x) M1,
+// M3 = M1 (x) M1 with M1 computed once, plus the MCP2/3/4 ratios ratio(A, Mk)
+// fused into the products' epilogues.  Every output is nullable; M1 lives in
+// scratch when not requested.
+int maxmins_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, float* M1, int64_t ld1, float* M2,
+                int64_t ld2, float* M3, int64_t ld3, float* R2, int64_t ldr2, float* R3, int64_t ldr3, float* R4,
+                int64_t ldr4) {
+    if (n < 0) return fail(h, MCPG_ERR_ARG, "maxmins: negative size");
+    if (n == 0) return MCPG_OK;
+    if (!A) return fail(h, MCPG_ERR_ARG, "maxmins: null input");
+    if (lda < n || (M1 && ld1 < n) || (M2 && ld2 < n) || (M3 && ld3 < n) || (R2 && ldr2 < n) || (R3 && ldr3 < n) ||
+        (R4 && ldr4 < n))
+        return fail(h, MCPG_ERR_ARG, "maxmins: leading dimension too small");
+    const float* a;
+    int64_t la;
+    int rc = aligned_view(h, A, lda, n, n, S_IN0, &a, &la);
+    if (rc) return rc;
+    float* m1 = M1;
+    int64_t l1 = ld1;
+    if (!m1 || (l1 % 4) != 0 || ((uintptr_t)m1 & 15u)) {
+        void* p;
+        l1 = round_up(n, 32);
+        if ((rc = scratch(h, S_M1, (size_t)(n * l1) * sizeof(float), &p))) return rc;
+        m1 = (float*)p;
+    }
+    mcpg::MaxminParams p{};
+    p.rows = n; p.cols = n; p.k_len = n;
+    p.A = a; p.lda = la; p.B = a; p.ldb = la; p.C = m1; p.ldc = l1; p.E = a; p.lde = la; p.R = R2; p.ldr = ldr2;
+    {
+        PROF(h, "maxmin");
+        CK(h, mcpg::launch_maxmin(p, R2 ? mcpg::MM_RATIO : mcpg::MM_PLAIN, 1, h->stream, &h->launches),
+           "maxmin kernel (M1)");
+    }
+    if (M2 || R3) {
+        mcpg::MaxminParams q{};
+        q.rows = n; q.cols = n; q.k_len = n;
+        q.A = a; q.lda = la; q.B = m1; q.ldb = l1; q.C = M2; q.ldc = ld2; q.E = a; q.lde = la; q.R = R3; q.ldr = ldr3;
+        PROF(h, "maxmin");
+        CK(h, mcpg::launch_maxmin(q, R3 ? mcpg::MM_RATIO : mcpg::MM_PLAIN, 0, h->stream, &h->launches),
+           "maxmin kernel (M2)");
+    }
+    if (M3 || R4) {
+        mcpg::MaxminParams q{};
+        q.rows = n; q.cols = n; q.k_len = n;
+        q.A = m1; q.lda = l1; q.B = m1; q.ldb = l1; q.C = M3; q.ldc = ld3; q.E = a; q.lde = la; q.R = R4; q.ldr = ldr4;
+        PROF(h, "maxmin");
+        CK(h, mcpg::launch_maxmin(q, R4 ? mcpg::MM_RATIO : mcpg::MM_PLAIN, 1, h->stream, &h->launches),
+           "maxmin kernel (M3)");
+    }
+    if (M1 && m1 != M1) CK(h, mcpg::launch_copy2d(m1, l1, M1, ld1, n, n, h->stream), "copy2d");
+    return MCPG_OK;
+}
+
 }  // namespace
 
 // =====================================================================
@@ -1383,6 +1437,15 @@ int mcpg_bspline_mi_bwd(mcpg_handle* h, const float* X, int64_t n, int64_t m, in
     if ((rc = mi_bwd_dev(h, dXin, n, m, lx, bins, order, dG, lg, dOut, lo))) return rc;
     if ((rc = copy_out(h, dX, lddx, dOut, lo, n, m))) return rc;
     return finish(h);
+}
+
+
+int mcpg_maxmins_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, float* M1, int64_t ld1, float* M2,
+                     int64_t ld2, float* M3, int64_t ld3, float* R2, int64_t ldr2, float* R3, int64_t ldr3, float* R4,
+                     int64_t ldr4) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    return maxmins_dev(h, A, n, lda, M1, ld1, M2, ld2, M3, ld3, R2, ldr2, R3, ldr3, R4, ldr4);
 }
 
 }  // extern "C"

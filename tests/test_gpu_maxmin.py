@@ -110,3 +110,25 @@ def test_injected_allocation_failure_is_reported(built_lib):
         assert np.array_equal(h.maxmin(np.ones((8, 8), np.float32)), np.ones((8, 8), np.float32))
     finally:
         h.close()
+
+
+@pytest.mark.parametrize("n", [3, 130, 257])
+def test_maxmins_shared_m1_matches_oracle(gpu, port, n):
+    import torch
+    rng = np.random.default_rng(300 + n)
+    A = rng.random((n, n)).astype(np.float32)
+    A = np.maximum(A, A.T)
+    np.fill_diagonal(A, 0)
+    Ad = torch.from_numpy(A).cuda()
+    outs = [torch.empty((n, n), device="cuda") for _ in range(6)]
+    gpu.maxmins_dev(Ad, *outs)
+    gpu.synchronize()
+    M1, M2, M3, R2, R3, R4 = (o.cpu().numpy() for o in outs)
+    for pl, M, R in ((2, M1, R2), (3, M2, R3), (4, M3, R4)):
+        Mo, Ro = port.mcp(A, pl)
+        assert np.array_equal(bits(M), bits(Mo)) and np.array_equal(bits(R), bits(Ro)), pl
+    # ratios only (M1 in scratch)
+    R3b = torch.empty((n, n), device="cuda")
+    gpu.maxmins_dev(Ad, R3=R3b)
+    gpu.synchronize()
+    assert np.array_equal(bits(R3b.cpu().numpy()), bits(port.mcp(A, 3)[1]))
