@@ -455,8 +455,8 @@ def pipeline_arm(args, ws, rank, local):
     tc_ms = prof.get("mi_tc", {}).get("ms", float("nan"))
     ldw = -(-m // 64) * 64
     w_bytes = n * m * 4 + 2 * n * b * ldw * 2
-    mm = prof.get("maxmin", {"launches": 0, "ms": float("nan")})
-    # executed min/max work: M1 and M3 symmetric (n^3 / 2), M2 full (n^3), DPI symmetric (n^3 / 2)
+    mm_ms = st["mcp234"] * 1e3
+    # executed min/max work: M1 and M3 symmetric (n^3 / 2 triples each), M2 full (n^3)
     mm_ops_exec = 2.0 * (0.5 + 1.0 + 0.5) * n ** 3
     stages = {
         "bspline_weights": {"ms": w_ms, "GB/s": w_bytes / (w_ms / 1e3) / 1e9, "frac_hbm": w_bytes / (w_ms / 1e3) / hbm},
@@ -464,13 +464,16 @@ def pipeline_arm(args, ws, rank, local):
                   "frac_tensor_algorithmic": mi_flops / (tc_ms / 1e3) / tc_peak,
                   "frac_tensor_issued": 3.0 * mi_flops * (128 / 120) / (tc_ms / 1e3) / tc_peak
                   if args.precision.endswith("x3") else None},
-        "maxmin_M1_M2_M3": {"ms": mm["ms"], "launches": mm["launches"],
-                            "Gop/s_executed": mm_ops_exec / (mm["ms"] / 1e3) / 1e9,
-                            "frac_alu_peak": mm_ops_exec / (mm["ms"] / 1e3) / alu_peak},
+        "maxmin_M1_M2_M3_with_ratios": {"ms": mm_ms, "Gop/s_executed": mm_ops_exec / (mm_ms / 1e3) / 1e9,
+                                        "frac_alu_peak": mm_ops_exec / (mm_ms / 1e3) / alu_peak},
     }
     dpi_ms = st["dpi"] * 1e3
     stages["dpi"] = {"ms": dpi_ms, "removed": removed[0],
                      "frac_alu_peak": 2.0 * 0.5 * n ** 3 / (dpi_ms / 1e3) / alu_peak}
+    if args.closure:
+        cl_ms = st["closure"] * 1e3
+        stages["closure"] = {"ms": cl_ms, "iterations": iters,
+                             "frac_alu_peak": 2.0 * 0.5 * n ** 3 * iters / (cl_ms / 1e3) / alu_peak}
     line = {"mode": "pipeline", "genes": n, "samples": m, "precision": args.precision,
             "stage_s": st, "wall_s": wall, "stages": stages, "closure_iterations": iters, "clocks": clk,
             "kernel_profile": prof, "sms": sms}

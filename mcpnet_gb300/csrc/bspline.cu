@@ -22,6 +22,8 @@
 #include <cuda_fp16.h>
 #include <math.h>
 
+#include <cmath>
+
 #include "common.cuh"
 #include "internal.h"
 
@@ -33,6 +35,13 @@ constexpr int WTHREADS = 256;
 
 struct Knots {
     float v[KNOTS_MAX];
+    // When every nonzero knot span is a power of two (10 bins / order 3: spans
+    // of 1/8 and 1/4), n / span == n * (1 / span) exactly, so the recursion's
+    // divisions become multiplications by these exact reciprocals without
+    // changing a bit.  r1[p][i] = 1 / (t[i+p-1] - t[i]), r2[p][i] = 1 / (t[i+p] - t[i+1]).
+    int pow2;
+    float r1[KMAX_ORDER + 1][KNOTS_MAX];
+    float r2[KMAX_ORDER + 1][KNOTS_MAX];
 };
 
 enum OutKind { OUT_REF = 0, OUT_T32 = 1, OUT_BF16 = 2, OUT_FP16 = 3 };
@@ -46,6 +55,27 @@ void host_knots(int bins, int order, Knots& k) {
     for (int i = 0; i < order; ++i) k.v[i] = 0.0f;
     for (int i = order; i < order + nint; ++i) k.v[i] = (float)((double)(float)(i - order + 1) * nf);
     for (int i = order + nint; i < 2 * order + nint; ++i) k.v[i] = 1.0f;
+    // exact reciprocals of the knot spans, when they are all powers of two
+    k.pow2 = 1;
+    for (int p = 0; p <= KMAX_ORDER; ++p)
+        for (int i = 0; i < KNOTS_MAX; ++i) k.r1[p][i] = k.r2[p][i] = 0.0f;
+    auto pow2_or_zero = [](float d) {
+        if (!(d >= 1e-10f)) return true;
+        int e = 0;
+        return std::frexp(d, &e) == 0.5f;
+    };
+    for (int p = 2; p <= order; ++p)
+        for (int i = 0; i + p < KNOTS_MAX && i < bins + order - p; ++i) {
+            const float d1 = k.v[i + p - 1] - k.v[i], d2 = k.v[i + p] - k.v[i + 1];
+            if (!pow2_or_zero(d1) || !pow2_or_zero(d2)) k.pow2 = 0;
+            k.r1[p][i] = d1 >= 1e-10f ? 1.0f / d1 : 0.0f;
+            k.r2[p][i] = d2 >= 1e-10f ? 1.0f / d2 : 0.0f;
+        }
+}
+
+// n / d for a knot span d: an exact multiplication when the spans are powers of two.
+__device__ __forceinline__ float span_div(const Knots& kv, float n, float d, float rinv) {
+    return kv.pow2 ? __fmul_rn(n, rinv) : __fdiv_rn(n, d);
 }
 
 // All bins' basis values at t, bottom-up.  N[i] holds basis(i, p, t) for the
@@ -92,13 +122,13 @@ __device__ __forceinline__ void basis_all(const Knots& kv, int bins_rt, int orde
                 float e1, e2;
                 if (d1 < 1e-10) {
                     e1 = 0.0f;
-                    e2 = __fmul_rn(__fdiv_rn(n2v, d2), N[i + 1]);
+                    e2 = __fmul_rn(span_div(kv, n2v, d2, kv.r2[p][i]), N[i + 1]);
                 } else if (d2 < 1e-10) {
                     e2 = 0.0f;
-                    e1 = __fmul_rn(__fdiv_rn(n1v, d1), N[i]);
+                    e1 = __fmul_rn(span_div(kv, n1v, d1, kv.r1[p][i]), N[i]);
                 } else {
-                    e1 = __fmul_rn(__fdiv_rn(n1v, d1), N[i]);
-                    e2 = __fmul_rn(__fdiv_rn(n2v, d2), N[i + 1]);
+                    e1 = __fmul_rn(span_div(kv, n1v, d1, kv.r1[p][i]), N[i]);
+                    e2 = __fmul_rn(span_div(kv, n2v, d2, kv.r2[p][i]), N[i + 1]);
                 }
                 const float s = __fadd_rn(e1, e2);
                 r = (s < 0.0f) ? 0.0f : s;
