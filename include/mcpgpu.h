@@ -147,6 +147,16 @@ MCPG_API int mcpg_maxmins_dev(mcpg_handle* h, const float* A, int64_t n, int64_t
                               float* M2, int64_t ld2, float* M3, int64_t ld3, float* R2, int64_t ldr2, float* R3,
                               int64_t ldr3, float* R4, int64_t ldr4);
 
+/* ---- ensemble combination (compute_combo, mcpnet_helper.hpp:507-573) ----
+ * out = mi / (c0 mi + c1 M1 + c2 M2 + c3 M3), the combination summed in
+ * double in that order (a term skipped when its coefficient is 0, added
+ * unscaled when it is 1), |mi| < FLT_EPSILON -> 0, |combination| <
+ * FLT_EPSILON -> FLT_MAX, else the double quotient rounded to float.
+ * coeffs: 4 doubles on the host; Mk may be null when ck == 0. */
+MCPG_API int mcpg_combo_dev(mcpg_handle* h, const float* mi, int64_t ldm, const float* M1, int64_t ld1,
+                            const float* M2, int64_t ld2, const float* M3, int64_t ld3, int64_t rows, int64_t cols,
+                            const double* coeffs, float* out, int64_t ldo);
+
 /* ---- DPI filter ----
  * dpi_kernel<float> (include/mcp/filter/dpi.hpp:42-69) over all (x, z), then
  * mask<float,true> (include/mcp/filter/threshold.hpp:33-54), as apps/filter/dpi.cpp:236-287.

@@ -58,6 +58,7 @@ ABI = [
     ("mcpg_set_diagonal_dev", C.c_int, [_vp, _vp, _i64, _i64, _i64, C.c_float]),
     ("mcpg_mcp", C.c_int, [_vp, _vp, _i64, _i64, C.c_int, C.c_int, _vp, _i64, _vp, _i64]),
     ("mcpg_mcp_dev", C.c_int, [_vp, _vp, _i64, _i64, C.c_int, C.c_int, _vp, _i64, _vp, _i64]),
+    ("mcpg_combo_dev", C.c_int, [_vp, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _i64, _i64, _vp, _vp, _i64]),
     ("mcpg_maxmins_dev", C.c_int, [_vp, _vp, _i64, _i64] + [_vp, _i64] * 6),
     ("mcpg_dpi", C.c_int, [_vp, _vp, _i64, _i64, C.c_float, _vp, _i64, _vp, C.POINTER(C.c_int64)]),
     ("mcpg_dpi_dev", C.c_int, [_vp, _vp, _i64, _i64, C.c_float, _vp, _i64, _vp, C.POINTER(C.c_int64)]),
@@ -445,6 +446,15 @@ class Handle:
         for t in (M1, M2, M3, R2, R3, R4):
             args += [self._dp(t), self._ld(t) if t is not None else n]
         self._check(self._L.mcpg_maxmins_dev(self._h, self._dp(A), n, self._ld(A), *args), "maxmins_dev")
+
+    def combo_dev(self, mi, M1, M2, M3, coeffs, out):
+        """compute_combo: out = mi / (c0 mi + c1 M1 + c2 M2 + c3 M3) (torch CUDA tensors; Mk may be None when ck == 0)."""
+        cs = np.ascontiguousarray(coeffs, dtype=np.float64)
+        rows, cols = mi.shape
+        ld = lambda t: self._ld(t) if t is not None else cols
+        self._check(self._L.mcpg_combo_dev(self._h, self._dp(mi), self._ld(mi), self._dp(M1), ld(M1), self._dp(M2),
+                                            ld(M2), self._dp(M3), ld(M3), rows, cols, cs.ctypes.data, self._dp(out),
+                                            self._ld(out)), "combo_dev")
 
     def dpi_dev(self, A, out, tol=0.1, mask=None):
         n = A.shape[0]

@@ -168,21 +168,26 @@ int check_handle(mcpg_handle* h) {
 // ---------------- staging helpers for the host entry points ----------------
 int stage_in(mcpg_handle* h, int slot, const float* src, int64_t ld_src, int64_t rows, int64_t cols, float** dev,
              int64_t* ld_dev) {
-    const int64_t ld = round_up(cols > 0 ? cols : 1, 32);  // 128-byte rows
+    const int64_t ld = round_up(cols > 0 ? cols : 1, 4);  // 16-byte rows for the vectorised kernels
     void* p;
     int rc = scratch(h, slot, (size_t)(rows * ld) * sizeof(float), &p);
     if (rc) return rc;
-    if (rows > 0 && cols > 0)
-        CK(h, cudaMemcpy2DAsync(p, ld * sizeof(float), src, ld_src * sizeof(float), cols * sizeof(float), rows,
-                                cudaMemcpyHostToDevice, h->stream),
-           "host-to-device copy");
+    if (rows > 0 && cols > 0) {
+        if (ld == cols && ld_src == cols)  // contiguous on both sides: one linear copy
+            CK(h, cudaMemcpyAsync(p, src, (size_t)(rows * cols) * sizeof(float), cudaMemcpyHostToDevice, h->stream),
+               "host-to-device copy");
+        else
+            CK(h, cudaMemcpy2DAsync(p, ld * sizeof(float), src, ld_src * sizeof(float), cols * sizeof(float), rows,
+                                    cudaMemcpyHostToDevice, h->stream),
+               "host-to-device copy");
+    }
     *dev = (float*)p;
     *ld_dev = ld;
     return MCPG_OK;
 }
 
 int stage_out_alloc(mcpg_handle* h, int slot, int64_t rows, int64_t cols, float** dev, int64_t* ld_dev) {
-    const int64_t ld = round_up(cols > 0 ? cols : 1, 32);
+    const int64_t ld = round_up(cols > 0 ? cols : 1, 4);
     void* p;
     int rc = scratch(h, slot, (size_t)(rows * ld) * sizeof(float), &p);
     if (rc) return rc;
@@ -194,9 +199,13 @@ int stage_out_alloc(mcpg_handle* h, int slot, int64_t rows, int64_t cols, float*
 int copy_out(mcpg_handle* h, float* dst, int64_t ld_dst, const float* src, int64_t ld_src, int64_t rows,
              int64_t cols) {
     if (!dst || rows <= 0 || cols <= 0) return MCPG_OK;
-    CK(h, cudaMemcpy2DAsync(dst, ld_dst * sizeof(float), src, ld_src * sizeof(float), cols * sizeof(float), rows,
-                            cudaMemcpyDeviceToHost, h->stream),
-       "device-to-host copy");
+    if (ld_dst == cols && ld_src == cols)
+        CK(h, cudaMemcpyAsync(dst, src, (size_t)(rows * cols) * sizeof(float), cudaMemcpyDeviceToHost, h->stream),
+           "device-to-host copy");
+    else
+        CK(h, cudaMemcpy2DAsync(dst, ld_dst * sizeof(float), src, ld_src * sizeof(float), cols * sizeof(float), rows,
+                                cudaMemcpyDeviceToHost, h->stream),
+           "device-to-host copy");
     return MCPG_OK;
 }
 
@@ -1446,6 +1455,26 @@ int mcpg_maxmins_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, flo
     int rc = check_handle(h);
     if (rc) return rc;
     return maxmins_dev(h, A, n, lda, M1, ld1, M2, ld2, M3, ld3, R2, ldr2, R3, ldr3, R4, ldr4);
+}
+
+
+int mcpg_combo_dev(mcpg_handle* h, const float* mi, int64_t ldm, const float* M1, int64_t ld1, const float* M2,
+                   int64_t ld2, const float* M3, int64_t ld3, int64_t rows, int64_t cols, const double* coeffs,
+                   float* out, int64_t ldo) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (rows < 0 || cols < 0) return fail(h, MCPG_ERR_ARG, "combo: negative size");
+    if (rows == 0 || cols == 0) return MCPG_OK;
+    if (!mi || !out || !coeffs) return fail(h, MCPG_ERR_ARG, "combo: null pointer");
+    if ((coeffs[1] != 0.0 && !M1) || (coeffs[2] != 0.0 && !M2) || (coeffs[3] != 0.0 && !M3))
+        return fail(h, MCPG_ERR_ARG, "combo: a matrix with a nonzero coefficient is null");
+    if (ldm < cols || ldo < cols || (M1 && ld1 < cols) || (M2 && ld2 < cols) || (M3 && ld3 < cols))
+        return fail(h, MCPG_ERR_ARG, "combo: leading dimension too small");
+    PROF(h, "combo");
+    CK(h, mcpg::launch_combo(mi, ldm, M1, ld1, M2, ld2, M3, ld3, rows, cols, coeffs, out, ldo, h->stream,
+                             &h->launches),
+       "combo kernel");
+    return MCPG_OK;
 }
 
 }  // extern "C"

@@ -141,6 +141,19 @@ __device__ __forceinline__ void basis_all(const Knots& kv, int bins_rt, int orde
         if (a < bins) out[a] = N[a];
 }
 
+// Per-thread bin sums in FP32 with Neumaier compensation (sum + carry): the FP64
+// pipe of this part is far slower than FP32, and the compensated pair keeps
+// the per-thread partial to about 2^-48 relative before the FP64 block reduction.
+struct CompSum {
+    float s = 0.0f, c = 0.0f;
+    __device__ __forceinline__ void add(float v) {
+        const float t = __fadd_rn(s, v);
+        c = __fadd_rn(c, (fabsf(s) >= fabsf(v)) ? __fadd_rn(__fsub_rn(s, t), v) : __fadd_rn(__fsub_rn(v, t), s));
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+};
+
 template <typename T>
 __device__ __forceinline__ T block_reduce(T v, T (*op)(T, T), T* scratch) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -181,9 +194,7 @@ __global__ void __launch_bounds__(WTHREADS) bspline_weights_kernel(const float* 
     const float scale = (mx > mn) ? (float)(1.0 / (double)__fsub_rn(mx, mn)) : 1.0f;
     const float offset = (mx > mn) ? mn : 0.0f;
 
-    double acc[NB];
-#pragma unroll
-    for (int a = 0; a < NB; ++a) acc[a] = 0.0;
+    CompSum acc[NB];
 
     float w[NB];
     for (int64_t s = threadIdx.x; s < m; s += blockDim.x) {
@@ -191,7 +202,7 @@ __global__ void __launch_bounds__(WTHREADS) bspline_weights_kernel(const float* 
         basis_all<BT, OT>(kv, bins_rt, order_rt, t, w);
 #pragma unroll
         for (int a = 0; a < NB; ++a)
-            if (a < bins) acc[a] += (double)w[a];
+            if (a < bins) acc[a].add(w[a]);
         if (OUT == OUT_REF) {
             float* W = static_cast<float*>(out0) + g * ((int64_t)bins * m + 1);
             for (int a = 0; a < bins; ++a) W[(int64_t)a * m + s] = w[a];
@@ -228,7 +239,7 @@ __global__ void __launch_bounds__(WTHREADS) bspline_weights_kernel(const float* 
 #pragma unroll
     for (int a = 0; a < NB; ++a) {
         if (a >= bins) break;
-        double v = acc[a];
+        double v = acc[a].value();
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
         if (lane == 0) psum[a][warp] = v;
@@ -313,20 +324,18 @@ __global__ void __launch_bounds__(WTHREADS) mi_bwd_x_kernel(const float* __restr
 
     // marginals p_a -> log2 p_a + 1/ln 2
     float w[NB], prev[NB + 1];
-    double acc[NB];
-#pragma unroll
-    for (int a = 0; a < NB; ++a) acc[a] = 0.0;
+    CompSum acc[NB];
     for (int64_t s = threadIdx.x; s < m; s += blockDim.x) {
         const float t = __fmul_rn(scale, __fsub_rn(x[s], offset));
         basis_all<BT, OT>(kv, bins_rt, order_rt, t, w);
 #pragma unroll
         for (int a = 0; a < NB; ++a)
-            if (a < bins) acc[a] += (double)w[a];
+            if (a < bins) acc[a].add(w[a]);
     }
 #pragma unroll
     for (int a = 0; a < NB; ++a) {
         if (a >= bins) break;
-        double v = acc[a];
+        double v = acc[a].value();
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
         if (lane == 0) psum[a][warp] = v;

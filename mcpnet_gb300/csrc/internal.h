@@ -69,6 +69,11 @@ cudaError_t launch_maxmin_route(const float* A, int64_t lda, const float* B, int
 cudaError_t launch_ratio_bwd(const float* A, int64_t lda, const float* M, int64_t ldm, int64_t rows, int64_t cols,
                              const float* dR, int64_t lddr, float* dA, int64_t ldda, float* dM, int64_t lddm,
                              cudaStream_t stream, int64_t* launches);
+// compute_combo: out = mi / (cs0 mi + cs1 M1 + cs2 M2 + cs3 M3) in double with the
+// ratio's epsilon guards; Mk may be null when csk == 0 (cs: host, 4 values).
+cudaError_t launch_combo(const float* mi, int64_t ldm, const float* M1, int64_t ld1, const float* M2, int64_t ld2,
+                         const float* M3, int64_t ld3, int64_t rows, int64_t cols, const double* cs, float* out,
+                         int64_t ldo, cudaStream_t stream, int64_t* launches);
 // Copies a rows x cols matrix between arbitrary leading dimensions (device to device).
 cudaError_t launch_copy2d(const float* src, int64_t lds, float* dst, int64_t ldd, int64_t rows, int64_t cols,
                           cudaStream_t stream);

@@ -477,6 +477,30 @@ __global__ void ratio_bwd_kernel(const float* A, int64_t lda, const float* M, in
     }
 }
 
+// compute_combo (mcpnet_helper.hpp:507-573), in double with the reference's
+// summation order; explicit _rn intrinsics keep nvcc from fusing the
+// multiply-adds, so the result matches the reference built without FMA.
+__global__ void combo_kernel(const float* mi, int64_t ldm, const float* M1, int64_t ld1, const float* M2, int64_t ld2,
+                             const float* M3, int64_t ld3, int64_t rows, int64_t cols, double a, double b, double c,
+                             double d, float* out, int64_t ldo) {
+    const int64_t total = rows * cols;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = t / cols, j = t - i * cols;
+        const float v = mi[i * ldm + j];
+        double mm = 0.0;
+        if (a == 1.0) mm = __dadd_rn(mm, (double)v); else if (a != 0.0) mm = __dadd_rn(mm, __dmul_rn(a, (double)v));
+        if (b == 1.0) mm = __dadd_rn(mm, (double)M1[i * ld1 + j]);
+        else if (b != 0.0) mm = __dadd_rn(mm, __dmul_rn(b, (double)M1[i * ld1 + j]));
+        if (c == 1.0) mm = __dadd_rn(mm, (double)M2[i * ld2 + j]);
+        else if (c != 0.0) mm = __dadd_rn(mm, __dmul_rn(c, (double)M2[i * ld2 + j]));
+        if (d == 1.0) mm = __dadd_rn(mm, (double)M3[i * ld3 + j]);
+        else if (d != 0.0) mm = __dadd_rn(mm, __dmul_rn(d, (double)M3[i * ld3 + j]));
+        out[i * ldo + j] = (fabsf(v) < FLT_EPSILON) ? 0.0f
+                         : (fabs(mm) < (double)FLT_EPSILON) ? FLT_MAX
+                         : __double2float_rn(__ddiv_rn((double)v, mm));
+    }
+}
+
 unsigned ew_blocks(int64_t total) {
     int64_t b = ceil_div(total, 256);
     if (b > 152 * 32) b = 152 * 32;
@@ -573,6 +597,16 @@ cudaError_t launch_ratio_bwd(const float* A, int64_t lda, const float* M, int64_
     if (launches) ++*launches;
     ratio_bwd_kernel<<<ew_blocks(rows * cols), 256, 0, stream>>>(A, lda, M, ldm, rows, cols, dR, lddr, dA, ldda, dM,
                                                                 lddm);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_combo(const float* mi, int64_t ldm, const float* M1, int64_t ld1, const float* M2, int64_t ld2,
+                         const float* M3, int64_t ld3, int64_t rows, int64_t cols, const double* cs, float* out,
+                         int64_t ldo, cudaStream_t stream, int64_t* launches) {
+    if (rows <= 0 || cols <= 0) return cudaSuccess;
+    if (launches) ++*launches;
+    combo_kernel<<<ew_blocks(rows * cols), 256, 0, stream>>>(mi, ldm, M1, ld1, M2, ld2, M3, ld3, rows, cols, cs[0],
+                                                            cs[1], cs[2], cs[3], out, ldo);
     return cudaGetLastError();
 }
 

@@ -216,6 +216,31 @@ void FN(orc_ratio)(const REAL* A, int64_t lda, const REAL* M, int64_t ldm, int64
         }
 }
 
+/* compute_combo -- apps/pipeline/mcpnet_helper.hpp:507-573: the ensemble
+ * score mi / (a mi + b M1 + c M2 + d M3), the combination summed in double in
+ * that order (a term skipped when its coefficient is 0, added unscaled when it
+ * is 1), with ratio_kernel's epsilon guards.  M1..M3 may be NULL when their
+ * coefficient is 0. */
+void FN(orc_combo)(const REAL* mi, const REAL* M1, const REAL* M2, const REAL* M3, int64_t rows, int64_t cols,
+                   int64_t ld, const double* cs, REAL* out, int64_t ldo) {
+    const REAL eps = (sizeof(REAL) == 4) ? (REAL)FLT_EPSILON : (REAL)DBL_EPSILON;
+    const REAL big = (sizeof(REAL) == 4) ? (REAL)FLT_MAX : (REAL)DBL_MAX;
+    const double a = cs[0], b = cs[1], c = cs[2], d = cs[3];
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < rows; ++i)
+        for (int64_t j = 0; j < cols; ++j) {
+            const int64_t o = i * ld + j;
+            double mm = 0.0;
+            if (a == 1.0) mm += mi[o]; else if (a != 0.0) mm += a * mi[o];
+            if (b == 1.0) mm += M1[o]; else if (b != 0.0) mm += b * M1[o];
+            if (c == 1.0) mm += M2[o]; else if (c != 0.0) mm += c * M2[o];
+            if (d == 1.0) mm += M3[o]; else if (d != 0.0) mm += d * M3[o];
+            out[i * ldo + j] = (fabs((double)mi[o]) < eps) ? (REAL)0
+                             : (fabs(mm) < eps) ? big
+                             : (REAL)((double)mi[o] / mm);
+        }
+}
+
 /* max_kernel over (M, M^T) -- combine.hpp:42-58 as used by apps/filter/mcp.cpp:463-476 */
 void FN(orc_max_transpose)(const REAL* M, int64_t n, int64_t ldm, REAL* out, int64_t ldo) {
 #pragma omp parallel for schedule(static)

@@ -170,6 +170,19 @@ class _Port(_TfCompositions):
         getattr(self.L, f"orc_max_transpose_{self._dt(M)}")(M.ctypes.data, n, n, out.ctypes.data, n)
         return out
 
+    def combo(self, mi, M1, M2, M3, cs):
+        mi = np.ascontiguousarray(mi)
+        rows, cols = mi.shape
+        cs = np.ascontiguousarray(cs, dtype=np.float64)
+        ptr = lambda x: None if x is None else np.ascontiguousarray(x, dtype=mi.dtype).ctypes.data
+        keep = [None if x is None else np.ascontiguousarray(x, dtype=mi.dtype) for x in (M1, M2, M3)]
+        out = np.empty_like(mi)
+        f = getattr(self.L, f"orc_combo_{self._dt(mi)}")
+        f.argtypes = [_vp] * 4 + [_i64, _i64, _i64, _vp, _vp, _i64]
+        f(mi.ctypes.data, *(None if k is None else k.ctypes.data for k in keep), rows, cols, cols, cs.ctypes.data,
+          out.ctypes.data, cols)
+        return out
+
     def dpi(self, A, tol=0.1):
         """tol is the float tolerance of `dpi --single`; the multiplier uses (double)tol."""
         A = np.ascontiguousarray(A)

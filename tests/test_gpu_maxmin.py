@@ -132,3 +132,27 @@ def test_maxmins_shared_m1_matches_oracle(gpu, port, n):
     gpu.maxmins_dev(Ad, R3=R3b)
     gpu.synchronize()
     assert np.array_equal(bits(R3b.cpu().numpy()), bits(port.mcp(A, 3)[1]))
+
+
+@pytest.mark.parametrize("cs", [(1.0, 0.0, 0.0, 0.0), (0.0, 1.0, 0.0, 0.0), (0.5, 0.25, 1.0, 0.0),
+                                (0.1, 0.2, 0.3, 0.4), (0.0, 0.0, 0.0, 0.0)])
+def test_combo_matches_oracle(gpu, port, cs):
+    """compute_combo, the ensemble MCP score, bit-exact against the oracle's
+    restatement (the reference routine itself needs the absent splash
+    patterns, so this op is pinned only through the restatement)."""
+    import torch
+    rng = np.random.default_rng(int(sum(cs) * 100))
+    n = 133
+    A = rng.random((n, n)).astype(np.float32)
+    A = np.maximum(A, A.T)
+    np.fill_diagonal(A, 0)
+    A[0, :5] = [1e-9, 0, 0.5, 0.25, 0.75]
+    M1 = port.maxmin(A)
+    M2 = port.maxmin(A, M1)
+    M3 = port.maxmin(M1)
+    ref = port.combo(A, M1, M2, M3, cs)
+    t = lambda x: torch.from_numpy(np.ascontiguousarray(x)).cuda()
+    out = torch.empty((n, n), device="cuda")
+    gpu.combo_dev(t(A), t(M1), t(M2), t(M3), cs, out)
+    gpu.synchronize()
+    assert np.array_equal(bits(out.cpu().numpy()), bits(ref))
