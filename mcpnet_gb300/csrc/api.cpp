@@ -62,6 +62,9 @@ struct mcpg_handle {
     void* buf[NSLOTS] = {};
     size_t cap[NSLOTS] = {};
     int fail_allocs = 0;  // test hook: number of upcoming scratch allocations to fail
+    // host MI: a second stream copies finished row slabs back while later slabs compute
+    cudaStream_t copy_stream = nullptr;
+    std::vector<cudaEvent_t> slab_events;
     // optional per-kernel timing (mcpg_profile): CUDA events around each launch
     bool prof = false;
     struct Span { const char* name; cudaEvent_t a, b; };
@@ -215,8 +218,21 @@ int finish(mcpg_handle* h) {
 }
 
 // ---------------- device implementations ----------------
-int mi_dev(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_t ldx, int bins, int order, int precision,
-           float* MI, int64_t ldmi, double* H) {
+// ---- B-spline MI in three steps: weights (prepare), gene-range launches, finish ----
+struct MiPlan {
+    int precision = 0, fmt = 0, split = 0, bins = 0;
+    int64_t n = 0, m = 0;
+    const void* w0 = nullptr;  // FP32 sample-major or 16-bit hi weights
+    const void* w1 = nullptr;  // 16-bit lo weights
+    int64_t ld = 0;            // weight leading dimension
+    double* H = nullptr;
+    float* MI = nullptr;
+    int64_t ldmi = 0;
+    int* flag = nullptr;       // tensor-core timeout flag
+};
+
+int mi_prepare(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_t ldx, int bins, int order, int precision,
+               float* MI, int64_t ldmi, double* H, MiPlan& pl) {
     if (n < 1 || m < 1) return fail(h, MCPG_ERR_ARG, "bspline_mi: need n >= 1 and m >= 1 (got %lld, %lld)",
                                     (long long)n, (long long)m);
     if (ldx < m || ldmi < n) return fail(h, MCPG_ERR_ARG, "bspline_mi: leading dimension too small");
@@ -226,73 +242,92 @@ int mi_dev(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_t ldx, in
                     bins, order);
     if (precision < MCPG_MI_FP32 || precision > MCPG_MI_FP16X3)
         return fail(h, MCPG_ERR_ARG, "bspline_mi: unknown precision %d", precision);
-    double* Hd = H;
-    if (!Hd) {
+    pl = MiPlan{};
+    pl.precision = precision; pl.bins = bins; pl.n = n; pl.m = m; pl.MI = MI; pl.ldmi = ldmi; pl.H = H;
+    int rc;
+    if (!pl.H) {
         void* p;
-        int rc = scratch(h, S_H, (size_t)n * sizeof(double), &p);
-        if (rc) return rc;
-        Hd = (double*)p;
+        if ((rc = scratch(h, S_H, (size_t)n * sizeof(double), &p))) return rc;
+        pl.H = (double*)p;
     }
     if (precision == MCPG_MI_FP32) {
         if (bins > 12) return fail(h, MCPG_ERR_UNSUPPORTED, "bspline_mi FP32: bins > 12 not supported");
         const int64_t ldwt = round_up(n, 16) * bins;
         const int64_t m_pad = round_up(m, 16);
         void* p;
-        int rc = scratch(h, S_W0, (size_t)(m_pad * ldwt) * sizeof(float), &p);
-        if (rc) return rc;
+        if ((rc = scratch(h, S_W0, (size_t)(m_pad * ldwt) * sizeof(float), &p))) return rc;
         CK(h, cudaMemsetAsync(p, 0, (size_t)(m_pad * ldwt) * sizeof(float), h->stream), "memset weights");
-        {
-            PROF(h, "bspline_weights");
-            CK(h, mcpg::launch_bspline_weights_fp32(X, n, m, ldx, bins, order, (float*)p, ldwt, Hd, h->stream,
-                                                     &h->launches),
-               "bspline weights kernel");
-        }
-        {
-            PROF(h, "mi_fp32");
-            CK(h, mcpg::launch_mi_fp32((const float*)p, ldwt, Hd, n, m, bins, MI, ldmi, h->stream, &h->launches),
-               "MI FP32 kernel");
-        }
+        PROF(h, "bspline_weights");
+        CK(h, mcpg::launch_bspline_weights_fp32(X, n, m, ldx, bins, order, (float*)p, ldwt, pl.H, h->stream,
+                                                 &h->launches),
+           "bspline weights kernel");
+        pl.w0 = p;
+        pl.ld = ldwt;
         return MCPG_OK;
     }
-    const int fmt = (precision == MCPG_MI_FP16 || precision == MCPG_MI_FP16X3) ? 1 : 0;
-    const int split = (precision == MCPG_MI_BF16X3 || precision == MCPG_MI_FP16X3) ? 1 : 0;
+    if (bins != 10) return fail(h, MCPG_ERR_UNSUPPORTED, "bspline_mi tensor-core path: only 10 bins (got %d)", bins);
+    pl.fmt = (precision == MCPG_MI_FP16 || precision == MCPG_MI_FP16X3) ? 1 : 0;
+    pl.split = (precision == MCPG_MI_BF16X3 || precision == MCPG_MI_FP16X3) ? 1 : 0;
     const int64_t ldw = round_up(m, 64);
     const int64_t rows = round_up(n * bins, 256) + 256;  // whole tiles stay in bounds
     void *hi, *lo = nullptr;
-    int rc = scratch(h, S_W0, (size_t)(rows * ldw) * 2, &hi);
-    if (rc) return rc;
-    if (split) {
-        rc = scratch(h, S_W1, (size_t)(rows * ldw) * 2, &lo);
-        if (rc) return rc;
-    }
+    if ((rc = scratch(h, S_W0, (size_t)(rows * ldw) * 2, &hi))) return rc;
+    if (pl.split && (rc = scratch(h, S_W1, (size_t)(rows * ldw) * 2, &lo))) return rc;
     // rows beyond n*bins must be zero (they are read by the last tiles)
     const size_t tail = (size_t)((rows - n * bins) * ldw) * 2;
     CK(h, cudaMemsetAsync((char*)hi + (size_t)(n * bins * ldw) * 2, 0, tail, h->stream), "memset weights");
     if (lo) CK(h, cudaMemsetAsync((char*)lo + (size_t)(n * bins * ldw) * 2, 0, tail, h->stream), "memset weights");
     {
         PROF(h, "bspline_weights16");
-        CK(h, mcpg::launch_bspline_weights_16(X, n, m, ldx, bins, order, fmt, (uint16_t*)hi, (uint16_t*)lo, ldw, Hd,
-                                               h->stream, &h->launches),
+        CK(h, mcpg::launch_bspline_weights_16(X, n, m, ldx, bins, order, pl.fmt, (uint16_t*)hi, (uint16_t*)lo, ldw,
+                                               pl.H, h->stream, &h->launches),
            "bspline weights kernel");
     }
     void* flag;
-    rc = scratch(h, S_SMALL, 64, &flag);
-    if (rc) return rc;
+    if ((rc = scratch(h, S_SMALL, 64, &flag))) return rc;
     CK(h, cudaMemsetAsync(flag, 0, sizeof(int), h->stream), "memset flag");
+    pl.w0 = hi; pl.w1 = lo; pl.ld = ldw; pl.flag = (int*)flag;
+    return MCPG_OK;
+}
+
+// Pairs (i, j >= i) with i in [g0, g1); g0 a multiple of 48 (both kernels' gene tiles).
+int mi_launch(mcpg_handle* h, const MiPlan& pl, int64_t g0, int64_t g1) {
+    if (pl.precision == MCPG_MI_FP32) {
+        PROF(h, "mi_fp32");
+        CK(h, mcpg::launch_mi_fp32((const float*)pl.w0, pl.ld, pl.H, pl.n, pl.m, pl.bins, pl.MI, pl.ldmi, h->stream,
+                                   &h->launches, g0, g1),
+           "MI FP32 kernel");
+        return MCPG_OK;
+    }
     cudaError_t e;
     {
         PROF(h, "mi_tc");
-            e = mcpg::launch_mi_tc((const uint16_t*)hi, (const uint16_t*)lo, ldw, Hd, n, m, bins, fmt, split, MI,
-                                           ldmi, (int*)flag, h->stream, &h->launches);
+        e = mcpg::launch_mi_tc((const uint16_t*)pl.w0, (const uint16_t*)pl.w1, pl.ld, pl.H, pl.n, pl.m, pl.bins,
+                               pl.fmt, pl.split, pl.MI, pl.ldmi, pl.flag, h->stream, &h->launches, g0, g1);
     }
     if (e == cudaErrorNotSupported)
         return fail(h, MCPG_ERR_UNSUPPORTED, "bspline_mi tensor-core path: unsupported shape or device");
     CK(h, e, "MI tensor-core kernel");
+    return MCPG_OK;
+}
+
+// Synchronises the stream and reports a tensor-core timeout, if any.
+int mi_finish(mcpg_handle* h, const MiPlan& pl) {
+    if (!pl.flag) return MCPG_OK;
     int timed_out = 0;
-    CK(h, cudaMemcpyAsync(&timed_out, flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream), "read flag");
+    CK(h, cudaMemcpyAsync(&timed_out, pl.flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream), "read flag");
     CK(h, cudaStreamSynchronize(h->stream), "stream synchronize");
     if (timed_out) return fail(h, MCPG_ERR_DEVICE_TIMEOUT, "MI tensor-core kernel: a bounded barrier wait gave up");
     return MCPG_OK;
+}
+
+int mi_dev(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_t ldx, int bins, int order, int precision,
+           float* MI, int64_t ldmi, double* H) {
+    MiPlan pl;
+    int rc = mi_prepare(h, X, n, m, ldx, bins, order, precision, MI, ldmi, H, pl);
+    if (rc) return rc;
+    if ((rc = mi_launch(h, pl, 0, n))) return rc;
+    return mi_finish(h, pl);
 }
 
 int maxmin_dev(mcpg_handle* h, const float* A, int64_t lda, const float* B, int64_t ldb, int64_t rows, int64_t cols,
@@ -940,6 +975,8 @@ int mcpg_destroy(mcpg_handle* h) {
     cudaSetDevice(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
     mcpg_profile(h, 0);
+    for (cudaEvent_t e : h->slab_events) cudaEventDestroy(e);
+    if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
     for (int i = 0; i < NSLOTS; ++i)
         if (h->buf[i]) cudaFree(h->buf[i]);
     if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
@@ -1039,9 +1076,40 @@ int mcpg_bspline_mi(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_
         if ((rc = scratch(h, S_H, (size_t)n * sizeof(double), &p))) return rc;
         dH = (double*)p;
     }
-    if ((rc = mi_dev(h, dX, n, m, lx, bins, order, precision, dMI, lmi, dH))) return rc;
-    if ((rc = copy_out(h, MI, ldmi, dMI, lmi, n, n))) return rc;
+    MiPlan pl;
+    if ((rc = mi_prepare(h, dX, n, m, lx, bins, order, precision, dMI, lmi, dH, pl))) return rc;
+    // Row slabs of 48-gene multiples: once slab k has run, rows < its end are
+    // final (row i's j >= i entries come from its own slab, the j < i ones are
+    // mirrors written by earlier slabs), so their copy to the host overlaps
+    // the next slabs' compute on a second stream.
+    if (!h->copy_stream) CK(h, cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking), "create stream");
+    const int64_t nslab = n >= 48 * 16 ? 16 : 1;
+    while ((int64_t)h->slab_events.size() < nslab) {
+        cudaEvent_t e;
+        CK(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "create event");
+        h->slab_events.push_back(e);
+    }
+    int64_t g0 = 0;
+    for (int64_t k = 0; k < nslab; ++k) {
+        int64_t g1 = (k + 1 == nslab) ? n : ((n * (k + 1) / nslab) / 48) * 48;
+        if (g1 <= g0) continue;
+        if ((rc = mi_launch(h, pl, g0, g1))) return rc;
+        CK(h, cudaEventRecord(h->slab_events[(size_t)k], h->stream), "record event");
+        CK(h, cudaStreamWaitEvent(h->copy_stream, h->slab_events[(size_t)k], 0), "stream wait");
+        const int64_t r = g1 - g0;
+        if (ldmi == n && lmi == n)
+            CK(h, cudaMemcpyAsync(MI + g0 * ldmi, dMI + g0 * lmi, (size_t)(r * n) * sizeof(float),
+                                  cudaMemcpyDeviceToHost, h->copy_stream),
+               "device-to-host copy");
+        else
+            CK(h, cudaMemcpy2DAsync(MI + g0 * ldmi, ldmi * sizeof(float), dMI + g0 * lmi, lmi * sizeof(float),
+                                    n * sizeof(float), r, cudaMemcpyDeviceToHost, h->copy_stream),
+               "device-to-host copy");
+        g0 = g1;
+    }
+    if ((rc = mi_finish(h, pl))) return rc;
     if (H) CK(h, cudaMemcpyAsync(H, dH, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "copy H");
+    CK(h, cudaStreamSynchronize(h->copy_stream), "copy stream synchronize");
     return finish(h);
 }
 

@@ -91,8 +91,11 @@ cudaError_t launch_bspline_weights_16(const float* X, int64_t n, int64_t m, int6
                                       int fmt, uint16_t* Whi, uint16_t* Wlo, int64_t ldw, double* H,
                                       cudaStream_t stream, int64_t* launches);
 // FP32 MI from sample-major weights (CUDA cores), symmetric output.
+// Covers gene pairs (i, j >= i) with i in [gene0, gene1) (gene0 a multiple of 16;
+// gene1 = -1 for n): rows i < gene1 of MI are complete once every earlier range ran.
 cudaError_t launch_mi_fp32(const float* Wt, int64_t ldwt, const double* H, int64_t n, int64_t m, int bins,
-                           float* MI, int64_t ldmi, cudaStream_t stream, int64_t* launches);
+                           float* MI, int64_t ldmi, cudaStream_t stream, int64_t* launches, int64_t gene0 = 0,
+                           int64_t gene1 = -1);
 // MI adjoint, slab of gene tiles [tile0, tile0 + tiles) (16 genes each) x all genes:
 // Q[(i - 16*tile0)*bins + a][j*bins + b] = Gs_ij (log2 P_ab + 1/ln 2) [P_ab > 0],
 // Gs_ij = G[i][j] + G[j][i] (i != j), recomputing P from the sample-major weights.
@@ -108,8 +111,9 @@ cudaError_t launch_mi_bwd_x(const float* X, int64_t n, int64_t m, int64_t ldx, i
                             cudaStream_t stream, int64_t* launches);
 // Tensor-core MI (tcgen05) from 16-bit weights; split != 0 adds the lo terms.
 // Returns cudaErrorNotSupported when the shape/bins is outside the kernel's tiling.
+// Gene range as launch_mi_fp32 (gene0 a multiple of 12).
 cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, int64_t ldw, const double* H, int64_t n,
                          int64_t m, int bins, int fmt, int split, float* MI, int64_t ldmi, int* timeout_flag,
-                         cudaStream_t stream, int64_t* launches);
+                         cudaStream_t stream, int64_t* launches, int64_t gene0 = 0, int64_t gene1 = -1);
 
 }  // namespace mcpg

@@ -60,14 +60,15 @@ struct QArgs {
 template <int BINS, int EPI>
 __global__ void __launch_bounds__(THREADS, 1)
     mi_fp32_kernel(const float* __restrict__ Wt, int64_t ldwt, const double* __restrict__ H, int64_t n,
-                   int64_t m_pad, float inv_m, float* __restrict__ MI, int64_t ldmi, int64_t T, const QArgs qa) {
+                   int64_t m_pad, float inv_m, float* __restrict__ MI, int64_t ldmi, int64_t T, const QArgs qa,
+                   int64_t tile_base) {
     using C = MiCfg<BINS>;
     extern __shared__ float4 smem_f4[];
     float* smem = reinterpret_cast<float*>(smem_f4);
 
     int64_t ti, tj;
     if (EPI == 0) {
-        tri_tile(blockIdx.x, T, ti, tj);
+        tri_tile(tile_base + blockIdx.x, T, ti, tj);
     } else {
         ti = qa.q_tile0 + blockIdx.x / T;
         tj = blockIdx.x % T;
@@ -173,16 +174,20 @@ __global__ void __launch_bounds__(THREADS, 1)
 
 template <int BINS>
 cudaError_t launch_bins(const float* Wt, int64_t ldwt, const double* H, int64_t n, int64_t m, float* MI, int64_t ldmi,
-                        cudaStream_t stream) {
+                        cudaStream_t stream, int64_t t0, int64_t t1) {
     using C = MiCfg<BINS>;
     auto kern = mi_fp32_kernel<BINS, 0>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM);
     if (e != cudaSuccess) return e;
     const int64_t T = ceil_div(n, G);
-    const int64_t tiles = T * (T + 1) / 2;
+    if (t1 > T) t1 = T;
+    if (t0 >= t1) return cudaSuccess;
+    // triangle rows [t0, t1): tiles start(t) = t*T - t(t-1)/2
+    const int64_t start0 = t0 * T - t0 * (t0 - 1) / 2, start1 = t1 * T - t1 * (t1 - 1) / 2;
+    const int64_t tiles = start1 - start0;
     const int64_t m_pad = ceil_div(m, BKS) * BKS;
     const float inv_m = 1.0f / (float)m;  // norm_factor = FT(1) / FT(m), BSplineMI.hpp:321
-    kern<<<(unsigned)tiles, THREADS, C::SMEM, stream>>>(Wt, ldwt, H, n, m_pad, inv_m, MI, ldmi, T, QArgs{});
+    kern<<<(unsigned)tiles, THREADS, C::SMEM, stream>>>(Wt, ldwt, H, n, m_pad, inv_m, MI, ldmi, T, QArgs{}, start0);
     return cudaGetLastError();
 }
 
@@ -197,7 +202,7 @@ cudaError_t launch_q_bins(const float* Wt, int64_t ldwt, int64_t n, int64_t m, c
     const int64_t m_pad = ceil_div(m, BKS) * BKS;
     const float inv_m = 1.0f / (float)m;
     kern<<<(unsigned)(tiles_a * T), THREADS, C::SMEM, stream>>>(Wt, ldwt, nullptr, n, m_pad, inv_m, nullptr, 0, T,
-                                                                qa);
+                                                                qa, 0);
     return cudaGetLastError();
 }
 
@@ -228,21 +233,24 @@ cudaError_t launch_mi_q(const float* Wt, int64_t ldwt, const float* G, int64_t l
 // Wt must be zero-padded: ldwt >= ceil(n/16)*16*bins (multiple of 4), rows
 // s in [m, ceil(m/16)*16) zero.
 cudaError_t launch_mi_fp32(const float* Wt, int64_t ldwt, const double* H, int64_t n, int64_t m, int bins, float* MI,
-                           int64_t ldmi, cudaStream_t stream, int64_t* launches) {
-    if (n <= 0) return cudaSuccess;
+                           int64_t ldmi, cudaStream_t stream, int64_t* launches, int64_t gene0, int64_t gene1) {
+    if (gene1 < 0 || gene1 > n) gene1 = n;
+    if (n <= 0 || gene0 >= gene1) return cudaSuccess;
+    if (gene0 % G) return cudaErrorInvalidValue;
+    const int64_t t0 = gene0 / G, t1 = ceil_div(gene1, G);
     if (launches) ++*launches;
     switch (bins) {
-        case 2: return launch_bins<2>(Wt, ldwt, H, n, m, MI, ldmi, stream);
-        case 3: return launch_bins<3>(Wt, ldwt, H, n, m, MI, ldmi, stream);
-        case 4: return launch_bins<4>(Wt, ldwt, H, n, m, MI, ldmi, stream);
-        case 5: return launch_bins<5>(Wt, ldwt, H, n, m, MI, ldmi, stream);
-        case 6: return launch_bins<6>(Wt, ldwt, H, n, m, MI, ldmi, stream);
-        case 7: return launch_bins<7>(Wt, ldwt, H, n, m, MI, ldmi, stream);
-        case 8: return launch_bins<8>(Wt, ldwt, H, n, m, MI, ldmi, stream);
-        case 9: return launch_bins<9>(Wt, ldwt, H, n, m, MI, ldmi, stream);
-        case 10: return launch_bins<10>(Wt, ldwt, H, n, m, MI, ldmi, stream);
-        case 11: return launch_bins<11>(Wt, ldwt, H, n, m, MI, ldmi, stream);
-        case 12: return launch_bins<12>(Wt, ldwt, H, n, m, MI, ldmi, stream);
+        case 2: return launch_bins<2>(Wt, ldwt, H, n, m, MI, ldmi, stream, t0, t1);
+        case 3: return launch_bins<3>(Wt, ldwt, H, n, m, MI, ldmi, stream, t0, t1);
+        case 4: return launch_bins<4>(Wt, ldwt, H, n, m, MI, ldmi, stream, t0, t1);
+        case 5: return launch_bins<5>(Wt, ldwt, H, n, m, MI, ldmi, stream, t0, t1);
+        case 6: return launch_bins<6>(Wt, ldwt, H, n, m, MI, ldmi, stream, t0, t1);
+        case 7: return launch_bins<7>(Wt, ldwt, H, n, m, MI, ldmi, stream, t0, t1);
+        case 8: return launch_bins<8>(Wt, ldwt, H, n, m, MI, ldmi, stream, t0, t1);
+        case 9: return launch_bins<9>(Wt, ldwt, H, n, m, MI, ldmi, stream, t0, t1);
+        case 10: return launch_bins<10>(Wt, ldwt, H, n, m, MI, ldmi, stream, t0, t1);
+        case 11: return launch_bins<11>(Wt, ldwt, H, n, m, MI, ldmi, stream, t0, t1);
+        case 12: return launch_bins<12>(Wt, ldwt, H, n, m, MI, ldmi, stream, t0, t1);
         default: return cudaErrorNotSupported;
     }
 }

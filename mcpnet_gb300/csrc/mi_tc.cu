@@ -157,6 +157,7 @@ struct TcArgs {
     int64_t ldmi;
     int64_t n;
     int TI, TJ;        // A tiles (12 genes), B tiles (24 genes)
+    int I0, TIr;       // this launch covers A tiles [I0, I0 + TIr)
     int ktiles;        // K / 64
     float inv_m;
     uint32_t idesc;
@@ -201,8 +202,8 @@ __device__ __forceinline__ bool tile_of(int64_t L, const TcArgs& a, int& I, int&
     const int g = (int)(L / per_group);
     const int r = (int)(L - (int64_t)g * per_group);
     J = r / GI;
-    I = g * GI + (r - J * GI);
-    return I < a.TI && J >= j_min_for(I);
+    I = a.I0 + g * GI + (r - J * GI);
+    return I < a.I0 + a.TIr && I < a.TI && J >= j_min_for(I);
 }
 
 // Persistent, warp-specialised CTA (one per SM):
@@ -427,9 +428,11 @@ bool make_map(CUtensorMap* map, const uint16_t* base, int fmt, int64_t rows, int
 // beyond row n*bins and beyond column m; ldw a multiple of 64.
 cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, int64_t ldw, const double* H, int64_t n, int64_t m,
                          int bins, int fmt, int split, float* MI, int64_t ldmi, int* timeout_flag, cudaStream_t stream,
-                         int64_t* launches) {
+                         int64_t* launches, int64_t gene0, int64_t gene1) {
     if (bins != BINS || (ldw % BK) != 0) return cudaErrorNotSupported;
-    if (n <= 0) return cudaSuccess;
+    if (gene1 < 0 || gene1 > n) gene1 = n;
+    if (n <= 0 || gene0 >= gene1) return cudaSuccess;
+    if (gene0 % GA) return cudaErrorInvalidValue;
     int dev = 0;
     cudaGetDevice(&dev);
     int major = 0;
@@ -453,12 +456,14 @@ cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, int64_t ldw, 
     a.n = n;
     a.TI = (int)((n + GA - 1) / GA);
     a.TJ = (int)((n + GBN - 1) / GBN);
+    a.I0 = (int)(gene0 / GA);
+    a.TIr = (int)((gene1 + GA - 1) / GA) - a.I0;
     a.ktiles = (int)(ldw / BK);
     a.inv_m = 1.0f / (float)m;
     a.idesc = idesc_f16(fmt == 0 ? 1u : 0u, MROWS, NCOLS);
     a.err = timeout_flag;
     a.dbg = g_tc_debug_dump;
-    const int groups = (a.TI + GI - 1) / GI;
+    const int groups = (a.TIr + GI - 1) / GI;
     const int64_t n_slots = (int64_t)groups * GI * a.TJ;
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

@@ -48,3 +48,18 @@ def test_mi_tc_unsupported_bins_report(gpu, built_lib):
     with pytest.raises(built_lib.MCPGError) as e:
         gpu.bspline_mi(X, 8, 3, "bf16x3")
     assert e.value.status == built_lib.ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("prec", ["bf16x3", "fp32"])
+def test_host_slabbed_mi_equals_device_mi(gpu, built_lib, prec):
+    """The host entry point computes in row slabs and copies finished slabs back
+    while later ones compute; the result is bit-identical to one device call."""
+    import torch
+    n, m = 1000, 300
+    X = built_lib.synth_grn(n, m, seed=55)
+    host = gpu.bspline_mi(X, 10, 3, prec)
+    Xd = torch.from_numpy(X).cuda()
+    dev = torch.empty((n, n), device="cuda")
+    gpu.bspline_mi_dev(Xd, dev, 10, 3, prec)
+    gpu.synchronize()
+    assert np.array_equal(host, dev.cpu().numpy())
