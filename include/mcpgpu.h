@@ -256,6 +256,79 @@ MCPG_API int mcpg_closure(mcpg_handle* h, const float* A, int64_t n, int64_t lda
 MCPG_API int mcpg_closure_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, int max_iter,
                               float* out, int64_t ldo, int* iterations);
 
+/* ---- gold-standard evaluation: AUPR and AUROC ----
+ * mcpg_aupr_auroc: aupr_kernel::operator()(pos, pos_count, neg, neg_count)
+ * (include/mcp/transform/aupr.hpp:565-584 -> average_compute_1sort, 127-236)
+ * and auroc_kernel::operator() of the same arguments (auroc.hpp:562-579 ->
+ * average_compute_1sort, 151-252):
+ *   AUPR  = sum over the distinct positive scores t of
+ *           TP(>=t) / (TP(>=t) + FP(>=t)) * #pos(==t) / n_pos     (0 if n_pos == 0)
+ *   AUROC = n_pos < n_neg ? 1 - sum over distinct positive t of #neg(>=t)/n_neg * #pos(==t)/n_pos
+ *                         :     sum over distinct negative t of #pos(>=t)/n_pos * #neg(==t)/n_neg
+ *           (an empty sorted side gives a sum of 0, as the reference).
+ * Every term is rounded as the reference rounds it; the terms are summed by a
+ * deterministic compensated reduction rather than the reference's left-to-right
+ * loop, so results agree with it to the rounding of a double sum (a few ulps).
+ * NaN scores return MCPG_ERR_ARG.  aupr / auroc: host doubles (either nullable).
+ * The _dev form takes device score vectors. */
+MCPG_API int mcpg_aupr_auroc(mcpg_handle* h, const float* pos, int64_t n_pos, const float* neg, int64_t n_neg,
+                             double* aupr, double* auroc);
+MCPG_API int mcpg_aupr_auroc_dev(mcpg_handle* h, const float* pos, int64_t n_pos, const float* neg, int64_t n_neg,
+                                 double* aupr, double* auroc);
+
+/* Truth regions of a rows x cols score matrix and its int8 label matrix
+ * (1 = positive, 0 = negative, anything else unknown, as the reference's
+ * aligned_matrix<char> truth):
+ *   MCPG_TRUTH_LOWER  entries (i, j) with j < i     select_lower_triangle, mcpnet_helper.hpp:862-891
+ *   MCPG_TRUTH_ALL    every entry                   (aupr_kernel::compute_full_mat, aupr.hpp:356-387)
+ *   MCPG_TRUTH_TF     rows are TFs: row i is gene row_gene[i]; (i, j) is kept unless
+ *                     j == row_gene[i], or row_gene[i] > j and col_tf[j] != 0
+ *                     (select_tfs_from_mat, mcpnet_helper.hpp:893-940)
+ * row_gene (int32 per row) and col_tf (uint8 per column) are used by
+ * MCPG_TRUTH_TF only (null otherwise). */
+#define MCPG_TRUTH_LOWER 0
+#define MCPG_TRUTH_ALL 1
+#define MCPG_TRUTH_TF 2
+
+/* compute_aupr_auroc (apps/pipeline/mcpnet_helper.hpp:1050-1071): selects the
+ * labelled entries of the region (select_values2, mcpnet_helper.hpp:947-998)
+ * and returns their AUPR / AUROC as mcpg_aupr_auroc, without materialising the
+ * negative scores.  n_pos / n_neg (nullable) get the selected counts.  The
+ * host form takes host values / labels / row_gene / col_tf; the _dev form,
+ * device ones. */
+MCPG_API int mcpg_eval_truth(mcpg_handle* h, const float* values, int64_t rows, int64_t cols, int64_t ldv,
+                             const int8_t* labels, int64_t ldl, int region, const int32_t* row_gene,
+                             const uint8_t* col_tf, double* aupr, double* auroc, int64_t* n_pos, int64_t* n_neg);
+MCPG_API int mcpg_eval_truth_dev(mcpg_handle* h, const float* values, int64_t rows, int64_t cols, int64_t ldv,
+                                 const int8_t* labels, int64_t ldl, int region, const int32_t* row_gene,
+                                 const uint8_t* col_tf, double* aupr, double* auroc, int64_t* n_pos,
+                                 int64_t* n_neg);
+
+/* select_values2 (mcpnet_helper.hpp:947-998) over the region: the positive and
+ * negative scores in row-major order into device arrays pos / neg of
+ * capacities pos_cap / neg_cap (either nullable with capacity 0 to count only).
+ * n_pos / n_neg get the counts; MCPG_ERR_ARG if a capacity is too small (the
+ * counts are still set). */
+MCPG_API int mcpg_select_truth_dev(mcpg_handle* h, const float* values, int64_t rows, int64_t cols, int64_t ldv,
+                                   const int8_t* labels, int64_t ldl, int region, const int32_t* row_gene,
+                                   const uint8_t* col_tf, float* pos, int64_t pos_cap, float* neg, int64_t neg_cap,
+                                   int64_t* n_pos, int64_t* n_neg);
+
+/* Ensemble coefficient search (apps/pipeline/mcpnet.cpp:575-616): for every
+ * row c of coeffs (n_coeffs x 4 host doubles) the AUPR / AUROC of
+ * compute_combo(mi, M1, M2, M3, c) (mcpg_combo_dev) over the labelled entries
+ * of the region.  The combo values are formed only at the labelled entries
+ * (bit-identical to the full matrix's).  Rows equal to (1, 0, 0, 0) are
+ * skipped as the reference does (NaN in aupr / auroc).  aupr / auroc: host
+ * arrays of n_coeffs (nullable); best (nullable) gets the reference's choice:
+ * the first row whose AUPR exceeds every earlier one and 0, else 0.  Mk may be
+ * null when column k of every row is 0. */
+MCPG_API int mcpg_combo_eval_dev(mcpg_handle* h, const float* mi, int64_t ldm, const float* M1, int64_t ld1,
+                                 const float* M2, int64_t ld2, const float* M3, int64_t ld3, int64_t rows,
+                                 int64_t cols, const int8_t* labels, int64_t ldl, int region, const int32_t* row_gene,
+                                 const uint8_t* col_tf, const double* coeffs, int64_t n_coeffs, double* aupr,
+                                 double* auroc, int64_t* best);
+
 /* ---- B-spline MI without any device allocation (no counterpart in the reference) ----
  * For callers that cannot call cudaMalloc -- an application whose device
  * memory belongs entirely to its own pool allocator, or a latency-critical

@@ -81,7 +81,17 @@ ABI = [
     ("mcpg_bspline_mi_bwd_dev", C.c_int, [_vp, _vp, _i64, _i64, _i64, C.c_int, C.c_int, _vp, _i64, _vp, _i64]),
     ("mcpg_synth_grn", C.c_int, [_i64, _i64, C.c_uint64, _vp, _i64, _vp, _i64, C.POINTER(C.c_int64)]),
     ("mcpg_bspline_mi_fp32_noalloc", C.c_int, [_vp, _i64, _i64, _i64, C.c_int, C.c_int, _vp, _i64, _vp, _vp]),
+    ("mcpg_aupr_auroc", C.c_int, [_vp, _vp, _i64, _vp, _i64, _vp, _vp]),
+    ("mcpg_aupr_auroc_dev", C.c_int, [_vp, _vp, _i64, _vp, _i64, _vp, _vp]),
+    ("mcpg_eval_truth", C.c_int, [_vp, _vp, _i64, _i64, _i64, _vp, _i64, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp]),
+    ("mcpg_eval_truth_dev", C.c_int, [_vp, _vp, _i64, _i64, _i64, _vp, _i64, C.c_int, _vp, _vp, _vp, _vp, _vp,
+                                      _vp]),
+    ("mcpg_select_truth_dev", C.c_int, [_vp, _vp, _i64, _i64, _i64, _vp, _i64, C.c_int, _vp, _vp, _vp, _i64, _vp,
+                                        _i64, _vp, _vp]),
+    ("mcpg_combo_eval_dev", C.c_int, [_vp, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _i64, _i64, _vp, _i64,
+                                      C.c_int, _vp, _vp, _vp, _i64, _vp, _vp, _vp]),
 ]
+TRUTH_REGIONS = {"lower": 0, "all": 1, "tf": 2}
 
 _lib = None
 
@@ -455,6 +465,80 @@ class Handle:
         self._check(self._L.mcpg_combo_dev(self._h, self._dp(mi), self._ld(mi), self._dp(M1), ld(M1), self._dp(M2),
                                             ld(M2), self._dp(M3), ld(M3), rows, cols, cs.ctypes.data, self._dp(out),
                                             self._ld(out)), "combo_dev")
+
+    # ---- gold-standard evaluation ----
+    def aupr_auroc(self, pos, neg):
+        """AUPR and AUROC of positive / negative score vectors (aupr_kernel / auroc_kernel)."""
+        pos, neg = _f32(pos).ravel(), _f32(neg).ravel()
+        a, b = C.c_double(0), C.c_double(0)
+        self._check(self._L.mcpg_aupr_auroc(self._h, _ptr(pos), pos.size, _ptr(neg), neg.size, C.byref(a),
+                                             C.byref(b)), "aupr_auroc")
+        return a.value, b.value
+
+    def aupr_auroc_dev(self, pos, neg):
+        """As aupr_auroc, for contiguous 1-D float32 CUDA tensors."""
+        a, b = C.c_double(0), C.c_double(0)
+        self._check(self._L.mcpg_aupr_auroc_dev(self._h, self._dp(pos), pos.numel(), self._dp(neg), neg.numel(),
+                                                 C.byref(a), C.byref(b)), "aupr_auroc_dev")
+        return a.value, b.value
+
+    def eval_truth(self, values, labels, region="lower", row_gene=None, col_tf=None):
+        """compute_aupr_auroc over a host score matrix and int8 label matrix.
+
+        Returns (aupr, auroc, n_pos, n_neg)."""
+        values = _f32(values)
+        labels = np.ascontiguousarray(labels, dtype=np.int8)
+        rows, cols = values.shape
+        if labels.shape != values.shape:
+            raise ValueError("labels must have the shape of values")
+        rg = None if row_gene is None else np.ascontiguousarray(row_gene, dtype=np.int32)
+        ct = None if col_tf is None else np.ascontiguousarray(col_tf, dtype=np.uint8)
+        a, b, npos, nneg = C.c_double(0), C.c_double(0), C.c_int64(0), C.c_int64(0)
+        self._check(self._L.mcpg_eval_truth(self._h, _ptr(values), rows, cols, cols, _ptr(labels), cols,
+                                             TRUTH_REGIONS[region], _ptr(rg), _ptr(ct), C.byref(a), C.byref(b),
+                                             C.byref(npos), C.byref(nneg)), "eval_truth")
+        return a.value, b.value, npos.value, nneg.value
+
+    def eval_truth_dev(self, values, labels, region="lower", row_gene=None, col_tf=None):
+        """As eval_truth for CUDA tensors (values float32, labels int8, row_gene int32, col_tf uint8)."""
+        rows, cols = values.shape
+        a, b, npos, nneg = C.c_double(0), C.c_double(0), C.c_int64(0), C.c_int64(0)
+        self._check(self._L.mcpg_eval_truth_dev(self._h, self._dp(values), rows, cols, self._ld(values),
+                                                 self._dp(labels), self._ld(labels), TRUTH_REGIONS[region],
+                                                 self._dp(row_gene), self._dp(col_tf), C.byref(a), C.byref(b),
+                                                 C.byref(npos), C.byref(nneg)), "eval_truth_dev")
+        return a.value, b.value, npos.value, nneg.value
+
+    def select_truth_dev(self, values, labels, region="lower", row_gene=None, col_tf=None):
+        """select_values2: (pos, neg) float32 CUDA tensors in row-major order."""
+        import torch
+        rows, cols = values.shape
+        npos, nneg = C.c_int64(0), C.c_int64(0)
+        args = (self._h, self._dp(values), rows, cols, self._ld(values), self._dp(labels), self._ld(labels),
+                TRUTH_REGIONS[region], self._dp(row_gene), self._dp(col_tf))
+        self._check(self._L.mcpg_select_truth_dev(*args, None, 0, None, 0, C.byref(npos), C.byref(nneg)),
+                    "select_truth_dev")
+        pos = torch.empty(npos.value, dtype=torch.float32, device=values.device)
+        neg = torch.empty(nneg.value, dtype=torch.float32, device=values.device)
+        self._check(self._L.mcpg_select_truth_dev(*args, self._dp(pos), pos.numel(), self._dp(neg), neg.numel(),
+                                                   C.byref(npos), C.byref(nneg)), "select_truth_dev")
+        return pos, neg
+
+    def combo_eval_dev(self, mi, M1, M2, M3, labels, coeffs, region="lower", row_gene=None, col_tf=None):
+        """Ensemble coefficient search: per coefficient row the AUPR / AUROC of compute_combo at the
+        labelled entries.  Returns (aupr ndarray, auroc ndarray, best row)."""
+        cs = np.ascontiguousarray(np.asarray(coeffs, dtype=np.float64).reshape(-1, 4))
+        rows, cols = mi.shape
+        ld = lambda t: self._ld(t) if t is not None else cols
+        a = np.empty(cs.shape[0], dtype=np.float64)
+        b = np.empty(cs.shape[0], dtype=np.float64)
+        best = C.c_int64(0)
+        self._check(self._L.mcpg_combo_eval_dev(self._h, self._dp(mi), self._ld(mi), self._dp(M1), ld(M1),
+                                                 self._dp(M2), ld(M2), self._dp(M3), ld(M3), rows, cols,
+                                                 self._dp(labels), self._ld(labels), TRUTH_REGIONS[region],
+                                                 self._dp(row_gene), self._dp(col_tf), cs.ctypes.data, cs.shape[0],
+                                                 _ptr(a), _ptr(b), C.byref(best)), "combo_eval_dev")
+        return a, b, best.value
 
     def dpi_dev(self, A, out, tol=0.1, mask=None):
         n = A.shape[0]

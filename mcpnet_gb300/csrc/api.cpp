@@ -48,6 +48,20 @@ enum Slot {
     S_GS,        // MI adjoint pair sums
     S_IN3,       // staged host input 3
     S_IN4,       // staged host input 4
+    S_EV_CNT,    // evaluation: per-item label counts
+    S_EV_OFF,    // evaluation: scanned per-item counts
+    S_EV_KP,     // evaluation: positive keys
+    S_EV_KN,     // evaluation: negative keys
+    S_EV_ALT,    // evaluation: radix-sort ping-pong buffer
+    S_EV_BH,     // evaluation: radix-sort block histograms
+    S_EV_BHOFF,  // evaluation: scanned block histograms
+    S_EV_TMP,    // evaluation: scan partials
+    S_EV_HIST,   // evaluation: lt / eq histograms and their prefix sums
+    S_EV_RED,    // evaluation: flag, curve sums and partials
+    S_EV_GP,     // evaluation: gathered positive (mi, M1, M2, M3)
+    S_EV_GN,     // evaluation: gathered negative (mi, M1, M2, M3)
+    S_EV_LAB,    // evaluation: staged labels
+    S_EV_AUX,    // evaluation: staged row_gene / col_tf
     NSLOTS
 };
 
@@ -923,6 +937,360 @@ int maxmins_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, float* M
     return MCPG_OK;
 }
 
+// ---- gold-standard evaluation (AUPR / AUROC) ----
+struct EvalWs {
+    int* flag;         // NaN seen
+    unsigned* ticket;  // curve reduction
+    double* out;       // curve sums [2]
+    double* part;      // curve partials
+};
+
+int ev_ws(mcpg_handle* h, EvalWs& w) {
+    void* p;
+    int rc = scratch(h, S_EV_RED, 64 + (size_t)mcpg::curve_part_elems() * sizeof(double), &p);
+    if (rc) return rc;
+    char* b = (char*)p;
+    w.flag = (int*)b;
+    w.ticket = (unsigned*)(b + 8);
+    w.out = (double*)(b + 16);
+    w.part = (double*)(b + 64);
+    CK(h, cudaMemsetAsync(w.flag, 0, sizeof(int), h->stream), "memset");
+    return MCPG_OK;
+}
+
+int ev_nan_check(mcpg_handle* h, const EvalWs& w) {
+    int f = 0;
+    CK(h, cudaMemcpyAsync(&f, w.flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream), "device-to-host copy");
+    CK(h, cudaStreamSynchronize(h->stream), "stream synchronize");
+    if (f) return fail(h, MCPG_ERR_ARG, "evaluation: NaN score among the labelled entries");
+    return MCPG_OK;
+}
+
+int ev_sort(mcpg_handle* h, uint32_t* keys, int64_t n) {
+    if (n <= 1) return MCPG_OK;
+    const int64_t nb = mcpg::radix_blocks(n);
+    void *alt, *bh, *bo, *tmp;
+    int rc;
+    if ((rc = scratch(h, S_EV_ALT, (size_t)n * 4, &alt))) return rc;
+    if ((rc = scratch(h, S_EV_BH, (size_t)(256 * nb) * 4, &bh))) return rc;
+    if ((rc = scratch(h, S_EV_BHOFF, (size_t)(256 * nb + 1) * 8, &bo))) return rc;
+    if ((rc = scratch(h, S_EV_TMP, (size_t)mcpg::scan_tmp_elems(256 * nb) * 8, &tmp))) return rc;
+    PROF(h, "radix_sort");
+    CK(h, mcpg::launch_radix_sort(keys, (uint32_t*)alt, n, (uint32_t*)bh, (uint64_t*)bo, (uint64_t*)tmp, h->stream,
+                                  &h->launches),
+       "radix sort");
+    return MCPG_OK;
+}
+
+// Places the Y scores (through `count(lt, eq)`) into the sorted X and returns
+// the two curve sums of launch_curve in res.
+template <class Count>
+int ev_curve(mcpg_handle* h, const uint32_t* X, int64_t nX, int64_t nY, const EvalWs& w, Count count, double res[2]) {
+    if (nX >= ((int64_t)1 << 31)) return fail(h, MCPG_ERR_UNSUPPORTED, "evaluation: more than 2^31 - 1 sorted scores");
+    void *hist, *tmp;
+    int rc;
+    if ((rc = scratch(h, S_EV_HIST, (size_t)(4 * nX + 3) * 8, &hist))) return rc;
+    if ((rc = scratch(h, S_EV_TMP, (size_t)mcpg::scan_tmp_elems(nX) * 8, &tmp))) return rc;
+    uint64_t* lt = (uint64_t*)hist;
+    uint64_t* eq = lt + nX + 1;
+    uint64_t* work = eq + nX + 1;
+    {
+        PROF(h, "rank_count");
+        CK(h, count(lt, eq), "rank count");
+    }
+    {
+        PROF(h, "curve");
+        CK(h, mcpg::launch_curve(X, nX, nY, lt, eq, work, (uint64_t*)tmp, w.part, w.ticket, w.out, h->stream,
+                                 &h->launches),
+           "curve");
+    }
+    CK(h, cudaMemcpyAsync(res, w.out, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "device-to-host copy");
+    CK(h, cudaStreamSynchronize(h->stream), "stream synchronize");
+    return MCPG_OK;
+}
+
+// AUPR / AUROC from P positive keys kp (any order; sorted here in place), N
+// negatives ranked by neg_rank(X, nX, lt, eq), and -- only for the AUROC
+// branch n_pos >= n_neg > 0 -- compact negative keys from neg_keys(&kn).
+template <class NegRank, class NegKeys>
+int ev_aupr_auroc(mcpg_handle* h, const EvalWs& w, uint32_t* kp, int64_t P, int64_t N, NegRank neg_rank,
+                  NegKeys neg_keys, double* aupr, double* auroc) {
+    double res[2] = {0.0, 0.0};
+    int rc;
+    if (P > 0) {
+        if ((rc = ev_sort(h, kp, P))) return rc;
+        if ((rc = ev_curve(h, kp, P, N, w,
+                           [&](uint64_t* lt, uint64_t* eq) { return neg_rank((const uint32_t*)kp, P, lt, eq); },
+                           res)))
+            return rc;
+    }
+    const double pr = P == 0 ? 0.0 : res[0];
+    double roc;
+    if (P < N) {
+        roc = P == 0 ? 1.0 : 1.0 - res[1];
+    } else if (N == 0) {
+        roc = 0.0;
+    } else {
+        uint32_t* kn = nullptr;
+        if ((rc = neg_keys(&kn))) return rc;
+        if ((rc = ev_sort(h, kn, N))) return rc;
+        double r2[2];
+        if ((rc = ev_curve(h, kn, N, P, w,
+                           [&](uint64_t* lt, uint64_t* eq) {
+                               return mcpg::launch_rank_count_keys(kn, N, kp, P, lt, eq, h->stream, &h->launches);
+                           },
+                           r2)))
+            return rc;
+        roc = r2[1];
+    }
+    if ((rc = ev_nan_check(h, w))) return rc;
+    if (aupr) *aupr = pr;
+    if (auroc) *auroc = roc;
+    return MCPG_OK;
+}
+
+int aupr_auroc_dev(mcpg_handle* h, const float* pos, int64_t P, const float* neg, int64_t N, double* aupr,
+                   double* auroc) {
+    if (P < 0 || N < 0) return fail(h, MCPG_ERR_ARG, "aupr_auroc: negative count");
+    if ((P > 0 && !pos) || (N > 0 && !neg)) return fail(h, MCPG_ERR_ARG, "aupr_auroc: null score vector");
+    EvalWs w;
+    int rc;
+    if ((rc = ev_ws(h, w))) return rc;
+    void *kp, *kn;
+    if ((rc = scratch(h, S_EV_KP, (size_t)P * 4, &kp))) return rc;
+    if ((rc = scratch(h, S_EV_KN, (size_t)N * 4, &kn))) return rc;
+    {
+        PROF(h, "keys");
+        CK(h, mcpg::launch_keys_from_floats(pos, P, (uint32_t*)kp, w.flag, h->stream, &h->launches), "keys");
+        if (P > 0) CK(h, mcpg::launch_keys_from_floats(neg, N, (uint32_t*)kn, w.flag, h->stream, &h->launches), "keys");
+    }
+    uint32_t* knk = (uint32_t*)kn;
+    return ev_aupr_auroc(
+        h, w, (uint32_t*)kp, P, N,
+        [&](const uint32_t* X, int64_t nX, uint64_t* lt, uint64_t* eq) {
+            return mcpg::launch_rank_count_keys(X, nX, knk, N, lt, eq, h->stream, &h->launches);
+        },
+        [&](uint32_t** out) {
+            if (P == 0) {  // keys not made above
+                PROF(h, "keys");
+                CK(h, mcpg::launch_keys_from_floats(neg, N, knk, w.flag, h->stream, &h->launches), "keys");
+            }
+            *out = knk;
+            return MCPG_OK;
+        },
+        aupr, auroc);
+}
+
+int truth_region(mcpg_handle* h, const char* who, const int8_t* labels, int64_t rows, int64_t cols, int64_t ldl,
+                 int region, const int32_t* row_gene, const uint8_t* col_tf, mcpg::TruthRegion* r) {
+    if (rows < 0 || cols < 0) return fail(h, MCPG_ERR_ARG, "%s: negative size", who);
+    if (rows > 0 && cols > 0 && !labels) return fail(h, MCPG_ERR_ARG, "%s: null labels", who);
+    if (ldl < cols) return fail(h, MCPG_ERR_ARG, "%s: label leading dimension too small", who);
+    if (region != MCPG_TRUTH_LOWER && region != MCPG_TRUTH_ALL && region != MCPG_TRUTH_TF)
+        return fail(h, MCPG_ERR_ARG, "%s: unknown truth region %d", who, region);
+    if (region == MCPG_TRUTH_TF && rows > 0 && cols > 0 && (!row_gene || !col_tf))
+        return fail(h, MCPG_ERR_ARG, "%s: MCPG_TRUTH_TF needs row_gene and col_tf", who);
+    r->labels = labels;
+    r->ldl = ldl;
+    r->rows = rows;
+    r->cols = cols;
+    r->mode = region;
+    r->row_gene = row_gene;
+    r->col_tf = col_tf;
+    return MCPG_OK;
+}
+
+// Per-item counts and their scans; P / N on the host.
+int truth_offsets(mcpg_handle* h, const mcpg::TruthRegion& r, uint64_t** offp, uint64_t** offn, int64_t* P,
+                  int64_t* N) {
+    const int64_t items = mcpg::truth_items(r);
+    void *cnt, *off, *tmp;
+    int rc;
+    if ((rc = scratch(h, S_EV_CNT, (size_t)(2 * items) * 4, &cnt))) return rc;
+    if ((rc = scratch(h, S_EV_OFF, (size_t)(2 * (items + 1)) * 8, &off))) return rc;
+    if ((rc = scratch(h, S_EV_TMP, (size_t)mcpg::scan_tmp_elems(items) * 8, &tmp))) return rc;
+    uint32_t* cp = (uint32_t*)cnt;
+    uint32_t* cn = cp + items;
+    *offp = (uint64_t*)off;
+    *offn = *offp + items + 1;
+    {
+        PROF(h, "truth_count");
+        CK(h, mcpg::launch_truth_count(r, cp, cn, h->stream, &h->launches), "truth count");
+        CK(h, mcpg::launch_scan_u32(cp, items, *offp, (uint64_t*)tmp, h->stream, &h->launches), "scan");
+        CK(h, mcpg::launch_scan_u32(cn, items, *offn, (uint64_t*)tmp, h->stream, &h->launches), "scan");
+    }
+    uint64_t tot[2];
+    CK(h, cudaMemcpyAsync(&tot[0], *offp + items, 8, cudaMemcpyDeviceToHost, h->stream), "device-to-host copy");
+    CK(h, cudaMemcpyAsync(&tot[1], *offn + items, 8, cudaMemcpyDeviceToHost, h->stream), "device-to-host copy");
+    CK(h, cudaStreamSynchronize(h->stream), "stream synchronize");
+    *P = (int64_t)tot[0];
+    *N = (int64_t)tot[1];
+    return MCPG_OK;
+}
+
+int gather_one(mcpg_handle* h, const mcpg::TruthRegion& r, int lab, const uint64_t* off, const float* v, int64_t ldv,
+               float* dst, int* flag) {
+    mcpg::GatherSrc g{};
+    g.n = 1;
+    g.src[0] = v;
+    g.lds[0] = ldv;
+    g.dst[0] = dst;
+    PROF(h, "truth_gather");
+    CK(h, mcpg::launch_truth_gather(r, lab, off, g, flag, h->stream, &h->launches), "truth gather");
+    return MCPG_OK;
+}
+
+int eval_truth_dev(mcpg_handle* h, const float* values, int64_t ldv, const mcpg::TruthRegion& r, double* aupr,
+                   double* auroc, int64_t* n_pos, int64_t* n_neg) {
+    if (r.rows > 0 && r.cols > 0 && (!values || ldv < r.cols))
+        return fail(h, MCPG_ERR_ARG, "eval_truth: null values or leading dimension too small");
+    EvalWs w;
+    int rc;
+    if ((rc = ev_ws(h, w))) return rc;
+    uint64_t *offp = nullptr, *offn = nullptr;
+    int64_t P = 0, N = 0;
+    if ((rc = truth_offsets(h, r, &offp, &offn, &P, &N))) return rc;
+    if (n_pos) *n_pos = P;
+    if (n_neg) *n_neg = N;
+    void* kp;
+    if ((rc = scratch(h, S_EV_KP, (size_t)P * 4, &kp))) return rc;
+    if (P > 0) {
+        if ((rc = gather_one(h, r, 1, offp, values, ldv, (float*)kp, w.flag))) return rc;
+        PROF(h, "keys");
+        CK(h, mcpg::launch_keys_from_floats((const float*)kp, P, (uint32_t*)kp, w.flag, h->stream, &h->launches),
+           "keys");
+    }
+    return ev_aupr_auroc(
+        h, w, (uint32_t*)kp, P, N,
+        [&](const uint32_t* X, int64_t nX, uint64_t* lt, uint64_t* eq) {
+            return mcpg::launch_rank_count_matrix(X, nX, r, values, ldv, 0, lt, eq, w.flag, h->stream,
+                                                  &h->launches);
+        },
+        [&](uint32_t** out) {
+            void* kn;
+            int rc2 = scratch(h, S_EV_KN, (size_t)N * 4, &kn);
+            if (rc2) return rc2;
+            if ((rc2 = gather_one(h, r, 0, offn, values, ldv, (float*)kn, w.flag))) return rc2;
+            PROF(h, "keys");
+            CK(h, mcpg::launch_keys_from_floats((const float*)kn, N, (uint32_t*)kn, w.flag, h->stream, &h->launches),
+               "keys");
+            *out = (uint32_t*)kn;
+            return MCPG_OK;
+        },
+        aupr, auroc);
+}
+
+int select_truth_dev(mcpg_handle* h, const float* values, int64_t ldv, const mcpg::TruthRegion& r, float* pos,
+                     int64_t pos_cap, float* neg, int64_t neg_cap, int64_t* n_pos, int64_t* n_neg) {
+    if (r.rows > 0 && r.cols > 0 && (!values || ldv < r.cols))
+        return fail(h, MCPG_ERR_ARG, "select_truth: null values or leading dimension too small");
+    if (pos_cap < 0 || neg_cap < 0) return fail(h, MCPG_ERR_ARG, "select_truth: negative capacity");
+    EvalWs w;
+    int rc;
+    if ((rc = ev_ws(h, w))) return rc;
+    uint64_t *offp = nullptr, *offn = nullptr;
+    int64_t P = 0, N = 0;
+    if ((rc = truth_offsets(h, r, &offp, &offn, &P, &N))) return rc;
+    if (n_pos) *n_pos = P;
+    if (n_neg) *n_neg = N;
+    if ((pos && P > pos_cap) || (neg && N > neg_cap))
+        return fail(h, MCPG_ERR_ARG, "select_truth: capacity too small (need %lld positives, %lld negatives)",
+                    (long long)P, (long long)N);
+    if (pos && P > 0 && (rc = gather_one(h, r, 1, offp, values, ldv, pos, w.flag))) return rc;
+    if (neg && N > 0 && (rc = gather_one(h, r, 0, offn, values, ldv, neg, w.flag))) return rc;
+    return finish(h);
+}
+
+int combo_eval_dev(mcpg_handle* h, const float* const mats[4], const int64_t lds[4], const mcpg::TruthRegion& r,
+                   const double* coeffs, int64_t nc, double* aupr, double* auroc, int64_t* best) {
+    if (nc < 0 || (nc > 0 && !coeffs)) return fail(h, MCPG_ERR_ARG, "combo_eval: bad coefficient table");
+    if (r.rows > 0 && r.cols > 0) {
+        if (!mats[0] || lds[0] < r.cols) return fail(h, MCPG_ERR_ARG, "combo_eval: null mi or leading dimension");
+        for (int k = 1; k < 4; ++k) {
+            if (mats[k] && lds[k] < r.cols) return fail(h, MCPG_ERR_ARG, "combo_eval: leading dimension too small");
+            for (int64_t c = 0; c < nc; ++c)
+                if (!mats[k] && coeffs[4 * c + k] != 0.0)
+                    return fail(h, MCPG_ERR_ARG, "combo_eval: coefficient row %lld uses a null matrix", (long long)c);
+        }
+    }
+    EvalWs w;
+    int rc;
+    if ((rc = ev_ws(h, w))) return rc;
+    uint64_t *offp = nullptr, *offn = nullptr;
+    int64_t P = 0, N = 0;
+    if ((rc = truth_offsets(h, r, &offp, &offn, &P, &N))) return rc;
+    void *gp, *gn, *kp;
+    if ((rc = scratch(h, S_EV_GP, (size_t)(4 * P) * 4, &gp))) return rc;
+    if ((rc = scratch(h, S_EV_GN, (size_t)(4 * N) * 4, &gn))) return rc;
+    if ((rc = scratch(h, S_EV_KP, (size_t)P * 4, &kp))) return rc;
+    const float* gpk[4];
+    const float* gnk[4];
+    for (int lab = 0; lab < 2; ++lab) {
+        mcpg::GatherSrc g{};
+        float* base = (float*)(lab ? gp : gn);
+        const int64_t cnt = lab ? P : N;
+        for (int k = 0; k < 4; ++k) {
+            (lab ? gpk : gnk)[k] = base + k * cnt;
+            if (!mats[k]) continue;
+            g.src[g.n] = mats[k];
+            g.lds[g.n] = lds[k];
+            g.dst[g.n] = base + k * cnt;
+            ++g.n;
+        }
+        if (cnt == 0) continue;
+        PROF(h, "truth_gather");
+        CK(h, mcpg::launch_truth_gather(r, lab, lab ? offp : offn, g, w.flag, h->stream, &h->launches),
+           "truth gather");
+    }
+    double max_aupr = 0.0;
+    int64_t co = 0;
+    for (int64_t c = 0; c < nc; ++c) {
+        const double* cs = coeffs + 4 * c;
+        if (cs[0] == 1.0 && cs[1] == 0.0 && cs[2] == 0.0 && cs[3] == 0.0) {  // mcpnet.cpp:589
+            if (aupr) aupr[c] = NAN;
+            if (auroc) auroc[c] = NAN;
+            continue;
+        }
+        mcpg::ComboSrc sp{}, sn{};
+        for (int k = 0; k < 4; ++k) {
+            sp.g[k] = gpk[k];
+            sn.g[k] = gnk[k];
+            sp.cs[k] = sn.cs[k] = cs[k];
+        }
+        sp.n = P;
+        sn.n = N;
+        {
+            PROF(h, "keys");
+            CK(h, mcpg::launch_combo_keys(sp, (uint32_t*)kp, w.flag, h->stream, &h->launches), "combo keys");
+        }
+        double a = 0.0, b = 0.0;
+        rc = ev_aupr_auroc(
+            h, w, (uint32_t*)kp, P, N,
+            [&](const uint32_t* X, int64_t nX, uint64_t* lt, uint64_t* eq) {
+                return mcpg::launch_rank_count_combo(X, nX, sn, lt, eq, w.flag, h->stream, &h->launches);
+            },
+            [&](uint32_t** out) {
+                void* kn;
+                int rc2 = scratch(h, S_EV_KN, (size_t)N * 4, &kn);
+                if (rc2) return rc2;
+                PROF(h, "keys");
+                CK(h, mcpg::launch_combo_keys(sn, (uint32_t*)kn, w.flag, h->stream, &h->launches), "combo keys");
+                *out = (uint32_t*)kn;
+                return MCPG_OK;
+            },
+            &a, &b);
+        if (rc) return rc;
+        if (aupr) aupr[c] = a;
+        if (auroc) auroc[c] = b;
+        if (a > max_aupr) {  // mcpnet.cpp:602-606
+            max_aupr = a;
+            co = c;
+        }
+    }
+    if (best) *best = co;
+    return MCPG_OK;
+}
+
 }  // namespace
 
 // =====================================================================
@@ -1543,6 +1911,92 @@ int mcpg_combo_dev(mcpg_handle* h, const float* mi, int64_t ldm, const float* M1
                              &h->launches),
        "combo kernel");
     return MCPG_OK;
+}
+
+int mcpg_aupr_auroc_dev(mcpg_handle* h, const float* pos, int64_t n_pos, const float* neg, int64_t n_neg,
+                        double* aupr, double* auroc) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    return aupr_auroc_dev(h, pos, n_pos, neg, n_neg, aupr, auroc);
+}
+
+int mcpg_aupr_auroc(mcpg_handle* h, const float* pos, int64_t n_pos, const float* neg, int64_t n_neg, double* aupr,
+                    double* auroc) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (n_pos < 0 || n_neg < 0) return fail(h, MCPG_ERR_ARG, "aupr_auroc: negative count");
+    if ((n_pos > 0 && !pos) || (n_neg > 0 && !neg)) return fail(h, MCPG_ERR_ARG, "aupr_auroc: null score vector");
+    float *dp = nullptr, *dn = nullptr;
+    int64_t ld;
+    if ((rc = stage_in(h, S_IN0, pos, n_pos, 1, n_pos, &dp, &ld))) return rc;
+    if ((rc = stage_in(h, S_IN1, neg, n_neg, 1, n_neg, &dn, &ld))) return rc;
+    return aupr_auroc_dev(h, dp, n_pos, dn, n_neg, aupr, auroc);
+}
+
+int mcpg_eval_truth_dev(mcpg_handle* h, const float* values, int64_t rows, int64_t cols, int64_t ldv,
+                        const int8_t* labels, int64_t ldl, int region, const int32_t* row_gene, const uint8_t* col_tf,
+                        double* aupr, double* auroc, int64_t* n_pos, int64_t* n_neg) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    mcpg::TruthRegion r{};
+    if ((rc = truth_region(h, "eval_truth", labels, rows, cols, ldl, region, row_gene, col_tf, &r))) return rc;
+    return eval_truth_dev(h, values, ldv, r, aupr, auroc, n_pos, n_neg);
+}
+
+int mcpg_eval_truth(mcpg_handle* h, const float* values, int64_t rows, int64_t cols, int64_t ldv, const int8_t* labels,
+                    int64_t ldl, int region, const int32_t* row_gene, const uint8_t* col_tf, double* aupr,
+                    double* auroc, int64_t* n_pos, int64_t* n_neg) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    mcpg::TruthRegion r{};
+    if ((rc = truth_region(h, "eval_truth", labels, rows, cols, ldl, region, row_gene, col_tf, &r))) return rc;
+    if (rows > 0 && cols > 0 && (!values || ldv < cols))
+        return fail(h, MCPG_ERR_ARG, "eval_truth: null values or leading dimension too small");
+    float* dv = nullptr;
+    int64_t ld = 0;
+    if ((rc = stage_in(h, S_IN0, values, ldv, rows, cols, &dv, &ld))) return rc;
+    void *lab, *aux;
+    if ((rc = scratch(h, S_EV_LAB, (size_t)(rows * cols), &lab))) return rc;
+    if (rows > 0 && cols > 0)
+        CK(h, cudaMemcpy2DAsync(lab, (size_t)cols, labels, (size_t)ldl, (size_t)cols, (size_t)rows,
+                                cudaMemcpyHostToDevice, h->stream),
+           "host-to-device copy");
+    r.labels = (const int8_t*)lab;
+    r.ldl = cols;
+    if (region == MCPG_TRUTH_TF && rows > 0 && cols > 0) {
+        if ((rc = scratch(h, S_EV_AUX, (size_t)(rows * 4 + cols), &aux))) return rc;
+        CK(h, cudaMemcpyAsync(aux, row_gene, (size_t)rows * 4, cudaMemcpyHostToDevice, h->stream),
+           "host-to-device copy");
+        CK(h, cudaMemcpyAsync((char*)aux + rows * 4, col_tf, (size_t)cols, cudaMemcpyHostToDevice, h->stream),
+           "host-to-device copy");
+        r.row_gene = (const int32_t*)aux;
+        r.col_tf = (const uint8_t*)aux + rows * 4;
+    }
+    return eval_truth_dev(h, dv, ld, r, aupr, auroc, n_pos, n_neg);
+}
+
+int mcpg_select_truth_dev(mcpg_handle* h, const float* values, int64_t rows, int64_t cols, int64_t ldv,
+                          const int8_t* labels, int64_t ldl, int region, const int32_t* row_gene,
+                          const uint8_t* col_tf, float* pos, int64_t pos_cap, float* neg, int64_t neg_cap,
+                          int64_t* n_pos, int64_t* n_neg) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    mcpg::TruthRegion r{};
+    if ((rc = truth_region(h, "select_truth", labels, rows, cols, ldl, region, row_gene, col_tf, &r))) return rc;
+    return select_truth_dev(h, values, ldv, r, pos, pos_cap, neg, neg_cap, n_pos, n_neg);
+}
+
+int mcpg_combo_eval_dev(mcpg_handle* h, const float* mi, int64_t ldm, const float* M1, int64_t ld1, const float* M2,
+                        int64_t ld2, const float* M3, int64_t ld3, int64_t rows, int64_t cols, const int8_t* labels,
+                        int64_t ldl, int region, const int32_t* row_gene, const uint8_t* col_tf, const double* coeffs,
+                        int64_t n_coeffs, double* aupr, double* auroc, int64_t* best) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    mcpg::TruthRegion r{};
+    if ((rc = truth_region(h, "combo_eval", labels, rows, cols, ldl, region, row_gene, col_tf, &r))) return rc;
+    const float* mats[4] = {mi, M1, M2, M3};
+    const int64_t lds[4] = {ldm, ld1, ld2, ld3};
+    return combo_eval_dev(h, mats, lds, r, coeffs, n_coeffs, aupr, auroc, best);
 }
 
 }  // extern "C"

@@ -36,4 +36,21 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 
 __host__ __device__ __forceinline__ int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
+// One entry of compute_combo (apps/pipeline/mcpnet_helper.hpp:507-573): the
+// denominator is summed in double in the reference's order, coefficient 1 adds
+// the value itself and coefficient 0 skips the term; explicit _rn intrinsics
+// keep nvcc from fusing the multiply-adds.  m1..m3 are only read when their
+// coefficient is non-zero.
+__device__ __forceinline__ float combo_value(float v, float m1, float m2, float m3, double a, double b, double c,
+                                             double d) {
+    double mm = 0.0;
+    if (a == 1.0) mm = __dadd_rn(mm, (double)v); else if (a != 0.0) mm = __dadd_rn(mm, __dmul_rn(a, (double)v));
+    if (b == 1.0) mm = __dadd_rn(mm, (double)m1); else if (b != 0.0) mm = __dadd_rn(mm, __dmul_rn(b, (double)m1));
+    if (c == 1.0) mm = __dadd_rn(mm, (double)m2); else if (c != 0.0) mm = __dadd_rn(mm, __dmul_rn(c, (double)m2));
+    if (d == 1.0) mm = __dadd_rn(mm, (double)m3); else if (d != 0.0) mm = __dadd_rn(mm, __dmul_rn(d, (double)m3));
+    return (fabsf(v) < 1.1920928955078125e-07f) ? 0.0f                       // FLT_EPSILON
+         : (fabs(mm) < 1.1920928955078125e-07) ? 3.4028234663852886e+38f     // FLT_MAX
+         : __double2float_rn(__ddiv_rn((double)v, mm));
+}
+
 }  // namespace mcpg

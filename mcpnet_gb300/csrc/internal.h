@@ -116,4 +116,69 @@ cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, int64_t ldw, 
                          int64_t m, int bins, int fmt, int split, float* MI, int64_t ldmi, int* timeout_flag,
                          cudaStream_t stream, int64_t* launches, int64_t gene0 = 0, int64_t gene1 = -1);
 
+// ---------------- gold-standard evaluation (eval.cu) ----------------
+enum TruthMode : int {
+    TRUTH_LOWER = 0,  // entries (i, j), j < i          select_lower_triangle
+    TRUTH_ALL = 1,    // every entry
+    TRUTH_TF = 2,     // TF rows: j != g(i), and not (g(i) > j and j is a TF)   select_tfs_from_mat
+};
+struct TruthRegion {
+    const int8_t* labels; int64_t ldl;   // 1 = positive, 0 = negative, anything else unknown
+    int64_t rows, cols;
+    int mode;
+    const int32_t* row_gene;             // TRUTH_TF: global gene index of each row (device)
+    const uint8_t* col_tf;               // TRUTH_TF: non-zero where the column gene is a TF (device)
+};
+struct GatherSrc {                       // up to four matrices gathered at the selected entries
+    int n;
+    const float* src[4]; int64_t lds[4];
+    float* dst[4];
+};
+struct ComboSrc {                        // gathered (mi, M1, M2, M3) and the combo coefficients
+    const float* g[4];
+    int64_t n;
+    double cs[4];
+};
+// Work items of a region: rows x ceil(cols / 4096) row segments.
+int64_t truth_items(const TruthRegion& r);
+// Scratch sizes (elements): scan partials for n inputs; radix-sort blocks of n keys;
+// curve partials.
+int64_t scan_tmp_elems(int64_t n);
+int64_t radix_blocks(int64_t n);
+int64_t curve_part_elems();
+// Per-item counts of positive and negative labels inside the region.
+cudaError_t launch_truth_count(const TruthRegion& r, uint32_t* cpos, uint32_t* cneg, cudaStream_t stream,
+                               int64_t* launches);
+// out[0..n) = exclusive prefix sum of in, out[n] = total (tmp: scan_tmp_elems(n)).
+cudaError_t launch_scan_u32(const uint32_t* in, int64_t n, uint64_t* out, uint64_t* tmp, cudaStream_t stream,
+                            int64_t* launches);
+// Writes, in row-major order, every selected entry labelled `lab` of the g.n
+// sources to g.dst at positions off[item] + rank (off: scanned per-item counts).
+cudaError_t launch_truth_gather(const TruthRegion& r, int lab, const uint64_t* off, const GatherSrc& g, int* nan_flag,
+                                cudaStream_t stream, int64_t* launches);
+// Order-preserving 32-bit keys of float scores (-0 as +0); NaN sets *nan_flag.
+cudaError_t launch_keys_from_floats(const float* v, int64_t n, uint32_t* keys, int* nan_flag, cudaStream_t stream,
+                                    int64_t* launches);
+cudaError_t launch_combo_keys(const ComboSrc& c, uint32_t* keys, int* nan_flag, cudaStream_t stream,
+                              int64_t* launches);
+// Ascending LSD radix sort of keys in place (alt: n keys; bh: 256*radix_blocks(n);
+// bh_off: 256*radix_blocks(n)+1; tmp: scan_tmp_elems(256*radix_blocks(n))).
+cudaError_t launch_radix_sort(uint32_t* keys, uint32_t* alt, int64_t n, uint32_t* bh, uint64_t* bh_off,
+                              uint64_t* tmp, cudaStream_t stream, int64_t* launches);
+// lt[i] / eq[i] (nX + 1 each, zeroed here) = number of Y keys whose lower_bound
+// in the sorted X is i and that are < X[i] / == X[i].  nX in [1, 2^31).
+cudaError_t launch_rank_count_matrix(const uint32_t* X, int64_t nX, const TruthRegion& r, const float* v, int64_t ldv,
+                                     int lab, uint64_t* lt, uint64_t* eq, int* nan_flag, cudaStream_t stream,
+                                     int64_t* launches);
+cudaError_t launch_rank_count_keys(const uint32_t* X, int64_t nX, const uint32_t* Y, int64_t nY, uint64_t* lt,
+                                   uint64_t* eq, cudaStream_t stream, int64_t* launches);
+cudaError_t launch_rank_count_combo(const uint32_t* X, int64_t nX, const ComboSrc& c, uint64_t* lt, uint64_t* eq,
+                                    int* nan_flag, cudaStream_t stream, int64_t* launches);
+// out[0] = sum of AUPR terms (X = positives, Y = negatives), out[1] = sum of
+// AUROC terms (#Y >= t / |Y|) (run / |X|) over the distinct thresholds t of X.
+// work: 2*nX + 1; tmp: scan_tmp_elems(nX); part: curve_part_elems().
+cudaError_t launch_curve(const uint32_t* X, int64_t nX, int64_t nY, const uint64_t* lt, const uint64_t* eq,
+                         uint64_t* work, uint64_t* tmp, double* part, unsigned* ticket, double* out,
+                         cudaStream_t stream, int64_t* launches);
+
 }  // namespace mcpg

@@ -487,17 +487,10 @@ __global__ void combo_kernel(const float* mi, int64_t ldm, const float* M1, int6
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
         const int64_t i = t / cols, j = t - i * cols;
         const float v = mi[i * ldm + j];
-        double mm = 0.0;
-        if (a == 1.0) mm = __dadd_rn(mm, (double)v); else if (a != 0.0) mm = __dadd_rn(mm, __dmul_rn(a, (double)v));
-        if (b == 1.0) mm = __dadd_rn(mm, (double)M1[i * ld1 + j]);
-        else if (b != 0.0) mm = __dadd_rn(mm, __dmul_rn(b, (double)M1[i * ld1 + j]));
-        if (c == 1.0) mm = __dadd_rn(mm, (double)M2[i * ld2 + j]);
-        else if (c != 0.0) mm = __dadd_rn(mm, __dmul_rn(c, (double)M2[i * ld2 + j]));
-        if (d == 1.0) mm = __dadd_rn(mm, (double)M3[i * ld3 + j]);
-        else if (d != 0.0) mm = __dadd_rn(mm, __dmul_rn(d, (double)M3[i * ld3 + j]));
-        out[i * ldo + j] = (fabsf(v) < FLT_EPSILON) ? 0.0f
-                         : (fabs(mm) < (double)FLT_EPSILON) ? FLT_MAX
-                         : __double2float_rn(__ddiv_rn((double)v, mm));
+        const float m1 = (b != 0.0) ? M1[i * ld1 + j] : 0.0f;
+        const float m2 = (c != 0.0) ? M2[i * ld2 + j] : 0.0f;
+        const float m3 = (d != 0.0) ? M3[i * ld3 + j] : 0.0f;
+        out[i * ldo + j] = combo_value(v, m1, m2, m3, a, b, c, d);
     }
 }
 

@@ -101,7 +101,35 @@ class _TfCompositions:
         return M, self.ratio(tg, M)
 
 
-class _Port(_TfCompositions):
+class _EvalCompositions:
+    """compute_aupr_auroc and the ensemble coefficient search composed from
+    the selection, combo and curve routines of the concrete oracle."""
+
+    REGIONS = {"lower": 0, "all": 1, "tf": 2}
+
+    def eval_truth(self, values, labels, region="lower", row_gene=None, col_tf=None):
+        """compute_aupr_auroc (apps/pipeline/mcpnet_helper.hpp:1050-1071)."""
+        pos, neg = self.select_truth(values, labels, region, row_gene, col_tf)
+        a, b = self.aupr_auroc(pos, neg)
+        return a, b, pos.size, neg.size
+
+    def combo_eval(self, mi, M1, M2, M3, labels, coeffs, region="lower", row_gene=None, col_tf=None):
+        """The coefficient loop of apps/pipeline/mcpnet.cpp:575-616."""
+        cs = np.asarray(coeffs, dtype=np.float64).reshape(-1, 4)
+        pr = np.full(cs.shape[0], np.nan)
+        roc = np.full(cs.shape[0], np.nan)
+        best, top = 0, 0.0
+        for i, c in enumerate(cs):
+            if c[0] == 1 and c[1] == 0 and c[2] == 0 and c[3] == 0:
+                continue
+            R = port().combo(mi, M1, M2, M3, c)
+            pr[i], roc[i], _, _ = self.eval_truth(R, labels, region, row_gene, col_tf)
+            if pr[i] > top:
+                top, best = pr[i], i
+        return pr, roc, best
+
+
+class _Port(_TfCompositions, _EvalCompositions):
     """The C restatement (float and double)."""
 
     def __init__(self, path: Path):
@@ -109,6 +137,12 @@ class _Port(_TfCompositions):
         for sfx in ("f32", "f64"):
             _bind(self.L, sfx, "orc_")
         self.L.orc_num_threads.restype = C.c_int
+        for name in ("orc_aupr", "orc_auroc"):
+            f = getattr(self.L, name)
+            f.restype = C.c_double
+            f.argtypes = [_vp, _i64, _vp, _i64]
+        self.L.orc_select_truth.argtypes = [_vp, _i64, _i64, _i64, _vp, _i64, C.c_int, _vp, _vp, _vp, _vp, _vp,
+                                            _vp]
 
     @staticmethod
     def _dt(a):
@@ -243,6 +277,28 @@ class _Port(_TfCompositions):
                                                         dR.ctypes.data, cols, dA.ctypes.data, cols, dM.ctypes.data,
                                                         cols)
 
+    def aupr_auroc(self, pos, neg):
+        """aupr_kernel / auroc_kernel::operator()(pos, count, neg, count), sums in double."""
+        pos = np.ascontiguousarray(pos, dtype=np.float64).ravel()
+        neg = np.ascontiguousarray(neg, dtype=np.float64).ravel()
+        return (float(self.L.orc_aupr(pos.ctypes.data, pos.size, neg.ctypes.data, neg.size)),
+                float(self.L.orc_auroc(pos.ctypes.data, pos.size, neg.ctypes.data, neg.size)))
+
+    def select_truth(self, values, labels, region="lower", row_gene=None, col_tf=None):
+        """select_lower_triangle / select_tfs_from_mat + select_values2: (pos, neg) float32, row-major."""
+        V = np.ascontiguousarray(values, dtype=np.float32)
+        Lb = np.ascontiguousarray(labels, dtype=np.int8)
+        rows, cols = V.shape
+        rg = None if row_gene is None else np.ascontiguousarray(row_gene, dtype=np.int32)
+        ct = None if col_tf is None else np.ascontiguousarray(col_tf, dtype=np.uint8)
+        pos = np.empty(rows * cols + 1, dtype=np.float32)
+        neg = np.empty(rows * cols + 1, dtype=np.float32)
+        npos, nneg = C.c_int64(0), C.c_int64(0)
+        ptr = lambda a: None if a is None else a.ctypes.data
+        self.L.orc_select_truth(V.ctypes.data, rows, cols, cols, Lb.ctypes.data, cols, self.REGIONS[region], ptr(rg),
+                                ptr(ct), pos.ctypes.data, C.byref(npos), neg.ctypes.data, C.byref(nneg))
+        return pos[:npos.value].copy(), neg[:nneg.value].copy()
+
     def closure(self, A, max_iter=64):
         A = np.ascontiguousarray(A)
         n = A.shape[0]
@@ -267,7 +323,7 @@ class _Port(_TfCompositions):
         return M, self.ratio(A, M)
 
 
-class _Ref(_TfCompositions):
+class _Ref(_TfCompositions, _EvalCompositions):
     """MCPNet's own kernels driven over whole matrices (float, plus f64 MI)."""
 
     def __init__(self, path: Path):
@@ -286,7 +342,22 @@ class _Ref(_TfCompositions):
         L.ref_maxmin_masked_f32.argtypes = [_vp, _i64, _vp, _i64, _i64, _i64, _i64, _vp, _vp, _i64]
         L.ref_dpi_tf_f32.argtypes = [_vp, _i64, _i64, C.c_float, _vp, _vp, _i64, _vp]
         L.ref_dpi_tf_f32.restype = C.c_int64
+        L.ref_aupr_auroc_f32.argtypes = [_vp, _i64, _vp, _i64, _vp]
+        L.ref_aupr_auroc_f64.argtypes = [_vp, _i64, _vp, _i64, _vp]
         self.L = L
+
+    def aupr_auroc(self, pos, neg, dtype=np.float32):
+        """MCPNet's aupr_kernel / auroc_kernel with IT = dtype, OT = double."""
+        pos = np.ascontiguousarray(pos, dtype=dtype).ravel()
+        neg = np.ascontiguousarray(neg, dtype=dtype).ravel()
+        out = np.zeros(2, dtype=np.float64)
+        f = self.L.ref_aupr_auroc_f32 if dtype == np.float32 else self.L.ref_aupr_auroc_f64
+        f(pos.ctypes.data, pos.size, neg.ctypes.data, neg.size, out.ctypes.data)
+        return float(out[0]), float(out[1])
+
+    def select_truth(self, values, labels, region="lower", row_gene=None, col_tf=None):
+        """The selection loops are app code (not compiled here): the restatement stands in."""
+        return port().select_truth(values, labels, region, row_gene, col_tf)
 
     def maxmin_masked(self, A, B, mask):
         A = np.ascontiguousarray(A, dtype=np.float32)

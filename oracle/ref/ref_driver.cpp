@@ -13,6 +13,8 @@
 //   compute_ratio         apps/pipeline/mcpnet_helper.hpp:172-184
 //   DPI mask + apply      apps/filter/dpi.cpp:236-287
 //   MCP3 symmetrisation   apps/filter/mcp.cpp:463-476
+//   AUPR / AUROC          aupr_kernel / auroc_kernel::operator()(pos, count, neg, count)
+//                         include/mcp/transform/aupr.hpp:565-584, auroc.hpp:562-579
 // The InnerProduct SYMM=true pattern is restated as "compute j >= i, mirror".
 #include <cstdint>
 #include <cstring>
@@ -25,6 +27,8 @@
 #include "mcp/filter/dpi.hpp"
 #include "mcp/filter/threshold.hpp"
 #include "mcp/transform/combine.hpp"
+#include "mcp/transform/aupr.hpp"
+#include "mcp/transform/auroc.hpp"
 
 namespace {
 
@@ -202,6 +206,21 @@ int64_t ref_dpi_tf_f32(const float* A, int64_t n, int64_t lda, float tol, const 
 // tol arrives as float, as under `--single` (apps/filter/dpi.cpp:63,69-74).
 int64_t ref_dpi_f32(const float* A, int64_t n, int64_t lda, float tol, float* out, int64_t ldo, uint8_t* mask) {
     return dpi<float>(A, n, lda, (double)tol, out, ldo, mask);
+}
+
+// AUPR and AUROC of score vectors with the reference's kernels; IT = float or
+// double comparisons, OT = double (the sums before any rounding to float).
+void ref_aupr_auroc_f32(const float* pos, int64_t np, const float* neg, int64_t nn, double* out) {
+    mcp::kernel::aupr_kernel<float, char, double> pr;
+    mcp::kernel::auroc_kernel<float, char, double> roc;
+    out[0] = pr(pos, (size_t)np, neg, (size_t)nn);
+    out[1] = roc(pos, (size_t)np, neg, (size_t)nn);
+}
+void ref_aupr_auroc_f64(const double* pos, int64_t np, const double* neg, int64_t nn, double* out) {
+    mcp::kernel::aupr_kernel<double, char, double> pr;
+    mcp::kernel::auroc_kernel<double, char, double> roc;
+    out[0] = pr(pos, (size_t)np, neg, (size_t)nn);
+    out[1] = roc(pos, (size_t)np, neg, (size_t)nn);
 }
 
 }  // extern "C"

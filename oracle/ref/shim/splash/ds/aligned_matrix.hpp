@@ -1,5 +1,6 @@
 // Stand-in for splash::ds::aligned_matrix: a row-major matrix view with the
-// three accessors MCPNet's hot-path headers call (rows, columns, data(row)).
+// accessors MCPNet's hot-path and evaluation headers call (rows, columns,
+// data(row), data(row, col), at).
 // Test infrastructure only.
 #pragma once
 #include <cstddef>
@@ -17,6 +18,8 @@ class aligned_matrix {
     size_t columns() const { return cols_; }
     T* data(size_t r) { return ptr_ + r * ld_; }
     T const* data(size_t r) const { return ptr_ + r * ld_; }
+    T* data(size_t r, size_t c) { return ptr_ + r * ld_ + c; }
+    T const* data(size_t r, size_t c) const { return ptr_ + r * ld_ + c; }
     T& at(size_t r, size_t c) { return ptr_[r * ld_ + c]; }
 };
 

@@ -8,6 +8,18 @@
 #include <cstddef>
 #include <cmath>
 #include <cassert>
+#include <chrono>
+#include <cstring>
+
+// Logging and timing used by the evaluation kernels (aupr.hpp, auroc.hpp):
+// printing is dropped, timing is a steady clock.
+#ifndef FMT_ROOT_PRINT
+#define FMT_ROOT_PRINT(...) do {} while (0)
+#endif
+inline std::chrono::steady_clock::time_point getSysTime() { return std::chrono::steady_clock::now(); }
+inline double get_duration_s(std::chrono::steady_clock::time_point a, std::chrono::steady_clock::time_point b) {
+    return std::chrono::duration<double>(b - a).count();
+}
 
 namespace splash { namespace kernel {
 
@@ -32,5 +44,8 @@ class binary_op : public kernel_counter {};
 
 template <typename IT, typename IT2, typename IT3, typename OT, DEGREE D = DEGREE::VECTOR>
 class ternary_op : public kernel_counter {};
+
+template <typename IT, typename LABEL, typename OT, DEGREE D = DEGREE::VECTOR>
+class masked_reduce : public kernel_counter {};
 
 }}

@@ -16,6 +16,15 @@ Fixtures (all float32 unless noted):
                  symmetrised MCP3), DPI_out, DPI_mask (uint8), DPI_removed, tol
   maxmin_rect.npz  A (33 x 77), B (45 x 77) with negative entries, C = A (x) B
   dpi_ties.npz   a matrix with repeated values and zeros, DPI outputs at tol 0 and 0.1
+  tf_90.npz      TF-restricted MCP / DPI / masked max-min outputs
+  eval_cases.npz AUPR / AUROC of score vectors from the reference's aupr_kernel /
+                 auroc_kernel (IT = float and IT = double, OT = double), incl.
+                 ties, +-0, empty sides and both AUROC branches
+  eval_truth.npz an MI matrix, its max-min products, int8 truth labels from the
+                 synthetic GRN, TF rows, and AUPR / AUROC of each truth region
+                 and of a coefficient table of combo scores
+
+    python tests/golden/make_golden.py --only eval   # regenerate the eval fixtures only
 """
 from __future__ import annotations
 
@@ -37,10 +46,22 @@ def synth(n, m, seed):
 
 
 def main():
+    import argparse
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--only", choices=["core", "eval"], default=None)
+    args = ap.parse_args()
     O.build(with_ref=True)
     R = O.ref()
     if R is None:
         raise SystemExit("reference kernels not built (MCPNet sources not found)")
+    if args.only != "eval":
+        core(R)
+    if args.only != "core":
+        evaluation(R)
+    print("wrote", sorted(p.name for p in HERE.glob("*.npz")))
+
+
+def core(R):
 
     # ---- MI ----
     for name, (n, m, seed, bins, order) in {
@@ -104,7 +125,80 @@ def main():
     tf["mask_general"] = general
     tf["MM_general"] = R.maxmin_masked(A, A, general)
     np.savez_compressed(HERE / "tf_90.npz", **tf)
-    print("wrote", sorted(p.name for p in HERE.glob("*.npz")))
+
+
+def eval_cases(rng):
+    """(pos, neg) float32 score vectors covering the curve code's branches."""
+    q = lambda a, k: (np.floor(a * k) / k).astype(np.float32)
+    c = []
+    c.append((rng.random(200).astype(np.float32), (rng.random(3000) * 0.8).astype(np.float32)))  # P < N
+    c.append((q(rng.random(150), 7), q(rng.random(400) * 0.9, 7)))                                # heavy ties
+    c.append((rng.random(500).astype(np.float32), (rng.random(120) * 1.2).astype(np.float32)))    # P > N
+    c.append((q(rng.random(50), 5), q(rng.random(50), 5)))                                        # P == N, ties
+    c.append((np.zeros(0, np.float32), rng.random(10).astype(np.float32)))                        # no positives
+    c.append((rng.random(10).astype(np.float32), np.zeros(0, np.float32)))                        # no negatives
+    c.append((np.zeros(0, np.float32), np.zeros(0, np.float32)))                                  # nothing
+    c.append((np.array([0.25], np.float32), np.array([0.25], np.float32)))                        # one tie
+    c.append((np.array([-0.0, 1.0, -2.5, 0.0, 3.0], np.float32),                                  # +-0, negatives
+              np.array([0.0, -0.0, -2.5, -3.0, 0.5, 1.0, 1.0], np.float32)))
+    c.append((np.full(5, 0.5, np.float32), np.full(7, 0.5, np.float32)))                          # all equal
+    c.append((rng.normal(0.3, 1.0, 1500).astype(np.float32), rng.normal(0.0, 1.0, 30000).astype(np.float32)))
+    c.append((q(rng.random(12000), 1000), q(rng.random(3000), 1000)))                             # P > N, ties
+    return c
+
+
+def evaluation(R):
+    rng = np.random.default_rng(77)
+    ev = {}
+    cases = eval_cases(rng)
+    for k, (pos, neg) in enumerate(cases):
+        ev[f"pos_{k}"], ev[f"neg_{k}"] = pos, neg
+        ev[f"ref32_{k}"] = np.array(R.aupr_auroc(pos, neg, np.float32))
+        ev[f"ref64_{k}"] = np.array(R.aupr_auroc(pos, neg, np.float64))
+    ev["ncases"] = np.int64(len(cases))
+    np.savez_compressed(HERE / "eval_cases.npz", **ev)
+
+    # ---- a truth matrix on an MI network of a synthetic GRN ----
+    import mcpnet_gb300 as M
+    n = 90
+    X, E = M.synth_grn(n, 300, seed=51, with_edges=True)
+    A = R.bspline_mi(X)
+    np.fill_diagonal(A, 0.0)
+    Lb = np.full((n, n), -1, dtype=np.int8)
+    unk = rng.random((n, n)) < 0.3
+    Lb[~unk] = 0
+    Lb = np.minimum(Lb, Lb.T)                       # symmetric, as a truth matrix
+    Lb[E[:, 0], E[:, 1]] = 1
+    Lb[E[:, 1], E[:, 0]] = 1
+    np.fill_diagonal(Lb, -1)
+    tf = rng.random(n) < 0.2
+    tf_idx = np.nonzero(tf)[0].astype(np.int32)
+    out = {"A": A, "labels": Lb, "tf_idx": tf_idx, "col_tf": tf.astype(np.uint8)}
+    for region, V, L, rg, ct in (("lower", A, Lb, None, None), ("all", A, Lb, None, None),
+                                  ("tf", A[tf_idx], Lb[tf_idx], tf_idx, tf.astype(np.uint8))):
+        pos, neg = O.port().select_truth(V, L, region, rg, ct)
+        out[f"{region}_pos"], out[f"{region}_neg"] = pos, neg
+        out[f"{region}_ref"] = np.array(R.aupr_auroc(pos, neg, np.float32))
+    M1, _ = R.mcp(A, 2)
+    M2, _ = R.mcp(A, 3)
+    M3, _ = R.mcp(A, 4)
+    out.update(M1=M1, M2=M2, M3=M3)
+    cs = np.array([[1, 0, 0, 0], [0.25, 0.25, 0.25, 0.25], [0, 1, 0, 0], [0.5, 0.5, 0, 0], [0, 0, 0, 1],
+                   [0.1, 0.2, 0.3, 0.4], [0, 0.5, 0.5, 0]], dtype=np.float64)
+    out["coeffs"] = cs
+    pr = np.full(len(cs), np.nan)
+    roc = np.full(len(cs), np.nan)
+    best, top = 0, 0.0
+    for i, c in enumerate(cs):
+        if c[0] == 1 and not c[1:].any():
+            continue
+        S = O.port().combo(A, M1, M2, M3, c)
+        pos, neg = O.port().select_truth(S, Lb, "lower")
+        pr[i], roc[i] = R.aupr_auroc(pos, neg, np.float32)
+        if pr[i] > top:
+            top, best = pr[i], i
+    out.update(combo_aupr=pr, combo_auroc=roc, combo_best=np.int64(best))
+    np.savez_compressed(HERE / "eval_truth.npz", **out)
 
 
 if __name__ == "__main__":

@@ -160,3 +160,59 @@ def test_tf_variants_bit_exact(port, golden):
     assert np.array_equal(out, g["DPI_out"]) and np.array_equal(mask, g["DPI_mask"])
     assert removed == int(g["DPI_removed"])
     assert np.array_equal(port.maxmin_masked(A, A, g["mask_general"]), g["MM_general"])
+
+
+def test_eval_cases_bit_exact(port, golden):
+    """The restated AUPR / AUROC equal MCPNet's aupr_kernel / auroc_kernel
+    bit for bit (same sequential double sums), for float and double scores."""
+    g = golden("eval_cases")
+    for k in range(int(g["ncases"])):
+        got = port.aupr_auroc(g[f"pos_{k}"], g[f"neg_{k}"])
+        assert got == tuple(g[f"ref32_{k}"]) == tuple(g[f"ref64_{k}"]), k
+
+
+def test_eval_truth_regions(port, golden):
+    g = golden("eval_truth")
+    A, L = g["A"], g["labels"]
+    ti, ct = g["tf_idx"], g["col_tf"]
+    for region, V, Lb, rg, c in (("lower", A, L, None, None), ("all", A, L, None, None),
+                                  ("tf", A[ti], L[ti], ti, ct)):
+        pos, neg = port.select_truth(V, Lb, region, rg, c)
+        assert np.array_equal(pos, g[f"{region}_pos"]) and np.array_equal(neg, g[f"{region}_neg"]), region
+        a, b, npos, nneg = port.eval_truth(V, Lb, region, rg, c)
+        assert (a, b) == tuple(g[f"{region}_ref"]), region
+        assert (npos, nneg) == (pos.size, neg.size)
+
+
+def test_eval_truth_lower_matches_reference_loop(golden):
+    """select_lower_triangle keeps (i, j) with j < i and label 0/1, row-major."""
+    g = golden("eval_truth")
+    A, L = g["A"], g["labels"]
+    n = A.shape[0]
+    pos = [A[i, j] for i in range(n) for j in range(i) if L[i, j] == 1]
+    neg = [A[i, j] for i in range(n) for j in range(i) if L[i, j] == 0]
+    assert np.array_equal(np.array(pos, np.float32), g["lower_pos"])
+    assert np.array_equal(np.array(neg, np.float32), g["lower_neg"])
+
+
+def test_combo_eval_oracle(port, golden):
+    g = golden("eval_truth")
+    pr, roc, best = port.combo_eval(g["A"], g["M1"], g["M2"], g["M3"], g["labels"], g["coeffs"])
+    np.testing.assert_array_equal(pr, g["combo_aupr"])
+    np.testing.assert_array_equal(roc, g["combo_auroc"])
+    assert best == int(g["combo_best"])
+    assert np.isnan(pr[0])  # the (1, 0, 0, 0) row is skipped
+
+
+def test_eval_against_reference_build(port):
+    """Random vectors with ties straight against MCPNet's kernels (where built)."""
+    from oracle import oracle as O
+    ref = O.ref()
+    if ref is None:
+        pytest.skip("reference kernels not built in this checkout")
+    rng = np.random.default_rng(5)
+    for _ in range(100):
+        k = int(rng.integers(1, 9))
+        pos = (rng.integers(0, 4 * k, int(rng.integers(0, 80))) / k).astype(np.float32)
+        neg = (rng.integers(0, 4 * k, int(rng.integers(0, 80))) / k - 0.2).astype(np.float32)
+        assert port.aupr_auroc(pos, neg) == ref.aupr_auroc(pos, neg)
