@@ -387,8 +387,11 @@ def pipeline_arm(args, ws, rank, local):
     """The whole MCPNet compute core once, stage by stage (the large single-GPU
     configuration: 32,768 genes x 4,096 samples by default): B-spline MI
     (tensor cores), diagonal reset, the three max-min products with the
-    MCP2/3/4 ratios fused (M1 shared), the DPI filter and optionally the
-    max-capacity closure.  Prints one JSON line with per-stage times and
+    MCP2/3/4 ratios fused (M1 shared), the DPI filter, optionally the
+    max-capacity closure, then the gold-standard evaluation (AUPR / AUROC of
+    the MI and MCP2 networks against the synthetic GRN's edges, every other
+    pair a negative) and the ensemble coefficient search over a 35-row
+    coefficient grid.  Prints one JSON line with per-stage times and
     roofline fractions, and the reference CPU path's time on the host cores
     extrapolated from timed row slabs."""
     import torch
@@ -434,9 +437,33 @@ def pipeline_arm(args, ws, rank, local):
     t_all0 = time.perf_counter()
     st["mi"] = timed(lambda: h.bspline_mi_dev(X, A, b, args.order, args.precision))
     st["diagonal"] = timed(lambda: h.set_diagonal_dev(A, 0.0))
-    st["mcp234"] = timed(lambda: h.maxmins_dev(A, R2=R2, R3=R3, R4=R4))
+    if args.no_eval:
+        st["mcp234"] = timed(lambda: h.maxmins_dev(A, R2=R2, R3=R3, R4=R4))
+    else:  # the ensemble search below needs the three products too
+        M1, M2, M3 = (torch.empty((n, n), **f32) for _ in range(3))
+        st["mcp234"] = timed(lambda: h.maxmins_dev(A, M1, M2, M3, R2=R2, R3=R3, R4=R4))
     removed = [0]
     st["dpi"] = timed(lambda: removed.__setitem__(0, h.dpi_dev(A, D, 0.1)))
+    ev = {}
+    if not args.no_eval:
+        # gold standard: the synthetic GRN's edges are positives, every other pair a negative
+        _, E = M.synth_grn(n, 1, seed=args.seed, with_edges=True)
+        Lb = torch.zeros((n, n), dtype=torch.int8, device=dev)
+        Ed = torch.from_numpy(E.astype(np.int64)).to(dev)
+        Lb[Ed[:, 0], Ed[:, 1]] = 1
+        Lb[Ed[:, 1], Ed[:, 0]] = 1
+        coeffs = np.array([(a, b_, c, 4 - a - b_ - c) for a in range(5) for b_ in range(5 - a)
+                           for c in range(5 - a - b_)], dtype=np.float64) / 4.0  # 35 rows, step 0.25
+        r = [None]
+        h.eval_truth_dev(A, Lb)  # untimed: grows the evaluation workspace to this size
+        h.combo_eval_dev(A, M1, M2, M3, Lb, coeffs[1:2])
+        st["eval_mi"] = timed(lambda: r.__setitem__(0, h.eval_truth_dev(A, Lb)))
+        ev["mi"] = r[0]
+        st["eval_mcp2"] = timed(lambda: r.__setitem__(0, h.eval_truth_dev(R2, Lb)))
+        ev["mcp2"] = r[0]
+        st["combo_search"] = timed(lambda: r.__setitem__(0, h.combo_eval_dev(A, M1, M2, M3, Lb, coeffs)))
+        ev["combo"] = r[0]
+        ev["coeffs"] = coeffs
     iters = None
     if args.closure:
         Cl = torch.empty((n, n), **f32)
@@ -474,6 +501,22 @@ def pipeline_arm(args, ws, rank, local):
         cl_ms = st["closure"] * 1e3
         stages["closure"] = {"ms": cl_ms, "iterations": iters,
                              "frac_alu_peak": 2.0 * 0.5 * n ** 3 * iters / (cl_ms / 1e3) / alu_peak}
+    if not args.no_eval:
+        npos, nneg = ev["mi"][2], ev["mi"][3]
+        lower = n * (n - 1) // 2
+        # labels read by the count, gather and rank passes over the lower triangle; every
+        # negative's and positive's score read once
+        ev_bytes = 3 * lower + 4 * (npos + nneg)
+        for key in ("eval_mi", "eval_mcp2"):
+            e_ms = st[key] * 1e3
+            stages[key] = {"ms": e_ms, "aupr": ev[key[5:]][0], "auroc": ev[key[5:]][1], "n_pos": npos,
+                           "n_neg": nneg, "GB/s": ev_bytes / (e_ms / 1e3) / 1e9,
+                           "frac_hbm": ev_bytes / (e_ms / 1e3) / hbm}
+        pr, roc, best = ev["combo"]
+        stages["combo_search"] = {"ms": st["combo_search"] * 1e3, "rows": len(ev["coeffs"]),
+                                  "ms_per_row": st["combo_search"] * 1e3 / (len(ev["coeffs"]) - 1),
+                                  "best_row": int(best), "best_coeffs": ev["coeffs"][best].tolist(),
+                                  "best_aupr": float(pr[best]), "best_auroc": float(roc[best])}
     line = {"mode": "pipeline", "genes": n, "samples": m, "precision": args.precision,
             "stage_s": st, "wall_s": wall, "stages": stages, "closure_iterations": iters, "clocks": clk,
             "kernel_profile": prof, "sms": sms}
@@ -492,8 +535,17 @@ def pipeline_arm(args, ws, rank, local):
         mm_row_s = (time.perf_counter() - t0) / rows
         cpu_mi_s = pairs / v
         cpu_mm_s = mm_row_s * n * (0.5 + 1.0 + 0.5 + 0.5)  # M1, M2, M3 as the reference's SYMM patterns + DPI bound
+        cpu_ev_s = None
+        if not args.no_eval:
+            # compute_aupr_auroc on a row slab of the lower triangle, scaled by entries
+            Lh = Lb.cpu().numpy()
+            er = min(n, 4096)
+            t0 = time.perf_counter()
+            P.eval_truth(Ah[:er], Lh[:er], "lower")
+            cpu_ev_s = (time.perf_counter() - t0) * (n * (n - 1) / 2) / (er * (er - 1) / 2)
         line["cpu_baseline"] = {"kind": sampler.kind, "cores": info["threads"],
                                 "mi_s_extrapolated": cpu_mi_s, "maxmin_dpi_s_extrapolated": cpu_mm_s,
+                                "eval_one_matrix_s_extrapolated": cpu_ev_s,
                                 "total_s_extrapolated": cpu_mi_s + cpu_mm_s,
                                 "sample": f"MI {sampler.describe(info)}; max-min rows 0..{rows} x {n} x {n} "
                                           f"({mm_row_s:.3f} s/row); DPI counted as one symmetric product "
@@ -527,6 +579,8 @@ def main(argv=None):
     ap.add_argument("--pipeline", action="store_true",
                     help="run the whole compute core once, stage by stage (defaults to 32768 x 4096)")
     ap.add_argument("--closure", action="store_true", help="with --pipeline: add the max-capacity closure")
+    ap.add_argument("--no-eval", action="store_true",
+                    help="with --pipeline: skip the gold-standard evaluation and the ensemble coefficient search")
     ap.add_argument("--cpu-genes", type=int, default=8192,
                     help="with --pipeline: genes of the CPU MI sample (its weights are built on the host)")
     args = ap.parse_args(argv)

@@ -49,8 +49,12 @@ constexpr int RS_THREADS = 256;                      // radix sort
 constexpr int RS_WARPS = RS_THREADS / 32;
 constexpr int RS_ITEMS = 16;
 constexpr int RS_TILE = RS_THREADS * RS_ITEMS;
-constexpr int RC_SKEYS = 6144;                       // keys (or splitters) of X held in shared memory
-constexpr int RC_SHIST = 2048;                       // bins kept in shared memory when |X| + 1 fits
+constexpr int RC_SKEYS = 8192;                       // keys (or splitters) of X held in shared memory
+constexpr int RC_SBINS = 4096;                       // histogram bins held in shared memory
+constexpr int RC_SLOW = 3072;                        // ... when |X| + 1 > RC_SBINS: the lowest bins
+constexpr int RC_SHIGH = RC_SBINS - RC_SLOW;         //     and the highest (scores below / above most of X)
+constexpr size_t RC_SMEM = (size_t)RC_SKEYS * 4 + (size_t)2 * RC_SBINS * 4;
+constexpr int RC_BATCH = EV_PER_THREAD;              // keys placed per thread per call
 
 __device__ __forceinline__ uint32_t order_key(float f) {
     uint32_t u = __float_as_uint(f);
@@ -356,46 +360,79 @@ struct RankCtx {
     uint64_t* lt;
     uint64_t* eq;
     const uint32_t* sk;  // shared: all of X (full) or splitters X[q * stride]
-    uint32_t* shl;       // shared histograms (shist)
+    uint32_t* shl;       // shared histogram windows (RC_SBINS bins each)
     uint32_t* she;
     int64_t stride;
+    int64_t hi0;         // first bin of the high window (bins >= hi0 map to RC_SLOW + bin - hi0)
     int nsk;
-    bool full, shist;
+    bool full;
 
+    // Shared-memory slot of a bin, or -1 for the global histogram.  Scores of
+    // the negatives of a network pile up below (or above) most positives, so
+    // the windows take the contended bins; with |X| + 1 <= RC_SBINS every bin
+    // is in shared memory.
+    __device__ __forceinline__ int slot(uint32_t bin) const {
+        if ((int64_t)bin < RC_SLOW) return (int)bin;
+        if ((int64_t)bin >= hi0) return RC_SLOW + (int)((int64_t)bin - hi0);
+        return -1;
+    }
+
+    // Places RC_BATCH keys per thread (has[j] false: no key).  The lower_bound
+    // searches run interleaved over the batch ("monobound": every key takes
+    // the same number of steps, so the loads of one step are independent).
     // Every lane of the warp calls this (ballot / match inside).
-    __device__ __forceinline__ void place(bool has, uint32_t key) const {
-        uint32_t bin = 0;
-        bool e = false;
-        if (has) {
-            int lo = 0, hi = nsk;
-            while (lo < hi) {
-                const int mid = (lo + hi) >> 1;
-                if (sk[mid] < key) lo = mid + 1; else hi = mid;
+    __device__ __forceinline__ void place(const bool (&has)[RC_BATCH], const uint32_t (&key)[RC_BATCH]) const {
+        int base[RC_BATCH];
+#pragma unroll
+        for (int j = 0; j < RC_BATCH; ++j) base[j] = 0;
+        if (nsk > 0) {
+            int n = nsk;
+            while (n > 1) {
+                const int half = n >> 1;
+#pragma unroll
+                for (int j = 0; j < RC_BATCH; ++j) base[j] = sk[base[j] + half] < key[j] ? base[j] + half : base[j];
+                n -= half;
             }
-            if (full) {
-                bin = (uint32_t)lo;
-                e = lo < nsk && sk[lo] == key;
-            } else if (lo == 0) {
-                bin = 0;
-                e = sk[0] == key;
-            } else {
-                int64_t a = (int64_t)(lo - 1) * stride + 1;
-                int64_t b = (int64_t)lo * stride < nX ? (int64_t)lo * stride : nX;
-                while (a < b) {
-                    const int64_t mid = (a + b) >> 1;
-                    if (__ldg(X + mid) < key) a = mid + 1; else b = mid;
-                }
-                bin = (uint32_t)a;
-                e = a < nX && __ldg(X + a) == key;
-            }
+#pragma unroll
+            for (int j = 0; j < RC_BATCH; ++j) base[j] += sk[base[j]] < key[j] ? 1 : 0;
         }
-        const uint32_t act = __ballot_sync(FULL, has);
-        if (has) {
-            const uint32_t peers = __match_any_sync(act, (bin << 1) | (e ? 1u : 0u));
-            if ((threadIdx.x & 31) == __ffs(peers) - 1) {
-                const uint32_t c = __popc(peers);
-                if (shist) atomicAdd(e ? she + bin : shl + bin, c);
-                else atomicAdd((unsigned long long*)(e ? eq + bin : lt + bin), (unsigned long long)c);
+        int bin[RC_BATCH];  // nX < 2^31
+        if (full) {
+#pragma unroll
+            for (int j = 0; j < RC_BATCH; ++j) bin[j] = base[j];
+        } else {
+            // the answer lies in [(q-1)*stride + 1, min(q*stride, nX)] for q = base >= 1
+            const int nx = (int)nX, st = (int)stride;
+#pragma unroll
+            for (int j = 0; j < RC_BATCH; ++j) bin[j] = base[j] > 0 ? (base[j] - 1) * st + 1 : 0;
+            int n = st - 1;
+            while (n > 1) {
+                const int half = n >> 1;
+#pragma unroll
+                for (int j = 0; j < RC_BATCH; ++j) {
+                    const int idx = bin[j] + half;
+                    const bool lt = base[j] > 0 && idx < nx && __ldg(X + idx) < key[j];
+                    bin[j] = lt ? idx : bin[j];
+                }
+                n -= half;
+            }
+#pragma unroll
+            for (int j = 0; j < RC_BATCH; ++j)
+                bin[j] += (base[j] > 0 && n == 1 && bin[j] < nx && __ldg(X + bin[j]) < key[j]) ? 1 : 0;
+        }
+#pragma unroll
+        for (int j = 0; j < RC_BATCH; ++j) {
+            const bool e = has[j] && bin[j] < (int)nX && (full ? sk[bin[j]] : __ldg(X + bin[j])) == key[j];
+            const uint32_t b = (uint32_t)bin[j];
+            const uint32_t act = __ballot_sync(FULL, has[j]);
+            if (has[j]) {
+                const uint32_t peers = __match_any_sync(act, (b << 1) | (e ? 1u : 0u));
+                if ((threadIdx.x & 31) == __ffs(peers) - 1) {
+                    const uint32_t c = __popc(peers);
+                    const int sl = slot(b);
+                    if (sl >= 0) atomicAdd(e ? she + sl : shl + sl, c);
+                    else atomicAdd((unsigned long long*)(e ? eq + b : lt + b), (unsigned long long)c);
+                }
             }
         }
     }
@@ -414,13 +451,17 @@ struct YMatrix {  // selected entries of one label in a score matrix
             if (s.c0 >= s.c1) continue;  // uniform over the block
             const int8_t* lrow = r.labels + s.row * r.ldl;
             const float* vrow = v + s.row * ldv;
-            for (int k = 0; k < EV_PER_THREAD; ++k) {
+            bool has[RC_BATCH];
+            uint32_t key[RC_BATCH];
+#pragma unroll
+            for (int k = 0; k < RC_BATCH; ++k) {  // RC_BATCH == EV_PER_THREAD: the thread's whole segment
                 const int64_t col = s.c0 + k * EV_THREADS + threadIdx.x;
-                const bool has = col < s.c1 && in_region(r, s.row, col) && lrow[col] == lab;
-                const float f = has ? vrow[col] : 0.0f;
-                bad |= has && is_nan(f);
-                c.place(has, order_key(f));
+                has[k] = col < s.c1 && in_region(r, s.row, col) && lrow[col] == lab;
+                const float f = has[k] ? vrow[col] : 0.0f;
+                bad |= has[k] && is_nan(f);
+                key[k] = order_key(f);
             }
+            c.place(has, key);
         }
         return bad;
     }
@@ -430,10 +471,17 @@ struct YKeys {  // a compact array of keys
     const uint32_t* k;
     int64_t n;
     __device__ __forceinline__ bool run(const RankCtx& c) const {
-        for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x; i0 < n; i0 += (int64_t)gridDim.x * blockDim.x) {
-            const int64_t i = i0 + threadIdx.x;
-            const bool has = i < n;
-            c.place(has, has ? k[i] : 0u);
+        const int64_t step = (int64_t)gridDim.x * EV_CHUNK;
+        for (int64_t i0 = (int64_t)blockIdx.x * EV_CHUNK; i0 < n; i0 += step) {
+            bool has[RC_BATCH];
+            uint32_t key[RC_BATCH];
+#pragma unroll
+            for (int j = 0; j < RC_BATCH; ++j) {
+                const int64_t i = i0 + j * EV_THREADS + threadIdx.x;
+                has[j] = i < n;
+                key[j] = has[j] ? k[i] : 0u;
+            }
+            c.place(has, key);
         }
         return false;
     }
@@ -443,22 +491,31 @@ struct YCombo {  // combo values of gathered (mi, M1, M2, M3) tuples
     ComboSrc s;
     __device__ __forceinline__ bool run(const RankCtx& c) const {
         bool bad = false;
-        for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x; i0 < s.n; i0 += (int64_t)gridDim.x * blockDim.x) {
-            const int64_t i = i0 + threadIdx.x;
-            const bool has = i < s.n;
-            const float f = has ? combo_at(s, i) : 0.0f;
-            bad |= has && is_nan(f);
-            c.place(has, order_key(f));
+        const int64_t step = (int64_t)gridDim.x * EV_CHUNK;
+        for (int64_t i0 = (int64_t)blockIdx.x * EV_CHUNK; i0 < s.n; i0 += step) {
+            bool has[RC_BATCH];
+            uint32_t key[RC_BATCH];
+#pragma unroll
+            for (int j = 0; j < RC_BATCH; ++j) {
+                const int64_t i = i0 + j * EV_THREADS + threadIdx.x;
+                has[j] = i < s.n;
+                const float f = has[j] ? combo_at(s, i) : 0.0f;
+                bad |= has[j] && is_nan(f);
+                key[j] = order_key(f);
+            }
+            c.place(has, key);
         }
         return bad;
     }
 };
 
 template <class Y>
-__global__ void __launch_bounds__(EV_THREADS) rank_count_kernel(const uint32_t* X, int64_t nX, Y y, uint64_t* lt,
+__global__ void __launch_bounds__(EV_THREADS, 3) rank_count_kernel(const uint32_t* X, int64_t nX, Y y, uint64_t* lt,
                                                                 uint64_t* eq, int* nan_flag) {
-    __shared__ uint32_t sk[RC_SKEYS];
-    __shared__ uint32_t shl[RC_SHIST], she[RC_SHIST];
+    extern __shared__ __align__(16) uint32_t rc_smem[];
+    uint32_t* sk = rc_smem;
+    uint32_t* shl = sk + RC_SKEYS;
+    uint32_t* she = shl + RC_SBINS;
     RankCtx c;
     c.X = X;
     c.nX = nX;
@@ -470,19 +527,18 @@ __global__ void __launch_bounds__(EV_THREADS) rank_count_kernel(const uint32_t* 
     c.full = nX <= RC_SKEYS;
     c.stride = c.full ? 1 : ceil_div(nX, RC_SKEYS);
     c.nsk = (int)(c.full ? nX : ceil_div(nX, c.stride));
-    c.shist = nX + 1 <= RC_SHIST;
+    c.hi0 = nX + 1 <= RC_SBINS ? (int64_t)RC_SLOW : nX + 1 - RC_SHIGH;
+    const int nsb = nX + 1 <= RC_SBINS ? (int)(nX + 1) : RC_SBINS;  // used slots
     for (int i = threadIdx.x; i < c.nsk; i += blockDim.x) sk[i] = X[(int64_t)i * c.stride];
-    if (c.shist)
-        for (int i = threadIdx.x; i <= nX; i += blockDim.x) shl[i] = she[i] = 0;
+    for (int i = threadIdx.x; i < RC_SBINS; i += blockDim.x) shl[i] = she[i] = 0;
     __syncthreads();
     const bool bad = y.run(c);
     if (bad) atomicOr(nan_flag, 1);
-    if (c.shist) {
-        __syncthreads();
-        for (int i = threadIdx.x; i <= nX; i += blockDim.x) {
-            if (shl[i]) atomicAdd((unsigned long long*)(lt + i), (unsigned long long)shl[i]);
-            if (she[i]) atomicAdd((unsigned long long*)(eq + i), (unsigned long long)she[i]);
-        }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nsb; i += blockDim.x) {
+        const int64_t bin = i < RC_SLOW ? i : c.hi0 + (i - RC_SLOW);
+        if (shl[i]) atomicAdd((unsigned long long*)(lt + bin), (unsigned long long)shl[i]);
+        if (she[i]) atomicAdd((unsigned long long*)(eq + bin), (unsigned long long)she[i]);
     }
 }
 
@@ -653,6 +709,22 @@ cudaError_t launch_radix_sort(uint32_t* keys, uint32_t* alt, int64_t n, uint32_t
 }
 
 static cudaError_t rank_prep(int64_t nX, uint64_t* lt, uint64_t* eq, cudaStream_t st) {
+    static uint64_t attr_done = 0;  // opt in to the 64 KB of dynamic shared memory once per device
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const uint64_t bit = 1ull << (dev & 63);
+    if (!(attr_done & bit)) {
+        cudaError_t a = cudaFuncSetAttribute(rank_count_kernel<YMatrix>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)RC_SMEM);
+        if (a == cudaSuccess)
+            a = cudaFuncSetAttribute(rank_count_kernel<YKeys>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)RC_SMEM);
+        if (a == cudaSuccess)
+            a = cudaFuncSetAttribute(rank_count_kernel<YCombo>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)RC_SMEM);
+        if (a != cudaSuccess) return a;
+        attr_done |= bit;
+    }
     cudaError_t e = cudaMemsetAsync(lt, 0, (size_t)(nX + 1) * sizeof(uint64_t), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(eq, 0, (size_t)(nX + 1) * sizeof(uint64_t), st);
     return e;
@@ -667,7 +739,7 @@ cudaError_t launch_rank_count_matrix(const uint32_t* X, int64_t nX, const TruthR
     const int64_t items = truth_items(r);
     if (items == 0) return cudaSuccess;
     YMatrix y{r, ceil_div(r.cols, EV_CHUNK), items, v, ldv, lab};
-    rank_count_kernel<YMatrix><<<grid_for(items, 1, 152 * 4), EV_THREADS, 0, st>>>(X, nX, y, lt, eq, nan_flag);
+    rank_count_kernel<YMatrix><<<grid_for(items, 1, 152 * 3), EV_THREADS, RC_SMEM, st>>>(X, nX, y, lt, eq, nan_flag);
     if (launches) ++*launches;
     return cudaGetLastError();
 }
@@ -678,7 +750,7 @@ cudaError_t launch_rank_count_keys(const uint32_t* X, int64_t nX, const uint32_t
     cudaError_t e = rank_prep(nX, lt, eq, st);
     if (e != cudaSuccess || nY <= 0) return e;
     YKeys y{Y, nY};
-    rank_count_kernel<YKeys><<<grid_for(nY, EV_CHUNK, 152 * 4), EV_THREADS, 0, st>>>(X, nX, y, lt, eq, nullptr);
+    rank_count_kernel<YKeys><<<grid_for(nY, EV_CHUNK, 152 * 3), EV_THREADS, RC_SMEM, st>>>(X, nX, y, lt, eq, nullptr);
     if (launches) ++*launches;
     return cudaGetLastError();
 }
@@ -689,7 +761,7 @@ cudaError_t launch_rank_count_combo(const uint32_t* X, int64_t nX, const ComboSr
     cudaError_t e = rank_prep(nX, lt, eq, st);
     if (e != cudaSuccess || c.n <= 0) return e;
     YCombo y{c};
-    rank_count_kernel<YCombo><<<grid_for(c.n, EV_CHUNK, 152 * 4), EV_THREADS, 0, st>>>(X, nX, y, lt, eq, nan_flag);
+    rank_count_kernel<YCombo><<<grid_for(c.n, EV_CHUNK, 152 * 3), EV_THREADS, RC_SMEM, st>>>(X, nX, y, lt, eq, nan_flag);
     if (launches) ++*launches;
     return cudaGetLastError();
 }
