@@ -256,6 +256,33 @@ MCPG_API int mcpg_closure(mcpg_handle* h, const float* A, int64_t n, int64_t lda
 MCPG_API int mcpg_closure_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, int max_iter,
                               float* out, int64_t ldo, int* iterations);
 
+/* ---- adaptive-partitioning MI (the reference's default MI method) ----
+ * compute_ap_mi (apps/pipeline/mcpnet_helper.hpp:101-164; apps/correlation/mi.cpp:119-178):
+ *   1. optional noise U[0, noise) added to every value (the apps add U[0, 1e-5)
+ *      to break ties, mi.cpp:121-131; here a seeded counter-based generator, so
+ *      the draw differs from the reference's);
+ *   2. rank transform, descending (splash::kernel::Rank<T, size_t, 0, false>;
+ *      the splash source is absent from the reference: tied values share the
+ *      lowest rank here);
+ *   3. IntegralCumulativeHistogramKernel (include/mcp/correlation/
+ *      AdaptivePartitioningMI.hpp:414-438) and AdaptivePartitionRankMIKernel2
+ *      (:443-648) for every pair j >= i, mirrored (symmetric InnerProduct).
+ * MI is n x n float (bits).  Given the same ranks the result equals the
+ * reference's kernel except where CUDA's and the C library's log2 differ in
+ * the last bit.  m <= 16384 (MCPG_ERR_UNSUPPORTED above).
+ * mcpg_ap_ranks_dev: step 1-2 only (ranks: int32, n x ldr).
+ * mcpg_ap_mi_ranks[_dev]: step 3 from caller-supplied ranks in [0, m). */
+MCPG_API int mcpg_ap_ranks_dev(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_t ldx, float noise,
+                               uint64_t seed, int32_t* R, int64_t ldr);
+MCPG_API int mcpg_ap_mi_ranks(mcpg_handle* h, const int32_t* R, int64_t n, int64_t m, int64_t ldr, float* MI,
+                              int64_t ldmi);
+MCPG_API int mcpg_ap_mi_ranks_dev(mcpg_handle* h, const int32_t* R, int64_t n, int64_t m, int64_t ldr, float* MI,
+                                  int64_t ldmi);
+MCPG_API int mcpg_ap_mi(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_t ldx, float noise,
+                        uint64_t seed, float* MI, int64_t ldmi);
+MCPG_API int mcpg_ap_mi_dev(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_t ldx, float noise,
+                            uint64_t seed, float* MI, int64_t ldmi);
+
 /* ---- gold-standard evaluation: AUPR and AUROC ----
  * mcpg_aupr_auroc: aupr_kernel::operator()(pos, pos_count, neg, neg_count)
  * (include/mcp/transform/aupr.hpp:565-584 -> average_compute_1sort, 127-236)

@@ -91,7 +91,15 @@ ABI = [
     ("mcpg_combo_eval_dev", C.c_int, [_vp, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _i64, _i64, _vp, _i64,
                                       C.c_int, _vp, _vp, _vp, _i64, _vp, _vp, _vp]),
 ]
+ABI += [
+    ("mcpg_ap_ranks_dev", C.c_int, [_vp, _vp, _i64, _i64, _i64, C.c_float, C.c_uint64, _vp, _i64]),
+    ("mcpg_ap_mi_ranks", C.c_int, [_vp, _vp, _i64, _i64, _i64, _vp, _i64]),
+    ("mcpg_ap_mi_ranks_dev", C.c_int, [_vp, _vp, _i64, _i64, _i64, _vp, _i64]),
+    ("mcpg_ap_mi", C.c_int, [_vp, _vp, _i64, _i64, _i64, C.c_float, C.c_uint64, _vp, _i64]),
+    ("mcpg_ap_mi_dev", C.c_int, [_vp, _vp, _i64, _i64, _i64, C.c_float, C.c_uint64, _vp, _i64]),
+]
 TRUTH_REGIONS = {"lower": 0, "all": 1, "tf": 2}
+AP_NOISE = 1e-5  # the reference apps' tie-breaking noise amplitude (apps/correlation/mi.cpp:128-129)
 
 _lib = None
 
@@ -465,6 +473,38 @@ class Handle:
         self._check(self._L.mcpg_combo_dev(self._h, self._dp(mi), self._ld(mi), self._dp(M1), ld(M1), self._dp(M2),
                                             ld(M2), self._dp(M3), ld(M3), rows, cols, cs.ctypes.data, self._dp(out),
                                             self._ld(out)), "combo_dev")
+
+    # ---- adaptive-partitioning MI ----
+    def ap_mi(self, X, noise: float = 0.0, seed: int = 1):
+        """compute_ap_mi: (noise) -> descending ranks -> AP MI, n x n float32 (bits)."""
+        X = _f32(X)
+        n, m = X.shape
+        MI = np.empty((n, n), dtype=np.float32)
+        self._check(self._L.mcpg_ap_mi(self._h, _ptr(X), n, m, m, noise, seed, _ptr(MI), n), "ap_mi")
+        return MI
+
+    def ap_mi_ranks(self, R):
+        """AP MI from integer ranks in [0, m) (n x m)."""
+        R = np.ascontiguousarray(R, dtype=np.int32)
+        n, m = R.shape
+        MI = np.empty((n, n), dtype=np.float32)
+        self._check(self._L.mcpg_ap_mi_ranks(self._h, _ptr(R), n, m, m, _ptr(MI), n), "ap_mi_ranks")
+        return MI
+
+    def ap_ranks_dev(self, X, R, noise: float = 0.0, seed: int = 1):
+        n, m = X.shape
+        self._check(self._L.mcpg_ap_ranks_dev(self._h, self._dp(X), n, m, self._ld(X), noise, seed, self._dp(R),
+                                               self._ld(R)), "ap_ranks_dev")
+
+    def ap_mi_dev(self, X, MI, noise: float = 0.0, seed: int = 1):
+        n, m = X.shape
+        self._check(self._L.mcpg_ap_mi_dev(self._h, self._dp(X), n, m, self._ld(X), noise, seed, self._dp(MI),
+                                            self._ld(MI)), "ap_mi_dev")
+
+    def ap_mi_ranks_dev(self, R, MI):
+        n, m = R.shape
+        self._check(self._L.mcpg_ap_mi_ranks_dev(self._h, self._dp(R), n, m, self._ld(R), self._dp(MI),
+                                                  self._ld(MI)), "ap_mi_ranks_dev")
 
     # ---- gold-standard evaluation ----
     def aupr_auroc(self, pos, neg):

@@ -62,6 +62,8 @@ enum Slot {
     S_EV_GN,     // evaluation: gathered negative (mi, M1, M2, M3)
     S_EV_LAB,    // evaluation: staged labels
     S_EV_AUX,    // evaluation: staged row_gene / col_tf
+    S_AP_R,      // AP MI: int32 ranks
+    S_AP_TAB,    // AP MI: uint16 ranks, order and cumulative histograms
     NSLOTS
 };
 
@@ -1291,6 +1293,75 @@ int combo_eval_dev(mcpg_handle* h, const float* const mats[4], const int64_t lds
     return MCPG_OK;
 }
 
+// ---- adaptive-partitioning MI ----
+int ap_check(mcpg_handle* h, int64_t n, int64_t m, const void* in, int64_t ld, const float* MI, int64_t ldmi) {
+    if (n < 0 || m < 0) return fail(h, MCPG_ERR_ARG, "ap_mi: negative size");
+    if (n > 0 && m > 0 && (!in || ld < m)) return fail(h, MCPG_ERR_ARG, "ap_mi: null input or leading dimension");
+    if (n > 0 && (!MI || ldmi < n)) return fail(h, MCPG_ERR_ARG, "ap_mi: null output or leading dimension");
+    if (m > mcpg::ap_max_samples())
+        return fail(h, MCPG_ERR_UNSUPPORTED, "ap_mi: at most %lld samples", (long long)mcpg::ap_max_samples());
+    if (n > 0 && m == 0) return fail(h, MCPG_ERR_ARG, "ap_mi: no samples");
+    return MCPG_OK;
+}
+
+int ap_flag_check(mcpg_handle* h, int* dflag) {
+    int f = 0;
+    CK(h, cudaMemcpyAsync(&f, dflag, sizeof(int), cudaMemcpyDeviceToHost, h->stream), "device-to-host copy");
+    CK(h, cudaStreamSynchronize(h->stream), "stream synchronize");
+    if (f & 1) return fail(h, MCPG_ERR_ARG, "ap_mi: NaN value or rank outside [0, m)");
+    if (f & 2) return fail(h, MCPG_ERR_CUDA, "ap_mi: window walk out of bounds (internal error)");
+    return MCPG_OK;
+}
+
+int ap_mi_from_ranks(mcpg_handle* h, const int32_t* R, int64_t n, int64_t m, int64_t ldr, float* MI, int64_t ldmi,
+                     int* flag, unsigned* counter) {
+    const int64_t ldc = round_up(m + 1, 8);
+    void* tab;
+    int rc = scratch(h, S_AP_TAB, (size_t)(n * (2 * m + ldc)) * 2, &tab);
+    if (rc) return rc;
+    uint16_t* xr = (uint16_t*)tab;
+    uint16_t* order = xr + n * m;
+    uint16_t* cH = order + n * m;
+    {
+        PROF(h, "ap_prep");
+        CK(h, mcpg::launch_ap_prep(R, n, m, ldr, xr, order, cH, ldc, flag, h->stream, &h->launches), "ap prep");
+    }
+    {
+        PROF(h, "ap_mi");
+        CK(h, mcpg::launch_ap_mi(xr, order, cH, ldc, n, m, MI, ldmi, counter, flag, h->stream, &h->launches),
+           "ap mi");
+    }
+    return ap_flag_check(h, flag);
+}
+
+int ap_small(mcpg_handle* h, int** flag, unsigned** counter) {
+    void* p;
+    int rc = scratch(h, S_SMALL, 64, &p);
+    if (rc) return rc;
+    *flag = (int*)p;
+    *counter = (unsigned*)((char*)p + 16);
+    CK(h, cudaMemsetAsync(p, 0, 64, h->stream), "memset");
+    return MCPG_OK;
+}
+
+int ap_mi_dev(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_t ldx, float noise, uint64_t seed, float* MI,
+              int64_t ldmi) {
+    int rc = ap_check(h, n, m, X, ldx, MI, ldmi);
+    if (rc || n == 0) return rc;
+    if (!(noise >= 0.0f)) return fail(h, MCPG_ERR_ARG, "ap_mi: noise amplitude must be >= 0");
+    int* flag;
+    unsigned* counter;
+    if ((rc = ap_small(h, &flag, &counter))) return rc;
+    void* r;
+    if ((rc = scratch(h, S_AP_R, (size_t)(n * m) * 4, &r))) return rc;
+    {
+        PROF(h, "ap_ranks");
+        CK(h, mcpg::launch_ap_ranks(X, n, m, ldx, noise, seed, (int32_t*)r, m, flag, h->stream, &h->launches),
+           "ap ranks");
+    }
+    return ap_mi_from_ranks(h, (const int32_t*)r, n, m, m, MI, ldmi, flag, counter);
+}
+
 }  // namespace
 
 // =====================================================================
@@ -1997,6 +2068,80 @@ int mcpg_combo_eval_dev(mcpg_handle* h, const float* mi, int64_t ldm, const floa
     const float* mats[4] = {mi, M1, M2, M3};
     const int64_t lds[4] = {ldm, ld1, ld2, ld3};
     return combo_eval_dev(h, mats, lds, r, coeffs, n_coeffs, aupr, auroc, best);
+}
+
+int mcpg_ap_ranks_dev(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_t ldx, float noise, uint64_t seed,
+                      int32_t* R, int64_t ldr) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (n < 0 || m < 0) return fail(h, MCPG_ERR_ARG, "ap_ranks: negative size");
+    if (n == 0 || m == 0) return MCPG_OK;
+    if (!X || !R || ldx < m || ldr < m) return fail(h, MCPG_ERR_ARG, "ap_ranks: null pointer or leading dimension");
+    if (m > mcpg::ap_max_samples())
+        return fail(h, MCPG_ERR_UNSUPPORTED, "ap_ranks: at most %lld samples", (long long)mcpg::ap_max_samples());
+    if (!(noise >= 0.0f)) return fail(h, MCPG_ERR_ARG, "ap_ranks: noise amplitude must be >= 0");
+    int* flag;
+    unsigned* counter;
+    if ((rc = ap_small(h, &flag, &counter))) return rc;
+    {
+        PROF(h, "ap_ranks");
+        CK(h, mcpg::launch_ap_ranks(X, n, m, ldx, noise, seed, R, ldr, flag, h->stream, &h->launches), "ap ranks");
+    }
+    return ap_flag_check(h, flag);
+}
+
+int mcpg_ap_mi_ranks_dev(mcpg_handle* h, const int32_t* R, int64_t n, int64_t m, int64_t ldr, float* MI,
+                         int64_t ldmi) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if ((rc = ap_check(h, n, m, R, ldr, MI, ldmi)) || n == 0) return rc;
+    int* flag;
+    unsigned* counter;
+    if ((rc = ap_small(h, &flag, &counter))) return rc;
+    return ap_mi_from_ranks(h, R, n, m, ldr, MI, ldmi, flag, counter);
+}
+
+int mcpg_ap_mi_ranks(mcpg_handle* h, const int32_t* R, int64_t n, int64_t m, int64_t ldr, float* MI, int64_t ldmi) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if ((rc = ap_check(h, n, m, R, ldr, MI, ldmi)) || n == 0) return rc;
+    void* r;
+    if ((rc = scratch(h, S_AP_R, (size_t)(n * m) * 4, &r))) return rc;
+    CK(h, cudaMemcpy2DAsync(r, (size_t)m * 4, R, (size_t)ldr * 4, (size_t)m * 4, (size_t)n, cudaMemcpyHostToDevice,
+                            h->stream),
+       "host-to-device copy");
+    float* dmi;
+    int64_t ldd;
+    if ((rc = stage_out_alloc(h, S_OUT0, n, n, &dmi, &ldd))) return rc;
+    int* flag;
+    unsigned* counter;
+    if ((rc = ap_small(h, &flag, &counter))) return rc;
+    if ((rc = ap_mi_from_ranks(h, (const int32_t*)r, n, m, m, dmi, ldd, flag, counter))) return rc;
+    if ((rc = copy_out(h, MI, ldmi, dmi, ldd, n, n))) return rc;
+    return finish(h);
+}
+
+int mcpg_ap_mi_dev(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_t ldx, float noise, uint64_t seed,
+                   float* MI, int64_t ldmi) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    return ap_mi_dev(h, X, n, m, ldx, noise, seed, MI, ldmi);
+}
+
+int mcpg_ap_mi(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_t ldx, float noise, uint64_t seed, float* MI,
+               int64_t ldmi) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if ((rc = ap_check(h, n, m, X, ldx, MI, ldmi)) || n == 0) return rc;
+    float* dx;
+    int64_t lx;
+    if ((rc = stage_in(h, S_IN0, X, ldx, n, m, &dx, &lx))) return rc;
+    float* dmi;
+    int64_t ldd;
+    if ((rc = stage_out_alloc(h, S_OUT0, n, n, &dmi, &ldd))) return rc;
+    if ((rc = ap_mi_dev(h, dx, n, m, lx, noise, seed, dmi, ldd))) return rc;
+    if ((rc = copy_out(h, MI, ldmi, dmi, ldd, n, n))) return rc;
+    return finish(h);
 }
 
 }  // extern "C"

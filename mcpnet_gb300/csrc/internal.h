@@ -181,4 +181,21 @@ cudaError_t launch_curve(const uint32_t* X, int64_t nX, int64_t nY, const uint64
                          uint64_t* work, uint64_t* tmp, double* part, unsigned* ticket, double* out,
                          cudaStream_t stream, int64_t* launches);
 
+// ---------------- adaptive-partitioning MI (apmi.cu) ----------------
+int64_t ap_max_samples();
+// Descending ranks of each gene's samples (ties share the lowest rank), after
+// adding U[0, noise) to every value when noise > 0 (seeded, counter-based).
+// *flag |= 1 on a NaN.
+cudaError_t launch_ap_ranks(const float* X, int64_t n, int64_t m, int64_t ldx, float noise, uint64_t seed,
+                            int32_t* R, int64_t ldr, int* flag, cudaStream_t stream, int64_t* launches);
+// Ranks -> uint16 ranks (n x m), samples ordered by rank (n x m) and cumulative
+// histograms (n x ldc, m + 1 used).  *flag |= 1 on a rank outside [0, m).
+cudaError_t launch_ap_prep(const int32_t* R, int64_t n, int64_t m, int64_t ldr, uint16_t* xr, uint16_t* order,
+                           uint16_t* cH, int64_t ldc, int* flag, cudaStream_t stream, int64_t* launches);
+// Symmetric AP MI (float) from the prepared rank tables; next_i: device counter.
+// *flag |= 2 if a pair's window walk broke its bounds (the entry is NaN).
+cudaError_t launch_ap_mi(const uint16_t* xr, const uint16_t* order, const uint16_t* cH, int64_t ldc, int64_t n,
+                         int64_t m, float* MI, int64_t ldmi, unsigned* next_i, int* flag, cudaStream_t stream,
+                         int64_t* launches);
+
 }  // namespace mcpg

@@ -144,3 +144,115 @@ void orc_select_truth(const float* V, int64_t rows, int64_t cols, int64_t ldv, c
     *np = p;
     *nn = q;
 }
+
+/* ---------------- adaptive-partitioning MI ----------------
+ * Rank transform: stands in for splash::kernel::Rank<T, size_t, 0, false>
+ * (apps/pipeline/mcpnet_helper.hpp:122-131), whose source is not in the
+ * reference snapshot: descending order (the largest value gets rank 0), tied
+ * values share the lowest rank of their group.  Parity of this step is
+ * unpinned; the MI below is pinned against the reference's own kernels given
+ * the ranks. */
+typedef struct { float v; int64_t i; } orc_vi;
+static int orc_cmp_desc(const void* a, const void* b) {
+    const orc_vi* x = (const orc_vi*)a;
+    const orc_vi* y = (const orc_vi*)b;
+    if (x->v > y->v) return -1;
+    if (x->v < y->v) return 1;
+    return (x->i > y->i) - (x->i < y->i);
+}
+void orc_ranks_desc(const float* X, int64_t n, int64_t m, int64_t ldx, int64_t* R) {
+#pragma omp parallel for schedule(static)
+    for (int64_t g = 0; g < n; ++g) {
+        orc_vi* t = (orc_vi*)malloc((size_t)(m > 0 ? m : 1) * sizeof(orc_vi));
+        for (int64_t s = 0; s < m; ++s) {
+            t[s].v = X[g * ldx + s];
+            t[s].i = s;
+        }
+        qsort(t, (size_t)m, sizeof(orc_vi), orc_cmp_desc);
+        int64_t head = 0;
+        for (int64_t p = 0; p < m; ++p) {
+            if (p > 0 && t[p].v != t[p - 1].v) head = p;
+            R[g * m + t[p].i] = head;
+        }
+        free(t);
+    }
+}
+
+/* One pair of AdaptivePartitionRankMIKernel2::operator() (AdaptivePartitioningMI.hpp:535-648)
+ * with x-ranks grouped by y-rank as _createSparseMatrix (:461-491) builds them.
+ * cx / cy: cumulative rank histograms (IntegralCumulativeHistogramKernel, :414-438):
+ * c[k] = number of samples with rank < k, k = 0..m. */
+typedef struct { int64_t x1, y1, x2, y2, npts; int whole; } orc_win;
+
+static double orc_ap_term(const int64_t* cx, const int64_t* cy, const orc_win* w) {
+    /* compute_for_window (:518-531) */
+    const int64_t nx = cx[w->x2] - cx[w->x1], ny = cy[w->y2] - cy[w->y1];
+    return (double)w->npts * log2((double)w->npts / (double)(nx * ny));
+}
+
+static double orc_ap_pair(const int64_t* rx, const int64_t* ry, const int64_t* cx, const int64_t* cy, int64_t m,
+                          int64_t* xg, int64_t* fill, orc_win* stack) {
+    for (int64_t k = 0; k <= m; ++k) fill[k] = 0;
+    for (int64_t s = 0; s < m; ++s) xg[cy[ry[s]] + fill[ry[s]]++] = rx[s];
+    int64_t top = 0;
+    stack[top++] = (orc_win){0, 0, m, m, m, 1};
+    double mi = 0.0;
+    while (top > 0) {
+        orc_win w = stack[top - 1];
+        const int64_t mx = (w.x1 + w.x2) >> 1, my = (w.y1 + w.y2) >> 1;
+        orc_win sub[4] = {{w.x1, w.y1, mx, my, 0, 0}, {mx, w.y1, w.x2, my, 0, 0},
+                          {w.x1, my, mx, w.y2, 0, 0}, {mx, my, w.x2, w.y2, 0, 0}};
+        for (int q = 0; q < 4; ++q) { /* _getNumPointsInWindow (:493-516) */
+            orc_win* s = &sub[q];
+            if (s->x1 >= s->x2 || s->y1 >= s->y2) continue;
+            if (cx[s->x2] - cx[s->x1] == 0 || cy[s->y2] - cy[s->y1] == 0) continue;
+            for (int64_t k = cy[s->y1]; k < cy[s->y2]; ++k) s->npts += (xg[k] >= s->x1 && xg[k] < s->x2);
+        }
+        const double e = (double)w.npts / 4.0;
+        double chi = 0.0;
+        for (int q = 0; q < 4; ++q) {
+            const double d = (double)sub[q].npts - e;
+            chi += d * d;
+        }
+        chi /= e;
+        --top; /* the window is consumed either way */
+        if (chi > 7.815 || w.whole) {
+            for (int q = 0; q < 4; ++q) {
+                const orc_win* s = &sub[q];
+                const int split = ((s->x1 + 1) < s->x2 || (s->y1 + 1) < s->y2) && s->npts > 2;
+                if (split) stack[top++] = *s;
+                else if (s->npts > 0) mi += orc_ap_term(cx, cy, s);
+            }
+        } else if (w.npts > 0) {
+            mi += orc_ap_term(cx, cy, &w);
+        }
+    }
+    return mi / (double)m + log2((double)m);
+}
+
+void orc_ap_mi(const int64_t* R, int64_t n, int64_t m, float* out, int64_t ldo) {
+    int64_t* C = (int64_t*)calloc((size_t)(n * (m + 1)), sizeof(int64_t));
+    for (int64_t g = 0; g < n; ++g) {
+        int64_t* c = C + g * (m + 1);
+        for (int64_t s = 0; s < m; ++s) ++c[R[g * m + s] + 1];
+        for (int64_t k = 1; k <= m; ++k) c[k] += c[k - 1];
+    }
+#pragma omp parallel
+    {
+        int64_t* xg = (int64_t*)malloc((size_t)(m + 1) * sizeof(int64_t));
+        int64_t* fill = (int64_t*)malloc((size_t)(m + 1) * sizeof(int64_t));
+        orc_win* stack = (orc_win*)malloc((size_t)(4 * 64 + 4 * m + 8) * sizeof(orc_win));
+#pragma omp for schedule(dynamic, 1)
+        for (int64_t i = 0; i < n; ++i)
+            for (int64_t j = i; j < n; ++j) {
+                const float v = (float)orc_ap_pair(R + i * m, R + j * m, C + i * (m + 1), C + j * (m + 1), m, xg,
+                                                   fill, stack);
+                out[i * ldo + j] = v;
+                out[j * ldo + i] = v;
+            }
+        free(xg);
+        free(fill);
+        free(stack);
+    }
+    free(C);
+}

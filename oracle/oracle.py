@@ -143,6 +143,8 @@ class _Port(_TfCompositions, _EvalCompositions):
             f.argtypes = [_vp, _i64, _vp, _i64]
         self.L.orc_select_truth.argtypes = [_vp, _i64, _i64, _i64, _vp, _i64, C.c_int, _vp, _vp, _vp, _vp, _vp,
                                             _vp]
+        self.L.orc_ranks_desc.argtypes = [_vp, _i64, _i64, _i64, _vp]
+        self.L.orc_ap_mi.argtypes = [_vp, _i64, _i64, _vp, _i64]
 
     @staticmethod
     def _dt(a):
@@ -284,6 +286,22 @@ class _Port(_TfCompositions, _EvalCompositions):
         return (float(self.L.orc_aupr(pos.ctypes.data, pos.size, neg.ctypes.data, neg.size)),
                 float(self.L.orc_auroc(pos.ctypes.data, pos.size, neg.ctypes.data, neg.size)))
 
+    def ap_ranks(self, X):
+        """Descending ranks per gene, ties sharing the lowest rank (int64, n x m)."""
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        n, m = X.shape
+        R = np.empty((n, m), dtype=np.int64)
+        self.L.orc_ranks_desc(X.ctypes.data, n, m, m, R.ctypes.data)
+        return R
+
+    def ap_mi(self, R):
+        """AP MI (AdaptivePartitionRankMIKernel2, symmetric) from integer ranks, float32."""
+        R = np.ascontiguousarray(R, dtype=np.int64)
+        n, m = R.shape
+        out = np.empty((n, n), dtype=np.float32)
+        self.L.orc_ap_mi(R.ctypes.data, n, m, out.ctypes.data, n)
+        return out
+
     def select_truth(self, values, labels, region="lower", row_gene=None, col_tf=None):
         """select_lower_triangle / select_tfs_from_mat + select_values2: (pos, neg) float32, row-major."""
         V = np.ascontiguousarray(values, dtype=np.float32)
@@ -343,6 +361,7 @@ class _Ref(_TfCompositions, _EvalCompositions):
         L.ref_dpi_tf_f32.argtypes = [_vp, _i64, _i64, C.c_float, _vp, _vp, _i64, _vp]
         L.ref_dpi_tf_f32.restype = C.c_int64
         L.ref_aupr_auroc_f32.argtypes = [_vp, _i64, _vp, _i64, _vp]
+        L.ref_ap_mi_f32.argtypes = [_vp, _i64, _i64, _vp, _i64]
         L.ref_aupr_auroc_f64.argtypes = [_vp, _i64, _vp, _i64, _vp]
         self.L = L
 
@@ -354,6 +373,14 @@ class _Ref(_TfCompositions, _EvalCompositions):
         f = self.L.ref_aupr_auroc_f32 if dtype == np.float32 else self.L.ref_aupr_auroc_f64
         f(pos.ctypes.data, pos.size, neg.ctypes.data, neg.size, out.ctypes.data)
         return float(out[0]), float(out[1])
+
+    def ap_mi(self, R):
+        """MCPNet's IntegralCumulativeHistogramKernel + AdaptivePartitionRankMIKernel2 on given ranks."""
+        R = np.ascontiguousarray(R, dtype=np.int64)
+        n, m = R.shape
+        out = np.empty((n, n), dtype=np.float32)
+        self.L.ref_ap_mi_f32(R.ctypes.data, n, m, out.ctypes.data, n)
+        return out
 
     def select_truth(self, values, labels, region="lower", row_gene=None, col_tf=None):
         """The selection loops are app code (not compiled here): the restatement stands in."""

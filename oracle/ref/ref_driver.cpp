@@ -13,6 +13,8 @@
 //   compute_ratio         apps/pipeline/mcpnet_helper.hpp:172-184
 //   DPI mask + apply      apps/filter/dpi.cpp:236-287
 //   MCP3 symmetrisation   apps/filter/mcp.cpp:463-476
+//   AP MI (ranks given)   IntegralCumulativeHistogramKernel + AdaptivePartitionRankMIKernel2,
+//                         as apps/pipeline/mcpnet_helper.hpp:136-163 (InnerProduct SYMM)
 //   AUPR / AUROC          aupr_kernel / auroc_kernel::operator()(pos, count, neg, count)
 //                         include/mcp/transform/aupr.hpp:565-584, auroc.hpp:562-579
 // The InnerProduct SYMM=true pattern is restated as "compute j >= i, mirror".
@@ -29,6 +31,7 @@
 #include "mcp/transform/combine.hpp"
 #include "mcp/transform/aupr.hpp"
 #include "mcp/transform/auroc.hpp"
+#include "mcp/correlation/AdaptivePartitioningMI.hpp"
 
 namespace {
 
@@ -221,6 +224,27 @@ void ref_aupr_auroc_f64(const double* pos, int64_t np, const double* neg, int64_
     mcp::kernel::auroc_kernel<double, char, double> roc;
     out[0] = pr(pos, (size_t)np, neg, (size_t)nn);
     out[1] = roc(pos, (size_t)np, neg, (size_t)nn);
+}
+
+// Adaptive-partitioning MI from integer ranks (n x m, ranks in [0, m)) with the
+// reference's cumulative-histogram and MI kernels; out[i][j] = out[j][i] for
+// j >= i computed as kernel(i, j), as the symmetric InnerProduct does.
+void ref_ap_mi_f32(const int64_t* ranks, int64_t n, int64_t m, float* out, int64_t ldo) {
+    std::vector<size_t> R((size_t)(n * m)), H((size_t)(n * (m + 1)), 0);
+    for (int64_t i = 0; i < n * m; ++i) R[(size_t)i] = (size_t)ranks[i];
+    mcp::kernel::IntegralCumulativeHistogramKernel<size_t, 0> hist;
+    for (int64_t i = 0; i < n; ++i) hist(R.data() + i * m, (size_t)m, H.data() + i * (m + 1));
+#pragma omp parallel
+    {
+        mcp::kernel::AdaptivePartitionRankMIKernel2<size_t, float, 0> k(H.data(), (size_t)(m + 1) * sizeof(size_t));
+#pragma omp for schedule(dynamic, 1)
+        for (int64_t i = 0; i < n; ++i)
+            for (int64_t j = i; j < n; ++j) {
+                float v = k((size_t)i, (size_t)j, R.data() + i * m, R.data() + j * m, (size_t)m);
+                out[i * ldo + j] = v;
+                out[j * ldo + i] = v;
+            }
+    }
 }
 
 }  // extern "C"

@@ -16,6 +16,9 @@
 #ifndef FMT_ROOT_PRINT
 #define FMT_ROOT_PRINT(...) do {} while (0)
 #endif
+#ifndef FMT_PRINT_RT
+#define FMT_PRINT_RT(...) do {} while (0)
+#endif
 inline std::chrono::steady_clock::time_point getSysTime() { return std::chrono::steady_clock::now(); }
 inline double get_duration_s(std::chrono::steady_clock::time_point a, std::chrono::steady_clock::time_point b) {
     return std::chrono::duration<double>(b - a).count();

@@ -20,6 +20,9 @@ Fixtures (all float32 unless noted):
   eval_cases.npz AUPR / AUROC of score vectors from the reference's aupr_kernel /
                  auroc_kernel (IT = float and IT = double, OT = double), incl.
                  ties, +-0, empty sides and both AUROC branches
+  ap_mi.npz      adaptive-partitioning MI from the reference's own kernels
+                 (IntegralCumulativeHistogramKernel + AdaptivePartitionRankMIKernel2)
+                 on ranks of synthetic expression (with and without ties; tiny m)
   eval_truth.npz an MI matrix, its max-min products, int8 truth labels from the
                  synthetic GRN, TF rows, and AUPR / AUROC of each truth region
                  and of a coefficient table of combo scores
@@ -48,16 +51,18 @@ def synth(n, m, seed):
 def main():
     import argparse
     ap = argparse.ArgumentParser()
-    ap.add_argument("--only", choices=["core", "eval"], default=None)
+    ap.add_argument("--only", choices=["core", "eval", "ap"], default=None)
     args = ap.parse_args()
     O.build(with_ref=True)
     R = O.ref()
     if R is None:
         raise SystemExit("reference kernels not built (MCPNet sources not found)")
-    if args.only != "eval":
+    if args.only in (None, "core"):
         core(R)
-    if args.only != "core":
+    if args.only in (None, "eval"):
         evaluation(R)
+    if args.only in (None, "ap"):
+        ap_mi(R)
     print("wrote", sorted(p.name for p in HERE.glob("*.npz")))
 
 
@@ -199,6 +204,23 @@ def evaluation(R):
             top, best = pr[i], i
     out.update(combo_aupr=pr, combo_auroc=roc, combo_best=np.int64(best))
     np.savez_compressed(HERE / "eval_truth.npz", **out)
+
+
+def ap_mi(R):
+    import mcpnet_gb300 as M
+    P = O.port()
+    out = {}
+    cases = {"g40x300": M.synth_grn(40, 300, seed=61), "g24x1000": M.synth_grn(24, 1000, seed=62),
+             "g9x7": M.synth_grn(9, 7, seed=63), "g5x3": M.synth_grn(5, 3, seed=64),
+             "g4x1": M.synth_grn(4, 1, seed=65), "g6x2": M.synth_grn(6, 2, seed=66),
+             "ties15x80": (np.round(np.random.default_rng(67).random((15, 80)) * 6) / 6).astype(np.float32)}
+    for name, X in cases.items():
+        Rk = P.ap_ranks(X)
+        out[f"{name}_X"] = X
+        out[f"{name}_R"] = Rk.astype(np.int32)
+        out[f"{name}_MI"] = R.ap_mi(Rk)
+    out["names"] = np.array(sorted(cases))
+    np.savez_compressed(HERE / "ap_mi.npz", **out)
 
 
 if __name__ == "__main__":

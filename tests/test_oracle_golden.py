@@ -216,3 +216,21 @@ def test_eval_against_reference_build(port):
         pos = (rng.integers(0, 4 * k, int(rng.integers(0, 80))) / k).astype(np.float32)
         neg = (rng.integers(0, 4 * k, int(rng.integers(0, 80))) / k - 0.2).astype(np.float32)
         assert port.aupr_auroc(pos, neg) == ref.aupr_auroc(pos, neg)
+
+
+def test_ap_mi_bit_exact(port, golden):
+    """The AP MI restatement equals MCPNet's IntegralCumulativeHistogramKernel +
+    AdaptivePartitionRankMIKernel2 bit for bit, given the ranks (which come
+    from the oracle's rank transform: the reference's own lives in the absent
+    splash module)."""
+    g = golden("ap_mi")
+    for name in g["names"]:
+        R = port.ap_ranks(g[f"{name}_X"])
+        assert np.array_equal(R, g[f"{name}_R"]), name
+        mi = port.ap_mi(R)
+        assert np.array_equal(mi.view(np.uint32), g[f"{name}_MI"].view(np.uint32)), name
+
+
+def test_ap_ranks_ties_share_lowest(port):
+    X = np.array([[0.5, 0.9, 0.5, 0.1, 0.9, -0.0, 0.0]], dtype=np.float32)
+    assert port.ap_ranks(X).tolist() == [[2, 0, 2, 4, 0, 5, 5]]
