@@ -146,6 +146,9 @@ MCPG_API int mcpg_mcp_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda
 MCPG_API int mcpg_maxmins_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, float* M1, int64_t ld1,
                               float* M2, int64_t ld2, float* M3, int64_t ld3, float* R2, int64_t ldr2, float* R3,
                               int64_t ldr3, float* R4, int64_t ldr4);
+MCPG_API int mcpg_maxmins(mcpg_handle* h, const float* A, int64_t n, int64_t lda, float* M1, int64_t ld1,
+                          float* M2, int64_t ld2, float* M3, int64_t ld3, float* R2, int64_t ldr2, float* R3,
+                          int64_t ldr3, float* R4, int64_t ldr4);
 
 /* ---- ensemble combination (compute_combo, mcpnet_helper.hpp:507-573) ----
  * out = mi / (c0 mi + c1 M1 + c2 M2 + c3 M3), the combination summed in
@@ -156,6 +159,9 @@ MCPG_API int mcpg_maxmins_dev(mcpg_handle* h, const float* A, int64_t n, int64_t
 MCPG_API int mcpg_combo_dev(mcpg_handle* h, const float* mi, int64_t ldm, const float* M1, int64_t ld1,
                             const float* M2, int64_t ld2, const float* M3, int64_t ld3, int64_t rows, int64_t cols,
                             const double* coeffs, float* out, int64_t ldo);
+MCPG_API int mcpg_combo(mcpg_handle* h, const float* mi, int64_t ldm, const float* M1, int64_t ld1,
+                        const float* M2, int64_t ld2, const float* M3, int64_t ld3, int64_t rows, int64_t cols,
+                        const double* coeffs, float* out, int64_t ldo);
 
 /* ---- DPI filter ----
  * dpi_kernel<float> (include/mcp/filter/dpi.hpp:42-69) over all (x, z), then
@@ -355,6 +361,12 @@ MCPG_API int mcpg_combo_eval_dev(mcpg_handle* h, const float* mi, int64_t ldm, c
                                  int64_t cols, const int8_t* labels, int64_t ldl, int region, const int32_t* row_gene,
                                  const uint8_t* col_tf, const double* coeffs, int64_t n_coeffs, double* aupr,
                                  double* auroc, int64_t* best);
+/* Host-buffer form of mcpg_combo_eval_dev (matrices, labels, row_gene and col_tf on the host). */
+MCPG_API int mcpg_combo_eval(mcpg_handle* h, const float* mi, int64_t ldm, const float* M1, int64_t ld1,
+                             const float* M2, int64_t ld2, const float* M3, int64_t ld3, int64_t rows, int64_t cols,
+                             const int8_t* labels, int64_t ldl, int region, const int32_t* row_gene,
+                             const uint8_t* col_tf, const double* coeffs, int64_t n_coeffs, double* aupr,
+                             double* auroc, int64_t* best);
 
 /* ---- B-spline MI without any device allocation (no counterpart in the reference) ----
  * For callers that cannot call cudaMalloc -- an application whose device

@@ -11,6 +11,11 @@
 //   compute_mcp2/3/4(g2g, dmcp)           mcpnet_helper.hpp:199-206, 271-278, 358-365
 //   dpi_filter(input, tol, out)           apps/filter/dpi.cpp:236-287
 //   set_diagonal(m, value)                apps/pipeline/mcpnet.cpp:299-308
+//   compute_ap_mi(input, dmi, add_noise)  mcpnet_helper.hpp:101-164   (adaptive-partitioning MI)
+//   compute_maxmins(g2g, m1, m2, m3)      mcpnet_helper.hpp:437-460
+//   compute_combo(mi, m1, m2, m3, c, out) mcpnet_helper.hpp:507-573
+//   compute_aupr_auroc(truth, values)     mcpnet_helper.hpp:1050-1071 (AUPR returned, AUROC too)
+//   select_combo(...)                     the coefficient loop of apps/pipeline/mcpnet.cpp:575-616
 //
 // Matrices are float, row-major with a leading dimension (the layout of
 // splash::ds::aligned_matrix<float> with its padded column_bytes()).  Errors
@@ -176,6 +181,79 @@ inline int max_capacity_closure(Context& ctx, const Matrix<float>& a, Matrix<flo
     ctx.check(mcpg_closure(ctx.handle(), a.data(), n, a.ld(), max_iter, out.data(), out.ld(), &it),
               "max_capacity_closure");
     return it;
+}
+
+// compute_ap_mi: optional U[0, 1e-5) noise (the reference adds it: add_noise = true),
+// descending ranks, adaptive-partitioning MI in bits.  dmi is resized to n x n.
+inline void compute_ap_mi(Context& ctx, const Matrix<float>& input, Matrix<float>& dmi, bool add_noise = false,
+                          uint64_t seed = 1) {
+    const int64_t n = input.rows(), m = input.columns();
+    dmi.resize(n, n);
+    ctx.check(mcpg_ap_mi(ctx.handle(), input.data(), n, m, input.ld(), add_noise ? 1e-5f : 0.0f, seed, dmi.data(),
+                         dmi.ld()),
+              "compute_ap_mi");
+}
+
+// compute_maxmins: M1 = A (x) A, M2 = A (x) M1, M3 = M1 (x) M1.
+inline void compute_maxmins(Context& ctx, const Matrix<float>& g2g, Matrix<float>& m1, Matrix<float>& m2,
+                            Matrix<float>& m3) {
+    const int64_t n = g2g.rows();
+    m1.resize(n, n);
+    m2.resize(n, n);
+    m3.resize(n, n);
+    ctx.check(mcpg_maxmins(ctx.handle(), g2g.data(), n, g2g.ld(), m1.data(), m1.ld(), m2.data(), m2.ld(), m3.data(),
+                           m3.ld(), nullptr, 0, nullptr, 0, nullptr, 0),
+              "compute_maxmins");
+}
+
+// compute_combo: out = mi / (c0 mi + c1 m1 + c2 m2 + c3 m3) (coefficients as doubles).
+inline void compute_combo(Context& ctx, const Matrix<float>& mi, const Matrix<float>& m1, const Matrix<float>& m2,
+                          const Matrix<float>& m3, const double coeffs[4], Matrix<float>& out) {
+    out.resize(mi.rows(), mi.columns());
+    ctx.check(mcpg_combo(ctx.handle(), mi.data(), mi.ld(), m1.data(), m1.ld(), m2.data(), m2.ld(), m3.data(), m3.ld(),
+                         mi.rows(), mi.columns(), coeffs, out.data(), out.ld()),
+              "compute_combo");
+}
+
+// Truth labels for evaluation: 1 = positive, 0 = negative, anything else unknown.
+enum class TruthRegion : int { LowerTriangle = MCPG_TRUTH_LOWER, All = MCPG_TRUTH_ALL, TFRows = MCPG_TRUTH_TF };
+
+struct Curves {
+    double aupr = 0.0, auroc = 0.0;
+    int64_t n_pos = 0, n_neg = 0;
+};
+
+// compute_aupr_auroc over the labelled entries of `values` (same shape as labels).
+inline Curves compute_aupr_auroc(Context& ctx, const Matrix<int8_t>& labels, const Matrix<float>& values,
+                                 TruthRegion region = TruthRegion::LowerTriangle,
+                                 const std::vector<int32_t>* row_gene = nullptr,
+                                 const std::vector<uint8_t>* col_tf = nullptr) {
+    if (labels.rows() != values.rows() || labels.columns() != values.columns())
+        throw Error(MCPG_ERR_ARG, "compute_aupr_auroc: labels and values differ in shape");
+    Curves c;
+    ctx.check(mcpg_eval_truth(ctx.handle(), values.data(), values.rows(), values.columns(), values.ld(), labels.data(),
+                              labels.ld(), (int)region, row_gene ? row_gene->data() : nullptr,
+                              col_tf ? col_tf->data() : nullptr, &c.aupr, &c.auroc, &c.n_pos, &c.n_neg),
+              "compute_aupr_auroc");
+    return c;
+}
+
+// The ensemble coefficient search: AUPR / AUROC of every coefficient row
+// (n x 4, row-major) and the reference's choice of row.
+inline int64_t select_combo(Context& ctx, const Matrix<float>& mi, const Matrix<float>& m1, const Matrix<float>& m2,
+                            const Matrix<float>& m3, const Matrix<int8_t>& labels, const std::vector<double>& coeffs,
+                            std::vector<double>* aupr = nullptr, std::vector<double>* auroc = nullptr,
+                            TruthRegion region = TruthRegion::LowerTriangle) {
+    const int64_t nc = (int64_t)(coeffs.size() / 4);
+    std::vector<double> a((size_t)nc), b((size_t)nc);
+    int64_t best = 0;
+    ctx.check(mcpg_combo_eval(ctx.handle(), mi.data(), mi.ld(), m1.data(), m1.ld(), m2.data(), m2.ld(), m3.data(),
+                              m3.ld(), mi.rows(), mi.columns(), labels.data(), labels.ld(), (int)region, nullptr,
+                              nullptr, coeffs.data(), nc, a.data(), b.data(), &best),
+              "select_combo");
+    if (aupr) *aupr = a;
+    if (auroc) *auroc = b;
+    return best;
 }
 
 }  // namespace mcpgpu

@@ -98,6 +98,12 @@ ABI += [
     ("mcpg_ap_mi", C.c_int, [_vp, _vp, _i64, _i64, _i64, C.c_float, C.c_uint64, _vp, _i64]),
     ("mcpg_ap_mi_dev", C.c_int, [_vp, _vp, _i64, _i64, _i64, C.c_float, C.c_uint64, _vp, _i64]),
 ]
+ABI += [
+    ("mcpg_maxmins", C.c_int, [_vp, _vp, _i64, _i64] + [_vp, _i64] * 6),
+    ("mcpg_combo", C.c_int, [_vp, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _i64, _i64, _vp, _vp, _i64]),
+    ("mcpg_combo_eval", C.c_int, [_vp, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _i64, _i64, _vp, _i64,
+                                  C.c_int, _vp, _vp, _vp, _i64, _vp, _vp, _vp]),
+]
 TRUTH_REGIONS = {"lower": 0, "all": 1, "tf": 2}
 AP_NOISE = 1e-5  # the reference apps' tie-breaking noise amplitude (apps/correlation/mi.cpp:128-129)
 
@@ -505,6 +511,47 @@ class Handle:
         n, m = R.shape
         self._check(self._L.mcpg_ap_mi_ranks_dev(self._h, self._dp(R), n, m, self._ld(R), self._dp(MI),
                                                   self._ld(MI)), "ap_mi_ranks_dev")
+
+    def maxmins(self, A, want=("M1", "M2", "M3", "R2", "R3", "R4")):
+        """compute_maxmins with the MCP2/3/4 ratios: dict of the requested n x n outputs."""
+        A = _f32(A)
+        n = A.shape[0]
+        names = ("M1", "M2", "M3", "R2", "R3", "R4")
+        out = {k: np.empty((n, n), dtype=np.float32) for k in names if k in want}
+        args = []
+        for k in names:
+            args += [_ptr(out.get(k)), n]
+        self._check(self._L.mcpg_maxmins(self._h, _ptr(A), n, n, *args), "maxmins")
+        return out
+
+    def combo(self, mi, M1, M2, M3, coeffs):
+        """compute_combo on host matrices (Mk may be None when its coefficient is 0)."""
+        mi = _f32(mi)
+        rows, cols = mi.shape
+        cs = np.ascontiguousarray(coeffs, dtype=np.float64)
+        keep = [None if x is None else _f32(x) for x in (M1, M2, M3)]
+        out = np.empty((rows, cols), dtype=np.float32)
+        self._check(self._L.mcpg_combo(self._h, _ptr(mi), cols, _ptr(keep[0]), cols, _ptr(keep[1]), cols,
+                                        _ptr(keep[2]), cols, rows, cols, cs.ctypes.data, _ptr(out), cols), "combo")
+        return out
+
+    def combo_eval(self, mi, M1, M2, M3, labels, coeffs, region="lower", row_gene=None, col_tf=None):
+        """Host form of combo_eval_dev: (aupr ndarray, auroc ndarray, best row)."""
+        mi = _f32(mi)
+        rows, cols = mi.shape
+        keep = [None if x is None else _f32(x) for x in (M1, M2, M3)]
+        labels = np.ascontiguousarray(labels, dtype=np.int8)
+        cs = np.ascontiguousarray(np.asarray(coeffs, dtype=np.float64).reshape(-1, 4))
+        rg = None if row_gene is None else np.ascontiguousarray(row_gene, dtype=np.int32)
+        ct = None if col_tf is None else np.ascontiguousarray(col_tf, dtype=np.uint8)
+        a = np.empty(cs.shape[0], dtype=np.float64)
+        b = np.empty(cs.shape[0], dtype=np.float64)
+        best = C.c_int64(0)
+        self._check(self._L.mcpg_combo_eval(self._h, _ptr(mi), cols, _ptr(keep[0]), cols, _ptr(keep[1]), cols,
+                                             _ptr(keep[2]), cols, rows, cols, _ptr(labels), cols,
+                                             TRUTH_REGIONS[region], _ptr(rg), _ptr(ct), cs.ctypes.data, cs.shape[0],
+                                             _ptr(a), _ptr(b), C.byref(best)), "combo_eval")
+        return a, b, best.value
 
     # ---- gold-standard evaluation ----
     def aupr_auroc(self, pos, neg):

@@ -1,29 +1,43 @@
 // mcpgpu_cli -- C++ host program mirroring MCPNet's `mi`, `mcp`, `dpi` and
 // `mcpnet` apps for the GPU method, over the mcpgpu C ABI (include/mcpgpu.hpp).
 //
-//   mcpgpu_cli mi     -i expr.exp -o mi.exp [-b 10] [-l 3] [-m 2]
+//   mcpgpu_cli mi     -i expr.exp -o mi.exp [-m 1] [-b 10] [-l 3] [--seed S]
 //   mcpgpu_cli mcp    -i mi.exp -o mcp.exp -m {1,2,3} [--diagonal 0] [-x maxmin.exp]
 //   mcpgpu_cli dpi    -i mi.exp -o dpi.exp [-l 0.1] [--diagonal 0]     (diagonal 0 by default)
-//   mcpgpu_cli mcpnet -i expr.exp -o prefix [--mi-method 2] [-m 1 2 3] [--diagonal 0]
-//   mcpgpu_cli convert -i a.exp -o b.bin          (no GPU needed)
+//   mcpgpu_cli mcpnet -i expr.exp -o prefix [--mi-method 1] [--mi-input] [-m 1 2 3 4] [-f coeffs.exp]
+//                     [--eval (-g truth.txt | -x truth.exp)] [--diagonal 0] [--seed S]
+//   mcpgpu_cli convert -i a.exp -o b.csv          (no GPU needed)
 //
 // Method values keep the reference's numbering and add the GPU forms:
-//   MI  (`mi -m`, `mcpnet --mi-method`): 0 = B-spline (the reference's CPU
-//       method; here the FP32 GPU path), 2 = B-spline on tensor cores, BF16 hi+lo
-//       split (default), 3 = BF16, 4 = FP16, 5 = FP16 hi+lo.
-//   MCP (`mcp -m`, `mcpnet -m`): 1 = MCP2, 2 = MCP3, 3 = MCP4, as
-//       apps/filter/mcp.cpp:62-66 and apps/pipeline/mcpnet.cpp:63-68.
+//   MI  (`mi -m`, `mcpnet --mi-method`): 0 = B-spline (the reference's method;
+//       here the FP32 GPU path), 1 = adaptive partitioning (the reference's
+//       default; U[0, 1e-5) tie-breaking noise added first, as mi.cpp:121-131 and
+//       mcpnet.cpp:293 do), 2 = B-spline on tensor cores, BF16 hi+lo split,
+//       3 = BF16, 4 = FP16, 5 = FP16 hi+lo.
+//   MCP (`mcp -m`, `mcpnet -m`): 1 = MCP2, 2 = MCP3, 3 = MCP4 (apps/filter/mcp.cpp:62-66),
+//       and for mcpnet 4 = ensemble MCP (apps/pipeline/mcpnet.cpp:63-68, 519-719
+//       without the Stouffer variant).
+// mcpnet outputs follow apps/pipeline/mcpnet.cpp: <prefix>_{bs|ap|inmi}.mi.<ext>,
+// .mcp2/.mcp3/.mcp4.<ext>, and for the ensemble .mcp_<c0>_<c1>_<c2>_<c3>.<ext>
+// (coefficients with three decimals) -- every coefficient row without --eval,
+// the row of highest AUPR with it.  <ext> is the input's (exp, csv or bin).
+// --eval prints `Computed,auprroc,<name>,<aupr>,<auroc>` per evaluated matrix:
+//   -g list of "source target label" lines (label 1 / 0 / other = unknown):
+//      the listed pairs of known genes, source != target (select_from_list);
+//   -x label matrix (same gene order as the input): entries below the
+//      diagonal (select_lower_triangle, mcpnet_helper.hpp:862-891).
 // Matrix files: EXP (tab-separated "Id Alias <samples>" header, rows
-// "<gene> --- <values>", the reference's text format, data/r10c10.exp) or raw
-// binary ".bin" (int64 rows, int64 cols, float32 row-major).  Genes are rows;
-// a samples-by-genes EXP is not transposed (as the reference does when the
-// header names match) -- pass genes as rows.
+// "<gene> --- <values>", the reference's text format, data/r10c10.exp), CSV
+// (the same columns separated by commas; the Alias column is optional when
+// reading) or raw binary ".bin" (int64 rows, int64 cols, float32 row-major).
+// Genes are rows.
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
 #include <iostream>
+#include <map>
 #include <sstream>
 #include <string>
 #include <vector>
@@ -43,6 +57,23 @@ bool ends_with(const std::string& s, const std::string& e) {
     return s.size() >= e.size() && s.compare(s.size() - e.size(), e.size(), e) == 0;
 }
 
+std::string ext_of(const std::string& path) {
+    if (ends_with(path, ".bin")) return ".bin";
+    if (ends_with(path, ".csv")) return ".csv";
+    return ".exp";
+}
+
+std::vector<std::string> split(const std::string& line, char sep) {
+    std::vector<std::string> out;
+    std::stringstream ss(line);
+    std::string tok;
+    while (std::getline(ss, tok, sep)) {
+        if (!tok.empty() && tok.back() == '\r') tok.pop_back();
+        out.push_back(tok);
+    }
+    return out;
+}
+
 Named read_matrix(const std::string& path) {
     Named r;
     if (ends_with(path, ".bin")) {
@@ -59,34 +90,27 @@ Named read_matrix(const std::string& path) {
         for (int64_t j = 0; j < cols; ++j) r.cols.push_back(std::to_string(j));
         return r;
     }
+    const char sep = ends_with(path, ".csv") ? ',' : '\t';
     std::ifstream f(path);
     if (!f) throw std::runtime_error("cannot open " + path);
     std::string line;
     if (!std::getline(f, line)) throw std::runtime_error("empty file " + path);
-    {
-        std::stringstream ss(line);
-        std::string tok;
-        std::getline(ss, tok, '\t');  // Id
-        std::getline(ss, tok, '\t');  // Alias
-        while (std::getline(ss, tok, '\t')) r.cols.push_back(tok);
-    }
+    std::vector<std::string> head = split(line, sep);
+    const bool alias = head.size() >= 2 && head[1] == "Alias";
+    const size_t skip = alias ? 2 : 1;
+    for (size_t k = skip; k < head.size(); ++k) r.cols.push_back(head[k]);
     std::vector<float> vals;
     while (std::getline(f, line)) {
-        if (line.empty()) continue;
-        std::stringstream ss(line);
-        std::string tok;
-        std::getline(ss, tok, '\t');
-        r.rows.push_back(tok);
-        std::getline(ss, tok, '\t');  // alias
-        size_t c = 0;
-        while (std::getline(ss, tok, '\t')) {
-            vals.push_back(std::strtof(tok.c_str(), nullptr));
-            ++c;
-        }
-        if (c != r.cols.size()) throw std::runtime_error("row " + r.rows.back() + " has the wrong number of values");
+        if (line.empty() || line == "\r") continue;
+        std::vector<std::string> tok = split(line, sep);
+        if (tok.size() != r.cols.size() + skip)
+            throw std::runtime_error("row " + (tok.empty() ? std::string("?") : tok[0]) + " of " + path +
+                                     " has the wrong number of values");
+        r.rows.push_back(tok[0]);
+        for (size_t k = skip; k < tok.size(); ++k) vals.push_back(std::strtof(tok[k].c_str(), nullptr));
     }
     r.m = Matrix<float>((int64_t)r.rows.size(), (int64_t)r.cols.size());
-    std::memcpy(r.m.data(), vals.data(), vals.size() * sizeof(float));
+    if (!vals.empty()) std::memcpy(r.m.data(), vals.data(), vals.size() * sizeof(float));
     return r;
 }
 
@@ -101,26 +125,28 @@ void write_matrix(const std::string& path, const Matrix<float>& m, const std::ve
         if (!f) throw std::runtime_error("cannot write " + path);
         return;
     }
+    const char sep = ends_with(path, ".csv") ? ',' : '\t';
     std::FILE* f = std::fopen(path.c_str(), "w");
     if (!f) throw std::runtime_error("cannot write " + path);
-    std::fprintf(f, "Id\tAlias");
+    std::fprintf(f, "Id%cAlias", sep);
     for (int64_t j = 0; j < m.columns(); ++j)
-        std::fprintf(f, "\t%s", j < (int64_t)cols.size() ? cols[(size_t)j].c_str() : std::to_string(j).c_str());
+        std::fprintf(f, "%c%s", sep, j < (int64_t)cols.size() ? cols[(size_t)j].c_str() : std::to_string(j).c_str());
     std::fprintf(f, "\n");
     for (int64_t i = 0; i < m.rows(); ++i) {
-        std::fprintf(f, "%s\t---", i < (int64_t)rows.size() ? rows[(size_t)i].c_str() : std::to_string(i).c_str());
-        for (int64_t j = 0; j < m.columns(); ++j) std::fprintf(f, "\t%.9g", (double)m.at(i, j));
+        std::fprintf(f, "%s%c---", i < (int64_t)rows.size() ? rows[(size_t)i].c_str() : std::to_string(i).c_str(), sep);
+        for (int64_t j = 0; j < m.columns(); ++j) std::fprintf(f, "%c%.9g", sep, (double)m.at(i, j));
         std::fprintf(f, "\n");
     }
     std::fclose(f);
 }
 
 struct Args {
-    std::string cmd, in, out, maxmin_out;
-    int bins = 10, order = 3, mi_method = 2;
+    std::string cmd, in, out, maxmin_out, coeffs, truth_list, truth_mat;
+    int bins = 10, order = 3, mi_method = 1;
     std::vector<int> methods;
     float diagonal = 0.0f, tol = 0.1f;
-    bool order_set = false, diagonal_set = false;
+    uint64_t seed = 1;
+    bool diagonal_set = false, mi_input = false, eval = false;
 };
 
 Args parse(int argc, char** argv) {
@@ -136,40 +162,126 @@ Args parse(int argc, char** argv) {
         if (k == "-i" || k == "--input") a.in = next();
         else if (k == "-o" || k == "--output") a.out = next();
         else if (k == "-b" || k == "--bins") a.bins = std::atoi(next().c_str());
-        else if (k == "--spline_order") { a.order = std::atoi(next().c_str()); a.order_set = true; }
+        else if (k == "--spline_order") a.order = std::atoi(next().c_str());
         else if (k == "-l" || k == "--tolerance") {
             std::string v = next();
-            if (a.cmd == "mi") { a.order = std::atoi(v.c_str()); a.order_set = true; }  // mi -l = spline order
+            if (a.cmd == "mi") a.order = std::atoi(v.c_str());  // mi -l = spline order
             else a.tol = std::strtof(v.c_str(), nullptr);
         } else if (k == "--mi-method") a.mi_method = std::atoi(next().c_str());
+        else if (k == "--mi-input") a.mi_input = true;
         else if (k == "-m" || k == "--method") {
             a.methods.push_back(std::atoi(next().c_str()));
             while (i + 1 < argc && argv[i + 1][0] != '-') a.methods.push_back(std::atoi(argv[++i]));
         } else if (k == "--diagonal") {
             a.diagonal = std::strtof(next().c_str(), nullptr);
             a.diagonal_set = true;
-        }
-        else if (k == "-x" || k == "--maxmin-output") a.maxmin_out = next();
+        } else if (k == "-x") {
+            if (a.cmd == "mcp") a.maxmin_out = next();  // mcp -x = max-min output
+            else a.truth_mat = next();                  // mcpnet -x = truth matrix
+        } else if (k == "--maxmin-output") a.maxmin_out = next();
+        else if (k == "--groundtruth-matrix") a.truth_mat = next();
+        else if (k == "-g" || k == "--groundtruth-list") a.truth_list = next();
+        else if (k == "-f" || k == "--coefficients") a.coeffs = next();
+        else if (k == "--eval") a.eval = true;
+        else if (k == "--seed") a.seed = std::strtoull(next().c_str(), nullptr, 10);
         else throw std::runtime_error("unknown option " + k);
     }
     if (a.in.empty() || a.out.empty()) throw std::runtime_error("-i and -o are required");
+    if (a.eval && a.truth_list.empty() == a.truth_mat.empty())
+        throw std::runtime_error("--eval needs exactly one of -g (truth list) and -x (truth matrix)");
     return a;
-}
-
-mcpgpu::MIPrecision mi_precision(int method) {
-    switch (method) {
-        case 0: return mcpgpu::MIPrecision::FP32;
-        case 2: return mcpgpu::MIPrecision::BF16X3;
-        case 3: return mcpgpu::MIPrecision::BF16;
-        case 4: return mcpgpu::MIPrecision::FP16;
-        case 5: return mcpgpu::MIPrecision::FP16X3;
-        default: throw std::runtime_error("unsupported MI method " + std::to_string(method) +
-                                          " (0 = B-spline FP32, 2..5 = tensor-core forms)");
-    }
 }
 
 double now_s() {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// MI by method number; returns the output-name tag of the method.
+std::string compute_mi(mcpgpu::Context& ctx, const Named& in, int method, int bins, int order, uint64_t seed,
+                       Matrix<float>& mi) {
+    switch (method) {
+        case 0: mcpgpu::compute_mi(ctx, in.m, bins, mi, mcpgpu::MIPrecision::FP32, order); return "_bs";
+        case 1: mcpgpu::compute_ap_mi(ctx, in.m, mi, true, seed); return "_ap";
+        case 2: mcpgpu::compute_mi(ctx, in.m, bins, mi, mcpgpu::MIPrecision::BF16X3, order); return "_bs";
+        case 3: mcpgpu::compute_mi(ctx, in.m, bins, mi, mcpgpu::MIPrecision::BF16, order); return "_bs";
+        case 4: mcpgpu::compute_mi(ctx, in.m, bins, mi, mcpgpu::MIPrecision::FP16, order); return "_bs";
+        case 5: mcpgpu::compute_mi(ctx, in.m, bins, mi, mcpgpu::MIPrecision::FP16X3, order); return "_bs";
+        default:
+            throw std::runtime_error("unsupported MI method " + std::to_string(method) +
+                                     " (0 = B-spline FP32, 1 = adaptive partitioning, 2..5 = tensor-core B-spline)");
+    }
+}
+
+// Truth labels over the gene x gene matrix and the region they are read from.
+struct Truth {
+    Matrix<int8_t> labels;
+    mcpgpu::TruthRegion region = mcpgpu::TruthRegion::LowerTriangle;
+};
+
+Truth read_truth(const Args& a, const std::vector<std::string>& genes) {
+    Truth t;
+    const int64_t n = (int64_t)genes.size();
+    t.labels = Matrix<int8_t>(n, n);
+    for (int64_t i = 0; i < n; ++i)
+        for (int64_t j = 0; j < n; ++j) t.labels.at(i, j) = -1;
+    if (!a.truth_list.empty()) {  // read_groundtruth + select_from_list (mcpnet_helper.hpp:641-668, 840-859)
+        std::map<std::string, int64_t> id;
+        for (int64_t i = 0; i < n; ++i) id[genes[(size_t)i]] = i;
+        std::ifstream f(a.truth_list);
+        if (!f) throw std::runtime_error("cannot open " + a.truth_list);
+        std::string s, d;
+        int g;
+        while (f >> s >> d >> g) {
+            if (s == d) continue;
+            auto is = id.find(s), it = id.find(d);
+            if (is == id.end() || it == id.end()) continue;
+            t.labels.at(is->second, it->second) = (int8_t)((g == 1 || g == 0) ? g : -1);
+        }
+        t.region = mcpgpu::TruthRegion::All;
+    } else {
+        Named m = read_matrix(a.truth_mat);
+        if (m.m.rows() != n || m.m.columns() != n)
+            throw std::runtime_error("truth matrix is " + std::to_string(m.m.rows()) + " x " +
+                                     std::to_string(m.m.columns()) + ", expected " + std::to_string(n) + " x " +
+                                     std::to_string(n));
+        for (int64_t i = 0; i < n; ++i)
+            for (int64_t j = 0; j < n; ++j) {
+                const float v = m.m.at(i, j);
+                t.labels.at(i, j) = (int8_t)(v == 1.0f ? 1 : v == 0.0f ? 0 : -1);
+            }
+        t.region = mcpgpu::TruthRegion::LowerTriangle;
+    }
+    return t;
+}
+
+void report(mcpgpu::Context& ctx, const Truth& t, const Matrix<float>& values, const std::string& name) {
+    mcpgpu::Curves c = mcpgpu::compute_aupr_auroc(ctx, t.labels, values, t.region);
+    std::printf("Computed,auprroc,%s,%.12g,%.12g,pos=%lld,neg=%lld\n", name.c_str(), c.aupr, c.auroc,
+                (long long)c.n_pos, (long long)c.n_neg);
+}
+
+std::string coeff_tag(const double* c) {
+    char b[128];
+    std::snprintf(b, sizeof b, "%.3f_%.3f_%.3f_%.3f", c[0], c[1], c[2], c[3]);
+    return b;
+}
+
+std::vector<double> read_coeffs(const std::string& path) {
+    std::vector<double> cs;
+    if (path.empty()) return {0.25, 0.25, 0.25, 0.25};  // mcpnet.cpp:533-539
+    if (ends_with(path, ".exp") || ends_with(path, ".csv") || ends_with(path, ".bin")) {
+        Named m = read_matrix(path);
+        if (m.m.columns() != 4) throw std::runtime_error("coefficient file must have 4 columns");
+        for (int64_t i = 0; i < m.m.rows(); ++i)
+            for (int64_t j = 0; j < 4; ++j) cs.push_back(m.m.at(i, j));
+        return cs;
+    }
+    std::ifstream f(path);  // plain text: 4 numbers per row
+    if (!f) throw std::runtime_error("cannot open " + path);
+    double v;
+    while (f >> v) cs.push_back(v);
+    if (cs.empty() || cs.size() % 4) throw std::runtime_error("coefficient file must hold rows of 4 numbers");
+    return cs;
 }
 
 }  // namespace
@@ -185,9 +297,9 @@ int main(int argc, char** argv) {
         }
         mcpgpu::Context ctx(0);
         if (a.cmd == "mi") {
-            int method = a.methods.empty() ? 2 : a.methods[0];
+            int method = a.methods.empty() ? 1 : a.methods[0];
             Matrix<float> mi;
-            mcpgpu::compute_mi(ctx, in.m, a.bins, mi, mi_precision(method), a.order);
+            compute_mi(ctx, in, method, a.bins, a.order, a.seed, mi);
             std::printf("Computed,MI,,%.6f,sec\n", now_s() - t0);
             write_matrix(a.out, mi, in.rows, in.rows);
         } else if (a.cmd == "mcp") {
@@ -207,20 +319,62 @@ int main(int argc, char** argv) {
             std::printf("Mask removing %lld elements \n", (long long)removed);
             write_matrix(a.out, out, in.rows, in.rows);
         } else if (a.cmd == "mcpnet") {
+            const std::string ext = ext_of(a.in);
+            const std::vector<std::string>& genes = in.rows;
+            Truth truth;
+            if (a.eval) truth = read_truth(a, genes);
             Matrix<float> mi;
-            mcpgpu::compute_mi(ctx, in.m, a.bins, mi, mi_precision(a.mi_method), 3);
-            std::printf("Computed,MI,,%.6f,sec\n", now_s() - t0);
-            write_matrix(a.out + "_bs.mi" + (ends_with(a.in, ".bin") ? ".bin" : ".exp"), mi, in.rows, in.rows);
-            mcpgpu::set_diagonal(mi, a.diagonal);
+            std::string prefix = a.out;
+            if (a.mi_input) {
+                if (in.m.rows() != in.m.columns()) throw std::runtime_error("--mi-input needs a square MI matrix");
+                mi = in.m;
+                prefix += "_inmi";
+            } else {
+                prefix += compute_mi(ctx, in, a.mi_method, a.bins, a.order, a.seed, mi);
+                std::printf("Computed,MI,,%.6f,sec\n", now_s() - t0);
+                write_matrix(prefix + ".mi" + ext, mi, genes, genes);
+            }
+            mcpgpu::set_diagonal(mi, a.diagonal);  // mcpnet.cpp:299-308 (negative: keep)
+            if (a.eval) report(ctx, truth, mi, "mi");
             std::vector<int> ms = a.methods.empty() ? std::vector<int>{1} : a.methods;
             for (int method : ms) {
-                if (method < 1 || method > 3) throw std::runtime_error("mcpnet -m accepts 1, 2, 3");
+                if (method < 1 || method > 4) throw std::runtime_error("mcpnet -m accepts 1, 2, 3, 4");
                 double t1 = now_s();
-                Matrix<float> ratio;
-                mcpgpu::compute_mcp(ctx, mi, method + 1, ratio);
-                std::printf("Computed,MCP%d,,%.6f,sec\n", method + 1, now_s() - t1);
-                write_matrix(a.out + "_bs.mcp" + std::to_string(method + 1) + (ends_with(a.in, ".bin") ? ".bin" : ".exp"),
-                             ratio, in.rows, in.rows);
+                if (method <= 3) {
+                    Matrix<float> ratio;
+                    mcpgpu::compute_mcp(ctx, mi, method + 1, ratio);
+                    std::printf("Computed,MCP%d,,%.6f,sec\n", method + 1, now_s() - t1);
+                    if (a.eval) report(ctx, truth, ratio, "mcp" + std::to_string(method + 1));
+                    write_matrix(prefix + ".mcp" + std::to_string(method + 1) + ext, ratio, genes, genes);
+                    continue;
+                }
+                // ensemble MCP (mcpnet.cpp:519-719)
+                std::vector<double> cs = read_coeffs(a.coeffs);
+                Matrix<float> m1, m2, m3, combo;
+                mcpgpu::compute_maxmins(ctx, mi, m1, m2, m3);
+                std::printf("Computed,MAXMIN 1 2 3,,%.6f,sec\n", now_s() - t1);
+                const int64_t nc = (int64_t)(cs.size() / 4);
+                if (a.eval) {
+                    std::vector<double> pr, roc;
+                    int64_t best = mcpgpu::select_combo(ctx, mi, m1, m2, m3, truth.labels, cs, &pr, &roc,
+                                                        truth.region);
+                    for (int64_t c = 0; c < nc; ++c)
+                        if (pr[(size_t)c] == pr[(size_t)c])  // rows (1,0,0,0) are skipped (NaN)
+                            std::printf("Computed,Combo AUPR %.12g,(%s),AUROC %.12g\n", pr[(size_t)c],
+                                        coeff_tag(&cs[(size_t)(4 * c)]).c_str(), roc[(size_t)c]);
+                    const double* c = &cs[(size_t)(4 * best)];
+                    mcpgpu::compute_combo(ctx, mi, m1, m2, m3, c, combo);
+                    std::printf("Computed,MAX Combo aupr %.12g,(%s)\n", pr[(size_t)best], coeff_tag(c).c_str());
+                    write_matrix(prefix + ".mcp_" + coeff_tag(c) + ext, combo, genes, genes);
+                } else {
+                    for (int64_t r = 0; r < nc; ++r) {
+                        const double* c = &cs[(size_t)(4 * r)];
+                        if (c[0] == 1 && c[1] == 0 && c[2] == 0 && c[3] == 0) continue;  // mcpnet.cpp:589
+                        mcpgpu::compute_combo(ctx, mi, m1, m2, m3, c, combo);
+                        write_matrix(prefix + ".mcp_" + coeff_tag(c) + ext, combo, genes, genes);
+                    }
+                }
+                std::printf("ALL Combos in %.6f sec\n", now_s() - t1);
             }
         } else {
             throw std::runtime_error("unknown command " + a.cmd);

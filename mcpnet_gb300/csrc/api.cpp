@@ -2144,4 +2144,106 @@ int mcpg_ap_mi(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_t ldx
     return finish(h);
 }
 
+int mcpg_maxmins(mcpg_handle* h, const float* A, int64_t n, int64_t lda, float* M1, int64_t ld1, float* M2,
+                 int64_t ld2, float* M3, int64_t ld3, float* R2, int64_t ldr2, float* R3, int64_t ldr3, float* R4,
+                 int64_t ldr4) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (n < 0) return fail(h, MCPG_ERR_ARG, "maxmins: negative size");
+    if (n == 0) return MCPG_OK;
+    if (!A || lda < n) return fail(h, MCPG_ERR_ARG, "maxmins: null input or leading dimension");
+    float* dA;
+    int64_t la;
+    if ((rc = stage_in(h, S_IN2, A, lda, n, n, &dA, &la))) return rc;
+    // device outputs for the requested host outputs (each in its own scratch slot)
+    float* host[6] = {M1, M2, M3, R2, R3, R4};
+    const int64_t hld[6] = {ld1, ld2, ld3, ldr2, ldr3, ldr4};
+    const int slots[6] = {S_OUT0, S_OUT1, S_IN3, S_IN4, S_TFA, S_TFB};
+    float* dev[6] = {};
+    int64_t dld[6] = {};
+    for (int k = 0; k < 6; ++k) {
+        if (!host[k]) continue;
+        if (hld[k] < n) return fail(h, MCPG_ERR_ARG, "maxmins: leading dimension too small");
+        if ((rc = stage_out_alloc(h, slots[k], n, n, &dev[k], &dld[k]))) return rc;
+    }
+    if ((rc = maxmins_dev(h, dA, n, la, dev[0], dld[0], dev[1], dld[1], dev[2], dld[2], dev[3], dld[3], dev[4], dld[4],
+                          dev[5], dld[5])))
+        return rc;
+    for (int k = 0; k < 6; ++k)
+        if (host[k] && (rc = copy_out(h, host[k], hld[k], dev[k], dld[k], n, n))) return rc;
+    return finish(h);
+}
+
+int mcpg_combo(mcpg_handle* h, const float* mi, int64_t ldm, const float* M1, int64_t ld1, const float* M2, int64_t ld2,
+               const float* M3, int64_t ld3, int64_t rows, int64_t cols, const double* coeffs, float* out, int64_t ldo) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (rows < 0 || cols < 0) return fail(h, MCPG_ERR_ARG, "combo: negative size");
+    if (rows == 0 || cols == 0) return MCPG_OK;
+    if (!mi || !out || !coeffs) return fail(h, MCPG_ERR_ARG, "combo: null pointer");
+    if ((coeffs[1] != 0.0 && !M1) || (coeffs[2] != 0.0 && !M2) || (coeffs[3] != 0.0 && !M3))
+        return fail(h, MCPG_ERR_ARG, "combo: a matrix with a nonzero coefficient is null");
+    const float* src[4] = {mi, M1, M2, M3};
+    const int64_t lds[4] = {ldm, ld1, ld2, ld3};
+    const int slots[4] = {S_IN1, S_IN2, S_IN3, S_IN4};
+    float* d[4] = {};
+    int64_t dl[4] = {cols, cols, cols, cols};
+    for (int k = 0; k < 4; ++k) {
+        if (!src[k] || (k > 0 && coeffs[k] == 0.0)) continue;
+        if (lds[k] < cols) return fail(h, MCPG_ERR_ARG, "combo: leading dimension too small");
+        if ((rc = stage_in(h, slots[k], src[k], lds[k], rows, cols, &d[k], &dl[k]))) return rc;
+    }
+    float* dout;
+    int64_t ld;
+    if ((rc = stage_out_alloc(h, S_OUT0, rows, cols, &dout, &ld))) return rc;
+    {
+        PROF(h, "combo");
+        CK(h, mcpg::launch_combo(d[0], dl[0], d[1], dl[1], d[2], dl[2], d[3], dl[3], rows, cols, coeffs, dout, ld,
+                                 h->stream, &h->launches),
+           "combo kernel");
+    }
+    if ((rc = copy_out(h, out, ldo, dout, ld, rows, cols))) return rc;
+    return finish(h);
+}
+
+int mcpg_combo_eval(mcpg_handle* h, const float* mi, int64_t ldm, const float* M1, int64_t ld1, const float* M2,
+                    int64_t ld2, const float* M3, int64_t ld3, int64_t rows, int64_t cols, const int8_t* labels,
+                    int64_t ldl, int region, const int32_t* row_gene, const uint8_t* col_tf, const double* coeffs,
+                    int64_t n_coeffs, double* aupr, double* auroc, int64_t* best) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    mcpg::TruthRegion r{};
+    if ((rc = truth_region(h, "combo_eval", labels, rows, cols, ldl, region, row_gene, col_tf, &r))) return rc;
+    const float* src[4] = {mi, M1, M2, M3};
+    const int64_t lds[4] = {ldm, ld1, ld2, ld3};
+    const int slots[4] = {S_IN1, S_IN2, S_IN3, S_IN4};
+    const float* d[4] = {};
+    int64_t dl[4] = {cols, cols, cols, cols};
+    for (int k = 0; k < 4 && rows > 0 && cols > 0; ++k) {
+        if (!src[k]) continue;
+        if (lds[k] < cols) return fail(h, MCPG_ERR_ARG, "combo_eval: leading dimension too small");
+        float* p;
+        if ((rc = stage_in(h, slots[k], src[k], lds[k], rows, cols, &p, &dl[k]))) return rc;
+        d[k] = p;
+    }
+    void *lab, *aux;
+    if ((rc = scratch(h, S_EV_LAB, (size_t)(rows * cols), &lab))) return rc;
+    if (rows > 0 && cols > 0)
+        CK(h, cudaMemcpy2DAsync(lab, (size_t)cols, labels, (size_t)ldl, (size_t)cols, (size_t)rows,
+                                cudaMemcpyHostToDevice, h->stream),
+           "host-to-device copy");
+    r.labels = (const int8_t*)lab;
+    r.ldl = cols;
+    if (region == MCPG_TRUTH_TF && rows > 0 && cols > 0) {
+        if ((rc = scratch(h, S_EV_AUX, (size_t)(rows * 4 + cols), &aux))) return rc;
+        CK(h, cudaMemcpyAsync(aux, row_gene, (size_t)rows * 4, cudaMemcpyHostToDevice, h->stream),
+           "host-to-device copy");
+        CK(h, cudaMemcpyAsync((char*)aux + rows * 4, col_tf, (size_t)cols, cudaMemcpyHostToDevice, h->stream),
+           "host-to-device copy");
+        r.row_gene = (const int32_t*)aux;
+        r.col_tf = (const uint8_t*)aux + rows * 4;
+    }
+    return combo_eval_dev(h, d, dl, r, coeffs, n_coeffs, aupr, auroc, best);
+}
+
 }  // extern "C"

@@ -71,3 +71,79 @@ def test_cli_pipeline_matches_oracle(built_lib, port, tmp_path):
     assert r.returncode == 0
     M, R = port.mcp(A, 3, symmetrize=True)
     assert np.array_equal(read_exp(tmp_path / "m3.exp"), R) and np.array_equal(read_exp(tmp_path / "mm3.exp"), M)
+
+
+def read_text_matrix(path, sep):
+    lines = Path(path).read_text().splitlines()
+    skip = 2 if lines[0].split(sep)[1] == "Alias" else 1
+    return np.array([[float(v) for v in l.split(sep)[skip:]] for l in lines[1:]], dtype=np.float32)
+
+
+def test_csv_round_trip(built_lib, tmp_path):
+    X = built_lib.synth_grn(7, 11, seed=3)
+    write_exp(tmp_path / "x.exp", X)
+    r = run("convert", "-i", tmp_path / "x.exp", "-o", tmp_path / "x.csv")
+    assert r.returncode == 0, r.stderr
+    assert np.array_equal(read_text_matrix(tmp_path / "x.csv", ","), X)
+    # a CSV without the Alias column reads too
+    with open(tmp_path / "y.csv", "w") as f:
+        f.write("Id," + ",".join(f"s{j}" for j in range(11)) + "\n")
+        for i in range(7):
+            f.write(f"g{i}," + ",".join(repr(float(v)) for v in X[i]) + "\n")
+    r = run("convert", "-i", tmp_path / "y.csv", "-o", tmp_path / "y.exp")
+    assert r.returncode == 0, r.stderr
+    assert np.array_equal(read_exp(tmp_path / "y.exp"), X)
+
+
+@pytest.mark.gpu
+def test_cli_ap_mi(built_lib, gpu, tmp_path):
+    """`mi -m 1` (the reference's default): seeded U[0, 1e-5) noise, ranks, AP MI."""
+    X = built_lib.synth_grn(50, 300, seed=12)
+    write_exp(tmp_path / "x.exp", X)
+    r = run("mi", "-i", tmp_path / "x.exp", "-o", tmp_path / "ap.exp", "--seed", "5")
+    assert r.returncode == 0, r.stderr
+    got = read_exp(tmp_path / "ap.exp")
+    X32 = read_exp(tmp_path / "x.exp")
+    assert np.array_equal(got, gpu.ap_mi(X32, noise=1e-5, seed=5))
+
+
+@pytest.mark.gpu
+def test_cli_ensemble_eval(built_lib, port, tmp_path):
+    """mcpnet --mi-input -m 2 4 -f coeffs --eval -g truth: AUPRs and the chosen
+    combo against the oracle's composition of the reference's loop."""
+    n = 70
+    X, E = built_lib.synth_grn(n, 250, seed=14, with_edges=True)
+    A = port.bspline_mi(X)
+    np.fill_diagonal(A, 0)
+    names = [f"g{i}" for i in range(n)]
+    write_exp(tmp_path / "mi.exp", A, names)
+    rng = np.random.default_rng(2)
+    L = np.full((n, n), -1, np.int8)
+    with open(tmp_path / "truth.txt", "w") as f:
+        for s, t in E:
+            f.write(f"g{s}\tg{t}\t1\n")
+            L[s, t] = 1
+        for _ in range(600):
+            s, t = rng.integers(0, n, 2)
+            if s != t and L[s, t] == -1:
+                f.write(f"g{s}\tg{t}\t0\n")
+                L[s, t] = 0
+    cs = np.array([[0.25, 0.25, 0.25, 0.25], [1, 0, 0, 0], [0.5, 0.5, 0, 0], [0, 0, 0.5, 0.5]])
+    np.savetxt(tmp_path / "coeffs.txt", cs)
+    r = run("mcpnet", "-i", tmp_path / "mi.exp", "-o", tmp_path / "o", "--mi-input", "-m", "1", "4", "-f",
+            tmp_path / "coeffs.txt", "--eval", "-g", tmp_path / "truth.txt")
+    assert r.returncode == 0, r.stderr
+    M = port.maxmin(A, A)
+    M2 = port.maxmin(A, M)
+    M3 = port.maxmin(M, M)
+    pr, roc, best = port.combo_eval(A, M, M2, M3, L, cs, region="all")
+    lines = [l for l in r.stdout.splitlines() if l.startswith("Computed,Combo AUPR")]
+    got = [float(l.split()[2].split(",")[0]) for l in lines]
+    want = [p for p in pr if p == p]
+    assert len(got) == len(want) and np.allclose(got, want, rtol=0, atol=1e-11)
+    tag = "_".join(f"{c:.3f}" for c in cs[best])
+    chosen = read_exp(tmp_path / f"o_inmi.mcp_{tag}.exp")
+    assert np.array_equal(chosen, port.combo(A, M, M2, M3, cs[best]))
+    mcp2 = [l for l in r.stdout.splitlines() if l.startswith("Computed,auprroc,mcp2,")][0].split(",")
+    a, b, _, _ = port.eval_truth(port.mcp(A, 2)[1], L, "all")
+    assert abs(float(mcp2[3]) - a) <= 1e-11 and abs(float(mcp2[4]) - b) <= 1e-11
