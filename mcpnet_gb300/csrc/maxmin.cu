@@ -10,12 +10,14 @@
 //
 // Kernel shape (FP32 ALU bound, no tensor cores):
 //  - CTA tile 128 x 128 outputs, 256 threads, 8 x 8 outputs per thread held in
-//    registers; k staged through shared memory in 32-wide slices by a 3-stage
+//    registers; k staged through shared memory in 64-wide slices by a 2-stage
 //    cp.async pipeline (operand rows are k-contiguous in HBM, so no transpose).
 //  - inner step per thread and 4 k: 16 LDS.128 feed 64 x 2 x (min, min, max3):
 //    1.5 FP32 min/max instructions per (i, j, k) triple using the sm_100+
-//    3-input max.  (BK 32 / 3 stages / LDS.128 measured best of a sweep over
-//    BK 16-32, 3-4 stages, LDS.64/128 on GB300.)
+//    3-input max.  (BK 64 / 2 stages / LDS.128 measured best on GB300 of
+//    BK 16/32/64, 2-4 stages, LDS.64/128: at n = 20,000 BK 32 / 3 stages ran
+//    670.9 ms, BK 64 / 2 stages 656.0 ms; half as many barriers and loader
+//    rounds per min/max instruction.)
 //  - fused epilogues: MCP ratio (combine.hpp:210-222), closure step
 //    B <- max(B, B (x) B) with a changed flag, DPI mask + apply
 //    (dpi.hpp:56-68, threshold.hpp:46-53) with the y in {x, z} exclusion done
@@ -32,10 +34,10 @@ namespace mcpg {
 namespace {
 
 #ifndef MCPG_MM_BK
-#define MCPG_MM_BK 32
+#define MCPG_MM_BK 64
 #endif
 #ifndef MCPG_MM_STAGES
-#define MCPG_MM_STAGES 3
+#define MCPG_MM_STAGES 2
 #endif
 #ifndef MCPG_MM_MINB
 #define MCPG_MM_MINB 1
@@ -47,7 +49,7 @@ constexpr int BM = 128, BN = 128, BK = MCPG_MM_BK, STAGES = MCPG_MM_STAGES, THRE
 constexpr int KSTEP = MCPG_MM_KSTEP;  // k values per shared-memory load (2: LDS.64, 4: LDS.128)
 constexpr int LDS = BK + 4;  // row stride in floats: 16B-aligned, 4 consecutive rows -> 4 distinct bank groups
 constexpr int TILE_FLOATS = BM * LDS;
-constexpr size_t SMEM_BYTES = (size_t)STAGES * 2 * TILE_FLOATS * sizeof(float);  // 80 KB
+constexpr size_t SMEM_BYTES = (size_t)STAGES * 2 * TILE_FLOATS * sizeof(float);  // 136 KB
 
 // Per-thread view of the operand rows it stages: with CPR = BK/4 chunks of 16
 // bytes per row, thread t copies chunk q = t % CPR of rows t / CPR + h * RSTEP
