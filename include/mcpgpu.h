@@ -289,6 +289,30 @@ MCPG_API int mcpg_ap_mi(mcpg_handle* h, const float* X, int64_t n, int64_t m, in
 MCPG_API int mcpg_ap_mi_dev(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_t ldx, float noise,
                             uint64_t seed, float* MI, int64_t ldmi);
 
+/* ---- Stouffer / CLR transforms ----
+ * compute_stouffer (apps/pipeline/mcpnet_helper.hpp:575-586) and the transform
+ * app (apps/transform/transform.cpp:214-231): per-row statistics, then per entry
+ * stouffer_vector_kernel (include/mcp/transform/stouffer.hpp:57-82):
+ *   out = ((x - mean_i) * (|sd_i| < eps ? 0 : 1/sd_i) + (|sd_j| < eps ? 0 : (x - mean_j) / sd_j)) * sqrt(1/2)
+ * or clr_vector_kernel (include/mcp/transform/clr.hpp:52-73): sqrt(zi^2 + zj^2),
+ * in float exactly as those kernels.  The statistics come, in the reference,
+ * from splash::kernel::GaussianParamsExclude1<T,T,true>, which is not in the
+ * reference snapshot; here they are the FP64 mean and unbiased (N-1) standard
+ * deviation of the row, rounded to float, over every entry
+ * (MCPG_ROWSTATS_ALL) or every entry but the diagonal
+ * (MCPG_ROWSTATS_EXCLUDE_DIAGONAL) -- the statistics' parity is unpinned.
+ * A: n x n.  mcpg_row_stats_dev: rows x cols, mean / sd device float arrays. */
+#define MCPG_TRANSFORM_STOUFFER 0
+#define MCPG_TRANSFORM_CLR 1
+#define MCPG_ROWSTATS_ALL 0
+#define MCPG_ROWSTATS_EXCLUDE_DIAGONAL 1
+MCPG_API int mcpg_row_stats_dev(mcpg_handle* h, const float* A, int64_t rows, int64_t cols, int64_t lda,
+                                int stats_mode, float* mean, float* sd);
+MCPG_API int mcpg_transform(mcpg_handle* h, const float* A, int64_t n, int64_t lda, int transform, int stats_mode,
+                            float* out, int64_t ldo);
+MCPG_API int mcpg_transform_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, int transform,
+                                int stats_mode, float* out, int64_t ldo);
+
 /* ---- gold-standard evaluation: AUPR and AUROC ----
  * mcpg_aupr_auroc: aupr_kernel::operator()(pos, pos_count, neg, neg_count)
  * (include/mcp/transform/aupr.hpp:565-584 -> average_compute_1sort, 127-236)
@@ -361,6 +385,16 @@ MCPG_API int mcpg_combo_eval_dev(mcpg_handle* h, const float* mi, int64_t ldm, c
                                  int64_t cols, const int8_t* labels, int64_t ldl, int region, const int32_t* row_gene,
                                  const uint8_t* col_tf, const double* coeffs, int64_t n_coeffs, double* aupr,
                                  double* auroc, int64_t* best);
+/* The Stouffer half of the same loop (mcpnet.cpp:622-661): for every row c the
+ * AUPR / AUROC of the Stouffer transform (mcpg_transform_dev, stats_mode) of
+ * the full combo matrix over the labelled entries, and the row chosen by the
+ * same rule.  Needs two n x n float scratch matrices; rows == cols. */
+MCPG_API int mcpg_combo_stouffer_eval_dev(mcpg_handle* h, const float* mi, int64_t ldm, const float* M1,
+                                          int64_t ld1, const float* M2, int64_t ld2, const float* M3, int64_t ld3,
+                                          int64_t n, const int8_t* labels, int64_t ldl, int region,
+                                          const int32_t* row_gene, const uint8_t* col_tf, const double* coeffs,
+                                          int64_t n_coeffs, int stats_mode, double* aupr, double* auroc,
+                                          int64_t* best);
 /* Host-buffer form of mcpg_combo_eval_dev (matrices, labels, row_gene and col_tf on the host). */
 MCPG_API int mcpg_combo_eval(mcpg_handle* h, const float* mi, int64_t ldm, const float* M1, int64_t ld1,
                              const float* M2, int64_t ld2, const float* M3, int64_t ld3, int64_t rows, int64_t cols,

@@ -104,6 +104,15 @@ ABI += [
     ("mcpg_combo_eval", C.c_int, [_vp, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _i64, _i64, _vp, _i64,
                                   C.c_int, _vp, _vp, _vp, _i64, _vp, _vp, _vp]),
 ]
+ABI += [
+    ("mcpg_row_stats_dev", C.c_int, [_vp, _vp, _i64, _i64, _i64, C.c_int, _vp, _vp]),
+    ("mcpg_transform", C.c_int, [_vp, _vp, _i64, _i64, C.c_int, C.c_int, _vp, _i64]),
+    ("mcpg_transform_dev", C.c_int, [_vp, _vp, _i64, _i64, C.c_int, C.c_int, _vp, _i64]),
+    ("mcpg_combo_stouffer_eval_dev", C.c_int, [_vp, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _i64, _vp, _i64,
+                                               C.c_int, _vp, _vp, _vp, _i64, C.c_int, _vp, _vp, _vp]),
+]
+TRANSFORMS = {"stouffer": 0, "clr": 1}
+ROW_STATS = {"all": 0, "exclude_diagonal": 1}
 TRUTH_REGIONS = {"lower": 0, "all": 1, "tf": 2}
 AP_NOISE = 1e-5  # the reference apps' tie-breaking noise amplitude (apps/correlation/mi.cpp:128-129)
 
@@ -551,6 +560,41 @@ class Handle:
                                              _ptr(keep[2]), cols, rows, cols, _ptr(labels), cols,
                                              TRUTH_REGIONS[region], _ptr(rg), _ptr(ct), cs.ctypes.data, cs.shape[0],
                                              _ptr(a), _ptr(b), C.byref(best)), "combo_eval")
+        return a, b, best.value
+
+    # ---- Stouffer / CLR ----
+    def transform(self, A, kind="stouffer", stats="exclude_diagonal"):
+        """compute_stouffer (or CLR) of an n x n host matrix."""
+        A = _f32(A)
+        n = A.shape[0]
+        out = np.empty((n, n), dtype=np.float32)
+        self._check(self._L.mcpg_transform(self._h, _ptr(A), n, n, TRANSFORMS[kind], ROW_STATS[stats], _ptr(out), n),
+                    "transform")
+        return out
+
+    def transform_dev(self, A, out, kind="stouffer", stats="exclude_diagonal"):
+        n = A.shape[0]
+        self._check(self._L.mcpg_transform_dev(self._h, self._dp(A), n, self._ld(A), TRANSFORMS[kind],
+                                                ROW_STATS[stats], self._dp(out), self._ld(out)), "transform_dev")
+
+    def row_stats_dev(self, A, mean, sd, stats="exclude_diagonal"):
+        rows, cols = A.shape
+        self._check(self._L.mcpg_row_stats_dev(self._h, self._dp(A), rows, cols, self._ld(A), ROW_STATS[stats],
+                                                self._dp(mean), self._dp(sd)), "row_stats_dev")
+
+    def combo_stouffer_eval_dev(self, mi, M1, M2, M3, labels, coeffs, region="lower", row_gene=None, col_tf=None,
+                                stats="exclude_diagonal"):
+        """The Stouffer half of the ensemble coefficient search: (aupr, auroc, best row)."""
+        cs = np.ascontiguousarray(np.asarray(coeffs, dtype=np.float64).reshape(-1, 4))
+        n = mi.shape[0]
+        ld = lambda t: self._ld(t) if t is not None else n
+        a = np.empty(cs.shape[0], dtype=np.float64)
+        b = np.empty(cs.shape[0], dtype=np.float64)
+        best = C.c_int64(0)
+        self._check(self._L.mcpg_combo_stouffer_eval_dev(
+            self._h, self._dp(mi), self._ld(mi), self._dp(M1), ld(M1), self._dp(M2), ld(M2), self._dp(M3), ld(M3), n,
+            self._dp(labels), self._ld(labels), TRUTH_REGIONS[region], self._dp(row_gene), self._dp(col_tf),
+            cs.ctypes.data, cs.shape[0], ROW_STATS[stats], _ptr(a), _ptr(b), C.byref(best)), "combo_stouffer_eval_dev")
         return a, b, best.value
 
     # ---- gold-standard evaluation ----

@@ -64,6 +64,9 @@ enum Slot {
     S_EV_AUX,    // evaluation: staged row_gene / col_tf
     S_AP_R,      // AP MI: int32 ranks
     S_AP_TAB,    // AP MI: uint16 ranks, order and cumulative histograms
+    S_ST_STATS,  // Stouffer: row means and standard deviations
+    S_ST_A,      // Stouffer ensemble: the combo matrix
+    S_ST_B,      // Stouffer ensemble: its transform
     NSLOTS
 };
 
@@ -1362,6 +1365,88 @@ int ap_mi_dev(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_t ldx,
     return ap_mi_from_ranks(h, (const int32_t*)r, n, m, m, MI, ldmi, flag, counter);
 }
 
+// ---- Stouffer / CLR ----
+int transform_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, int transform, int stats_mode, float* out,
+                  int64_t ldo) {
+    if (n < 0) return fail(h, MCPG_ERR_ARG, "transform: negative size");
+    if (n == 0) return MCPG_OK;
+    if (!A || !out || lda < n || ldo < n) return fail(h, MCPG_ERR_ARG, "transform: null pointer or leading dimension");
+    if (transform != MCPG_TRANSFORM_STOUFFER && transform != MCPG_TRANSFORM_CLR)
+        return fail(h, MCPG_ERR_ARG, "transform: unknown transform %d", transform);
+    if (stats_mode != MCPG_ROWSTATS_ALL && stats_mode != MCPG_ROWSTATS_EXCLUDE_DIAGONAL)
+        return fail(h, MCPG_ERR_ARG, "transform: unknown statistics mode %d", stats_mode);
+    void* st;
+    int rc = scratch(h, S_ST_STATS, (size_t)(2 * n) * sizeof(float), &st);
+    if (rc) return rc;
+    float* mean = (float*)st;
+    float* sd = mean + n;
+    {
+        PROF(h, "row_stats");
+        CK(h, mcpg::launch_row_stats(A, n, n, lda, stats_mode == MCPG_ROWSTATS_EXCLUDE_DIAGONAL, mean, sd, h->stream,
+                                     &h->launches),
+           "row stats");
+    }
+    {
+        PROF(h, "transform");
+        CK(h, mcpg::launch_transform(A, n, lda, mean, sd, transform == MCPG_TRANSFORM_CLR, out, ldo, h->stream,
+                                     &h->launches),
+           "transform");
+    }
+    return MCPG_OK;
+}
+
+int combo_stouffer_eval_dev(mcpg_handle* h, const float* const mats[4], const int64_t lds[4],
+                            const mcpg::TruthRegion& r, const double* coeffs, int64_t nc, int stats_mode,
+                            double* aupr, double* auroc, int64_t* best) {
+    const int64_t n = r.rows;
+    if (r.rows != r.cols) return fail(h, MCPG_ERR_ARG, "combo_stouffer_eval: the matrices must be square");
+    if (nc < 0 || (nc > 0 && !coeffs)) return fail(h, MCPG_ERR_ARG, "combo_stouffer_eval: bad coefficient table");
+    if (n > 0) {
+        if (!mats[0] || lds[0] < n) return fail(h, MCPG_ERR_ARG, "combo_stouffer_eval: null mi or leading dimension");
+        for (int k = 1; k < 4; ++k) {
+            if (mats[k] && lds[k] < n) return fail(h, MCPG_ERR_ARG, "combo_stouffer_eval: leading dimension too small");
+            for (int64_t c = 0; c < nc; ++c)
+                if (!mats[k] && coeffs[4 * c + k] != 0.0)
+                    return fail(h, MCPG_ERR_ARG, "combo_stouffer_eval: coefficient row %lld uses a null matrix",
+                                (long long)c);
+        }
+    }
+    float *cm = nullptr, *tm = nullptr;
+    int64_t ldc = 0;
+    int rc;
+    if ((rc = stage_out_alloc(h, S_ST_A, n, n, &cm, &ldc))) return rc;
+    if ((rc = stage_out_alloc(h, S_ST_B, n, n, &tm, &ldc))) return rc;
+    double max_aupr = 0.0;
+    int64_t co = 0;
+    for (int64_t c = 0; c < nc; ++c) {
+        const double* cs = coeffs + 4 * c;
+        if (cs[0] == 1.0 && cs[1] == 0.0 && cs[2] == 0.0 && cs[3] == 0.0) {  // mcpnet.cpp:589
+            if (aupr) aupr[c] = NAN;
+            if (auroc) auroc[c] = NAN;
+            continue;
+        }
+        double a = 0.0, b = 0.0;
+        if (n > 0) {
+            {
+                PROF(h, "combo");
+                CK(h, mcpg::launch_combo(mats[0], lds[0], mats[1], lds[1], mats[2], lds[2], mats[3], lds[3], n, n, cs,
+                                         cm, ldc, h->stream, &h->launches),
+                   "combo kernel");
+            }
+            if ((rc = transform_dev(h, cm, n, ldc, MCPG_TRANSFORM_STOUFFER, stats_mode, tm, ldc))) return rc;
+            if ((rc = eval_truth_dev(h, tm, ldc, r, &a, &b, nullptr, nullptr))) return rc;
+        }
+        if (aupr) aupr[c] = a;
+        if (auroc) auroc[c] = b;
+        if (a > max_aupr) {  // mcpnet.cpp:644-648
+            max_aupr = a;
+            co = c;
+        }
+    }
+    if (best) *best = co;
+    return MCPG_OK;
+}
+
 }  // namespace
 
 // =====================================================================
@@ -2244,6 +2329,59 @@ int mcpg_combo_eval(mcpg_handle* h, const float* mi, int64_t ldm, const float* M
         r.col_tf = (const uint8_t*)aux + rows * 4;
     }
     return combo_eval_dev(h, d, dl, r, coeffs, n_coeffs, aupr, auroc, best);
+}
+
+int mcpg_row_stats_dev(mcpg_handle* h, const float* A, int64_t rows, int64_t cols, int64_t lda, int stats_mode,
+                       float* mean, float* sd) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (rows < 0 || cols < 0) return fail(h, MCPG_ERR_ARG, "row_stats: negative size");
+    if (rows == 0) return MCPG_OK;
+    if (!A || !mean || !sd || lda < cols) return fail(h, MCPG_ERR_ARG, "row_stats: null pointer or leading dimension");
+    if (stats_mode != MCPG_ROWSTATS_ALL && stats_mode != MCPG_ROWSTATS_EXCLUDE_DIAGONAL)
+        return fail(h, MCPG_ERR_ARG, "row_stats: unknown statistics mode %d", stats_mode);
+    PROF(h, "row_stats");
+    CK(h, mcpg::launch_row_stats(A, rows, cols, lda, stats_mode == MCPG_ROWSTATS_EXCLUDE_DIAGONAL, mean, sd,
+                                 h->stream, &h->launches),
+       "row stats");
+    return MCPG_OK;
+}
+
+int mcpg_transform_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, int transform, int stats_mode,
+                       float* out, int64_t ldo) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    return transform_dev(h, A, n, lda, transform, stats_mode, out, ldo);
+}
+
+int mcpg_transform(mcpg_handle* h, const float* A, int64_t n, int64_t lda, int transform, int stats_mode, float* out,
+                   int64_t ldo) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (n < 0) return fail(h, MCPG_ERR_ARG, "transform: negative size");
+    if (n == 0) return MCPG_OK;
+    if (!A || !out || lda < n || ldo < n) return fail(h, MCPG_ERR_ARG, "transform: null pointer or leading dimension");
+    float *da, *dout;
+    int64_t la, lo;
+    if ((rc = stage_in(h, S_IN0, A, lda, n, n, &da, &la))) return rc;
+    if ((rc = stage_out_alloc(h, S_OUT0, n, n, &dout, &lo))) return rc;
+    if ((rc = transform_dev(h, da, n, la, transform, stats_mode, dout, lo))) return rc;
+    if ((rc = copy_out(h, out, ldo, dout, lo, n, n))) return rc;
+    return finish(h);
+}
+
+int mcpg_combo_stouffer_eval_dev(mcpg_handle* h, const float* mi, int64_t ldm, const float* M1, int64_t ld1,
+                                 const float* M2, int64_t ld2, const float* M3, int64_t ld3, int64_t n,
+                                 const int8_t* labels, int64_t ldl, int region, const int32_t* row_gene,
+                                 const uint8_t* col_tf, const double* coeffs, int64_t n_coeffs, int stats_mode,
+                                 double* aupr, double* auroc, int64_t* best) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    mcpg::TruthRegion r{};
+    if ((rc = truth_region(h, "combo_stouffer_eval", labels, n, n, ldl, region, row_gene, col_tf, &r))) return rc;
+    const float* mats[4] = {mi, M1, M2, M3};
+    const int64_t lds[4] = {ldm, ld1, ld2, ld3};
+    return combo_stouffer_eval_dev(h, mats, lds, r, coeffs, n_coeffs, stats_mode, aupr, auroc, best);
 }
 
 }  // extern "C"

@@ -1,0 +1,115 @@
+// Stouffer and CLR transforms of a gene x gene score matrix
+// (compute_stouffer, apps/pipeline/mcpnet_helper.hpp:575-586; the transform
+// app, apps/transform/transform.cpp:214-231):
+//   * row statistics (mean, standard deviation) per row, in FP64: the
+//     reference takes them from splash::kernel::GaussianParamsExclude1<T,T,true>
+//     (unbiased variance), whose source is not in the reference snapshot.  Here
+//     the mean and the unbiased (N - 1) variance are two-pass FP64 sums over
+//     the row, optionally without the diagonal entry; they are rounded to the
+//     float pair the reference's kernels take.
+//   * per entry exactly stouffer_vector_kernel / clr_vector_kernel
+//     (include/mcp/transform/stouffer.hpp:57-82, clr.hpp:52-73) in float:
+//       denom_i = |sd_i| < eps ? 0 : (float)(1.0 / sd_i)
+//       zi = (x - mean_i) * denom_i,  zj = |sd_j| < eps ? 0 : (x - mean_j) / sd_j
+//       Stouffer (zi + zj) * (float)sqrt(1/2),  CLR sqrt(zi^2 + zj^2)
+//     with explicit _rn intrinsics so nvcc contracts nothing.
+#include <cuda_runtime.h>
+#include <float.h>
+#include <stdint.h>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace mcpg {
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+constexpr int ST_THREADS = 256;
+
+__device__ __forceinline__ double block_sum_d(double v, double* sh /*32*/) {
+    for (int o = 16; o > 0; o >>= 1) v = __dadd_rn(v, __shfl_down_sync(FULL, v, o));
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x == 0)
+        for (int i = 0; i < nw; ++i) t = __dadd_rn(t, sh[i]);  // fixed order: reproducible
+    __syncthreads();
+    if (threadIdx.x == 0) sh[0] = t;
+    __syncthreads();
+    t = sh[0];
+    __syncthreads();
+    return t;
+}
+
+// One block per row (grid-stride): two FP64 passes over the row.
+__global__ void __launch_bounds__(ST_THREADS) row_stats_kernel(const float* A, int64_t rows, int64_t cols,
+                                                               int64_t lda, int excl_diag, float* mean, float* sd) {
+    __shared__ double sh[32];
+    for (int64_t i = blockIdx.x; i < rows; i += gridDim.x) {
+        const float* row = A + i * lda;
+        double s = 0.0;
+        for (int64_t j = threadIdx.x; j < cols; j += blockDim.x)
+            if (!(excl_diag && j == i)) s = __dadd_rn(s, (double)row[j]);
+        const int64_t N = cols - ((excl_diag && i < cols) ? 1 : 0);
+        const double tot = block_sum_d(s, sh);
+        const double mu = N > 0 ? __ddiv_rn(tot, (double)N) : 0.0;
+        double q = 0.0;
+        for (int64_t j = threadIdx.x; j < cols; j += blockDim.x)
+            if (!(excl_diag && j == i)) {
+                const double d = __dadd_rn((double)row[j], -mu);
+                q = __dadd_rn(q, __dmul_rn(d, d));
+            }
+        const double ss = block_sum_d(q, sh);
+        if (threadIdx.x == 0) {
+            mean[i] = __double2float_rn(mu);
+            sd[i] = N > 1 ? __double2float_rn(__dsqrt_rn(__ddiv_rn(ss, (double)(N - 1)))) : 0.0f;
+        }
+    }
+}
+
+template <int CLR>
+__global__ void transform_kernel(const float* A, int64_t n, int64_t lda, const float* mean, const float* sd,
+                                 float* out, int64_t ldo) {
+    const float isqrt2 = 0.70710678118654752440f;
+    const int64_t total = n * n;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = t / n, j = t - i * n;
+        const float x = A[i * lda + j];
+        const float si = sd[i], sj = sd[j];
+        const float denom = fabsf(si) < FLT_EPSILON ? 0.0f : __frcp_rn(si);  // (float)(1.0 / sd): double rounding innocuous
+        const float zi = __fmul_rn(__fsub_rn(x, mean[i]), denom);
+        const float zj = fabsf(sj) < FLT_EPSILON ? 0.0f : __fdiv_rn(__fsub_rn(x, mean[j]), sj);
+        out[i * ldo + j] = CLR ? __fsqrt_rn(__fadd_rn(__fmul_rn(zi, zi), __fmul_rn(zj, zj)))
+                               : __fmul_rn(__fadd_rn(zi, zj), isqrt2);
+    }
+}
+
+unsigned ew_grid(int64_t total) {
+    int64_t b = ceil_div(total, 256);
+    if (b > 152 * 32) b = 152 * 32;
+    if (b < 1) b = 1;
+    return (unsigned)b;
+}
+
+}  // namespace
+
+cudaError_t launch_row_stats(const float* A, int64_t rows, int64_t cols, int64_t lda, int excl_diag, float* mean,
+                             float* sd, cudaStream_t st, int64_t* launches) {
+    if (rows <= 0) return cudaSuccess;
+    const int64_t grid = rows < 152 * 8 ? rows : 152 * 8;
+    row_stats_kernel<<<(unsigned)grid, ST_THREADS, 0, st>>>(A, rows, cols, lda, excl_diag, mean, sd);
+    if (launches) ++*launches;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_transform(const float* A, int64_t n, int64_t lda, const float* mean, const float* sd, int clr,
+                             float* out, int64_t ldo, cudaStream_t st, int64_t* launches) {
+    if (n <= 0) return cudaSuccess;
+    if (clr) transform_kernel<1><<<ew_grid(n * n), 256, 0, st>>>(A, n, lda, mean, sd, out, ldo);
+    else transform_kernel<0><<<ew_grid(n * n), 256, 0, st>>>(A, n, lda, mean, sd, out, ldo);
+    if (launches) ++*launches;
+    return cudaGetLastError();
+}
+
+}  // namespace mcpg

@@ -256,3 +256,44 @@ void orc_ap_mi(const int64_t* R, int64_t n, int64_t m, float* out, int64_t ldo) 
     }
     free(C);
 }
+
+/* ---------------- Stouffer / CLR ----------------
+ * Row statistics standing in for splash::kernel::GaussianParamsExclude1<T,T,true>
+ * (the splash source is absent from the reference; parity unpinned): FP64
+ * mean and unbiased (N - 1) standard deviation of each row, two passes,
+ * without the diagonal entry when excl_diag; rounded to float. */
+void orc_row_stats(const float* A, int64_t rows, int64_t cols, int64_t lda, int excl_diag, float* mean, float* sd) {
+    for (int64_t i = 0; i < rows; ++i) {
+        const float* r = A + i * lda;
+        const int64_t N = cols - ((excl_diag && i < cols) ? 1 : 0);
+        double s = 0.0;
+        for (int64_t j = 0; j < cols; ++j)
+            if (!(excl_diag && j == i)) s += (double)r[j];
+        const double mu = N > 0 ? s / (double)N : 0.0;
+        double q = 0.0;
+        for (int64_t j = 0; j < cols; ++j)
+            if (!(excl_diag && j == i)) {
+                const double d = (double)r[j] - mu;
+                q += d * d;
+            }
+        mean[i] = (float)mu;
+        sd[i] = N > 1 ? (float)sqrt(q / (double)(N - 1)) : 0.0f;
+    }
+}
+
+/* stouffer_vector_kernel (include/mcp/transform/stouffer.hpp:57-82) and
+ * clr_vector_kernel (include/mcp/transform/clr.hpp:52-73) for every row, with
+ * row i's statistics as aux1 and every row's as aux2; float arithmetic. */
+void orc_transform(const float* A, int64_t n, int64_t lda, const float* mean, const float* sd, int clr, float* out,
+                   int64_t ldo) {
+    const float isqrt2 = 0.70710678118654752440f;
+    for (int64_t i = 0; i < n; ++i) {
+        const float denom = (fabsf(sd[i]) < FLT_EPSILON) ? 0.0f : (float)(1.0 / (double)sd[i]);
+        for (int64_t j = 0; j < n; ++j) {
+            const float x = A[i * lda + j];
+            const float zi = (x - mean[i]) * denom;
+            const float zj = (fabsf(sd[j]) < FLT_EPSILON) ? 0.0f : (x - mean[j]) / sd[j];
+            out[i * ldo + j] = clr ? sqrtf(zi * zi + zj * zj) : (zi + zj) * isqrt2;
+        }
+    }
+}

@@ -144,6 +144,8 @@ class _Port(_TfCompositions, _EvalCompositions):
         self.L.orc_select_truth.argtypes = [_vp, _i64, _i64, _i64, _vp, _i64, C.c_int, _vp, _vp, _vp, _vp, _vp,
                                             _vp]
         self.L.orc_ranks_desc.argtypes = [_vp, _i64, _i64, _i64, _vp]
+        self.L.orc_row_stats.argtypes = [_vp, _i64, _i64, _i64, C.c_int, _vp, _vp]
+        self.L.orc_transform.argtypes = [_vp, _i64, _i64, _vp, _vp, C.c_int, _vp, _i64]
         self.L.orc_ap_mi.argtypes = [_vp, _i64, _i64, _vp, _i64]
 
     @staticmethod
@@ -286,6 +288,31 @@ class _Port(_TfCompositions, _EvalCompositions):
         return (float(self.L.orc_aupr(pos.ctypes.data, pos.size, neg.ctypes.data, neg.size)),
                 float(self.L.orc_auroc(pos.ctypes.data, pos.size, neg.ctypes.data, neg.size)))
 
+    STATS = {"all": 0, "exclude_diagonal": 1}
+
+    def row_stats(self, A, mode="exclude_diagonal"):
+        """FP64 row mean / unbiased sd rounded to float (stands in for GaussianParamsExclude1)."""
+        A = np.ascontiguousarray(A, dtype=np.float32)
+        rows, cols = A.shape
+        mean = np.empty(rows, np.float32)
+        sd = np.empty(rows, np.float32)
+        self.L.orc_row_stats(A.ctypes.data, rows, cols, cols, self.STATS[mode], mean.ctypes.data, sd.ctypes.data)
+        return mean, sd
+
+    def transform_with_stats(self, A, mean, sd, clr=False):
+        """stouffer_vector_kernel / clr_vector_kernel restated, given the row statistics."""
+        A = np.ascontiguousarray(A, dtype=np.float32)
+        n = A.shape[0]
+        mean = np.ascontiguousarray(mean, dtype=np.float32)
+        sd = np.ascontiguousarray(sd, dtype=np.float32)
+        out = np.empty_like(A)
+        self.L.orc_transform(A.ctypes.data, n, n, mean.ctypes.data, sd.ctypes.data, int(clr), out.ctypes.data, n)
+        return out
+
+    def transform(self, A, clr=False, mode="exclude_diagonal"):
+        mean, sd = self.row_stats(A, mode)
+        return self.transform_with_stats(A, mean, sd, clr)
+
     def ap_ranks(self, X):
         """Descending ranks per gene, ties sharing the lowest rank (int64, n x m)."""
         X = np.ascontiguousarray(X, dtype=np.float32)
@@ -362,6 +389,7 @@ class _Ref(_TfCompositions, _EvalCompositions):
         L.ref_dpi_tf_f32.restype = C.c_int64
         L.ref_aupr_auroc_f32.argtypes = [_vp, _i64, _vp, _i64, _vp]
         L.ref_ap_mi_f32.argtypes = [_vp, _i64, _i64, _vp, _i64]
+        L.ref_transform_f32.argtypes = [_vp, _i64, _i64, _vp, _vp, C.c_int, _vp, _i64]
         L.ref_aupr_auroc_f64.argtypes = [_vp, _i64, _vp, _i64, _vp]
         self.L = L
 
@@ -373,6 +401,16 @@ class _Ref(_TfCompositions, _EvalCompositions):
         f = self.L.ref_aupr_auroc_f32 if dtype == np.float32 else self.L.ref_aupr_auroc_f64
         f(pos.ctypes.data, pos.size, neg.ctypes.data, neg.size, out.ctypes.data)
         return float(out[0]), float(out[1])
+
+    def transform_with_stats(self, A, mean, sd, clr=False):
+        """MCPNet's stouffer_vector_kernel / clr_vector_kernel with the given row statistics."""
+        A = np.ascontiguousarray(A, dtype=np.float32)
+        n = A.shape[0]
+        mean = np.ascontiguousarray(mean, dtype=np.float32)
+        sd = np.ascontiguousarray(sd, dtype=np.float32)
+        out = np.empty_like(A)
+        self.L.ref_transform_f32(A.ctypes.data, n, n, mean.ctypes.data, sd.ctypes.data, int(clr), out.ctypes.data, n)
+        return out
 
     def ap_mi(self, R):
         """MCPNet's IntegralCumulativeHistogramKernel + AdaptivePartitionRankMIKernel2 on given ranks."""

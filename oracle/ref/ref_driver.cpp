@@ -15,6 +15,8 @@
 //   MCP3 symmetrisation   apps/filter/mcp.cpp:463-476
 //   AP MI (ranks given)   IntegralCumulativeHistogramKernel + AdaptivePartitionRankMIKernel2,
 //                         as apps/pipeline/mcpnet_helper.hpp:136-163 (InnerProduct SYMM)
+//   Stouffer / CLR        stouffer_vector_kernel / clr_vector_kernel per row with given row
+//                         statistics (include/mcp/transform/stouffer.hpp:57-82, clr.hpp:52-73)
 //   AUPR / AUROC          aupr_kernel / auroc_kernel::operator()(pos, count, neg, count)
 //                         include/mcp/transform/aupr.hpp:565-584, auroc.hpp:562-579
 // The InnerProduct SYMM=true pattern is restated as "compute j >= i, mirror".
@@ -32,6 +34,8 @@
 #include "mcp/transform/aupr.hpp"
 #include "mcp/transform/auroc.hpp"
 #include "mcp/correlation/AdaptivePartitioningMI.hpp"
+#include "mcp/transform/stouffer.hpp"
+#include "mcp/transform/clr.hpp"
 
 namespace {
 
@@ -244,6 +248,22 @@ void ref_ap_mi_f32(const int64_t* ranks, int64_t n, int64_t m, float* out, int64
                 out[i * ldo + j] = v;
                 out[j * ldo + i] = v;
             }
+    }
+}
+
+// The reference's Stouffer (clr = 0) or CLR (clr = 1) vector kernel over every
+// row of the n x n matrix A with the given per-row (mean, sd) as float pairs,
+// as GlobalReduceTransform hands them to the kernel (aux1 = row i's, aux2 =
+// every row's).
+void ref_transform_f32(const float* A, int64_t n, int64_t lda, const float* mean, const float* sd, int clr,
+                       float* out, int64_t ldo) {
+    std::vector<std::pair<float, float>> aux((size_t)n);
+    for (int64_t i = 0; i < n; ++i) aux[(size_t)i] = std::make_pair(mean[i], sd[i]);
+    mcp::kernel::stouffer_vector_kernel<float> st;
+    mcp::kernel::clr_vector_kernel<float> cl;
+    for (int64_t i = 0; i < n; ++i) {
+        if (clr) cl(A + i * lda, aux.data() + i, aux.data(), (size_t)n, out + i * ldo);
+        else st(A + i * lda, aux.data() + i, aux.data(), (size_t)n, out + i * ldo);
     }
 }
 

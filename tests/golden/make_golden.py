@@ -23,6 +23,9 @@ Fixtures (all float32 unless noted):
   ap_mi.npz      adaptive-partitioning MI from the reference's own kernels
                  (IntegralCumulativeHistogramKernel + AdaptivePartitionRankMIKernel2)
                  on ranks of synthetic expression (with and without ties; tiny m)
+  stouffer.npz   the reference's stouffer_vector_kernel / clr_vector_kernel on an MI
+                 matrix with the oracle's row statistics (both statistics modes,
+                 and a constant row whose deviation is 0)
   eval_truth.npz an MI matrix, its max-min products, int8 truth labels from the
                  synthetic GRN, TF rows, and AUPR / AUROC of each truth region
                  and of a coefficient table of combo scores
@@ -51,7 +54,7 @@ def synth(n, m, seed):
 def main():
     import argparse
     ap = argparse.ArgumentParser()
-    ap.add_argument("--only", choices=["core", "eval", "ap"], default=None)
+    ap.add_argument("--only", choices=["core", "eval", "ap", "stouffer"], default=None)
     args = ap.parse_args()
     O.build(with_ref=True)
     R = O.ref()
@@ -63,6 +66,8 @@ def main():
         evaluation(R)
     if args.only in (None, "ap"):
         ap_mi(R)
+    if args.only in (None, "stouffer"):
+        stouffer(R)
     print("wrote", sorted(p.name for p in HERE.glob("*.npz")))
 
 
@@ -222,6 +227,20 @@ def ap_mi(R):
     out["names"] = np.array(sorted(cases))
     np.savez_compressed(HERE / "ap_mi.npz", **out)
 
+
+
+def stouffer(R):
+    P = O.port()
+    with np.load(HERE / "mcp_70.npz") as z:
+        A = z["A"].copy()
+    A[5, :] = np.float32(0.25)  # a constant row: sd 0 -> its z-scores are 0
+    out = {"A": A}
+    for mode in ("all", "exclude_diagonal"):
+        mean, sd = P.row_stats(A, mode)
+        out[f"{mode}_mean"], out[f"{mode}_sd"] = mean, sd
+        out[f"{mode}_stouffer"] = R.transform_with_stats(A, mean, sd, clr=False)
+        out[f"{mode}_clr"] = R.transform_with_stats(A, mean, sd, clr=True)
+    np.savez_compressed(HERE / "stouffer.npz", **out)
 
 if __name__ == "__main__":
     main()

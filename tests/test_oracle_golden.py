@@ -234,3 +234,19 @@ def test_ap_mi_bit_exact(port, golden):
 def test_ap_ranks_ties_share_lowest(port):
     X = np.array([[0.5, 0.9, 0.5, 0.1, 0.9, -0.0, 0.0]], dtype=np.float32)
     assert port.ap_ranks(X).tolist() == [[2, 0, 2, 4, 0, 5, 5]]
+
+
+def test_stouffer_clr_bit_exact(port, golden):
+    """The restated Stouffer / CLR element transforms equal MCPNet's
+    stouffer_vector_kernel / clr_vector_kernel given the same row statistics
+    (the statistics themselves stand in for the absent splash
+    GaussianParamsExclude1 and are not pinned)."""
+    g = golden("stouffer")
+    A = g["A"]
+    for mode in ("all", "exclude_diagonal"):
+        mean, sd = port.row_stats(A, mode)
+        assert np.array_equal(mean, g[f"{mode}_mean"]) and np.array_equal(sd, g[f"{mode}_sd"])
+        assert sd[5] == 0.0
+        for clr, key in ((False, "stouffer"), (True, "clr")):
+            got = port.transform_with_stats(A, mean, sd, clr)
+            assert np.array_equal(got.view(np.uint32), g[f"{mode}_{key}"].view(np.uint32)), (mode, key)
