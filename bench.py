@@ -391,7 +391,7 @@ def pipeline_arm(args, ws, rank, local):
     max-capacity closure, then the gold-standard evaluation (AUPR / AUROC of
     the MI and MCP2 networks against the synthetic GRN's edges, every other
     pair a negative) and the ensemble coefficient search over a 35-row
-    coefficient grid.  Prints one JSON line with per-stage times and
+    coefficient grid, plain and Stouffer-transformed.  Prints one JSON line with per-stage times and
     roofline fractions, and the reference CPU path's time on the host cores
     extrapolated from timed row slabs."""
     import torch
@@ -463,6 +463,10 @@ def pipeline_arm(args, ws, rank, local):
         ev["mcp2"] = r[0]
         st["combo_search"] = timed(lambda: r.__setitem__(0, h.combo_eval_dev(A, M1, M2, M3, Lb, coeffs)))
         ev["combo"] = r[0]
+        h.combo_stouffer_eval_dev(A, M1, M2, M3, Lb, coeffs[1:2])  # untimed: workspace
+        st["combo_stouffer_search"] = timed(
+            lambda: r.__setitem__(0, h.combo_stouffer_eval_dev(A, M1, M2, M3, Lb, coeffs)))
+        ev["combo_stouffer"] = r[0]
         ev["coeffs"] = coeffs
     iters = None
     if args.closure:
@@ -512,11 +516,12 @@ def pipeline_arm(args, ws, rank, local):
             stages[key] = {"ms": e_ms, "aupr": ev[key[5:]][0], "auroc": ev[key[5:]][1], "n_pos": npos,
                            "n_neg": nneg, "GB/s": ev_bytes / (e_ms / 1e3) / 1e9,
                            "frac_hbm": ev_bytes / (e_ms / 1e3) / hbm}
-        pr, roc, best = ev["combo"]
-        stages["combo_search"] = {"ms": st["combo_search"] * 1e3, "rows": len(ev["coeffs"]),
-                                  "ms_per_row": st["combo_search"] * 1e3 / (len(ev["coeffs"]) - 1),
-                                  "best_row": int(best), "best_coeffs": ev["coeffs"][best].tolist(),
-                                  "best_aupr": float(pr[best]), "best_auroc": float(roc[best])}
+        for key in ("combo_search", "combo_stouffer_search"):
+            pr, roc, best = ev["combo" if key == "combo_search" else "combo_stouffer"]
+            stages[key] = {"ms": st[key] * 1e3, "rows": len(ev["coeffs"]),
+                           "ms_per_row": st[key] * 1e3 / (len(ev["coeffs"]) - 1),
+                           "best_row": int(best), "best_coeffs": ev["coeffs"][best].tolist(),
+                           "best_aupr": float(pr[best]), "best_auroc": float(roc[best])}
     line = {"mode": "pipeline", "genes": n, "samples": m, "precision": args.precision,
             "stage_s": st, "wall_s": wall, "stages": stages, "closure_iterations": iters, "clocks": clk,
             "kernel_profile": prof, "sms": sms}

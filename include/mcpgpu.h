@@ -395,6 +395,11 @@ MCPG_API int mcpg_combo_stouffer_eval_dev(mcpg_handle* h, const float* mi, int64
                                           const int32_t* row_gene, const uint8_t* col_tf, const double* coeffs,
                                           int64_t n_coeffs, int stats_mode, double* aupr, double* auroc,
                                           int64_t* best);
+MCPG_API int mcpg_combo_stouffer_eval(mcpg_handle* h, const float* mi, int64_t ldm, const float* M1, int64_t ld1,
+                                      const float* M2, int64_t ld2, const float* M3, int64_t ld3, int64_t n,
+                                      const int8_t* labels, int64_t ldl, int region, const int32_t* row_gene,
+                                      const uint8_t* col_tf, const double* coeffs, int64_t n_coeffs, int stats_mode,
+                                      double* aupr, double* auroc, int64_t* best);
 /* Host-buffer form of mcpg_combo_eval_dev (matrices, labels, row_gene and col_tf on the host). */
 MCPG_API int mcpg_combo_eval(mcpg_handle* h, const float* mi, int64_t ldm, const float* M1, int64_t ld1,
                              const float* M2, int64_t ld2, const float* M3, int64_t ld3, int64_t rows, int64_t cols,

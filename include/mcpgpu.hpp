@@ -16,6 +16,8 @@
 //   compute_combo(mi, m1, m2, m3, c, out) mcpnet_helper.hpp:507-573
 //   compute_aupr_auroc(truth, values)     mcpnet_helper.hpp:1050-1071 (AUPR returned, AUROC too)
 //   select_combo(...)                     the coefficient loop of apps/pipeline/mcpnet.cpp:575-616
+//   compute_stouffer(in, out)             mcpnet_helper.hpp:575-586 (row statistics: see mcpgpu.h)
+//   select_combo_stouffer(...)            the Stouffer half of that loop, mcpnet.cpp:622-661
 //
 // Matrices are float, row-major with a leading dimension (the layout of
 // splash::ds::aligned_matrix<float> with its padded column_bytes()).  Errors
@@ -251,6 +253,36 @@ inline int64_t select_combo(Context& ctx, const Matrix<float>& mi, const Matrix<
                               m3.ld(), mi.rows(), mi.columns(), labels.data(), labels.ld(), (int)region, nullptr,
                               nullptr, coeffs.data(), nc, a.data(), b.data(), &best),
               "select_combo");
+    if (aupr) *aupr = a;
+    if (auroc) *auroc = b;
+    return best;
+}
+
+// compute_stouffer (or CLR with clr = true): row statistics then the per-entry transform.
+inline void compute_stouffer(Context& ctx, const Matrix<float>& in, Matrix<float>& out, bool clr = false,
+                             int stats_mode = MCPG_ROWSTATS_EXCLUDE_DIAGONAL) {
+    const int64_t n = in.rows();
+    out.resize(n, n);
+    ctx.check(mcpg_transform(ctx.handle(), in.data(), n, in.ld(), clr ? MCPG_TRANSFORM_CLR : MCPG_TRANSFORM_STOUFFER,
+                             stats_mode, out.data(), out.ld()),
+              "compute_stouffer");
+}
+
+// The Stouffer half of the coefficient search: per row the AUPR / AUROC of the
+// Stouffer-transformed combo matrix, and the reference's choice of row.
+inline int64_t select_combo_stouffer(Context& ctx, const Matrix<float>& mi, const Matrix<float>& m1,
+                                     const Matrix<float>& m2, const Matrix<float>& m3, const Matrix<int8_t>& labels,
+                                     const std::vector<double>& coeffs, std::vector<double>* aupr = nullptr,
+                                     std::vector<double>* auroc = nullptr,
+                                     TruthRegion region = TruthRegion::LowerTriangle,
+                                     int stats_mode = MCPG_ROWSTATS_EXCLUDE_DIAGONAL) {
+    const int64_t nc = (int64_t)(coeffs.size() / 4);
+    std::vector<double> a((size_t)nc), b((size_t)nc);
+    int64_t best = 0;
+    ctx.check(mcpg_combo_stouffer_eval(ctx.handle(), mi.data(), mi.ld(), m1.data(), m1.ld(), m2.data(), m2.ld(),
+                                       m3.data(), m3.ld(), mi.rows(), labels.data(), labels.ld(), (int)region,
+                                       nullptr, nullptr, coeffs.data(), nc, stats_mode, a.data(), b.data(), &best),
+              "select_combo_stouffer");
     if (aupr) *aupr = a;
     if (auroc) *auroc = b;
     return best;

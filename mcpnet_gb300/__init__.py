@@ -111,6 +111,10 @@ ABI += [
     ("mcpg_combo_stouffer_eval_dev", C.c_int, [_vp, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _i64, _vp, _i64,
                                                C.c_int, _vp, _vp, _vp, _i64, C.c_int, _vp, _vp, _vp]),
 ]
+ABI += [
+    ("mcpg_combo_stouffer_eval", C.c_int, [_vp, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _i64, _vp, _i64,
+                                           C.c_int, _vp, _vp, _vp, _i64, C.c_int, _vp, _vp, _vp]),
+]
 TRANSFORMS = {"stouffer": 0, "clr": 1}
 ROW_STATS = {"all": 0, "exclude_diagonal": 1}
 TRUTH_REGIONS = {"lower": 0, "all": 1, "tf": 2}

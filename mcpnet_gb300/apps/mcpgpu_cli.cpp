@@ -15,12 +15,13 @@
 //       mcpnet.cpp:293 do), 2 = B-spline on tensor cores, BF16 hi+lo split,
 //       3 = BF16, 4 = FP16, 5 = FP16 hi+lo.
 //   MCP (`mcp -m`, `mcpnet -m`): 1 = MCP2, 2 = MCP3, 3 = MCP4 (apps/filter/mcp.cpp:62-66),
-//       and for mcpnet 4 = ensemble MCP (apps/pipeline/mcpnet.cpp:63-68, 519-719
-//       without the Stouffer variant).
+//       and for mcpnet 4 = ensemble MCP (apps/pipeline/mcpnet.cpp:63-68, 519-719)
+//       with its Stouffer variant (row statistics: see include/mcpgpu.h).
 // mcpnet outputs follow apps/pipeline/mcpnet.cpp: <prefix>_{bs|ap|inmi}.mi.<ext>,
 // .mcp2/.mcp3/.mcp4.<ext>, and for the ensemble .mcp_<c0>_<c1>_<c2>_<c3>.<ext>
-// (coefficients with three decimals) -- every coefficient row without --eval,
-// the row of highest AUPR with it.  <ext> is the input's (exp, csv or bin).
+// and the Stouffer-transformed .mcpst_<c0>_<c1>_<c2>_<c3>.<ext> (coefficients
+// with three decimals) -- every coefficient row without --eval, the rows of
+// highest AUPR with it.  <ext> is the input's (exp, csv or bin).
 // --eval prints `Computed,auprroc,<name>,<aupr>,<auroc>` per evaluated matrix:
 //   -g list of "source target label" lines (label 1 / 0 / other = unknown):
 //      the listed pairs of known genes, source != target (select_from_list);
@@ -366,12 +367,30 @@ int main(int argc, char** argv) {
                     mcpgpu::compute_combo(ctx, mi, m1, m2, m3, c, combo);
                     std::printf("Computed,MAX Combo aupr %.12g,(%s)\n", pr[(size_t)best], coeff_tag(c).c_str());
                     write_matrix(prefix + ".mcp_" + coeff_tag(c) + ext, combo, genes, genes);
+                    // the Stouffer half (mcpnet.cpp:622-661, 691-708)
+                    std::vector<double> spr, sroc;
+                    int64_t sbest = mcpgpu::select_combo_stouffer(ctx, mi, m1, m2, m3, truth.labels, cs, &spr, &sroc,
+                                                                  truth.region);
+                    for (int64_t r = 0; r < nc; ++r)
+                        if (spr[(size_t)r] == spr[(size_t)r])
+                            std::printf("Computed,Combo Stouffer AUPR %.12g,(%s),AUROC %.12g\n", spr[(size_t)r],
+                                        coeff_tag(&cs[(size_t)(4 * r)]).c_str(), sroc[(size_t)r]);
+                    const double* sc = &cs[(size_t)(4 * sbest)];
+                    Matrix<float> st;
+                    mcpgpu::compute_combo(ctx, mi, m1, m2, m3, sc, combo);
+                    mcpgpu::compute_stouffer(ctx, combo, st);
+                    std::printf("Computed,MAX Combo AND Stouffer aupr %.12g,(%s)\n", spr[(size_t)sbest],
+                                coeff_tag(sc).c_str());
+                    write_matrix(prefix + ".mcpst_" + coeff_tag(sc) + ext, st, genes, genes);
                 } else {
+                    Matrix<float> st;
                     for (int64_t r = 0; r < nc; ++r) {
                         const double* c = &cs[(size_t)(4 * r)];
                         if (c[0] == 1 && c[1] == 0 && c[2] == 0 && c[3] == 0) continue;  // mcpnet.cpp:589
                         mcpgpu::compute_combo(ctx, mi, m1, m2, m3, c, combo);
                         write_matrix(prefix + ".mcp_" + coeff_tag(c) + ext, combo, genes, genes);
+                        mcpgpu::compute_stouffer(ctx, combo, st);
+                        write_matrix(prefix + ".mcpst_" + coeff_tag(c) + ext, st, genes, genes);
                     }
                 }
                 std::printf("ALL Combos in %.6f sec\n", now_s() - t1);

@@ -2384,4 +2384,44 @@ int mcpg_combo_stouffer_eval_dev(mcpg_handle* h, const float* mi, int64_t ldm, c
     return combo_stouffer_eval_dev(h, mats, lds, r, coeffs, n_coeffs, stats_mode, aupr, auroc, best);
 }
 
+int mcpg_combo_stouffer_eval(mcpg_handle* h, const float* mi, int64_t ldm, const float* M1, int64_t ld1,
+                             const float* M2, int64_t ld2, const float* M3, int64_t ld3, int64_t n,
+                             const int8_t* labels, int64_t ldl, int region, const int32_t* row_gene,
+                             const uint8_t* col_tf, const double* coeffs, int64_t n_coeffs, int stats_mode,
+                             double* aupr, double* auroc, int64_t* best) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    mcpg::TruthRegion r{};
+    if ((rc = truth_region(h, "combo_stouffer_eval", labels, n, n, ldl, region, row_gene, col_tf, &r))) return rc;
+    const float* src[4] = {mi, M1, M2, M3};
+    const int64_t lds[4] = {ldm, ld1, ld2, ld3};
+    const int slots[4] = {S_IN1, S_IN2, S_IN3, S_IN4};
+    const float* d[4] = {};
+    int64_t dl[4] = {n, n, n, n};
+    for (int k = 0; k < 4 && n > 0; ++k) {
+        if (!src[k]) continue;
+        if (lds[k] < n) return fail(h, MCPG_ERR_ARG, "combo_stouffer_eval: leading dimension too small");
+        float* p;
+        if ((rc = stage_in(h, slots[k], src[k], lds[k], n, n, &p, &dl[k]))) return rc;
+        d[k] = p;
+    }
+    void *lab, *aux;
+    if ((rc = scratch(h, S_EV_LAB, (size_t)(n * n), &lab))) return rc;
+    if (n > 0)
+        CK(h, cudaMemcpy2DAsync(lab, (size_t)n, labels, (size_t)ldl, (size_t)n, (size_t)n, cudaMemcpyHostToDevice,
+                                h->stream),
+           "host-to-device copy");
+    r.labels = (const int8_t*)lab;
+    r.ldl = n;
+    if (region == MCPG_TRUTH_TF && n > 0) {
+        if ((rc = scratch(h, S_EV_AUX, (size_t)(n * 4 + n), &aux))) return rc;
+        CK(h, cudaMemcpyAsync(aux, row_gene, (size_t)n * 4, cudaMemcpyHostToDevice, h->stream), "host-to-device copy");
+        CK(h, cudaMemcpyAsync((char*)aux + n * 4, col_tf, (size_t)n, cudaMemcpyHostToDevice, h->stream),
+           "host-to-device copy");
+        r.row_gene = (const int32_t*)aux;
+        r.col_tf = (const uint8_t*)aux + n * 4;
+    }
+    return combo_stouffer_eval_dev(h, d, dl, r, coeffs, n_coeffs, stats_mode, aupr, auroc, best);
+}
+
 }  // extern "C"

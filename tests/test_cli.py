@@ -144,6 +144,11 @@ def test_cli_ensemble_eval(built_lib, port, tmp_path):
     tag = "_".join(f"{c:.3f}" for c in cs[best])
     chosen = read_exp(tmp_path / f"o_inmi.mcp_{tag}.exp")
     assert np.array_equal(chosen, port.combo(A, M, M2, M3, cs[best]))
+    st = [l for l in r.stdout.splitlines() if l.startswith("Computed,Combo Stouffer AUPR")]
+    assert len(st) == len(want)
+    sbest = [l for l in r.stdout.splitlines() if l.startswith("Computed,MAX Combo AND Stouffer")][0]
+    stag = sbest.split("(")[1].split(")")[0]
+    assert (tmp_path / f"o_inmi.mcpst_{stag}.exp").exists()
     mcp2 = [l for l in r.stdout.splitlines() if l.startswith("Computed,auprroc,mcp2,")][0].split(",")
     a, b, _, _ = port.eval_truth(port.mcp(A, 2)[1], L, "all")
     assert abs(float(mcp2[3]) - a) <= 1e-11 and abs(float(mcp2[4]) - b) <= 1e-11
