@@ -185,6 +185,12 @@ def reference_arm(args, ws, rank):
     print(json.dumps(line), flush=True)
 
 
+# (kernel, precision, genes, samples, bins, order) -> (DRAM bytes per launch, ncu summary)
+MEASURED_TRAFFIC = {
+    ("mi_tc", "bf16x3", 20000, 2000, 10, 3): (43.58e9 + 1.61e9, "profiles/mi_tc_traffic_20000x2000.md"),
+}
+
+
 def workload_config(args, precision):
     return {"workload": f"bspline-mi {args.genes} genes x {args.samples} samples, {args.bins} bins, order "
                         f"{args.order}, {precision}; max-min products at n={args.genes}",
@@ -264,8 +270,12 @@ def gpu_arm(args, ws, rank, local):
             else "fallback 1.9 PFLOP/s"
         bound = "tensor"
     achieved_tf = flops / (k_ms / 1e3) / 1e12
+    # DRAM bytes of one launch from an ncu capture of this exact workload (dram__bytes_read.sum +
+    # dram__bytes_write.sum, a one-pass capture of the full-size launch); other workloads: null
+    traffic = MEASURED_TRAFFIC.get((kname, args.precision, n, m, args.bins, args.order))
     roofline = {"bound": bound, "kernel": kname, "achieved": achieved_tf, "peak": peak_tf, "unit": "TFLOP/s",
-                "frac": achieved_tf / peak_tf, "traffic": None, "peak_source": peak_src,
+                "frac": achieved_tf / peak_tf, "traffic": traffic[0] if traffic else None,
+                "traffic_source": traffic[1] if traffic else None, "peak_source": peak_src,
                 "kernel_ms": k_ms, "algorithmic_flop_per_launch": flops,
                 "note": "achieved counts 2*b^2*m flops per unordered gene pair; the hi+lo split issues 3x "
                         "that on the tensor pipe"}
