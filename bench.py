@@ -435,7 +435,9 @@ def pipeline_arm(args, ws, rank, local):
     # warm-up on a small problem (module load, workspace)
     Xs = X[:256].contiguous()
     As = torch.empty((256, 256), **f32)
-    h.bspline_mi_dev(Xs, As, b, args.order, args.precision)
+    mi_fn = ((lambda src, dst: h.ap_mi_dev(src, dst, noise=1e-5, seed=args.seed)) if args.mi_method == "ap" else
+             (lambda src, dst: h.bspline_mi_dev(src, dst, b, args.order, args.precision)))
+    mi_fn(Xs, As)
     h.set_diagonal_dev(As, 0.0)
     h.maxmins_dev(As, R2=torch.empty_like(As))
     torch.cuda.synchronize(dev)
@@ -445,7 +447,7 @@ def pipeline_arm(args, ws, rank, local):
     h.profile(True)
     st = {}
     t_all0 = time.perf_counter()
-    st["mi"] = timed(lambda: h.bspline_mi_dev(X, A, b, args.order, args.precision))
+    st["mi"] = timed(lambda: mi_fn(X, A))
     st["diagonal"] = timed(lambda: h.set_diagonal_dev(A, 0.0))
     if args.no_eval:
         st["mcp234"] = timed(lambda: h.maxmins_dev(A, R2=R2, R3=R3, R4=R4))
@@ -499,15 +501,19 @@ def pipeline_arm(args, ws, rank, local):
     mm_ms = st["mcp234"] * 1e3
     # executed min/max work: M1 and M3 symmetric (n^3 / 2 triples each), M2 full (n^3)
     mm_ops_exec = 2.0 * (0.5 + 1.0 + 0.5) * n ** 3
-    stages = {
-        "bspline_weights": {"ms": w_ms, "GB/s": w_bytes / (w_ms / 1e3) / 1e9, "frac_hbm": w_bytes / (w_ms / 1e3) / hbm},
-        "mi_tc": {"ms": tc_ms, "TFLOP/s_algorithmic": mi_flops / (tc_ms / 1e3) / 1e12,
-                  "frac_tensor_algorithmic": mi_flops / (tc_ms / 1e3) / tc_peak,
-                  "frac_tensor_issued": 3.0 * mi_flops * (128 / 120) / (tc_ms / 1e3) / tc_peak
-                  if args.precision.endswith("x3") else None},
-        "maxmin_M1_M2_M3_with_ratios": {"ms": mm_ms, "Gop/s_executed": mm_ops_exec / (mm_ms / 1e3) / 1e9,
-                                        "frac_alu_peak": mm_ops_exec / (mm_ms / 1e3) / alu_peak},
-    }
+    stages = {}
+    if args.mi_method == "ap":
+        stages["ap_mi"] = {"ms": st["mi"] * 1e3, "pairs_per_s": n * (n + 1) / 2 / st["mi"],
+                           "kernels": {k: v for k, v in prof.items() if k.startswith("ap_")}}
+    else:
+        stages["bspline_weights"] = {"ms": w_ms, "GB/s": w_bytes / (w_ms / 1e3) / 1e9,
+                                     "frac_hbm": w_bytes / (w_ms / 1e3) / hbm}
+        stages["mi_tc"] = {"ms": tc_ms, "TFLOP/s_algorithmic": mi_flops / (tc_ms / 1e3) / 1e12,
+                           "frac_tensor_algorithmic": mi_flops / (tc_ms / 1e3) / tc_peak,
+                           "frac_tensor_issued": 3.0 * mi_flops * (128 / 120) / (tc_ms / 1e3) / tc_peak
+                           if args.precision.endswith("x3") else None}
+    stages["maxmin_M1_M2_M3_with_ratios"] = {"ms": mm_ms, "Gop/s_executed": mm_ops_exec / (mm_ms / 1e3) / 1e9,
+                                             "frac_alu_peak": mm_ops_exec / (mm_ms / 1e3) / alu_peak}
     dpi_ms = st["dpi"] * 1e3
     stages["dpi"] = {"ms": dpi_ms, "removed": removed[0],
                      "frac_alu_peak": 2.0 * 0.5 * n ** 3 / (dpi_ms / 1e3) / alu_peak}
@@ -532,7 +538,7 @@ def pipeline_arm(args, ws, rank, local):
                            "ms_per_row": st[key] * 1e3 / (len(ev["coeffs"]) - 1),
                            "best_row": int(best), "best_coeffs": ev["coeffs"][best].tolist(),
                            "best_aupr": float(pr[best]), "best_auroc": float(roc[best])}
-    line = {"mode": "pipeline", "genes": n, "samples": m, "precision": args.precision,
+    line = {"mode": "pipeline", "genes": n, "samples": m, "mi_method": args.mi_method, "precision": args.precision,
             "stage_s": st, "wall_s": wall, "stages": stages, "closure_iterations": iters, "clocks": clk,
             "kernel_profile": prof, "sms": sms}
     if not args.no_cpu:
@@ -581,6 +587,8 @@ def main(argv=None):
     ap.add_argument("--bins", type=int, default=10)
     ap.add_argument("--order", type=int, default=3)
     ap.add_argument("--precision", default="bf16x3", choices=["fp32", "bf16", "bf16x3", "fp16", "fp16x3"])
+    ap.add_argument("--mi-method", default="bspline", choices=["bspline", "ap"],
+                    help="with --pipeline: B-spline MI (default) or adaptive-partitioning MI (U[0,1e-5) noise)")
     ap.add_argument("--seed", type=int, default=20260001)
     ap.add_argument("--fp32-steps", type=int, default=2)
     ap.add_argument("--maxmin-steps", type=int, default=2)
