@@ -17,7 +17,8 @@
 //    3-input max.  (BK 64 / 2 stages / LDS.128 measured best on GB300 of
 //    BK 16/32/64, 2-4 stages, LDS.64/128: at n = 20,000 BK 32 / 3 stages ran
 //    670.9 ms, BK 64 / 2 stages 656.0 ms; half as many barriers and loader
-//    rounds per min/max instruction.)
+//    rounds per min/max instruction.  A 512-thread 8 x 4 thread tile, twice the
+//    resident warps at 128 registers, ran 665.4 ms.)
 //  - fused epilogues: MCP ratio (combine.hpp:210-222), closure step
 //    B <- max(B, B (x) B) with a changed flag, DPI mask + apply
 //    (dpi.hpp:56-68, threshold.hpp:46-53) with the y in {x, z} exclusion done
@@ -45,7 +46,14 @@ namespace {
 #ifndef MCPG_MM_KSTEP
 #define MCPG_MM_KSTEP 4
 #endif
-constexpr int BM = 128, BN = 128, BK = MCPG_MM_BK, STAGES = MCPG_MM_STAGES, THREADS = 256;
+#ifndef MCPG_MM_TN
+#define MCPG_MM_TN 8
+#endif
+// Thread tile 8 x TN: 16 threads down the tile's rows, BN / TN across its columns.
+constexpr int TN = MCPG_MM_TN;
+constexpr int BM = 128, BN = 128, BK = MCPG_MM_BK, STAGES = MCPG_MM_STAGES, THREADS = 16 * (BN / TN);
+constexpr int TXS = BN / TN;  // column step between a thread's outputs
+constexpr int NTXB = TXS / 8; // column blocks of 8 threads per warp row
 constexpr int KSTEP = MCPG_MM_KSTEP;  // k values per shared-memory load (2: LDS.64, 4: LDS.128)
 constexpr int LDS = BK + 4;  // row stride in floats: 16B-aligned, 4 consecutive rows -> 4 distinct bank groups
 constexpr int TILE_FLOATS = BM * LDS;
@@ -53,11 +61,11 @@ constexpr size_t SMEM_BYTES = (size_t)STAGES * 2 * TILE_FLOATS * sizeof(float); 
 
 // Per-thread view of the operand rows it stages: with CPR = BK/4 chunks of 16
 // bytes per row, thread t copies chunk q = t % CPR of rows t / CPR + h * RSTEP
-// (h < CPR/2) of both operand tiles.
+// (h < HPT) of both operand tiles.
 constexpr int CPR = BK / 4;
-constexpr int HPT = CPR / 2;            // rows per thread per operand
 constexpr int RSTEP = THREADS / CPR;    // row step between a thread's rows
-static_assert(HPT * RSTEP * CPR == BM * CPR && BM == BN, "loader covers the tile");
+constexpr int HPT = BM / RSTEP;         // rows per thread per operand
+static_assert(HPT * RSTEP == BM && RSTEP * CPR == THREADS && BM == BN, "loader covers the tile");
 
 struct StageLoader {
     const float* a[HPT];
@@ -113,8 +121,8 @@ __global__ void __launch_bounds__(THREADS, MCPG_MM_MINB) maxmin_kernel(const Max
 
     const int tid = threadIdx.x;
     const int warp = tid >> 5, lane = tid & 31;
-    const int ty = ((warp >> 1) << 2) + (lane >> 3);  // 0..15
-    const int tx = ((warp & 1) << 3) + (lane & 7);    // 0..15
+    const int ty = ((warp / NTXB) << 2) + (lane >> 3);  // 0..15
+    const int tx = ((warp % NTXB) << 3) + (lane & 7);   // 0..TXS-1
 
     // DPI: NaN is the neutral element of the NaN-ignoring max, so an output with
     // no admissible y stays NaN and compares false (the reference keeps it).
@@ -122,28 +130,32 @@ __global__ void __launch_bounds__(THREADS, MCPG_MM_MINB) maxmin_kernel(const Max
     constexpr bool WIT = (MODE == MM_WITNESS);
     constexpr bool GEMM = (MODE == MM_GEMM);
     const float init = EXCL ? __int_as_float(0x7fc00000) : (GEMM ? 0.0f : -INFINITY);
-    int32_t kidx[WIT ? 8 : 1][WIT ? 8 : 1];
+    int32_t kidx[WIT ? 8 : 1][WIT ? TN : 1];
     if (WIT) {
 #pragma unroll
         for (int q = 0; q < (WIT ? 8 : 1); ++q)
 #pragma unroll
-            for (int r = 0; r < (WIT ? 8 : 1); ++r) kidx[q][r] = -1;
+            for (int r = 0; r < (WIT ? TN : 1); ++r) kidx[q][r] = -1;
     }
     // excluded k per owned row / column (EXCL modes)
-    int64_t exr[8], exc[8];
+    int64_t exr[8], exc[TN];
     if (EXCL) {
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
-            const int64_t i = i0 + ty + 16 * q, j = j0 + tx + 16 * q;
+            const int64_t i = i0 + ty + 16 * q;
             exr[q] = p.excl_row ? (i < p.rows ? (int64_t)p.excl_row[i] : -1) : i;
-            exc[q] = p.excl_col ? (j < p.cols ? (int64_t)p.excl_col[j] : -1) : j;
+        }
+#pragma unroll
+        for (int r = 0; r < TN; ++r) {
+            const int64_t j = j0 + tx + TXS * r;
+            exc[r] = p.excl_col ? (j < p.cols ? (int64_t)p.excl_col[j] : -1) : j;
         }
     }
-    float acc[8][8];
+    float acc[8][TN];
 #pragma unroll
     for (int q = 0; q < 8; ++q)
 #pragma unroll
-        for (int r = 0; r < 8; ++r) acc[q][r] = init;
+        for (int r = 0; r < TN; ++r) acc[q][r] = init;
 
     StageLoader ld;
     ld.init(p, i0, j0, tid);
@@ -184,8 +196,8 @@ __global__ void __launch_bounds__(THREADS, MCPG_MM_MINB) maxmin_kernel(const Max
 #pragma unroll
                     for (int q = 0; q < 8; ++q) a[q] = *reinterpret_cast<const float4*>(a_base + q * 16 * LDS + kk);
 #pragma unroll
-                    for (int r = 0; r < 8; ++r) {
-                        const float4 b = *reinterpret_cast<const float4*>(b_base + r * 16 * LDS + kk);
+                    for (int r = 0; r < TN; ++r) {
+                        const float4 b = *reinterpret_cast<const float4*>(b_base + r * TXS * LDS + kk);
 #pragma unroll
                         for (int q = 0; q < 8; ++q) {
                             if (GEMM) {
@@ -213,8 +225,8 @@ __global__ void __launch_bounds__(THREADS, MCPG_MM_MINB) maxmin_kernel(const Max
 #pragma unroll
                     for (int q = 0; q < 8; ++q) a[q] = *reinterpret_cast<const float2*>(a_base + q * 16 * LDS + kk);
 #pragma unroll
-                    for (int r = 0; r < 8; ++r) {
-                        const float2 b = *reinterpret_cast<const float2*>(b_base + r * 16 * LDS + kk);
+                    for (int r = 0; r < TN; ++r) {
+                        const float2 b = *reinterpret_cast<const float2*>(b_base + r * TXS * LDS + kk);
 #pragma unroll
                         for (int q = 0; q < 8; ++q)
                             acc[q][r] = fmax3(acc[q][r], fmin2(a[q].x, b.x), fmin2(a[q].y, b.y));
@@ -227,8 +239,8 @@ __global__ void __launch_bounds__(THREADS, MCPG_MM_MINB) maxmin_kernel(const Max
 #pragma unroll
                     for (int q = 0; q < 8; ++q) a[q] = *reinterpret_cast<const float4*>(a_base + q * 16 * LDS + kk);
 #pragma unroll
-                    for (int r = 0; r < 8; ++r) {
-                        const float4 b = *reinterpret_cast<const float4*>(b_base + r * 16 * LDS + kk);
+                    for (int r = 0; r < TN; ++r) {
+                        const float4 b = *reinterpret_cast<const float4*>(b_base + r * TXS * LDS + kk);
 #pragma unroll
                         for (int q = 0; q < 8; ++q) {
                             acc[q][r] = fmax3(acc[q][r], fmin2(a[q].x, b.x), fmin2(a[q].y, b.y));
@@ -240,15 +252,15 @@ __global__ void __launch_bounds__(THREADS, MCPG_MM_MINB) maxmin_kernel(const Max
         } else {
             for (int kk = 0; kk < (int)kmax; ++kk) {
                 const int64_t y = k0 + kk;
-                float a[8], b[8];
+                float a[8], b[TN];
 #pragma unroll
                 for (int q = 0; q < 8; ++q) a[q] = a_base[q * 16 * LDS + kk];
 #pragma unroll
-                for (int r = 0; r < 8; ++r) b[r] = b_base[r * 16 * LDS + kk];
+                for (int r = 0; r < TN; ++r) b[r] = b_base[r * TXS * LDS + kk];
 #pragma unroll
                 for (int q = 0; q < 8; ++q)
 #pragma unroll
-                    for (int r = 0; r < 8; ++r) {
+                    for (int r = 0; r < TN; ++r) {
                         if (GEMM) {
                             acc[q][r] = fmaf(a[q], b[r], acc[q][r]);
                             continue;
@@ -276,8 +288,8 @@ __global__ void __launch_bounds__(THREADS, MCPG_MM_MINB) maxmin_kernel(const Max
         const int64_t i = i0 + ty + 16 * q;
         if (i >= p.rows) continue;
 #pragma unroll
-        for (int r = 0; r < 8; ++r) {
-            const int64_t j = j0 + tx + 16 * r;
+        for (int r = 0; r < TN; ++r) {
+            const int64_t j = j0 + tx + TXS * r;
             if (j >= p.cols) continue;
             const float m = acc[q][r];
             if (MODE == MM_PLAIN || MODE == MM_EXCL || MODE == MM_GEMM) {
