@@ -1262,6 +1262,7 @@ int combo_eval_dev(mcpg_handle* h, const float* const mats[4], const int64_t lds
             sn.g[k] = gnk[k];
             sp.cs[k] = sn.cs[k] = cs[k];
         }
+        sp.kc = sn.kc = mcpg::make_combo_coef(cs);
         sp.n = P;
         sn.n = N;
         {

@@ -269,8 +269,8 @@ __global__ void keys_from_floats_kernel(const float* v, int64_t n, uint32_t* key
 }
 
 __device__ __forceinline__ float combo_at(const ComboSrc& c, int64_t i) {
-    return combo_value(c.g[0][i], c.cs[1] != 0.0 ? c.g[1][i] : 0.0f, c.cs[2] != 0.0 ? c.g[2][i] : 0.0f,
-                       c.cs[3] != 0.0 ? c.g[3][i] : 0.0f, c.cs[0], c.cs[1], c.cs[2], c.cs[3]);
+    return combo_value_ff(c.g[0][i], c.cs[1] != 0.0 ? c.g[1][i] : 0.0f, c.cs[2] != 0.0 ? c.g[2][i] : 0.0f,
+                          c.cs[3] != 0.0 ? c.g[3][i] : 0.0f, c.kc);
 }
 
 __global__ void combo_keys_kernel(ComboSrc c, uint32_t* keys, int* nan_flag) {

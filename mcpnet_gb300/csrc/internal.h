@@ -134,10 +134,28 @@ struct GatherSrc {                       // up to four matrices gathered at the 
     const float* src[4]; int64_t lds[4];
     float* dst[4];
 };
+// compute_combo coefficients prepared once per launch: kind 0 = skipped (0),
+// 1 = added as is (1), 2 = scaled; hi + lo = the double coefficient to 2^-48.
+struct ComboCoef {
+    double c[4];
+    float hi[4], lo[4];
+    int kind[4];
+};
+inline ComboCoef make_combo_coef(const double* cs) {
+    ComboCoef k;
+    for (int i = 0; i < 4; ++i) {
+        k.c[i] = cs[i];
+        k.kind[i] = cs[i] == 0.0 ? 0 : (cs[i] == 1.0 ? 1 : 2);
+        k.hi[i] = (float)cs[i];
+        k.lo[i] = (float)(cs[i] - (double)k.hi[i]);
+    }
+    return k;
+}
 struct ComboSrc {                        // gathered (mi, M1, M2, M3) and the combo coefficients
     const float* g[4];
     int64_t n;
     double cs[4];
+    ComboCoef kc;                        // make_combo_coef(cs)
 };
 // Work items of a region: rows x ceil(cols / 4096) row segments.
 int64_t truth_items(const TruthRegion& r);

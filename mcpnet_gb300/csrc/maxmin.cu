@@ -491,20 +491,19 @@ __global__ void ratio_bwd_kernel(const float* A, int64_t lda, const float* M, in
     }
 }
 
-// compute_combo (mcpnet_helper.hpp:507-573), in double with the reference's
-// summation order; explicit _rn intrinsics keep nvcc from fusing the
-// multiply-adds, so the result matches the reference built without FMA.
+// compute_combo (mcpnet_helper.hpp:507-573): combo_value_ff gives the
+// reference's double-precision result, mostly without the FP64 pipe.
 __global__ void combo_kernel(const float* mi, int64_t ldm, const float* M1, int64_t ld1, const float* M2, int64_t ld2,
-                             const float* M3, int64_t ld3, int64_t rows, int64_t cols, double a, double b, double c,
-                             double d, float* out, int64_t ldo) {
+                             const float* M3, int64_t ld3, int64_t rows, int64_t cols, const ComboCoef k, float* out,
+                             int64_t ldo) {
     const int64_t total = rows * cols;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
         const int64_t i = t / cols, j = t - i * cols;
         const float v = mi[i * ldm + j];
-        const float m1 = (b != 0.0) ? M1[i * ld1 + j] : 0.0f;
-        const float m2 = (c != 0.0) ? M2[i * ld2 + j] : 0.0f;
-        const float m3 = (d != 0.0) ? M3[i * ld3 + j] : 0.0f;
-        out[i * ldo + j] = combo_value(v, m1, m2, m3, a, b, c, d);
+        const float m1 = k.kind[1] ? M1[i * ld1 + j] : 0.0f;
+        const float m2 = k.kind[2] ? M2[i * ld2 + j] : 0.0f;
+        const float m3 = k.kind[3] ? M3[i * ld3 + j] : 0.0f;
+        out[i * ldo + j] = combo_value_ff(v, m1, m2, m3, k);
     }
 }
 
@@ -612,8 +611,8 @@ cudaError_t launch_combo(const float* mi, int64_t ldm, const float* M1, int64_t 
                          int64_t ldo, cudaStream_t stream, int64_t* launches) {
     if (rows <= 0 || cols <= 0) return cudaSuccess;
     if (launches) ++*launches;
-    combo_kernel<<<ew_blocks(rows * cols), 256, 0, stream>>>(mi, ldm, M1, ld1, M2, ld2, M3, ld3, rows, cols, cs[0],
-                                                            cs[1], cs[2], cs[3], out, ldo);
+    combo_kernel<<<ew_blocks(rows * cols), 256, 0, stream>>>(mi, ldm, M1, ld1, M2, ld2, M3, ld3, rows, cols,
+                                                            make_combo_coef(cs), out, ldo);
     return cudaGetLastError();
 }
 

@@ -23,11 +23,12 @@
 // (2 x 92 KB with the split, 4 x 46 KB without) feeds the MMAs through
 // mbarriers, and two TMEM accumulators let the epilogue of one tile overlap the
 // main loop of the next.  Only gene-tile pairs that contain some j >= i run;
-// tiles are visited in groups of GI = 32 A-tiles, B tiles outer, so that a
-// group's A tiles (32 x 0.98 MB with the split) stay resident in the 129 MB L2
-// while the B tiles stream through it once per group.  Measured at 20,000 x
-// 2,000 (BF16x3): GI 8 144.4 ms, 16 134.5 ms, 32 133.3 ms, 64 162.7 ms (the
-// group no longer fits beside the streaming B tiles).
+// tiles are visited in groups of GI A-tiles, B tiles outer, so that a group's
+// A tiles stay resident in the 129 MB L2 while the B tiles stream through it
+// once per group.  GI is the power of two that keeps a group within
+// group_bytes() of tile operands.  Measured with the split (BF16x3): at 20,000
+// x 2,000 (1 MB per A tile) GI 8 144.4 ms, 16 134.5 ms, 32 133.3 ms, 64 162.7
+// ms; at 32,768 x 4,096 (2 MB per A tile) GI 8 902 ms, 16 972 ms, 32 987 ms.
 //
 // Every mbarrier wait is bounded (2 s of %globaltimer): on expiry the kernel
 // raises *err, stops issuing work, drains what it issued (bounded), frees its
@@ -49,10 +50,9 @@ constexpr int MROWS = 128;             // MMA M
 constexpr int NCOLS = GBN * BINS;      // MMA N = 240
 constexpr int BK = 64;                 // samples per stage (128 bytes of 16-bit)
 constexpr int TMEM_COLS = 256;
-#ifndef MCPG_TC_GI
-#define MCPG_TC_GI 32
-#endif
-constexpr int GI = MCPG_TC_GI;         // A tiles per rasterization group
+// A-tile bytes of one rasterization group: 32 MB up to 2,048 samples, 16 MB beyond
+// (longer rows mean larger B tiles streaming past the group in L2).
+inline int64_t group_bytes(int64_t ldw) { return ldw <= 2048 ? (32ll << 20) : (16ll << 20); }
 constexpr uint32_t A_BYTES = MROWS * BK * 2;   // 16 KB
 constexpr uint32_t B_BYTES = NCOLS * BK * 2;   // 30 KB
 constexpr int PSTRIDE = GBN + 1;       // epilogue partials row stride (floats)
@@ -163,6 +163,7 @@ struct TcArgs {
     int64_t ldmi;
     int64_t n;
     int TI, TJ;        // A tiles (12 genes), B tiles (24 genes)
+    int GI;            // A tiles per rasterization group
     int I0, TIr;       // this launch covers A tiles [I0, I0 + TIr)
     int ktiles;        // K / 64
     float inv_m;
@@ -201,14 +202,14 @@ __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 
-// Linear tile index -> (I, J): groups of GI A tiles, B tiles outer within a
+// Linear tile index -> (I, J): groups of a.GI A tiles, B tiles outer within a
 // group.  Returns false for rectangle slots outside the upper triangle.
 __device__ __forceinline__ bool tile_of(int64_t L, const TcArgs& a, int& I, int& J) {
-    const int64_t per_group = (int64_t)GI * a.TJ;
+    const int64_t per_group = (int64_t)a.GI * a.TJ;
     const int g = (int)(L / per_group);
     const int r = (int)(L - (int64_t)g * per_group);
-    J = r / GI;
-    I = a.I0 + g * GI + (r - J * GI);
+    J = r / a.GI;
+    I = a.I0 + g * a.GI + (r - J * a.GI);
     return I < a.I0 + a.TIr && I < a.TI && J >= j_min_for(I);
 }
 
@@ -469,8 +470,17 @@ cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, int64_t ldw, 
     a.idesc = idesc_f16(fmt == 0 ? 1u : 0u, MROWS, NCOLS);
     a.err = timeout_flag;
     a.dbg = g_tc_debug_dump;
-    const int groups = (a.TIr + GI - 1) / GI;
-    const int64_t n_slots = (int64_t)groups * GI * a.TJ;
+    {
+        const int64_t tile_bytes = (int64_t)MROWS * ldw * 2 * (split ? 2 : 1);
+        int gi = 1;
+        while (gi < 64 && (int64_t)(2 * gi) * tile_bytes <= group_bytes(ldw)) gi *= 2;
+#ifdef MCPG_TC_GI
+        gi = MCPG_TC_GI;  // fixed group size (tuning builds)
+#endif
+        a.GI = gi < 4 ? 4 : gi;
+    }
+    const int groups = (a.TIr + a.GI - 1) / a.GI;
+    const int64_t n_slots = (int64_t)groups * a.GI * a.TJ;
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int64_t grid = n_slots < sms ? n_slots : sms;
