@@ -207,6 +207,18 @@ MCPG_API int mcpg_dpi_tf(mcpg_handle* h, const float* A, int64_t n, int64_t lda,
                          float* out, int64_t ldo, uint8_t* mask, int64_t* removed);
 MCPG_API int mcpg_dpi_tf_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, float tol, const float* tfs,
                              float* out, int64_t ldo, uint8_t* mask, int64_t* removed);
+/* compute_maxmins_tfs (mcpnet_helper.hpp:470-505), the TF form of the
+ * ensemble's three products.  With T the TF rows of the n x n MI matrix A
+ * (t x n, gene order; filter_local_mat_rows_by_tfs, mcpnet.cpp:317-325) and
+ * (x)m the TF-masked product of mcpg_maxmin_masked:
+ *   M1 = T (x)m A,  M2 = M1 (x)m A,  M3 = M1 (x)m (A (x)m A).
+ * Every output is t x n and nullable; T (nullable) gets the TF rows, which are
+ * the mi operand of the TF ensemble.  Nothing is written when t == 0. */
+MCPG_API int mcpg_maxmins_tf(mcpg_handle* h, const float* A, int64_t n, int64_t lda, const float* tfs, float* T,
+                             int64_t ldt, float* M1, int64_t ld1, float* M2, int64_t ld2, float* M3, int64_t ld3);
+MCPG_API int mcpg_maxmins_tf_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, const float* tfs,
+                                 float* T, int64_t ldt, float* M1, int64_t ld1, float* M2, int64_t ld2, float* M3,
+                                 int64_t ld3);
 
 /* ---- adjoints (no counterpart in the reference) ----
  * Forward/backward pairs for sample-level sensitivity of MCP scores.  Every
@@ -312,6 +324,21 @@ MCPG_API int mcpg_transform(mcpg_handle* h, const float* A, int64_t n, int64_t l
                             float* out, int64_t ldo);
 MCPG_API int mcpg_transform_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, int transform,
                                 int stats_mode, float* out, int64_t ldo);
+/* compute_stouffer_tf (mcpnet_helper.hpp:589-634) of a rows x cols (TFs x
+ * genes) matrix: z-scores of every row across its cols entries and of every
+ * column across its rows entries (splash::kernel::StandardScore<T,T,false>,
+ * absent from the reference snapshot: here FP64 two-pass mean and population
+ * standard deviation rounded to float, z = |sd| < FLT_EPSILON ? 0 :
+ * (x - mean) / sd in float), combined per entry by zscored_stouffer_kernel
+ * (include/mcp/transform/stouffer.hpp:84-100): (z_row + z_col) * sqrt(1/2). */
+MCPG_API int mcpg_stouffer_tf(mcpg_handle* h, const float* A, int64_t rows, int64_t cols, int64_t lda, float* out,
+                              int64_t ldo);
+MCPG_API int mcpg_stouffer_tf_dev(mcpg_handle* h, const float* A, int64_t rows, int64_t cols, int64_t lda,
+                                  float* out, int64_t ldo);
+/* The statistics mcpg_stouffer_tf_dev uses, into device float arrays: row_mean /
+ * row_sd (rows entries) and col_mean / col_sd (cols entries). */
+MCPG_API int mcpg_stouffer_tf_stats_dev(mcpg_handle* h, const float* A, int64_t rows, int64_t cols, int64_t lda,
+                                        float* row_mean, float* row_sd, float* col_mean, float* col_sd);
 
 /* ---- gold-standard evaluation: AUPR and AUROC ----
  * mcpg_aupr_auroc: aupr_kernel::operator()(pos, pos_count, neg, neg_count)
@@ -400,6 +427,21 @@ MCPG_API int mcpg_combo_stouffer_eval(mcpg_handle* h, const float* mi, int64_t l
                                       const int8_t* labels, int64_t ldl, int region, const int32_t* row_gene,
                                       const uint8_t* col_tf, const double* coeffs, int64_t n_coeffs, int stats_mode,
                                       double* aupr, double* auroc, int64_t* best);
+/* The Stouffer half of the TF loop (mcpnet.cpp:622-626 with --tf-input): as
+ * mcpg_combo_stouffer_eval_dev with the TF transform (mcpg_stouffer_tf_dev) of
+ * each rows x cols (TFs x genes) combo matrix; region is normally
+ * MCPG_TRUTH_TF (select_tfs_from_mat) or MCPG_TRUTH_ALL (select_from_list). */
+MCPG_API int mcpg_combo_stouffer_tf_eval_dev(mcpg_handle* h, const float* mi, int64_t ldm, const float* M1,
+                                             int64_t ld1, const float* M2, int64_t ld2, const float* M3,
+                                             int64_t ld3, int64_t rows, int64_t cols, const int8_t* labels,
+                                             int64_t ldl, int region, const int32_t* row_gene, const uint8_t* col_tf,
+                                             const double* coeffs, int64_t n_coeffs, double* aupr, double* auroc,
+                                             int64_t* best);
+MCPG_API int mcpg_combo_stouffer_tf_eval(mcpg_handle* h, const float* mi, int64_t ldm, const float* M1, int64_t ld1,
+                                         const float* M2, int64_t ld2, const float* M3, int64_t ld3, int64_t rows,
+                                         int64_t cols, const int8_t* labels, int64_t ldl, int region,
+                                         const int32_t* row_gene, const uint8_t* col_tf, const double* coeffs,
+                                         int64_t n_coeffs, double* aupr, double* auroc, int64_t* best);
 /* Host-buffer form of mcpg_combo_eval_dev (matrices, labels, row_gene and col_tf on the host). */
 MCPG_API int mcpg_combo_eval(mcpg_handle* h, const float* mi, int64_t ldm, const float* M1, int64_t ld1,
                              const float* M2, int64_t ld2, const float* M3, int64_t ld3, int64_t rows, int64_t cols,

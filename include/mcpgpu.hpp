@@ -26,6 +26,7 @@
 #pragma once
 
 #include <cstdint>
+#include <initializer_list>
 #include <stdexcept>
 #include <string>
 #include <utility>
@@ -245,13 +246,16 @@ inline Curves compute_aupr_auroc(Context& ctx, const Matrix<int8_t>& labels, con
 inline int64_t select_combo(Context& ctx, const Matrix<float>& mi, const Matrix<float>& m1, const Matrix<float>& m2,
                             const Matrix<float>& m3, const Matrix<int8_t>& labels, const std::vector<double>& coeffs,
                             std::vector<double>* aupr = nullptr, std::vector<double>* auroc = nullptr,
-                            TruthRegion region = TruthRegion::LowerTriangle) {
+                            TruthRegion region = TruthRegion::LowerTriangle,
+                            const std::vector<int32_t>* row_gene = nullptr,
+                            const std::vector<uint8_t>* col_tf = nullptr) {
     const int64_t nc = (int64_t)(coeffs.size() / 4);
     std::vector<double> a((size_t)nc), b((size_t)nc);
     int64_t best = 0;
     ctx.check(mcpg_combo_eval(ctx.handle(), mi.data(), mi.ld(), m1.data(), m1.ld(), m2.data(), m2.ld(), m3.data(),
-                              m3.ld(), mi.rows(), mi.columns(), labels.data(), labels.ld(), (int)region, nullptr,
-                              nullptr, coeffs.data(), nc, a.data(), b.data(), &best),
+                              m3.ld(), mi.rows(), mi.columns(), labels.data(), labels.ld(), (int)region,
+                              row_gene ? row_gene->data() : nullptr, col_tf ? col_tf->data() : nullptr, coeffs.data(),
+                              nc, a.data(), b.data(), &best),
               "select_combo");
     if (aupr) *aupr = a;
     if (auroc) *auroc = b;
@@ -283,6 +287,77 @@ inline int64_t select_combo_stouffer(Context& ctx, const Matrix<float>& mi, cons
                                        m3.data(), m3.ld(), mi.rows(), labels.data(), labels.ld(), (int)region,
                                        nullptr, nullptr, coeffs.data(), nc, stats_mode, a.data(), b.data(), &best),
               "select_combo_stouffer");
+    if (aupr) *aupr = a;
+    if (auroc) *auroc = b;
+    return best;
+}
+
+// ---- TF-restricted forms (--tf-input) ----
+// tfs: one value per gene, +inf for a transcription factor, -inf otherwise
+// (load_tfs, mcpnet_helper.hpp:1074-1123).  Outputs have one row per TF, in
+// gene order.
+
+// compute_mcp{2,3,4}_tfs (path_len 2..4, tf_gene_transition 0..path_len-1).
+inline void compute_mcp_tfs(Context& ctx, const Matrix<float>& g2g, const std::vector<float>& tfs, int path_len,
+                            int tf_gene_transition, Matrix<float>& dmcp, Matrix<float>* maxmin_out = nullptr) {
+    const int64_t n = g2g.rows();
+    int64_t t = 0;
+    for (float v : tfs) t += v > 0.0f;
+    dmcp.resize(t, n);
+    if (maxmin_out) maxmin_out->resize(t, n);
+    ctx.check(mcpg_mcp_tf(ctx.handle(), g2g.data(), n, g2g.ld(), tfs.data(), path_len, tf_gene_transition,
+                          maxmin_out ? maxmin_out->data() : nullptr, maxmin_out ? maxmin_out->ld() : n, dmcp.data(),
+                          dmcp.ld()),
+              "compute_mcp_tfs");
+}
+
+// dpi_tf_kernel + mask over the n x n matrix; returns the removed count.
+inline int64_t dpi_filter_tfs(Context& ctx, const Matrix<float>& input, float tolerance, const std::vector<float>& tfs,
+                              Matrix<float>& output) {
+    const int64_t n = input.rows();
+    output.resize(n, n);
+    int64_t removed = 0;
+    ctx.check(mcpg_dpi_tf(ctx.handle(), input.data(), n, input.ld(), tolerance, tfs.data(), output.data(),
+                          output.ld(), nullptr, &removed),
+              "dpi_filter_tfs");
+    return removed;
+}
+
+// compute_maxmins_tfs; tf_rows (the mi operand of the TF ensemble) gets the TF rows of g2g.
+inline void compute_maxmins_tfs(Context& ctx, const Matrix<float>& g2g, const std::vector<float>& tfs,
+                                Matrix<float>& tf_rows, Matrix<float>& m1, Matrix<float>& m2, Matrix<float>& m3) {
+    const int64_t n = g2g.rows();
+    int64_t t = 0;
+    for (float v : tfs) t += v > 0.0f;
+    for (Matrix<float>* m : {&tf_rows, &m1, &m2, &m3}) m->resize(t, n);
+    ctx.check(mcpg_maxmins_tf(ctx.handle(), g2g.data(), n, g2g.ld(), tfs.data(), tf_rows.data(), tf_rows.ld(),
+                              m1.data(), m1.ld(), m2.data(), m2.ld(), m3.data(), m3.ld()),
+              "compute_maxmins_tfs");
+}
+
+// compute_stouffer_tf of a TFs x genes matrix.
+inline void compute_stouffer_tf(Context& ctx, const Matrix<float>& in, Matrix<float>& out) {
+    out.resize(in.rows(), in.columns());
+    ctx.check(mcpg_stouffer_tf(ctx.handle(), in.data(), in.rows(), in.columns(), in.ld(), out.data(), out.ld()),
+              "compute_stouffer_tf");
+}
+
+// The Stouffer half of the TF coefficient search.
+inline int64_t select_combo_stouffer_tf(Context& ctx, const Matrix<float>& mi, const Matrix<float>& m1,
+                                        const Matrix<float>& m2, const Matrix<float>& m3, const Matrix<int8_t>& labels,
+                                        const std::vector<double>& coeffs, std::vector<double>* aupr,
+                                        std::vector<double>* auroc, TruthRegion region,
+                                        const std::vector<int32_t>* row_gene = nullptr,
+                                        const std::vector<uint8_t>* col_tf = nullptr) {
+    const int64_t nc = (int64_t)(coeffs.size() / 4);
+    std::vector<double> a((size_t)nc), b((size_t)nc);
+    int64_t best = 0;
+    ctx.check(mcpg_combo_stouffer_tf_eval(ctx.handle(), mi.data(), mi.ld(), m1.data(), m1.ld(), m2.data(), m2.ld(),
+                                          m3.data(), m3.ld(), mi.rows(), mi.columns(), labels.data(), labels.ld(),
+                                          (int)region, row_gene ? row_gene->data() : nullptr,
+                                          col_tf ? col_tf->data() : nullptr, coeffs.data(), nc, a.data(), b.data(),
+                                          &best),
+              "select_combo_stouffer_tf");
     if (aupr) *aupr = a;
     if (auroc) *auroc = b;
     return best;

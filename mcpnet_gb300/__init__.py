@@ -115,6 +115,17 @@ ABI += [
     ("mcpg_combo_stouffer_eval", C.c_int, [_vp, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _i64, _vp, _i64,
                                            C.c_int, _vp, _vp, _vp, _i64, C.c_int, _vp, _vp, _vp]),
 ]
+ABI += [
+    ("mcpg_maxmins_tf", C.c_int, [_vp, _vp, _i64, _i64, _vp] + [_vp, _i64] * 4),
+    ("mcpg_maxmins_tf_dev", C.c_int, [_vp, _vp, _i64, _i64, _vp] + [_vp, _i64] * 4),
+    ("mcpg_stouffer_tf", C.c_int, [_vp, _vp, _i64, _i64, _i64, _vp, _i64]),
+    ("mcpg_stouffer_tf_dev", C.c_int, [_vp, _vp, _i64, _i64, _i64, _vp, _i64]),
+    ("mcpg_stouffer_tf_stats_dev", C.c_int, [_vp, _vp, _i64, _i64, _i64, _vp, _vp, _vp, _vp]),
+    ("mcpg_combo_stouffer_tf_eval", C.c_int, [_vp, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _i64, _i64, _vp,
+                                              _i64, C.c_int, _vp, _vp, _vp, _i64, _vp, _vp, _vp]),
+    ("mcpg_combo_stouffer_tf_eval_dev", C.c_int, [_vp, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _i64, _i64, _vp,
+                                                  _i64, C.c_int, _vp, _vp, _vp, _i64, _vp, _vp, _vp]),
+]
 TRANSFORMS = {"stouffer": 0, "clr": 1}
 ROW_STATS = {"all": 0, "exclude_diagonal": 1}
 TRUTH_REGIONS = {"lower": 0, "all": 1, "tf": 2}
@@ -312,6 +323,29 @@ class Handle:
         self._check(self._L.mcpg_mcp_tf(self._h, _ptr(A), n, n, _ptr(tfs), path_len, transition, _ptr(M), n,
                                          _ptr(R), n), "mcp_tf")
         return M, R
+
+    def maxmins_tf(self, A, tfs):
+        """compute_maxmins_tfs: returns (T, M1, M2, M3), each t x n (T = the TF rows of A)."""
+        A = _f32(A)
+        tfs = _f32(tfs)
+        n = A.shape[0]
+        t = int((tfs > 0).sum())
+        outs = [np.empty((t, n), dtype=np.float32) for _ in range(4)]
+        args = []
+        for o in outs:
+            args += [_ptr(o), n]
+        self._check(self._L.mcpg_maxmins_tf(self._h, _ptr(A), n, n, _ptr(tfs), *args), "maxmins_tf")
+        return tuple(outs)
+
+    def maxmins_tf_dev(self, A, tfs, T=None, M1=None, M2=None, M3=None):
+        """compute_maxmins_tfs into t x n CUDA tensors (each optional); tfs is a host array."""
+        tfs = _f32(tfs)
+        n = A.shape[0]
+        args = []
+        for o in (T, M1, M2, M3):
+            args += [self._dp(o), self._ld(o) if o is not None else n]
+        self._check(self._L.mcpg_maxmins_tf_dev(self._h, self._dp(A), n, self._ld(A), _ptr(tfs), *args),
+                    "maxmins_tf_dev")
 
     def dpi_tf(self, A, tfs, tol: float = 0.1, want_mask: bool = False):
         A = _f32(A)
@@ -580,6 +614,63 @@ class Handle:
         n = A.shape[0]
         self._check(self._L.mcpg_transform_dev(self._h, self._dp(A), n, self._ld(A), TRANSFORMS[kind],
                                                 ROW_STATS[stats], self._dp(out), self._ld(out)), "transform_dev")
+
+    def stouffer_tf(self, A):
+        """compute_stouffer_tf of a t x n host matrix."""
+        A = _f32(A)
+        rows, cols = A.shape
+        out = np.empty((rows, cols), dtype=np.float32)
+        self._check(self._L.mcpg_stouffer_tf(self._h, _ptr(A), rows, cols, cols, _ptr(out), cols), "stouffer_tf")
+        return out
+
+    def stouffer_tf_dev(self, A, out):
+        rows, cols = A.shape
+        self._check(self._L.mcpg_stouffer_tf_dev(self._h, self._dp(A), rows, cols, self._ld(A), self._dp(out),
+                                                  self._ld(out)), "stouffer_tf_dev")
+
+    def stouffer_tf_stats_dev(self, A):
+        """The statistics of stouffer_tf_dev: (row_mean, row_sd, col_mean, col_sd) float32 CUDA tensors."""
+        import torch
+        rows, cols = A.shape
+        r = [torch.empty(rows, dtype=torch.float32, device=A.device) for _ in range(2)]
+        c = [torch.empty(cols, dtype=torch.float32, device=A.device) for _ in range(2)]
+        self._check(self._L.mcpg_stouffer_tf_stats_dev(self._h, self._dp(A), rows, cols, self._ld(A), self._dp(r[0]),
+                                                        self._dp(r[1]), self._dp(c[0]), self._dp(c[1])),
+                    "stouffer_tf_stats_dev")
+        return r[0], r[1], c[0], c[1]
+
+    def combo_stouffer_tf_eval(self, mi, M1, M2, M3, labels, coeffs, region="tf", row_gene=None, col_tf=None):
+        """Host form of the TF Stouffer coefficient search: (aupr, auroc, best row)."""
+        mi = _f32(mi)
+        rows, cols = mi.shape
+        keep = [None if x is None else _f32(x) for x in (M1, M2, M3)]
+        labels = np.ascontiguousarray(labels, dtype=np.int8)
+        cs = np.ascontiguousarray(np.asarray(coeffs, dtype=np.float64).reshape(-1, 4))
+        rg = None if row_gene is None else np.ascontiguousarray(row_gene, dtype=np.int32)
+        ct = None if col_tf is None else np.ascontiguousarray(col_tf, dtype=np.uint8)
+        a = np.empty(cs.shape[0], dtype=np.float64)
+        b = np.empty(cs.shape[0], dtype=np.float64)
+        best = C.c_int64(0)
+        self._check(self._L.mcpg_combo_stouffer_tf_eval(
+            self._h, _ptr(mi), cols, _ptr(keep[0]), cols, _ptr(keep[1]), cols, _ptr(keep[2]), cols, rows, cols,
+            _ptr(labels), cols, TRUTH_REGIONS[region], _ptr(rg), _ptr(ct), cs.ctypes.data, cs.shape[0], _ptr(a),
+            _ptr(b), C.byref(best)), "combo_stouffer_tf_eval")
+        return a, b, best.value
+
+    def combo_stouffer_tf_eval_dev(self, mi, M1, M2, M3, labels, coeffs, region="tf", row_gene=None, col_tf=None):
+        """The TF Stouffer coefficient search on CUDA tensors: (aupr, auroc, best row)."""
+        cs = np.ascontiguousarray(np.asarray(coeffs, dtype=np.float64).reshape(-1, 4))
+        rows, cols = mi.shape
+        ld = lambda t: self._ld(t) if t is not None else cols
+        a = np.empty(cs.shape[0], dtype=np.float64)
+        b = np.empty(cs.shape[0], dtype=np.float64)
+        best = C.c_int64(0)
+        self._check(self._L.mcpg_combo_stouffer_tf_eval_dev(
+            self._h, self._dp(mi), self._ld(mi), self._dp(M1), ld(M1), self._dp(M2), ld(M2), self._dp(M3), ld(M3),
+            rows, cols, self._dp(labels), self._ld(labels), TRUTH_REGIONS[region], self._dp(row_gene),
+            self._dp(col_tf), cs.ctypes.data, cs.shape[0], _ptr(a), _ptr(b), C.byref(best)),
+            "combo_stouffer_tf_eval_dev")
+        return a, b, best.value
 
     def row_stats_dev(self, A, mean, sd, stats="exclude_diagonal"):
         rows, cols = A.shape

@@ -5,7 +5,7 @@
 //   mcpgpu_cli mcp    -i mi.exp -o mcp.exp -m {1,2,3} [--diagonal 0] [-x maxmin.exp]
 //   mcpgpu_cli dpi    -i mi.exp -o dpi.exp [-l 0.1] [--diagonal 0]     (diagonal 0 by default)
 //   mcpgpu_cli mcpnet -i expr.exp -o prefix [--mi-method 1] [--mi-input] [-m 1 2 3 4] [-f coeffs.exp]
-//                     [--eval (-g truth.txt | -x truth.exp)] [--diagonal 0] [--seed S]
+//                     [--eval (-g truth.txt | -x truth.exp)] [--diagonal 0] [--seed S] [--tf-input tfs.txt]
 //   mcpgpu_cli convert -i a.exp -o b.csv          (no GPU needed)
 //
 // Method values keep the reference's numbering and add the GPU forms:
@@ -22,6 +22,14 @@
 // and the Stouffer-transformed .mcpst_<c0>_<c1>_<c2>_<c3>.<ext> (coefficients
 // with three decimals) -- every coefficient row without --eval, the rows of
 // highest AUPR with it.  <ext> is the input's (exp, csv or bin).
+// --tf-input (one gene name per line; load_tfs, mcpnet_helper.hpp:1074-1123)
+// restricts mcpnet to transcription-factor sources as mcpnet.cpp does: the
+// prefix gets "_tf", every output has one row per TF (gene order) and all
+// genes as columns -- the MI rows of the TFs, compute_mcp{2,3,4}_tfs with TF
+// transitions 1 / 2 / 3, the ensemble from compute_maxmins_tfs and the TF
+// Stouffer transform (compute_stouffer_tf); the truth keeps TF sources only
+// (filter_list_by_tfs / filter_mat_rows_by_tfs, then select_from_list /
+// select_tfs_from_mat).
 // --eval prints `Computed,auprroc,<name>,<aupr>,<auroc>` per evaluated matrix:
 //   -g list of "source target label" lines (label 1 / 0 / other = unknown):
 //      the listed pairs of known genes, source != target (select_from_list);
@@ -38,7 +46,9 @@
 #include <cstring>
 #include <fstream>
 #include <iostream>
+#include <cmath>
 #include <map>
+#include <set>
 #include <sstream>
 #include <string>
 #include <vector>
@@ -142,7 +152,7 @@ void write_matrix(const std::string& path, const Matrix<float>& m, const std::ve
 }
 
 struct Args {
-    std::string cmd, in, out, maxmin_out, coeffs, truth_list, truth_mat;
+    std::string cmd, in, out, maxmin_out, coeffs, truth_list, truth_mat, tf_input;
     int bins = 10, order = 3, mi_method = 1;
     std::vector<int> methods;
     float diagonal = 0.0f, tol = 0.1f;
@@ -185,6 +195,7 @@ Args parse(int argc, char** argv) {
         else if (k == "-f" || k == "--coefficients") a.coeffs = next();
         else if (k == "--eval") a.eval = true;
         else if (k == "--seed") a.seed = std::strtoull(next().c_str(), nullptr, 10);
+        else if (k == "--tf-input") a.tf_input = next();
         else throw std::runtime_error("unknown option " + k);
     }
     if (a.in.empty() || a.out.empty()) throw std::runtime_error("-i and -o are required");
@@ -213,29 +224,75 @@ std::string compute_mi(mcpgpu::Context& ctx, const Named& in, int method, int bi
     }
 }
 
-// Truth labels over the gene x gene matrix and the region they are read from.
+std::string trim(const std::string& s) {
+    const char* ws = " \t\r\n\f\v";
+    const size_t b = s.find_first_not_of(ws);
+    if (b == std::string::npos) return "";
+    return s.substr(b, s.find_last_not_of(ws) - b + 1);
+}
+
+// The TF selection of --tf-input (load_tfs, mcpnet_helper.hpp:1074-1123).
+struct TfSel {
+    bool on = false;
+    std::vector<float> tfs;         // per gene: +inf for a TF, -inf otherwise
+    std::vector<int32_t> rows;      // gene index of every TF, in gene order
+    std::vector<uint8_t> col_tf;    // per gene: 1 for a TF
+    std::vector<std::string> names;
+};
+
+TfSel load_tfs(const std::string& path, const std::vector<std::string>& genes) {
+    TfSel t;
+    if (path.empty()) return t;
+    std::ifstream f(path);
+    if (!f) throw std::runtime_error("cannot open " + path);
+    std::set<std::string> names;
+    std::string line;
+    while (std::getline(f, line)) names.insert(trim(line));
+    t.on = true;
+    for (size_t i = 0; i < genes.size(); ++i) {
+        const bool tf = names.count(trim(genes[i])) > 0;
+        t.tfs.push_back(tf ? INFINITY : -INFINITY);
+        t.col_tf.push_back(tf ? 1 : 0);
+        if (tf) {
+            t.rows.push_back((int32_t)i);
+            t.names.push_back(genes[i]);
+        }
+    }
+    return t;
+}
+
+// Truth labels over the output matrix (genes x genes, or TFs x genes) and the
+// region they are read from.
 struct Truth {
     Matrix<int8_t> labels;
     mcpgpu::TruthRegion region = mcpgpu::TruthRegion::LowerTriangle;
+    const TfSel* tf = nullptr;
 };
 
-Truth read_truth(const Args& a, const std::vector<std::string>& genes) {
+Truth read_truth(const Args& a, const std::vector<std::string>& genes, const TfSel& tf) {
     Truth t;
     const int64_t n = (int64_t)genes.size();
-    t.labels = Matrix<int8_t>(n, n);
-    for (int64_t i = 0; i < n; ++i)
+    const int64_t rows = tf.on ? (int64_t)tf.rows.size() : n;
+    t.labels = Matrix<int8_t>(rows, n);
+    for (int64_t i = 0; i < rows; ++i)
         for (int64_t j = 0; j < n; ++j) t.labels.at(i, j) = -1;
-    if (!a.truth_list.empty()) {  // read_groundtruth + select_from_list (mcpnet_helper.hpp:641-668, 840-859)
-        std::map<std::string, int64_t> id;
+    if (!a.truth_list.empty()) {
+        // read_groundtruth + select_from_list (mcpnet_helper.hpp:641-668, 840-859); with TFs only
+        // the pairs whose source is a TF (filter_list_by_tfs, mcpnet_helper.hpp:1173-1193)
+        std::map<std::string, int64_t> src, id;
         for (int64_t i = 0; i < n; ++i) id[genes[(size_t)i]] = i;
+        if (tf.on)
+            for (int64_t r = 0; r < rows; ++r) src[tf.names[(size_t)r]] = r;
+        else
+            src = id;
         std::ifstream f(a.truth_list);
         if (!f) throw std::runtime_error("cannot open " + a.truth_list);
         std::string s, d;
         int g;
         while (f >> s >> d >> g) {
             if (s == d) continue;
-            auto is = id.find(s), it = id.find(d);
-            if (is == id.end() || it == id.end()) continue;
+            auto is = src.find(s), it = id.find(d);
+            if (is == src.end() || it == id.end()) continue;
             t.labels.at(is->second, it->second) = (int8_t)((g == 1 || g == 0) ? g : -1);
         }
         t.region = mcpgpu::TruthRegion::All;
@@ -245,18 +302,21 @@ Truth read_truth(const Args& a, const std::vector<std::string>& genes) {
             throw std::runtime_error("truth matrix is " + std::to_string(m.m.rows()) + " x " +
                                      std::to_string(m.m.columns()) + ", expected " + std::to_string(n) + " x " +
                                      std::to_string(n));
-        for (int64_t i = 0; i < n; ++i)
+        // with TFs: its TF rows (filter_mat_rows_by_tfs) and select_tfs_from_mat's region
+        for (int64_t i = 0; i < rows; ++i)
             for (int64_t j = 0; j < n; ++j) {
-                const float v = m.m.at(i, j);
+                const float v = m.m.at(tf.on ? tf.rows[(size_t)i] : i, j);
                 t.labels.at(i, j) = (int8_t)(v == 1.0f ? 1 : v == 0.0f ? 0 : -1);
             }
-        t.region = mcpgpu::TruthRegion::LowerTriangle;
+        t.region = tf.on ? mcpgpu::TruthRegion::TFRows : mcpgpu::TruthRegion::LowerTriangle;
     }
+    t.tf = tf.on ? &tf : nullptr;
     return t;
 }
 
 void report(mcpgpu::Context& ctx, const Truth& t, const Matrix<float>& values, const std::string& name) {
-    mcpgpu::Curves c = mcpgpu::compute_aupr_auroc(ctx, t.labels, values, t.region);
+    mcpgpu::Curves c = mcpgpu::compute_aupr_auroc(ctx, t.labels, values, t.region, t.tf ? &t.tf->rows : nullptr,
+                                                  t.tf ? &t.tf->col_tf : nullptr);
     std::printf("Computed,auprroc,%s,%.12g,%.12g,pos=%lld,neg=%lld\n", name.c_str(), c.aupr, c.auroc,
                 (long long)c.n_pos, (long long)c.n_neg);
 }
@@ -296,6 +356,12 @@ int main(int argc, char** argv) {
             write_matrix(a.out, in.m, in.rows, in.cols);
             return 0;
         }
+        // the TF list is checked before the device is touched (mcpnet.cpp:207-211)
+        const TfSel tf = a.cmd == "mcpnet" ? load_tfs(a.tf_input, in.rows) : TfSel{};
+        if (tf.on && tf.rows.empty()) {
+            std::fprintf(stderr, "ERROR: no transcription factors in the specified file\n");
+            return 1;
+        }
         mcpgpu::Context ctx(0);
         if (a.cmd == "mi") {
             int method = a.methods.empty() ? 1 : a.methods[0];
@@ -322,10 +388,12 @@ int main(int argc, char** argv) {
         } else if (a.cmd == "mcpnet") {
             const std::string ext = ext_of(a.in);
             const std::vector<std::string>& genes = in.rows;
+            if (tf.on) std::printf("TFs specified, found %zu\n", tf.rows.size());
+            const std::vector<std::string>& row_names = tf.on ? tf.names : genes;
             Truth truth;
-            if (a.eval) truth = read_truth(a, genes);
+            if (a.eval) truth = read_truth(a, genes, tf);
             Matrix<float> mi;
-            std::string prefix = a.out;
+            std::string prefix = a.out + (tf.on ? "_tf" : "");
             if (a.mi_input) {
                 if (in.m.rows() != in.m.columns()) throw std::runtime_error("--mi-input needs a square MI matrix");
                 mi = in.m;
@@ -333,64 +401,83 @@ int main(int argc, char** argv) {
             } else {
                 prefix += compute_mi(ctx, in, a.mi_method, a.bins, a.order, a.seed, mi);
                 std::printf("Computed,MI,,%.6f,sec\n", now_s() - t0);
-                write_matrix(prefix + ".mi" + ext, mi, genes, genes);
             }
             mcpgpu::set_diagonal(mi, a.diagonal);  // mcpnet.cpp:299-308 (negative: keep)
-            if (a.eval) report(ctx, truth, mi, "mi");
+            Matrix<float> mi_tf;  // the TF rows (filter_local_mat_rows_by_tfs, mcpnet.cpp:317-325)
+            if (tf.on) {
+                mi_tf = Matrix<float>((int64_t)tf.rows.size(), mi.columns());
+                for (size_t r = 0; r < tf.rows.size(); ++r)
+                    for (int64_t j = 0; j < mi.columns(); ++j) mi_tf.at((int64_t)r, j) = mi.at(tf.rows[r], j);
+            }
+            const Matrix<float>& mi_out = tf.on ? mi_tf : mi;
+            if (a.eval) report(ctx, truth, mi_out, "mi");
+            if (!a.mi_input) write_matrix(prefix + ".mi" + ext, mi_out, row_names, genes);
             std::vector<int> ms = a.methods.empty() ? std::vector<int>{1} : a.methods;
             for (int method : ms) {
                 if (method < 1 || method > 4) throw std::runtime_error("mcpnet -m accepts 1, 2, 3, 4");
                 double t1 = now_s();
                 if (method <= 3) {
                     Matrix<float> ratio;
-                    mcpgpu::compute_mcp(ctx, mi, method + 1, ratio);
+                    if (tf.on) mcpgpu::compute_mcp_tfs(ctx, mi, tf.tfs, method + 1, method, ratio);  // mcpnet.cpp:377,428,475
+                    else mcpgpu::compute_mcp(ctx, mi, method + 1, ratio);
                     std::printf("Computed,MCP%d,,%.6f,sec\n", method + 1, now_s() - t1);
                     if (a.eval) report(ctx, truth, ratio, "mcp" + std::to_string(method + 1));
-                    write_matrix(prefix + ".mcp" + std::to_string(method + 1) + ext, ratio, genes, genes);
+                    write_matrix(prefix + ".mcp" + std::to_string(method + 1) + ext, ratio, row_names, genes);
                     continue;
                 }
                 // ensemble MCP (mcpnet.cpp:519-719)
                 std::vector<double> cs = read_coeffs(a.coeffs);
                 Matrix<float> m1, m2, m3, combo;
-                mcpgpu::compute_maxmins(ctx, mi, m1, m2, m3);
+                if (tf.on) mcpgpu::compute_maxmins_tfs(ctx, mi, tf.tfs, mi_tf, m1, m2, m3);
+                else mcpgpu::compute_maxmins(ctx, mi, m1, m2, m3);
                 std::printf("Computed,MAXMIN 1 2 3,,%.6f,sec\n", now_s() - t1);
+                const Matrix<float>& base = tf.on ? mi_tf : mi;
+                auto stouffer = [&](const Matrix<float>& c, Matrix<float>& st) {
+                    if (tf.on) mcpgpu::compute_stouffer_tf(ctx, c, st);  // mcpnet.cpp:623-628
+                    else mcpgpu::compute_stouffer(ctx, c, st);
+                };
                 const int64_t nc = (int64_t)(cs.size() / 4);
                 if (a.eval) {
+                    const std::vector<int32_t>* rg = tf.on ? &tf.rows : nullptr;
+                    const std::vector<uint8_t>* ct = tf.on ? &tf.col_tf : nullptr;
                     std::vector<double> pr, roc;
-                    int64_t best = mcpgpu::select_combo(ctx, mi, m1, m2, m3, truth.labels, cs, &pr, &roc,
-                                                        truth.region);
+                    int64_t best = mcpgpu::select_combo(ctx, base, m1, m2, m3, truth.labels, cs, &pr, &roc,
+                                                        truth.region, rg, ct);
                     for (int64_t c = 0; c < nc; ++c)
                         if (pr[(size_t)c] == pr[(size_t)c])  // rows (1,0,0,0) are skipped (NaN)
                             std::printf("Computed,Combo AUPR %.12g,(%s),AUROC %.12g\n", pr[(size_t)c],
                                         coeff_tag(&cs[(size_t)(4 * c)]).c_str(), roc[(size_t)c]);
                     const double* c = &cs[(size_t)(4 * best)];
-                    mcpgpu::compute_combo(ctx, mi, m1, m2, m3, c, combo);
+                    mcpgpu::compute_combo(ctx, base, m1, m2, m3, c, combo);
                     std::printf("Computed,MAX Combo aupr %.12g,(%s)\n", pr[(size_t)best], coeff_tag(c).c_str());
-                    write_matrix(prefix + ".mcp_" + coeff_tag(c) + ext, combo, genes, genes);
+                    write_matrix(prefix + ".mcp_" + coeff_tag(c) + ext, combo, row_names, genes);
                     // the Stouffer half (mcpnet.cpp:622-661, 691-708)
                     std::vector<double> spr, sroc;
-                    int64_t sbest = mcpgpu::select_combo_stouffer(ctx, mi, m1, m2, m3, truth.labels, cs, &spr, &sroc,
-                                                                  truth.region);
+                    int64_t sbest =
+                        tf.on ? mcpgpu::select_combo_stouffer_tf(ctx, base, m1, m2, m3, truth.labels, cs, &spr, &sroc,
+                                                                 truth.region, rg, ct)
+                              : mcpgpu::select_combo_stouffer(ctx, base, m1, m2, m3, truth.labels, cs, &spr, &sroc,
+                                                              truth.region);
                     for (int64_t r = 0; r < nc; ++r)
                         if (spr[(size_t)r] == spr[(size_t)r])
                             std::printf("Computed,Combo Stouffer AUPR %.12g,(%s),AUROC %.12g\n", spr[(size_t)r],
                                         coeff_tag(&cs[(size_t)(4 * r)]).c_str(), sroc[(size_t)r]);
                     const double* sc = &cs[(size_t)(4 * sbest)];
                     Matrix<float> st;
-                    mcpgpu::compute_combo(ctx, mi, m1, m2, m3, sc, combo);
-                    mcpgpu::compute_stouffer(ctx, combo, st);
+                    mcpgpu::compute_combo(ctx, base, m1, m2, m3, sc, combo);
+                    stouffer(combo, st);
                     std::printf("Computed,MAX Combo AND Stouffer aupr %.12g,(%s)\n", spr[(size_t)sbest],
                                 coeff_tag(sc).c_str());
-                    write_matrix(prefix + ".mcpst_" + coeff_tag(sc) + ext, st, genes, genes);
+                    write_matrix(prefix + ".mcpst_" + coeff_tag(sc) + ext, st, row_names, genes);
                 } else {
                     Matrix<float> st;
                     for (int64_t r = 0; r < nc; ++r) {
                         const double* c = &cs[(size_t)(4 * r)];
                         if (c[0] == 1 && c[1] == 0 && c[2] == 0 && c[3] == 0) continue;  // mcpnet.cpp:589
-                        mcpgpu::compute_combo(ctx, mi, m1, m2, m3, c, combo);
-                        write_matrix(prefix + ".mcp_" + coeff_tag(c) + ext, combo, genes, genes);
-                        mcpgpu::compute_stouffer(ctx, combo, st);
-                        write_matrix(prefix + ".mcpst_" + coeff_tag(c) + ext, st, genes, genes);
+                        mcpgpu::compute_combo(ctx, base, m1, m2, m3, c, combo);
+                        write_matrix(prefix + ".mcp_" + coeff_tag(c) + ext, combo, row_names, genes);
+                        stouffer(combo, st);
+                        write_matrix(prefix + ".mcpst_" + coeff_tag(c) + ext, st, row_names, genes);
                     }
                 }
                 std::printf("ALL Combos in %.6f sec\n", now_s() - t1);

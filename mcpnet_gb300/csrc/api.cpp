@@ -689,6 +689,50 @@ int mcp_tf_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, const flo
     return MCPG_OK;
 }
 
+// compute_maxmins_tfs (mcpnet_helper.hpp:470-505): with T the TF rows of A
+// (t x n, gene order) and (x)m the TF-masked product,
+//   M1 = T (x)m A,  M2 = M1 (x)m A,  M3 = M1 (x)m (A (x)m A).
+// Every output is t x n and nullable (M1 is kept in scratch when M2 or M3 needs
+// it); T_out, when given, gets T.
+int maxmins_tf_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, const float* tfs, float* T_out,
+                   int64_t ldto, float* M1, int64_t ld1, float* M2, int64_t ld2, float* M3, int64_t ld3) {
+    if (n < 0) return fail(h, MCPG_ERR_ARG, "maxmins_tf: negative size");
+    if (n == 0) return MCPG_OK;
+    if (!A || !tfs) return fail(h, MCPG_ERR_ARG, "maxmins_tf: null pointer");
+    if (lda < n || (T_out && ldto < n) || (M1 && ld1 < n) || (M2 && ld2 < n) || (M3 && ld3 < n))
+        return fail(h, MCPG_ERR_ARG, "maxmins_tf: leading dimension too small");
+    TfSet ts = tf_set(tfs, n);
+    const int64_t t = (int64_t)ts.idx.size();
+    if (t == 0) return MCPG_OK;
+    const int64_t ldt = round_up(n, 32);
+    int rc;
+    void *idx, *tg;
+    if ((rc = upload(h, S_TFEX, ts.idx.data(), (size_t)t * sizeof(int), &idx))) return rc;
+    if ((rc = scratch(h, S_TFROWS, (size_t)(t * ldt) * sizeof(float), &tg))) return rc;
+    CK(h, mcpg::launch_gather(A, lda, (const int*)idx, nullptr, t, n, (float*)tg, ldt, h->stream, &h->launches),
+       "gather kernel");
+    const float* TG = (const float*)tg;
+    if (T_out) CK(h, mcpg::launch_copy2d(TG, ldt, T_out, ldto, t, n, h->stream), "copy2d");
+    if (!M1 && !M2 && !M3) return MCPG_OK;
+    float* m1 = M1;
+    int64_t l1 = ld1;
+    if (!m1) {
+        void* p;
+        if ((rc = scratch(h, S_M3, (size_t)(t * ldt) * sizeof(float), &p))) return rc;
+        m1 = (float*)p;
+        l1 = ldt;
+    }
+    if ((rc = maxmin_masked_dev(h, TG, ldt, A, lda, t, n, n, tfs, m1, l1))) return rc;   // ttg
+    if (M2 && (rc = maxmin_masked_dev(h, m1, l1, A, lda, t, n, n, tfs, M2, ld2))) return rc;  // tttg
+    if (M3) {
+        void* g2;  // gtg = A (x)m A, symmetric
+        if ((rc = scratch(h, S_M1, (size_t)(n * ldt) * sizeof(float), &g2))) return rc;
+        if ((rc = maxmin_masked_dev(h, A, lda, A, lda, n, n, n, tfs, (float*)g2, ldt))) return rc;
+        if ((rc = maxmin_masked_dev(h, m1, l1, (const float*)g2, ldt, t, n, n, tfs, M3, ld3))) return rc;  // ttttg
+    }
+    return MCPG_OK;
+}
+
 // dpi_tf_kernel (dpi.hpp:74-110) over all (x, z), then mask<float,true>.
 int dpi_tf_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, float tol, const float* tfs, float* out,
                int64_t ldo, uint8_t* mask, int64_t* removed) {
@@ -1383,7 +1427,7 @@ int transform_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, int tr
     float* sd = mean + n;
     {
         PROF(h, "row_stats");
-        CK(h, mcpg::launch_row_stats(A, n, n, lda, stats_mode == MCPG_ROWSTATS_EXCLUDE_DIAGONAL, mean, sd, h->stream,
+        CK(h, mcpg::launch_row_stats(A, n, n, lda, stats_mode == MCPG_ROWSTATS_EXCLUDE_DIAGONAL, 1, mean, sd, h->stream,
                                      &h->launches),
            "row stats");
     }
@@ -1396,16 +1440,60 @@ int transform_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, int tr
     return MCPG_OK;
 }
 
+// compute_stouffer_tf (mcpnet_helper.hpp:589-634) of a rows x cols (TFs x genes)
+// matrix: population z-scores of every row and every column, combined by
+// zscored_stouffer_kernel (stouffer.hpp:84-100).
+int tf_stats_dev(mcpg_handle* h, const float* A, int64_t rows, int64_t cols, int64_t lda, float* rmean, float* rsd,
+                 float* cmean, float* csd) {
+    {
+        PROF(h, "row_stats");
+        CK(h, mcpg::launch_row_stats(A, rows, cols, lda, 0, 0, rmean, rsd, h->stream, &h->launches), "row stats");
+    }
+    {
+        PROF(h, "col_stats");
+        CK(h, mcpg::launch_col_stats(A, rows, cols, lda, cmean, csd, h->stream, &h->launches), "column stats");
+    }
+    return MCPG_OK;
+}
+
+int stouffer_tf_dev(mcpg_handle* h, const float* A, int64_t rows, int64_t cols, int64_t lda, float* out, int64_t ldo) {
+    if (rows < 0 || cols < 0) return fail(h, MCPG_ERR_ARG, "stouffer_tf: negative size");
+    if (rows == 0 || cols == 0) return MCPG_OK;
+    if (!A || !out || lda < cols || ldo < cols)
+        return fail(h, MCPG_ERR_ARG, "stouffer_tf: null pointer or leading dimension");
+    void* st;
+    int rc = scratch(h, S_ST_STATS, (size_t)(2 * rows + 2 * cols) * sizeof(float), &st);
+    if (rc) return rc;
+    float* rmean = (float*)st;
+    float* rsd = rmean + rows;
+    float* cmean = rsd + rows;
+    float* csd = cmean + cols;
+    if ((rc = tf_stats_dev(h, A, rows, cols, lda, rmean, rsd, cmean, csd))) return rc;
+    {
+        PROF(h, "transform");
+        CK(h, mcpg::launch_stouffer_tf(A, rows, cols, lda, rmean, rsd, cmean, csd, out, ldo, h->stream, &h->launches),
+           "TF Stouffer transform");
+    }
+    return MCPG_OK;
+}
+
+// Stouffer form of the coefficient search: stats_mode MCPG_ROWSTATS_* (square
+// matrices, mcpg_transform_dev) or ST_TF (compute_stouffer_tf, any shape).
+constexpr int ST_TF = -1;
 int combo_stouffer_eval_dev(mcpg_handle* h, const float* const mats[4], const int64_t lds[4],
                             const mcpg::TruthRegion& r, const double* coeffs, int64_t nc, int stats_mode,
                             double* aupr, double* auroc, int64_t* best) {
-    const int64_t n = r.rows;
-    if (r.rows != r.cols) return fail(h, MCPG_ERR_ARG, "combo_stouffer_eval: the matrices must be square");
+    const int64_t rows = r.rows, cols = r.cols;
+    if (stats_mode != ST_TF && rows != cols)
+        return fail(h, MCPG_ERR_ARG, "combo_stouffer_eval: the matrices must be square");
     if (nc < 0 || (nc > 0 && !coeffs)) return fail(h, MCPG_ERR_ARG, "combo_stouffer_eval: bad coefficient table");
-    if (n > 0) {
-        if (!mats[0] || lds[0] < n) return fail(h, MCPG_ERR_ARG, "combo_stouffer_eval: null mi or leading dimension");
+    const bool live = rows > 0 && cols > 0;
+    if (live) {
+        if (!mats[0] || lds[0] < cols)
+            return fail(h, MCPG_ERR_ARG, "combo_stouffer_eval: null mi or leading dimension");
         for (int k = 1; k < 4; ++k) {
-            if (mats[k] && lds[k] < n) return fail(h, MCPG_ERR_ARG, "combo_stouffer_eval: leading dimension too small");
+            if (mats[k] && lds[k] < cols)
+                return fail(h, MCPG_ERR_ARG, "combo_stouffer_eval: leading dimension too small");
             for (int64_t c = 0; c < nc; ++c)
                 if (!mats[k] && coeffs[4 * c + k] != 0.0)
                     return fail(h, MCPG_ERR_ARG, "combo_stouffer_eval: coefficient row %lld uses a null matrix",
@@ -1415,8 +1503,8 @@ int combo_stouffer_eval_dev(mcpg_handle* h, const float* const mats[4], const in
     float *cm = nullptr, *tm = nullptr;
     int64_t ldc = 0;
     int rc;
-    if ((rc = stage_out_alloc(h, S_ST_A, n, n, &cm, &ldc))) return rc;
-    if ((rc = stage_out_alloc(h, S_ST_B, n, n, &tm, &ldc))) return rc;
+    if ((rc = stage_out_alloc(h, S_ST_A, rows, cols, &cm, &ldc))) return rc;
+    if ((rc = stage_out_alloc(h, S_ST_B, rows, cols, &tm, &ldc))) return rc;
     double max_aupr = 0.0;
     int64_t co = 0;
     for (int64_t c = 0; c < nc; ++c) {
@@ -1427,14 +1515,16 @@ int combo_stouffer_eval_dev(mcpg_handle* h, const float* const mats[4], const in
             continue;
         }
         double a = 0.0, b = 0.0;
-        if (n > 0) {
+        if (live) {
             {
                 PROF(h, "combo");
-                CK(h, mcpg::launch_combo(mats[0], lds[0], mats[1], lds[1], mats[2], lds[2], mats[3], lds[3], n, n, cs,
-                                         cm, ldc, h->stream, &h->launches),
+                CK(h, mcpg::launch_combo(mats[0], lds[0], mats[1], lds[1], mats[2], lds[2], mats[3], lds[3], rows,
+                                         cols, cs, cm, ldc, h->stream, &h->launches),
                    "combo kernel");
             }
-            if ((rc = transform_dev(h, cm, n, ldc, MCPG_TRANSFORM_STOUFFER, stats_mode, tm, ldc))) return rc;
+            rc = stats_mode == ST_TF ? stouffer_tf_dev(h, cm, rows, cols, ldc, tm, ldc)
+                                     : transform_dev(h, cm, rows, ldc, MCPG_TRANSFORM_STOUFFER, stats_mode, tm, ldc);
+            if (rc) return rc;
             if ((rc = eval_truth_dev(h, tm, ldc, r, &a, &b, nullptr, nullptr))) return rc;
         }
         if (aupr) aupr[c] = a;
@@ -1445,6 +1535,43 @@ int combo_stouffer_eval_dev(mcpg_handle* h, const float* const mats[4], const in
         }
     }
     if (best) *best = co;
+    return MCPG_OK;
+}
+
+// Host inputs of the coefficient searches (mi, M1..M3, labels and the TF
+// region's row_gene / col_tf) copied to the device; r gets the device region.
+int stage_search(mcpg_handle* h, const char* name, const float* const src[4], const int64_t lds[4], int64_t rows,
+                 int64_t cols, const int8_t* labels, int64_t ldl, int region, const int32_t* row_gene,
+                 const uint8_t* col_tf, const float* d[4], int64_t dl[4], mcpg::TruthRegion* r) {
+    int rc;
+    if ((rc = truth_region(h, name, labels, rows, cols, ldl, region, row_gene, col_tf, r))) return rc;
+    const int slots[4] = {S_IN1, S_IN2, S_IN3, S_IN4};
+    for (int k = 0; k < 4; ++k) {
+        d[k] = nullptr;
+        dl[k] = cols;
+        if (!src[k] || rows <= 0 || cols <= 0) continue;
+        if (lds[k] < cols) return fail(h, MCPG_ERR_ARG, "%s: leading dimension too small", name);
+        float* p;
+        if ((rc = stage_in(h, slots[k], src[k], lds[k], rows, cols, &p, &dl[k]))) return rc;
+        d[k] = p;
+    }
+    void *lab, *aux;
+    if ((rc = scratch(h, S_EV_LAB, (size_t)(rows * cols), &lab))) return rc;
+    if (rows > 0 && cols > 0)
+        CK(h, cudaMemcpy2DAsync(lab, (size_t)cols, labels, (size_t)ldl, (size_t)cols, (size_t)rows,
+                                cudaMemcpyHostToDevice, h->stream),
+           "host-to-device copy");
+    r->labels = (const int8_t*)lab;
+    r->ldl = cols;
+    if (region == MCPG_TRUTH_TF && rows > 0 && cols > 0) {
+        if ((rc = scratch(h, S_EV_AUX, (size_t)(rows * 4 + cols), &aux))) return rc;
+        CK(h, cudaMemcpyAsync(aux, row_gene, (size_t)rows * 4, cudaMemcpyHostToDevice, h->stream),
+           "host-to-device copy");
+        CK(h, cudaMemcpyAsync((char*)aux + rows * 4, col_tf, (size_t)cols, cudaMemcpyHostToDevice, h->stream),
+           "host-to-device copy");
+        r->row_gene = (const int32_t*)aux;
+        r->col_tf = (const uint8_t*)aux + rows * 4;
+    }
     return MCPG_OK;
 }
 
@@ -2298,37 +2425,13 @@ int mcpg_combo_eval(mcpg_handle* h, const float* mi, int64_t ldm, const float* M
                     int64_t n_coeffs, double* aupr, double* auroc, int64_t* best) {
     int rc = check_handle(h);
     if (rc) return rc;
-    mcpg::TruthRegion r{};
-    if ((rc = truth_region(h, "combo_eval", labels, rows, cols, ldl, region, row_gene, col_tf, &r))) return rc;
     const float* src[4] = {mi, M1, M2, M3};
     const int64_t lds[4] = {ldm, ld1, ld2, ld3};
-    const int slots[4] = {S_IN1, S_IN2, S_IN3, S_IN4};
-    const float* d[4] = {};
-    int64_t dl[4] = {cols, cols, cols, cols};
-    for (int k = 0; k < 4 && rows > 0 && cols > 0; ++k) {
-        if (!src[k]) continue;
-        if (lds[k] < cols) return fail(h, MCPG_ERR_ARG, "combo_eval: leading dimension too small");
-        float* p;
-        if ((rc = stage_in(h, slots[k], src[k], lds[k], rows, cols, &p, &dl[k]))) return rc;
-        d[k] = p;
-    }
-    void *lab, *aux;
-    if ((rc = scratch(h, S_EV_LAB, (size_t)(rows * cols), &lab))) return rc;
-    if (rows > 0 && cols > 0)
-        CK(h, cudaMemcpy2DAsync(lab, (size_t)cols, labels, (size_t)ldl, (size_t)cols, (size_t)rows,
-                                cudaMemcpyHostToDevice, h->stream),
-           "host-to-device copy");
-    r.labels = (const int8_t*)lab;
-    r.ldl = cols;
-    if (region == MCPG_TRUTH_TF && rows > 0 && cols > 0) {
-        if ((rc = scratch(h, S_EV_AUX, (size_t)(rows * 4 + cols), &aux))) return rc;
-        CK(h, cudaMemcpyAsync(aux, row_gene, (size_t)rows * 4, cudaMemcpyHostToDevice, h->stream),
-           "host-to-device copy");
-        CK(h, cudaMemcpyAsync((char*)aux + rows * 4, col_tf, (size_t)cols, cudaMemcpyHostToDevice, h->stream),
-           "host-to-device copy");
-        r.row_gene = (const int32_t*)aux;
-        r.col_tf = (const uint8_t*)aux + rows * 4;
-    }
+    const float* d[4];
+    int64_t dl[4];
+    mcpg::TruthRegion r{};
+    if ((rc = stage_search(h, "combo_eval", src, lds, rows, cols, labels, ldl, region, row_gene, col_tf, d, dl, &r)))
+        return rc;
     return combo_eval_dev(h, d, dl, r, coeffs, n_coeffs, aupr, auroc, best);
 }
 
@@ -2342,7 +2445,7 @@ int mcpg_row_stats_dev(mcpg_handle* h, const float* A, int64_t rows, int64_t col
     if (stats_mode != MCPG_ROWSTATS_ALL && stats_mode != MCPG_ROWSTATS_EXCLUDE_DIAGONAL)
         return fail(h, MCPG_ERR_ARG, "row_stats: unknown statistics mode %d", stats_mode);
     PROF(h, "row_stats");
-    CK(h, mcpg::launch_row_stats(A, rows, cols, lda, stats_mode == MCPG_ROWSTATS_EXCLUDE_DIAGONAL, mean, sd,
+    CK(h, mcpg::launch_row_stats(A, rows, cols, lda, stats_mode == MCPG_ROWSTATS_EXCLUDE_DIAGONAL, 1, mean, sd,
                                  h->stream, &h->launches),
        "row stats");
     return MCPG_OK;
@@ -2392,37 +2495,118 @@ int mcpg_combo_stouffer_eval(mcpg_handle* h, const float* mi, int64_t ldm, const
                              double* aupr, double* auroc, int64_t* best) {
     int rc = check_handle(h);
     if (rc) return rc;
-    mcpg::TruthRegion r{};
-    if ((rc = truth_region(h, "combo_stouffer_eval", labels, n, n, ldl, region, row_gene, col_tf, &r))) return rc;
+    if (stats_mode != MCPG_ROWSTATS_ALL && stats_mode != MCPG_ROWSTATS_EXCLUDE_DIAGONAL)
+        return fail(h, MCPG_ERR_ARG, "combo_stouffer_eval: unknown statistics mode %d", stats_mode);
     const float* src[4] = {mi, M1, M2, M3};
     const int64_t lds[4] = {ldm, ld1, ld2, ld3};
-    const int slots[4] = {S_IN1, S_IN2, S_IN3, S_IN4};
-    const float* d[4] = {};
-    int64_t dl[4] = {n, n, n, n};
-    for (int k = 0; k < 4 && n > 0; ++k) {
-        if (!src[k]) continue;
-        if (lds[k] < n) return fail(h, MCPG_ERR_ARG, "combo_stouffer_eval: leading dimension too small");
-        float* p;
-        if ((rc = stage_in(h, slots[k], src[k], lds[k], n, n, &p, &dl[k]))) return rc;
-        d[k] = p;
-    }
-    void *lab, *aux;
-    if ((rc = scratch(h, S_EV_LAB, (size_t)(n * n), &lab))) return rc;
-    if (n > 0)
-        CK(h, cudaMemcpy2DAsync(lab, (size_t)n, labels, (size_t)ldl, (size_t)n, (size_t)n, cudaMemcpyHostToDevice,
-                                h->stream),
-           "host-to-device copy");
-    r.labels = (const int8_t*)lab;
-    r.ldl = n;
-    if (region == MCPG_TRUTH_TF && n > 0) {
-        if ((rc = scratch(h, S_EV_AUX, (size_t)(n * 4 + n), &aux))) return rc;
-        CK(h, cudaMemcpyAsync(aux, row_gene, (size_t)n * 4, cudaMemcpyHostToDevice, h->stream), "host-to-device copy");
-        CK(h, cudaMemcpyAsync((char*)aux + n * 4, col_tf, (size_t)n, cudaMemcpyHostToDevice, h->stream),
-           "host-to-device copy");
-        r.row_gene = (const int32_t*)aux;
-        r.col_tf = (const uint8_t*)aux + n * 4;
-    }
+    const float* d[4];
+    int64_t dl[4];
+    mcpg::TruthRegion r{};
+    if ((rc = stage_search(h, "combo_stouffer_eval", src, lds, n, n, labels, ldl, region, row_gene, col_tf, d, dl,
+                           &r)))
+        return rc;
     return combo_stouffer_eval_dev(h, d, dl, r, coeffs, n_coeffs, stats_mode, aupr, auroc, best);
+}
+
+int mcpg_combo_stouffer_tf_eval_dev(mcpg_handle* h, const float* mi, int64_t ldm, const float* M1, int64_t ld1,
+                                    const float* M2, int64_t ld2, const float* M3, int64_t ld3, int64_t rows,
+                                    int64_t cols, const int8_t* labels, int64_t ldl, int region,
+                                    const int32_t* row_gene, const uint8_t* col_tf, const double* coeffs,
+                                    int64_t n_coeffs, double* aupr, double* auroc, int64_t* best) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    mcpg::TruthRegion r{};
+    if ((rc = truth_region(h, "combo_stouffer_tf_eval", labels, rows, cols, ldl, region, row_gene, col_tf, &r)))
+        return rc;
+    const float* mats[4] = {mi, M1, M2, M3};
+    const int64_t lds[4] = {ldm, ld1, ld2, ld3};
+    return combo_stouffer_eval_dev(h, mats, lds, r, coeffs, n_coeffs, ST_TF, aupr, auroc, best);
+}
+
+int mcpg_combo_stouffer_tf_eval(mcpg_handle* h, const float* mi, int64_t ldm, const float* M1, int64_t ld1,
+                                const float* M2, int64_t ld2, const float* M3, int64_t ld3, int64_t rows, int64_t cols,
+                                const int8_t* labels, int64_t ldl, int region, const int32_t* row_gene,
+                                const uint8_t* col_tf, const double* coeffs, int64_t n_coeffs, double* aupr,
+                                double* auroc, int64_t* best) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    const float* src[4] = {mi, M1, M2, M3};
+    const int64_t lds[4] = {ldm, ld1, ld2, ld3};
+    const float* d[4];
+    int64_t dl[4];
+    mcpg::TruthRegion r{};
+    if ((rc = stage_search(h, "combo_stouffer_tf_eval", src, lds, rows, cols, labels, ldl, region, row_gene, col_tf,
+                           d, dl, &r)))
+        return rc;
+    return combo_stouffer_eval_dev(h, d, dl, r, coeffs, n_coeffs, ST_TF, aupr, auroc, best);
+}
+
+int mcpg_stouffer_tf_stats_dev(mcpg_handle* h, const float* A, int64_t rows, int64_t cols, int64_t lda,
+                               float* row_mean, float* row_sd, float* col_mean, float* col_sd) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (rows < 0 || cols < 0) return fail(h, MCPG_ERR_ARG, "stouffer_tf_stats: negative size");
+    if (rows == 0 || cols == 0) return MCPG_OK;
+    if (!A || !row_mean || !row_sd || !col_mean || !col_sd || lda < cols)
+        return fail(h, MCPG_ERR_ARG, "stouffer_tf_stats: null pointer or leading dimension");
+    return tf_stats_dev(h, A, rows, cols, lda, row_mean, row_sd, col_mean, col_sd);
+}
+
+int mcpg_stouffer_tf_dev(mcpg_handle* h, const float* A, int64_t rows, int64_t cols, int64_t lda, float* out,
+                         int64_t ldo) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    return stouffer_tf_dev(h, A, rows, cols, lda, out, ldo);
+}
+
+int mcpg_stouffer_tf(mcpg_handle* h, const float* A, int64_t rows, int64_t cols, int64_t lda, float* out,
+                     int64_t ldo) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (rows < 0 || cols < 0) return fail(h, MCPG_ERR_ARG, "stouffer_tf: negative size");
+    if (rows == 0 || cols == 0) return MCPG_OK;
+    if (!A || !out || lda < cols || ldo < cols)
+        return fail(h, MCPG_ERR_ARG, "stouffer_tf: null pointer or leading dimension");
+    float *da, *dout;
+    int64_t la, lo;
+    if ((rc = stage_in(h, S_IN0, A, lda, rows, cols, &da, &la))) return rc;
+    if ((rc = stage_out_alloc(h, S_OUT0, rows, cols, &dout, &lo))) return rc;
+    if ((rc = stouffer_tf_dev(h, da, rows, cols, la, dout, lo))) return rc;
+    if ((rc = copy_out(h, out, ldo, dout, lo, rows, cols))) return rc;
+    return finish(h);
+}
+
+int mcpg_maxmins_tf_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, const float* tfs, float* T,
+                        int64_t ldt, float* M1, int64_t ld1, float* M2, int64_t ld2, float* M3, int64_t ld3) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    return maxmins_tf_dev(h, A, n, lda, tfs, T, ldt, M1, ld1, M2, ld2, M3, ld3);
+}
+
+int mcpg_maxmins_tf(mcpg_handle* h, const float* A, int64_t n, int64_t lda, const float* tfs, float* T, int64_t ldt,
+                    float* M1, int64_t ld1, float* M2, int64_t ld2, float* M3, int64_t ld3) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (n < 0) return fail(h, MCPG_ERR_ARG, "maxmins_tf: negative size");
+    if (n == 0) return MCPG_OK;
+    if (!A || !tfs) return fail(h, MCPG_ERR_ARG, "maxmins_tf: null pointer");
+    if (lda < n || (T && ldt < n) || (M1 && ld1 < n) || (M2 && ld2 < n) || (M3 && ld3 < n))
+        return fail(h, MCPG_ERR_ARG, "maxmins_tf: leading dimension too small");
+    const int64_t t = (int64_t)tf_set(tfs, n).idx.size();
+    if (t == 0) return MCPG_OK;
+    float *da, *o[4] = {};
+    int64_t la, lo[4] = {};
+    // (the masked products use only the TF slots)
+    if ((rc = stage_in(h, S_IN2, A, lda, n, n, &da, &la))) return rc;
+    float* const host[4] = {T, M1, M2, M3};
+    const int64_t hld[4] = {ldt, ld1, ld2, ld3};
+    const int slots[4] = {S_OUT0, S_OUT1, S_IN3, S_IN4};
+    for (int k = 0; k < 4; ++k)
+        if (host[k] && (rc = stage_out_alloc(h, slots[k], t, n, &o[k], &lo[k]))) return rc;
+    if ((rc = maxmins_tf_dev(h, da, n, la, tfs, o[0], lo[0], o[1], lo[1], o[2], lo[2], o[3], lo[3]))) return rc;
+    for (int k = 0; k < 4; ++k)
+        if (host[k] && (rc = copy_out(h, host[k], hld[k], o[k], lo[k], t, n))) return rc;
+    return finish(h);
 }
 
 }  // extern "C"

@@ -218,9 +218,16 @@ cudaError_t launch_ap_mi(const uint16_t* xr, const uint16_t* order, const uint16
 
 // ---------------- Stouffer / CLR (stouffer.cu) ----------------
 // mean[i], sd[i] (float, from FP64 two-pass sums) of row i; excl_diag skips A[i][i];
-// sd uses the unbiased (N - 1) variance, 0 when N < 2.
-cudaError_t launch_row_stats(const float* A, int64_t rows, int64_t cols, int64_t lda, int excl_diag, float* mean,
-                             float* sd, cudaStream_t stream, int64_t* launches);
+// sd uses the (N - ddof) variance (ddof 1: unbiased, 0: population), 0 when N <= ddof.
+cudaError_t launch_row_stats(const float* A, int64_t rows, int64_t cols, int64_t lda, int excl_diag, int ddof,
+                             float* mean, float* sd, cudaStream_t stream, int64_t* launches);
+// mean[j], sd[j] of column j over the rows (FP64 two-pass, population variance).
+cudaError_t launch_col_stats(const float* A, int64_t rows, int64_t cols, int64_t lda, float* mean, float* sd,
+                             cudaStream_t stream, int64_t* launches);
+// out[i][j] = zscored_stouffer_kernel of the row and column z-scores of A[i][j].
+cudaError_t launch_stouffer_tf(const float* A, int64_t rows, int64_t cols, int64_t lda, const float* rmean,
+                               const float* rsd, const float* cmean, const float* csd, float* out, int64_t ldo,
+                               cudaStream_t stream, int64_t* launches);
 // out[i][j] = stouffer_vector_kernel (clr = 0) or clr_vector_kernel (clr = 1) of A[i][j]
 // with row i's and row j's statistics.
 cudaError_t launch_transform(const float* A, int64_t n, int64_t lda, const float* mean, const float* sd, int clr,

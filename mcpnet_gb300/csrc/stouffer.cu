@@ -13,6 +13,13 @@
 //       zi = (x - mean_i) * denom_i,  zj = |sd_j| < eps ? 0 : (x - mean_j) / sd_j
 //       Stouffer (zi + zj) * (float)sqrt(1/2),  CLR sqrt(zi^2 + zj^2)
 //     with explicit _rn intrinsics so nvcc contracts nothing.
+//   * the TF form (compute_stouffer_tf, mcpnet_helper.hpp:589-634) of a t x n
+//     matrix: every row z-scored across its n entries and every column across
+//     its t entries with splash::kernel::StandardScore<T,T,false> (population
+//     statistics; also absent from the snapshot -- here FP64 two-pass mean and
+//     population sd rounded to float, z = |sd| < eps ? 0 : (x - mean) / sd in
+//     float), then zscored_stouffer_kernel (stouffer.hpp:84-100):
+//     (z_row + z_col) * (float)sqrt(1/2).
 #include <cuda_runtime.h>
 #include <float.h>
 #include <stdint.h>
@@ -42,9 +49,11 @@ __device__ __forceinline__ double block_sum_d(double v, double* sh /*32*/) {
     return t;
 }
 
-// One block per row (grid-stride): two FP64 passes over the row.
+// One block per row (grid-stride): two FP64 passes over the row; the variance
+// divides by N - ddof (ddof 1: unbiased, 0: population).
 __global__ void __launch_bounds__(ST_THREADS) row_stats_kernel(const float* A, int64_t rows, int64_t cols,
-                                                               int64_t lda, int excl_diag, float* mean, float* sd) {
+                                                               int64_t lda, int excl_diag, int ddof, float* mean,
+                                                               float* sd) {
     __shared__ double sh[32];
     for (int64_t i = blockIdx.x; i < rows; i += gridDim.x) {
         const float* row = A + i * lda;
@@ -63,7 +72,7 @@ __global__ void __launch_bounds__(ST_THREADS) row_stats_kernel(const float* A, i
         const double ss = block_sum_d(q, sh);
         if (threadIdx.x == 0) {
             mean[i] = __double2float_rn(mu);
-            sd[i] = N > 1 ? __double2float_rn(__dsqrt_rn(__ddiv_rn(ss, (double)(N - 1)))) : 0.0f;
+            sd[i] = N > ddof ? __double2float_rn(__dsqrt_rn(__ddiv_rn(ss, (double)(N - ddof)))) : 0.0f;
         }
     }
 }
@@ -85,6 +94,58 @@ __global__ void transform_kernel(const float* A, int64_t n, int64_t lda, const f
     }
 }
 
+// Population statistics of each column over the rows: blocks of 32 columns x
+// CS_Y row strides (coalesced 128-byte row segments), FP64 partial sums
+// combined across the strides in a fixed order.
+constexpr int CS_Y = 8;
+__global__ void __launch_bounds__(32 * CS_Y) col_stats_kernel(const float* A, int64_t rows, int64_t cols, int64_t lda,
+                                                              float* mean, float* sd) {
+    __shared__ double sh[CS_Y][33];
+    const int64_t j = (int64_t)blockIdx.x * 32 + threadIdx.x;
+    const bool live = j < cols;
+    double s = 0.0;
+    if (live)
+        for (int64_t i = threadIdx.y; i < rows; i += CS_Y) s = __dadd_rn(s, (double)A[i * lda + j]);
+    sh[threadIdx.y][threadIdx.x] = s;
+    __syncthreads();
+    double tot = 0.0;
+    for (int y = 0; y < CS_Y; ++y) tot = __dadd_rn(tot, sh[y][threadIdx.x]);
+    const double mu = rows > 0 ? __ddiv_rn(tot, (double)rows) : 0.0;
+    __syncthreads();
+    double q = 0.0;
+    if (live)
+        for (int64_t i = threadIdx.y; i < rows; i += CS_Y) {
+            const double d = __dadd_rn((double)A[i * lda + j], -mu);
+            q = __dadd_rn(q, __dmul_rn(d, d));
+        }
+    sh[threadIdx.y][threadIdx.x] = q;
+    __syncthreads();
+    if (threadIdx.y == 0 && live) {
+        double ss = 0.0;
+        for (int y = 0; y < CS_Y; ++y) ss = __dadd_rn(ss, sh[y][threadIdx.x]);
+        mean[j] = __double2float_rn(mu);
+        sd[j] = rows > 0 ? __double2float_rn(__dsqrt_rn(__ddiv_rn(ss, (double)rows))) : 0.0f;
+    }
+}
+
+__device__ __forceinline__ float zscore(float x, float mean, float sd) {
+    return fabsf(sd) < FLT_EPSILON ? 0.0f : __fdiv_rn(__fsub_rn(x, mean), sd);
+}
+
+// zscored_stouffer_kernel over a rows x cols matrix with row and column statistics.
+__global__ void stouffer_tf_kernel(const float* A, int64_t rows, int64_t cols, int64_t lda, const float* rmean,
+                                   const float* rsd, const float* cmean, const float* csd, float* out, int64_t ldo) {
+    const float isqrt2 = 0.70710678118654752440f;
+    const int64_t total = rows * cols;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = t / cols, j = t - i * cols;
+        const float x = A[i * lda + j];
+        const float zi = zscore(x, rmean[i], rsd[i]);
+        const float zj = zscore(x, cmean[j], csd[j]);
+        out[i * ldo + j] = __fmul_rn(__fadd_rn(zi, zj), isqrt2);
+    }
+}
+
 unsigned ew_grid(int64_t total) {
     int64_t b = ceil_div(total, 256);
     if (b > 152 * 32) b = 152 * 32;
@@ -94,11 +155,11 @@ unsigned ew_grid(int64_t total) {
 
 }  // namespace
 
-cudaError_t launch_row_stats(const float* A, int64_t rows, int64_t cols, int64_t lda, int excl_diag, float* mean,
-                             float* sd, cudaStream_t st, int64_t* launches) {
+cudaError_t launch_row_stats(const float* A, int64_t rows, int64_t cols, int64_t lda, int excl_diag, int ddof,
+                             float* mean, float* sd, cudaStream_t st, int64_t* launches) {
     if (rows <= 0) return cudaSuccess;
     const int64_t grid = rows < 152 * 8 ? rows : 152 * 8;
-    row_stats_kernel<<<(unsigned)grid, ST_THREADS, 0, st>>>(A, rows, cols, lda, excl_diag, mean, sd);
+    row_stats_kernel<<<(unsigned)grid, ST_THREADS, 0, st>>>(A, rows, cols, lda, excl_diag, ddof, mean, sd);
     if (launches) ++*launches;
     return cudaGetLastError();
 }
@@ -108,6 +169,23 @@ cudaError_t launch_transform(const float* A, int64_t n, int64_t lda, const float
     if (n <= 0) return cudaSuccess;
     if (clr) transform_kernel<1><<<ew_grid(n * n), 256, 0, st>>>(A, n, lda, mean, sd, out, ldo);
     else transform_kernel<0><<<ew_grid(n * n), 256, 0, st>>>(A, n, lda, mean, sd, out, ldo);
+    if (launches) ++*launches;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_col_stats(const float* A, int64_t rows, int64_t cols, int64_t lda, float* mean, float* sd,
+                             cudaStream_t st, int64_t* launches) {
+    if (cols <= 0) return cudaSuccess;
+    col_stats_kernel<<<(unsigned)ceil_div(cols, 32), dim3(32, CS_Y), 0, st>>>(A, rows, cols, lda, mean, sd);
+    if (launches) ++*launches;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stouffer_tf(const float* A, int64_t rows, int64_t cols, int64_t lda, const float* rmean,
+                               const float* rsd, const float* cmean, const float* csd, float* out, int64_t ldo,
+                               cudaStream_t st, int64_t* launches) {
+    if (rows <= 0 || cols <= 0) return cudaSuccess;
+    stouffer_tf_kernel<<<ew_grid(rows * cols), 256, 0, st>>>(A, rows, cols, lda, rmean, rsd, cmean, csd, out, ldo);
     if (launches) ++*launches;
     return cudaGetLastError();
 }

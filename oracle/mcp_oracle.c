@@ -281,6 +281,61 @@ void orc_row_stats(const float* A, int64_t rows, int64_t cols, int64_t lda, int 
     }
 }
 
+/* orc_row_stats with the population (N) variance, the row half of
+ * compute_stouffer_tf (StandardScore<T,T,false>). */
+void orc_row_stats_pop(const float* A, int64_t rows, int64_t cols, int64_t lda, float* mean, float* sd) {
+    for (int64_t i = 0; i < rows; ++i) {
+        const float* r = A + i * lda;
+        double s = 0.0;
+        for (int64_t j = 0; j < cols; ++j) s += (double)r[j];
+        const double mu = cols > 0 ? s / (double)cols : 0.0;
+        double q = 0.0;
+        for (int64_t j = 0; j < cols; ++j) {
+            const double d = (double)r[j] - mu;
+            q += d * d;
+        }
+        mean[i] = (float)mu;
+        sd[i] = cols > 0 ? (float)sqrt(q / (double)cols) : 0.0f;
+    }
+}
+
+/* Population statistics of each column of a rows x cols matrix (FP64
+ * two-pass, rounded to float): the column half of compute_stouffer_tf
+ * (mcpnet_helper.hpp:600-614; StandardScore<T,T,false> on the transpose). */
+void orc_col_stats(const float* A, int64_t rows, int64_t cols, int64_t lda, float* mean, float* sd) {
+    for (int64_t j = 0; j < cols; ++j) {
+        double s = 0.0;
+        for (int64_t i = 0; i < rows; ++i) s += (double)A[i * lda + j];
+        const double mu = rows > 0 ? s / (double)rows : 0.0;
+        double q = 0.0;
+        for (int64_t i = 0; i < rows; ++i) {
+            const double d = (double)A[i * lda + j] - mu;
+            q += d * d;
+        }
+        mean[j] = (float)mu;
+        sd[j] = rows > 0 ? (float)sqrt(q / (double)rows) : 0.0f;
+    }
+}
+
+/* compute_stouffer_tf (mcpnet_helper.hpp:589-634) given the row statistics
+ * (population, over each row's cols entries) and the column statistics: the
+ * z-scores in float, |sd| < FLT_EPSILON -> 0, then zscored_stouffer_kernel
+ * (include/mcp/transform/stouffer.hpp:84-100): (z_row + z_col) * sqrt(1/2).
+ * The z matrices go to zr / zc when those are not null (rows x cols, ld cols). */
+void orc_stouffer_tf(const float* A, int64_t rows, int64_t cols, int64_t lda, const float* rmean, const float* rsd,
+                     const float* cmean, const float* csd, float* out, int64_t ldo, float* zr, float* zc) {
+    const float isqrt2 = 0.70710678118654752440f;
+    for (int64_t i = 0; i < rows; ++i)
+        for (int64_t j = 0; j < cols; ++j) {
+            const float x = A[i * lda + j];
+            const float zi = (fabsf(rsd[i]) < FLT_EPSILON) ? 0.0f : (x - rmean[i]) / rsd[i];
+            const float zj = (fabsf(csd[j]) < FLT_EPSILON) ? 0.0f : (x - cmean[j]) / csd[j];
+            if (zr) zr[i * cols + j] = zi;
+            if (zc) zc[i * cols + j] = zj;
+            out[i * ldo + j] = (zi + zj) * isqrt2;
+        }
+}
+
 /* stouffer_vector_kernel (include/mcp/transform/stouffer.hpp:57-82) and
  * clr_vector_kernel (include/mcp/transform/clr.hpp:52-73) for every row, with
  * row i's statistics as aux1 and every row's as aux2; float arithmetic. */

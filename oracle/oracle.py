@@ -100,6 +100,16 @@ class _TfCompositions:
             M = mm(M2, M1, transition in (2, 3))
         return M, self.ratio(tg, M)
 
+    def maxmins_tf(self, A, tfs):
+        """compute_maxmins_tfs (apps/pipeline/mcpnet_helper.hpp:470-505): (T, M1, M2, M3)."""
+        A = np.ascontiguousarray(A, dtype=np.float32)
+        tfs = np.ascontiguousarray(tfs, dtype=np.float32)
+        tg = self.tf_rows(A, tfs)
+        M1 = self.maxmin_masked(tg, A, tfs)             # ttg
+        M2 = self.maxmin_masked(M1, A, tfs)             # tttg
+        M3 = self.maxmin_masked(M1, self.maxmin_masked(A, A, tfs), tfs)  # ttttg
+        return tg, M1, M2, M3
+
 
 class _EvalCompositions:
     """compute_aupr_auroc and the ensemble coefficient search composed from
@@ -128,6 +138,21 @@ class _EvalCompositions:
                 top, best = pr[i], i
         return pr, roc, best
 
+    def combo_stouffer_tf_eval(self, mi, M1, M2, M3, labels, coeffs, region="tf", row_gene=None, col_tf=None):
+        """The TF Stouffer half of the loop (apps/pipeline/mcpnet.cpp:622-661 with --tf-input)."""
+        cs = np.asarray(coeffs, dtype=np.float64).reshape(-1, 4)
+        pr = np.full(cs.shape[0], np.nan)
+        roc = np.full(cs.shape[0], np.nan)
+        best, top = 0, 0.0
+        for i, c in enumerate(cs):
+            if c[0] == 1 and c[1] == 0 and c[2] == 0 and c[3] == 0:
+                continue
+            R = port().stouffer_tf(port().combo(mi, M1, M2, M3, c))
+            pr[i], roc[i], _, _ = self.eval_truth(R, labels, region, row_gene, col_tf)
+            if pr[i] > top:
+                top, best = pr[i], i
+        return pr, roc, best
+
 
 class _Port(_TfCompositions, _EvalCompositions):
     """The C restatement (float and double)."""
@@ -146,6 +171,9 @@ class _Port(_TfCompositions, _EvalCompositions):
         self.L.orc_ranks_desc.argtypes = [_vp, _i64, _i64, _i64, _vp]
         self.L.orc_row_stats.argtypes = [_vp, _i64, _i64, _i64, C.c_int, _vp, _vp]
         self.L.orc_transform.argtypes = [_vp, _i64, _i64, _vp, _vp, C.c_int, _vp, _i64]
+        self.L.orc_row_stats_pop.argtypes = [_vp, _i64, _i64, _i64, _vp, _vp]
+        self.L.orc_col_stats.argtypes = [_vp, _i64, _i64, _i64, _vp, _vp]
+        self.L.orc_stouffer_tf.argtypes = [_vp, _i64, _i64, _i64, _vp, _vp, _vp, _vp, _vp, _i64, _vp, _vp]
         self.L.orc_ap_mi.argtypes = [_vp, _i64, _i64, _vp, _i64]
 
     @staticmethod
@@ -313,6 +341,34 @@ class _Port(_TfCompositions, _EvalCompositions):
         mean, sd = self.row_stats(A, mode)
         return self.transform_with_stats(A, mean, sd, clr)
 
+    def tf_stats(self, A):
+        """Population row and column statistics of a t x n matrix, FP64 rounded to float (stand in for
+        StandardScore<T,T,false>): (row_mean, row_sd, col_mean, col_sd)."""
+        A = np.ascontiguousarray(A, dtype=np.float32)
+        rows, cols = A.shape
+        rm, rs = np.empty(rows, np.float32), np.empty(rows, np.float32)
+        cm, cs = np.empty(cols, np.float32), np.empty(cols, np.float32)
+        self.L.orc_row_stats_pop(A.ctypes.data, rows, cols, cols, rm.ctypes.data, rs.ctypes.data)
+        self.L.orc_col_stats(A.ctypes.data, rows, cols, cols, cm.ctypes.data, cs.ctypes.data)
+        return rm, rs, cm, cs
+
+    def stouffer_tf_with_stats(self, A, rmean, rsd, cmean, csd, want_z=False):
+        """compute_stouffer_tf given the statistics; with want_z also the row / column z-score matrices."""
+        A = np.ascontiguousarray(A, dtype=np.float32)
+        rows, cols = A.shape
+        f = lambda v: np.ascontiguousarray(v, dtype=np.float32)
+        rmean, rsd, cmean, csd = f(rmean), f(rsd), f(cmean), f(csd)
+        out = np.empty_like(A)
+        zr = np.empty_like(A) if want_z else None
+        zc = np.empty_like(A) if want_z else None
+        self.L.orc_stouffer_tf(A.ctypes.data, rows, cols, cols, rmean.ctypes.data, rsd.ctypes.data, cmean.ctypes.data,
+                               csd.ctypes.data, out.ctypes.data, cols, None if zr is None else zr.ctypes.data,
+                               None if zc is None else zc.ctypes.data)
+        return (out, zr, zc) if want_z else out
+
+    def stouffer_tf(self, A):
+        return self.stouffer_tf_with_stats(A, *self.tf_stats(A))
+
     def ap_ranks(self, X):
         """Descending ranks per gene, ties sharing the lowest rank (int64, n x m)."""
         X = np.ascontiguousarray(X, dtype=np.float32)
@@ -390,6 +446,7 @@ class _Ref(_TfCompositions, _EvalCompositions):
         L.ref_aupr_auroc_f32.argtypes = [_vp, _i64, _vp, _i64, _vp]
         L.ref_ap_mi_f32.argtypes = [_vp, _i64, _i64, _vp, _i64]
         L.ref_transform_f32.argtypes = [_vp, _i64, _i64, _vp, _vp, C.c_int, _vp, _i64]
+        L.ref_zscored_stouffer_f32.argtypes = [_vp, _vp, _i64, _i64, _vp]
         L.ref_aupr_auroc_f64.argtypes = [_vp, _i64, _vp, _i64, _vp]
         self.L = L
 
@@ -410,6 +467,15 @@ class _Ref(_TfCompositions, _EvalCompositions):
         sd = np.ascontiguousarray(sd, dtype=np.float32)
         out = np.empty_like(A)
         self.L.ref_transform_f32(A.ctypes.data, n, n, mean.ctypes.data, sd.ctypes.data, int(clr), out.ctypes.data, n)
+        return out
+
+    def zscored_stouffer(self, zi, zj):
+        """MCPNet's zscored_stouffer_kernel on row-aligned row / column z-score matrices."""
+        zi = np.ascontiguousarray(zi, dtype=np.float32)
+        zj = np.ascontiguousarray(zj, dtype=np.float32)
+        rows, cols = zi.shape
+        out = np.empty_like(zi)
+        self.L.ref_zscored_stouffer_f32(zi.ctypes.data, zj.ctypes.data, rows, cols, out.ctypes.data)
         return out
 
     def ap_mi(self, R):

@@ -267,4 +267,12 @@ void ref_transform_f32(const float* A, int64_t n, int64_t lda, const float* mean
     }
 }
 
+// zscored_stouffer_kernel<float> (include/mcp/transform/stouffer.hpp:84-100)
+// over rows of the row z-scores zi and column z-scores zj (rows x cols, ld
+// cols), as the BinaryOp pattern of compute_stouffer_tf hands them over.
+void ref_zscored_stouffer_f32(const float* zi, const float* zj, int64_t rows, int64_t cols, float* out) {
+    mcp::kernel::zscored_stouffer_kernel<float> k;
+    for (int64_t i = 0; i < rows; ++i) k(zi + i * cols, zj + i * cols, (size_t)cols, out + i * cols);
+}
+
 }  // extern "C"

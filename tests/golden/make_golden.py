@@ -29,8 +29,15 @@ Fixtures (all float32 unless noted):
   eval_truth.npz an MI matrix, its max-min products, int8 truth labels from the
                  synthetic GRN, TF rows, and AUPR / AUROC of each truth region
                  and of a coefficient table of combo scores
+  tf_ensemble.npz  the TF ensemble on eval_truth's matrix and TFs: T, M1, M2, M3
+                 of compute_maxmins_tfs from the reference's masked max-min
+                 kernel; a t x n matrix with a constant row and column, its
+                 (oracle) statistics and the reference's zscored_stouffer_kernel
+                 output; the combo and TF-Stouffer coefficient searches over the
+                 TF truth rows
 
     python tests/golden/make_golden.py --only eval   # regenerate the eval fixtures only
+    python tests/golden/make_golden.py --only tf     # the TF ensemble fixture only
 """
 from __future__ import annotations
 
@@ -54,7 +61,7 @@ def synth(n, m, seed):
 def main():
     import argparse
     ap = argparse.ArgumentParser()
-    ap.add_argument("--only", choices=["core", "eval", "ap", "stouffer"], default=None)
+    ap.add_argument("--only", choices=["core", "eval", "ap", "stouffer", "tf"], default=None)
     args = ap.parse_args()
     O.build(with_ref=True)
     R = O.ref()
@@ -68,6 +75,8 @@ def main():
         ap_mi(R)
     if args.only in (None, "stouffer"):
         stouffer(R)
+    if args.only in (None, "tf"):
+        tf_ensemble(R)
     print("wrote", sorted(p.name for p in HERE.glob("*.npz")))
 
 
@@ -241,6 +250,30 @@ def stouffer(R):
         out[f"{mode}_stouffer"] = R.transform_with_stats(A, mean, sd, clr=False)
         out[f"{mode}_clr"] = R.transform_with_stats(A, mean, sd, clr=True)
     np.savez_compressed(HERE / "stouffer.npz", **out)
+
+def tf_ensemble(R):
+    P = O.port()
+    with np.load(HERE / "eval_truth.npz") as z:
+        A, labels, tf_idx, col_tf, cs = z["A"], z["labels"], z["tf_idx"], z["col_tf"], z["coeffs"]
+    n = A.shape[0]
+    tfs = np.full(n, -np.inf, dtype=np.float32)
+    tfs[tf_idx] = np.inf
+    T, M1, M2, M3 = R.maxmins_tf(A, tfs)
+    out = {"A": A, "tfs": tfs, "T": T, "M1": M1, "M2": M2, "M3": M3}
+    S = P.combo(T, M1, M2, M3, np.array([0.25, 0.25, 0.25, 0.25]))
+    S[3, :] = np.float32(0.5)   # a constant row and a constant column: sd 0 -> z 0
+    S[:, 7] = np.float32(0.5)
+    rm, rs, cm, csd = P.tf_stats(S)
+    _, zr, zc = P.stouffer_tf_with_stats(S, rm, rs, cm, csd, want_z=True)
+    out.update(st_in=S, st_rmean=rm, st_rsd=rs, st_cmean=cm, st_csd=csd, st_out=R.zscored_stouffer(zr, zc))
+    lab = np.ascontiguousarray(labels[tf_idx])
+    out.update(labels_tf=lab, row_gene=tf_idx.astype(np.int32), col_tf=col_tf, coeffs=cs)
+    pr, roc, best = R.combo_eval(T, M1, M2, M3, lab, cs, "tf", tf_idx, col_tf)
+    out.update(combo_aupr=pr, combo_auroc=roc, combo_best=np.int64(best))
+    pr, roc, best = R.combo_stouffer_tf_eval(T, M1, M2, M3, lab, cs, "tf", tf_idx, col_tf)
+    out.update(st_aupr=pr, st_auroc=roc, st_best=np.int64(best))
+    np.savez_compressed(HERE / "tf_ensemble.npz", **out)
+
 
 if __name__ == "__main__":
     main()

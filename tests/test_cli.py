@@ -56,10 +56,12 @@ def test_cli_pipeline_matches_oracle(built_lib, port, tmp_path):
     write_exp(tmp_path / "x.exp", X)
     r = run("mcpnet", "-i", tmp_path / "x.exp", "-o", tmp_path / "out", "--mi-method", "0", "-m", "1", "2", "3")
     assert r.returncode == 0, r.stderr
-    mi = read_exp(tmp_path / "out_bs.mi.exp")
-    np.testing.assert_allclose(mi, port.bspline_mi(X.astype(np.float64)), rtol=0, atol=2e-5)
+    mi = read_exp(tmp_path / "out_bs.mi.exp")  # written after the diagonal reset, as mcpnet.cpp:299-356
+    want = port.bspline_mi(X.astype(np.float64))
+    np.fill_diagonal(want, 0)
+    np.testing.assert_allclose(mi, want, rtol=0, atol=2e-5)
+    assert not np.diag(mi).any()
     A = mi.copy()
-    np.fill_diagonal(A, 0)
     for k, pl in ((2, 2), (3, 3), (4, 4)):
         got = read_exp(tmp_path / f"out_bs.mcp{k}.exp")
         assert np.array_equal(got, port.mcp(A, pl)[1])
@@ -152,3 +154,86 @@ def test_cli_ensemble_eval(built_lib, port, tmp_path):
     mcp2 = [l for l in r.stdout.splitlines() if l.startswith("Computed,auprroc,mcp2,")][0].split(",")
     a, b, _, _ = port.eval_truth(port.mcp(A, 2)[1], L, "all")
     assert abs(float(mcp2[3]) - a) <= 1e-11 and abs(float(mcp2[4]) - b) <= 1e-11
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("truth", ["matrix", "list"])
+def test_cli_tf_input(built_lib, port, tmp_path, truth):
+    """mcpnet --tf-input: TF rows only, compute_mcp{2,3,4}_tfs with transitions
+    1 / 2 / 3, the TF ensemble and its TF Stouffer search, the truth reduced to
+    TF sources -- against the oracle's composition of the reference's steps."""
+    n = 64
+    X, E = built_lib.synth_grn(n, 240, seed=21, with_edges=True)
+    A = port.bspline_mi(X)
+    np.fill_diagonal(A, 0)
+    names = [f"g{i}" for i in range(n)]
+    write_exp(tmp_path / "mi.exp", A, names)
+    tf_rows = np.array([i for i in range(n) if i % 5 == 1 or i in (0, 2)], np.int32)
+    with open(tmp_path / "tfs.txt", "w") as f:
+        f.write("  missing_gene \n")
+        for i in tf_rows:
+            f.write(f" g{i}\t\n")
+    tfs = np.full(n, -np.inf, np.float32)
+    tfs[tf_rows] = np.inf
+    col_tf = (tfs > 0).astype(np.uint8)
+    rng = np.random.default_rng(4)
+    L = np.full((n, n), -1, np.int8)
+    for s, t in E:
+        L[s, t] = L[t, s] = 1
+    for _ in range(900):
+        s, t = rng.integers(0, n, 2)
+        if s != t and L[s, t] == -1:
+            L[s, t] = L[t, s] = 0
+    if truth == "matrix":
+        write_exp(tmp_path / "truth.exp", L.astype(np.float32), names)
+        targs = ["-x", tmp_path / "truth.exp"]
+        Lt, region, rg, ct = L[tf_rows], "tf", tf_rows, col_tf
+    else:
+        with open(tmp_path / "truth.txt", "w") as f:
+            for s in range(n):
+                for t in range(n):
+                    if L[s, t] in (0, 1):
+                        f.write(f"g{s}\tg{t}\t{L[s, t]}\n")
+        targs = ["-g", tmp_path / "truth.txt"]
+        Lt = L[tf_rows].copy()
+        Lt[np.arange(len(tf_rows)), tf_rows] = -1
+        region, rg, ct = "all", None, None
+    cs = np.array([[0.25, 0.25, 0.25, 0.25], [0.5, 0.5, 0, 0], [0, 1, 0, 0], [0.2, 0.3, 0.1, 0.4]])
+    np.savetxt(tmp_path / "coeffs.txt", cs)
+    r = run("mcpnet", "-i", tmp_path / "mi.exp", "-o", tmp_path / "o", "--mi-input", "--tf-input",
+            tmp_path / "tfs.txt", "-m", "1", "2", "3", "4", "-f", tmp_path / "coeffs.txt", "--eval", *targs)
+    assert r.returncode == 0, r.stderr
+    out = lambda name: read_exp(tmp_path / f"o_tf_inmi.{name}.exp")
+    header = (tmp_path / "o_tf_inmi.mcp2.exp").read_text().splitlines()
+    assert [l.split("\t")[0] for l in header[1:]] == [f"g{i}" for i in tf_rows]
+    for k in (2, 3, 4):
+        M, R = port.mcp_tf(A, tfs, k, k - 1)
+        assert np.array_equal(out(f"mcp{k}"), R), k
+        line = [l for l in r.stdout.splitlines() if l.startswith(f"Computed,auprroc,mcp{k},")][0].split(",")
+        a, b, _, _ = port.eval_truth(R, Lt, region, rg, ct)
+        assert abs(float(line[3]) - a) <= 1e-11 and abs(float(line[4]) - b) <= 1e-11
+    T, M1, M2, M3 = port.maxmins_tf(A, tfs)
+    pr, roc, best = port.combo_eval(T, M1, M2, M3, Lt, cs, region, rg, ct)
+    got = [float(l.split()[2].split(",")[0]) for l in r.stdout.splitlines() if l.startswith("Computed,Combo AUPR")]
+    assert np.allclose(got, pr, rtol=0, atol=1e-11)
+    tag = "_".join(f"{c:.3f}" for c in cs[best])
+    assert np.array_equal(out(f"mcp_{tag}"), port.combo(T, M1, M2, M3, cs[best]))
+    spr, sroc, sbest = port.combo_stouffer_tf_eval(T, M1, M2, M3, Lt, cs, region, rg, ct)
+    got = [float(l.split()[3].split(",")[0]) for l in r.stdout.splitlines()
+           if l.startswith("Computed,Combo Stouffer AUPR")]
+    assert np.allclose(got, spr, rtol=0, atol=1e-6)  # statistics to an ulp: AUPR close, not equal
+    stag = [l for l in r.stdout.splitlines() if l.startswith("Computed,MAX Combo AND Stouffer")][0]
+    stag = stag.split("(")[1].split(")")[0]
+    st = out(f"mcpst_{stag}")
+    want = port.stouffer_tf(port.combo(T, M1, M2, M3, np.array([float(v) for v in stag.split("_")])))
+    np.testing.assert_allclose(st, want, rtol=1e-5, atol=1e-5)
+
+
+def test_cli_tf_input_without_tfs(built_lib, tmp_path):
+    """A TF file naming no gene stops mcpnet with the reference's message."""
+    A = np.eye(4, dtype=np.float32)
+    write_exp(tmp_path / "mi.exp", A)
+    (tmp_path / "tfs.txt").write_text("nothing\n")
+    r = run("mcpnet", "-i", tmp_path / "mi.exp", "-o", tmp_path / "o", "--mi-input", "--tf-input",
+            tmp_path / "tfs.txt")
+    assert r.returncode != 0 and "no transcription factors" in r.stderr

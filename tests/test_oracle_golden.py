@@ -250,3 +250,53 @@ def test_stouffer_clr_bit_exact(port, golden):
         for clr, key in ((False, "stouffer"), (True, "clr")):
             got = port.transform_with_stats(A, mean, sd, clr)
             assert np.array_equal(got.view(np.uint32), g[f"{mode}_{key}"].view(np.uint32)), (mode, key)
+
+
+def test_maxmins_tf_oracle(port, golden):
+    """compute_maxmins_tfs restated on the oracle's masked max-min equals the
+    composition of MCPNet's own mcp2_maxmin_kernel<float,true,true> bit for bit."""
+    g = golden("tf_ensemble")
+    got = port.maxmins_tf(g["A"], g["tfs"])
+    for name, m in zip(("T", "M1", "M2", "M3"), got):
+        assert np.array_equal(m.view(np.uint32), g[name].view(np.uint32)), name
+
+
+def test_stouffer_tf_bit_exact(port, golden):
+    """The restated TF Stouffer combine equals MCPNet's zscored_stouffer_kernel
+    given the same z-scores; a constant row and a constant column give z = 0
+    (the population statistics stand in for the absent splash StandardScore
+    and are not pinned)."""
+    g = golden("tf_ensemble")
+    S = g["st_in"]
+    stats = port.tf_stats(S)
+    for got, key in zip(stats, ("st_rmean", "st_rsd", "st_cmean", "st_csd")):
+        assert np.array_equal(got, g[key]), key
+    assert stats[1][3] == 0.0 and stats[3][7] == 0.0
+    out = port.stouffer_tf_with_stats(S, *stats)
+    assert np.array_equal(out.view(np.uint32), g["st_out"].view(np.uint32))
+
+
+def test_stouffer_tf_population_statistics(port):
+    """Row and column statistics are the FP64 population mean / sd."""
+    rng = np.random.default_rng(3)
+    S = rng.random((7, 11)).astype(np.float32)
+    rm, rs, cm, cs = port.tf_stats(S)
+    S64 = S.astype(np.float64)
+    np.testing.assert_array_equal(rm, S64.mean(1).astype(np.float32))
+    np.testing.assert_allclose(rs, S64.std(1), rtol=1e-6)
+    np.testing.assert_array_equal(cm, S64.mean(0).astype(np.float32))
+    np.testing.assert_allclose(cs, S64.std(0), rtol=1e-6)
+
+
+def test_tf_searches_oracle(port, golden):
+    """The TF combo and TF-Stouffer coefficient searches over the TF truth rows."""
+    g = golden("tf_ensemble")
+    args = (g["T"], g["M1"], g["M2"], g["M3"], g["labels_tf"], g["coeffs"], "tf", g["row_gene"], g["col_tf"])
+    pr, roc, best = port.combo_eval(*args)
+    np.testing.assert_array_equal(pr, g["combo_aupr"])
+    np.testing.assert_array_equal(roc, g["combo_auroc"])
+    assert best == int(g["combo_best"])
+    pr, roc, best = port.combo_stouffer_tf_eval(*args)
+    np.testing.assert_array_equal(pr, g["st_aupr"])
+    np.testing.assert_array_equal(roc, g["st_auroc"])
+    assert best == int(g["st_best"])
