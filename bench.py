@@ -480,6 +480,33 @@ def pipeline_arm(args, ws, rank, local):
             lambda: r.__setitem__(0, h.combo_stouffer_eval_dev(A, M1, M2, M3, Lb, coeffs)))
         ev["combo_stouffer"] = r[0]
         ev["coeffs"] = coeffs
+    tfst = {}
+    if args.tfs > 0:
+        # --tf-input: a seeded set of TF genes (the synthetic GRN has no TF annotation)
+        t = min(args.tfs, n)
+        tf_idx = np.sort(np.random.default_rng(args.seed + 7).choice(n, size=t, replace=False)).astype(np.int32)
+        tfs = np.full(n, -np.inf, np.float32)
+        tfs[tf_idx] = np.inf
+        Rt = [torch.empty((t, n), **f32) for _ in range(3)]
+        Tm, M1t, M2t, M3t = (torch.empty((t, n), **f32) for _ in range(4))
+        tf_stages = {
+            "mcp_tf": lambda: [h.mcp_tf_dev(A, tfs, k, k - 1, R=Rt[k - 2]) for k in (2, 3, 4)],
+            "maxmins_tf": lambda: h.maxmins_tf_dev(A, tfs, Tm, M1t, M2t, M3t),
+            "dpi_tf": lambda: tfst.__setitem__("removed", h.dpi_tf_dev(A, D, tfs, 0.1)),
+        }
+        if not args.no_eval:
+            rows_d = torch.from_numpy(tf_idx).to(dev)
+            Lt = Lb[rows_d.long()].contiguous()
+            ct = torch.from_numpy((tfs > 0).astype(np.uint8)).to(dev)
+            tf_stages["tf_eval_mcp2"] = lambda: tfst.__setitem__("mcp2", h.eval_truth_dev(Rt[0], Lt, "tf", rows_d, ct))
+            tf_stages["tf_combo_search"] = lambda: tfst.__setitem__(
+                "combo", h.combo_eval_dev(Tm, M1t, M2t, M3t, Lt, coeffs, "tf", rows_d, ct))
+            tf_stages["tf_combo_stouffer_search"] = lambda: tfst.__setitem__(
+                "combo_stouffer", h.combo_stouffer_tf_eval_dev(Tm, M1t, M2t, M3t, Lt, coeffs, "tf", rows_d, ct))
+        for key, fn in tf_stages.items():
+            fn()  # untimed: grows this stage's workspace
+            st[key] = timed(fn)
+        tfst["t"] = t
     iters = None
     if args.closure:
         Cl = torch.empty((n, n), **f32)
@@ -538,6 +565,26 @@ def pipeline_arm(args, ws, rank, local):
                            "ms_per_row": st[key] * 1e3 / (len(ev["coeffs"]) - 1),
                            "best_row": int(best), "best_coeffs": ev["coeffs"][best].tolist(),
                            "best_aupr": float(pr[best]), "best_auroc": float(roc[best])}
+    if args.tfs > 0:
+        t = tfst["t"]
+        # executed triples: MCP2 T(x)A; MCP3 A(x)A (symmetric) + T(x)M1; MCP4 A(x)A + T(x)A + M2(x)M1
+        # (every masked product runs over the t TF columns)
+        tri = {"mcp_tf": n * n * t + 4.0 * t * t * n, "maxmins_tf": 0.5 * n * n * t + 3.0 * t * t * n,
+               "dpi_tf": 0.5 * n ** 3 + 0.5 * n * n * t}
+        for key in ("mcp_tf", "maxmins_tf", "dpi_tf"):
+            ms_ = st[key] * 1e3
+            stages[key] = {"ms": ms_, "tfs": t, "Gop/s_executed": 2 * tri[key] / (ms_ / 1e3) / 1e9,
+                           "frac_alu_peak": 2 * tri[key] / (ms_ / 1e3) / alu_peak}
+        stages["dpi_tf"]["removed"] = tfst["removed"]
+        if not args.no_eval:
+            stages["tf_eval_mcp2"] = {"ms": st["tf_eval_mcp2"] * 1e3, "aupr": tfst["mcp2"][0],
+                                      "auroc": tfst["mcp2"][1], "n_pos": tfst["mcp2"][2], "n_neg": tfst["mcp2"][3]}
+            for key, k in (("tf_combo_search", "combo"), ("tf_combo_stouffer_search", "combo_stouffer")):
+                pr, roc, best = tfst[k]
+                stages[key] = {"ms": st[key] * 1e3, "rows": len(coeffs),
+                               "ms_per_row": st[key] * 1e3 / (len(coeffs) - 1), "best_row": int(best),
+                               "best_coeffs": coeffs[best].tolist(), "best_aupr": float(pr[best]),
+                               "best_auroc": float(roc[best])}
     line = {"mode": "pipeline", "genes": n, "samples": m, "mi_method": args.mi_method, "precision": args.precision,
             "stage_s": st, "wall_s": wall, "stages": stages, "closure_iterations": iters, "clocks": clk,
             "kernel_profile": prof, "sms": sms}
@@ -602,6 +649,9 @@ def main(argv=None):
     ap.add_argument("--pipeline", action="store_true",
                     help="run the whole compute core once, stage by stage (defaults to 32768 x 4096)")
     ap.add_argument("--closure", action="store_true", help="with --pipeline: add the max-capacity closure")
+    ap.add_argument("--tfs", type=int, default=0,
+                    help="with --pipeline: add the --tf-input stages (TF MCP2/3/4, TF max-min products, TF DPI, "
+                         "TF evaluation and searches) for this many seeded TF genes")
     ap.add_argument("--no-eval", action="store_true",
                     help="with --pipeline: skip the gold-standard evaluation and the ensemble coefficient search")
     ap.add_argument("--cpu-genes", type=int, default=8192,

@@ -518,6 +518,23 @@ class Handle:
             args += [self._dp(t), self._ld(t) if t is not None else n]
         self._check(self._L.mcpg_maxmins_dev(self._h, self._dp(A), n, self._ld(A), *args), "maxmins_dev")
 
+    def mcp_tf_dev(self, A, tfs, path_len: int, transition: int, M=None, R=None):
+        """compute_mcp{2,3,4}_tfs into t x n CUDA tensors (each optional); tfs is a host array."""
+        tfs = _f32(tfs)
+        n = A.shape[0]
+        self._check(self._L.mcpg_mcp_tf_dev(self._h, self._dp(A), n, self._ld(A), _ptr(tfs), path_len, transition,
+                                             self._dp(M), self._ld(M) if M is not None else n, self._dp(R),
+                                             self._ld(R) if R is not None else n), "mcp_tf_dev")
+
+    def dpi_tf_dev(self, A, out, tfs, tol: float = 0.1, mask=None):
+        """dpi_tf_kernel + mask on CUDA tensors; returns the removed count."""
+        tfs = _f32(tfs)
+        n = A.shape[0]
+        removed = C.c_int64(0)
+        self._check(self._L.mcpg_dpi_tf_dev(self._h, self._dp(A), n, self._ld(A), tol, _ptr(tfs), self._dp(out),
+                                             self._ld(out), self._dp(mask), C.byref(removed)), "dpi_tf_dev")
+        return removed.value
+
     def combo_dev(self, mi, M1, M2, M3, coeffs, out):
         """compute_combo: out = mi / (c0 mi + c1 M1 + c2 M2 + c3 M3) (torch CUDA tensors; Mk may be None when ck == 0)."""
         cs = np.ascontiguousarray(coeffs, dtype=np.float64)
