@@ -378,9 +378,27 @@ def gpu_arm(args, ws, rank, local):
             host_call()
             ts.append(time.perf_counter() - t0)
         e_s = reduce_max(float(np.mean(ts)), ws)
+        access = int(L.mcpg_last_host_access(h._h))
         line["e2e"] = {"value": ws * pairs / e_s, "unit": UNIT, "h2d_bytes_per_step": n * m * 4,
                        "d2h_bytes_per_step": n * n * 4, "ms_per_step": e_s * 1e3,
-                       "api": "mcpg_bspline_mi (host buffers, pinned)"}
+                       "api": "mcpg_bspline_mi (host buffers, pinned)",
+                       "transfer": ("in place over NVLink-C2C: the kernels read X from and write MI to the host "
+                                    "buffers" if access == 3 else "staged copies (slab-overlapped device-to-host)"),
+                       "host_access_bits": access}
+        # the same call on pageable buffers (what MCPNet's aligned_matrix holds), output pages touched
+        xg, mg = np.array(X_host, dtype=np.float32), np.zeros((n, n), np.float32)
+        pg = lambda: L.mcpg_bspline_mi(h._h, xg.ctypes.data, n, m, m, args.bins, args.order, pr, mg.ctypes.data, n,
+                                       None)
+        assert pg() == 0
+        tp = []
+        for _ in range(args.e2e_steps):
+            t0 = time.perf_counter()
+            assert pg() == 0
+            tp.append(time.perf_counter() - t0)
+        p_s = reduce_max(float(np.mean(tp)), ws)
+        line["e2e_pageable"] = {"value": ws * pairs / p_s, "unit": UNIT, "ms_per_step": p_s * 1e3,
+                                "host_access_bits": int(L.mcpg_last_host_access(h._h))}
+        del xg, mg
 
     # ---- CPU baseline (rank 0, N = 1 only) ----
     if rank == 0 and ws == 1 and not args.no_cpu:

@@ -466,6 +466,24 @@ MCPG_API int mcpg_combo_eval(mcpg_handle* h, const float* mi, int64_t ldm, const
 MCPG_API int mcpg_bspline_mi_fp32_noalloc(const float* X, int64_t n, int64_t m, int64_t ldx, int bins, int order,
                                           float* MI, int64_t ldmi, double* H, void* cuda_stream);
 
+/* ---- host buffers addressed in place (no counterpart in the reference) ----
+ * On a device that accesses pageable host memory coherently through the host's
+ * page tables (GB300 / Grace over NVLink-C2C), mcpg_bspline_mi and mcpg_ap_mi
+ * let their kernels read X from and write MI to the caller's host buffers
+ * directly -- no staging copies -- when every page of the buffer is mapped and
+ * resident; an output buffer whose pages are not populated yet is populated by
+ * the host first (its contents, padding included, are left as they are).
+ * Other buffers, and other devices, take the staged path (copies through device
+ * scratch).  Results are identical either way.  MCPG_HOST_ACCESS_STAGED forces
+ * the staged path on this handle; mcpg_last_host_access returns which buffers
+ * the last such call used in place (MCPG_HOST_DIRECT_* bits). */
+#define MCPG_HOST_ACCESS_AUTO 0
+#define MCPG_HOST_ACCESS_STAGED 1
+#define MCPG_HOST_DIRECT_INPUT 1
+#define MCPG_HOST_DIRECT_OUTPUT 2
+MCPG_API int mcpg_set_host_access(mcpg_handle* h, int mode);
+MCPG_API int mcpg_last_host_access(const mcpg_handle* h);
+
 /* ---- testing hook: make the next `count` device scratch allocations of this
  * handle fail with MCPG_ERR_OOM (exercises the error path without a GPU fault). */
 MCPG_API int mcpg_test_fail_allocs(mcpg_handle* h, int count);

@@ -126,6 +126,11 @@ ABI += [
     ("mcpg_combo_stouffer_tf_eval_dev", C.c_int, [_vp, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _i64, _i64, _vp,
                                                   _i64, C.c_int, _vp, _vp, _vp, _i64, _vp, _vp, _vp]),
 ]
+ABI += [
+    ("mcpg_set_host_access", C.c_int, [_vp, C.c_int]),
+    ("mcpg_last_host_access", C.c_int, [_vp]),
+]
+HOST_ACCESS = {"auto": 0, "staged": 1}
 TRANSFORMS = {"stouffer": 0, "clr": 1}
 ROW_STATS = {"all": 0, "exclude_diagonal": 1}
 TRUTH_REGIONS = {"lower": 0, "all": 1, "tf": 2}
@@ -631,6 +636,15 @@ class Handle:
         n = A.shape[0]
         self._check(self._L.mcpg_transform_dev(self._h, self._dp(A), n, self._ld(A), TRANSFORMS[kind],
                                                 ROW_STATS[stats], self._dp(out), self._ld(out)), "transform_dev")
+
+    def set_host_access(self, mode="auto"):
+        """'auto': host entry points address pageable / pinned host buffers in place where the device can;
+        'staged': always copy through device scratch."""
+        self._check(self._L.mcpg_set_host_access(self._h, HOST_ACCESS[mode]), "set_host_access")
+
+    def last_host_access(self) -> int:
+        """MCPG_HOST_DIRECT_* bits (1 input, 2 output) of the last host MI call."""
+        return int(self._L.mcpg_last_host_access(self._h))
 
     def stouffer_tf(self, A):
         """compute_stouffer_tf of a t x n host matrix."""

@@ -14,6 +14,9 @@
 #include <string>
 #include <vector>
 
+#include <sys/mman.h>
+#include <unistd.h>
+
 #include "../../include/mcpgpu.h"
 #include "internal.h"
 
@@ -84,6 +87,11 @@ struct mcpg_handle {
     // host MI: a second stream copies finished row slabs back while later slabs compute
     cudaStream_t copy_stream = nullptr;
     std::vector<cudaEvent_t> slab_events;
+    // host entry points: kernels address the caller's buffers in place when the
+    // device reads host memory through the host page tables (-1: not queried)
+    int ats = -1;
+    int host_access = MCPG_HOST_ACCESS_AUTO;
+    int last_direct = 0;  // MCPG_HOST_DIRECT_* of the last host call that can use them
     // optional per-kernel timing (mcpg_profile): CUDA events around each launch
     bool prof = false;
     struct Span { const char* name; cudaEvent_t a, b; };
@@ -565,6 +573,67 @@ TfSet tf_set(const float* v, int64_t n) {
         if (!(v[i] == INFINITY || v[i] == -INFINITY)) t.pm_inf = false;
     }
     return t;
+}
+
+// ---------------- host buffers addressed in place ----------------
+// On a device that reads and writes pageable memory coherently through the
+// host's page tables (Grace + Blackwell over NVLink-C2C: ATS), a kernel can use
+// the caller's host buffer itself -- no staging copy, no host-to-device or
+// device-to-host transfer.  host_direct says whether [p, p + bytes) qualifies:
+// every page must be mapped (mincore), and resident, because a first touch by
+// the GPU is a slow IOMMU fault; an output whose pages are not yet populated is
+// populated writable by the host first (MADV_POPULATE_WRITE leaves the contents
+// as they are), in parallel.  Anything else is staged as before.
+#ifndef MADV_POPULATE_WRITE
+#define MADV_POPULATE_WRITE 23
+#endif
+
+bool ats_device(mcpg_handle* h) {
+    if (h->ats < 0) {
+        int a = 0, b = 0;
+        h->ats = (cudaDeviceGetAttribute(&a, cudaDevAttrPageableMemoryAccess, h->device) == cudaSuccess &&
+                  cudaDeviceGetAttribute(&b, cudaDevAttrPageableMemoryAccessUsesHostPageTables, h->device) ==
+                      cudaSuccess &&
+                  a == 1 && b == 1)
+                     ? 1
+                     : 0;
+        cudaGetLastError();
+    }
+    return h->ats == 1;
+}
+
+bool host_direct(mcpg_handle* h, const void* p, size_t bytes, bool for_write) {
+    if (h->host_access != MCPG_HOST_ACCESS_AUTO || !p || bytes == 0 || !ats_device(h)) return false;
+    const long ps = sysconf(_SC_PAGESIZE);
+    if (ps <= 0) return false;
+    const uintptr_t page = (uintptr_t)ps;
+    const uintptr_t b = (uintptr_t)p & ~(page - 1);
+    const uintptr_t e = ((uintptr_t)p + bytes + page - 1) & ~(page - 1);
+    std::vector<unsigned char> vec((size_t)((e - b) / page));
+    if (mincore((void*)b, (size_t)(e - b), vec.data()) != 0) return false;  // a page is not mapped
+    bool resident = true;
+    for (unsigned char v : vec)
+        if (!(v & 1)) {
+            resident = false;
+            break;
+        }
+    if (resident) return true;
+    if (!for_write) return false;
+    const size_t chunk = (size_t)16 << 20;  // 16 MiB per task, page-aligned
+    const int64_t nchunks = (int64_t)(((e - b) + chunk - 1) / chunk);
+    int bad = 0;
+#pragma omp parallel for schedule(dynamic) reduction(| : bad)
+    for (int64_t c = 0; c < nchunks; ++c) {
+        const uintptr_t c0 = b + (uintptr_t)c * chunk;
+        const uintptr_t c1 = c0 + chunk < e ? c0 + chunk : e;
+        if (madvise((void*)c0, (size_t)(c1 - c0), MADV_POPULATE_WRITE) != 0) bad |= 1;
+    }
+    return bad == 0;
+}
+
+// Bytes spanned by a rows x cols float matrix with leading dimension ld.
+size_t span_bytes(int64_t rows, int64_t cols, int64_t ld) {
+    return rows > 0 && cols > 0 ? (size_t)((rows - 1) * ld + cols) * sizeof(float) : 0;
 }
 
 int upload(mcpg_handle* h, int slot, const void* src, size_t bytes, void** dev) {
@@ -1704,6 +1773,17 @@ int mcpg_test_fail_allocs(mcpg_handle* h, int count) {
     return MCPG_OK;
 }
 
+int mcpg_set_host_access(mcpg_handle* h, int mode) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (mode != MCPG_HOST_ACCESS_AUTO && mode != MCPG_HOST_ACCESS_STAGED)
+        return fail(h, MCPG_ERR_ARG, "set_host_access: unknown mode %d", mode);
+    h->host_access = mode;
+    return MCPG_OK;
+}
+
+int mcpg_last_host_access(const mcpg_handle* h) { return h ? h->last_direct : 0; }
+
 // ---- MI ----
 int mcpg_bspline_mi_dev(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_t ldx, int bins, int order,
                         int precision, float* MI, int64_t ldmi, double* H) {
@@ -1720,8 +1800,21 @@ int mcpg_bspline_mi(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_
     if (n < 1 || m < 1 || ldx < m || ldmi < n) return fail(h, MCPG_ERR_ARG, "bspline_mi: bad shape");
     float *dX, *dMI;
     int64_t lx, lmi;
-    if ((rc = stage_in(h, S_IN0, X, ldx, n, m, &dX, &lx))) return rc;
-    if ((rc = stage_out_alloc(h, S_OUT0, n, n, &dMI, &lmi))) return rc;
+    const bool x_direct = host_direct(h, X, span_bytes(n, m, ldx), false);
+    const bool mi_direct = host_direct(h, MI, span_bytes(n, n, ldmi), true);
+    h->last_direct = (x_direct ? MCPG_HOST_DIRECT_INPUT : 0) | (mi_direct ? MCPG_HOST_DIRECT_OUTPUT : 0);
+    if (x_direct) {
+        dX = const_cast<float*>(X);
+        lx = ldx;
+    } else if ((rc = stage_in(h, S_IN0, X, ldx, n, m, &dX, &lx))) {
+        return rc;
+    }
+    if (mi_direct) {
+        dMI = MI;
+        lmi = ldmi;
+    } else if ((rc = stage_out_alloc(h, S_OUT0, n, n, &dMI, &lmi))) {
+        return rc;
+    }
     double* dH = nullptr;
     if (H) {
         void* p;
@@ -1730,6 +1823,12 @@ int mcpg_bspline_mi(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_
     }
     MiPlan pl;
     if ((rc = mi_prepare(h, dX, n, m, lx, bins, order, precision, dMI, lmi, dH, pl))) return rc;
+    if (mi_direct) {  // the kernels write the caller's buffer: one launch, nothing to copy back
+        if ((rc = mi_launch(h, pl, 0, n))) return rc;
+        if ((rc = mi_finish(h, pl))) return rc;
+        if (H) CK(h, cudaMemcpyAsync(H, dH, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "copy H");
+        return finish(h);
+    }
     // Row slabs of 48-gene multiples: once slab k has run, rows < its end are
     // final (row i's j >= i entries come from its own slab, the j < i ones are
     // mirrors written by earlier slabs), so their copy to the host overlaps
@@ -2348,12 +2447,25 @@ int mcpg_ap_mi(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_t ldx
     if ((rc = ap_check(h, n, m, X, ldx, MI, ldmi)) || n == 0) return rc;
     float* dx;
     int64_t lx;
-    if ((rc = stage_in(h, S_IN0, X, ldx, n, m, &dx, &lx))) return rc;
+    const bool x_direct = host_direct(h, X, span_bytes(n, m, ldx), false);
+    const bool mi_direct = host_direct(h, MI, span_bytes(n, n, ldmi), true);
+    h->last_direct = (x_direct ? MCPG_HOST_DIRECT_INPUT : 0) | (mi_direct ? MCPG_HOST_DIRECT_OUTPUT : 0);
+    if (x_direct) {
+        dx = const_cast<float*>(X);
+        lx = ldx;
+    } else if ((rc = stage_in(h, S_IN0, X, ldx, n, m, &dx, &lx))) {
+        return rc;
+    }
     float* dmi;
     int64_t ldd;
-    if ((rc = stage_out_alloc(h, S_OUT0, n, n, &dmi, &ldd))) return rc;
+    if (mi_direct) {
+        dmi = MI;
+        ldd = ldmi;
+    } else if ((rc = stage_out_alloc(h, S_OUT0, n, n, &dmi, &ldd))) {
+        return rc;
+    }
     if ((rc = ap_mi_dev(h, dx, n, m, lx, noise, seed, dmi, ldd))) return rc;
-    if ((rc = copy_out(h, MI, ldmi, dmi, ldd, n, n))) return rc;
+    if (!mi_direct && (rc = copy_out(h, MI, ldmi, dmi, ldd, n, n))) return rc;
     return finish(h);
 }
 
