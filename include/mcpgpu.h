@@ -468,15 +468,18 @@ MCPG_API int mcpg_bspline_mi_fp32_noalloc(const float* X, int64_t n, int64_t m, 
 
 /* ---- host buffers addressed in place (no counterpart in the reference) ----
  * On a device that accesses pageable host memory coherently through the host's
- * page tables (GB300 / Grace over NVLink-C2C), mcpg_bspline_mi and mcpg_ap_mi
- * let their kernels read X from and write MI to the caller's host buffers
- * directly -- no staging copies -- when every page of the buffer is mapped and
- * resident; an output buffer whose pages are not populated yet is populated by
+ * page tables (GB300 / Grace over NVLink-C2C), the host entry points let their
+ * kernels use the caller's host buffers directly -- no staging copies -- when
+ * every page of the buffer is mapped and resident: every output that is written
+ * once (MI, max-min products other than an M1 that later products read again,
+ * ratios, DPI outputs and masks, the closure, combos, transforms) and every
+ * input that is read once (X of the MI entry points, the combo and ratio
+ * operands).  An output buffer whose pages are not populated yet is populated by
  * the host first (its contents, padding included, are left as they are).
  * Other buffers, and other devices, take the staged path (copies through device
  * scratch).  Results are identical either way.  MCPG_HOST_ACCESS_STAGED forces
- * the staged path on this handle; mcpg_last_host_access returns which buffers
- * the last such call used in place (MCPG_HOST_DIRECT_* bits). */
+ * the staged path on this handle; mcpg_last_host_access returns which kinds of
+ * buffer the last call used in place (MCPG_HOST_DIRECT_* bits). */
 #define MCPG_HOST_ACCESS_AUTO 0
 #define MCPG_HOST_ACCESS_STAGED 1
 #define MCPG_HOST_DIRECT_INPUT 1

@@ -190,12 +190,16 @@ struct ProfScope {
 
 int check_handle(mcpg_handle* h) {
     if (!h) return MCPG_ERR_ARG;
+    h->last_direct = 0;  // the host buffers this call addresses in place, if any
     cudaError_t e = cudaSetDevice(h->device);
     if (e != cudaSuccess) return cuda_fail(h, e, "cudaSetDevice");
     return MCPG_OK;
 }
 
 // ---------------- staging helpers for the host entry points ----------------
+bool host_direct(mcpg_handle* h, const void* p, size_t bytes, bool for_write);
+size_t span_bytes(int64_t rows, int64_t cols, int64_t ld);
+
 int stage_in(mcpg_handle* h, int slot, const float* src, int64_t ld_src, int64_t rows, int64_t cols, float** dev,
              int64_t* ld_dev) {
     const int64_t ld = round_up(cols > 0 ? cols : 1, 4);  // 16-byte rows for the vectorised kernels
@@ -226,9 +230,36 @@ int stage_out_alloc(mcpg_handle* h, int slot, int64_t rows, int64_t cols, float*
     return MCPG_OK;
 }
 
+// A host input matrix that the kernels read exactly once: the caller's buffer
+// itself when host_direct allows, else a staged device copy.
+int in_view(mcpg_handle* h, int slot, const float* host, int64_t ld_host, int64_t rows, int64_t cols, float** dev,
+            int64_t* ld_dev) {
+    if (host && rows > 0 && cols > 0 && host_direct(h, host, span_bytes(rows, cols, ld_host), false)) {
+        *dev = const_cast<float*>(host);
+        *ld_dev = ld_host;
+        h->last_direct |= MCPG_HOST_DIRECT_INPUT;
+        return MCPG_OK;
+    }
+    return stage_in(h, slot, host, ld_host, rows, cols, dev, ld_dev);
+}
+
+// A host output matrix: the caller's buffer itself when the kernels can write it
+// in place (host_direct; the result is written once), else device scratch that
+// copy_out brings back.
+int out_view(mcpg_handle* h, int slot, float* host, int64_t ld_host, int64_t rows, int64_t cols, float** dev,
+             int64_t* ld_dev) {
+    if (host && rows > 0 && cols > 0 && host_direct(h, host, span_bytes(rows, cols, ld_host), true)) {
+        *dev = host;
+        *ld_dev = ld_host;
+        h->last_direct |= MCPG_HOST_DIRECT_OUTPUT;
+        return MCPG_OK;
+    }
+    return stage_out_alloc(h, slot, rows, cols, dev, ld_dev);
+}
+
 int copy_out(mcpg_handle* h, float* dst, int64_t ld_dst, const float* src, int64_t ld_src, int64_t rows,
              int64_t cols) {
-    if (!dst || rows <= 0 || cols <= 0) return MCPG_OK;
+    if (!dst || rows <= 0 || cols <= 0 || dst == src) return MCPG_OK;  // dst == src: written in place
     if (ld_dst == cols && ld_src == cols)
         CK(h, cudaMemcpyAsync(dst, src, (size_t)(rows * cols) * sizeof(float), cudaMemcpyDeviceToHost, h->stream),
            "device-to-host copy");
@@ -1920,7 +1951,7 @@ int mcpg_maxmin(mcpg_handle* h, const float* A, int64_t lda, const float* B, int
     } else if ((rc = stage_in(h, S_IN1, B, ldb, cols, k, &dB, &lb))) {
         return rc;
     }
-    if ((rc = stage_out_alloc(h, S_OUT0, rows, cols, &dC, &lc))) return rc;
+    if ((rc = out_view(h, S_OUT0, C, ldc, rows, cols, &dC, &lc))) return rc;
     if ((rc = maxmin_dev(h, dA, la, dB, lb, rows, cols, k, dC, lc))) return rc;
     if ((rc = copy_out(h, C, ldc, dC, lc, rows, cols))) return rc;
     return finish(h);
@@ -1952,10 +1983,13 @@ int mcpg_ratio(mcpg_handle* h, const float* A, int64_t lda, const float* M, int6
     if (lda < cols || ldm < cols || ldr < cols) return fail(h, MCPG_ERR_ARG, "ratio: leading dimension too small");
     float *dA, *dM, *dR;
     int64_t la, lm, lr;
-    if ((rc = stage_in(h, S_IN0, A, lda, rows, cols, &dA, &la))) return rc;
-    if ((rc = stage_in(h, S_IN1, M, ldm, rows, cols, &dM, &lm))) return rc;
-    if ((rc = stage_out_alloc(h, S_OUT0, rows, cols, &dR, &lr))) return rc;
-    if ((rc = mcpg_ratio_dev(h, dA, la, dM, lm, rows, cols, dR, lr))) return rc;
+    if ((rc = in_view(h, S_IN0, A, lda, rows, cols, &dA, &la))) return rc;   // each read once
+    if ((rc = in_view(h, S_IN1, M, ldm, rows, cols, &dM, &lm))) return rc;
+    if ((rc = out_view(h, S_OUT0, R, ldr, rows, cols, &dR, &lr))) return rc;
+    {
+        PROF(h, "ratio");
+        CK(h, mcpg::launch_ratio(dA, la, dM, lm, rows, cols, dR, lr, h->stream, &h->launches), "ratio kernel");
+    }
     if ((rc = copy_out(h, R, ldr, dR, lr, rows, cols))) return rc;
     return finish(h);
 }
@@ -1990,8 +2024,8 @@ int mcpg_mcp(mcpg_handle* h, const float* A, int64_t n, int64_t lda, int path_le
     float *dA, *dM = nullptr, *dR = nullptr;
     int64_t la, lm = 0, lr = 0;
     if ((rc = stage_in(h, S_IN0, A, lda, n, n, &dA, &la))) return rc;
-    if (Mout && (rc = stage_out_alloc(h, S_OUT0, n, n, &dM, &lm))) return rc;
-    if (Rout && (rc = stage_out_alloc(h, S_OUT1, n, n, &dR, &lr))) return rc;
+    if (Mout && (rc = out_view(h, S_OUT0, Mout, ldm, n, n, &dM, &lm))) return rc;
+    if (Rout && (rc = out_view(h, S_OUT1, Rout, ldr, n, n, &dR, &lr))) return rc;
     if ((rc = mcp_dev(h, dA, n, la, path_len, symmetrize, dM, lm, dR, lr))) return rc;
     if ((rc = copy_out(h, Mout, ldm, dM, lm, n, n))) return rc;
     if ((rc = copy_out(h, Rout, ldr, dR, lr, n, n))) return rc;
@@ -2018,16 +2052,20 @@ int mcpg_dpi(mcpg_handle* h, const float* A, int64_t n, int64_t lda, float tol, 
     float *dA, *dO;
     int64_t la, lo;
     if ((rc = stage_in(h, S_IN0, A, lda, n, n, &dA, &la))) return rc;
-    if ((rc = stage_out_alloc(h, S_OUT0, n, n, &dO, &lo))) return rc;
+    if ((rc = out_view(h, S_OUT0, out, ldo, n, n, &dO, &lo))) return rc;
     uint8_t* dMask = nullptr;
-    if (mask) {
+    const bool mask_direct = mask && host_direct(h, mask, (size_t)(n * n), true);
+    if (mask_direct) {
+        dMask = mask;
+    } else if (mask) {
         void* p;
         if ((rc = scratch(h, S_MASK, (size_t)(n * n), &p))) return rc;
         dMask = (uint8_t*)p;
     }
     if ((rc = dpi_dev(h, dA, n, la, tol, dO, lo, dMask, removed))) return rc;
     if ((rc = copy_out(h, out, ldo, dO, lo, n, n))) return rc;
-    if (mask) CK(h, cudaMemcpyAsync(mask, dMask, (size_t)(n * n), cudaMemcpyDeviceToHost, h->stream), "copy mask");
+    if (mask && !mask_direct)
+        CK(h, cudaMemcpyAsync(mask, dMask, (size_t)(n * n), cudaMemcpyDeviceToHost, h->stream), "copy mask");
     return finish(h);
 }
 
@@ -2051,7 +2089,7 @@ int mcpg_closure(mcpg_handle* h, const float* A, int64_t n, int64_t lda, int max
     float *dA, *dO;
     int64_t la, lo;
     if ((rc = stage_in(h, S_IN0, A, lda, n, n, &dA, &la))) return rc;
-    if ((rc = stage_out_alloc(h, S_OUT0, n, n, &dO, &lo))) return rc;
+    if ((rc = out_view(h, S_OUT0, out, ldo, n, n, &dO, &lo))) return rc;
     int crc = closure_dev(h, dA, n, la, max_iter, dO, lo, iterations);
     if (crc && crc != MCPG_ERR_NOT_CONVERGED) return crc;
     std::string keep = h->err;
@@ -2087,7 +2125,7 @@ int mcpg_maxmin_masked(mcpg_handle* h, const float* A, int64_t lda, const float*
     } else if ((rc = stage_in(h, S_IN1, B, ldb, cols, k, &dB, &lb))) {
         return rc;
     }
-    if ((rc = stage_out_alloc(h, S_OUT0, rows, cols, &dC, &lc))) return rc;
+    if ((rc = out_view(h, S_OUT0, C, ldc, rows, cols, &dC, &lc))) return rc;
     if ((rc = maxmin_masked_dev(h, dA, la, dB, lb, rows, cols, k, mask, dC, lc))) return rc;
     if ((rc = copy_out(h, C, ldc, dC, lc, rows, cols))) return rc;
     return finish(h);
@@ -2113,8 +2151,8 @@ int mcpg_mcp_tf(mcpg_handle* h, const float* A, int64_t n, int64_t lda, const fl
     float *dA, *dM = nullptr, *dR = nullptr;
     int64_t la, lm = 0, lr = 0;
     if ((rc = stage_in(h, S_IN0, A, lda, n, n, &dA, &la))) return rc;
-    if (Mout && t > 0 && (rc = stage_out_alloc(h, S_OUT0, t, n, &dM, &lm))) return rc;
-    if (Rout && t > 0 && (rc = stage_out_alloc(h, S_OUT1, t, n, &dR, &lr))) return rc;
+    if (Mout && t > 0 && (rc = out_view(h, S_OUT0, Mout, ldm, t, n, &dM, &lm))) return rc;
+    if (Rout && t > 0 && (rc = out_view(h, S_OUT1, Rout, ldr, t, n, &dR, &lr))) return rc;
     if ((rc = mcp_tf_dev(h, dA, n, la, tfs, path_len, tf_gene_transition, dM, lm, dR, lr))) return rc;
     if (t > 0) {
         if ((rc = copy_out(h, Mout, ldm, dM, lm, t, n))) return rc;
@@ -2142,16 +2180,20 @@ int mcpg_dpi_tf(mcpg_handle* h, const float* A, int64_t n, int64_t lda, float to
     float *dA, *dO;
     int64_t la, lo;
     if ((rc = stage_in(h, S_IN2, A, lda, n, n, &dA, &la))) return rc;
-    if ((rc = stage_out_alloc(h, S_OUT0, n, n, &dO, &lo))) return rc;
+    if ((rc = out_view(h, S_OUT0, out, ldo, n, n, &dO, &lo))) return rc;
     uint8_t* dMask = nullptr;
-    if (mask) {
+    const bool mask_direct = mask && host_direct(h, mask, (size_t)(n * n), true);
+    if (mask_direct) {
+        dMask = mask;
+    } else if (mask) {
         void* p;
         if ((rc = scratch(h, S_OUT1, (size_t)(n * n), &p))) return rc;
         dMask = (uint8_t*)p;
     }
     if ((rc = dpi_tf_dev(h, dA, n, la, tol, tfs, dO, lo, dMask, removed))) return rc;
     if ((rc = copy_out(h, out, ldo, dO, lo, n, n))) return rc;
-    if (mask) CK(h, cudaMemcpyAsync(mask, dMask, (size_t)(n * n), cudaMemcpyDeviceToHost, h->stream), "copy mask");
+    if (mask && !mask_direct)
+        CK(h, cudaMemcpyAsync(mask, dMask, (size_t)(n * n), cudaMemcpyDeviceToHost, h->stream), "copy mask");
     return finish(h);
 }
 
@@ -2489,7 +2531,10 @@ int mcpg_maxmins(mcpg_handle* h, const float* A, int64_t n, int64_t lda, float* 
     for (int k = 0; k < 6; ++k) {
         if (!host[k]) continue;
         if (hld[k] < n) return fail(h, MCPG_ERR_ARG, "maxmins: leading dimension too small");
-        if ((rc = stage_out_alloc(h, slots[k], n, n, &dev[k], &dld[k]))) return rc;
+        // M1 is an operand of the later products: it stays in device memory
+        rc = k == 0 ? stage_out_alloc(h, slots[k], n, n, &dev[k], &dld[k])
+                    : out_view(h, slots[k], host[k], hld[k], n, n, &dev[k], &dld[k]);
+        if (rc) return rc;
     }
     if ((rc = maxmins_dev(h, dA, n, la, dev[0], dld[0], dev[1], dld[1], dev[2], dld[2], dev[3], dld[3], dev[4], dld[4],
                           dev[5], dld[5])))
@@ -2516,11 +2561,11 @@ int mcpg_combo(mcpg_handle* h, const float* mi, int64_t ldm, const float* M1, in
     for (int k = 0; k < 4; ++k) {
         if (!src[k] || (k > 0 && coeffs[k] == 0.0)) continue;
         if (lds[k] < cols) return fail(h, MCPG_ERR_ARG, "combo: leading dimension too small");
-        if ((rc = stage_in(h, slots[k], src[k], lds[k], rows, cols, &d[k], &dl[k]))) return rc;
+        if ((rc = in_view(h, slots[k], src[k], lds[k], rows, cols, &d[k], &dl[k]))) return rc;
     }
     float* dout;
     int64_t ld;
-    if ((rc = stage_out_alloc(h, S_OUT0, rows, cols, &dout, &ld))) return rc;
+    if ((rc = out_view(h, S_OUT0, out, ldo, rows, cols, &dout, &ld))) return rc;
     {
         PROF(h, "combo");
         CK(h, mcpg::launch_combo(d[0], dl[0], d[1], dl[1], d[2], dl[2], d[3], dl[3], rows, cols, coeffs, dout, ld,
@@ -2580,7 +2625,7 @@ int mcpg_transform(mcpg_handle* h, const float* A, int64_t n, int64_t lda, int t
     float *da, *dout;
     int64_t la, lo;
     if ((rc = stage_in(h, S_IN0, A, lda, n, n, &da, &la))) return rc;
-    if ((rc = stage_out_alloc(h, S_OUT0, n, n, &dout, &lo))) return rc;
+    if ((rc = out_view(h, S_OUT0, out, ldo, n, n, &dout, &lo))) return rc;
     if ((rc = transform_dev(h, da, n, la, transform, stats_mode, dout, lo))) return rc;
     if ((rc = copy_out(h, out, ldo, dout, lo, n, n))) return rc;
     return finish(h);
@@ -2682,7 +2727,7 @@ int mcpg_stouffer_tf(mcpg_handle* h, const float* A, int64_t rows, int64_t cols,
     float *da, *dout;
     int64_t la, lo;
     if ((rc = stage_in(h, S_IN0, A, lda, rows, cols, &da, &la))) return rc;
-    if ((rc = stage_out_alloc(h, S_OUT0, rows, cols, &dout, &lo))) return rc;
+    if ((rc = out_view(h, S_OUT0, out, ldo, rows, cols, &dout, &lo))) return rc;
     if ((rc = stouffer_tf_dev(h, da, rows, cols, la, dout, lo))) return rc;
     if ((rc = copy_out(h, out, ldo, dout, lo, rows, cols))) return rc;
     return finish(h);
@@ -2713,8 +2758,12 @@ int mcpg_maxmins_tf(mcpg_handle* h, const float* A, int64_t n, int64_t lda, cons
     float* const host[4] = {T, M1, M2, M3};
     const int64_t hld[4] = {ldt, ld1, ld2, ld3};
     const int slots[4] = {S_OUT0, S_OUT1, S_IN3, S_IN4};
-    for (int k = 0; k < 4; ++k)
-        if (host[k] && (rc = stage_out_alloc(h, slots[k], t, n, &o[k], &lo[k]))) return rc;
+    for (int k = 0; k < 4; ++k) {  // M1 (k = 1) is an operand of M2 and M3: it stays in device memory
+        if (!host[k]) continue;
+        rc = k == 1 ? stage_out_alloc(h, slots[k], t, n, &o[k], &lo[k])
+                    : out_view(h, slots[k], host[k], hld[k], t, n, &o[k], &lo[k]);
+        if (rc) return rc;
+    }
     if ((rc = maxmins_tf_dev(h, da, n, la, tfs, o[0], lo[0], o[1], lo[1], o[2], lo[2], o[3], lo[3]))) return rc;
     for (int k = 0; k < 4; ++k)
         if (host[k] && (rc = copy_out(h, host[k], hld[k], o[k], lo[k], t, n))) return rc;

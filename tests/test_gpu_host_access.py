@@ -108,3 +108,67 @@ def test_ap_mi_in_place(gpu, built_lib):
 def test_host_access_mode_checked(gpu):
     import mcpnet_gb300 as M
     assert M.lib().mcpg_set_host_access(gpu._h, 7) == M.ERR_ARG
+
+
+def _both(gpu, fn):
+    """fn() with in-place host access and with staged copies; returns both results and the in-place bits."""
+    gpu.set_host_access("auto")
+    a = fn()
+    bits = gpu.last_host_access()
+    gpu.set_host_access("staged")
+    try:
+        b = fn()
+        assert gpu.last_host_access() == 0
+    finally:
+        gpu.set_host_access("auto")
+    return a, b, bits
+
+
+def _flat(x):
+    if isinstance(x, dict):
+        return _flat([x[k] for k in sorted(x)])
+    if isinstance(x, (tuple, list)):
+        out = []
+        for y in x:
+            out += _flat(y)
+        return out
+    return [x]
+
+
+def _same(a, b):
+    for x, y in zip(_flat(a), _flat(b)):
+        if isinstance(x, np.ndarray):
+            assert x.dtype == y.dtype and np.array_equal(x.view(np.uint8), y.view(np.uint8))
+        else:
+            assert x == y
+
+
+def test_host_entry_points_in_place(gpu, built_lib):
+    """Every host entry point that writes its outputs in place gives the staged
+    path's bits; outputs that are operands of later products (M1) stay staged."""
+    n = 300
+    X = built_lib.synth_grn(n, 200, seed=35)
+    A = gpu.bspline_mi(X)
+    np.fill_diagonal(A, 0)
+    B = np.ascontiguousarray(A[:, ::-1])
+    tfs = np.where(np.arange(n) % 7 == 0, np.inf, -np.inf).astype(np.float32)
+    cases = {
+        "maxmin": (lambda: gpu.maxmin(A, B), DIRECT_OUT),
+        "ratio": (lambda: gpu.ratio(A, B), DIRECT_IN | DIRECT_OUT),
+        "mcp3_sym": (lambda: gpu.mcp(A, 3, symmetrize=True), DIRECT_OUT),
+        "mcp4": (lambda: gpu.mcp(A, 4), DIRECT_OUT),
+        "dpi": (lambda: gpu.dpi(A, 0.1, want_mask=True), DIRECT_OUT),
+        "closure": (lambda: gpu.closure(A), DIRECT_OUT),
+        "maxmins": (lambda: gpu.maxmins(A), DIRECT_OUT),
+        "maxmin_masked": (lambda: gpu.maxmin_masked(A, B, tfs), DIRECT_OUT),
+        "mcp_tf": (lambda: gpu.mcp_tf(A, tfs, 4, 3), DIRECT_OUT),
+        "maxmins_tf": (lambda: gpu.maxmins_tf(A, tfs), DIRECT_OUT),
+        "dpi_tf": (lambda: gpu.dpi_tf(A, tfs, 0.1, want_mask=True), DIRECT_OUT),
+        "transform": (lambda: gpu.transform(A), DIRECT_OUT),
+        "stouffer_tf": (lambda: gpu.stouffer_tf(A[:40]), DIRECT_OUT),
+        "combo": (lambda: gpu.combo(A, B, A, B, [0.25, 0.25, 0.25, 0.25]), DIRECT_IN | DIRECT_OUT),
+    }
+    for name, (fn, want_bits) in cases.items():
+        a, b, bits = _both(gpu, fn)
+        assert bits == want_bits, name
+        _same(a, b)
