@@ -3,7 +3,9 @@
 //
 //   mcpgpu_cli mi     -i expr.exp -o mi.exp [-m 1] [-b 10] [-l 3] [--seed S]
 //   mcpgpu_cli mcp    -i mi.exp -o mcp.exp -m {1,2,3} [--diagonal 0] [-x maxmin.exp]
-//   mcpgpu_cli dpi    -i mi.exp -o dpi.exp [-l 0.1] [--diagonal 0]     (diagonal 0 by default)
+//                     [-f tfs.txt [--tf-gene-transition T]] [--clamped]
+//   mcpgpu_cli mcp    -i mi.exp -o mcp.exp -m 5 --first a.exp --second b.exp [--diagonal 0] [-x maxmin.exp]
+//   mcpgpu_cli dpi    -i mi.exp -o dpi.exp [-l 0.1] [--diagonal 0] [-f tfs.txt]   (diagonal 0 by default)
 //   mcpgpu_cli mcpnet -i expr.exp -o prefix [--mi-method 1] [--mi-input] [-m 1 2 3 4] [-f coeffs.exp]
 //                     [--eval (-g truth.txt | -x truth.exp)] [--diagonal 0] [--seed S] [--tf-input tfs.txt]
 //   mcpgpu_cli convert -i a.exp -o b.csv          (no GPU needed)
@@ -17,6 +19,14 @@
 //   MCP (`mcp -m`, `mcpnet -m`): 1 = MCP2, 2 = MCP3, 3 = MCP4 (apps/filter/mcp.cpp:62-66),
 //       and for mcpnet 4 = ensemble MCP (apps/pipeline/mcpnet.cpp:63-68, 519-719)
 //       with its Stouffer variant (row statistics: see include/mcpgpu.h).
+// mcp -f / dpi -f (apps/filter/mcp.cpp:94-95, dpi.cpp:80-81) keep TF rows: mcp runs
+// compute_mcp{2,3,4}_tfs with --tf-gene-transition (the app's default -1 acts as 0
+// for MCP2 / MCP3 and as 1 for MCP4, whose second product masks on any value but 0,
+// mcp.cpp:526-537), without MCP3's max(M, M^T); dpi runs dpi_tf_kernel over all pairs
+// and writes the TF rows (dpi.cpp:224-303; its --tf-gene-transition is unused).
+// mcp -m 5 (MCP from partials, mcp.cpp:616-650): ratio(input, first (x) second); the app
+// itself reads --first for both operands (mcp.cpp:185-195), here --second is read.
+// --clamped is accepted and, as in the app, changes nothing.
 // mcpnet outputs follow apps/pipeline/mcpnet.cpp: <prefix>_{bs|ap|inmi}.mi.<ext>,
 // .mcp2/.mcp3/.mcp4.<ext>, and for the ensemble .mcp_<c0>_<c1>_<c2>_<c3>.<ext>
 // and the Stouffer-transformed .mcpst_<c0>_<c1>_<c2>_<c3>.<ext> (coefficients
@@ -152,8 +162,8 @@ void write_matrix(const std::string& path, const Matrix<float>& m, const std::ve
 }
 
 struct Args {
-    std::string cmd, in, out, maxmin_out, coeffs, truth_list, truth_mat, tf_input;
-    int bins = 10, order = 3, mi_method = 1;
+    std::string cmd, in, out, maxmin_out, coeffs, truth_list, truth_mat, tf_input, first, second;
+    int bins = 10, order = 3, mi_method = 1, tf_transition = -1;
     std::vector<int> methods;
     float diagonal = 0.0f, tol = 0.1f;
     uint64_t seed = 1;
@@ -192,7 +202,14 @@ Args parse(int argc, char** argv) {
         } else if (k == "--maxmin-output") a.maxmin_out = next();
         else if (k == "--groundtruth-matrix") a.truth_mat = next();
         else if (k == "-g" || k == "--groundtruth-list") a.truth_list = next();
-        else if (k == "-f" || k == "--coefficients") a.coeffs = next();
+        else if (k == "-f") {
+            if (a.cmd == "mcpnet") a.coeffs = next();  // mcpnet -f = coefficients
+            else a.tf_input = next();                  // mcp / dpi -f = TF list
+        } else if (k == "--coefficients") a.coeffs = next();
+        else if (k == "--tf-gene-transition") a.tf_transition = std::atoi(next().c_str());
+        else if (k == "--first") a.first = next();
+        else if (k == "--second") a.second = next();
+        else if (k == "--clamped") {}
         else if (k == "--eval") a.eval = true;
         else if (k == "--seed") a.seed = std::strtoull(next().c_str(), nullptr, 10);
         else if (k == "--tf-input") a.tf_input = next();
@@ -357,7 +374,7 @@ int main(int argc, char** argv) {
             return 0;
         }
         // the TF list is checked before the device is touched (mcpnet.cpp:207-211)
-        const TfSel tf = a.cmd == "mcpnet" ? load_tfs(a.tf_input, in.rows) : TfSel{};
+        const TfSel tf = a.cmd == "convert" ? TfSel{} : load_tfs(a.tf_input, in.rows);
         if (tf.on && tf.rows.empty()) {
             std::fprintf(stderr, "ERROR: no transcription factors in the specified file\n");
             return 1;
@@ -371,20 +388,50 @@ int main(int argc, char** argv) {
             write_matrix(a.out, mi, in.rows, in.rows);
         } else if (a.cmd == "mcp") {
             int method = a.methods.empty() ? 1 : a.methods[0];
-            if (method < 1 || method > 3) throw std::runtime_error("mcp -m must be 1 (MCP2), 2 (MCP3) or 3 (MCP4)");
+            if (method != 5 && (method < 1 || method > 3))
+                throw std::runtime_error("mcp -m must be 1 (MCP2), 2 (MCP3), 3 (MCP4) or 5 (MCP from partials)");
             if (a.diagonal_set) mcpgpu::set_diagonal(in.m, a.diagonal);  // the mcp app resets only on request
             Matrix<float> ratio, maxmin;
-            // the mcp app symmetrises MCP3 (apps/filter/mcp.cpp:463-476)
-            mcpgpu::compute_mcp(ctx, in.m, method + 1, ratio, &maxmin, method == 2);
-            std::printf("Compute MCP%d in %.6f sec\n", method + 1, now_s() - t0);
-            if (!a.maxmin_out.empty()) write_matrix(a.maxmin_out, maxmin, in.rows, in.rows);
-            write_matrix(a.out, ratio, in.rows, in.rows);
+            if (method == 5) {  // MCP from partials (mcp.cpp:616-650)
+                if (tf.on) throw std::runtime_error("transcription factors are not supported with mcp -m 5");
+                if (a.first.empty() || a.second.empty()) throw std::runtime_error("mcp -m 5 needs --first and --second");
+                Named f1 = read_matrix(a.first), f2 = read_matrix(a.second);
+                if (a.diagonal_set) {
+                    mcpgpu::set_diagonal(f1.m, a.diagonal);
+                    mcpgpu::set_diagonal(f2.m, a.diagonal);
+                }
+                if (f1.m.columns() != f2.m.columns() || f1.m.rows() != in.m.rows() || f2.m.rows() != in.m.columns())
+                    throw std::runtime_error("mcp -m 5: --first must be n x k and --second n x k for an n x n input");
+                mcpgpu::maxmin(ctx, f1.m, f2.m, maxmin);
+                mcpgpu::compute_ratio(ctx, in.m, maxmin, ratio);
+            } else if (tf.on) {
+                // the app's default transition -1 (mcp.cpp:77) takes the branches of 0 for MCP2 / MCP3 and of 1 for
+                // MCP4 (its second product is masked for every value but 0)
+                int tr = a.tf_transition;
+                if (tr < 0) tr = method == 3 ? 1 : 0;
+                mcpgpu::compute_mcp_tfs(ctx, in.m, tf.tfs, method + 1, tr, ratio, &maxmin);
+            } else {
+                // the mcp app symmetrises MCP3 (apps/filter/mcp.cpp:463-476)
+                mcpgpu::compute_mcp(ctx, in.m, method + 1, ratio, &maxmin, method == 2);
+            }
+            std::printf("Compute MCP%d in %.6f sec\n", method == 5 ? 2 : method + 1, now_s() - t0);
+            const std::vector<std::string>& rn = tf.on ? tf.names : in.rows;
+            if (!a.maxmin_out.empty()) write_matrix(a.maxmin_out, maxmin, rn, in.rows);
+            write_matrix(a.out, ratio, rn, in.rows);
         } else if (a.cmd == "dpi") {
             mcpgpu::set_diagonal(in.m, a.diagonal);
             Matrix<float> out;
-            int64_t removed = mcpgpu::dpi_filter(ctx, in.m, a.tol, out);
+            int64_t removed = tf.on ? mcpgpu::dpi_filter_tfs(ctx, in.m, a.tol, tf.tfs, out)
+                                    : mcpgpu::dpi_filter(ctx, in.m, a.tol, out);
             std::printf("Mask removing %lld elements \n", (long long)removed);
-            write_matrix(a.out, out, in.rows, in.rows);
+            if (tf.on) {  // keep the TF rows (dpi.cpp:292-303)
+                Matrix<float> rows((int64_t)tf.rows.size(), out.columns());
+                for (size_t r = 0; r < tf.rows.size(); ++r)
+                    for (int64_t j = 0; j < out.columns(); ++j) rows.at((int64_t)r, j) = out.at(tf.rows[r], j);
+                write_matrix(a.out, rows, tf.names, in.rows);
+            } else {
+                write_matrix(a.out, out, in.rows, in.rows);
+            }
         } else if (a.cmd == "mcpnet") {
             const std::string ext = ext_of(a.in);
             const std::vector<std::string>& genes = in.rows;

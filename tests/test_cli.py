@@ -237,3 +237,46 @@ def test_cli_tf_input_without_tfs(built_lib, tmp_path):
     r = run("mcpnet", "-i", tmp_path / "mi.exp", "-o", tmp_path / "o", "--mi-input", "--tf-input",
             tmp_path / "tfs.txt")
     assert r.returncode != 0 and "no transcription factors" in r.stderr
+
+
+@pytest.mark.gpu
+def test_cli_mcp_dpi_tf_and_partials(built_lib, port, tmp_path):
+    """mcp -f / dpi -f keep TF rows (compute_mcp{2,3,4}_tfs; dpi_tf_kernel over all
+    pairs), the mcp app's default transition -1 (0 for MCP2 / MCP3, 1 for MCP4), and
+    mcp -m 5: ratio(input, first (x) second)."""
+    n = 48
+    X = built_lib.synth_grn(n, 200, seed=23)
+    A = port.bspline_mi(X)
+    np.fill_diagonal(A, 0)
+    names = [f"g{i}" for i in range(n)]
+    write_exp(tmp_path / "mi.exp", A, names)
+    tf_rows = [i for i in range(n) if i % 4 == 3]
+    (tmp_path / "tfs.txt").write_text("".join(f"g{i}\n" for i in tf_rows))
+    tfs = np.full(n, -np.inf, np.float32)
+    tfs[tf_rows] = np.inf
+    for method, tr, want_tr in ((1, None, 0), (2, None, 0), (3, None, 1), (3, 2, 2), (1, 1, 1)):
+        extra = [] if tr is None else ["--tf-gene-transition", tr]
+        r = run("mcp", "-i", tmp_path / "mi.exp", "-o", tmp_path / "m.exp", "-m", method, "-f", tmp_path / "tfs.txt",
+                "-x", tmp_path / "mm.exp", *extra)
+        assert r.returncode == 0, r.stderr
+        M, R = port.mcp_tf(A, tfs, method + 1, want_tr)
+        assert np.array_equal(read_exp(tmp_path / "m.exp"), R), (method, tr)
+        assert np.array_equal(read_exp(tmp_path / "mm.exp"), M), (method, tr)
+        rows = [l.split("\t")[0] for l in (tmp_path / "m.exp").read_text().splitlines()[1:]]
+        assert rows == [f"g{i}" for i in tf_rows]
+    r = run("dpi", "-i", tmp_path / "mi.exp", "-o", tmp_path / "d.exp", "-l", "0.1", "-f", tmp_path / "tfs.txt")
+    assert r.returncode == 0, r.stderr
+    out, _, removed = port.dpi_tf(A, tfs, 0.1)
+    assert np.array_equal(read_exp(tmp_path / "d.exp"), out[tf_rows])
+    assert f"Mask removing {removed} elements" in r.stdout
+    rng = np.random.default_rng(5)
+    F1 = rng.random((n, 30)).astype(np.float32)
+    F2 = rng.random((n, 30)).astype(np.float32)
+    write_exp(tmp_path / "f1.exp", F1, names)
+    write_exp(tmp_path / "f2.exp", F2, names)
+    r = run("mcp", "-i", tmp_path / "mi.exp", "-o", tmp_path / "p.exp", "-m", "5", "--first", tmp_path / "f1.exp",
+            "--second", tmp_path / "f2.exp", "-x", tmp_path / "pm.exp", "--clamped")
+    assert r.returncode == 0, r.stderr
+    MM = port.maxmin(F1, F2)
+    assert np.array_equal(read_exp(tmp_path / "pm.exp"), MM)
+    assert np.array_equal(read_exp(tmp_path / "p.exp"), port.ratio(A, MM))
