@@ -335,6 +335,14 @@ MCPG_API int mcpg_stouffer_tf(mcpg_handle* h, const float* A, int64_t rows, int6
                               int64_t ldo);
 MCPG_API int mcpg_stouffer_tf_dev(mcpg_handle* h, const float* A, int64_t rows, int64_t cols, int64_t lda,
                                   float* out, int64_t ldo);
+/* The TF transform of the transform app (apps/transform/transform.cpp:156-209):
+ * the same z-scores combined by zscored_stouffer_kernel (MCPG_TRANSFORM_STOUFFER,
+ * = mcpg_stouffer_tf) or zscored_clr_kernel (MCPG_TRANSFORM_CLR,
+ * include/mcp/transform/clr.hpp:75-88: sqrt(z_row^2 + z_col^2)). */
+MCPG_API int mcpg_transform_tf(mcpg_handle* h, const float* A, int64_t rows, int64_t cols, int64_t lda, int transform,
+                               float* out, int64_t ldo);
+MCPG_API int mcpg_transform_tf_dev(mcpg_handle* h, const float* A, int64_t rows, int64_t cols, int64_t lda,
+                                   int transform, float* out, int64_t ldo);
 /* The statistics mcpg_stouffer_tf_dev uses, into device float arrays: row_mean /
  * row_sd (rows entries) and col_mean / col_sd (cols entries). */
 MCPG_API int mcpg_stouffer_tf_stats_dev(mcpg_handle* h, const float* A, int64_t rows, int64_t cols, int64_t lda,

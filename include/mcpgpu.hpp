@@ -335,10 +335,12 @@ inline void compute_maxmins_tfs(Context& ctx, const Matrix<float>& g2g, const st
               "compute_maxmins_tfs");
 }
 
-// compute_stouffer_tf of a TFs x genes matrix.
-inline void compute_stouffer_tf(Context& ctx, const Matrix<float>& in, Matrix<float>& out) {
+// compute_stouffer_tf of a TFs x genes matrix (clr = true: the transform app's
+// zscored_clr_kernel instead).
+inline void compute_stouffer_tf(Context& ctx, const Matrix<float>& in, Matrix<float>& out, bool clr = false) {
     out.resize(in.rows(), in.columns());
-    ctx.check(mcpg_stouffer_tf(ctx.handle(), in.data(), in.rows(), in.columns(), in.ld(), out.data(), out.ld()),
+    ctx.check(mcpg_transform_tf(ctx.handle(), in.data(), in.rows(), in.columns(), in.ld(),
+                                clr ? MCPG_TRANSFORM_CLR : MCPG_TRANSFORM_STOUFFER, out.data(), out.ld()),
               "compute_stouffer_tf");
 }
 

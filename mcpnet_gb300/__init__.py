@@ -121,6 +121,8 @@ ABI += [
     ("mcpg_stouffer_tf", C.c_int, [_vp, _vp, _i64, _i64, _i64, _vp, _i64]),
     ("mcpg_stouffer_tf_dev", C.c_int, [_vp, _vp, _i64, _i64, _i64, _vp, _i64]),
     ("mcpg_stouffer_tf_stats_dev", C.c_int, [_vp, _vp, _i64, _i64, _i64, _vp, _vp, _vp, _vp]),
+    ("mcpg_transform_tf", C.c_int, [_vp, _vp, _i64, _i64, _i64, C.c_int, _vp, _i64]),
+    ("mcpg_transform_tf_dev", C.c_int, [_vp, _vp, _i64, _i64, _i64, C.c_int, _vp, _i64]),
     ("mcpg_combo_stouffer_tf_eval", C.c_int, [_vp, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _i64, _i64, _vp,
                                               _i64, C.c_int, _vp, _vp, _vp, _i64, _vp, _vp, _vp]),
     ("mcpg_combo_stouffer_tf_eval_dev", C.c_int, [_vp, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _i64, _i64, _vp,
@@ -653,6 +655,20 @@ class Handle:
         out = np.empty((rows, cols), dtype=np.float32)
         self._check(self._L.mcpg_stouffer_tf(self._h, _ptr(A), rows, cols, cols, _ptr(out), cols), "stouffer_tf")
         return out
+
+    def transform_tf(self, A, kind="stouffer"):
+        """The transform app's TF form (row and column z-scores; Stouffer or CLR) of a t x n host matrix."""
+        A = _f32(A)
+        rows, cols = A.shape
+        out = np.empty((rows, cols), dtype=np.float32)
+        self._check(self._L.mcpg_transform_tf(self._h, _ptr(A), rows, cols, cols, TRANSFORMS[kind], _ptr(out), cols),
+                    "transform_tf")
+        return out
+
+    def transform_tf_dev(self, A, out, kind="stouffer"):
+        rows, cols = A.shape
+        self._check(self._L.mcpg_transform_tf_dev(self._h, self._dp(A), rows, cols, self._ld(A), TRANSFORMS[kind],
+                                                   self._dp(out), self._ld(out)), "transform_tf_dev")
 
     def stouffer_tf_dev(self, A, out):
         rows, cols = A.shape

@@ -8,6 +8,7 @@
 //   mcpgpu_cli dpi    -i mi.exp -o dpi.exp [-l 0.1] [--diagonal 0] [-f tfs.txt]   (diagonal 0 by default)
 //   mcpgpu_cli mcpnet -i expr.exp -o prefix [--mi-method 1] [--mi-input] [-m 1 2 3 4] [-f coeffs.exp]
 //                     [--eval (-g truth.txt | -x truth.exp)] [--diagonal 0] [--seed S] [--tf-input tfs.txt]
+//   mcpgpu_cli transform -i mi.exp -o out.exp -m {1,2} [-f tfs.txt]   (1 = CLR, 2 = Stouffer)
 //   mcpgpu_cli convert -i a.exp -o b.csv          (no GPU needed)
 //
 // Method values keep the reference's numbering and add the GPU forms:
@@ -27,6 +28,10 @@
 // mcp -m 5 (MCP from partials, mcp.cpp:616-650): ratio(input, first (x) second); the app
 // itself reads --first for both operands (mcp.cpp:185-195), here --second is read.
 // --clamped is accepted and, as in the app, changes nothing.
+// transform (apps/transform/transform.cpp): -m 1 CLR, 2 Stouffer of the square matrix with
+// each row's mean and unbiased sd without its diagonal entry (GaussianParamsExclude1); with
+// -f, the TF rows z-scored by row and by column (StandardScore) and combined by
+// zscored_clr_kernel / zscored_stouffer_kernel (transform.cpp:156-209).
 // mcpnet outputs follow apps/pipeline/mcpnet.cpp: <prefix>_{bs|ap|inmi}.mi.<ext>,
 // .mcp2/.mcp3/.mcp4.<ext>, and for the ensemble .mcp_<c0>_<c1>_<c2>_<c3>.<ext>
 // and the Stouffer-transformed .mcpst_<c0>_<c1>_<c2>_<c3>.<ext> (coefficients
@@ -172,7 +177,8 @@ struct Args {
 
 Args parse(int argc, char** argv) {
     Args a;
-    if (argc < 2) throw std::runtime_error("usage: mcpgpu_cli {mi|mcp|dpi|mcpnet|convert} -i IN -o OUT [options]");
+    if (argc < 2)
+        throw std::runtime_error("usage: mcpgpu_cli {mi|mcp|dpi|mcpnet|transform|convert} -i IN -o OUT [options]");
     a.cmd = argv[1];
     for (int i = 2; i < argc; ++i) {
         std::string k = argv[i];
@@ -432,6 +438,21 @@ int main(int argc, char** argv) {
             } else {
                 write_matrix(a.out, out, in.rows, in.rows);
             }
+        } else if (a.cmd == "transform") {
+            int method = a.methods.empty() ? 2 : a.methods[0];
+            if (method != 1 && method != 2) throw std::runtime_error("transform -m must be 1 (CLR) or 2 (Stouffer)");
+            if (in.m.rows() != in.m.columns()) throw std::runtime_error("transform needs a square matrix");
+            Matrix<float> out;
+            if (tf.on) {
+                Matrix<float> rows((int64_t)tf.rows.size(), in.m.columns());
+                for (size_t r = 0; r < tf.rows.size(); ++r)
+                    for (int64_t j = 0; j < in.m.columns(); ++j) rows.at((int64_t)r, j) = in.m.at(tf.rows[r], j);
+                mcpgpu::compute_stouffer_tf(ctx, rows, out, method == 1);
+            } else {
+                mcpgpu::compute_stouffer(ctx, in.m, out, method == 1);
+            }
+            std::printf("Transformed in %.6f sec\n", now_s() - t0);
+            write_matrix(a.out, out, tf.on ? tf.names : in.rows, in.rows);
         } else if (a.cmd == "mcpnet") {
             const std::string ext = ext_of(a.in);
             const std::vector<std::string>& genes = in.rows;

@@ -1556,7 +1556,8 @@ int tf_stats_dev(mcpg_handle* h, const float* A, int64_t rows, int64_t cols, int
     return MCPG_OK;
 }
 
-int stouffer_tf_dev(mcpg_handle* h, const float* A, int64_t rows, int64_t cols, int64_t lda, float* out, int64_t ldo) {
+int stouffer_tf_dev(mcpg_handle* h, const float* A, int64_t rows, int64_t cols, int64_t lda, float* out, int64_t ldo,
+                    int clr = 0) {
     if (rows < 0 || cols < 0) return fail(h, MCPG_ERR_ARG, "stouffer_tf: negative size");
     if (rows == 0 || cols == 0) return MCPG_OK;
     if (!A || !out || lda < cols || ldo < cols)
@@ -1571,8 +1572,9 @@ int stouffer_tf_dev(mcpg_handle* h, const float* A, int64_t rows, int64_t cols, 
     if ((rc = tf_stats_dev(h, A, rows, cols, lda, rmean, rsd, cmean, csd))) return rc;
     {
         PROF(h, "transform");
-        CK(h, mcpg::launch_stouffer_tf(A, rows, cols, lda, rmean, rsd, cmean, csd, out, ldo, h->stream, &h->launches),
-           "TF Stouffer transform");
+        CK(h, mcpg::launch_stouffer_tf(A, rows, cols, lda, rmean, rsd, cmean, csd, clr, out, ldo, h->stream,
+                                       &h->launches),
+           "TF transform");
     }
     return MCPG_OK;
 }
@@ -2714,6 +2716,34 @@ int mcpg_stouffer_tf_dev(mcpg_handle* h, const float* A, int64_t rows, int64_t c
     int rc = check_handle(h);
     if (rc) return rc;
     return stouffer_tf_dev(h, A, rows, cols, lda, out, ldo);
+}
+
+int mcpg_transform_tf_dev(mcpg_handle* h, const float* A, int64_t rows, int64_t cols, int64_t lda, int transform,
+                          float* out, int64_t ldo) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (transform != MCPG_TRANSFORM_STOUFFER && transform != MCPG_TRANSFORM_CLR)
+        return fail(h, MCPG_ERR_ARG, "transform_tf: unknown transform %d", transform);
+    return stouffer_tf_dev(h, A, rows, cols, lda, out, ldo, transform == MCPG_TRANSFORM_CLR);
+}
+
+int mcpg_transform_tf(mcpg_handle* h, const float* A, int64_t rows, int64_t cols, int64_t lda, int transform,
+                      float* out, int64_t ldo) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (transform != MCPG_TRANSFORM_STOUFFER && transform != MCPG_TRANSFORM_CLR)
+        return fail(h, MCPG_ERR_ARG, "transform_tf: unknown transform %d", transform);
+    if (rows < 0 || cols < 0) return fail(h, MCPG_ERR_ARG, "transform_tf: negative size");
+    if (rows == 0 || cols == 0) return MCPG_OK;
+    if (!A || !out || lda < cols || ldo < cols)
+        return fail(h, MCPG_ERR_ARG, "transform_tf: null pointer or leading dimension");
+    float *da, *dout;
+    int64_t la, lo;
+    if ((rc = stage_in(h, S_IN0, A, lda, rows, cols, &da, &la))) return rc;
+    if ((rc = out_view(h, S_OUT0, out, ldo, rows, cols, &dout, &lo))) return rc;
+    if ((rc = stouffer_tf_dev(h, da, rows, cols, la, dout, lo, transform == MCPG_TRANSFORM_CLR))) return rc;
+    if ((rc = copy_out(h, out, ldo, dout, lo, rows, cols))) return rc;
+    return finish(h);
 }
 
 int mcpg_stouffer_tf(mcpg_handle* h, const float* A, int64_t rows, int64_t cols, int64_t lda, float* out,

@@ -224,10 +224,11 @@ cudaError_t launch_row_stats(const float* A, int64_t rows, int64_t cols, int64_t
 // mean[j], sd[j] of column j over the rows (FP64 two-pass, population variance).
 cudaError_t launch_col_stats(const float* A, int64_t rows, int64_t cols, int64_t lda, float* mean, float* sd,
                              cudaStream_t stream, int64_t* launches);
-// out[i][j] = zscored_stouffer_kernel of the row and column z-scores of A[i][j].
+// out[i][j] = zscored_stouffer_kernel (clr = 0) or zscored_clr_kernel (clr = 1) of the
+// row and column z-scores of A[i][j].
 cudaError_t launch_stouffer_tf(const float* A, int64_t rows, int64_t cols, int64_t lda, const float* rmean,
-                               const float* rsd, const float* cmean, const float* csd, float* out, int64_t ldo,
-                               cudaStream_t stream, int64_t* launches);
+                               const float* rsd, const float* cmean, const float* csd, int clr, float* out,
+                               int64_t ldo, cudaStream_t stream, int64_t* launches);
 // out[i][j] = stouffer_vector_kernel (clr = 0) or clr_vector_kernel (clr = 1) of A[i][j]
 // with row i's and row j's statistics.
 cudaError_t launch_transform(const float* A, int64_t n, int64_t lda, const float* mean, const float* sd, int clr,

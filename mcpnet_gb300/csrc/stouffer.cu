@@ -19,7 +19,8 @@
 //     statistics; also absent from the snapshot -- here FP64 two-pass mean and
 //     population sd rounded to float, z = |sd| < eps ? 0 : (x - mean) / sd in
 //     float), then zscored_stouffer_kernel (stouffer.hpp:84-100):
-//     (z_row + z_col) * (float)sqrt(1/2).
+//     (z_row + z_col) * (float)sqrt(1/2), or zscored_clr_kernel (clr.hpp:75-88):
+//     sqrt(z_row^2 + z_col^2).
 #include <cuda_runtime.h>
 #include <float.h>
 #include <stdint.h>
@@ -132,7 +133,9 @@ __device__ __forceinline__ float zscore(float x, float mean, float sd) {
     return fabsf(sd) < FLT_EPSILON ? 0.0f : __fdiv_rn(__fsub_rn(x, mean), sd);
 }
 
-// zscored_stouffer_kernel over a rows x cols matrix with row and column statistics.
+// zscored_stouffer_kernel (CLR = 0) or zscored_clr_kernel (CLR = 1) over a rows x
+// cols matrix with row and column statistics.
+template <int CLR>
 __global__ void stouffer_tf_kernel(const float* A, int64_t rows, int64_t cols, int64_t lda, const float* rmean,
                                    const float* rsd, const float* cmean, const float* csd, float* out, int64_t ldo) {
     const float isqrt2 = 0.70710678118654752440f;
@@ -142,7 +145,8 @@ __global__ void stouffer_tf_kernel(const float* A, int64_t rows, int64_t cols, i
         const float x = A[i * lda + j];
         const float zi = zscore(x, rmean[i], rsd[i]);
         const float zj = zscore(x, cmean[j], csd[j]);
-        out[i * ldo + j] = __fmul_rn(__fadd_rn(zi, zj), isqrt2);
+        out[i * ldo + j] = CLR ? __fsqrt_rn(__fadd_rn(__fmul_rn(zi, zi), __fmul_rn(zj, zj)))
+                               : __fmul_rn(__fadd_rn(zi, zj), isqrt2);
     }
 }
 
@@ -182,10 +186,15 @@ cudaError_t launch_col_stats(const float* A, int64_t rows, int64_t cols, int64_t
 }
 
 cudaError_t launch_stouffer_tf(const float* A, int64_t rows, int64_t cols, int64_t lda, const float* rmean,
-                               const float* rsd, const float* cmean, const float* csd, float* out, int64_t ldo,
-                               cudaStream_t st, int64_t* launches) {
+                               const float* rsd, const float* cmean, const float* csd, int clr, float* out,
+                               int64_t ldo, cudaStream_t st, int64_t* launches) {
     if (rows <= 0 || cols <= 0) return cudaSuccess;
-    stouffer_tf_kernel<<<ew_grid(rows * cols), 256, 0, st>>>(A, rows, cols, lda, rmean, rsd, cmean, csd, out, ldo);
+    if (clr)
+        stouffer_tf_kernel<1><<<ew_grid(rows * cols), 256, 0, st>>>(A, rows, cols, lda, rmean, rsd, cmean, csd, out,
+                                                                     ldo);
+    else
+        stouffer_tf_kernel<0><<<ew_grid(rows * cols), 256, 0, st>>>(A, rows, cols, lda, rmean, rsd, cmean, csd, out,
+                                                                     ldo);
     if (launches) ++*launches;
     return cudaGetLastError();
 }

@@ -320,10 +320,11 @@ void orc_col_stats(const float* A, int64_t rows, int64_t cols, int64_t lda, floa
 /* compute_stouffer_tf (mcpnet_helper.hpp:589-634) given the row statistics
  * (population, over each row's cols entries) and the column statistics: the
  * z-scores in float, |sd| < FLT_EPSILON -> 0, then zscored_stouffer_kernel
- * (include/mcp/transform/stouffer.hpp:84-100): (z_row + z_col) * sqrt(1/2).
+ * (include/mcp/transform/stouffer.hpp:84-100): (z_row + z_col) * sqrt(1/2), or
+ * with clr zscored_clr_kernel (clr.hpp:75-88): sqrt(z_row^2 + z_col^2).
  * The z matrices go to zr / zc when those are not null (rows x cols, ld cols). */
 void orc_stouffer_tf(const float* A, int64_t rows, int64_t cols, int64_t lda, const float* rmean, const float* rsd,
-                     const float* cmean, const float* csd, float* out, int64_t ldo, float* zr, float* zc) {
+                     const float* cmean, const float* csd, int clr, float* out, int64_t ldo, float* zr, float* zc) {
     const float isqrt2 = 0.70710678118654752440f;
     for (int64_t i = 0; i < rows; ++i)
         for (int64_t j = 0; j < cols; ++j) {
@@ -332,7 +333,7 @@ void orc_stouffer_tf(const float* A, int64_t rows, int64_t cols, int64_t lda, co
             const float zj = (fabsf(csd[j]) < FLT_EPSILON) ? 0.0f : (x - cmean[j]) / csd[j];
             if (zr) zr[i * cols + j] = zi;
             if (zc) zc[i * cols + j] = zj;
-            out[i * ldo + j] = (zi + zj) * isqrt2;
+            out[i * ldo + j] = clr ? sqrtf(zi * zi + zj * zj) : (zi + zj) * isqrt2;
         }
 }
 

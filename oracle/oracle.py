@@ -173,7 +173,7 @@ class _Port(_TfCompositions, _EvalCompositions):
         self.L.orc_transform.argtypes = [_vp, _i64, _i64, _vp, _vp, C.c_int, _vp, _i64]
         self.L.orc_row_stats_pop.argtypes = [_vp, _i64, _i64, _i64, _vp, _vp]
         self.L.orc_col_stats.argtypes = [_vp, _i64, _i64, _i64, _vp, _vp]
-        self.L.orc_stouffer_tf.argtypes = [_vp, _i64, _i64, _i64, _vp, _vp, _vp, _vp, _vp, _i64, _vp, _vp]
+        self.L.orc_stouffer_tf.argtypes = [_vp, _i64, _i64, _i64, _vp, _vp, _vp, _vp, C.c_int, _vp, _i64, _vp, _vp]
         self.L.orc_ap_mi.argtypes = [_vp, _i64, _i64, _vp, _i64]
 
     @staticmethod
@@ -352,8 +352,9 @@ class _Port(_TfCompositions, _EvalCompositions):
         self.L.orc_col_stats(A.ctypes.data, rows, cols, cols, cm.ctypes.data, cs.ctypes.data)
         return rm, rs, cm, cs
 
-    def stouffer_tf_with_stats(self, A, rmean, rsd, cmean, csd, want_z=False):
-        """compute_stouffer_tf given the statistics; with want_z also the row / column z-score matrices."""
+    def stouffer_tf_with_stats(self, A, rmean, rsd, cmean, csd, want_z=False, clr=False):
+        """compute_stouffer_tf given the statistics (clr: the transform app's zscored_clr_kernel); with
+        want_z also the row / column z-score matrices."""
         A = np.ascontiguousarray(A, dtype=np.float32)
         rows, cols = A.shape
         f = lambda v: np.ascontiguousarray(v, dtype=np.float32)
@@ -362,12 +363,12 @@ class _Port(_TfCompositions, _EvalCompositions):
         zr = np.empty_like(A) if want_z else None
         zc = np.empty_like(A) if want_z else None
         self.L.orc_stouffer_tf(A.ctypes.data, rows, cols, cols, rmean.ctypes.data, rsd.ctypes.data, cmean.ctypes.data,
-                               csd.ctypes.data, out.ctypes.data, cols, None if zr is None else zr.ctypes.data,
+                               csd.ctypes.data, int(clr), out.ctypes.data, cols, None if zr is None else zr.ctypes.data,
                                None if zc is None else zc.ctypes.data)
         return (out, zr, zc) if want_z else out
 
-    def stouffer_tf(self, A):
-        return self.stouffer_tf_with_stats(A, *self.tf_stats(A))
+    def stouffer_tf(self, A, clr=False):
+        return self.stouffer_tf_with_stats(A, *self.tf_stats(A), clr=clr)
 
     def ap_ranks(self, X):
         """Descending ranks per gene, ties sharing the lowest rank (int64, n x m)."""
@@ -447,6 +448,7 @@ class _Ref(_TfCompositions, _EvalCompositions):
         L.ref_ap_mi_f32.argtypes = [_vp, _i64, _i64, _vp, _i64]
         L.ref_transform_f32.argtypes = [_vp, _i64, _i64, _vp, _vp, C.c_int, _vp, _i64]
         L.ref_zscored_stouffer_f32.argtypes = [_vp, _vp, _i64, _i64, _vp]
+        L.ref_zscored_clr_f32.argtypes = [_vp, _vp, _i64, _i64, _vp]
         L.ref_aupr_auroc_f64.argtypes = [_vp, _i64, _vp, _i64, _vp]
         self.L = L
 
@@ -476,6 +478,15 @@ class _Ref(_TfCompositions, _EvalCompositions):
         rows, cols = zi.shape
         out = np.empty_like(zi)
         self.L.ref_zscored_stouffer_f32(zi.ctypes.data, zj.ctypes.data, rows, cols, out.ctypes.data)
+        return out
+
+    def zscored_clr(self, zi, zj):
+        """MCPNet's zscored_clr_kernel on row-aligned row / column z-score matrices."""
+        zi = np.ascontiguousarray(zi, dtype=np.float32)
+        zj = np.ascontiguousarray(zj, dtype=np.float32)
+        rows, cols = zi.shape
+        out = np.empty_like(zi)
+        self.L.ref_zscored_clr_f32(zi.ctypes.data, zj.ctypes.data, rows, cols, out.ctypes.data)
         return out
 
     def ap_mi(self, R):

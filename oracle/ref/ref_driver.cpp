@@ -275,4 +275,11 @@ void ref_zscored_stouffer_f32(const float* zi, const float* zj, int64_t rows, in
     for (int64_t i = 0; i < rows; ++i) k(zi + i * cols, zj + i * cols, (size_t)cols, out + i * cols);
 }
 
+// zscored_clr_kernel<float> (include/mcp/transform/clr.hpp:75-88), as the
+// transform app's GlobalBinaryOp hands rows over (apps/transform/transform.cpp:192-198).
+void ref_zscored_clr_f32(const float* zi, const float* zj, int64_t rows, int64_t cols, float* out) {
+    mcp::kernel::zscored_clr_kernel<float> k;
+    for (int64_t i = 0; i < rows; ++i) k(zi + i * cols, zj + i * cols, (size_t)cols, out + i * cols);
+}
+
 }  // extern "C"

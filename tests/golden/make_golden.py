@@ -33,7 +33,7 @@ Fixtures (all float32 unless noted):
                  of compute_maxmins_tfs from the reference's masked max-min
                  kernel; a t x n matrix with a constant row and column, its
                  (oracle) statistics and the reference's zscored_stouffer_kernel
-                 output; the combo and TF-Stouffer coefficient searches over the
+                 and zscored_clr_kernel outputs; the combo and TF-Stouffer coefficient searches over the
                  TF truth rows
 
     python tests/golden/make_golden.py --only eval   # regenerate the eval fixtures only
@@ -265,7 +265,8 @@ def tf_ensemble(R):
     S[:, 7] = np.float32(0.5)
     rm, rs, cm, csd = P.tf_stats(S)
     _, zr, zc = P.stouffer_tf_with_stats(S, rm, rs, cm, csd, want_z=True)
-    out.update(st_in=S, st_rmean=rm, st_rsd=rs, st_cmean=cm, st_csd=csd, st_out=R.zscored_stouffer(zr, zc))
+    out.update(st_in=S, st_rmean=rm, st_rsd=rs, st_cmean=cm, st_csd=csd, st_out=R.zscored_stouffer(zr, zc),
+               clr_out=R.zscored_clr(zr, zc))
     lab = np.ascontiguousarray(labels[tf_idx])
     out.update(labels_tf=lab, row_gene=tf_idx.astype(np.int32), col_tf=col_tf, coeffs=cs)
     pr, roc, best = R.combo_eval(T, M1, M2, M3, lab, cs, "tf", tf_idx, col_tf)

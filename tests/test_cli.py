@@ -280,3 +280,35 @@ def test_cli_mcp_dpi_tf_and_partials(built_lib, port, tmp_path):
     MM = port.maxmin(F1, F2)
     assert np.array_equal(read_exp(tmp_path / "pm.exp"), MM)
     assert np.array_equal(read_exp(tmp_path / "p.exp"), port.ratio(A, MM))
+
+
+@pytest.mark.gpu
+def test_cli_transform(built_lib, port, tmp_path):
+    """transform -m 1 / 2: CLR / Stouffer of the square matrix (the GPU's statistics
+    are within an ulp of the oracle's, so the values agree to float rounding), and
+    with -f the TF form, equal bit for bit to the library's own call."""
+    n = 40
+    X = built_lib.synth_grn(n, 150, seed=24)
+    A = port.bspline_mi(X)
+    np.fill_diagonal(A, 0)
+    names = [f"g{i}" for i in range(n)]
+    write_exp(tmp_path / "mi.exp", A, names)
+    tf_rows = [1, 5, 6, 22, 39]
+    (tmp_path / "tfs.txt").write_text("".join(f"g{i}\n" for i in tf_rows))
+    import mcpnet_gb300 as M
+    h = M.Handle(0)
+    try:
+        for method, kind in ((1, "clr"), (2, "stouffer")):
+            r = run("transform", "-i", tmp_path / "mi.exp", "-o", tmp_path / "t.exp", "-m", method)
+            assert r.returncode == 0, r.stderr
+            got = read_exp(tmp_path / "t.exp")
+            assert np.array_equal(got, h.transform(A, kind))
+            np.testing.assert_allclose(got, port.transform(A, clr=(kind == "clr")), rtol=1e-5, atol=1e-5)
+            r = run("transform", "-i", tmp_path / "mi.exp", "-o", tmp_path / "tf.exp", "-m", method, "-f",
+                    tmp_path / "tfs.txt")
+            assert r.returncode == 0, r.stderr
+            got = read_exp(tmp_path / "tf.exp")
+            assert np.array_equal(got, h.transform_tf(A[tf_rows], kind))
+            np.testing.assert_allclose(got, port.stouffer_tf(A[tf_rows], clr=(kind == "clr")), rtol=1e-5, atol=1e-5)
+    finally:
+        h.close()

@@ -81,6 +81,14 @@ def test_stouffer_tf_golden(gpu, port, golden):
     gpu.stouffer_tf_dev(dS, o2)
     torch.cuda.synchronize()
     assert same_bits(o2.cpu().numpy(), out)
+    assert same_bits(gpu.transform_tf(S, "stouffer"), out)
+    clr = gpu.transform_tf(S, "clr")
+    assert same_bits(clr, port.stouffer_tf_with_stats(S, *stats, clr=True))
+    if all(np.array_equal(a, g[k]) for a, k in zip(stats, ("st_rmean", "st_rsd", "st_cmean", "st_csd"))):
+        assert same_bits(clr, g["clr_out"])
+    gpu.transform_tf_dev(dS, o2, "clr")
+    torch.cuda.synchronize()
+    assert same_bits(o2.cpu().numpy(), clr)
 
 
 @pytest.mark.parametrize("rows,cols", [(1, 1), (1, 9), (9, 1), (33, 300), (300, 33), (64, 4100)])

@@ -274,6 +274,8 @@ def test_stouffer_tf_bit_exact(port, golden):
     assert stats[1][3] == 0.0 and stats[3][7] == 0.0
     out = port.stouffer_tf_with_stats(S, *stats)
     assert np.array_equal(out.view(np.uint32), g["st_out"].view(np.uint32))
+    clr = port.stouffer_tf_with_stats(S, *stats, clr=True)  # the transform app's zscored_clr_kernel
+    assert np.array_equal(clr.view(np.uint32), g["clr_out"].view(np.uint32))
 
 
 def test_stouffer_tf_population_statistics(port):
