@@ -450,6 +450,52 @@ MCPG_API int mcpg_combo_stouffer_tf_eval(mcpg_handle* h, const float* mi, int64_
                                          int64_t cols, const int8_t* labels, int64_t ldl, int region,
                                          const int32_t* row_gene, const uint8_t* col_tf, const double* coeffs,
                                          int64_t n_coeffs, double* aupr, double* auroc, int64_t* best);
+/* ---- semi-supervised split evaluation (the eval_mcpnet app) ----
+ * The labelled entries of the region in the reference's mask order (row-major:
+ * select_lower_triangle, select_from_list's sorted mask, select_tfs_from_mat) are
+ * shuffled for iteration i = 1..iterations by std::shuffle with a std::mt19937
+ * seeded with i (shuffle_truth, apps/pipeline/eval_mcpnet.cpp:214-224); a part j
+ * trains on the first train_counts[j] shuffled entries and tests on the rest
+ * (the app uses counts (size_t)(f * entries) for f = 0.005, 0.01, 0.02, 0.05,
+ * 0.1, and also 0.2 .. 0.5 with TFs).  All AUPRs are aupr_kernel's
+ * (compute_aupr2, mcpnet_helper.hpp:1017-1035).  Fewer than 2^32 entries.
+ *
+ * mcpg_split_aupr: eval_aupr_mcp (eval_mcpnet.cpp:227-301) of one score matrix:
+ * full_aupr (nullable) over all entries; train_aupr / test_aupr (nullable,
+ * iterations x parts, row-major). */
+MCPG_API int mcpg_split_aupr(mcpg_handle* h, const float* values, int64_t rows, int64_t cols, int64_t ldv,
+                             const int8_t* labels, int64_t ldl, int region, const int32_t* row_gene,
+                             const uint8_t* col_tf, int64_t iterations, const int64_t* train_counts, int64_t parts,
+                             double* full_aupr, double* train_aupr, double* test_aupr);
+MCPG_API int mcpg_split_aupr_dev(mcpg_handle* h, const float* values, int64_t rows, int64_t cols, int64_t ldv,
+                                 const int8_t* labels, int64_t ldl, int region, const int32_t* row_gene,
+                                 const uint8_t* col_tf, int64_t iterations, const int64_t* train_counts,
+                                 int64_t parts, double* full_aupr, double* train_aupr, double* test_aupr);
+/* mcpg_split_combo_eval: eval_combos over the splits (eval_mcpnet.cpp:319-462,
+ * 814-893, the app's default --permute-combo): per iteration and part the
+ * coefficient row of highest training AUPR (the first strictly larger; row 0
+ * when none is; rows (1, 0, 0, 0) skipped), its test AUPR and its AUPR over all
+ * entries, and the same for the Stouffer-transformed combos.  stouffer:
+ * MCPG_STOUFFER_NONE, a MCPG_ROWSTATS_* mode (square matrices, as
+ * mcpg_transform) or MCPG_STOUFFER_TF (as mcpg_stouffer_tf).  results:
+ * iterations x parts x 6 host doubles -- train, test, Stouffer train, Stouffer
+ * test, full, Stouffer full (the Stouffer ones 0 without it); best (nullable):
+ * iterations x parts x 2 chosen rows.  Keeps n_coeffs x entries floats of
+ * Stouffer scores in device scratch. */
+#define MCPG_STOUFFER_NONE (-1)
+#define MCPG_STOUFFER_TF 2
+MCPG_API int mcpg_split_combo_eval(mcpg_handle* h, const float* mi, int64_t ldm, const float* M1, int64_t ld1,
+                                   const float* M2, int64_t ld2, const float* M3, int64_t ld3, int64_t rows,
+                                   int64_t cols, const int8_t* labels, int64_t ldl, int region,
+                                   const int32_t* row_gene, const uint8_t* col_tf, const double* coeffs,
+                                   int64_t n_coeffs, int stouffer, int64_t iterations, const int64_t* train_counts,
+                                   int64_t parts, double* results, int64_t* best);
+MCPG_API int mcpg_split_combo_eval_dev(mcpg_handle* h, const float* mi, int64_t ldm, const float* M1, int64_t ld1,
+                                       const float* M2, int64_t ld2, const float* M3, int64_t ld3, int64_t rows,
+                                       int64_t cols, const int8_t* labels, int64_t ldl, int region,
+                                       const int32_t* row_gene, const uint8_t* col_tf, const double* coeffs,
+                                       int64_t n_coeffs, int stouffer, int64_t iterations,
+                                       const int64_t* train_counts, int64_t parts, double* results, int64_t* best);
 /* Host-buffer form of mcpg_combo_eval_dev (matrices, labels, row_gene and col_tf on the host). */
 MCPG_API int mcpg_combo_eval(mcpg_handle* h, const float* mi, int64_t ldm, const float* M1, int64_t ld1,
                              const float* M2, int64_t ld2, const float* M3, int64_t ld3, int64_t rows, int64_t cols,

@@ -132,7 +132,25 @@ ABI += [
     ("mcpg_set_host_access", C.c_int, [_vp, C.c_int]),
     ("mcpg_last_host_access", C.c_int, [_vp]),
 ]
+ABI += [
+    ("mcpg_split_aupr", C.c_int, [_vp, _vp, _i64, _i64, _i64, _vp, _i64, C.c_int, _vp, _vp, _i64, _vp, _i64, _vp,
+                                  _vp, _vp]),
+    ("mcpg_split_aupr_dev", C.c_int, [_vp, _vp, _i64, _i64, _i64, _vp, _i64, C.c_int, _vp, _vp, _i64, _vp, _i64, _vp,
+                                      _vp, _vp]),
+    ("mcpg_split_combo_eval", C.c_int, [_vp, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _i64, _i64, _vp, _i64,
+                                        C.c_int, _vp, _vp, _vp, _i64, C.c_int, _i64, _vp, _i64, _vp, _vp]),
+    ("mcpg_split_combo_eval_dev", C.c_int, [_vp, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _i64, _i64, _vp, _i64,
+                                            C.c_int, _vp, _vp, _vp, _i64, C.c_int, _i64, _vp, _i64, _vp, _vp]),
+]
+STOUFFER_MODES = {"none": -1, "all": 0, "exclude_diagonal": 1, "tf": 2}
 HOST_ACCESS = {"auto": 0, "staged": 1}
+
+
+def train_counts(entries: int, tf: bool = False):
+    """The eval_mcpnet app's training sizes (apps/pipeline/eval_mcpnet.cpp:240-250): (size_t)(f * entries)
+    for f = 0.005, 0.01, 0.02, 0.05, 0.1, and with TFs also 0.2, 0.3, 0.4, 0.5."""
+    fr = [0.005, 0.01, 0.02, 0.05, 0.1] + ([0.2, 0.3, 0.4, 0.5] if tf else [])
+    return np.array([int(f * float(entries)) for f in fr], dtype=np.int64)
 TRANSFORMS = {"stouffer": 0, "clr": 1}
 ROW_STATS = {"all": 0, "exclude_diagonal": 1}
 TRUTH_REGIONS = {"lower": 0, "all": 1, "tf": 2}
@@ -674,6 +692,71 @@ class Handle:
         rows, cols = A.shape
         self._check(self._L.mcpg_stouffer_tf_dev(self._h, self._dp(A), rows, cols, self._ld(A), self._dp(out),
                                                   self._ld(out)), "stouffer_tf_dev")
+
+    # ---- semi-supervised split evaluation (eval_mcpnet) ----
+    def split_aupr(self, values, labels, iterations, train_counts, region="lower", row_gene=None, col_tf=None):
+        """eval_aupr_mcp on host arrays: (full AUPR, train[iters, parts], test[iters, parts])."""
+        values = _f32(values)
+        labels = np.ascontiguousarray(labels, dtype=np.int8)
+        rows, cols = values.shape
+        tc = np.ascontiguousarray(train_counts, dtype=np.int64)
+        rg = None if row_gene is None else np.ascontiguousarray(row_gene, dtype=np.int32)
+        ct = None if col_tf is None else np.ascontiguousarray(col_tf, dtype=np.uint8)
+        full = C.c_double(0)
+        tr = np.zeros((iterations, tc.size))
+        te = np.zeros((iterations, tc.size))
+        self._check(self._L.mcpg_split_aupr(self._h, _ptr(values), rows, cols, cols, _ptr(labels), cols,
+                                             TRUTH_REGIONS[region], _ptr(rg), _ptr(ct), iterations, _ptr(tc), tc.size,
+                                             C.byref(full), _ptr(tr), _ptr(te)), "split_aupr")
+        return full.value, tr, te
+
+    def split_aupr_dev(self, values, labels, iterations, train_counts, region="lower", row_gene=None, col_tf=None):
+        """As split_aupr for CUDA tensors (values float32, labels int8, row_gene int32, col_tf uint8)."""
+        rows, cols = values.shape
+        tc = np.ascontiguousarray(train_counts, dtype=np.int64)
+        full = C.c_double(0)
+        tr = np.zeros((iterations, tc.size))
+        te = np.zeros((iterations, tc.size))
+        self._check(self._L.mcpg_split_aupr_dev(self._h, self._dp(values), rows, cols, self._ld(values),
+                                                 self._dp(labels), self._ld(labels), TRUTH_REGIONS[region],
+                                                 self._dp(row_gene), self._dp(col_tf), iterations, _ptr(tc), tc.size,
+                                                 C.byref(full), _ptr(tr), _ptr(te)), "split_aupr_dev")
+        return full.value, tr, te
+
+    def split_combo_eval(self, mi, M1, M2, M3, labels, coeffs, iterations, train_counts, stouffer="none",
+                         region="lower", row_gene=None, col_tf=None):
+        """eval_combos over the shuffled splits on host arrays: (results[iters, parts, 6], best[iters, parts, 2])."""
+        mi = _f32(mi)
+        rows, cols = mi.shape
+        keep = [None if x is None else _f32(x) for x in (M1, M2, M3)]
+        labels = np.ascontiguousarray(labels, dtype=np.int8)
+        cs = np.ascontiguousarray(np.asarray(coeffs, dtype=np.float64).reshape(-1, 4))
+        tc = np.ascontiguousarray(train_counts, dtype=np.int64)
+        rg = None if row_gene is None else np.ascontiguousarray(row_gene, dtype=np.int32)
+        ct = None if col_tf is None else np.ascontiguousarray(col_tf, dtype=np.uint8)
+        res = np.zeros((iterations, tc.size, 6))
+        best = np.zeros((iterations, tc.size, 2), dtype=np.int64)
+        self._check(self._L.mcpg_split_combo_eval(
+            self._h, _ptr(mi), cols, _ptr(keep[0]), cols, _ptr(keep[1]), cols, _ptr(keep[2]), cols, rows, cols,
+            _ptr(labels), cols, TRUTH_REGIONS[region], _ptr(rg), _ptr(ct), cs.ctypes.data, cs.shape[0],
+            STOUFFER_MODES[stouffer], iterations, _ptr(tc), tc.size, _ptr(res), _ptr(best)), "split_combo_eval")
+        return res, best
+
+    def split_combo_eval_dev(self, mi, M1, M2, M3, labels, coeffs, iterations, train_counts, stouffer="none",
+                             region="lower", row_gene=None, col_tf=None):
+        """As split_combo_eval for CUDA tensors."""
+        rows, cols = mi.shape
+        ld = lambda t: self._ld(t) if t is not None else cols
+        cs = np.ascontiguousarray(np.asarray(coeffs, dtype=np.float64).reshape(-1, 4))
+        tc = np.ascontiguousarray(train_counts, dtype=np.int64)
+        res = np.zeros((iterations, tc.size, 6))
+        best = np.zeros((iterations, tc.size, 2), dtype=np.int64)
+        self._check(self._L.mcpg_split_combo_eval_dev(
+            self._h, self._dp(mi), self._ld(mi), self._dp(M1), ld(M1), self._dp(M2), ld(M2), self._dp(M3), ld(M3),
+            rows, cols, self._dp(labels), self._ld(labels), TRUTH_REGIONS[region], self._dp(row_gene),
+            self._dp(col_tf), cs.ctypes.data, cs.shape[0], STOUFFER_MODES[stouffer], iterations, _ptr(tc), tc.size,
+            _ptr(res), _ptr(best)), "split_combo_eval_dev")
+        return res, best
 
     def stouffer_tf_stats_dev(self, A):
         """The statistics of stouffer_tf_dev: (row_mean, row_sd, col_mean, col_sd) float32 CUDA tensors."""

@@ -11,6 +11,8 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <numeric>
+#include <random>
 #include <string>
 #include <vector>
 
@@ -70,6 +72,11 @@ enum Slot {
     S_ST_STATS,  // Stouffer: row means and standard deviations
     S_ST_A,      // Stouffer ensemble: the combo matrix
     S_ST_B,      // Stouffer ensemble: its transform
+    S_SP_VAL,    // split evaluation: the entries' scores (up to four sources) in mask order
+    S_SP_LAB,    // split evaluation: the entries' labels
+    S_SP_PERM,   // split evaluation: the shuffled entry order
+    S_SP_CNT,    // split evaluation: subset counters
+    S_SP_ST,     // split evaluation: Stouffer scores of every coefficient row at the entries
     NSLOTS
 };
 
@@ -1640,6 +1647,311 @@ int combo_stouffer_eval_dev(mcpg_handle* h, const float* const mats[4], const in
     return MCPG_OK;
 }
 
+// ---------------- semi-supervised split evaluation (eval_mcpnet) ----------------
+// The labelled entries of a region in the reference's mask order -- row-major,
+// as select_lower_triangle, the sorted mask of select_from_list
+// (mcpnet_helper.hpp:818-826) and select_tfs_from_mat produce it -- with their
+// scores from up to four sources (vals[k], null where src[k] is null) and labels.
+struct SplitEntries {
+    const float* vals[4] = {};
+    const int8_t* lab = nullptr;
+    const uint64_t* off = nullptr;  // scanned per-item entry counts (for later gathers)
+    int64_t E = 0;
+};
+
+int split_entries(mcpg_handle* h, const mcpg::TruthRegion& r, const float* const src[4], const int64_t lds[4],
+                  SplitEntries& se, int* flag) {
+    const int64_t items = mcpg::truth_items(r);
+    void *cnt, *off, *tmp;
+    int rc;
+    if ((rc = scratch(h, S_EV_CNT, (size_t)(2 * items + 1) * 4, &cnt))) return rc;
+    if ((rc = scratch(h, S_EV_OFF, (size_t)(items + 1) * 8, &off))) return rc;
+    if ((rc = scratch(h, S_EV_TMP, (size_t)mcpg::scan_tmp_elems(items) * 8, &tmp))) return rc;
+    uint32_t* cp = (uint32_t*)cnt;
+    uint32_t* cn = cp + items;
+    uint64_t tot = 0;
+    if (items > 0) {
+        PROF(h, "truth_count");
+        CK(h, mcpg::launch_truth_count(r, cp, cn, h->stream, &h->launches), "truth count");
+        CK(h, mcpg::launch_add_u32(cp, cn, items, cp, h->stream, &h->launches), "add");
+        CK(h, mcpg::launch_scan_u32(cp, items, (uint64_t*)off, (uint64_t*)tmp, h->stream, &h->launches), "scan");
+        CK(h, cudaMemcpyAsync(&tot, (uint64_t*)off + items, 8, cudaMemcpyDeviceToHost, h->stream),
+           "device-to-host copy");
+        CK(h, cudaStreamSynchronize(h->stream), "stream synchronize");
+    }
+    const int64_t E = (int64_t)tot;
+    if (E >= ((int64_t)1 << 32)) return fail(h, MCPG_ERR_UNSUPPORTED, "split evaluation: 2^32 or more labelled entries");
+    int nsrc = 0;
+    for (int k = 0; k < 4; ++k) nsrc += src[k] != nullptr;
+    void *val, *lab;
+    if ((rc = scratch(h, S_SP_VAL, (size_t)(nsrc > 0 ? nsrc : 1) * (size_t)(E > 0 ? E : 1) * 4, &val))) return rc;
+    if ((rc = scratch(h, S_SP_LAB, (size_t)(E > 0 ? E : 1), &lab))) return rc;
+    mcpg::GatherSrc g{};
+    for (int k = 0; k < 4; ++k) {
+        se.vals[k] = nullptr;
+        if (!src[k]) continue;
+        float* d = (float*)val + (size_t)g.n * (size_t)E;
+        se.vals[k] = d;
+        g.src[g.n] = src[k];
+        g.lds[g.n] = lds[k];
+        g.dst[g.n] = d;
+        ++g.n;
+    }
+    g.lab_dst = (int8_t*)lab;
+    se.lab = (const int8_t*)lab;
+    se.off = (const uint64_t*)off;
+    se.E = E;
+    if (E > 0) {
+        PROF(h, "truth_gather");
+        CK(h, mcpg::launch_truth_gather(r, -1, (const uint64_t*)off, g, flag, h->stream, &h->launches),
+           "truth gather");
+    }
+    return MCPG_OK;
+}
+
+// shuffle_truth (apps/pipeline/eval_mcpnet.cpp:214-224): std::shuffle with a
+// std::mt19937 seeded with `seed` over the E mask entries.  std::shuffle's swaps
+// depend only on the length and the generator, so the shuffled entry positions
+// are the reference's order of its (row, col, label) tuples.  seed 0 keeps the
+// mask order.  hp is host work space.
+int split_perm(mcpg_handle* h, int64_t E, uint64_t seed, std::vector<uint32_t>& hp, uint32_t* dperm) {
+    hp.resize((size_t)E);
+    std::iota(hp.begin(), hp.end(), 0u);
+    if (seed) {
+        std::mt19937 g((std::mt19937::result_type)seed);
+        std::shuffle(hp.begin(), hp.end(), g);
+    }
+    if (E > 0)
+        CK(h, cudaMemcpyAsync(dperm, hp.data(), (size_t)E * 4, cudaMemcpyHostToDevice, h->stream),
+           "host-to-device copy");
+    return MCPG_OK;
+}
+
+// compute_aupr2 (mcpnet_helper.hpp:1017-1035) over the shuffled entries
+// perm[a..b): their scores (vals, or the combo of *c) split by label into
+// positive and negative keys, then the AUPR of aupr_kernel.
+int split_aupr_range(mcpg_handle* h, const EvalWs& w, const SplitEntries& se, const uint32_t* perm, int64_t a,
+                     int64_t b, const float* vals, const mcpg::ComboSrc* c, double* aupr) {
+    void *kp, *kn, *cnt;
+    int rc;
+    const size_t cap = (size_t)(se.E > 0 ? se.E : 1) * 4;  // sized once for every range
+    if ((rc = scratch(h, S_EV_KP, cap, &kp))) return rc;
+    if ((rc = scratch(h, S_EV_KN, cap, &kn))) return rc;
+    if ((rc = scratch(h, S_SP_CNT, 16, &cnt))) return rc;
+    CK(h, cudaMemsetAsync(cnt, 0, 16, h->stream), "memset");
+    const mcpg::ComboSrc none{};
+    {
+        PROF(h, "split_keys");
+        CK(h, mcpg::launch_split_keys(perm, a, b, vals, c ? *c : none, c != nullptr, se.lab, (uint32_t*)kp,
+                                      (uint32_t*)kn, (unsigned long long*)cnt, w.flag, h->stream, &h->launches),
+           "split keys");
+    }
+    unsigned long long n[2] = {0, 0};
+    CK(h, cudaMemcpyAsync(n, cnt, 16, cudaMemcpyDeviceToHost, h->stream), "device-to-host copy");
+    CK(h, cudaStreamSynchronize(h->stream), "stream synchronize");
+    const int64_t P = (int64_t)n[0], N = (int64_t)n[1];
+    uint32_t* knk = (uint32_t*)kn;
+    double roc = 0.0;
+    return ev_aupr_auroc(
+        h, w, (uint32_t*)kp, P, N,
+        [&](const uint32_t* X, int64_t nX, uint64_t* lt, uint64_t* eq) {
+            return mcpg::launch_rank_count_keys(X, nX, knk, N, lt, eq, h->stream, &h->launches);
+        },
+        [&](uint32_t** out) {
+            *out = knk;
+            return MCPG_OK;
+        },
+        aupr, &roc);
+}
+
+int split_check(mcpg_handle* h, const char* who, int64_t iters, const int64_t* tc, int64_t parts, int64_t E) {
+    if (iters < 0 || parts < 0) return fail(h, MCPG_ERR_ARG, "%s: negative iteration or part count", who);
+    if (parts > 0 && !tc) return fail(h, MCPG_ERR_ARG, "%s: null train counts", who);
+    for (int64_t j = 0; j < parts; ++j)
+        if (tc[j] < 0 || tc[j] > E)
+            return fail(h, MCPG_ERR_ARG, "%s: train count %lld outside 0..%lld labelled entries", who,
+                        (long long)tc[j], (long long)E);
+    return MCPG_OK;
+}
+
+// eval_aupr_mcp (apps/pipeline/eval_mcpnet.cpp:227-301): the AUPR of all
+// labelled entries, then for iterations i = 1..iters the entries shuffled with
+// seed i and, per train count k, the AUPR of the first k (train) and of the
+// rest (test).  train / test: iters x parts, row-major.
+int split_aupr_dev(mcpg_handle* h, const float* values, int64_t ldv, const mcpg::TruthRegion& r, int64_t iters,
+                   const int64_t* tc, int64_t parts, double* full, double* train, double* test) {
+    if (r.rows > 0 && r.cols > 0 && (!values || ldv < r.cols))
+        return fail(h, MCPG_ERR_ARG, "split_aupr: null values or leading dimension too small");
+    EvalWs w;
+    int rc;
+    if ((rc = ev_ws(h, w))) return rc;
+    SplitEntries se;
+    const float* src[4] = {values, nullptr, nullptr, nullptr};
+    const int64_t lds[4] = {ldv, 0, 0, 0};
+    if ((rc = split_entries(h, r, src, lds, se, w.flag))) return rc;
+    if ((rc = split_check(h, "split_aupr", iters, tc, parts, se.E))) return rc;
+    void* perm;
+    if ((rc = scratch(h, S_SP_PERM, (size_t)(se.E > 0 ? se.E : 1) * 4, &perm))) return rc;
+    std::vector<uint32_t> hp;
+    const uint32_t* dp = (const uint32_t*)perm;
+    if ((rc = split_perm(h, se.E, 0, hp, (uint32_t*)perm))) return rc;
+    double a = 0.0;
+    if ((rc = split_aupr_range(h, w, se, dp, 0, se.E, se.vals[0], nullptr, &a))) return rc;
+    if (full) *full = a;
+    for (int64_t i = 1; i <= iters; ++i) {
+        if ((rc = split_perm(h, se.E, (uint64_t)i, hp, (uint32_t*)perm))) return rc;
+        for (int64_t j = 0; j < parts; ++j) {
+            double tr = 0.0, te = 0.0;
+            if ((rc = split_aupr_range(h, w, se, dp, 0, tc[j], se.vals[0], nullptr, &tr))) return rc;
+            if ((rc = split_aupr_range(h, w, se, dp, tc[j], se.E, se.vals[0], nullptr, &te))) return rc;
+            if (train) train[(i - 1) * parts + j] = tr;
+            if (test) test[(i - 1) * parts + j] = te;
+        }
+    }
+    return MCPG_OK;
+}
+
+// eval_combos over the shuffled splits (apps/pipeline/eval_mcpnet.cpp:319-462,
+// 814-893): per iteration i (seed i) and train count k, the coefficient row of
+// highest AUPR on the first k entries (the first strictly larger, row 0 when
+// none is), its AUPR on the rest and on all entries, and the same for the
+// Stouffer-transformed combos (stouffer: MCPG_STOUFFER_NONE, a row-statistics
+// mode for square matrices, or MCPG_STOUFFER_TF).  Rows (1, 0, 0, 0) are
+// skipped.  res: iters x parts x 6 (train, test, Stouffer train, Stouffer test,
+// full, Stouffer full; Stouffer values 0 without it); best: iters x parts x 2.
+// The scores of every row at the entries do not depend on the split: the
+// combos are formed from the gathered matrices on the fly, the Stouffer scores
+// (a full matrix transform per row) once per row and kept.
+int split_combo_dev(mcpg_handle* h, const float* const mats[4], const int64_t lds[4], const mcpg::TruthRegion& r,
+                    const double* coeffs, int64_t nc, int stouffer, int64_t iters, const int64_t* tc, int64_t parts,
+                    double* res, int64_t* best) {
+    const int64_t rows = r.rows, cols = r.cols;
+    if (nc < 1 || !coeffs) return fail(h, MCPG_ERR_ARG, "split_combo_eval: need at least one coefficient row");
+    if (stouffer != MCPG_STOUFFER_NONE && stouffer != MCPG_ROWSTATS_ALL && stouffer != MCPG_ROWSTATS_EXCLUDE_DIAGONAL &&
+        stouffer != MCPG_STOUFFER_TF)
+        return fail(h, MCPG_ERR_ARG, "split_combo_eval: unknown Stouffer mode %d", stouffer);
+    if ((stouffer == MCPG_ROWSTATS_ALL || stouffer == MCPG_ROWSTATS_EXCLUDE_DIAGONAL) && rows != cols)
+        return fail(h, MCPG_ERR_ARG, "split_combo_eval: the square Stouffer transform needs square matrices");
+    if (rows > 0 && cols > 0) {
+        if (!mats[0] || lds[0] < cols) return fail(h, MCPG_ERR_ARG, "split_combo_eval: null mi or leading dimension");
+        for (int k = 1; k < 4; ++k) {
+            if (mats[k] && lds[k] < cols) return fail(h, MCPG_ERR_ARG, "split_combo_eval: leading dimension too small");
+            for (int64_t c = 0; c < nc; ++c)
+                if (!mats[k] && coeffs[4 * c + k] != 0.0)
+                    return fail(h, MCPG_ERR_ARG, "split_combo_eval: coefficient row %lld uses a null matrix",
+                                (long long)c);
+        }
+    }
+    EvalWs w;
+    int rc;
+    if ((rc = ev_ws(h, w))) return rc;
+    SplitEntries se;
+    if ((rc = split_entries(h, r, mats, lds, se, w.flag))) return rc;
+    if ((rc = split_check(h, "split_combo_eval", iters, tc, parts, se.E))) return rc;
+    const int64_t E = se.E;
+    auto combo_src = [&](int64_t c) {
+        mcpg::ComboSrc s{};
+        for (int k = 0; k < 4; ++k) {
+            s.g[k] = se.vals[k];
+            s.cs[k] = coeffs[4 * c + k];
+        }
+        s.kc = mcpg::make_combo_coef(coeffs + 4 * c);
+        s.n = E;
+        return s;
+    };
+    auto skipped = [&](int64_t c) {
+        const double* cs = coeffs + 4 * c;
+        return cs[0] == 1.0 && cs[1] == 0.0 && cs[2] == 0.0 && cs[3] == 0.0;  // mcpnet.cpp:589
+    };
+    const bool with_st = stouffer != MCPG_STOUFFER_NONE;
+    float* st = nullptr;  // Stouffer scores of row c at the entries: st + c * E
+    if (with_st && E > 0) {
+        void* p;
+        if ((rc = scratch(h, S_SP_ST, (size_t)nc * (size_t)E * 4, &p))) return rc;
+        st = (float*)p;
+        float *cm = nullptr, *tm = nullptr;
+        int64_t ldc = 0;
+        if ((rc = stage_out_alloc(h, S_ST_A, rows, cols, &cm, &ldc))) return rc;
+        if ((rc = stage_out_alloc(h, S_ST_B, rows, cols, &tm, &ldc))) return rc;
+        for (int64_t c = 0; c < nc; ++c) {
+            {
+                PROF(h, "combo");
+                CK(h, mcpg::launch_combo(mats[0], lds[0], mats[1], lds[1], mats[2], lds[2], mats[3], lds[3], rows,
+                                         cols, coeffs + 4 * c, cm, ldc, h->stream, &h->launches),
+                   "combo kernel");
+            }
+            rc = stouffer == MCPG_STOUFFER_TF
+                     ? stouffer_tf_dev(h, cm, rows, cols, ldc, tm, ldc)
+                     : transform_dev(h, cm, rows, ldc, MCPG_TRANSFORM_STOUFFER, stouffer, tm, ldc);
+            if (rc) return rc;
+            mcpg::GatherSrc g{};
+            g.n = 1;
+            g.src[0] = tm;
+            g.lds[0] = ldc;
+            g.dst[0] = st + (size_t)c * (size_t)E;
+            PROF(h, "truth_gather");
+            CK(h, mcpg::launch_truth_gather(r, -1, se.off, g, w.flag, h->stream, &h->launches), "truth gather");
+        }
+    }
+    void* perm;
+    if ((rc = scratch(h, S_SP_PERM, (size_t)(E > 0 ? E : 1) * 4, &perm))) return rc;
+    const uint32_t* dp = (const uint32_t*)perm;
+    std::vector<uint32_t> hp;
+    // AUPR of every row over all entries (the split does not change it)
+    if ((rc = split_perm(h, E, 0, hp, (uint32_t*)perm))) return rc;
+    std::vector<double> full_p((size_t)nc, 0.0), full_s((size_t)nc, 0.0);
+    for (int64_t c = 0; c < nc; ++c) {
+        const mcpg::ComboSrc cs = combo_src(c);
+        if ((rc = split_aupr_range(h, w, se, dp, 0, E, nullptr, &cs, &full_p[(size_t)c]))) return rc;
+        if (with_st && (rc = split_aupr_range(h, w, se, dp, 0, E, st + (size_t)c * (size_t)E, nullptr,
+                                              &full_s[(size_t)c])))
+            return rc;
+    }
+    for (int64_t i = 1; i <= iters; ++i) {
+        if ((rc = split_perm(h, E, (uint64_t)i, hp, (uint32_t*)perm))) return rc;
+        for (int64_t j = 0; j < parts; ++j) {
+            const int64_t k = tc[j];
+            double max_p = 0.0, max_s = 0.0, a = 0.0;
+            int64_t co = 0, sco = 0;
+            for (int64_t c = 0; c < nc; ++c) {
+                if (skipped(c)) continue;
+                const mcpg::ComboSrc cs = combo_src(c);
+                if ((rc = split_aupr_range(h, w, se, dp, 0, k, nullptr, &cs, &a))) return rc;
+                if (a > max_p) {  // eval_mcpnet.cpp:370-373
+                    max_p = a;
+                    co = c;
+                }
+                if (!with_st) continue;
+                if ((rc = split_aupr_range(h, w, se, dp, 0, k, st + (size_t)c * (size_t)E, nullptr, &a))) return rc;
+                if (a > max_s) {
+                    max_s = a;
+                    sco = c;
+                }
+            }
+            double test_p = 0.0, test_s = 0.0;
+            const mcpg::ComboSrc cs = combo_src(co);
+            if ((rc = split_aupr_range(h, w, se, dp, k, E, nullptr, &cs, &test_p))) return rc;
+            if (with_st &&
+                (rc = split_aupr_range(h, w, se, dp, k, E, st + (size_t)sco * (size_t)E, nullptr, &test_s)))
+                return rc;
+            double* o = res ? res + ((i - 1) * parts + j) * 6 : nullptr;
+            if (o) {
+                o[0] = max_p;
+                o[1] = test_p;
+                o[2] = with_st ? max_s : 0.0;
+                o[3] = with_st ? test_s : 0.0;
+                o[4] = full_p[(size_t)co];
+                o[5] = with_st ? full_s[(size_t)sco] : 0.0;
+            }
+            if (best) {
+                best[((i - 1) * parts + j) * 2] = co;
+                best[((i - 1) * parts + j) * 2 + 1] = with_st ? sco : 0;
+            }
+        }
+    }
+    return MCPG_OK;
+}
+
 // Host inputs of the coefficient searches (mi, M1..M3, labels and the TF
 // region's row_gene / col_tf) copied to the device; r gets the device region.
 int stage_search(mcpg_handle* h, const char* name, const float* const src[4], const int64_t lds[4], int64_t rows,
@@ -2698,6 +3010,67 @@ int mcpg_combo_stouffer_tf_eval(mcpg_handle* h, const float* mi, int64_t ldm, co
                            d, dl, &r)))
         return rc;
     return combo_stouffer_eval_dev(h, d, dl, r, coeffs, n_coeffs, ST_TF, aupr, auroc, best);
+}
+
+int mcpg_split_aupr_dev(mcpg_handle* h, const float* values, int64_t rows, int64_t cols, int64_t ldv,
+                        const int8_t* labels, int64_t ldl, int region, const int32_t* row_gene, const uint8_t* col_tf,
+                        int64_t iterations, const int64_t* train_counts, int64_t parts, double* full_aupr,
+                        double* train_aupr, double* test_aupr) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    mcpg::TruthRegion r{};
+    if ((rc = truth_region(h, "split_aupr", labels, rows, cols, ldl, region, row_gene, col_tf, &r))) return rc;
+    return split_aupr_dev(h, values, ldv, r, iterations, train_counts, parts, full_aupr, train_aupr, test_aupr);
+}
+
+int mcpg_split_aupr(mcpg_handle* h, const float* values, int64_t rows, int64_t cols, int64_t ldv,
+                    const int8_t* labels, int64_t ldl, int region, const int32_t* row_gene, const uint8_t* col_tf,
+                    int64_t iterations, const int64_t* train_counts, int64_t parts, double* full_aupr,
+                    double* train_aupr, double* test_aupr) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    const float* src[4] = {values, nullptr, nullptr, nullptr};
+    const int64_t lds[4] = {ldv, 0, 0, 0};
+    const float* d[4];
+    int64_t dl[4];
+    mcpg::TruthRegion r{};
+    if ((rc = stage_search(h, "split_aupr", src, lds, rows, cols, labels, ldl, region, row_gene, col_tf, d, dl, &r)))
+        return rc;
+    return split_aupr_dev(h, d[0], dl[0], r, iterations, train_counts, parts, full_aupr, train_aupr, test_aupr);
+}
+
+int mcpg_split_combo_eval_dev(mcpg_handle* h, const float* mi, int64_t ldm, const float* M1, int64_t ld1,
+                              const float* M2, int64_t ld2, const float* M3, int64_t ld3, int64_t rows, int64_t cols,
+                              const int8_t* labels, int64_t ldl, int region, const int32_t* row_gene,
+                              const uint8_t* col_tf, const double* coeffs, int64_t n_coeffs, int stouffer,
+                              int64_t iterations, const int64_t* train_counts, int64_t parts, double* results,
+                              int64_t* best) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    mcpg::TruthRegion r{};
+    if ((rc = truth_region(h, "split_combo_eval", labels, rows, cols, ldl, region, row_gene, col_tf, &r))) return rc;
+    const float* mats[4] = {mi, M1, M2, M3};
+    const int64_t lds[4] = {ldm, ld1, ld2, ld3};
+    return split_combo_dev(h, mats, lds, r, coeffs, n_coeffs, stouffer, iterations, train_counts, parts, results,
+                           best);
+}
+
+int mcpg_split_combo_eval(mcpg_handle* h, const float* mi, int64_t ldm, const float* M1, int64_t ld1, const float* M2,
+                          int64_t ld2, const float* M3, int64_t ld3, int64_t rows, int64_t cols, const int8_t* labels,
+                          int64_t ldl, int region, const int32_t* row_gene, const uint8_t* col_tf,
+                          const double* coeffs, int64_t n_coeffs, int stouffer, int64_t iterations,
+                          const int64_t* train_counts, int64_t parts, double* results, int64_t* best) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    const float* src[4] = {mi, M1, M2, M3};
+    const int64_t lds[4] = {ldm, ld1, ld2, ld3};
+    const float* d[4];
+    int64_t dl[4];
+    mcpg::TruthRegion r{};
+    if ((rc = stage_search(h, "split_combo_eval", src, lds, rows, cols, labels, ldl, region, row_gene, col_tf, d, dl,
+                           &r)))
+        return rc;
+    return split_combo_dev(h, d, dl, r, coeffs, n_coeffs, stouffer, iterations, train_counts, parts, results, best);
 }
 
 int mcpg_stouffer_tf_stats_dev(mcpg_handle* h, const float* A, int64_t rows, int64_t cols, int64_t lda,

@@ -232,7 +232,8 @@ __global__ void __launch_bounds__(EV_THREADS) truth_gather_kernel(TruthRegion r,
         bool bad = false;
         for (int k = 0; k < EV_PER_THREAD; ++k) {
             const int64_t col = s.c0 + k * EV_THREADS + threadIdx.x;
-            const bool sel = col < s.c1 && in_region(r, s.row, col) && lrow[col] == lab;
+            const int8_t l = (col < s.c1 && in_region(r, s.row, col)) ? lrow[col] : (int8_t)-1;
+            const bool sel = lab < 0 ? (l == 0 || l == 1) : (l == lab);
             const uint32_t b = __ballot_sync(FULL, sel);
             if (lane == 0) swarp[w] = __popc(b);
             __syncthreads();
@@ -250,6 +251,7 @@ __global__ void __launch_bounds__(EV_THREADS) truth_gather_kernel(TruthRegion r,
                     bad |= is_nan(v);
                     g.dst[q][p] = v;
                 }
+                if (g.lab_dst) g.lab_dst[p] = l;
             }
             pos += tot;
             __syncthreads();
@@ -557,6 +559,46 @@ struct Neu {  // Neumaier compensated sum
     }
 };
 
+__global__ void add_u32_kernel(const uint32_t* a, const uint32_t* b, int64_t n, uint32_t* out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = a[i] + b[i];
+}
+
+// Warps take 32 consecutive positions of [a, b) (the loop bound is uniform over
+// a warp), ballot the positives and negatives and append them with one atomic
+// per warp and label.
+__global__ void split_keys_kernel(const uint32_t* perm, int64_t a, int64_t b, const float* vals, ComboSrc c, int combo,
+                                  const int8_t* lab, uint32_t* kp, uint32_t* kn, unsigned long long* cnt,
+                                  int* nan_flag) {
+    const int lane = threadIdx.x & 31;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    bool bad = false;
+    for (int64_t p0 = a + blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); p0 < b; p0 += stride) {
+        const int64_t p = p0 + lane;
+        int8_t l = -1;
+        float v = 0.0f;
+        if (p < b) {
+            const int64_t e = perm[p];
+            l = lab[e];
+            v = combo ? combo_at(c, e) : vals[e];
+        }
+        const bool isp = l == 1, isn = l == 0;
+        bad |= (isp || isn) && is_nan(v);
+        const uint32_t bp = __ballot_sync(FULL, isp), bn = __ballot_sync(FULL, isn);
+        unsigned long long basep = 0, basen = 0;
+        if (lane == 0) {
+            if (bp) basep = atomicAdd(&cnt[0], (unsigned long long)__popc(bp));
+            if (bn) basen = atomicAdd(&cnt[1], (unsigned long long)__popc(bn));
+        }
+        basep = __shfl_sync(FULL, basep, 0);
+        basen = __shfl_sync(FULL, basen, 0);
+        const uint32_t below = lanemask_lt();
+        if (isp) kp[basep + __popc(bp & below)] = order_key(v);
+        if (isn) kn[basen + __popc(bn & below)] = order_key(v);
+    }
+    if (bad) atomicOr(nan_flag, 1);
+}
+
 __global__ void add_u64_kernel(const uint64_t* a, const uint64_t* b, int64_t n, uint64_t* out) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         out[i] = a[i] + b[i];
@@ -669,6 +711,24 @@ cudaError_t launch_truth_gather(const TruthRegion& r, int lab, const uint64_t* o
     if (items == 0) return cudaSuccess;
     truth_gather_kernel<<<grid_for(items, 1, 152 * 16), EV_THREADS, 0, st>>>(r, ceil_div(r.cols, EV_CHUNK), items,
                                                                              lab, off, g, nan_flag);
+    if (launches) ++*launches;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_add_u32(const uint32_t* a, const uint32_t* b, int64_t n, uint32_t* out, cudaStream_t st,
+                           int64_t* launches) {
+    if (n <= 0) return cudaSuccess;
+    add_u32_kernel<<<grid_for(n, 256, 152 * 8), 256, 0, st>>>(a, b, n, out);
+    if (launches) ++*launches;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_split_keys(const uint32_t* perm, int64_t a, int64_t b, const float* vals, const ComboSrc& c,
+                              int combo, const int8_t* lab, uint32_t* kp, uint32_t* kn, unsigned long long* cnt,
+                              int* nan_flag, cudaStream_t st, int64_t* launches) {
+    if (b <= a) return cudaSuccess;
+    split_keys_kernel<<<grid_for(b - a, 256, 152 * 16), 256, 0, st>>>(perm, a, b, vals, c, combo, lab, kp, kn, cnt,
+                                                                     nan_flag);
     if (launches) ++*launches;
     return cudaGetLastError();
 }

@@ -133,6 +133,7 @@ struct GatherSrc {                       // up to four matrices gathered at the 
     int n;
     const float* src[4]; int64_t lds[4];
     float* dst[4];
+    int8_t* lab_dst;                     // nullable: the entries' labels (for lab < 0)
 };
 // compute_combo coefficients prepared once per launch: kind 0 = skipped (0),
 // 1 = added as is (1), 2 = scaled; hi + lo = the double coefficient to 2^-48.
@@ -170,10 +171,21 @@ cudaError_t launch_truth_count(const TruthRegion& r, uint32_t* cpos, uint32_t* c
 // out[0..n) = exclusive prefix sum of in, out[n] = total (tmp: scan_tmp_elems(n)).
 cudaError_t launch_scan_u32(const uint32_t* in, int64_t n, uint64_t* out, uint64_t* tmp, cudaStream_t stream,
                             int64_t* launches);
-// Writes, in row-major order, every selected entry labelled `lab` of the g.n
+// Writes, in row-major order, every selected entry labelled `lab` (lab < 0: every
+// entry labelled 0 or 1, with its label to g.lab_dst when given) of the g.n
 // sources to g.dst at positions off[item] + rank (off: scanned per-item counts).
 cudaError_t launch_truth_gather(const TruthRegion& r, int lab, const uint64_t* off, const GatherSrc& g, int* nan_flag,
                                 cudaStream_t stream, int64_t* launches);
+// out[i] = a[i] + b[i].
+cudaError_t launch_add_u32(const uint32_t* a, const uint32_t* b, int64_t n, uint32_t* out, cudaStream_t stream,
+                           int64_t* launches);
+// Entries perm[a..b) of mask-order entry arrays: the score (vals[e], or with
+// combo the compute_combo value of c at e) as an order key into kp (label 1) or
+// kn (label 0), compacted in no particular order; cnt[0] / cnt[1] (zeroed by the
+// caller) count them.  NaN sets *nan_flag.
+cudaError_t launch_split_keys(const uint32_t* perm, int64_t a, int64_t b, const float* vals, const ComboSrc& c,
+                              int combo, const int8_t* lab, uint32_t* kp, uint32_t* kn, unsigned long long* cnt,
+                              int* nan_flag, cudaStream_t stream, int64_t* launches);
 // Order-preserving 32-bit keys of float scores (-0 as +0); NaN sets *nan_flag.
 cudaError_t launch_keys_from_floats(const float* v, int64_t n, uint32_t* keys, int* nan_flag, cudaStream_t stream,
                                     int64_t* launches);

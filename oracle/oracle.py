@@ -138,6 +138,81 @@ class _EvalCompositions:
                 top, best = pr[i], i
         return pr, roc, best
 
+    @staticmethod
+    def mask_entries(values, labels, region="lower", row_gene=None, col_tf=None):
+        """The labelled entries (label 0 or 1) of the region in row-major order -- the reference's
+        mask order (select_lower_triangle; select_from_list, whose mask is sorted by row and column,
+        apps/pipeline/mcpnet_helper.hpp:818-826; select_tfs_from_mat) -- as (scores, labels)."""
+        V = np.asarray(values)
+        L = np.asarray(labels)
+        rows, cols = L.shape
+        i = np.arange(rows)[:, None]
+        j = np.arange(cols)[None, :]
+        keep = (L == 0) | (L == 1)
+        if region == "lower":
+            keep &= j < i
+        elif region == "tf":
+            g = np.asarray(row_gene, dtype=np.int64)[:, None]
+            keep &= (j != g) & ~((g > j) & (np.asarray(col_tf)[None, :] != 0))
+        idx = np.flatnonzero(keep)
+        return np.ascontiguousarray(V.reshape(rows, -1)[:, :cols].ravel()[idx]), L.ravel()[idx]
+
+    def _aupr_of(self, v, l):
+        return self.aupr_auroc(v[l == 1], v[l == 0])[0]
+
+    def split_aupr(self, values, labels, iterations, train_counts, region="lower", row_gene=None, col_tf=None):
+        """eval_aupr_mcp (apps/pipeline/eval_mcpnet.cpp:227-301): (full, train[iters, parts], test[iters, parts])."""
+        v, l = self.mask_entries(values, labels, region, row_gene, col_tf)
+        full = self._aupr_of(v, l)
+        tr = np.zeros((iterations, len(train_counts)))
+        te = np.zeros_like(tr)
+        for i in range(1, iterations + 1):
+            perm = port().shuffle_perm(v.size, i)
+            for jx, k in enumerate(train_counts):
+                a, b = perm[:k], perm[k:]
+                tr[i - 1, jx] = self._aupr_of(v[a], l[a])
+                te[i - 1, jx] = self._aupr_of(v[b], l[b])
+        return full, tr, te
+
+    def split_combo_eval(self, mi, M1, M2, M3, labels, coeffs, iterations, train_counts, stouffer_mats=None,
+                         region="lower", row_gene=None, col_tf=None):
+        """eval_combos over the shuffled splits (apps/pipeline/eval_mcpnet.cpp:319-462, 814-893):
+        results[iters, parts, 6] (train, test, Stouffer train, Stouffer test, full, Stouffer full) and
+        best[iters, parts, 2].  stouffer_mats: the Stouffer transform of every row's combo matrix, or None."""
+        cs = np.asarray(coeffs, dtype=np.float64).reshape(-1, 4)
+        P = port()
+        _, lab = self.mask_entries(mi, labels, region, row_gene, col_tf)
+        ent = [self.mask_entries(P.combo(mi, M1, M2, M3, c), labels, region, row_gene, col_tf)[0] for c in cs]
+        st = None if stouffer_mats is None else \
+            [self.mask_entries(S, labels, region, row_gene, col_tf)[0] for S in stouffer_mats]
+        full_p = [self._aupr_of(e, lab) for e in ent]
+        full_s = [self._aupr_of(e, lab) for e in st] if st is not None else None
+        skip = [c[0] == 1 and c[1] == 0 and c[2] == 0 and c[3] == 0 for c in cs]
+        res = np.zeros((iterations, len(train_counts), 6))
+        best = np.zeros((iterations, len(train_counts), 2), dtype=np.int64)
+        for i in range(1, iterations + 1):
+            perm = P.shuffle_perm(lab.size, i)
+            for jx, k in enumerate(train_counts):
+                tr, te = perm[:k], perm[k:]
+                mp = ms = 0.0
+                co = sco = 0
+                for c in range(len(cs)):
+                    if skip[c]:
+                        continue
+                    a = self._aupr_of(ent[c][tr], lab[tr])
+                    if a > mp:
+                        mp, co = a, c
+                    if st is not None:
+                        a = self._aupr_of(st[c][tr], lab[tr])
+                        if a > ms:
+                            ms, sco = a, c
+                r = res[i - 1, jx]
+                r[0], r[1], r[4] = mp, self._aupr_of(ent[co][te], lab[te]), full_p[co]
+                if st is not None:
+                    r[2], r[3], r[5] = ms, self._aupr_of(st[sco][te], lab[te]), full_s[sco]
+                best[i - 1, jx] = (co, sco)
+        return res, best
+
     def combo_stouffer_tf_eval(self, mi, M1, M2, M3, labels, coeffs, region="tf", row_gene=None, col_tf=None):
         """The TF Stouffer half of the loop (apps/pipeline/mcpnet.cpp:622-661 with --tf-input)."""
         cs = np.asarray(coeffs, dtype=np.float64).reshape(-1, 4)
@@ -171,6 +246,8 @@ class _Port(_TfCompositions, _EvalCompositions):
         self.L.orc_ranks_desc.argtypes = [_vp, _i64, _i64, _i64, _vp]
         self.L.orc_row_stats.argtypes = [_vp, _i64, _i64, _i64, C.c_int, _vp, _vp]
         self.L.orc_transform.argtypes = [_vp, _i64, _i64, _vp, _vp, C.c_int, _vp, _i64]
+        self.L.orc_shuffle_u32.argtypes = [_vp, _i64, C.c_uint32]
+        self.L.orc_shuffle_tuples.argtypes = [_i64, C.c_uint32, _vp]
         self.L.orc_row_stats_pop.argtypes = [_vp, _i64, _i64, _i64, _vp, _vp]
         self.L.orc_col_stats.argtypes = [_vp, _i64, _i64, _i64, _vp, _vp]
         self.L.orc_stouffer_tf.argtypes = [_vp, _i64, _i64, _i64, _vp, _vp, _vp, _vp, C.c_int, _vp, _i64, _vp, _vp]
@@ -340,6 +417,18 @@ class _Port(_TfCompositions, _EvalCompositions):
     def transform(self, A, clr=False, mode="exclude_diagonal"):
         mean, sd = self.row_stats(A, mode)
         return self.transform_with_stats(A, mean, sd, clr)
+
+    def shuffle_perm(self, n, seed):
+        """shuffle_truth's order of n mask entries for `seed` (std::shuffle, std::mt19937) as positions."""
+        a = np.empty(n, dtype=np.uint32)
+        self.L.orc_shuffle_u32(a.ctypes.data, n, seed)
+        return a.astype(np.int64)
+
+    def shuffle_tuples_order(self, n, seed):
+        """The same shuffle applied to the reference's (size_t, size_t, int) mask tuples."""
+        out = np.empty(n, dtype=np.int64)
+        self.L.orc_shuffle_tuples(n, seed, out.ctypes.data)
+        return out
 
     def tf_stats(self, A):
         """Population row and column statistics of a t x n matrix, FP64 rounded to float (stand in for

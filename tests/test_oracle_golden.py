@@ -302,3 +302,38 @@ def test_tf_searches_oracle(port, golden):
     np.testing.assert_array_equal(pr, g["st_aupr"])
     np.testing.assert_array_equal(roc, g["st_auroc"])
     assert best == int(g["st_best"])
+
+
+@pytest.mark.parametrize("n,seed", [(1, 1), (2, 1), (3, 2), (1000, 7), (100000, 3), (65536, 100)])
+def test_shuffle_positions_match_reference_tuples(port, n, seed):
+    """shuffle_truth (apps/pipeline/eval_mcpnet.cpp:214-224) shuffles (size_t, size_t, int)
+    tuples; std::shuffle's swaps depend only on the length and the std::mt19937, so the
+    shuffled positions used by the split evaluation give the same order."""
+    a = port.shuffle_perm(n, seed)
+    assert np.array_equal(a, port.shuffle_tuples_order(n, seed))
+    assert np.array_equal(np.sort(a), np.arange(n))
+
+
+def test_mask_entries_match_select_truth(port, golden):
+    """The mask order (row-major labelled entries of the region) restated in numpy
+    selects exactly the oracle's select_values2 vectors."""
+    g = golden("eval_truth")
+    A, L = g["A"], g["labels"]
+    ti, ct = g["tf_idx"], g["col_tf"]
+    for region, V, Lb, rg, c in (("lower", A, L, None, None), ("all", A, L, None, None),
+                                  ("tf", A[ti], L[ti], ti, ct)):
+        v, l = port.mask_entries(V, Lb, region, rg, c)
+        pos, neg = port.select_truth(V, Lb, region, rg, c)
+        assert np.array_equal(v[l == 1], pos) and np.array_equal(v[l == 0], neg), region
+
+
+def test_split_aupr_composition_edges(port, golden):
+    """A train part holding every entry reproduces the full AUPR and leaves an empty
+    test part (AUPR 0); an empty train part has AUPR 0."""
+    g = golden("eval_truth")
+    A, L = g["A"], g["labels"]
+    v, _ = port.mask_entries(A, L)
+    full, tr, te = port.split_aupr(A, L, 2, [0, v.size])
+    assert full == tuple(g["lower_ref"])[0]
+    assert np.all(tr[:, 0] == 0.0) and np.all(te[:, 1] == 0.0)
+    assert np.all(tr[:, 1] == full) and np.all(te[:, 0] == full)
