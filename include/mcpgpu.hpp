@@ -292,6 +292,61 @@ inline int64_t select_combo_stouffer(Context& ctx, const Matrix<float>& mi, cons
     return best;
 }
 
+// ---- semi-supervised split evaluation (the eval_mcpnet app) ----
+// The app's training sizes (size_t)(f * entries), f = 0.005 .. 0.1 (to 0.5 with TFs).
+inline std::vector<int64_t> train_counts(int64_t entries, bool tf) {
+    std::vector<double> fr = {0.005, 0.01, 0.02, 0.05, 0.1};
+    if (tf) fr.insert(fr.end(), {0.2, 0.3, 0.4, 0.5});
+    std::vector<int64_t> out;
+    for (double f : fr) out.push_back((int64_t)(size_t)(f * (double)entries));
+    return out;
+}
+
+struct SplitAupr {
+    double full = 0.0;
+    std::vector<double> train, test;  // iterations x parts, row-major
+};
+
+// eval_aupr_mcp: the AUPR of all labelled entries and of the shuffled train / test splits.
+inline SplitAupr split_aupr(Context& ctx, const Matrix<int8_t>& labels, const Matrix<float>& values, int64_t iterations,
+                            const std::vector<int64_t>& counts, TruthRegion region,
+                            const std::vector<int32_t>* row_gene = nullptr,
+                            const std::vector<uint8_t>* col_tf = nullptr) {
+    SplitAupr r;
+    const int64_t parts = (int64_t)counts.size();
+    r.train.assign((size_t)(iterations * parts), 0.0);
+    r.test.assign((size_t)(iterations * parts), 0.0);
+    ctx.check(mcpg_split_aupr(ctx.handle(), values.data(), values.rows(), values.columns(), values.ld(), labels.data(),
+                              labels.ld(), (int)region, row_gene ? row_gene->data() : nullptr,
+                              col_tf ? col_tf->data() : nullptr, iterations, counts.data(), parts, &r.full,
+                              r.train.data(), r.test.data()),
+              "split_aupr");
+    return r;
+}
+
+// eval_combos over the splits: results iterations x parts x 6 (train, test, Stouffer train,
+// Stouffer test, full, Stouffer full); stouffer: MCPG_STOUFFER_NONE, a MCPG_ROWSTATS_* mode or
+// MCPG_STOUFFER_TF.
+inline std::vector<double> split_combo_eval(Context& ctx, const Matrix<float>& mi, const Matrix<float>& m1,
+                                            const Matrix<float>& m2, const Matrix<float>& m3,
+                                            const Matrix<int8_t>& labels, const std::vector<double>& coeffs,
+                                            int stouffer, int64_t iterations, const std::vector<int64_t>& counts,
+                                            TruthRegion region, const std::vector<int32_t>* row_gene = nullptr,
+                                            const std::vector<uint8_t>* col_tf = nullptr,
+                                            std::vector<int64_t>* best = nullptr) {
+    const int64_t parts = (int64_t)counts.size();
+    std::vector<double> res((size_t)(iterations * parts * 6), 0.0);
+    std::vector<int64_t> b((size_t)(iterations * parts * 2), 0);
+    ctx.check(mcpg_split_combo_eval(ctx.handle(), mi.data(), mi.ld(), m1.data(), m1.ld(), m2.data(), m2.ld(),
+                                    m3.data(), m3.ld(), mi.rows(), mi.columns(), labels.data(), labels.ld(),
+                                    (int)region, row_gene ? row_gene->data() : nullptr,
+                                    col_tf ? col_tf->data() : nullptr, coeffs.data(), (int64_t)(coeffs.size() / 4),
+                                    stouffer, iterations, counts.data(), parts, res.data(), b.data()),
+              "split_combo_eval");
+    if (best) *best = b;
+    return res;
+}
+
 // ---- TF-restricted forms (--tf-input) ----
 // tfs: one value per gene, +inf for a transcription factor, -inf otherwise
 // (load_tfs, mcpnet_helper.hpp:1074-1123).  Outputs have one row per TF, in

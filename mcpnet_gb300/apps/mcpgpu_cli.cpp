@@ -9,6 +9,8 @@
 //   mcpgpu_cli mcpnet -i expr.exp -o prefix [--mi-method 1] [--mi-input] [-m 1 2 3 4] [-f coeffs.exp]
 //                     [--eval (-g truth.txt | -x truth.exp)] [--diagonal 0] [--seed S] [--tf-input tfs.txt]
 //   mcpgpu_cli transform -i mi.exp -o out.exp -m {1,2} [-f tfs.txt]   (1 = CLR, 2 = Stouffer)
+//   mcpgpu_cli eval_mcpnet (-i expr.exp [--mi-method 0] | --mi-file mi.exp) (-g truth.txt | -x truth.exp)
+//                     [-m 1 2 3 4 5] [-f coeffs.exp] [--iterations 100] [--diagonal 0] [--tf-input tfs.txt]
 //   mcpgpu_cli convert -i a.exp -o b.csv          (no GPU needed)
 //
 // Method values keep the reference's numbering and add the GPU forms:
@@ -32,6 +34,13 @@
 // each row's mean and unbiased sd without its diagonal entry (GaussianParamsExclude1); with
 // -f, the TF rows z-scored by row and by column (StandardScore) and combined by
 // zscored_clr_kernel / zscored_stouffer_kernel (transform.cpp:156-209).
+// eval_mcpnet (apps/pipeline/eval_mcpnet.cpp) prints the semi-supervised evaluation:
+// for MI and each MCP requested, the AUPR of the labelled entries and, over
+// --iterations shuffles of them (std::shuffle, std::mt19937 seeded 1, 2, ...), the
+// min / max / mean / stdev of the AUPRs of the first 0.5 / 1 / 2 / 5 / 10 % (to 50 %
+// with TFs) and of the rest; with -m 4 / 5 the ensemble's coefficient row chosen on
+// each training part (plain and, with 5, Stouffer), summarised every 10 iterations.
+// Its means divide by iterations - 1, as the app's (eval_mcpnet.cpp:307).
 // mcpnet outputs follow apps/pipeline/mcpnet.cpp: <prefix>_{bs|ap|inmi}.mi.<ext>,
 // .mcp2/.mcp3/.mcp4.<ext>, and for the ensemble .mcp_<c0>_<c1>_<c2>_<c3>.<ext>
 // and the Stouffer-transformed .mcpst_<c0>_<c1>_<c2>_<c3>.<ext> (coefficients
@@ -55,6 +64,7 @@
 // (the same columns separated by commas; the Alias column is optional when
 // reading) or raw binary ".bin" (int64 rows, int64 cols, float32 row-major).
 // Genes are rows.
+#include <cfloat>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -167,8 +177,9 @@ void write_matrix(const std::string& path, const Matrix<float>& m, const std::ve
 }
 
 struct Args {
-    std::string cmd, in, out, maxmin_out, coeffs, truth_list, truth_mat, tf_input, first, second;
-    int bins = 10, order = 3, mi_method = 1, tf_transition = -1;
+    std::string cmd, in, out, maxmin_out, coeffs, truth_list, truth_mat, tf_input, first, second, mi_file;
+    int bins = 10, order = 3, mi_method = -1, tf_transition = -1;
+    int64_t iterations = 100;
     std::vector<int> methods;
     float diagonal = 0.0f, tol = 0.1f;
     uint64_t seed = 1;
@@ -209,17 +220,28 @@ Args parse(int argc, char** argv) {
         else if (k == "--groundtruth-matrix") a.truth_mat = next();
         else if (k == "-g" || k == "--groundtruth-list") a.truth_list = next();
         else if (k == "-f") {
-            if (a.cmd == "mcpnet") a.coeffs = next();  // mcpnet -f = coefficients
+            if (a.cmd == "mcpnet" || a.cmd == "eval_mcpnet") a.coeffs = next();  // -f = coefficients there
             else a.tf_input = next();                  // mcp / dpi -f = TF list
         } else if (k == "--coefficients") a.coeffs = next();
         else if (k == "--tf-gene-transition") a.tf_transition = std::atoi(next().c_str());
         else if (k == "--first") a.first = next();
         else if (k == "--second") a.second = next();
-        else if (k == "--clamped") {}
+        else if (k == "--clamped" || k == "--permute-combo") {}  // no effect, as in the apps
+        else if (k == "--iterations") a.iterations = std::atoll(next().c_str());
+        else if (k == "--mi-file") a.mi_file = next();
         else if (k == "--eval") a.eval = true;
         else if (k == "--seed") a.seed = std::strtoull(next().c_str(), nullptr, 10);
         else if (k == "--tf-input") a.tf_input = next();
         else throw std::runtime_error("unknown option " + k);
+    }
+    if (a.cmd == "eval_mcpnet") {
+        if (a.in.empty() == a.mi_file.empty())
+            throw std::runtime_error("eval_mcpnet needs exactly one of -i (expression) and --mi-file");
+        if (a.truth_list.empty() == a.truth_mat.empty())
+            throw std::runtime_error("eval_mcpnet needs exactly one of -g (truth list) and -x (truth matrix)");
+        if (a.iterations < 0) throw std::runtime_error("--iterations must be >= 0");
+        a.eval = true;
+        return a;
     }
     if (a.in.empty() || a.out.empty()) throw std::runtime_error("-i and -o are required");
     if (a.eval && a.truth_list.empty() == a.truth_mat.empty())
@@ -368,12 +390,61 @@ std::vector<double> read_coeffs(const std::string& path) {
     return cs;
 }
 
+// Per part: min, max, sum and sum of squares of the AUPRs seen so far
+// (eval_mcpnet.cpp:255-300: min starts at DBL_MAX, the rest at 0).
+struct PartStats {
+    std::vector<double> s;
+    explicit PartStats(size_t parts) : s(4 * parts, 0.0) {
+        for (size_t j = 0; j < parts; ++j) s[4 * j] = DBL_MAX;
+    }
+    void add(size_t j, double a) {
+        s[4 * j] = std::min(s[4 * j], a);
+        s[4 * j + 1] = std::max(s[4 * j + 1], a);
+        s[4 * j + 2] += a;
+        s[4 * j + 3] += a * a;
+    }
+    // the app's lines (eval_mcpnet.cpp:305-317); its mean divides by i - 1
+    void print(const std::string& what, size_t j, int64_t i) const {
+        const double n = (double)i;
+        const double mean = s[4 * j + 2] / n;
+        const double sd = std::sqrt(n / (n - 1.0) * (s[4 * j + 3] / n - mean * mean));
+        std::printf("AUPR %s min,%.12g,decile %zu,iters %lld,sec\n", what.c_str(), s[4 * j], j, (long long)i);
+        std::printf("AUPR %s max,%.12g,decile %zu,iters %lld,sec\n", what.c_str(), s[4 * j + 1], j, (long long)i);
+        std::printf("AUPR %s mean,%.12g,decile %zu,iters %lld,sec\n", what.c_str(), s[4 * j + 2] / (n - 1.0), j,
+                    (long long)i);
+        std::printf("AUPR %s stdev,%.12g,decile %zu,iters %lld,sec\n", what.c_str(), sd, j, (long long)i);
+    }
+};
+
+// eval_aupr_mcp (eval_mcpnet.cpp:227-317) of one score matrix.
+void report_split(mcpgpu::Context& ctx, const Truth& t, const Matrix<float>& values, int64_t iterations,
+                  const std::string& tag) {
+    const mcpgpu::Curves c = mcpgpu::compute_aupr_auroc(ctx, t.labels, values, t.region,
+                                                       t.tf ? &t.tf->rows : nullptr, t.tf ? &t.tf->col_tf : nullptr);
+    const int64_t E = c.n_pos + c.n_neg;  // the labelled entries
+    const std::vector<int64_t> counts = mcpgpu::train_counts(E, t.tf != nullptr);
+    mcpgpu::SplitAupr r = mcpgpu::split_aupr(ctx, t.labels, values, iterations, counts, t.region,
+                                             t.tf ? &t.tf->rows : nullptr, t.tf ? &t.tf->col_tf : nullptr);
+    std::printf("AUPR %s,%.12g,,,sec\n", tag.c_str(), r.full);
+    const size_t parts = counts.size();
+    PartStats tr(parts), te(parts);
+    for (int64_t i = 0; i < iterations; ++i)
+        for (size_t j = 0; j < parts; ++j) {
+            tr.add(j, r.train[(size_t)i * parts + j]);
+            te.add(j, r.test[(size_t)i * parts + j]);
+        }
+    for (size_t j = 0; j < parts; ++j) {
+        tr.print(tag + " train", j, iterations);
+        te.print(tag + " test", j, iterations);
+    }
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
     try {
         Args a = parse(argc, argv);
-        Named in = read_matrix(a.in);
+        Named in = read_matrix(a.in.empty() ? a.mi_file : a.in);
         double t0 = now_s();
         if (a.cmd == "convert") {
             write_matrix(a.out, in.m, in.rows, in.cols);
@@ -453,6 +524,71 @@ int main(int argc, char** argv) {
             }
             std::printf("Transformed in %.6f sec\n", now_s() - t0);
             write_matrix(a.out, out, tf.on ? tf.names : in.rows, in.rows);
+        } else if (a.cmd == "eval_mcpnet") {  // apps/pipeline/eval_mcpnet.cpp:464-893
+            const std::vector<std::string>& genes = in.rows;
+            Truth truth = read_truth(a, genes, tf);
+            Matrix<float> mi;
+            if (!a.mi_file.empty()) {
+                if (in.m.rows() != in.m.columns()) throw std::runtime_error("--mi-file needs a square MI matrix");
+                mi = in.m;
+            } else {  // the app's default MI method is B-spline
+                compute_mi(ctx, in, a.mi_method < 0 ? 0 : a.mi_method, a.bins, a.order, a.seed, mi);
+                std::printf("Computed,MI,,%.6f,sec\n", now_s() - t0);
+            }
+            mcpgpu::set_diagonal(mi, a.diagonal);
+            Matrix<float> mi_tf;
+            if (tf.on) {
+                mi_tf = Matrix<float>((int64_t)tf.rows.size(), mi.columns());
+                for (size_t r = 0; r < tf.rows.size(); ++r)
+                    for (int64_t j = 0; j < mi.columns(); ++j) mi_tf.at((int64_t)r, j) = mi.at(tf.rows[r], j);
+            }
+            const std::string tag = tf.on ? "TF" : "full";
+            const Matrix<float>& base = tf.on ? mi_tf : mi;
+            report_split(ctx, truth, base, a.iterations, tag);
+            bool ens = false, with_st = false;
+            for (int method : a.methods) {
+                if (method < 1 || method > 5) throw std::runtime_error("eval_mcpnet -m accepts 1, 2, 3, 4, 5");
+                if (method >= 4) {
+                    ens = true;
+                    with_st |= method == 5;
+                    continue;
+                }
+                Matrix<float> ratio;
+                if (tf.on) mcpgpu::compute_mcp_tfs(ctx, mi, tf.tfs, method + 1, method, ratio);
+                else mcpgpu::compute_mcp(ctx, mi, method + 1, ratio);
+                std::printf("Computed,MCP%d,,%.6f,sec\n", method + 1, now_s() - t0);
+                report_split(ctx, truth, ratio, a.iterations, tag);
+            }
+            if (ens) {  // eval_combos over the splits (eval_mcpnet.cpp:737-893)
+                std::vector<double> cs = read_coeffs(a.coeffs);
+                Matrix<float> m1, m2, m3;
+                if (tf.on) mcpgpu::compute_maxmins_tfs(ctx, mi, tf.tfs, mi_tf, m1, m2, m3);
+                else mcpgpu::compute_maxmins(ctx, mi, m1, m2, m3);
+                const mcpgpu::Curves c = mcpgpu::compute_aupr_auroc(ctx, truth.labels, base, truth.region,
+                                                                   tf.on ? &tf.rows : nullptr,
+                                                                   tf.on ? &tf.col_tf : nullptr);
+                const std::vector<int64_t> counts = mcpgpu::train_counts(c.n_pos + c.n_neg, tf.on);
+                const int st = !with_st ? MCPG_STOUFFER_NONE
+                                        : (tf.on ? MCPG_STOUFFER_TF : MCPG_ROWSTATS_EXCLUDE_DIAGONAL);
+                std::vector<double> res = mcpgpu::split_combo_eval(ctx, base, m1, m2, m3, truth.labels, cs, st,
+                                                                   a.iterations, counts, truth.region,
+                                                                   tf.on ? &tf.rows : nullptr,
+                                                                   tf.on ? &tf.col_tf : nullptr);
+                const size_t parts = counts.size();
+                const char* names[6] = {"train", "test", "train", "test", "full", "full"};
+                std::vector<PartStats> stats(6, PartStats(parts));
+                for (int64_t i = 1; i <= a.iterations; ++i) {
+                    for (size_t j = 0; j < parts; ++j)
+                        for (int q = 0; q < 6; ++q) stats[(size_t)q].add(j, res[(((size_t)i - 1) * parts + j) * 6 + q]);
+                    if (i % 10) continue;  // the app reports every 10 iterations
+                    for (size_t j = 0; j < parts; ++j)
+                        for (int q : {0, 1, 2, 3, 4, 5})
+                            stats[(size_t)q].print(std::string(q == 2 || q == 3 || q == 5 ? "stouffer " : "") + tag +
+                                                       " " + names[q],
+                                                   j, i);
+                }
+            }
+            std::printf("eval_mcpnet done in %.6f sec\n", now_s() - t0);
         } else if (a.cmd == "mcpnet") {
             const std::string ext = ext_of(a.in);
             const std::vector<std::string>& genes = in.rows;
@@ -467,7 +603,7 @@ int main(int argc, char** argv) {
                 mi = in.m;
                 prefix += "_inmi";
             } else {
-                prefix += compute_mi(ctx, in, a.mi_method, a.bins, a.order, a.seed, mi);
+                prefix += compute_mi(ctx, in, a.mi_method < 0 ? 1 : a.mi_method, a.bins, a.order, a.seed, mi);
                 std::printf("Computed,MI,,%.6f,sec\n", now_s() - t0);
             }
             mcpgpu::set_diagonal(mi, a.diagonal);  // mcpnet.cpp:299-308 (negative: keep)

@@ -312,3 +312,73 @@ def test_cli_transform(built_lib, port, tmp_path):
             np.testing.assert_allclose(got, port.stouffer_tf(A[tf_rows], clr=(kind == "clr")), rtol=1e-5, atol=1e-5)
     finally:
         h.close()
+
+
+def _stats(vals, i):
+    """eval_mcpnet's per-part min / max / mean (sum / (i - 1)) / stdev over i iterations."""
+    v = np.asarray(vals, dtype=np.float64)[:i]
+    mean = v.sum() / i
+    return v.min(), v.max(), v.sum() / (i - 1), np.sqrt(i / (i - 1) * ((v * v).sum() / i - mean * mean))
+
+
+def _stat_lines(out, what):
+    got = {}
+    for l in out.splitlines():
+        if l.startswith(f"AUPR {what} "):
+            head, val, dec, it, _ = l.split(",")
+            # the first block for a tag (MI's, before the MCPs' blocks with the same tag)
+            got.setdefault((head[len(f"AUPR {what} "):], int(dec.split()[1]), int(it.split()[1])), float(val))
+    return got
+
+
+@pytest.mark.gpu
+def test_cli_eval_mcpnet(built_lib, port, tmp_path):
+    """eval_mcpnet --mi-file -x truth -m 1 4 5: the split AUPR summaries of MI and MCP2
+    against the oracle's composition of eval_aupr_mcp, and the ensemble summary
+    against the library's split coefficient search."""
+    import mcpnet_gb300 as M
+    n, iters = 60, 10
+    X, E = built_lib.synth_grn(n, 220, seed=25, with_edges=True)
+    A = port.bspline_mi(X)
+    np.fill_diagonal(A, 0)
+    names = [f"g{i}" for i in range(n)]
+    write_exp(tmp_path / "mi.exp", A, names)
+    L = np.zeros((n, n), np.int8)
+    for s, t in E:
+        L[s, t] = L[t, s] = 1
+    write_exp(tmp_path / "truth.exp", L.astype(np.float32), names)
+    cs = np.array([[0.25, 0.25, 0.25, 0.25], [0.5, 0.5, 0, 0], [0, 0.5, 0.25, 0.25]])
+    np.savetxt(tmp_path / "coeffs.txt", cs)
+    r = run("eval_mcpnet", "--mi-file", tmp_path / "mi.exp", "-x", tmp_path / "truth.exp", "-m", "1", "4", "5",
+            "-f", tmp_path / "coeffs.txt", "--iterations", iters)
+    assert r.returncode == 0, r.stderr
+    Am = A.copy()
+    E_ = port.mask_entries(Am, L)[0].size
+    tc = M.train_counts(E_)
+    heads = [l for l in r.stdout.splitlines() if l.startswith("AUPR full,")]
+    assert len(heads) == 2
+    for head, V in zip(heads, (Am, port.mcp(Am, 2)[1])):
+        full, tr, te = port.split_aupr(V, L, iters, tc)
+        assert abs(float(head.split(",")[1]) - full) <= 1e-11
+    got = _stat_lines(r.stdout, "full")
+    full, tr, te = port.split_aupr(Am, L, iters, tc)
+    for j in range(len(tc)):
+        for what, arr in (("train", tr[:, j]), ("test", te[:, j])):
+            want = _stats(arr, iters)
+            for name, w in zip(("min", "max", "mean", "stdev"), want):
+                assert abs(got[(f"{what} {name}", j, iters)] - w) <= 1e-9 * max(1.0, abs(w)), (what, name, j)
+    h = M.Handle(0)
+    try:
+        M1 = port.maxmin(Am, Am)
+        res, _ = h.split_combo_eval(Am, M1, port.maxmin(Am, M1), port.maxmin(M1, M1), L, cs, iters, tc,
+                                    "exclude_diagonal")
+    finally:
+        h.close()
+    st = _stat_lines(r.stdout, "stouffer full")
+    for j in range(len(tc)):
+        want = _stats(res[:, j, 2], iters)
+        assert abs(st[("train min", j, iters)] - want[0]) <= 1e-11
+        assert abs(st[("train max", j, iters)] - want[1]) <= 1e-11
+        want = _stats(res[:, j, 4], iters)
+        full_lines = {k: v for k, v in got.items() if k[0].startswith("full ")}
+        assert abs(full_lines[("full min", j, iters)] - want[0]) <= 1e-11
