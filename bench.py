@@ -498,6 +498,17 @@ def pipeline_arm(args, ws, rank, local):
             lambda: r.__setitem__(0, h.combo_stouffer_eval_dev(A, M1, M2, M3, Lb, coeffs)))
         ev["combo_stouffer"] = r[0]
         ev["coeffs"] = coeffs
+        if args.split_iters > 0:
+            # the eval_mcpnet app's semi-supervised evaluation: shuffled train / test splits
+            entries = ev["mi"][2] + ev["mi"][3]
+            tcs = M.train_counts(entries)
+            h.split_aupr_dev(R2, Lb, 1, tcs[:1])  # untimed: workspace
+            st["split_aupr_mcp2"] = timed(lambda: r.__setitem__(0, h.split_aupr_dev(R2, Lb, args.split_iters, tcs)))
+            ev["split_aupr"] = r[0]
+            st["split_combo_stouffer"] = timed(lambda: r.__setitem__(0, h.split_combo_eval_dev(
+                A, M1, M2, M3, Lb, coeffs, args.split_iters, tcs, "exclude_diagonal")))
+            ev["split_combo"] = r[0]
+            ev["split_entries"] = entries
     tfst = {}
     if args.tfs > 0:
         # --tf-input: a seeded set of TF genes (the synthetic GRN has no TF annotation)
@@ -603,6 +614,18 @@ def pipeline_arm(args, ws, rank, local):
                                "ms_per_row": st[key] * 1e3 / (len(coeffs) - 1), "best_row": int(best),
                                "best_coeffs": coeffs[best].tolist(), "best_aupr": float(pr[best]),
                                "best_auroc": float(roc[best])}
+    if not args.no_eval and args.split_iters > 0:
+        k = args.split_iters
+        full, tr, te = ev["split_aupr"]
+        stages["split_aupr_mcp2"] = {"ms": st["split_aupr_mcp2"] * 1e3, "iterations": k, "parts": int(tr.shape[1]),
+                                     "entries": int(ev["split_entries"]),
+                                     "ms_per_iteration": st["split_aupr_mcp2"] * 1e3 / k, "full_aupr": full,
+                                     "train_aupr_mean": tr.mean(0).tolist(), "test_aupr_mean": te.mean(0).tolist()}
+        res, best = ev["split_combo"]
+        stages["split_combo_stouffer"] = {"ms": st["split_combo_stouffer"] * 1e3, "iterations": k,
+                                          "rows": len(coeffs), "ms_per_iteration": st["split_combo_stouffer"] * 1e3 / k,
+                                          "test_aupr_mean": res[..., 1].mean(0).tolist(),
+                                          "stouffer_test_aupr_mean": res[..., 3].mean(0).tolist()}
     line = {"mode": "pipeline", "genes": n, "samples": m, "mi_method": args.mi_method, "precision": args.precision,
             "stage_s": st, "wall_s": wall, "stages": stages, "closure_iterations": iters, "clocks": clk,
             "kernel_profile": prof, "sms": sms}
@@ -667,6 +690,9 @@ def main(argv=None):
     ap.add_argument("--pipeline", action="store_true",
                     help="run the whole compute core once, stage by stage (defaults to 32768 x 4096)")
     ap.add_argument("--closure", action="store_true", help="with --pipeline: add the max-capacity closure")
+    ap.add_argument("--split-iters", type=int, default=0,
+                    help="with --pipeline: add the eval_mcpnet split evaluation (MCP2 split AUPRs and the Stouffer "
+                         "split coefficient search) over this many shuffles")
     ap.add_argument("--tfs", type=int, default=0,
                     help="with --pipeline: add the --tf-input stages (TF MCP2/3/4, TF max-min products, TF DPI, "
                          "TF evaluation and searches) for this many seeded TF genes")

@@ -14,8 +14,10 @@
 #include <numeric>
 #include <random>
 #include <string>
+#include <thread>
 #include <vector>
 
+#include <omp.h>
 #include <sys/mman.h>
 #include <unistd.h>
 
@@ -1714,15 +1716,86 @@ int split_entries(mcpg_handle* h, const mcpg::TruthRegion& r, const float* const
 // depend only on the length and the generator, so the shuffled entry positions
 // are the reference's order of its (row, col, label) tuples.  seed 0 keeps the
 // mask order.  hp is host work space.
-int split_perm(mcpg_handle* h, int64_t E, uint64_t seed, std::vector<uint32_t>& hp, uint32_t* dperm) {
+void shuffle_positions(std::vector<uint32_t>& hp, int64_t E, uint64_t seed) {
     hp.resize((size_t)E);
     std::iota(hp.begin(), hp.end(), 0u);
     if (seed) {
         std::mt19937 g((std::mt19937::result_type)seed);
         std::shuffle(hp.begin(), hp.end(), g);
     }
+}
+
+int split_perm(mcpg_handle* h, int64_t E, uint64_t seed, std::vector<uint32_t>& hp, uint32_t* dperm) {
+    shuffle_positions(hp, E, seed);
     if (E > 0)
         CK(h, cudaMemcpyAsync(dperm, hp.data(), (size_t)E * 4, cudaMemcpyHostToDevice, h->stream),
+           "host-to-device copy");
+    return MCPG_OK;
+}
+
+// The permutations of iterations i0 .. i0 + n - 1 are independent of one
+// another, so a batch is made on several host threads at once (each its own
+// std::mt19937), and the next batch is made on a background thread while the
+// GPU evaluates the current one.  A batch holds at most 1/16 of the host's
+// memory (64 GiB at most) in positions.
+struct PermBatch {
+    std::vector<std::vector<uint32_t>> p;
+    int64_t i0 = 0;
+};
+
+int64_t perm_batch_size(int64_t E, int64_t left) {
+    int64_t b = (int64_t)omp_get_max_threads();
+    const long pages = sysconf(_SC_PHYS_PAGES), psz = sysconf(_SC_PAGESIZE);
+    int64_t budget = (pages > 0 && psz > 0) ? (int64_t)pages * psz / 16 : ((int64_t)8 << 30);
+    if (budget > ((int64_t)64 << 30)) budget = (int64_t)64 << 30;
+    const int64_t cap = budget / ((E > 0 ? E : 1) * 4);
+    if (b > cap) b = cap;
+    if (b > left) b = left;
+    return b < 1 ? 1 : b;
+}
+
+void make_perm_batch(PermBatch& pb, int64_t E, int64_t i0, int64_t n) {
+    pb.p.resize((size_t)n);
+    pb.i0 = i0;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t b = 0; b < n; ++b) shuffle_positions(pb.p[(size_t)b], E, (uint64_t)(i0 + b));
+}
+
+class PermSource {
+  public:
+    PermSource(int64_t E, int64_t iters) : E_(E), iters_(iters) {}
+    ~PermSource() {
+        if (worker_.joinable()) worker_.join();
+    }
+    // The positions of iteration i (called for i = 1, 2, ... in order).
+    const std::vector<uint32_t>& get(int64_t i) {
+        if (i >= cur_.i0 + (int64_t)cur_.p.size()) {
+            if (worker_.joinable()) {
+                worker_.join();
+                std::swap(cur_, nxt_);
+            } else {
+                const int64_t n = perm_batch_size(E_, iters_ - next_ + 1);
+                make_perm_batch(cur_, E_, next_, n);
+                next_ += n;
+            }
+            if (next_ <= iters_) {  // the batch after this one, in the background
+                const int64_t i0 = next_, n = perm_batch_size(E_, iters_ - next_ + 1);
+                next_ += n;
+                worker_ = std::thread([this, i0, n] { make_perm_batch(nxt_, E_, i0, n); });
+            }
+        }
+        return cur_.p[(size_t)(i - cur_.i0)];
+    }
+
+  private:
+    int64_t E_, iters_, next_ = 1;
+    PermBatch cur_, nxt_;
+    std::thread worker_;
+};
+
+int upload_perm(mcpg_handle* h, const std::vector<uint32_t>& hp, uint32_t* dperm) {
+    if (!hp.empty())
+        CK(h, cudaMemcpyAsync(dperm, hp.data(), hp.size() * 4, cudaMemcpyHostToDevice, h->stream),
            "host-to-device copy");
     return MCPG_OK;
 }
@@ -1798,8 +1871,9 @@ int split_aupr_dev(mcpg_handle* h, const float* values, int64_t ldv, const mcpg:
     double a = 0.0;
     if ((rc = split_aupr_range(h, w, se, dp, 0, se.E, se.vals[0], nullptr, &a))) return rc;
     if (full) *full = a;
+    PermSource ps(se.E, iters);
     for (int64_t i = 1; i <= iters; ++i) {
-        if ((rc = split_perm(h, se.E, (uint64_t)i, hp, (uint32_t*)perm))) return rc;
+        if ((rc = upload_perm(h, ps.get(i), (uint32_t*)perm))) return rc;
         for (int64_t j = 0; j < parts; ++j) {
             double tr = 0.0, te = 0.0;
             if ((rc = split_aupr_range(h, w, se, dp, 0, tc[j], se.vals[0], nullptr, &tr))) return rc;
@@ -1907,8 +1981,9 @@ int split_combo_dev(mcpg_handle* h, const float* const mats[4], const int64_t ld
                                               &full_s[(size_t)c])))
             return rc;
     }
+    PermSource ps(E, iters);
     for (int64_t i = 1; i <= iters; ++i) {
-        if ((rc = split_perm(h, E, (uint64_t)i, hp, (uint32_t*)perm))) return rc;
+        if ((rc = upload_perm(h, ps.get(i), (uint32_t*)perm))) return rc;
         for (int64_t j = 0; j < parts; ++j) {
             const int64_t k = tc[j];
             double max_p = 0.0, max_s = 0.0, a = 0.0;
