@@ -38,6 +38,34 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 
 __host__ __device__ __forceinline__ int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
+// ---- element-wise traversal of a rows x cols matrix ----
+// Blocks of EW_TPB threads take (row, EW_SEG-column segment) items grid-stride;
+// a thread handles its EW_SEG / EW_TPB columns of the segment (coalesced across
+// the block) in one unrolled step, so that, with __restrict__ operands, their
+// loads are in flight together.  One 64-bit division per segment instead of one
+// per element.  Launch with ew_grid2d(rows, cols) blocks of EW_TPB threads.
+constexpr int EW_SEG = 1024, EW_TPB = 256;
+template <class F>
+__device__ __forceinline__ void for_each_entry(int64_t rows, int64_t cols, F&& f) {
+    const int64_t segs = (cols + EW_SEG - 1) / EW_SEG;
+    const int64_t items = rows * segs;
+    for (int64_t it = blockIdx.x; it < items; it += gridDim.x) {
+        const int64_t i = it / segs;
+        const int64_t c0 = (it - i * segs) * EW_SEG + threadIdx.x;
+        const int64_t c1 = c0 + EW_SEG - threadIdx.x < cols ? c0 + EW_SEG - threadIdx.x : cols;
+#pragma unroll
+        for (int k = 0; k < EW_SEG / EW_TPB; ++k) {
+            const int64_t j = c0 + k * EW_TPB;
+            if (j < c1) f(i, j);
+        }
+    }
+}
+inline unsigned ew_grid2d(int64_t rows, int64_t cols) {
+    int64_t items = rows * ceil_div(cols, EW_SEG);
+    if (items > 152 * 16) items = 152 * 16;
+    return (unsigned)(items < 1 ? 1 : items);
+}
+
 // One entry of compute_combo (apps/pipeline/mcpnet_helper.hpp:507-573): the
 // denominator is summed in double in the reference's order, coefficient 1 adds
 // the value itself and coefficient 0 skips the term; explicit _rn intrinsics

@@ -364,13 +364,10 @@ cudaError_t launch_one(const MaxminParams& p, cudaStream_t stream) {
 }
 
 // ---------------- element-wise helpers ----------------
-__global__ void ratio_kernel_ew(const float* A, int64_t lda, const float* M, int64_t ldm, int64_t rows, int64_t cols,
-                                float* R, int64_t ldr) {
-    const int64_t total = rows * cols;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t i = t / cols, j = t - i * cols;
-        R[i * ldr + j] = ratio_of(A[i * lda + j], M[i * ldm + j]);
-    }
+__global__ void __launch_bounds__(EW_TPB) ratio_kernel_ew(const float* __restrict__ A, int64_t lda,
+                                                         const float* __restrict__ M, int64_t ldm, int64_t rows,
+                                                         int64_t cols, float* __restrict__ R, int64_t ldr) {
+    for_each_entry(rows, cols, [&](int64_t i, int64_t j) { R[i * ldr + j] = ratio_of(A[i * lda + j], M[i * ldm + j]); });
 }
 
 __global__ void set_diag_kernel(float* A, int64_t nd, int64_t lda, float v) {
@@ -398,42 +395,34 @@ __global__ void max_transpose_kernel(const float* M, int64_t n, int64_t ldm, flo
     }
 }
 
-__global__ void copy2d_kernel(const float* src, int64_t lds, float* dst, int64_t ldd, int64_t rows, int64_t cols) {
-    const int64_t total = rows * cols;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t i = t / cols, j = t - i * cols;
-        dst[i * ldd + j] = src[i * lds + j];
-    }
+__global__ void __launch_bounds__(EW_TPB) copy2d_kernel(const float* __restrict__ src, int64_t lds,
+                                                       float* __restrict__ dst, int64_t ldd, int64_t rows,
+                                                       int64_t cols) {
+    for_each_entry(rows, cols, [&](int64_t i, int64_t j) { dst[i * ldd + j] = src[i * lds + j]; });
 }
 
 __global__ void gather_kernel(const float* src, int64_t lds, const int* ri, const int* ci, int64_t rows, int64_t cols,
                               float* dst, int64_t ldd) {
-    const int64_t total = rows * cols;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t r = t / cols, c = t - r * cols;
+    for_each_entry(rows, cols, [&](int64_t r, int64_t c) {
         const int64_t sr = ri ? ri[r] : r, sc = ci ? ci[c] : c;
         dst[r * ldd + c] = src[sr * lds + sc];
-    }
+    });
 }
 
 __global__ void fold_mask_kernel(const float* src, int64_t lds, const float* mask, int64_t rows, int64_t cols,
                                  float* dst, int64_t ldd) {
-    const int64_t total = rows * cols;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t r = t / cols, c = t - r * cols;
+    for_each_entry(rows, cols, [&](int64_t r, int64_t c) {
         const float a = src[r * lds + c], mk = mask[c];
         dst[r * ldd + c] = (mk < a) ? mk : a;  // min(a, mask[c]); min is exact, so folding the mask
                                                // into one operand equals the reference's 3-way min
-    }
+    });
 }
 
 __global__ void dpi_tf_apply_kernel(const float* A, int64_t lda, const float* Call, int64_t ld1, const float* Ctf,
                                     int64_t ld2, const uint8_t* tf, int64_t n, float tm, float* out, int64_t ldo,
                                     uint8_t* mask, unsigned long long* removed) {
-    const int64_t total = n * n;
     unsigned long long cnt = 0;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t x = t / n, z = t - x * n;
+    for_each_entry(n, n, [&](int64_t x, int64_t z) {
         const float e = A[x * lda + z];
         const float ixz = __fmul_rn(e, tm);  // dpi_tf_kernel keeps its multiplier in IT (float)
         const bool tfxz = (tf[x] != 0) != (tf[z] != 0);
@@ -443,7 +432,7 @@ __global__ void dpi_tf_apply_kernel(const float* A, int64_t lda, const float* Ca
         out[x * ldo + z] = o;
         cnt += (o != e);
         if (mask) mask[x * n + z] = del ? 1 : 0;
-    }
+    });
     if (removed) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
@@ -455,11 +444,9 @@ __global__ void maxmin_route_kernel(const float* A, int64_t lda, const float* B,
                                     int64_t cols, int64_t k, const float* C, int64_t ldc, const float* dC,
                                     int64_t lddc, const int32_t* K, int64_t ldk, float* dA, int64_t ldda, float* dB,
                                     int64_t lddb) {
-    const int64_t total = rows * cols;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t i = t / cols, j = t - i * cols;
+    for_each_entry(rows, cols, [&](int64_t i, int64_t j) {
         const float g = dC[i * lddc + j];
-        if (g == 0.0f) continue;
+        if (g == 0.0f) return;
         int64_t ks = -1;
         if (K) {
             ks = K[i * ldk + j];
@@ -472,46 +459,38 @@ __global__ void maxmin_route_kernel(const float* A, int64_t lda, const float* B,
                         break;
                     }
         }
-        if (ks < 0) continue;
+        if (ks < 0) return;
         const float a = A[i * lda + ks], b = B[j * ldb + ks];
         if (a <= b) atomicAdd(dA + i * ldda + ks, g);  // std::min(a, b) returns a on a tie
         else atomicAdd(dB + j * lddb + ks, g);
-    }
+    });
 }
 
 __global__ void ratio_bwd_kernel(const float* A, int64_t lda, const float* M, int64_t ldm, int64_t rows, int64_t cols,
                                  const float* dR, int64_t lddr, float* dA, int64_t ldda, float* dM, int64_t lddm) {
-    const int64_t total = rows * cols;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t i = t / cols, j = t - i * cols;
+    for_each_entry(rows, cols, [&](int64_t i, int64_t j) {
         const float a = A[i * lda + j], m = M[i * ldm + j], g = dR[i * lddr + j];
-        if (g == 0.0f || fabsf(a) < FLT_EPSILON || fabsf(m) < FLT_EPSILON) continue;
+        if (g == 0.0f || fabsf(a) < FLT_EPSILON || fabsf(m) < FLT_EPSILON) return;
         dA[i * ldda + j] += g / m;
         dM[i * lddm + j] -= g * a / (m * m);
-    }
+    });
 }
 
 // compute_combo (mcpnet_helper.hpp:507-573): combo_value_ff gives the
 // reference's double-precision result, mostly without the FP64 pipe.
-__global__ void combo_kernel(const float* mi, int64_t ldm, const float* M1, int64_t ld1, const float* M2, int64_t ld2,
-                             const float* M3, int64_t ld3, int64_t rows, int64_t cols, const ComboCoef k, float* out,
-                             int64_t ldo) {
-    const int64_t total = rows * cols;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t i = t / cols, j = t - i * cols;
+__global__ void __launch_bounds__(EW_TPB) combo_kernel(const float* __restrict__ mi, int64_t ldm,
+                                                      const float* __restrict__ M1, int64_t ld1,
+                                                      const float* __restrict__ M2, int64_t ld2,
+                                                      const float* __restrict__ M3, int64_t ld3, int64_t rows,
+                                                      int64_t cols, const ComboCoef k, float* __restrict__ out,
+                                                      int64_t ldo) {
+    for_each_entry(rows, cols, [&](int64_t i, int64_t j) {
         const float v = mi[i * ldm + j];
         const float m1 = k.kind[1] ? M1[i * ld1 + j] : 0.0f;
         const float m2 = k.kind[2] ? M2[i * ld2 + j] : 0.0f;
         const float m3 = k.kind[3] ? M3[i * ld3 + j] : 0.0f;
         out[i * ldo + j] = combo_value_ff(v, m1, m2, m3, k);
-    }
-}
-
-unsigned ew_blocks(int64_t total) {
-    int64_t b = ceil_div(total, 256);
-    if (b > 152 * 32) b = 152 * 32;
-    if (b < 1) b = 1;
-    return (unsigned)b;
+    });
 }
 
 }  // namespace
@@ -537,7 +516,7 @@ cudaError_t launch_ratio(const float* A, int64_t lda, const float* M, int64_t ld
                          float* R, int64_t ldr, cudaStream_t stream, int64_t* launches) {
     if (rows <= 0 || cols <= 0) return cudaSuccess;
     if (launches) ++*launches;
-    ratio_kernel_ew<<<ew_blocks(rows * cols), 256, 0, stream>>>(A, lda, M, ldm, rows, cols, R, ldr);
+    ratio_kernel_ew<<<ew_grid2d(rows, cols), 256, 0, stream>>>(A, lda, M, ldm, rows, cols, R, ldr);
     return cudaGetLastError();
 }
 
@@ -563,7 +542,7 @@ cudaError_t launch_gather(const float* src, int64_t lds, const int* ri, const in
                           float* dst, int64_t ldd, cudaStream_t stream, int64_t* launches) {
     if (rows <= 0 || cols <= 0) return cudaSuccess;
     if (launches) ++*launches;
-    gather_kernel<<<ew_blocks(rows * cols), 256, 0, stream>>>(src, lds, ri, ci, rows, cols, dst, ldd);
+    gather_kernel<<<ew_grid2d(rows, cols), 256, 0, stream>>>(src, lds, ri, ci, rows, cols, dst, ldd);
     return cudaGetLastError();
 }
 
@@ -571,7 +550,7 @@ cudaError_t launch_fold_mask(const float* src, int64_t lds, const float* mask, i
                              int64_t ldd, cudaStream_t stream, int64_t* launches) {
     if (rows <= 0 || cols <= 0) return cudaSuccess;
     if (launches) ++*launches;
-    fold_mask_kernel<<<ew_blocks(rows * cols), 256, 0, stream>>>(src, lds, mask, rows, cols, dst, ldd);
+    fold_mask_kernel<<<ew_grid2d(rows, cols), 256, 0, stream>>>(src, lds, mask, rows, cols, dst, ldd);
     return cudaGetLastError();
 }
 
@@ -580,7 +559,7 @@ cudaError_t launch_dpi_tf_apply(const float* A, int64_t lda, const float* Call, 
                                 uint8_t* mask, unsigned long long* removed, cudaStream_t stream, int64_t* launches) {
     if (n <= 0) return cudaSuccess;
     if (launches) ++*launches;
-    dpi_tf_apply_kernel<<<ew_blocks(n * n), 256, 0, stream>>>(A, lda, Call, ld1, Ctf, ld2, tf, n, tm, out, ldo, mask,
+    dpi_tf_apply_kernel<<<ew_grid2d(n, n), 256, 0, stream>>>(A, lda, Call, ld1, Ctf, ld2, tf, n, tm, out, ldo, mask,
                                                              removed);
     return cudaGetLastError();
 }
@@ -591,7 +570,7 @@ cudaError_t launch_maxmin_route(const float* A, int64_t lda, const float* B, int
                                 cudaStream_t stream, int64_t* launches) {
     if (rows <= 0 || cols <= 0) return cudaSuccess;
     if (launches) ++*launches;
-    maxmin_route_kernel<<<ew_blocks(rows * cols), 256, 0, stream>>>(A, lda, B, ldb, rows, cols, k, C, ldc, dC, lddc, K,
+    maxmin_route_kernel<<<ew_grid2d(rows, cols), 256, 0, stream>>>(A, lda, B, ldb, rows, cols, k, C, ldc, dC, lddc, K,
                                                                    ldk, dA, ldda, dB, lddb);
     return cudaGetLastError();
 }
@@ -601,7 +580,7 @@ cudaError_t launch_ratio_bwd(const float* A, int64_t lda, const float* M, int64_
                              cudaStream_t stream, int64_t* launches) {
     if (rows <= 0 || cols <= 0) return cudaSuccess;
     if (launches) ++*launches;
-    ratio_bwd_kernel<<<ew_blocks(rows * cols), 256, 0, stream>>>(A, lda, M, ldm, rows, cols, dR, lddr, dA, ldda, dM,
+    ratio_bwd_kernel<<<ew_grid2d(rows, cols), 256, 0, stream>>>(A, lda, M, ldm, rows, cols, dR, lddr, dA, ldda, dM,
                                                                 lddm);
     return cudaGetLastError();
 }
@@ -611,7 +590,7 @@ cudaError_t launch_combo(const float* mi, int64_t ldm, const float* M1, int64_t 
                          int64_t ldo, cudaStream_t stream, int64_t* launches) {
     if (rows <= 0 || cols <= 0) return cudaSuccess;
     if (launches) ++*launches;
-    combo_kernel<<<ew_blocks(rows * cols), 256, 0, stream>>>(mi, ldm, M1, ld1, M2, ld2, M3, ld3, rows, cols,
+    combo_kernel<<<ew_grid2d(rows, cols), 256, 0, stream>>>(mi, ldm, M1, ld1, M2, ld2, M3, ld3, rows, cols,
                                                             make_combo_coef(cs), out, ldo);
     return cudaGetLastError();
 }
@@ -619,7 +598,7 @@ cudaError_t launch_combo(const float* mi, int64_t ldm, const float* M1, int64_t 
 cudaError_t launch_copy2d(const float* src, int64_t lds, float* dst, int64_t ldd, int64_t rows, int64_t cols,
                           cudaStream_t stream) {
     if (rows <= 0 || cols <= 0) return cudaSuccess;
-    copy2d_kernel<<<ew_blocks(rows * cols), 256, 0, stream>>>(src, lds, dst, ldd, rows, cols);
+    copy2d_kernel<<<ew_grid2d(rows, cols), 256, 0, stream>>>(src, lds, dst, ldd, rows, cols);
     return cudaGetLastError();
 }
 
