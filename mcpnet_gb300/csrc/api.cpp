@@ -1140,21 +1140,22 @@ int ev_sort(mcpg_handle* h, uint32_t* keys, int64_t n) {
     return MCPG_OK;
 }
 
-// Places the Y scores (through `count(lt, eq)`) into the sorted X and returns
+// Places the Y scores (through `count(lt, eq, dir)`) into the sorted X and returns
 // the two curve sums of launch_curve in res.
 template <class Count>
 int ev_curve(mcpg_handle* h, const uint32_t* X, int64_t nX, int64_t nY, const EvalWs& w, Count count, double res[2]) {
     if (nX >= ((int64_t)1 << 31)) return fail(h, MCPG_ERR_UNSUPPORTED, "evaluation: more than 2^31 - 1 sorted scores");
     void *hist, *tmp;
     int rc;
-    if ((rc = scratch(h, S_EV_HIST, (size_t)(4 * nX + 3) * 8, &hist))) return rc;
+    if ((rc = scratch(h, S_EV_HIST, (size_t)(4 * nX + 3) * 8 + (size_t)mcpg::rank_dir_elems() * 4, &hist))) return rc;
     if ((rc = scratch(h, S_EV_TMP, (size_t)mcpg::scan_tmp_elems(nX) * 8, &tmp))) return rc;
     uint64_t* lt = (uint64_t*)hist;
     uint64_t* eq = lt + nX + 1;
     uint64_t* work = eq + nX + 1;
+    uint32_t* dir = (uint32_t*)(work + 2 * nX + 1);
     {
         PROF(h, "rank_count");
-        CK(h, count(lt, eq), "rank count");
+        CK(h, count(lt, eq, dir), "rank count");
     }
     {
         PROF(h, "curve");
@@ -1168,7 +1169,7 @@ int ev_curve(mcpg_handle* h, const uint32_t* X, int64_t nX, int64_t nY, const Ev
 }
 
 // AUPR / AUROC from P positive keys kp (any order; sorted here in place), N
-// negatives ranked by neg_rank(X, nX, lt, eq), and -- only for the AUROC
+// negatives ranked by neg_rank(X, nX, lt, eq, dir), and -- only for the AUROC
 // branch n_pos >= n_neg > 0 -- compact negative keys from neg_keys(&kn).
 template <class NegRank, class NegKeys>
 int ev_aupr_auroc(mcpg_handle* h, const EvalWs& w, uint32_t* kp, int64_t P, int64_t N, NegRank neg_rank,
@@ -1178,7 +1179,9 @@ int ev_aupr_auroc(mcpg_handle* h, const EvalWs& w, uint32_t* kp, int64_t P, int6
     if (P > 0) {
         if ((rc = ev_sort(h, kp, P))) return rc;
         if ((rc = ev_curve(h, kp, P, N, w,
-                           [&](uint64_t* lt, uint64_t* eq) { return neg_rank((const uint32_t*)kp, P, lt, eq); },
+                           [&](uint64_t* lt, uint64_t* eq, uint32_t* dir) {
+                               return neg_rank((const uint32_t*)kp, P, lt, eq, dir);
+                           },
                            res)))
             return rc;
     }
@@ -1194,8 +1197,9 @@ int ev_aupr_auroc(mcpg_handle* h, const EvalWs& w, uint32_t* kp, int64_t P, int6
         if ((rc = ev_sort(h, kn, N))) return rc;
         double r2[2];
         if ((rc = ev_curve(h, kn, N, P, w,
-                           [&](uint64_t* lt, uint64_t* eq) {
-                               return mcpg::launch_rank_count_keys(kn, N, kp, P, lt, eq, h->stream, &h->launches);
+                           [&](uint64_t* lt, uint64_t* eq, uint32_t* dir) {
+                               return mcpg::launch_rank_count_keys(kn, N, kp, P, lt, eq, dir, h->stream,
+                                                                   &h->launches);
                            },
                            r2)))
             return rc;
@@ -1225,8 +1229,8 @@ int aupr_auroc_dev(mcpg_handle* h, const float* pos, int64_t P, const float* neg
     uint32_t* knk = (uint32_t*)kn;
     return ev_aupr_auroc(
         h, w, (uint32_t*)kp, P, N,
-        [&](const uint32_t* X, int64_t nX, uint64_t* lt, uint64_t* eq) {
-            return mcpg::launch_rank_count_keys(X, nX, knk, N, lt, eq, h->stream, &h->launches);
+        [&](const uint32_t* X, int64_t nX, uint64_t* lt, uint64_t* eq, uint32_t* dir) {
+            return mcpg::launch_rank_count_keys(X, nX, knk, N, lt, eq, dir, h->stream, &h->launches);
         },
         [&](uint32_t** out) {
             if (P == 0) {  // keys not made above
@@ -1320,8 +1324,8 @@ int eval_truth_dev(mcpg_handle* h, const float* values, int64_t ldv, const mcpg:
     }
     return ev_aupr_auroc(
         h, w, (uint32_t*)kp, P, N,
-        [&](const uint32_t* X, int64_t nX, uint64_t* lt, uint64_t* eq) {
-            return mcpg::launch_rank_count_matrix(X, nX, r, values, ldv, 0, lt, eq, w.flag, h->stream,
+        [&](const uint32_t* X, int64_t nX, uint64_t* lt, uint64_t* eq, uint32_t* dir) {
+            return mcpg::launch_rank_count_matrix(X, nX, r, values, ldv, 0, lt, eq, dir, w.flag, h->stream,
                                                   &h->launches);
         },
         [&](uint32_t** out) {
@@ -1425,8 +1429,8 @@ int combo_eval_dev(mcpg_handle* h, const float* const mats[4], const int64_t lds
         double a = 0.0, b = 0.0;
         rc = ev_aupr_auroc(
             h, w, (uint32_t*)kp, P, N,
-            [&](const uint32_t* X, int64_t nX, uint64_t* lt, uint64_t* eq) {
-                return mcpg::launch_rank_count_combo(X, nX, sn, lt, eq, w.flag, h->stream, &h->launches);
+            [&](const uint32_t* X, int64_t nX, uint64_t* lt, uint64_t* eq, uint32_t* dir) {
+                return mcpg::launch_rank_count_combo(X, nX, sn, lt, eq, dir, w.flag, h->stream, &h->launches);
             },
             [&](uint32_t** out) {
                 void* kn;
@@ -1827,8 +1831,8 @@ int split_aupr_range(mcpg_handle* h, const EvalWs& w, const SplitEntries& se, co
     double roc = 0.0;
     return ev_aupr_auroc(
         h, w, (uint32_t*)kp, P, N,
-        [&](const uint32_t* X, int64_t nX, uint64_t* lt, uint64_t* eq) {
-            return mcpg::launch_rank_count_keys(X, nX, knk, N, lt, eq, h->stream, &h->launches);
+        [&](const uint32_t* X, int64_t nX, uint64_t* lt, uint64_t* eq, uint32_t* dir) {
+            return mcpg::launch_rank_count_keys(X, nX, knk, N, lt, eq, dir, h->stream, &h->launches);
         },
         [&](uint32_t** out) {
             *out = knk;

@@ -49,11 +49,19 @@ constexpr int RS_THREADS = 256;                      // radix sort
 constexpr int RS_WARPS = RS_THREADS / 32;
 constexpr int RS_ITEMS = 16;
 constexpr int RS_TILE = RS_THREADS * RS_ITEMS;
-constexpr int RC_SKEYS = 8192;                       // keys (or splitters) of X held in shared memory
+// Directory width and CTAs per SM: 20 bits (a 4 MB directory, L2-resident) and 4 CTAs
+// measured best of 16/18/20 bits x 3/4 CTAs on the evaluations of a 32,768-gene network.
+#ifndef MCPG_RC_DIR_BITS
+#define MCPG_RC_DIR_BITS 20
+#endif
+#ifndef MCPG_RC_MINB
+#define MCPG_RC_MINB 4
+#endif
+constexpr int RC_DIR_BITS = MCPG_RC_DIR_BITS;        // key prefix bits of the directory of X
+constexpr int64_t RC_DIR = ((int64_t)1 << RC_DIR_BITS) + 1;  // its entries
 constexpr int RC_SBINS = 4096;                       // histogram bins held in shared memory
 constexpr int RC_SLOW = 3072;                        // ... when |X| + 1 > RC_SBINS: the lowest bins
 constexpr int RC_SHIGH = RC_SBINS - RC_SLOW;         //     and the highest (scores below / above most of X)
-constexpr size_t RC_SMEM = (size_t)RC_SKEYS * 4 + (size_t)2 * RC_SBINS * 4;
 constexpr int RC_BATCH = EV_PER_THREAD;              // keys placed per thread per call
 
 __device__ __forceinline__ uint32_t order_key(float f) {
@@ -356,18 +364,35 @@ __global__ void __launch_bounds__(RS_THREADS) radix_scatter_kernel(const uint32_
 }
 
 // ---- rank counting: place every Y score into the sorted X by lower_bound ----
+// The directory D[b] = lower_bound(X, b << (32 - RC_DIR_BITS)), b = 0 .. 2^RC_DIR_BITS,
+// places a key in one look-up when no X key shares its prefix, and otherwise
+// narrows its search to the X keys of that prefix.
+__global__ void rank_dir_kernel(const uint32_t* X, int64_t nX, uint32_t* D) {
+    for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < RC_DIR; b += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t key = (uint64_t)b << (32 - RC_DIR_BITS);
+        int64_t lo = 0, n = nX;
+        while (n > 0) {
+            const int64_t half = n >> 1;
+            if ((uint64_t)X[lo + half] < key) {
+                lo += half + 1;
+                n -= half + 1;
+            } else {
+                n = half;
+            }
+        }
+        D[b] = (uint32_t)lo;
+    }
+}
+
 struct RankCtx {
     const uint32_t* X;
     int64_t nX;
     uint64_t* lt;
     uint64_t* eq;
-    const uint32_t* sk;  // shared: all of X (full) or splitters X[q * stride]
+    const uint32_t* D;   // directory of X
     uint32_t* shl;       // shared histogram windows (RC_SBINS bins each)
     uint32_t* she;
-    int64_t stride;
     int64_t hi0;         // first bin of the high window (bins >= hi0 map to RC_SLOW + bin - hi0)
-    int nsk;
-    bool full;
 
     // Shared-memory slot of a bin, or -1 for the global histogram.  Scores of
     // the negatives of a network pile up below (or above) most positives, so
@@ -379,53 +404,36 @@ struct RankCtx {
         return -1;
     }
 
-    // Places RC_BATCH keys per thread (has[j] false: no key).  The lower_bound
-    // searches run interleaved over the batch ("monobound": every key takes
-    // the same number of steps, so the loads of one step are independent).
-    // Every lane of the warp calls this (ballot / match inside).
+    // Places RC_BATCH keys per thread (has[j] false: no key): the directory
+    // gives each key's range of X keys with the same prefix, and lower_bound
+    // searches those ranges interleaved over the batch (the loads of one step
+    // are independent).  Every lane of the warp calls this (ballot / match inside).
     __device__ __forceinline__ void place(const bool (&has)[RC_BATCH], const uint32_t (&key)[RC_BATCH]) const {
-        int base[RC_BATCH];
+        int lo[RC_BATCH], n[RC_BATCH];
 #pragma unroll
-        for (int j = 0; j < RC_BATCH; ++j) base[j] = 0;
-        if (nsk > 0) {
-            int n = nsk;
-            while (n > 1) {
-                const int half = n >> 1;
-#pragma unroll
-                for (int j = 0; j < RC_BATCH; ++j) base[j] = sk[base[j] + half] < key[j] ? base[j] + half : base[j];
-                n -= half;
-            }
-#pragma unroll
-            for (int j = 0; j < RC_BATCH; ++j) base[j] += sk[base[j]] < key[j] ? 1 : 0;
+        for (int j = 0; j < RC_BATCH; ++j) {
+            const uint32_t b = key[j] >> (32 - RC_DIR_BITS);
+            lo[j] = (int)__ldg(D + b);
+            n[j] = has[j] ? (int)__ldg(D + b + 1) - lo[j] : 0;
         }
-        int bin[RC_BATCH];  // nX < 2^31
-        if (full) {
+        for (;;) {
+            bool any = false;
 #pragma unroll
-            for (int j = 0; j < RC_BATCH; ++j) bin[j] = base[j];
-        } else {
-            // the answer lies in [(q-1)*stride + 1, min(q*stride, nX)] for q = base >= 1
-            const int nx = (int)nX, st = (int)stride;
-#pragma unroll
-            for (int j = 0; j < RC_BATCH; ++j) bin[j] = base[j] > 0 ? (base[j] - 1) * st + 1 : 0;
-            int n = st - 1;
-            while (n > 1) {
-                const int half = n >> 1;
-#pragma unroll
-                for (int j = 0; j < RC_BATCH; ++j) {
-                    const int idx = bin[j] + half;
-                    const bool lt = base[j] > 0 && idx < nx && __ldg(X + idx) < key[j];
-                    bin[j] = lt ? idx : bin[j];
+            for (int j = 0; j < RC_BATCH; ++j) {
+                if (n[j] > 0) {
+                    const int half = n[j] >> 1;
+                    const bool below = __ldg(X + lo[j] + half) < key[j];
+                    lo[j] = below ? lo[j] + half + 1 : lo[j];
+                    n[j] = below ? n[j] - half - 1 : half;
+                    any = true;
                 }
-                n -= half;
             }
-#pragma unroll
-            for (int j = 0; j < RC_BATCH; ++j)
-                bin[j] += (base[j] > 0 && n == 1 && bin[j] < nx && __ldg(X + bin[j]) < key[j]) ? 1 : 0;
+            if (!any) break;
         }
 #pragma unroll
         for (int j = 0; j < RC_BATCH; ++j) {
-            const bool e = has[j] && bin[j] < (int)nX && (full ? sk[bin[j]] : __ldg(X + bin[j])) == key[j];
-            const uint32_t b = (uint32_t)bin[j];
+            const bool e = has[j] && lo[j] < (int)nX && __ldg(X + lo[j]) == key[j];
+            const uint32_t b = (uint32_t)lo[j];
             const uint32_t act = __ballot_sync(FULL, has[j]);
             if (has[j]) {
                 const uint32_t peers = __match_any_sync(act, (b << 1) | (e ? 1u : 0u));
@@ -512,26 +520,19 @@ struct YCombo {  // combo values of gathered (mi, M1, M2, M3) tuples
 };
 
 template <class Y>
-__global__ void __launch_bounds__(EV_THREADS, 3) rank_count_kernel(const uint32_t* X, int64_t nX, Y y, uint64_t* lt,
-                                                                uint64_t* eq, int* nan_flag) {
-    extern __shared__ __align__(16) uint32_t rc_smem[];
-    uint32_t* sk = rc_smem;
-    uint32_t* shl = sk + RC_SKEYS;
-    uint32_t* she = shl + RC_SBINS;
+__global__ void __launch_bounds__(EV_THREADS, MCPG_RC_MINB) rank_count_kernel(const uint32_t* X, int64_t nX, const uint32_t* D,
+                                                                Y y, uint64_t* lt, uint64_t* eq, int* nan_flag) {
+    __shared__ uint32_t shl[RC_SBINS], she[RC_SBINS];
     RankCtx c;
     c.X = X;
     c.nX = nX;
     c.lt = lt;
     c.eq = eq;
-    c.sk = sk;
+    c.D = D;
     c.shl = shl;
     c.she = she;
-    c.full = nX <= RC_SKEYS;
-    c.stride = c.full ? 1 : ceil_div(nX, RC_SKEYS);
-    c.nsk = (int)(c.full ? nX : ceil_div(nX, c.stride));
     c.hi0 = nX + 1 <= RC_SBINS ? (int64_t)RC_SLOW : nX + 1 - RC_SHIGH;
     const int nsb = nX + 1 <= RC_SBINS ? (int)(nX + 1) : RC_SBINS;  // used slots
-    for (int i = threadIdx.x; i < c.nsk; i += blockDim.x) sk[i] = X[(int64_t)i * c.stride];
     for (int i = threadIdx.x; i < RC_SBINS; i += blockDim.x) shl[i] = she[i] = 0;
     __syncthreads();
     const bool bad = y.run(c);
@@ -689,6 +690,7 @@ int64_t truth_items(const TruthRegion& r) {
 int64_t scan_tmp_elems(int64_t n) { return ceil_div(n > 0 ? n : 1, SC_TILE); }
 int64_t radix_blocks(int64_t n) { return ceil_div(n > 0 ? n : 1, RS_TILE); }
 int64_t curve_part_elems() { return 4 * CV_MAX_BLOCKS; }
+int64_t rank_dir_elems() { return RC_DIR; }
 
 cudaError_t launch_truth_count(const TruthRegion& r, uint32_t* cpos, uint32_t* cneg, cudaStream_t st,
                                int64_t* launches) {
@@ -768,60 +770,50 @@ cudaError_t launch_radix_sort(uint32_t* keys, uint32_t* alt, int64_t n, uint32_t
     return cudaGetLastError();  // four passes: the result is back in keys
 }
 
-static cudaError_t rank_prep(int64_t nX, uint64_t* lt, uint64_t* eq, cudaStream_t st) {
-    static uint64_t attr_done = 0;  // opt in to the 64 KB of dynamic shared memory once per device
-    int dev = 0;
-    cudaGetDevice(&dev);
-    const uint64_t bit = 1ull << (dev & 63);
-    if (!(attr_done & bit)) {
-        cudaError_t a = cudaFuncSetAttribute(rank_count_kernel<YMatrix>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)RC_SMEM);
-        if (a == cudaSuccess)
-            a = cudaFuncSetAttribute(rank_count_kernel<YKeys>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)RC_SMEM);
-        if (a == cudaSuccess)
-            a = cudaFuncSetAttribute(rank_count_kernel<YCombo>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)RC_SMEM);
-        if (a != cudaSuccess) return a;
-        attr_done |= bit;
-    }
+// Zeroes the histograms and builds the directory of X.
+static cudaError_t rank_prep(const uint32_t* X, int64_t nX, uint64_t* lt, uint64_t* eq, uint32_t* dir,
+                             cudaStream_t st, int64_t* launches) {
     cudaError_t e = cudaMemsetAsync(lt, 0, (size_t)(nX + 1) * sizeof(uint64_t), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(eq, 0, (size_t)(nX + 1) * sizeof(uint64_t), st);
-    return e;
+    if (e != cudaSuccess) return e;
+    rank_dir_kernel<<<grid_for(RC_DIR, 256, 152 * 2), 256, 0, st>>>(X, nX, dir);
+    if (launches) ++*launches;
+    return cudaGetLastError();
 }
 
 cudaError_t launch_rank_count_matrix(const uint32_t* X, int64_t nX, const TruthRegion& r, const float* v, int64_t ldv,
-                                     int lab, uint64_t* lt, uint64_t* eq, int* nan_flag, cudaStream_t st,
-                                     int64_t* launches) {
+                                     int lab, uint64_t* lt, uint64_t* eq, uint32_t* dir, int* nan_flag,
+                                     cudaStream_t st, int64_t* launches) {
     if (nX <= 0 || nX >= (int64_t)1 << 31) return cudaErrorInvalidValue;
-    cudaError_t e = rank_prep(nX, lt, eq, st);
+    cudaError_t e = rank_prep(X, nX, lt, eq, dir, st, launches);
     if (e != cudaSuccess) return e;
     const int64_t items = truth_items(r);
     if (items == 0) return cudaSuccess;
     YMatrix y{r, ceil_div(r.cols, EV_CHUNK), items, v, ldv, lab};
-    rank_count_kernel<YMatrix><<<grid_for(items, 1, 152 * 3), EV_THREADS, RC_SMEM, st>>>(X, nX, y, lt, eq, nan_flag);
+    rank_count_kernel<YMatrix><<<grid_for(items, 1, 152 * MCPG_RC_MINB), EV_THREADS, 0, st>>>(X, nX, dir, y, lt, eq, nan_flag);
     if (launches) ++*launches;
     return cudaGetLastError();
 }
 
 cudaError_t launch_rank_count_keys(const uint32_t* X, int64_t nX, const uint32_t* Y, int64_t nY, uint64_t* lt,
-                                   uint64_t* eq, cudaStream_t st, int64_t* launches) {
+                                   uint64_t* eq, uint32_t* dir, cudaStream_t st, int64_t* launches) {
     if (nX <= 0 || nX >= (int64_t)1 << 31) return cudaErrorInvalidValue;
-    cudaError_t e = rank_prep(nX, lt, eq, st);
+    cudaError_t e = rank_prep(X, nX, lt, eq, dir, st, launches);
     if (e != cudaSuccess || nY <= 0) return e;
     YKeys y{Y, nY};
-    rank_count_kernel<YKeys><<<grid_for(nY, EV_CHUNK, 152 * 3), EV_THREADS, RC_SMEM, st>>>(X, nX, y, lt, eq, nullptr);
+    rank_count_kernel<YKeys><<<grid_for(nY, EV_CHUNK, 152 * MCPG_RC_MINB), EV_THREADS, 0, st>>>(X, nX, dir, y, lt, eq, nullptr);
     if (launches) ++*launches;
     return cudaGetLastError();
 }
 
 cudaError_t launch_rank_count_combo(const uint32_t* X, int64_t nX, const ComboSrc& c, uint64_t* lt, uint64_t* eq,
-                                    int* nan_flag, cudaStream_t st, int64_t* launches) {
+                                    uint32_t* dir, int* nan_flag, cudaStream_t st, int64_t* launches) {
     if (nX <= 0 || nX >= (int64_t)1 << 31) return cudaErrorInvalidValue;
-    cudaError_t e = rank_prep(nX, lt, eq, st);
+    cudaError_t e = rank_prep(X, nX, lt, eq, dir, st, launches);
     if (e != cudaSuccess || c.n <= 0) return e;
     YCombo y{c};
-    rank_count_kernel<YCombo><<<grid_for(c.n, EV_CHUNK, 152 * 3), EV_THREADS, RC_SMEM, st>>>(X, nX, y, lt, eq, nan_flag);
+    rank_count_kernel<YCombo><<<grid_for(c.n, EV_CHUNK, 152 * MCPG_RC_MINB), EV_THREADS, 0, st>>>(X, nX, dir, y, lt, eq,
+                                                                                      nan_flag);
     if (launches) ++*launches;
     return cudaGetLastError();
 }

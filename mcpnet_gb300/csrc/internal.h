@@ -197,13 +197,15 @@ cudaError_t launch_radix_sort(uint32_t* keys, uint32_t* alt, int64_t n, uint32_t
                               uint64_t* tmp, cudaStream_t stream, int64_t* launches);
 // lt[i] / eq[i] (nX + 1 each, zeroed here) = number of Y keys whose lower_bound
 // in the sorted X is i and that are < X[i] / == X[i].  nX in [1, 2^31).
+// dir: rank_dir_elems() scratch for the key-prefix directory of X (built here).
+int64_t rank_dir_elems();
 cudaError_t launch_rank_count_matrix(const uint32_t* X, int64_t nX, const TruthRegion& r, const float* v, int64_t ldv,
-                                     int lab, uint64_t* lt, uint64_t* eq, int* nan_flag, cudaStream_t stream,
-                                     int64_t* launches);
+                                     int lab, uint64_t* lt, uint64_t* eq, uint32_t* dir, int* nan_flag,
+                                     cudaStream_t stream, int64_t* launches);
 cudaError_t launch_rank_count_keys(const uint32_t* X, int64_t nX, const uint32_t* Y, int64_t nY, uint64_t* lt,
-                                   uint64_t* eq, cudaStream_t stream, int64_t* launches);
+                                   uint64_t* eq, uint32_t* dir, cudaStream_t stream, int64_t* launches);
 cudaError_t launch_rank_count_combo(const uint32_t* X, int64_t nX, const ComboSrc& c, uint64_t* lt, uint64_t* eq,
-                                    int* nan_flag, cudaStream_t stream, int64_t* launches);
+                                    uint32_t* dir, int* nan_flag, cudaStream_t stream, int64_t* launches);
 // out[0] = sum of AUPR terms (X = positives, Y = negatives), out[1] = sum of
 // AUROC terms (#Y >= t / |Y|) (run / |X|) over the distinct thresholds t of X.
 // work: 2*nX + 1; tmp: scan_tmp_elems(nX); part: curve_part_elems().
