@@ -62,7 +62,13 @@ constexpr int64_t RC_DIR = ((int64_t)1 << RC_DIR_BITS) + 1;  // its entries
 constexpr int RC_SBINS = 4096;                       // histogram bins held in shared memory
 constexpr int RC_SLOW = 3072;                        // ... when |X| + 1 > RC_SBINS: the lowest bins
 constexpr int RC_SHIGH = RC_SBINS - RC_SLOW;         //     and the highest (scores below / above most of X)
-constexpr int RC_BATCH = EV_PER_THREAD;              // keys placed per thread per call
+// Keys per thread per step: 8 (with 4 CTAs) measured best of 16 / 8 / 4 keys x 4-6 CTAs per SM on
+// a 32,768-gene network (MI 9.8 ms, MCP2 11.6 ms, combo search 8.6 ms per row).
+#ifndef MCPG_RC_BATCH
+#define MCPG_RC_BATCH 8
+#endif
+constexpr int RC_BATCH = MCPG_RC_BATCH;              // keys placed per thread per call (divides EV_PER_THREAD)
+static_assert(EV_PER_THREAD % RC_BATCH == 0, "rank-count batch");
 
 __device__ __forceinline__ uint32_t order_key(float f) {
     uint32_t u = __float_as_uint(f);
@@ -461,17 +467,19 @@ struct YMatrix {  // selected entries of one label in a score matrix
             if (s.c0 >= s.c1) continue;  // uniform over the block
             const int8_t* lrow = r.labels + s.row * r.ldl;
             const float* vrow = v + s.row * ldv;
-            bool has[RC_BATCH];
-            uint32_t key[RC_BATCH];
+            for (int k0 = 0; k0 < EV_PER_THREAD; k0 += RC_BATCH) {  // the thread's segment, a batch at a time
+                bool has[RC_BATCH];
+                uint32_t key[RC_BATCH];
 #pragma unroll
-            for (int k = 0; k < RC_BATCH; ++k) {  // RC_BATCH == EV_PER_THREAD: the thread's whole segment
-                const int64_t col = s.c0 + k * EV_THREADS + threadIdx.x;
-                has[k] = col < s.c1 && in_region(r, s.row, col) && lrow[col] == lab;
-                const float f = has[k] ? vrow[col] : 0.0f;
-                bad |= has[k] && is_nan(f);
-                key[k] = order_key(f);
+                for (int k = 0; k < RC_BATCH; ++k) {
+                    const int64_t col = s.c0 + (k0 + k) * EV_THREADS + threadIdx.x;
+                    has[k] = col < s.c1 && in_region(r, s.row, col) && lrow[col] == lab;
+                    const float f = has[k] ? vrow[col] : 0.0f;
+                    bad |= has[k] && is_nan(f);
+                    key[k] = order_key(f);
+                }
+                c.place(has, key);
             }
-            c.place(has, key);
         }
         return bad;
     }
@@ -483,15 +491,17 @@ struct YKeys {  // a compact array of keys
     __device__ __forceinline__ bool run(const RankCtx& c) const {
         const int64_t step = (int64_t)gridDim.x * EV_CHUNK;
         for (int64_t i0 = (int64_t)blockIdx.x * EV_CHUNK; i0 < n; i0 += step) {
-            bool has[RC_BATCH];
-            uint32_t key[RC_BATCH];
+            for (int k0 = 0; k0 < EV_PER_THREAD; k0 += RC_BATCH) {
+                bool has[RC_BATCH];
+                uint32_t key[RC_BATCH];
 #pragma unroll
-            for (int j = 0; j < RC_BATCH; ++j) {
-                const int64_t i = i0 + j * EV_THREADS + threadIdx.x;
-                has[j] = i < n;
-                key[j] = has[j] ? k[i] : 0u;
+                for (int j = 0; j < RC_BATCH; ++j) {
+                    const int64_t i = i0 + (k0 + j) * EV_THREADS + threadIdx.x;
+                    has[j] = i < n;
+                    key[j] = has[j] ? k[i] : 0u;
+                }
+                c.place(has, key);
             }
-            c.place(has, key);
         }
         return false;
     }
@@ -503,17 +513,19 @@ struct YCombo {  // combo values of gathered (mi, M1, M2, M3) tuples
         bool bad = false;
         const int64_t step = (int64_t)gridDim.x * EV_CHUNK;
         for (int64_t i0 = (int64_t)blockIdx.x * EV_CHUNK; i0 < s.n; i0 += step) {
-            bool has[RC_BATCH];
-            uint32_t key[RC_BATCH];
+            for (int k0 = 0; k0 < EV_PER_THREAD; k0 += RC_BATCH) {
+                bool has[RC_BATCH];
+                uint32_t key[RC_BATCH];
 #pragma unroll
-            for (int j = 0; j < RC_BATCH; ++j) {
-                const int64_t i = i0 + j * EV_THREADS + threadIdx.x;
-                has[j] = i < s.n;
-                const float f = has[j] ? combo_at(s, i) : 0.0f;
-                bad |= has[j] && is_nan(f);
-                key[j] = order_key(f);
+                for (int j = 0; j < RC_BATCH; ++j) {
+                    const int64_t i = i0 + (k0 + j) * EV_THREADS + threadIdx.x;
+                    has[j] = i < s.n;
+                    const float f = has[j] ? combo_at(s, i) : 0.0f;
+                    bad |= has[j] && is_nan(f);
+                    key[j] = order_key(f);
+                }
+                c.place(has, key);
             }
-            c.place(has, key);
         }
         return bad;
     }
