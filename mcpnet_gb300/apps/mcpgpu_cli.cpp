@@ -11,6 +11,7 @@
 //   mcpgpu_cli transform -i mi.exp -o out.exp -m {1,2} [-f tfs.txt]   (1 = CLR, 2 = Stouffer)
 //   mcpgpu_cli eval_mcpnet (-i expr.exp [--mi-method 0] | --mi-file mi.exp) (-g truth.txt | -x truth.exp)
 //                     [-m 1 2 3 4 5] [-f coeffs.exp] [--iterations 100] [--diagonal 0] [--tf-input tfs.txt]
+//   mcpgpu_cli auc_pr_roc -i scores.exp (-g truth.txt | -x truth.exp)
 //   mcpgpu_cli convert -i a.exp -o b.csv          (no GPU needed)
 //
 // Method values keep the reference's numbering and add the GPU forms:
@@ -34,6 +35,9 @@
 // each row's mean and unbiased sd without its diagonal entry (GaussianParamsExclude1); with
 // -f, the TF rows z-scored by row and by column (StandardScore) and combined by
 // zscored_clr_kernel / zscored_stouffer_kernel (transform.cpp:156-209).
+// auc_pr_roc (apps/transform/auc_pr_roc.cpp) prints `Computed,aupr <a>,,<sec>,sec` and
+// `Computed,auroc <b>,,<sec>,sec` of a score matrix against the truth (list: the listed
+// pairs; matrix: below the diagonal).
 // eval_mcpnet (apps/pipeline/eval_mcpnet.cpp) prints the semi-supervised evaluation:
 // for MI and each MCP requested, the AUPR of the labelled entries and, over
 // --iterations shuffles of them (std::shuffle, std::mt19937 seeded 1, 2, ...), the
@@ -189,7 +193,8 @@ struct Args {
 Args parse(int argc, char** argv) {
     Args a;
     if (argc < 2)
-        throw std::runtime_error("usage: mcpgpu_cli {mi|mcp|dpi|mcpnet|transform|convert} -i IN -o OUT [options]");
+        throw std::runtime_error(
+            "usage: mcpgpu_cli {mi|mcp|dpi|mcpnet|eval_mcpnet|transform|auc_pr_roc|convert} -i IN [-o OUT] [options]");
     a.cmd = argv[1];
     for (int i = 2; i < argc; ++i) {
         std::string k = argv[i];
@@ -233,6 +238,13 @@ Args parse(int argc, char** argv) {
         else if (k == "--seed") a.seed = std::strtoull(next().c_str(), nullptr, 10);
         else if (k == "--tf-input") a.tf_input = next();
         else throw std::runtime_error("unknown option " + k);
+    }
+    if (a.cmd == "auc_pr_roc") {
+        if (a.in.empty()) throw std::runtime_error("auc_pr_roc needs -i (score matrix)");
+        if (a.truth_list.empty() == a.truth_mat.empty())
+            throw std::runtime_error("auc_pr_roc needs exactly one of -g (truth list) and -x (truth matrix)");
+        a.eval = true;
+        return a;
     }
     if (a.cmd == "eval_mcpnet") {
         if (a.in.empty() == a.mi_file.empty())
@@ -524,6 +536,14 @@ int main(int argc, char** argv) {
             }
             std::printf("Transformed in %.6f sec\n", now_s() - t0);
             write_matrix(a.out, out, tf.on ? tf.names : in.rows, in.rows);
+        } else if (a.cmd == "auc_pr_roc") {  // apps/transform/auc_pr_roc.cpp:380-460
+            if (in.m.rows() != in.m.columns()) throw std::runtime_error("auc_pr_roc needs a square score matrix");
+            const Truth truth = read_truth(a, in.rows, tf);
+            const double t1 = now_s();
+            const mcpgpu::Curves c = mcpgpu::compute_aupr_auroc(ctx, truth.labels, in.m, truth.region);
+            const double dt = now_s() - t1;
+            std::printf("Computed,aupr %.12g,,%.6f,sec\n", c.aupr, dt);
+            std::printf("Computed,auroc %.12g,,%.6f,sec\n", c.auroc, dt);
         } else if (a.cmd == "eval_mcpnet") {  // apps/pipeline/eval_mcpnet.cpp:464-893
             const std::vector<std::string>& genes = in.rows;
             Truth truth = read_truth(a, genes, tf);

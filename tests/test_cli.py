@@ -382,3 +382,36 @@ def test_cli_eval_mcpnet(built_lib, port, tmp_path):
         want = _stats(res[:, j, 4], iters)
         full_lines = {k: v for k, v in got.items() if k[0].startswith("full ")}
         assert abs(full_lines[("full min", j, iters)] - want[0]) <= 1e-11
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("truth", ["matrix", "list"])
+def test_cli_auc_pr_roc(built_lib, port, tmp_path, truth):
+    """auc_pr_roc: AUPR / AUROC of a score matrix against a truth matrix (below the
+    diagonal) or list (the listed pairs), as the oracle's compute_aupr_auroc."""
+    n = 50
+    X, E = built_lib.synth_grn(n, 180, seed=26, with_edges=True)
+    A = port.bspline_mi(X)
+    names = [f"g{i}" for i in range(n)]
+    write_exp(tmp_path / "s.exp", A, names)
+    L = np.zeros((n, n), np.int8)
+    for s_, t in E:
+        L[s_, t] = L[t, s_] = 1
+    if truth == "matrix":
+        write_exp(tmp_path / "t.exp", L.astype(np.float32), names)
+        targ, region, Lw = ["-x", tmp_path / "t.exp"], "lower", L
+    else:
+        Lw = np.full((n, n), -1, np.int8)
+        with open(tmp_path / "t.txt", "w") as f:
+            for i in range(n):
+                for j in range(n):
+                    if i != j and (i + j) % 3 == 0:
+                        f.write(f"g{i}\tg{j}\t{L[i, j]}\n")
+                        Lw[i, j] = L[i, j]
+        targ, region = ["-g", tmp_path / "t.txt"], "all"
+    r = run("auc_pr_roc", "-i", tmp_path / "s.exp", *targ)
+    assert r.returncode == 0, r.stderr
+    got = {l.split(",")[1].split()[0]: float(l.split(",")[1].split()[1]) for l in r.stdout.splitlines()
+           if l.startswith("Computed,au")}
+    a, b, _, _ = port.eval_truth(read_exp(tmp_path / "s.exp"), Lw, region)
+    assert abs(got["aupr"] - a) <= 1e-11 and abs(got["auroc"] - b) <= 1e-11
