@@ -277,8 +277,9 @@ def gpu_arm(args, ws, rank, local):
                 "frac": achieved_tf / peak_tf, "traffic": traffic[0] if traffic else None,
                 "traffic_source": traffic[1] if traffic else None, "peak_source": peak_src,
                 "kernel_ms": k_ms, "algorithmic_flop_per_launch": flops,
-                "note": "achieved counts 2*b^2*m flops per unordered gene pair; the hi+lo split issues 3x "
-                        "that on the tensor pipe"}
+                "note": "achieved counts 2*b^2*m flops per unordered gene pair; the BF16 hi+lo split issues 3x "
+                        "that on the tensor pipe, the FP8-corrected form (bf16f8) 1x BF16 + 2x FP8 (the "
+                        "time of 2x BF16)"}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
@@ -674,7 +675,7 @@ def main(argv=None):
     ap.add_argument("--samples", type=int, default=2000)
     ap.add_argument("--bins", type=int, default=10)
     ap.add_argument("--order", type=int, default=3)
-    ap.add_argument("--precision", default="bf16x3", choices=["fp32", "bf16", "bf16x3", "fp16", "fp16x3"])
+    ap.add_argument("--precision", default="bf16x3", choices=["fp32", "bf16", "bf16x3", "fp16", "fp16x3", "bf16f8"])
     ap.add_argument("--mi-method", default="bspline", choices=["bspline", "ap"],
                     help="with --pipeline: B-spline MI (default) or adaptive-partitioning MI (U[0,1e-5) noise)")
     ap.add_argument("--seed", type=int, default=20260001)

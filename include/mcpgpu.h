@@ -57,6 +57,8 @@ typedef struct mcpg_handle mcpg_handle;
 #define MCPG_MI_BF16X3 2 /* hi+lo BF16 split: hi*hi' + hi*lo' + lo*hi' on tcgen05 */
 #define MCPG_MI_FP16 3   /* weights rounded once to FP16, tcgen05 */
 #define MCPG_MI_FP16X3 4 /* hi+lo FP16 split on tcgen05 */
+#define MCPG_MI_BF16F8 5 /* BF16 hi*hi' (tcgen05 kind::f16) plus an E4M3 hi*lo' + lo*hi' correction
+                            (kind::f8f6f4, twice the rate) in the same FP32 accumulator */
 
 /* ---- library / handle ---- */
 MCPG_API int mcpg_version(void);

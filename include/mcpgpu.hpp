@@ -96,6 +96,7 @@ enum class MIPrecision : int {
     BF16X3 = MCPG_MI_BF16X3,
     FP16 = MCPG_MI_FP16,
     FP16X3 = MCPG_MI_FP16X3,
+    BF16F8 = MCPG_MI_BF16F8,
 };
 
 // compute_mi: scale -> B-spline weights (order 3, as the reference hard-codes)

@@ -31,7 +31,7 @@ LIB_PATH = _PKG / "_lib" / "libmcpgpu.so"
 
 OK, ERR_ARG, ERR_OOM, ERR_CUDA, ERR_NOT_CONVERGED, ERR_UNSUPPORTED, ERR_DEVICE_TIMEOUT = 0, -1, -2, -3, -4, -5, -6
 ERR_SCRATCH_LIMIT = -7
-PRECISIONS = {"fp32": 0, "bf16": 1, "bf16x3": 2, "fp16": 3, "fp16x3": 4}
+PRECISIONS = {"fp32": 0, "bf16": 1, "bf16x3": 2, "fp16": 3, "fp16x3": 4, "bf16f8": 5}
 
 # (name, restype, argtypes) of every exported symbol -- the full C ABI.
 _i64, _f32p, _f64p, _vp = C.c_int64, C.POINTER(C.c_float), C.POINTER(C.c_double), C.c_void_p

@@ -287,10 +287,11 @@ int finish(mcpg_handle* h) {
 // ---------------- device implementations ----------------
 // ---- B-spline MI in three steps: weights (prepare), gene-range launches, finish ----
 struct MiPlan {
-    int precision = 0, fmt = 0, split = 0, bins = 0;
+    int precision = 0, fmt = 0, split = 0, bins = 0;  // split: mcpg::TcMode
     int64_t n = 0, m = 0;
     const void* w0 = nullptr;  // FP32 sample-major or 16-bit hi weights
-    const void* w1 = nullptr;  // 16-bit lo weights
+    const void* w1 = nullptr;  // 16-bit lo weights, or the E4M3 H8 plane (split 2)
+    const void* w2 = nullptr;  // E4M3 L8 plane (split 2)
     int64_t ld = 0;            // weight leading dimension
     double* H = nullptr;
     float* MI = nullptr;
@@ -307,7 +308,7 @@ int mi_prepare(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_t ldx
     if (bins < 1 || bins > 32 || order < 1 || order > 8 || bins < order)
         return fail(h, MCPG_ERR_ARG, "bspline_mi: need 1 <= order <= bins <= 32, order <= 8 (got bins=%d order=%d)",
                     bins, order);
-    if (precision < MCPG_MI_FP32 || precision > MCPG_MI_FP16X3)
+    if (precision < MCPG_MI_FP32 || precision > MCPG_MI_BF16F8)
         return fail(h, MCPG_ERR_ARG, "bspline_mi: unknown precision %d", precision);
     pl = MiPlan{};
     pl.precision = precision; pl.bins = bins; pl.n = n; pl.m = m; pl.MI = MI; pl.ldmi = ldmi; pl.H = H;
@@ -334,17 +335,31 @@ int mi_prepare(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_t ldx
     }
     if (bins != 10) return fail(h, MCPG_ERR_UNSUPPORTED, "bspline_mi tensor-core path: only 10 bins (got %d)", bins);
     pl.fmt = (precision == MCPG_MI_FP16 || precision == MCPG_MI_FP16X3) ? 1 : 0;
-    pl.split = (precision == MCPG_MI_BF16X3 || precision == MCPG_MI_FP16X3) ? 1 : 0;
+    pl.split = (precision == MCPG_MI_BF16X3 || precision == MCPG_MI_FP16X3) ? mcpg::TC_SPLIT16
+               : precision == MCPG_MI_BF16F8                                ? mcpg::TC_F8C
+                                                                            : mcpg::TC_SINGLE;
     const int64_t ldw = round_up(m, 64);
     const int64_t rows = round_up(n * bins, 256) + 256;  // whole tiles stay in bounds
+    // S_W1: the 16-bit lo plane, or the two 8-bit planes H8 | L8 (the same bytes)
     void *hi, *lo = nullptr;
     if ((rc = scratch(h, S_W0, (size_t)(rows * ldw) * 2, &hi))) return rc;
     if (pl.split && (rc = scratch(h, S_W1, (size_t)(rows * ldw) * 2, &lo))) return rc;
+    uint8_t* l8 = pl.split == mcpg::TC_F8C ? (uint8_t*)lo + (size_t)(rows * ldw) : nullptr;
     // rows beyond n*bins must be zero (they are read by the last tiles)
-    const size_t tail = (size_t)((rows - n * bins) * ldw) * 2;
-    CK(h, cudaMemsetAsync((char*)hi + (size_t)(n * bins * ldw) * 2, 0, tail, h->stream), "memset weights");
-    if (lo) CK(h, cudaMemsetAsync((char*)lo + (size_t)(n * bins * ldw) * 2, 0, tail, h->stream), "memset weights");
-    {
+    const size_t done = (size_t)(n * bins * ldw), tail = (size_t)((rows - n * bins) * ldw);
+    CK(h, cudaMemsetAsync((char*)hi + done * 2, 0, tail * 2, h->stream), "memset weights");
+    if (pl.split == mcpg::TC_SPLIT16)
+        CK(h, cudaMemsetAsync((char*)lo + done * 2, 0, tail * 2, h->stream), "memset weights");
+    if (l8) {
+        CK(h, cudaMemsetAsync((char*)lo + done, 0, tail, h->stream), "memset weights");
+        CK(h, cudaMemsetAsync(l8 + done, 0, tail, h->stream), "memset weights");
+    }
+    if (l8) {
+        PROF(h, "bspline_weights_f8");
+        CK(h, mcpg::launch_bspline_weights_f8(X, n, m, ldx, bins, order, (uint16_t*)hi, (uint8_t*)lo, l8, ldw, pl.H,
+                                               h->stream, &h->launches),
+           "bspline weights kernel");
+    } else {
         PROF(h, "bspline_weights16");
         CK(h, mcpg::launch_bspline_weights_16(X, n, m, ldx, bins, order, pl.fmt, (uint16_t*)hi, (uint16_t*)lo, ldw,
                                                pl.H, h->stream, &h->launches),
@@ -353,7 +368,7 @@ int mi_prepare(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_t ldx
     void* flag;
     if ((rc = scratch(h, S_SMALL, 64, &flag))) return rc;
     CK(h, cudaMemsetAsync(flag, 0, sizeof(int), h->stream), "memset flag");
-    pl.w0 = hi; pl.w1 = lo; pl.ld = ldw; pl.flag = (int*)flag;
+    pl.w0 = hi; pl.w1 = lo; pl.w2 = l8; pl.ld = ldw; pl.flag = (int*)flag;
     return MCPG_OK;
 }
 
@@ -369,8 +384,10 @@ int mi_launch(mcpg_handle* h, const MiPlan& pl, int64_t g0, int64_t g1) {
     cudaError_t e;
     {
         PROF(h, "mi_tc");
-        e = mcpg::launch_mi_tc((const uint16_t*)pl.w0, (const uint16_t*)pl.w1, pl.ld, pl.H, pl.n, pl.m, pl.bins,
-                               pl.fmt, pl.split, pl.MI, pl.ldmi, pl.flag, h->stream, &h->launches, g0, g1);
+        const bool f8 = pl.split == mcpg::TC_F8C;
+        e = mcpg::launch_mi_tc((const uint16_t*)pl.w0, f8 ? nullptr : (const uint16_t*)pl.w1,
+                               f8 ? (const uint8_t*)pl.w1 : nullptr, (const uint8_t*)pl.w2, pl.ld, pl.H, pl.n, pl.m,
+                               pl.bins, pl.fmt, pl.split, pl.MI, pl.ldmi, pl.flag, h->stream, &h->launches, g0, g1);
     }
     if (e == cudaErrorNotSupported)
         return fail(h, MCPG_ERR_UNSUPPORTED, "bspline_mi tensor-core path: unsupported shape or device");

@@ -18,8 +18,13 @@
 //   OUT_T32   : Wt[s*ldwt + g*bins + a] (sample-major FP32, CUDA-core MI)
 //   OUT_BF16/OUT_FP16 : Whi/Wlo[(g*bins + a)*ldw + s] (gene-bin-major, K = samples
 //               contiguous, zero-padded to ldw; tcgen05 MI)
+//   OUT_BF16F8 : the same layout, three planes: Whi = bf16(w) * 2^8 (BF16), and the
+//               E4M3 correction operands H8 = e4m3(bf16(w) * 2^4), L8 = e4m3((w - bf16(w)) * 2^12).
+//               The scales multiply to 2^16 in every product (hi*hi, H8*L8, L8*H8), so
+//               the three contractions accumulate 2^16 * P into one FP32 accumulator.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
+#include <cuda_fp8.h>
 #include <math.h>
 
 #include <cmath>
@@ -44,7 +49,7 @@ struct Knots {
     float r2[KMAX_ORDER + 1][KNOTS_MAX];
 };
 
-enum OutKind { OUT_REF = 0, OUT_T32 = 1, OUT_BF16 = 2, OUT_FP16 = 3 };
+enum OutKind { OUT_REF = 0, OUT_T32 = 1, OUT_BF16 = 2, OUT_FP16 = 3, OUT_BF16F8 = 4 };
 
 void host_knots(int bins, int order, Knots& k) {
     // buildKnotVector<float> (BSplineMI.hpp:35-71): norm_factor in double,
@@ -173,7 +178,8 @@ template <int OUT, int BT, int OT>
 __global__ void __launch_bounds__(WTHREADS) bspline_weights_kernel(const float* __restrict__ X, int64_t n, int64_t m,
                                                                    int64_t ldx, int bins_rt, int order_rt, const Knots kv,
                                                                    void* __restrict__ out0, void* __restrict__ out1,
-                                                                   int64_t ldo, double* __restrict__ H) {
+                                                                   void* __restrict__ out2, int64_t ldo,
+                                                                   double* __restrict__ H) {
     __shared__ float fscratch[32];
     __shared__ double psum[KMAX_BINS][WTHREADS / 32];
     const int64_t g = blockIdx.x;
@@ -209,6 +215,16 @@ __global__ void __launch_bounds__(WTHREADS) bspline_weights_kernel(const float* 
         } else if (OUT == OUT_T32) {
             float* W = static_cast<float*>(out0) + s * ldo + g * bins;
             for (int a = 0; a < bins; ++a) W[a] = w[a];
+        } else if (OUT == OUT_BF16F8) {
+            for (int a = 0; a < bins; ++a) {
+                const int64_t o = (g * bins + a) * ldo + s;
+                const __nv_bfloat16 hi = __float2bfloat16_rn(w[a]);
+                const float hf = __bfloat162float(hi);
+                static_cast<__nv_bfloat16*>(out0)[o] = __float2bfloat16_rn(hf * 256.0f);
+                static_cast<__nv_fp8_storage_t*>(out1)[o] = __nv_cvt_float_to_fp8(hf * 16.0f, __NV_SATFINITE, __NV_E4M3);
+                static_cast<__nv_fp8_storage_t*>(out2)[o] =
+                    __nv_cvt_float_to_fp8(__fsub_rn(w[a], hf) * 4096.0f, __NV_SATFINITE, __NV_E4M3);
+            }
         } else {
             for (int a = 0; a < bins; ++a) {
                 const int64_t o = (g * bins + a) * ldo + s;
@@ -224,7 +240,16 @@ __global__ void __launch_bounds__(WTHREADS) bspline_weights_kernel(const float* 
             }
         }
     }
-    // zero the K padding of the 16-bit layouts
+    // zero the K padding of the tensor-core layouts
+    if (OUT == OUT_BF16F8) {
+        for (int64_t s = m + threadIdx.x; s < ldo; s += blockDim.x)
+            for (int a = 0; a < bins; ++a) {
+                const int64_t o = (g * bins + a) * ldo + s;
+                static_cast<uint16_t*>(out0)[o] = 0;
+                static_cast<uint8_t*>(out1)[o] = 0;
+                static_cast<uint8_t*>(out2)[o] = 0;
+            }
+    }
     if (OUT == OUT_BF16 || OUT == OUT_FP16) {
         for (int64_t s = m + threadIdx.x; s < ldo; s += blockDim.x)
             for (int a = 0; a < bins; ++a) {
@@ -431,10 +456,10 @@ cudaError_t launch_bspline_weights_ref(const float* X, int64_t n, int64_t m, int
     if (launches) ++*launches;
     if (bins == 10 && order == 3)
         bspline_weights_kernel<OUT_REF, 10, 3><<<(unsigned)n, WTHREADS, 0, stream>>>(X, n, m, ldx, bins, order, kv, W,
-                                                                                 nullptr, 0, H);
+                                                                                 nullptr, nullptr, 0, H);
     else
         bspline_weights_kernel<OUT_REF, 0, 0><<<(unsigned)n, WTHREADS, 0, stream>>>(X, n, m, ldx, bins, order, kv, W,
-                                                                               nullptr, 0, H);
+                                                                               nullptr, nullptr, 0, H);
     return cudaGetLastError();
 }
 
@@ -446,10 +471,10 @@ cudaError_t launch_bspline_weights_fp32(const float* X, int64_t n, int64_t m, in
     if (launches) ++*launches;
     if (bins == 10 && order == 3)
         bspline_weights_kernel<OUT_T32, 10, 3><<<(unsigned)n, WTHREADS, 0, stream>>>(X, n, m, ldx, bins, order, kv, Wt,
-                                                                                 nullptr, ldwt, H);
+                                                                                 nullptr, nullptr, ldwt, H);
     else
         bspline_weights_kernel<OUT_T32, 0, 0><<<(unsigned)n, WTHREADS, 0, stream>>>(X, n, m, ldx, bins, order, kv, Wt,
-                                                                               nullptr, ldwt, H);
+                                                                               nullptr, nullptr, ldwt, H);
     return cudaGetLastError();
 }
 
@@ -463,16 +488,32 @@ cudaError_t launch_bspline_weights_16(const float* X, int64_t n, int64_t m, int6
     const bool fast = bins == 10 && order == 3;
     if (fmt == 0 && fast)
         bspline_weights_kernel<OUT_BF16, 10, 3><<<(unsigned)n, WTHREADS, 0, stream>>>(X, n, m, ldx, bins, order, kv,
-                                                                                  Whi, Wlo, ldw, H);
+                                                                                  Whi, Wlo, nullptr, ldw, H);
     else if (fmt == 0)
         bspline_weights_kernel<OUT_BF16, 0, 0><<<(unsigned)n, WTHREADS, 0, stream>>>(X, n, m, ldx, bins, order, kv,
-                                                                                Whi, Wlo, ldw, H);
+                                                                                Whi, Wlo, nullptr, ldw, H);
     else if (fast)
         bspline_weights_kernel<OUT_FP16, 10, 3><<<(unsigned)n, WTHREADS, 0, stream>>>(X, n, m, ldx, bins, order, kv,
-                                                                                  Whi, Wlo, ldw, H);
+                                                                                  Whi, Wlo, nullptr, ldw, H);
     else
         bspline_weights_kernel<OUT_FP16, 0, 0><<<(unsigned)n, WTHREADS, 0, stream>>>(X, n, m, ldx, bins, order, kv,
-                                                                                Whi, Wlo, ldw, H);
+                                                                                Whi, Wlo, nullptr, ldw, H);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bspline_weights_f8(const float* X, int64_t n, int64_t m, int64_t ldx, int bins, int order,
+                                      uint16_t* Whi, uint8_t* H8, uint8_t* L8, int64_t ldw, double* H,
+                                      cudaStream_t stream, int64_t* launches) {
+    if (n <= 0) return cudaSuccess;
+    Knots kv;
+    host_knots(bins, order, kv);
+    if (launches) ++*launches;
+    if (bins == 10 && order == 3)
+        bspline_weights_kernel<OUT_BF16F8, 10, 3><<<(unsigned)n, WTHREADS, 0, stream>>>(X, n, m, ldx, bins, order, kv,
+                                                                                    Whi, H8, L8, ldw, H);
+    else
+        bspline_weights_kernel<OUT_BF16F8, 0, 0><<<(unsigned)n, WTHREADS, 0, stream>>>(X, n, m, ldx, bins, order, kv,
+                                                                                  Whi, H8, L8, ldw, H);
     return cudaGetLastError();
 }
 

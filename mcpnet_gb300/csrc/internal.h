@@ -90,6 +90,11 @@ cudaError_t launch_bspline_weights_fp32(const float* X, int64_t n, int64_t m, in
 cudaError_t launch_bspline_weights_16(const float* X, int64_t n, int64_t m, int64_t ldx, int bins, int order,
                                       int fmt, uint16_t* Whi, uint16_t* Wlo, int64_t ldw, double* H,
                                       cudaStream_t stream, int64_t* launches);
+// The same layout in three planes for the FP8-corrected form: Whi = bf16(w) * 2^8,
+// H8 = e4m3(bf16(w) * 2^4), L8 = e4m3((w - bf16(w)) * 2^12) (every product scaled 2^16).
+cudaError_t launch_bspline_weights_f8(const float* X, int64_t n, int64_t m, int64_t ldx, int bins, int order,
+                                      uint16_t* Whi, uint8_t* H8, uint8_t* L8, int64_t ldw, double* H,
+                                      cudaStream_t stream, int64_t* launches);
 // FP32 MI from sample-major weights (CUDA cores), symmetric output.
 // Covers gene pairs (i, j >= i) with i in [gene0, gene1) (gene0 a multiple of 16;
 // gene1 = -1 for n): rows i < gene1 of MI are complete once every earlier range ran.
@@ -109,12 +114,16 @@ cudaError_t launch_pair_sums(const float* G, int64_t ldg, int64_t n, float* gsum
 cudaError_t launch_mi_bwd_x(const float* X, int64_t n, int64_t m, int64_t ldx, int bins, int order, int64_t g0,
                             int64_t g1, const float* gsum, const float* dWq, int64_t lddw, float* dX, int64_t lddx,
                             cudaStream_t stream, int64_t* launches);
-// Tensor-core MI (tcgen05) from 16-bit weights; split != 0 adds the lo terms.
+// Tensor-core MI (tcgen05).  mode TC_SINGLE: 16-bit weights Whi; TC_SPLIT16: adds
+// the 16-bit lo terms from Wlo; TC_F8C: BF16 Whi (x 2^8) plus the E4M3 correction
+// planes H8 / L8 (launch_bspline_weights_f8).
 // Returns cudaErrorNotSupported when the shape/bins is outside the kernel's tiling.
 // Gene range as launch_mi_fp32 (gene0 a multiple of 12).
-cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, int64_t ldw, const double* H, int64_t n,
-                         int64_t m, int bins, int fmt, int split, float* MI, int64_t ldmi, int* timeout_flag,
-                         cudaStream_t stream, int64_t* launches, int64_t gene0 = 0, int64_t gene1 = -1);
+enum TcMode : int { TC_SINGLE = 0, TC_SPLIT16 = 1, TC_F8C = 2 };
+cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, const uint8_t* H8, const uint8_t* L8,
+                         int64_t ldw, const double* H, int64_t n, int64_t m, int bins, int fmt, int mode, float* MI,
+                         int64_t ldmi, int* timeout_flag, cudaStream_t stream, int64_t* launches, int64_t gene0 = 0,
+                         int64_t gene1 = -1);
 
 // ---------------- gold-standard evaluation (eval.cu) ----------------
 enum TruthMode : int {

@@ -10,17 +10,24 @@
 // split), gene-bin-major rows (row = gene*BINS + bin), K = samples contiguous,
 // zero-padded to a multiple of 64.  The split computes
 //   P = Whi Whi' + Whi Wlo' + Wlo Whi'      (the lo*lo term is below FP32 noise)
-// into one FP32 accumulator.
+// into one FP32 accumulator.  The FP8-corrected form keeps the hi*hi term in BF16
+// (kind::f16) and computes the two correction terms on the FP8 tensor path
+// (kind::f8f6f4, E4M3, twice the kind::f16 rate) from H8 = e4m3(16 hi) and
+// L8 = e4m3(4096 lo):  2^16 P = (256 Whi)(256 Whi)' + H8 L8' + L8 H8'.  A tile
+// first runs the correction over all samples (while the accumulator is small),
+// then the hi*hi term: per 64 samples 4 BF16 MMAs + 4 FP8 MMAs of equal duration,
+// against 12 for the BF16 split.  Its operands (8-bit: 64-byte rows, 64-byte
+// swizzle) fill the same 46 KB stages as the hi*hi slices, so the ring is 4 deep.
 //
 // CTA tile: A = 12 genes (120 of the 128 MMA rows), B = 24 genes (N = 240);
 // D = 128 x 240 FP32 in tensor memory (256 columns allocated).
 //   warp 0 / one lane : TMA producer (cp.async.bulk.tensor, 128B swizzle, 64-sample slices)
-//   warp 1 / one lane : tcgen05.mma issuer (kind::f16, M=128, N=240, K=16)
+//   warp 1 / one lane : tcgen05.mma issuer (kind::f16 K=16 / kind::f8f6f4 K=32, M=128, N=240)
 //   warps 2-5         : epilogue -- tcgen05.ld one row per thread, p*log2(p)
 //                       per (row, B gene) in FP32, cross-bin sums and
 //                       H_i + H_j - H_ij in FP64, symmetric store.
 // Persistent CTAs (one per SM) walk the tile list; a ring of 64-sample stages
-// (2 x 92 KB with the split, 4 x 46 KB without) feeds the MMAs through
+// (2 x 92 KB with the BF16 split, 4 x 46 KB otherwise) feeds the MMAs through
 // mbarriers, and two TMEM accumulators let the epilogue of one tile overlap the
 // main loop of the next.  Only gene-tile pairs that contain some j >= i run;
 // tiles are visited in groups of GI A-tiles, B tiles outer, so that a group's
@@ -55,6 +62,9 @@ constexpr int TMEM_COLS = 256;
 inline int64_t group_bytes(int64_t ldw) { return ldw <= 2048 ? (32ll << 20) : (16ll << 20); }
 constexpr uint32_t A_BYTES = MROWS * BK * 2;   // 16 KB
 constexpr uint32_t B_BYTES = NCOLS * BK * 2;   // 30 KB
+constexpr uint32_t A8_BYTES = MROWS * BK;      // 8 KB (8-bit correction operand)
+constexpr uint32_t B8_BYTES = NCOLS * BK;      // 15 KB
+static_assert(2 * (A8_BYTES + B8_BYTES) == A_BYTES + B_BYTES, "correction slices fill a hi*hi stage");
 constexpr int PSTRIDE = GBN + 1;       // epilogue partials row stride (floats)
 constexpr unsigned long long WAIT_NS = 2000000000ull;
 
@@ -122,6 +132,14 @@ __device__ __forceinline__ void mma_f16(uint32_t tmem_d, uint64_t adesc, uint64_
         "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
         "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accum));
 }
+// D[tmem] (+)= A[smem] * B[smem]^T, kind::f8f6f4 (E4M3 operands, K = 32).
+__device__ __forceinline__ void mma_f8(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                       uint32_t accum) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accum));
+}
 __device__ __forceinline__ void mma_commit(uint32_t bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
@@ -151,8 +169,21 @@ __device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
     return d;
 }
 
-// Instruction descriptor, kind::f16: F32 accumulate, A/B fmt (0 = F16, 1 = BF16),
-// both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
+// Shared-memory matrix descriptor for the 8-bit operands: K-major, 64-byte swizzle,
+// rows of 64 bytes, 8-row groups 512 bytes apart (SBO).
+__device__ __forceinline__ uint64_t sdesc_sw64(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)1 << 16;
+    d |= (uint64_t)(512 >> 4) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)4 << 61;                            // SWIZZLE_64B
+    return d;
+}
+
+// Instruction descriptor, kind::f16 / kind::f8f6f4: F32 accumulate, A/B fmt
+// (kind::f16: 0 = F16, 1 = BF16; kind::f8f6f4: 0 = E4M3), both K-major,
+// N >> 3 at bit 17, M >> 4 at bit 24.
 __host__ __device__ constexpr uint32_t idesc_f16(uint32_t fmt, uint32_t M, uint32_t N) {
     return (1u << 4) | (fmt << 7) | (fmt << 10) | ((N >> 3) << 17) | ((M >> 4) << 24);
 }
@@ -168,6 +199,7 @@ struct TcArgs {
     int ktiles;        // K / 64
     float inv_m;
     uint32_t idesc;
+    uint32_t idesc8;   // kind::f8f6f4 (TC_F8C)
     int* err;
     float* dbg;        // nullable: tile (0, 0) stores its raw 128 x 240 accumulator here
 };
@@ -219,11 +251,15 @@ __device__ __forceinline__ bool tile_of(int64_t L, const TcArgs& a, int& I, int&
 //   warps 2-5          epilogue, 128 threads = 128 accumulator rows
 // Two TMEM accumulators (2 x 256 columns) let the epilogue of tile t overlap the
 // main loop of tile t+1.
-template <bool SPLIT, int STAGES>
+// map_lo / mapb_lo carry Wlo (TC_SPLIT16) or H8 (TC_F8C); map_l8 / mapb_l8 carry L8.
+template <int MODE, int STAGES>
 __global__ void __launch_bounds__(192, 1)
     mi_tc_kernel(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CUtensorMap map_lo,
                  const __grid_constant__ CUtensorMap mapb_hi, const __grid_constant__ CUtensorMap mapb_lo,
+                 const __grid_constant__ CUtensorMap map_l8, const __grid_constant__ CUtensorMap mapb_l8,
                  const TcArgs args, const int64_t n_slots) {
+    constexpr bool SPLIT = MODE == TC_SPLIT16;
+    constexpr bool F8C = MODE == TC_F8C;
     extern __shared__ uint8_t smem_raw[];
     const uint32_t raw = smem_u32(smem_raw);
     const uint32_t base = (raw + 1023u) & ~1023u;
@@ -257,6 +293,7 @@ __global__ void __launch_bounds__(192, 1)
     tc_fence_after();
     const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(tmem_slot);
     const int KT = args.ktiles;
+    const int QT = F8C ? 2 * KT : KT;  // stages per tile: the correction slices, then hi*hi
 
     if (warp == 0) {
         if (lane == 0) {
@@ -267,7 +304,7 @@ __global__ void __launch_bounds__(192, 1)
                 int I, J;
                 if (!tile_of(L, args, I, J)) continue;
                 const int rowA = I * GA * BINS, rowB = J * GBN * BINS;
-                for (int kt = 0; kt < KT; ++kt, ++g) {
+                for (int q = 0; q < QT; ++q, ++g) {
                     const int s = (int)(g % STAGES);
                     const int64_t u = g / STAGES;
                     if (u > 0 && !(ok = mbar_wait_abortable(empty0 + 8 * s, (uint32_t)((u - 1) & 1), args.err,
@@ -275,6 +312,14 @@ __global__ void __launch_bounds__(192, 1)
                         break;
                     const uint32_t st = base + s * STAGE_BYTES;
                     mbar_expect_tx(full0 + 8 * s, STAGE_BYTES);
+                    if (F8C && q < KT) {
+                        tma_load_2d(st, &map_lo, q * BK, rowA, full0 + 8 * s);
+                        tma_load_2d(st + A8_BYTES, &map_l8, q * BK, rowA, full0 + 8 * s);
+                        tma_load_2d(st + A_BYTES, &mapb_lo, q * BK, rowB, full0 + 8 * s);
+                        tma_load_2d(st + A_BYTES + B8_BYTES, &mapb_l8, q * BK, rowB, full0 + 8 * s);
+                        continue;
+                    }
+                    const int kt = F8C ? q - KT : q;
                     tma_load_2d(st, &map_hi, kt * BK, rowA, full0 + 8 * s);
                     tma_load_2d(st + A_BYTES, &mapb_hi, kt * BK, rowB, full0 + 8 * s);
                     if (SPLIT) {
@@ -305,18 +350,30 @@ __global__ void __launch_bounds__(192, 1)
                     break;
                 tc_fence_after();
                 const uint32_t dacc = tmem + (uint32_t)(ab * TMEM_COLS);
-                for (int kt = 0; kt < KT; ++kt, ++g) {
+                for (int q = 0; q < QT; ++q, ++g) {
                     const int s = (int)(g % STAGES);
                     if (!(ok = mbar_wait_abortable(full0 + 8 * s, (uint32_t)((g / STAGES) & 1), args.err,
                                                    abort_flag)))
                         break;
                     tc_fence_after();
                     const uint32_t st = base + s * STAGE_BYTES;
+                    if (F8C && q < KT) {
+#pragma unroll
+                        for (int k = 0; k < BK / 32; ++k) {
+                            const uint64_t ah = sdesc_sw64(st + 32 * k), al = sdesc_sw64(st + A8_BYTES + 32 * k);
+                            const uint64_t bh = sdesc_sw64(st + A_BYTES + 32 * k);
+                            const uint64_t bl = sdesc_sw64(st + A_BYTES + B8_BYTES + 32 * k);
+                            mma_f8(dacc, ah, bl, args.idesc8, (q > 0 || k > 0) ? 1u : 0u);
+                            mma_f8(dacc, al, bh, args.idesc8, 1u);
+                        }
+                        mma_commit(empty0 + 8 * s);
+                        continue;
+                    }
 #pragma unroll
                     for (int k = 0; k < BK / 16; ++k) {
                         const uint64_t ahi = sdesc_sw128(st + 32 * k);
                         const uint64_t bhi = sdesc_sw128(st + A_BYTES + 32 * k);
-                        mma_f16(dacc, ahi, bhi, args.idesc, (kt > 0 || k > 0) ? 1u : 0u);
+                        mma_f16(dacc, ahi, bhi, args.idesc, (F8C || q > 0 || k > 0) ? 1u : 0u);
                         if (SPLIT) {
                             const uint64_t alo = sdesc_sw128(st + A_BYTES + B_BYTES + 32 * k);
                             const uint64_t blo = sdesc_sw128(st + 2 * A_BYTES + B_BYTES + 32 * k);
@@ -429,14 +486,42 @@ bool make_map(CUtensorMap* map, const uint16_t* base, int fmt, int64_t rows, int
     return r == CUDA_SUCCESS;
 }
 
+// 8-bit operand planes: 64-sample boxes of 64 bytes, 64-byte swizzle.
+bool make_map8(CUtensorMap* map, const uint8_t* base, int64_t rows, int64_t ldw, uint32_t box_rows) {
+    EncodeTiledFn enc = encode_fn();
+    if (!enc) return false;
+    cuuint64_t dims[2] = {(cuuint64_t)ldw, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)ldw};
+    cuuint32_t box[2] = {(cuuint32_t)BK, box_rows};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, (void*)base, dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
+template <int MODE, int STAGES>
+cudaError_t launch_mode(const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorMap& b0, const CUtensorMap& b1,
+                        const CUtensorMap& a2, const CUtensorMap& b2, const TcArgs& a, int64_t n_slots, int64_t grid,
+                        size_t smem, cudaStream_t stream) {
+    cudaError_t e = cudaFuncSetAttribute(mi_tc_kernel<MODE, STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    mi_tc_kernel<MODE, STAGES><<<(unsigned)grid, 192, smem, stream>>>(a0, a1, b0, b1, a2, b2, a, n_slots);
+    return cudaGetLastError();
+}
+
 }  // namespace
 
-// Whi/Wlo: rows >= ceil(n*bins/240)*240 + 256 rows of ldw 16-bit values, zero
-// beyond row n*bins and beyond column m; ldw a multiple of 64.
-cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, int64_t ldw, const double* H, int64_t n, int64_t m,
-                         int bins, int fmt, int split, float* MI, int64_t ldmi, int* timeout_flag, cudaStream_t stream,
-                         int64_t* launches, int64_t gene0, int64_t gene1) {
+// Whi/Wlo (16-bit) and H8/L8 (8-bit): rows >= ceil(n*bins/256)*256 + 256 rows of
+// ldw values, zero beyond row n*bins and beyond column m; ldw a multiple of 64.
+cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, const uint8_t* H8, const uint8_t* L8,
+                         int64_t ldw, const double* H, int64_t n, int64_t m, int bins, int fmt, int mode, float* MI,
+                         int64_t ldmi, int* timeout_flag, cudaStream_t stream, int64_t* launches, int64_t gene0,
+                         int64_t gene1) {
     if (bins != BINS || (ldw % BK) != 0) return cudaErrorNotSupported;
+    if (mode != TC_SINGLE && mode != TC_SPLIT16 && mode != TC_F8C) return cudaErrorInvalidValue;
+    if (mode == TC_F8C && fmt != 0) return cudaErrorInvalidValue;
     if (gene1 < 0 || gene1 > n) gene1 = n;
     if (n <= 0 || gene0 >= gene1) return cudaSuccess;
     if (gene0 % GA) return cudaErrorInvalidValue;
@@ -446,15 +531,18 @@ cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, int64_t ldw, 
     cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
     if (major < 10) return cudaErrorNotSupported;
     const int64_t rows = ((n * bins + 255) / 256) * 256 + 256;
-    CUtensorMap ma_hi, ma_lo, mb_hi, mb_lo;
+    CUtensorMap ma_hi, ma_lo, mb_hi, mb_lo, ma_l8, mb_l8;
     if (!make_map(&ma_hi, Whi, fmt, rows, ldw, MROWS) || !make_map(&mb_hi, Whi, fmt, rows, ldw, NCOLS))
         return cudaErrorNotSupported;
-    if (split) {
+    ma_lo = ma_l8 = ma_hi;
+    mb_lo = mb_l8 = mb_hi;
+    if (mode == TC_SPLIT16) {
         if (!Wlo || !make_map(&ma_lo, Wlo, fmt, rows, ldw, MROWS) || !make_map(&mb_lo, Wlo, fmt, rows, ldw, NCOLS))
             return cudaErrorNotSupported;
-    } else {
-        ma_lo = ma_hi;
-        mb_lo = mb_hi;
+    } else if (mode == TC_F8C) {
+        if (!H8 || !L8 || !make_map8(&ma_lo, H8, rows, ldw, MROWS) || !make_map8(&mb_lo, H8, rows, ldw, NCOLS) ||
+            !make_map8(&ma_l8, L8, rows, ldw, MROWS) || !make_map8(&mb_l8, L8, rows, ldw, NCOLS))
+            return cudaErrorNotSupported;
     }
     TcArgs a;
     a.H = H;
@@ -466,12 +554,14 @@ cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, int64_t ldw, 
     a.I0 = (int)(gene0 / GA);
     a.TIr = (int)((gene1 + GA - 1) / GA) - a.I0;
     a.ktiles = (int)(ldw / BK);
-    a.inv_m = 1.0f / (float)m;
+    // the FP8-corrected form accumulates 2^16 P (power-of-two scale: exact)
+    a.inv_m = (1.0f / (float)m) * (mode == TC_F8C ? 1.0f / 65536.0f : 1.0f);
     a.idesc = idesc_f16(fmt == 0 ? 1u : 0u, MROWS, NCOLS);
+    a.idesc8 = idesc_f16(0u, MROWS, NCOLS);  // E4M3 x E4M3 (format code 0 in kind::f8f6f4)
     a.err = timeout_flag;
     a.dbg = g_tc_debug_dump;
     {
-        const int64_t tile_bytes = (int64_t)MROWS * ldw * 2 * (split ? 2 : 1);
+        const int64_t tile_bytes = (int64_t)MROWS * ldw * 2 * (mode == TC_SINGLE ? 1 : 2);
         int gi = 1;
         while (gi < 64 && (int64_t)(2 * gi) * tile_bytes <= group_bytes(ldw)) gi *= 2;
 #ifdef MCPG_TC_GI
@@ -484,21 +574,15 @@ cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, int64_t ldw, 
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int64_t grid = n_slots < sms ? n_slots : sms;
-    const uint32_t stage_bytes = (split ? 2u : 1u) * (A_BYTES + B_BYTES);
-    const int stages = split ? 2 : 4;
+    const uint32_t stage_bytes = (mode == TC_SPLIT16 ? 2u : 1u) * (A_BYTES + B_BYTES);
+    const int stages = mode == TC_SPLIT16 ? 2 : 4;
     const size_t smem = 1024 + stages * stage_bytes + MROWS * PSTRIDE * 4 + 16 * stages + 32 + 16;
-    cudaError_t e;
     if (launches) ++*launches;
-    if (split) {
-        e = cudaFuncSetAttribute(mi_tc_kernel<true, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        mi_tc_kernel<true, 2><<<(unsigned)grid, 192, smem, stream>>>(ma_hi, ma_lo, mb_hi, mb_lo, a, n_slots);
-    } else {
-        e = cudaFuncSetAttribute(mi_tc_kernel<false, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        mi_tc_kernel<false, 4><<<(unsigned)grid, 192, smem, stream>>>(ma_hi, ma_lo, mb_hi, mb_lo, a, n_slots);
-    }
-    return cudaGetLastError();
+    if (mode == TC_SPLIT16)
+        return launch_mode<TC_SPLIT16, 2>(ma_hi, ma_lo, mb_hi, mb_lo, ma_l8, mb_l8, a, n_slots, grid, smem, stream);
+    if (mode == TC_F8C)
+        return launch_mode<TC_F8C, 4>(ma_hi, ma_lo, mb_hi, mb_lo, ma_l8, mb_l8, a, n_slots, grid, smem, stream);
+    return launch_mode<TC_SINGLE, 4>(ma_hi, ma_lo, mb_hi, mb_lo, ma_l8, mb_l8, a, n_slots, grid, smem, stream);
 }
 
 }  // namespace mcpg
