@@ -8,7 +8,9 @@ Workload (default): seeded synthetic GRN expression, 20,000 genes x 2,000
 samples, B-spline MI with 10 bins and spline order 3.
   * ``value``  -- B-spline MI gene pairs per second (n(n-1)/2 per step), one
     step = scale + weights + tensor-core contraction with the fused entropy
-    epilogue, inputs resident in HBM, timed with CUDA events on the library's
+    epilogue (default form bf16f8: BF16 hi*hi plus the E4M3 hi*lo + lo*hi
+    correction; ``mi_forms`` times bf16x3 beside it), inputs resident in HBM,
+    timed with CUDA events on the library's
     stream; W >= 3 untimed warm-up steps.  Working set (X 160 MB, weights
     1.6 GB, MI 1.6 GB) is larger than the 129 MB L2, so no flush is needed.
   * ``e2e``    -- the same metric through the host C ABI (mcpg_bspline_mi with
@@ -277,9 +279,9 @@ def gpu_arm(args, ws, rank, local):
                 "frac": achieved_tf / peak_tf, "traffic": traffic[0] if traffic else None,
                 "traffic_source": traffic[1] if traffic else None, "peak_source": peak_src,
                 "kernel_ms": k_ms, "algorithmic_flop_per_launch": flops,
-                "note": "achieved counts 2*b^2*m flops per unordered gene pair; the BF16 hi+lo split issues 3x "
-                        "that on the tensor pipe, the FP8-corrected form (bf16f8) 1x BF16 + 2x FP8 (the "
-                        "time of 2x BF16)"}
+                "note": "achieved counts 2*b^2*m flops per unordered gene pair; the FP8-corrected form "
+                        "(bf16f8) issues them once in BF16 and twice in FP8 (twice the BF16 rate: the time of "
+                        "2x BF16), the BF16 hi+lo split (bf16x3) 3x in BF16"}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
@@ -293,6 +295,7 @@ def gpu_arm(args, ws, rank, local):
     }
 
     # ---- plain FP32 GPU MI on the same input ----
+    MI32 = None
     if args.precision != "fp32" and not args.no_fp32:
         mi_step("fp32")
         torch.cuda.synchronize(dev)
@@ -313,6 +316,29 @@ def gpu_arm(args, ws, rank, local):
         line["mi_fp32"] = {"ms": f_ms, "pairs_per_s": pairs / (f_ms / 1e3),
                            "speedup_tc_vs_fp32": f_ms / (dev_s / args.steps * 1e3),
                            "max_abs_diff_vs_tc_bits": diff}
+
+    # ---- the other tensor-core forms on the same input (step time, max |diff| vs the FP32 MI) ----
+    others = [p for p in args.compare.split(",") if p in M.PRECISIONS and p not in (args.precision, "fp32")]
+    if args.precision != "fp32" and others:
+        line["mi_forms"] = {}
+        for prec in others:
+            for _ in range(2):
+                mi_step(prec)
+            torch.cuda.synchronize(dev)
+            ts = []
+            for _ in range(3):
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                mi_step(prec)
+                b.record(stream)
+                b.synchronize()
+                ts.append(a.elapsed_time(b))
+            o_ms = float(np.mean(ts))
+            rec = {"ms_per_step": o_ms, "pairs_per_s": pairs / (o_ms / 1e3)}
+            if MI32 is not None:
+                rec["max_abs_diff_vs_fp32_bits"] = float((MI - MI32).abs().max().item())
+            line["mi_forms"][prec] = rec
+        MI32 = None
 
     # ---- max-min products ----
     if not args.no_maxmin:
@@ -675,7 +701,10 @@ def main(argv=None):
     ap.add_argument("--samples", type=int, default=2000)
     ap.add_argument("--bins", type=int, default=10)
     ap.add_argument("--order", type=int, default=3)
-    ap.add_argument("--precision", default="bf16x3", choices=["fp32", "bf16", "bf16x3", "fp16", "fp16x3", "bf16f8"])
+    ap.add_argument("--precision", default="bf16f8", choices=["fp32", "bf16", "bf16x3", "fp16", "fp16x3", "bf16f8"])
+    ap.add_argument("--compare", default="bf16x3",
+                    help="comma-separated tensor-core forms timed beside the headline one on the same input "
+                         "('' for none)")
     ap.add_argument("--mi-method", default="bspline", choices=["bspline", "ap"],
                     help="with --pipeline: B-spline MI (default) or adaptive-partitioning MI (U[0,1e-5) noise)")
     ap.add_argument("--seed", type=int, default=20260001)

@@ -43,6 +43,8 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <math.h>
+#include <stdlib.h>
+#include <string.h>
 
 #include "common.cuh"
 #include "internal.h"
@@ -92,18 +94,16 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-// Bounded wait: false (and *err raised) if the phase did not complete in WAIT_NS.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err) {
-    if (mbar_try(bar, parity)) return true;
-    const unsigned long long t0 = gtimer();
-    for (;;) {
-        for (int i = 0; i < 256; ++i)
-            if (mbar_try(bar, parity)) return true;
-        if (gtimer() - t0 > WAIT_NS) {
-            atomicExch(err, 1);
-            return false;
-        }
-    }
+// try_wait with cluster-scope acquire: for phases completed by the peer CTA's arrivals.
+__device__ __forceinline__ bool mbar_try_cluster(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
+        "selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
 }
 
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar) {
@@ -230,6 +230,22 @@ __device__ __forceinline__ bool mbar_wait_abortable(uint32_t bar, uint32_t parit
     }
 }
 
+__device__ __forceinline__ bool mbar_wait_cluster_abortable(uint32_t bar, uint32_t parity, int* err,
+                                                            volatile int* abort_flag) {
+    if (mbar_try_cluster(bar, parity)) return true;
+    const unsigned long long t0 = gtimer();
+    for (;;) {
+        for (int i = 0; i < 64; ++i)
+            if (mbar_try_cluster(bar, parity)) return true;
+        if (*abort_flag) return false;
+        if (gtimer() - t0 > WAIT_NS) {
+            atomicExch(err, 1);
+            *abort_flag = 1;
+            return false;
+        }
+    }
+}
+
 __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
@@ -252,7 +268,7 @@ __device__ __forceinline__ bool tile_of(int64_t L, const TcArgs& a, int& I, int&
 // Two TMEM accumulators (2 x 256 columns) let the epilogue of tile t overlap the
 // main loop of tile t+1.
 // map_lo / mapb_lo carry Wlo (TC_SPLIT16) or H8 (TC_F8C); map_l8 / mapb_l8 carry L8.
-template <int MODE, int STAGES>
+template <int MODE, int STAGES, int SUB>
 __global__ void __launch_bounds__(192, 1)
     mi_tc_kernel(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CUtensorMap map_lo,
                  const __grid_constant__ CUtensorMap mapb_hi, const __grid_constant__ CUtensorMap mapb_lo,
@@ -264,7 +280,8 @@ __global__ void __launch_bounds__(192, 1)
     const uint32_t raw = smem_u32(smem_raw);
     const uint32_t base = (raw + 1023u) & ~1023u;
     uint8_t* gbase = smem_raw + (base - raw);
-    constexpr uint32_t STAGE_BYTES = (SPLIT ? 2 : 1) * (A_BYTES + B_BYTES);
+    constexpr uint32_t SLICE = (SPLIT ? 2 : 1) * (A_BYTES + B_BYTES);  // one 64-sample slice
+    constexpr uint32_t STAGE_BYTES = SUB * SLICE;
     constexpr uint32_t PART_BYTES = MROWS * PSTRIDE * 4;
     float* part = reinterpret_cast<float*>(gbase + STAGES * STAGE_BYTES);
     const uint32_t bars = base + STAGES * STAGE_BYTES + PART_BYTES;
@@ -293,7 +310,8 @@ __global__ void __launch_bounds__(192, 1)
     tc_fence_after();
     const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(tmem_slot);
     const int KT = args.ktiles;
-    const int QT = F8C ? 2 * KT : KT;  // stages per tile: the correction slices, then hi*hi
+    const int QP = (KT + SUB - 1) / SUB;  // stages per pass over the samples
+    const int QT = F8C ? 2 * QP : QP;     // stages per tile: the correction pass, then hi*hi
 
     if (warp == 0) {
         if (lane == 0) {
@@ -310,21 +328,28 @@ __global__ void __launch_bounds__(192, 1)
                     if (u > 0 && !(ok = mbar_wait_abortable(empty0 + 8 * s, (uint32_t)((u - 1) & 1), args.err,
                                                             abort_flag)))
                         break;
-                    const uint32_t st = base + s * STAGE_BYTES;
-                    mbar_expect_tx(full0 + 8 * s, STAGE_BYTES);
-                    if (F8C && q < KT) {
-                        tma_load_2d(st, &map_lo, q * BK, rowA, full0 + 8 * s);
-                        tma_load_2d(st + A8_BYTES, &map_l8, q * BK, rowA, full0 + 8 * s);
-                        tma_load_2d(st + A_BYTES, &mapb_lo, q * BK, rowB, full0 + 8 * s);
-                        tma_load_2d(st + A_BYTES + B8_BYTES, &mapb_l8, q * BK, rowB, full0 + 8 * s);
-                        continue;
-                    }
-                    const int kt = F8C ? q - KT : q;
-                    tma_load_2d(st, &map_hi, kt * BK, rowA, full0 + 8 * s);
-                    tma_load_2d(st + A_BYTES, &mapb_hi, kt * BK, rowB, full0 + 8 * s);
-                    if (SPLIT) {
-                        tma_load_2d(st + A_BYTES + B_BYTES, &map_lo, kt * BK, rowA, full0 + 8 * s);
-                        tma_load_2d(st + 2 * A_BYTES + B_BYTES, &mapb_lo, kt * BK, rowB, full0 + 8 * s);
+                    const uint32_t st = base + s * STAGE_BYTES, fb = full0 + 8 * s;
+                    const bool corr = F8C && q < QP;
+                    const int kt0 = (q % QP) * SUB, ns = KT - kt0 < SUB ? KT - kt0 : SUB;
+                    mbar_expect_tx(fb, (uint32_t)ns * SLICE);
+#pragma unroll
+                    for (int j = 0; j < SUB; ++j) {
+                        if (j >= ns) break;
+                        const uint32_t sl = st + j * SLICE;
+                        const int x = (kt0 + j) * BK;
+                        if (corr) {
+                            tma_load_2d(sl, &map_lo, x, rowA, fb);
+                            tma_load_2d(sl + A8_BYTES, &map_l8, x, rowA, fb);
+                            tma_load_2d(sl + A_BYTES, &mapb_lo, x, rowB, fb);
+                            tma_load_2d(sl + A_BYTES + B8_BYTES, &mapb_l8, x, rowB, fb);
+                            continue;
+                        }
+                        tma_load_2d(sl, &map_hi, x, rowA, fb);
+                        tma_load_2d(sl + A_BYTES, &mapb_hi, x, rowB, fb);
+                        if (SPLIT) {
+                            tma_load_2d(sl + A_BYTES + B_BYTES, &map_lo, x, rowA, fb);
+                            tma_load_2d(sl + 2 * A_BYTES + B_BYTES, &mapb_lo, x, rowB, fb);
+                        }
                     }
                 }
             }
@@ -357,28 +382,34 @@ __global__ void __launch_bounds__(192, 1)
                         break;
                     tc_fence_after();
                     const uint32_t st = base + s * STAGE_BYTES;
-                    if (F8C && q < KT) {
+                    const bool corr = F8C && q < QP;
+                    const int kt0 = (q % QP) * SUB, ns = KT - kt0 < SUB ? KT - kt0 : SUB;
 #pragma unroll
-                        for (int k = 0; k < BK / 32; ++k) {
-                            const uint64_t ah = sdesc_sw64(st + 32 * k), al = sdesc_sw64(st + A8_BYTES + 32 * k);
-                            const uint64_t bh = sdesc_sw64(st + A_BYTES + 32 * k);
-                            const uint64_t bl = sdesc_sw64(st + A_BYTES + B8_BYTES + 32 * k);
-                            mma_f8(dacc, ah, bl, args.idesc8, (q > 0 || k > 0) ? 1u : 0u);
-                            mma_f8(dacc, al, bh, args.idesc8, 1u);
+                    for (int j = 0; j < SUB; ++j) {
+                        if (j >= ns) break;
+                        const uint32_t sl = st + j * SLICE;
+                        if (corr) {
+#pragma unroll
+                            for (int k = 0; k < BK / 32; ++k) {
+                                const uint64_t ah = sdesc_sw64(sl + 32 * k), al = sdesc_sw64(sl + A8_BYTES + 32 * k);
+                                const uint64_t bh = sdesc_sw64(sl + A_BYTES + 32 * k);
+                                const uint64_t bl = sdesc_sw64(sl + A_BYTES + B8_BYTES + 32 * k);
+                                mma_f8(dacc, ah, bl, args.idesc8, (q > 0 || j > 0 || k > 0) ? 1u : 0u);
+                                mma_f8(dacc, al, bh, args.idesc8, 1u);
+                            }
+                            continue;
                         }
-                        mma_commit(empty0 + 8 * s);
-                        continue;
-                    }
 #pragma unroll
-                    for (int k = 0; k < BK / 16; ++k) {
-                        const uint64_t ahi = sdesc_sw128(st + 32 * k);
-                        const uint64_t bhi = sdesc_sw128(st + A_BYTES + 32 * k);
-                        mma_f16(dacc, ahi, bhi, args.idesc, (F8C || q > 0 || k > 0) ? 1u : 0u);
-                        if (SPLIT) {
-                            const uint64_t alo = sdesc_sw128(st + A_BYTES + B_BYTES + 32 * k);
-                            const uint64_t blo = sdesc_sw128(st + 2 * A_BYTES + B_BYTES + 32 * k);
-                            mma_f16(dacc, ahi, blo, args.idesc, 1u);
-                            mma_f16(dacc, alo, bhi, args.idesc, 1u);
+                        for (int k = 0; k < BK / 16; ++k) {
+                            const uint64_t ahi = sdesc_sw128(sl + 32 * k);
+                            const uint64_t bhi = sdesc_sw128(sl + A_BYTES + 32 * k);
+                            mma_f16(dacc, ahi, bhi, args.idesc, (F8C || q > 0 || j > 0 || k > 0) ? 1u : 0u);
+                            if (SPLIT) {
+                                const uint64_t alo = sdesc_sw128(sl + A_BYTES + B_BYTES + 32 * k);
+                                const uint64_t blo = sdesc_sw128(sl + 2 * A_BYTES + B_BYTES + 32 * k);
+                                mma_f16(dacc, ahi, blo, args.idesc, 1u);
+                                mma_f16(dacc, alo, bhi, args.idesc, 1u);
+                            }
                         }
                     }
                     mma_commit(empty0 + 8 * s);  // frees the stage once these MMAs have read it
@@ -453,6 +484,316 @@ __global__ void __launch_bounds__(192, 1)
     }
 }
 
+// ---------------------------------------------------------------- 2-SM form
+// A cluster of two CTAs (an SM pair) runs cta_group::2 MMAs of M = 256: each CTA
+// holds its own A tile (12 genes, 128 rows) and HALF of the B tile (12 of its 24
+// genes, 120 rows); the MMA reads both CTAs' shared memory and writes each CTA's
+// 128 x 240 accumulator into that CTA's tensor memory.  Per SM and per 64
+// samples the stages carry 31 KB instead of 46 KB for the same MMA time, which
+// is what the L2 -> SM path sustains at the tensor pipe's rate.  Tiles are 24 x 24
+// genes (pair index IP over A, J over B; only J >= IP run).
+//   leader (rank 0): warp 0 TMA for its halves, warp 1 the MMA issuer, warps 2-5 epilogue
+//   peer   (rank 1): warp 0 TMA for its halves, warps 2-5 epilogue
+// Full barriers live in the leader (its expect_tx covers both CTAs' bytes; the
+// peer's loads signal it through the cta_group::2 TMA form); stage-empty and
+// accumulator-full barriers in both CTAs (multicast commits); accumulator-empty in
+// the leader (8 arrivals: both CTAs' epilogue warps).
+constexpr uint32_t BH_BYTES = (NCOLS / 2) * BK * 2;   // 15 KB: half a B tile, 16-bit
+constexpr uint32_t BH8_BYTES = (NCOLS / 2) * BK;      // 7.5 KB: half a B tile, 8-bit
+static_assert(2 * (A8_BYTES + BH8_BYTES) == A_BYTES + BH_BYTES, "correction slices fill a hi*hi stage");
+
+__device__ __forceinline__ uint32_t cluster_rank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ uint32_t cluster_index() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%clusterid.x;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ uint32_t cluster_total() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%nclusterid.x;" : "=r"(r));
+    return r;
+}
+// shared::cluster address of this CTA's shared variable at saddr, in CTA `rank`
+__device__ __forceinline__ uint32_t map_to_rank(uint32_t saddr, uint32_t rank) {
+    uint32_t d;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(d) : "r"(saddr), "r"(rank));
+    return d;
+}
+__device__ __forceinline__ void cluster_sync_all() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\nbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_remote(uint32_t cluster_addr) {
+    asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(cluster_addr) : "memory");
+}
+// TMA into this CTA's shared memory, completing on a barrier of either CTA of the pair
+__device__ __forceinline__ void tma_load_2d_pair(uint32_t dst, const CUtensorMap* map, int x, int y,
+                                                 uint32_t bar_cluster) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.cta_group::2.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, "
+        "%3}], [%4];" ::"r"(dst),
+        "l"((unsigned long long)map), "r"(x), "r"(y), "r"(bar_cluster)
+        : "memory");
+}
+__device__ __forceinline__ void mma2_f16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accum) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accum));
+}
+__device__ __forceinline__ void mma2_f8(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                        uint32_t accum) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::2.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accum));
+}
+// arrive on the barrier at this shared offset in both CTAs once the issued MMAs completed
+__device__ __forceinline__ void mma2_commit_both(uint32_t bar) {
+    const uint16_t mask = 3;
+    asm volatile(
+        "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(bar),
+        "h"(mask)
+        : "memory");
+}
+
+// Pair tile (IP, J): groups of a.GI pair tiles, B tiles outer (as tile_of).
+__device__ __forceinline__ bool pair_tile_of(int64_t L, const TcArgs& a, int& IP, int& J) {
+    const int64_t per_group = (int64_t)a.GI * a.TJ;
+    const int g = (int)(L / per_group);
+    const int r = (int)(L - (int64_t)g * per_group);
+    J = r / a.GI;
+    IP = a.I0 + g * a.GI + (r - J * a.GI);
+    return IP < a.I0 + a.TIr && IP < a.TI && J >= IP;
+}
+
+// TcArgs in pair units: TI = pair tiles (24 genes), I0 / TIr = the launch's pair range.
+template <int MODE, int STAGES, int SUB>
+__global__ void __launch_bounds__(192, 1)
+    mi_tc_pair_kernel(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CUtensorMap map_lo,
+                      const __grid_constant__ CUtensorMap mapb_hi, const __grid_constant__ CUtensorMap mapb_lo,
+                      const __grid_constant__ CUtensorMap map_l8, const __grid_constant__ CUtensorMap mapb_l8,
+                      const TcArgs args, const int64_t n_slots) {
+    constexpr bool SPLIT = MODE == TC_SPLIT16;
+    constexpr bool F8C = MODE == TC_F8C;
+    constexpr uint32_t HALF = A_BYTES + BH_BYTES;                 // 31 KB
+    constexpr uint32_t SLICE = (SPLIT ? 2 : 1) * HALF;
+    constexpr uint32_t STAGE_BYTES = SUB * SLICE;
+    constexpr uint32_t PART_BYTES = MROWS * PSTRIDE * 4;
+    extern __shared__ uint8_t smem_raw[];
+    const uint32_t raw = smem_u32(smem_raw);
+    const uint32_t base = (raw + 1023u) & ~1023u;
+    uint8_t* gbase = smem_raw + (base - raw);
+    float* part = reinterpret_cast<float*>(gbase + STAGES * STAGE_BYTES);
+    const uint32_t bars = base + STAGES * STAGE_BYTES + PART_BYTES;
+    const uint32_t full0 = bars, empty0 = bars + 8 * STAGES;
+    const uint32_t tfull0 = bars + 16 * STAGES, tempty0 = tfull0 + 16;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(gbase + STAGES * STAGE_BYTES + PART_BYTES + 16 * STAGES + 32);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t rank = cluster_rank();
+    const bool leader = rank == 0;
+    const int64_t c0 = cluster_index(), nc = cluster_total();
+    if (tid == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(full0 + 8 * s, 1);
+            mbar_init(empty0 + 8 * s, 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(tfull0 + 8 * b, 1);
+            mbar_init(tempty0 + 8 * b, 8);
+        }
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(2 * TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;");
+    }
+    tc_fence_before();
+    cluster_sync_all();  // both CTAs' barriers initialised and tensor memory allocated
+    tc_fence_after();
+    const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(tmem_slot);
+    const int KT = args.ktiles;
+    const int QP = (KT + SUB - 1) / SUB;
+    const int QT = F8C ? 2 * QP : QP;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            // ---------------- TMA producer (both CTAs: own A tile, own half of B) ----------------
+            int64_t g = 0;
+            bool ok = true;
+            for (int64_t L = c0; L < n_slots && ok; L += nc) {
+                int IP, J;
+                if (!pair_tile_of(L, args, IP, J)) continue;
+                const int rowA = (2 * IP + (int)rank) * GA * BINS;
+                const int rowB = J * GBN * BINS + (int)rank * (NCOLS / 2);
+                for (int q = 0; q < QT; ++q, ++g) {
+                    const int s = (int)(g % STAGES);
+                    const int64_t u = g / STAGES;
+                    if (u > 0 && !(ok = mbar_wait_abortable(empty0 + 8 * s, (uint32_t)((u - 1) & 1), args.err,
+                                                            abort_flag)))
+                        break;
+                    const uint32_t st = base + s * STAGE_BYTES;
+                    const uint32_t fb = map_to_rank(full0 + 8 * s, 0);
+                    const bool corr = F8C && q < QP;
+                    const int kt0 = (q % QP) * SUB, ns = KT - kt0 < SUB ? KT - kt0 : SUB;
+                    if (leader) mbar_expect_tx(full0 + 8 * s, 2u * (uint32_t)ns * SLICE);
+#pragma unroll
+                    for (int j = 0; j < SUB; ++j) {
+                        if (j >= ns) break;
+                        const uint32_t sl = st + j * SLICE;
+                        const int x = (kt0 + j) * BK;
+                        if (corr) {
+                            tma_load_2d_pair(sl, &map_lo, x, rowA, fb);
+                            tma_load_2d_pair(sl + A8_BYTES, &map_l8, x, rowA, fb);
+                            tma_load_2d_pair(sl + A_BYTES, &mapb_lo, x, rowB, fb);
+                            tma_load_2d_pair(sl + A_BYTES + BH8_BYTES, &mapb_l8, x, rowB, fb);
+                            continue;
+                        }
+                        tma_load_2d_pair(sl, &map_hi, x, rowA, fb);
+                        tma_load_2d_pair(sl + A_BYTES, &mapb_hi, x, rowB, fb);
+                        if (SPLIT) {
+                            tma_load_2d_pair(sl + HALF, &map_lo, x, rowA, fb);
+                            tma_load_2d_pair(sl + HALF + A_BYTES, &mapb_lo, x, rowB, fb);
+                        }
+                    }
+                }
+            }
+            // drain: every stage this CTA filled has been consumed by the MMAs
+            // (the multicast commits reach both CTAs), so no load is still in flight
+            for (int s = 0; s < STAGES && (int64_t)s < g; ++s) {
+                const int64_t last = (g - 1 - s) / STAGES;
+                mbar_wait_abortable(empty0 + 8 * s, (uint32_t)(last & 1), args.err, abort_flag);
+            }
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        if (lane == 0 && leader) {
+            // ---------------- MMA issuer (leader only) ----------------
+            int64_t g = 0, t = 0;
+            bool ok = true;
+            for (int64_t L = c0; L < n_slots && ok; L += nc) {
+                int IP, J;
+                if (!pair_tile_of(L, args, IP, J)) continue;
+                const int ab = (int)(t & 1);
+                const int64_t ua = t >> 1;
+                if (ua > 0 && !(ok = mbar_wait_cluster_abortable(tempty0 + 8 * ab, (uint32_t)((ua - 1) & 1),
+                                                                 args.err, abort_flag)))
+                    break;
+                tc_fence_after();
+                const uint32_t dacc = tmem + (uint32_t)(ab * TMEM_COLS);
+                for (int q = 0; q < QT; ++q, ++g) {
+                    const int s = (int)(g % STAGES);
+                    if (!(ok = mbar_wait_abortable(full0 + 8 * s, (uint32_t)((g / STAGES) & 1), args.err,
+                                                   abort_flag)))
+                        break;
+                    tc_fence_after();
+                    const uint32_t st = base + s * STAGE_BYTES;
+                    const bool corr = F8C && q < QP;
+                    const int kt0 = (q % QP) * SUB, ns = KT - kt0 < SUB ? KT - kt0 : SUB;
+#pragma unroll
+                    for (int j = 0; j < SUB; ++j) {
+                        if (j >= ns) break;
+                        const uint32_t sl = st + j * SLICE;
+                        if (corr) {
+#pragma unroll
+                            for (int k = 0; k < BK / 32; ++k) {
+                                const uint64_t ah = sdesc_sw64(sl + 32 * k), al = sdesc_sw64(sl + A8_BYTES + 32 * k);
+                                const uint64_t bh = sdesc_sw64(sl + A_BYTES + 32 * k);
+                                const uint64_t bl = sdesc_sw64(sl + A_BYTES + BH8_BYTES + 32 * k);
+                                mma2_f8(dacc, ah, bl, args.idesc8, (q > 0 || j > 0 || k > 0) ? 1u : 0u);
+                                mma2_f8(dacc, al, bh, args.idesc8, 1u);
+                            }
+                            continue;
+                        }
+#pragma unroll
+                        for (int k = 0; k < BK / 16; ++k) {
+                            const uint64_t ahi = sdesc_sw128(sl + 32 * k);
+                            const uint64_t bhi = sdesc_sw128(sl + A_BYTES + 32 * k);
+                            mma2_f16(dacc, ahi, bhi, args.idesc, (F8C || q > 0 || j > 0 || k > 0) ? 1u : 0u);
+                            if (SPLIT) {
+                                const uint64_t alo = sdesc_sw128(sl + HALF + 32 * k);
+                                const uint64_t blo = sdesc_sw128(sl + HALF + A_BYTES + 32 * k);
+                                mma2_f16(dacc, ahi, blo, args.idesc, 1u);
+                                mma2_f16(dacc, alo, bhi, args.idesc, 1u);
+                            }
+                        }
+                    }
+                    mma2_commit_both(empty0 + 8 * s);
+                }
+                if (!ok) break;
+                mma2_commit_both(tfull0 + 8 * ab);
+                ++t;
+            }
+        }
+        __syncwarp();
+    } else {
+        // ---------------- epilogue: warps 2..5 of both CTAs, 128 rows each ----------------
+        const int row = ((warp & 3) << 5) + lane;
+        const int etid = tid - 64;
+        const uint32_t te_leader = map_to_rank(tempty0, 0);
+        int64_t t = 0;
+        for (int64_t L = c0; L < n_slots; L += nc) {
+            int IP, J;
+            if (!pair_tile_of(L, args, IP, J)) continue;
+            const int ab = (int)(t & 1);
+            const bool got = mbar_wait_abortable(tfull0 + 8 * ab, (uint32_t)((t >> 1) & 1), args.err, abort_flag);
+            tc_fence_after();
+            asm volatile("bar.sync 1, 128;" ::: "memory");
+            if (!got || *abort_flag) break;
+            float acc[GBN];
+#pragma unroll
+            for (int q = 0; q < GBN; ++q) acc[q] = 0.0f;
+            const uint32_t trow = tmem + (uint32_t)(ab * TMEM_COLS) + ((uint32_t)((warp & 3) * 32) << 16);
+#pragma unroll
+            for (int c = 0; c < NCOLS / 16; ++c) {
+                float v[16];
+                tmem_ld16(trow + c * 16, v);
+#pragma unroll
+                for (int e = 0; e < 16; ++e) {
+                    const int col = c * 16 + e;
+                    const float p = v[e] * args.inv_m;
+                    const float tt = (p > 0.0f) ? p * __log2f(p) : 0.0f;
+                    acc[col / BINS] += tt;
+                }
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive_remote(te_leader + 8 * ab);
+#pragma unroll
+            for (int q = 0; q < GBN; ++q) part[row * PSTRIDE + q] = acc[q];
+            asm volatile("bar.sync 1, 128;" ::: "memory");
+            const int64_t gi0 = (int64_t)(2 * IP + (int)rank) * GA, gj0 = (int64_t)J * GBN;
+            for (int p = etid; p < GA * GBN; p += 128) {
+                const int il = p / GBN, jl = p - il * GBN;
+                const int64_t i = gi0 + il, j = gj0 + jl;
+                if (i >= args.n || j >= args.n || j < i) continue;
+                double sum = 0.0;
+#pragma unroll
+                for (int a = 0; a < BINS; ++a) sum += (double)part[(il * BINS + a) * PSTRIDE + jl];
+                const float val = (float)(args.H[i] + args.H[j] + sum);
+                args.MI[i * args.ldmi + j] = val;
+                args.MI[j * args.ldmi + i] = val;
+            }
+            ++t;
+        }
+    }
+    tc_fence_before();
+    cluster_sync_all();  // no MMA, load or remote arrive of either CTA is outstanding
+    if (warp == 1) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * TMEM_COLS));
+    }
+}
+
 // ---------------------------------------------------------------- host side
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
@@ -500,16 +841,83 @@ bool make_map8(CUtensorMap* map, const uint8_t* base, int64_t rows, int64_t ldw,
     return r == CUDA_SUCCESS;
 }
 
-template <int MODE, int STAGES>
-cudaError_t launch_mode(const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorMap& b0, const CUtensorMap& b1,
-                        const CUtensorMap& a2, const CUtensorMap& b2, const TcArgs& a, int64_t n_slots, int64_t grid,
-                        size_t smem, cudaStream_t stream) {
-    cudaError_t e = cudaFuncSetAttribute(mi_tc_kernel<MODE, STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+// The 2-SM form: clusters of two CTAs, as many as fit at once (persistent).
+// Returns cudaErrorNotSupported when no cluster of two fits (the caller then
+// runs the 1-SM form).
+template <int MODE, int STAGES, int SUB>
+cudaError_t launch_pair(const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorMap& b0, const CUtensorMap& b1,
+                        const CUtensorMap& a2, const CUtensorMap& b2, const TcArgs& a, int64_t n_slots,
+                        cudaStream_t stream) {
+    constexpr uint32_t stage_bytes = SUB * (MODE == TC_SPLIT16 ? 2u : 1u) * (A_BYTES + BH_BYTES);
+    const size_t smem = 1024 + STAGES * stage_bytes + MROWS * PSTRIDE * 4 + 16 * STAGES + 32 + 16;
+    cudaError_t e = cudaFuncSetAttribute(mi_tc_pair_kernel<MODE, STAGES, SUB>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    mi_tc_kernel<MODE, STAGES><<<(unsigned)grid, 192, smem, stream>>>(a0, a1, b0, b1, a2, b2, a, n_slots);
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 2;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.blockDim = dim3(192, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int sms = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cfg.gridDim = dim3((unsigned)(sms & ~1), 1, 1);
+    int clusters = 0;
+    e = cudaOccupancyMaxActiveClusters(&clusters, mi_tc_pair_kernel<MODE, STAGES, SUB>, &cfg);
+    if (e != cudaSuccess || clusters < 1) {
+        cudaGetLastError();
+        return cudaErrorNotSupported;
+    }
+    const int64_t nclu = n_slots < clusters ? n_slots : clusters;
+    cfg.gridDim = dim3((unsigned)(2 * nclu), 1, 1);
+    e = cudaLaunchKernelEx(&cfg, mi_tc_pair_kernel<MODE, STAGES, SUB>, a0, a1, b0, b1, a2, b2, a, n_slots);
+    if (e != cudaSuccess) return e;
     return cudaGetLastError();
 }
+
+// 2-SM form unless MCPG_TC_FORM=1sm (the 1-SM form also runs when no pair fits).
+bool pair_form_enabled() {
+    static int v = -1;
+    if (v < 0) {
+        const char* e = getenv("MCPG_TC_FORM");
+        v = (e && strcmp(e, "1sm") == 0) ? 0 : 1;
+    }
+    return v == 1;
+}
+
+template <int MODE, int STAGES, int SUB>
+cudaError_t launch_mode(const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorMap& b0, const CUtensorMap& b1,
+                        const CUtensorMap& a2, const CUtensorMap& b2, const TcArgs& a, int64_t n_slots, int64_t grid,
+                        cudaStream_t stream) {
+    constexpr uint32_t stage_bytes = SUB * (MODE == TC_SPLIT16 ? 2u : 1u) * (A_BYTES + B_BYTES);
+    const size_t smem = 1024 + STAGES * stage_bytes + MROWS * PSTRIDE * 4 + 16 * STAGES + 32 + 16;
+    cudaError_t e = cudaFuncSetAttribute(mi_tc_kernel<MODE, STAGES, SUB>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    mi_tc_kernel<MODE, STAGES, SUB><<<(unsigned)grid, 192, smem, stream>>>(a0, a1, b0, b1, a2, b2, a, n_slots);
+    return cudaGetLastError();
+}
+
+// Slices (64 samples each) per pipeline stage of the 1-SM / 2-SM forms in the
+// single-pass and FP8-corrected modes (the BF16 split always runs one slice).
+// Measured at 20,000 x 2,000 (weights + MI, ms; FP8-corrected / single BF16):
+// 1-SM 1 slice x 4 stages 116.2 / 56.9, 2 x 2 123.6 / 61.6; 2-SM 1 x 6 117.9 /
+// 60.7, 2 x 3 112.0 / 54.1, 3 x 2 107.0 / 52.2 (BF16 split: 1-SM 139.4, 2-SM 131.6).
+#ifndef MCPG_TC_SUB
+#define MCPG_TC_SUB 1
+#endif
+#ifndef MCPG_TC_PSUB
+#define MCPG_TC_PSUB 3
+#endif
+constexpr int SUB1 = MCPG_TC_SUB, SUB2 = MCPG_TC_PSUB;
+static_assert((SUB1 == 1 || SUB1 == 2 || SUB1 == 4) && (SUB2 == 1 || SUB2 == 2 || SUB2 == 3 || SUB2 == 6),
+              "slices per stage");
 
 }  // namespace
 
@@ -531,19 +939,22 @@ cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, const uint8_t
     cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
     if (major < 10) return cudaErrorNotSupported;
     const int64_t rows = ((n * bins + 255) / 256) * 256 + 256;
+    if (mode == TC_SPLIT16 && !Wlo) return cudaErrorNotSupported;
+    if (mode == TC_F8C && (!H8 || !L8)) return cudaErrorNotSupported;
+    // A maps (128-row boxes) and B maps with b_rows-row boxes (240: whole B tile; 120: a pair's half)
     CUtensorMap ma_hi, ma_lo, mb_hi, mb_lo, ma_l8, mb_l8;
-    if (!make_map(&ma_hi, Whi, fmt, rows, ldw, MROWS) || !make_map(&mb_hi, Whi, fmt, rows, ldw, NCOLS))
-        return cudaErrorNotSupported;
-    ma_lo = ma_l8 = ma_hi;
-    mb_lo = mb_l8 = mb_hi;
-    if (mode == TC_SPLIT16) {
-        if (!Wlo || !make_map(&ma_lo, Wlo, fmt, rows, ldw, MROWS) || !make_map(&mb_lo, Wlo, fmt, rows, ldw, NCOLS))
-            return cudaErrorNotSupported;
-    } else if (mode == TC_F8C) {
-        if (!H8 || !L8 || !make_map8(&ma_lo, H8, rows, ldw, MROWS) || !make_map8(&mb_lo, H8, rows, ldw, NCOLS) ||
-            !make_map8(&ma_l8, L8, rows, ldw, MROWS) || !make_map8(&mb_l8, L8, rows, ldw, NCOLS))
-            return cudaErrorNotSupported;
-    }
+    auto make_maps = [&](uint32_t b_rows) -> bool {
+        if (!make_map(&ma_hi, Whi, fmt, rows, ldw, MROWS) || !make_map(&mb_hi, Whi, fmt, rows, ldw, b_rows))
+            return false;
+        ma_lo = ma_l8 = ma_hi;
+        mb_lo = mb_l8 = mb_hi;
+        if (mode == TC_SPLIT16)
+            return make_map(&ma_lo, Wlo, fmt, rows, ldw, MROWS) && make_map(&mb_lo, Wlo, fmt, rows, ldw, b_rows);
+        if (mode == TC_F8C)
+            return make_map8(&ma_lo, H8, rows, ldw, MROWS) && make_map8(&mb_lo, H8, rows, ldw, b_rows) &&
+                   make_map8(&ma_l8, L8, rows, ldw, MROWS) && make_map8(&mb_l8, L8, rows, ldw, b_rows);
+        return true;
+    };
     TcArgs a;
     a.H = H;
     a.MI = MI;
@@ -569,20 +980,40 @@ cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, const uint8_t
 #endif
         a.GI = gi < 4 ? 4 : gi;
     }
+    if (pair_form_enabled() && gene0 % (2 * GA) == 0 && make_maps(NCOLS / 2)) {
+        // pair units: 24-gene A tiles; same group bytes (a pair tile is two A tiles)
+        TcArgs p = a;
+        p.TI = (int)((n + 2 * GA - 1) / (2 * GA));
+        p.I0 = (int)(gene0 / (2 * GA));
+        p.TIr = (int)((gene1 + 2 * GA - 1) / (2 * GA)) - p.I0;
+        p.GI = a.GI / 2 < 2 ? 2 : a.GI / 2;
+        p.idesc = idesc_f16(fmt == 0 ? 1u : 0u, 2 * MROWS, NCOLS);
+        p.idesc8 = idesc_f16(0u, 2 * MROWS, NCOLS);
+        const int64_t pslots = (int64_t)((p.TIr + p.GI - 1) / p.GI) * p.GI * p.TJ;
+        cudaError_t e;
+        if (mode == TC_SPLIT16)
+            e = launch_pair<TC_SPLIT16, 3, 1>(ma_hi, ma_lo, mb_hi, mb_lo, ma_l8, mb_l8, p, pslots, stream);
+        else if (mode == TC_F8C)
+            e = launch_pair<TC_F8C, 6 / SUB2, SUB2>(ma_hi, ma_lo, mb_hi, mb_lo, ma_l8, mb_l8, p, pslots, stream);
+        else
+            e = launch_pair<TC_SINGLE, 6 / SUB2, SUB2>(ma_hi, ma_lo, mb_hi, mb_lo, ma_l8, mb_l8, p, pslots, stream);
+        if (e != cudaErrorNotSupported) {
+            if (launches) ++*launches;
+            return e;
+        }
+    }
+    if (!make_maps(NCOLS)) return cudaErrorNotSupported;
     const int groups = (a.TIr + a.GI - 1) / a.GI;
     const int64_t n_slots = (int64_t)groups * a.GI * a.TJ;
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int64_t grid = n_slots < sms ? n_slots : sms;
-    const uint32_t stage_bytes = (mode == TC_SPLIT16 ? 2u : 1u) * (A_BYTES + B_BYTES);
-    const int stages = mode == TC_SPLIT16 ? 2 : 4;
-    const size_t smem = 1024 + stages * stage_bytes + MROWS * PSTRIDE * 4 + 16 * stages + 32 + 16;
     if (launches) ++*launches;
     if (mode == TC_SPLIT16)
-        return launch_mode<TC_SPLIT16, 2>(ma_hi, ma_lo, mb_hi, mb_lo, ma_l8, mb_l8, a, n_slots, grid, smem, stream);
+        return launch_mode<TC_SPLIT16, 2, 1>(ma_hi, ma_lo, mb_hi, mb_lo, ma_l8, mb_l8, a, n_slots, grid, stream);
     if (mode == TC_F8C)
-        return launch_mode<TC_F8C, 4>(ma_hi, ma_lo, mb_hi, mb_lo, ma_l8, mb_l8, a, n_slots, grid, smem, stream);
-    return launch_mode<TC_SINGLE, 4>(ma_hi, ma_lo, mb_hi, mb_lo, ma_l8, mb_l8, a, n_slots, grid, smem, stream);
+        return launch_mode<TC_F8C, 4 / SUB1, SUB1>(ma_hi, ma_lo, mb_hi, mb_lo, ma_l8, mb_l8, a, n_slots, grid, stream);
+    return launch_mode<TC_SINGLE, 4 / SUB1, SUB1>(ma_hi, ma_lo, mb_hi, mb_lo, ma_l8, mb_l8, a, n_slots, grid, stream);
 }
 
 }  // namespace mcpg
