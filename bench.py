@@ -577,7 +577,7 @@ def pipeline_arm(args, ws, rank, local):
 
     pairs = n * (n - 1) // 2
     mi_flops = 2.0 * b * b * m * pairs
-    w_ms = prof.get("bspline_weights16", {}).get("ms", float("nan"))
+    w_ms = prof.get("bspline_weights_f8", prof.get("bspline_weights16", {})).get("ms", float("nan"))
     tc_ms = prof.get("mi_tc", {}).get("ms", float("nan"))
     ldw = -(-m // 64) * 64
     w_bytes = n * m * 4 + 2 * n * b * ldw * 2
@@ -593,8 +593,11 @@ def pipeline_arm(args, ws, rank, local):
                                      "frac_hbm": w_bytes / (w_ms / 1e3) / hbm}
         stages["mi_tc"] = {"ms": tc_ms, "TFLOP/s_algorithmic": mi_flops / (tc_ms / 1e3) / 1e12,
                            "frac_tensor_algorithmic": mi_flops / (tc_ms / 1e3) / tc_peak,
-                           "frac_tensor_issued": 3.0 * mi_flops * (128 / 120) / (tc_ms / 1e3) / tc_peak
-                           if args.precision.endswith("x3") else None}
+                           # BF16-equivalent issued work: x3 for the 16-bit split, x2 for bf16f8
+                           # (one BF16 pass + an E4M3 pass of twice the flops at twice the rate)
+                           "frac_tensor_issued": {"bf16x3": 3.0, "fp16x3": 3.0, "bf16f8": 2.0, "bf16": 1.0,
+                                                  "fp16": 1.0}.get(args.precision, 0.0)
+                           * mi_flops * (128 / 120) / (tc_ms / 1e3) / tc_peak}
     stages["maxmin_M1_M2_M3_with_ratios"] = {"ms": mm_ms, "Gop/s_executed": mm_ops_exec / (mm_ms / 1e3) / 1e9,
                                              "frac_alu_peak": mm_ops_exec / (mm_ms / 1e3) / alu_peak}
     dpi_ms = st["dpi"] * 1e3

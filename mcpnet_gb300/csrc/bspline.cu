@@ -45,6 +45,10 @@ struct Knots {
     // divisions become multiplications by these exact reciprocals without
     // changing a bit.  r1[p][i] = 1 / (t[i+p-1] - t[i]), r2[p][i] = 1 / (t[i+p] - t[i+1]).
     int pow2;
+    // The reference's guards compare a float against the double 1e-10.  For a float x,
+    // (double)x < 1e-10 exactly when x < eps, eps = the smallest float above 1e-10
+    // (1e-10 is not a float), so the guards run on the FP32 pipe with the same outcome.
+    float eps;
     float r1[KMAX_ORDER + 1][KNOTS_MAX];
     float r2[KMAX_ORDER + 1][KNOTS_MAX];
 };
@@ -60,6 +64,8 @@ void host_knots(int bins, int order, Knots& k) {
     for (int i = 0; i < order; ++i) k.v[i] = 0.0f;
     for (int i = order; i < order + nint; ++i) k.v[i] = (float)((double)(float)(i - order + 1) * nf);
     for (int i = order + nint; i < 2 * order + nint; ++i) k.v[i] = 1.0f;
+    k.eps = (float)1e-10;
+    if ((double)k.eps < 1e-10) k.eps = std::nextafter(k.eps, INFINITY);
     // exact reciprocals of the knot spans, when they are all powers of two
     k.pow2 = 1;
     for (int p = 0; p <= KMAX_ORDER; ++p)
@@ -101,7 +107,7 @@ __device__ __forceinline__ void basis_all(const Knots& kv, int bins_rt, int orde
         if (i >= n1) break;
         const float a = kv.v[i], b = kv.v[i + 1];
         const bool in = (t >= a && t < b && a < b) ||
-                        (fabs((double)__fsub_rn(t, b)) < 1e-10 && (i + 1 == bins));
+                        (fabsf(__fsub_rn(t, b)) < kv.eps && (i + 1 == bins));
         N[i] = in ? 1.0f : 0.0f;
     }
 #pragma unroll
@@ -121,14 +127,14 @@ __device__ __forceinline__ void basis_all(const Knots& kv, int bins_rt, int orde
             const float d2 = __fsub_rn(kv.v[i + p], kv.v[i + 1]);
             const float n2v = __fsub_rn(kv.v[i + p], t);
             float r;
-            if (d1 < 1e-10 && d2 < 1e-10) {
+            if (d1 < kv.eps && d2 < kv.eps) {
                 r = 0.0f;
             } else {
                 float e1, e2;
-                if (d1 < 1e-10) {
+                if (d1 < kv.eps) {
                     e1 = 0.0f;
                     e2 = __fmul_rn(span_div(kv, n2v, d2, kv.r2[p][i]), N[i + 1]);
-                } else if (d2 < 1e-10) {
+                } else if (d2 < kv.eps) {
                     e2 = 0.0f;
                     e1 = __fmul_rn(span_div(kv, n1v, d1, kv.r1[p][i]), N[i]);
                 } else {
