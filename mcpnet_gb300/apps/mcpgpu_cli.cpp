@@ -19,7 +19,8 @@
 //       here the FP32 GPU path), 1 = adaptive partitioning (the reference's
 //       default; U[0, 1e-5) tie-breaking noise added first, as mi.cpp:121-131 and
 //       mcpnet.cpp:293 do), 2 = B-spline on tensor cores, BF16 hi+lo split,
-//       3 = BF16, 4 = FP16, 5 = FP16 hi+lo.
+//       3 = BF16, 4 = FP16, 5 = FP16 hi+lo, 6 = BF16 hi*hi plus the E4M3
+//       hi*lo + lo*hi correction (the fastest form within 1e-4 nats).
 //   MCP (`mcp -m`, `mcpnet -m`): 1 = MCP2, 2 = MCP3, 3 = MCP4 (apps/filter/mcp.cpp:62-66),
 //       and for mcpnet 4 = ensemble MCP (apps/pipeline/mcpnet.cpp:63-68, 519-719)
 //       with its Stouffer variant (row statistics: see include/mcpgpu.h).
@@ -275,9 +276,10 @@ std::string compute_mi(mcpgpu::Context& ctx, const Named& in, int method, int bi
         case 3: mcpgpu::compute_mi(ctx, in.m, bins, mi, mcpgpu::MIPrecision::BF16, order); return "_bs";
         case 4: mcpgpu::compute_mi(ctx, in.m, bins, mi, mcpgpu::MIPrecision::FP16, order); return "_bs";
         case 5: mcpgpu::compute_mi(ctx, in.m, bins, mi, mcpgpu::MIPrecision::FP16X3, order); return "_bs";
+        case 6: mcpgpu::compute_mi(ctx, in.m, bins, mi, mcpgpu::MIPrecision::BF16F8, order); return "_bs";
         default:
             throw std::runtime_error("unsupported MI method " + std::to_string(method) +
-                                     " (0 = B-spline FP32, 1 = adaptive partitioning, 2..5 = tensor-core B-spline)");
+                                     " (0 = B-spline FP32, 1 = adaptive partitioning, 2..6 = tensor-core B-spline)");
     }
 }
 

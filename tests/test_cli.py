@@ -98,6 +98,21 @@ def test_csv_round_trip(built_lib, tmp_path):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("method,prec", [("2", "bf16x3"), ("6", "bf16f8")])
+def test_cli_tensor_core_mi(built_lib, gpu, tmp_path, method, prec):
+    """`mi -m 2` / `-m 6`: the tensor-core B-spline forms, the same matrix as the library call."""
+    X = built_lib.synth_grn(40, 300, seed=13)
+    write_exp(tmp_path / "x.exp", X)
+    r = run("mi", "-i", tmp_path / "x.exp", "-o", tmp_path / "mi.exp", "-m", method)
+    assert r.returncode == 0, r.stderr
+    want = gpu.bspline_mi(read_exp(tmp_path / "x.exp"), 10, 3, prec)
+    np.fill_diagonal(want, 0.0)
+    got = read_exp(tmp_path / "mi.exp")
+    np.fill_diagonal(got, 0.0)
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.gpu
 def test_cli_ap_mi(built_lib, gpu, tmp_path):
     """`mi -m 1` (the reference's default): seeded U[0, 1e-5) noise, ranks, AP MI."""
     X = built_lib.synth_grn(50, 300, seed=12)
