@@ -201,11 +201,7 @@ struct TcArgs {
     uint32_t idesc;
     uint32_t idesc8;   // kind::f8f6f4 (TC_F8C)
     int* err;
-    float* dbg;        // nullable: tile (0, 0) stores its raw 128 x 240 accumulator here
 };
-
-// Raw-accumulator dump target for kernel bring-up harnesses (null in the library).
-float* g_tc_debug_dump = nullptr;
 
 __device__ __forceinline__ int j_min_for(int I) {
     // first B tile with some j >= i for A tile I: 24 J + 23 >= 12 I
@@ -259,6 +255,50 @@ __device__ __forceinline__ bool tile_of(int64_t L, const TcArgs& a, int& I, int&
     J = r / a.GI;
     I = a.I0 + g * a.GI + (r - J * a.GI);
     return I < a.I0 + a.TIr && I < a.TI && J >= j_min_for(I);
+}
+
+// One tile's epilogue (warps 2-5, one accumulator row per thread): reads the
+// 128 x 240 accumulator at trow with tcgen05.ld, sums p*log2(p) per (row, B gene)
+// in FP32, hands the accumulator back through free_acc(), then forms
+// H_i + H_j - H_ij in FP64 for the tile's pairs (i in [gi0, gi0 + 12),
+// j in [gj0, gj0 + 24), j >= i) and stores both mirror entries.  The (n*bins)^2
+// joint table never leaves tensor memory.
+template <typename FreeAcc>
+__device__ __forceinline__ void epilogue_tile(uint32_t trow, float* part, int row, int etid, const TcArgs& args,
+                                              int64_t gi0, int64_t gj0, FreeAcc free_acc) {
+    float acc[GBN];
+#pragma unroll
+    for (int q = 0; q < GBN; ++q) acc[q] = 0.0f;
+#pragma unroll
+    for (int c = 0; c < NCOLS / 16; ++c) {
+        float v[16];
+        tmem_ld16(trow + c * 16, v);
+#pragma unroll
+        for (int e = 0; e < 16; ++e) {
+            const int col = c * 16 + e;
+            const float p = v[e] * args.inv_m;
+            const float tt = (p > 0.0f) ? p * __log2f(p) : 0.0f;
+            acc[col / BINS] += tt;
+        }
+    }
+    // the accumulator may be overwritten from here on
+    tc_fence_before();
+    __syncwarp();
+    free_acc();
+#pragma unroll
+    for (int q = 0; q < GBN; ++q) part[row * PSTRIDE + q] = acc[q];
+    asm volatile("bar.sync 1, 128;" ::: "memory");
+    for (int p = etid; p < GA * GBN; p += 128) {
+        const int il = p / GBN, jl = p - il * GBN;
+        const int64_t i = gi0 + il, j = gj0 + jl;
+        if (i >= args.n || j >= args.n || j < i) continue;
+        double sum = 0.0;
+#pragma unroll
+        for (int a = 0; a < BINS; ++a) sum += (double)part[(il * BINS + a) * PSTRIDE + jl];
+        const float val = (float)(args.H[i] + args.H[j] + sum);  // sum = -H_ij
+        args.MI[i * args.ldmi + j] = val;
+        args.MI[j * args.ldmi + i] = val;
+    }
 }
 
 // Persistent, warp-specialised CTA (one per SM):
@@ -434,45 +474,10 @@ __global__ void __launch_bounds__(192, 1)
             // uniform across the 128 epilogue threads (.sync.aligned loads below)
             asm volatile("bar.sync 1, 128;" ::: "memory");
             if (!got || *abort_flag) break;
-            float acc[GBN];
-#pragma unroll
-            for (int q = 0; q < GBN; ++q) acc[q] = 0.0f;
             const uint32_t trow = tmem + (uint32_t)(ab * TMEM_COLS) + ((uint32_t)((warp & 3) * 32) << 16);
-#pragma unroll
-            for (int c = 0; c < NCOLS / 16; ++c) {
-                float v[16];
-                tmem_ld16(trow + c * 16, v);
-                if (args.dbg && I == 0 && J == 0) {
-#pragma unroll
-                    for (int e = 0; e < 16; ++e) args.dbg[row * NCOLS + c * 16 + e] = v[e];
-                }
-#pragma unroll
-                for (int e = 0; e < 16; ++e) {
-                    const int col = c * 16 + e;
-                    const float p = v[e] * args.inv_m;
-                    const float tt = (p > 0.0f) ? p * __log2f(p) : 0.0f;
-                    acc[col / BINS] += tt;
-                }
-            }
-            // accumulator ab may be overwritten from here on
-            tc_fence_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(tempty0 + 8 * ab);
-#pragma unroll
-            for (int q = 0; q < GBN; ++q) part[row * PSTRIDE + q] = acc[q];
-            asm volatile("bar.sync 1, 128;" ::: "memory");
-            const int64_t gi0 = (int64_t)I * GA, gj0 = (int64_t)J * GBN;
-            for (int p = etid; p < GA * GBN; p += 128) {
-                const int il = p / GBN, jl = p - il * GBN;
-                const int64_t i = gi0 + il, j = gj0 + jl;
-                if (i >= args.n || j >= args.n || j < i) continue;
-                double sum = 0.0;
-#pragma unroll
-                for (int a = 0; a < BINS; ++a) sum += (double)part[(il * BINS + a) * PSTRIDE + jl];
-                const float val = (float)(args.H[i] + args.H[j] + sum);  // sum = -H_ij
-                args.MI[i * args.ldmi + j] = val;
-                args.MI[j * args.ldmi + i] = val;
-            }
+            epilogue_tile(trow, part, row, etid, args, (int64_t)I * GA, (int64_t)J * GBN, [&] {
+                if (lane == 0) mbar_arrive(tempty0 + 8 * ab);
+            });
             ++t;
         }
     }
@@ -749,40 +754,10 @@ __global__ void __launch_bounds__(192, 1)
             tc_fence_after();
             asm volatile("bar.sync 1, 128;" ::: "memory");
             if (!got || *abort_flag) break;
-            float acc[GBN];
-#pragma unroll
-            for (int q = 0; q < GBN; ++q) acc[q] = 0.0f;
             const uint32_t trow = tmem + (uint32_t)(ab * TMEM_COLS) + ((uint32_t)((warp & 3) * 32) << 16);
-#pragma unroll
-            for (int c = 0; c < NCOLS / 16; ++c) {
-                float v[16];
-                tmem_ld16(trow + c * 16, v);
-#pragma unroll
-                for (int e = 0; e < 16; ++e) {
-                    const int col = c * 16 + e;
-                    const float p = v[e] * args.inv_m;
-                    const float tt = (p > 0.0f) ? p * __log2f(p) : 0.0f;
-                    acc[col / BINS] += tt;
-                }
-            }
-            tc_fence_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive_remote(te_leader + 8 * ab);
-#pragma unroll
-            for (int q = 0; q < GBN; ++q) part[row * PSTRIDE + q] = acc[q];
-            asm volatile("bar.sync 1, 128;" ::: "memory");
-            const int64_t gi0 = (int64_t)(2 * IP + (int)rank) * GA, gj0 = (int64_t)J * GBN;
-            for (int p = etid; p < GA * GBN; p += 128) {
-                const int il = p / GBN, jl = p - il * GBN;
-                const int64_t i = gi0 + il, j = gj0 + jl;
-                if (i >= args.n || j >= args.n || j < i) continue;
-                double sum = 0.0;
-#pragma unroll
-                for (int a = 0; a < BINS; ++a) sum += (double)part[(il * BINS + a) * PSTRIDE + jl];
-                const float val = (float)(args.H[i] + args.H[j] + sum);
-                args.MI[i * args.ldmi + j] = val;
-                args.MI[j * args.ldmi + i] = val;
-            }
+            epilogue_tile(trow, part, row, etid, args, (int64_t)(2 * IP + (int)rank) * GA, (int64_t)J * GBN, [&] {
+                if (lane == 0) mbar_arrive_remote(te_leader + 8 * ab);
+            });
             ++t;
         }
     }
@@ -970,7 +945,6 @@ cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, const uint8_t
     a.idesc = idesc_f16(fmt == 0 ? 1u : 0u, MROWS, NCOLS);
     a.idesc8 = idesc_f16(0u, MROWS, NCOLS);  // E4M3 x E4M3 (format code 0 in kind::f8f6f4)
     a.err = timeout_flag;
-    a.dbg = g_tc_debug_dump;
     {
         const int64_t tile_bytes = (int64_t)MROWS * ldw * 2 * (mode == TC_SINGLE ? 1 : 2);
         int gi = 1;

@@ -72,3 +72,26 @@ def test_host_slabbed_mi_equals_device_mi(gpu, built_lib, prec):
     gpu.bspline_mi_dev(Xd, dev, 10, 3, prec)
     gpu.synchronize()
     assert np.array_equal(host, dev.cpu().numpy())
+
+
+@pytest.mark.parametrize("prec", ["bf16f8", "bf16x3"])
+def test_one_sm_form_matches_pair_form(gpu, built_lib, tmp_path, prec):
+    """The 1-SM kernel (MCPG_TC_FORM=1sm; also the fallback when no SM pair fits)
+    gives the default 2-SM kernel's MI to FP32 rounding.  The form is chosen once
+    per process, so the 1-SM run is a child process."""
+    import os
+    import subprocess
+    import sys
+    from pathlib import Path
+    root = Path(__file__).resolve().parent.parent
+    X = built_lib.synth_grn(250, 400, seed=91)
+    np.save(tmp_path / "x.npy", X)
+    code = (f"import sys, numpy as np; sys.path.insert(0, {str(root)!r}); import mcpnet_gb300 as M; "
+            f"X = np.load({str(tmp_path / 'x.npy')!r}); "
+            f"np.save({str(tmp_path / 'one.npy')!r}, M.Handle(0).bspline_mi(X, 10, 3, {prec!r}))")
+    r = subprocess.run([sys.executable, "-c", code], env=dict(os.environ, MCPG_TC_FORM="1sm"),
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    one = np.load(tmp_path / "one.npy")
+    pair = gpu.bspline_mi(X, 10, 3, prec)
+    assert np.abs(one - pair).max() <= 2e-6
