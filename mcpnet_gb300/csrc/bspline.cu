@@ -187,6 +187,7 @@ __global__ void __launch_bounds__(WTHREADS) bspline_weights_kernel(const float* 
                                                                    void* __restrict__ out2, int64_t ldo,
                                                                    double* __restrict__ H) {
     __shared__ float fscratch[32];
+    __shared__ float sh_scale;
     __shared__ double psum[KMAX_BINS][WTHREADS / 32];
     const int64_t g = blockIdx.x;
     if (g >= n) return;
@@ -203,7 +204,10 @@ __global__ void __launch_bounds__(WTHREADS) bspline_weights_kernel(const float* 
     }
     mn = block_reduce<float>(mn, op_min, fscratch);
     mx = block_reduce<float>(mx, op_max, fscratch);
-    const float scale = (mx > mn) ? (float)(1.0 / (double)__fsub_rn(mx, mn)) : 1.0f;
+    // the reference's 1 / (max - min) in double, once per gene (FP64 is a narrow pipe here)
+    if (threadIdx.x == 0) sh_scale = (mx > mn) ? (float)(1.0 / (double)__fsub_rn(mx, mn)) : 1.0f;
+    __syncthreads();
+    const float scale = sh_scale;
     const float offset = (mx > mn) ? mn : 0.0f;
 
     CompSum acc[NB];
@@ -266,28 +270,41 @@ __global__ void __launch_bounds__(WTHREADS) bspline_weights_kernel(const float* 
     }
 
     // ---- marginal entropy in FP64 (entropy1d_2, BSplineMI.hpp:204-224) ----
+    // Per-bin sums: each thread's compensated pair is reduced across the warp in
+    // float-float (TwoSum, about 2^-44 relative), converted to FP64 once per warp;
+    // lanes 0..bins-1 of warp 0 then sum the warps and form p log2 p in FP64.
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int a = 0; a < NB; ++a) {
         if (a >= bins) break;
-        double v = acc[a].value();
+        float hs = acc[a].s, hc = acc[a].c;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (lane == 0) psum[a][warp] = v;
+        for (int o = 16; o > 0; o >>= 1) {
+            const float s2 = __shfl_xor_sync(0xffffffffu, hs, o), c2 = __shfl_xor_sync(0xffffffffu, hc, o);
+            const float t = __fadd_rn(hs, s2);
+            const float bp = __fsub_rn(t, hs);
+            const float e = __fadd_rn(__fsub_rn(hs, __fsub_rn(t, bp)), __fsub_rn(s2, bp));
+            hc = __fadd_rn(__fadd_rn(hc, c2), e);
+            hs = t;
+        }
+        if (lane == 0) psum[a][warp] = (double)hs + (double)hc;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        double Hg = 0.0;
-        const double inv_m = 1.0 / (double)m;
-        for (int a = 0; a < bins; ++a) {
+    if (warp == 0) {
+        double term = 0.0;
+        if (lane < bins) {
             double p = 0.0;
-            for (int w2 = 0; w2 < (int)(blockDim.x >> 5); ++w2) p += psum[a][w2];
-            p *= inv_m;
-            if (p > 0.0) Hg += p * log2(p);
+            for (int w2 = 0; w2 < (int)(blockDim.x >> 5); ++w2) p += psum[lane][w2];
+            p *= 1.0 / (double)m;
+            if (p > 0.0) term = p * log2(p);
         }
-        Hg = -Hg;
-        if (H) H[g] = Hg;
-        if (OUT == OUT_REF) static_cast<float*>(out0)[g * ((int64_t)bins * m + 1) + (int64_t)bins * m] = (float)Hg;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) term += __shfl_xor_sync(0xffffffffu, term, o);
+        if (lane == 0) {
+            const double Hg = -term;
+            if (H) H[g] = Hg;
+            if (OUT == OUT_REF) static_cast<float*>(out0)[g * ((int64_t)bins * m + 1) + (int64_t)bins * m] = (float)Hg;
+        }
     }
 }
 
