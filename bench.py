@@ -286,8 +286,9 @@ def gpu_arm(args, ws, rank, local):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": dev_s / args.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "bf16" if args.precision.startswith("bf16") else ("f16" if args.precision.startswith("fp16")
-                                                                   else "f32"),
+        # operand types of the contraction (FP32 accumulation in every tensor-core form)
+        "dtype": {"bf16f8": "bf16+e4m3"}.get(args.precision, "bf16" if args.precision.startswith("bf16") else
+                                             ("f16" if args.precision.startswith("fp16") else "f32")),
         "data": "synthetic (seeded SEM GRN, in-degree ~ Poisson(2), weights +-U(0.5,1.5))",
         "config": workload_config(args, args.precision),
         "clocks": clk, "gpu_launches": launches, "roofline": roofline,
