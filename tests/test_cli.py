@@ -48,6 +48,13 @@ def test_bad_usage_reports(built_lib, tmp_path):
     assert run("mi").returncode != 0
     r = run("frobnicate", "-i", tmp_path / "none.exp", "-o", tmp_path / "o.exp")
     assert r.returncode != 0 and "cannot open" in r.stderr
+    # auc_pr_roc needs a score matrix and exactly one truth source (checked before any GPU work)
+    r = run("auc_pr_roc", "-i", tmp_path / "s.exp")
+    assert r.returncode != 0 and "exactly one of -g" in r.stderr
+    r = run("auc_pr_roc", "-i", tmp_path / "s.exp", "-g", tmp_path / "t.txt", "-x", tmp_path / "t.exp")
+    assert r.returncode != 0 and "exactly one of -g" in r.stderr
+    r = run("auc_pr_roc", "-g", tmp_path / "t.txt")
+    assert r.returncode != 0 and "needs -i" in r.stderr
 
 
 @pytest.mark.gpu
