@@ -459,6 +459,7 @@ cudaError_t launch_mi_bwd_x(const float* X, int64_t n, int64_t m, int64_t ldx, i
                             int64_t g1, const float* gsum, const float* dWq, int64_t lddw, float* dX, int64_t lddx,
                             cudaStream_t stream, int64_t* launches) {
     if (g1 <= g0) return cudaSuccess;
+    if (g0 < 0 || g1 > n) return cudaErrorInvalidValue;
     Knots kv;
     host_knots(bins, order, kv);
     if (launches) ++*launches;
