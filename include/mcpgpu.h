@@ -462,9 +462,14 @@ MCPG_API int mcpg_combo_stouffer_tf_eval(mcpg_handle* h, const float* mi, int64_
  * 0.1, and also 0.2 .. 0.5 with TFs).  All AUPRs are aupr_kernel's
  * (compute_aupr2, mcpnet_helper.hpp:1017-1035).  Fewer than 2^32 entries.
  *
+ * mcpg_shuffle_positions: iteration `seed`'s shuffled order as mask positions, out[k] =
+ * the position of the k-th shuffled entry among `entries` (seed 0: the mask order).
+ * Host only (no handle); MCPG_ERR_ARG for a negative count, 2^32 or more, or a null out.
+ *
  * mcpg_split_aupr: eval_aupr_mcp (eval_mcpnet.cpp:227-301) of one score matrix:
  * full_aupr (nullable) over all entries; train_aupr / test_aupr (nullable,
  * iterations x parts, row-major). */
+MCPG_API int mcpg_shuffle_positions(uint32_t* out, int64_t entries, uint64_t seed);
 MCPG_API int mcpg_split_aupr(mcpg_handle* h, const float* values, int64_t rows, int64_t cols, int64_t ldv,
                              const int8_t* labels, int64_t ldl, int region, const int32_t* row_gene,
                              const uint8_t* col_tf, int64_t iterations, const int64_t* train_counts, int64_t parts,

@@ -133,6 +133,7 @@ ABI += [
     ("mcpg_last_host_access", C.c_int, [_vp]),
 ]
 ABI += [
+    ("mcpg_shuffle_positions", C.c_int, [_vp, _i64, C.c_uint64]),
     ("mcpg_split_aupr", C.c_int, [_vp, _vp, _i64, _i64, _i64, _vp, _i64, C.c_int, _vp, _vp, _i64, _vp, _i64, _vp,
                                   _vp, _vp]),
     ("mcpg_split_aupr_dev", C.c_int, [_vp, _vp, _i64, _i64, _i64, _vp, _i64, C.c_int, _vp, _vp, _i64, _vp, _i64, _vp,
@@ -151,6 +152,18 @@ def train_counts(entries: int, tf: bool = False):
     for f = 0.005, 0.01, 0.02, 0.05, 0.1, and with TFs also 0.2, 0.3, 0.4, 0.5."""
     fr = [0.005, 0.01, 0.02, 0.05, 0.1] + ([0.2, 0.3, 0.4, 0.5] if tf else [])
     return np.array([int(f * float(entries)) for f in fr], dtype=np.int64)
+
+
+def shuffle_positions(entries: int, seed: int) -> np.ndarray:
+    """Iteration `seed`'s shuffled order of the eval_mcpnet app (shuffle_truth,
+    apps/pipeline/eval_mcpnet.cpp:214-224) as mask positions (host only; seed 0 keeps the order)."""
+    out = np.empty(max(int(entries), 0), dtype=np.uint32)
+    rc = lib().mcpg_shuffle_positions(out.ctypes.data if out.size else None, int(entries), int(seed))
+    if rc != 0:
+        raise MCPGError(rc, f"shuffle_positions: bad count {entries}")
+    return out
+
+
 TRANSFORMS = {"stouffer": 0, "clr": 1}
 ROW_STATS = {"all": 0, "exclude_diagonal": 1}
 TRUTH_REGIONS = {"lower": 0, "all": 1, "tf": 2}

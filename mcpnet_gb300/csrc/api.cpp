@@ -1732,18 +1732,89 @@ int split_entries(mcpg_handle* h, const mcpg::TruthRegion& r, const float* const
     return MCPG_OK;
 }
 
+// std::shuffle over E >= 65,536 positions with a 32-bit std::mt19937 swaps a[i]
+// with a[j], j uniform in [0, i], for i = 1 .. E-1 (up to 65,535 positions the
+// library draws two positions per generator call, and std::shuffle itself runs).
+// Every j depends only on the generator, so here the draws run D steps ahead of
+// the swaps and prefetch their targets' cache lines, hiding the random-access
+// latency that bounds the plain loop over a multi-GB array; the swaps keep their
+// order.  The draw is the multiply-shift reduction with rejection of Lemire,
+// "Fast Random Integer Generation in an Interval" (ACM TOMACS 29(1), 2019), the
+// method libstdc++'s uniform_int_distribution applies to a 32-bit generator.  The
+// result is checked against std::shuffle once per process; if they differ (another
+// standard library), std::shuffle runs instead.
+constexpr int64_t SHUFFLE_PAIRED_MAX = 65535;
+
+inline uint32_t draw_below(std::mt19937& g, uint32_t range) {  // uniform in [0, range)
+    uint64_t prod = (uint64_t)(uint32_t)g() * range;
+    uint32_t low = (uint32_t)prod;
+    if (low < range) {
+        const uint32_t threshold = (uint32_t)(0u - range) % range;
+        while (low < threshold) {
+            prod = (uint64_t)(uint32_t)g() * range;
+            low = (uint32_t)prod;
+        }
+    }
+    return (uint32_t)(prod >> 32);
+}
+
+void shuffle_prefetched(uint32_t* a, int64_t E, std::mt19937& g) {
+    constexpr int D = 32;  // steps of look-ahead (a power of two)
+    uint32_t ring[D];
+    const int64_t first = E - 1 < D ? E - 1 : D;
+    for (int64_t k = 1; k <= first; ++k) {  // the targets of steps 1 .. D
+        ring[(k - 1) & (D - 1)] = draw_below(g, (uint32_t)(k + 1));
+        __builtin_prefetch(a + ring[(k - 1) & (D - 1)], 1);
+    }
+    for (int64_t i = 1; i < E; ++i) {
+        const int slot = (int)((i - 1) & (D - 1));
+        const uint32_t j = ring[slot];
+        if (i + D < E) {  // the target of step i + D, drawn after those of steps < i + D
+            ring[slot] = draw_below(g, (uint32_t)(i + D + 1));
+            __builtin_prefetch(a + ring[slot], 1);
+        }
+        const uint32_t t = a[i];
+        a[i] = a[j];
+        a[j] = t;
+    }
+}
+
+bool prefetched_shuffle_matches() {
+    static const bool ok = [] {
+        for (uint32_t seed : {1u, 7u, 2026u}) {
+            const int64_t E = SHUFFLE_PAIRED_MAX + 1 + 4097;
+            std::vector<uint32_t> x((size_t)E), y;
+            std::iota(x.begin(), x.end(), 0u);
+            y = x;
+            std::mt19937 g1(seed), g2(seed);
+            std::shuffle(x.begin(), x.end(), g1);
+            shuffle_prefetched(y.data(), E, g2);
+            if (x != y || g1() != g2()) return false;  // same order and the same generator state after
+        }
+        return true;
+    }();
+    return ok;
+}
+
 // shuffle_truth (apps/pipeline/eval_mcpnet.cpp:214-224): std::shuffle with a
 // std::mt19937 seeded with `seed` over the E mask entries.  std::shuffle's swaps
 // depend only on the length and the generator, so the shuffled entry positions
 // are the reference's order of its (row, col, label) tuples.  seed 0 keeps the
 // mask order.  hp is host work space.
-void shuffle_positions(std::vector<uint32_t>& hp, int64_t E, uint64_t seed) {
-    hp.resize((size_t)E);
-    std::iota(hp.begin(), hp.end(), 0u);
+void shuffle_positions(uint32_t* a, int64_t E, uint64_t seed) {
+    std::iota(a, a + E, 0u);
     if (seed) {
         std::mt19937 g((std::mt19937::result_type)seed);
-        std::shuffle(hp.begin(), hp.end(), g);
+        if (E > SHUFFLE_PAIRED_MAX && E <= (int64_t)UINT32_MAX && prefetched_shuffle_matches())
+            shuffle_prefetched(a, E, g);
+        else
+            std::shuffle(a, a + E, g);
     }
+}
+
+void shuffle_positions(std::vector<uint32_t>& hp, int64_t E, uint64_t seed) {
+    hp.resize((size_t)E);
+    shuffle_positions(hp.data(), E, seed);
 }
 
 int split_perm(mcpg_handle* h, int64_t E, uint64_t seed, std::vector<uint32_t>& hp, uint32_t* dperm) {
@@ -3133,6 +3204,12 @@ int mcpg_split_aupr(mcpg_handle* h, const float* values, int64_t rows, int64_t c
     if ((rc = stage_search(h, "split_aupr", src, lds, rows, cols, labels, ldl, region, row_gene, col_tf, d, dl, &r)))
         return rc;
     return split_aupr_dev(h, d[0], dl[0], r, iterations, train_counts, parts, full_aupr, train_aupr, test_aupr);
+}
+
+int mcpg_shuffle_positions(uint32_t* out, int64_t entries, uint64_t seed) {
+    if (entries < 0 || entries > (int64_t)UINT32_MAX || (entries > 0 && !out)) return MCPG_ERR_ARG;
+    shuffle_positions(out, entries, seed);
+    return MCPG_OK;
 }
 
 int mcpg_split_combo_eval_dev(mcpg_handle* h, const float* mi, int64_t ldm, const float* M1, int64_t ld1,

@@ -337,3 +337,19 @@ def test_split_aupr_composition_edges(port, golden):
     assert full == tuple(g["lower_ref"])[0]
     assert np.all(tr[:, 0] == 0.0) and np.all(te[:, 1] == 0.0)
     assert np.all(tr[:, 1] == full) and np.all(te[:, 0] == full)
+
+
+@pytest.mark.parametrize("E", [0, 1, 2, 1000, 65535, 65536, 65537, 70001, 1 << 20])
+def test_library_shuffle_equals_std_shuffle(built_lib, port, E):
+    """mcpg_shuffle_positions (the split evaluation's shuffle; above 65,535 entries its draws
+    run ahead of the swaps with prefetching) gives std::shuffle's order for every seed, and
+    seed 0 keeps the mask order."""
+    assert np.array_equal(built_lib.shuffle_positions(E, 0), np.arange(E, dtype=np.uint32))
+    for seed in (1, 2, 99, 4000000007):
+        got = built_lib.shuffle_positions(E, seed).astype(np.int64)
+        assert np.array_equal(got, port.shuffle_perm(E, seed % (1 << 32)) if E else got), (E, seed)
+
+
+def test_library_shuffle_rejects_bad_counts(built_lib):
+    with pytest.raises(built_lib.MCPGError):
+        built_lib.shuffle_positions(-1, 1)
