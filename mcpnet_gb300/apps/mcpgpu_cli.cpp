@@ -69,7 +69,11 @@
 // (the same columns separated by commas; the Alias column is optional when
 // reading) or raw binary ".bin" (int64 rows, int64 cols, float32 row-major).
 // Genes are rows.
+#include <omp.h>
+
+#include <algorithm>
 #include <cfloat>
+#include <charconv>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -115,6 +119,16 @@ std::vector<std::string> split(const std::string& line, char sep) {
     return out;
 }
 
+// One float token (up to the separator): std::from_chars, or strtof for what it
+// does not take (a leading '+' or blank); an unparsable token reads as 0, as strtof.
+float parse_float(const char* b, const char* e) {
+    float v = 0.0f;
+    const auto r = std::from_chars(b, e, v);
+    if (r.ec == std::errc() && r.ptr != b) return v;
+    const std::string tok(b, e);
+    return std::strtof(tok.c_str(), nullptr);
+}
+
 Named read_matrix(const std::string& path) {
     Named r;
     if (ends_with(path, ".bin")) {
@@ -131,30 +145,68 @@ Named read_matrix(const std::string& path) {
         for (int64_t j = 0; j < cols; ++j) r.cols.push_back(std::to_string(j));
         return r;
     }
+    // Text (EXP: tab, CSV: comma): the whole file is read, its data lines located,
+    // then parsed in parallel straight into the matrix rows.
     const char sep = ends_with(path, ".csv") ? ',' : '\t';
-    std::ifstream f(path);
-    if (!f) throw std::runtime_error("cannot open " + path);
-    std::string line;
-    if (!std::getline(f, line)) throw std::runtime_error("empty file " + path);
-    std::vector<std::string> head = split(line, sep);
+    std::FILE* fp = std::fopen(path.c_str(), "rb");
+    if (!fp) throw std::runtime_error("cannot open " + path);
+    std::string text;
+    {
+        char chunk[1 << 16];
+        size_t got;
+        while ((got = std::fread(chunk, 1, sizeof chunk, fp)) > 0) text.append(chunk, got);
+        std::fclose(fp);
+    }
+    // line spans [b, e) without the newline or a trailing '\r'
+    std::vector<std::pair<size_t, size_t>> lines;
+    for (size_t pos = 0; pos < text.size();) {
+        const void* nl = std::memchr(text.data() + pos, '\n', text.size() - pos);
+        size_t e = nl ? (size_t)((const char*)nl - text.data()) : text.size();
+        const size_t next = nl ? e + 1 : text.size();
+        if (e > pos && text[e - 1] == '\r') --e;
+        if (e > pos || lines.empty()) lines.emplace_back(pos, e);  // the header may not be skipped
+        pos = next;
+    }
+    if (lines.empty() || text.empty()) throw std::runtime_error("empty file " + path);
+    std::vector<std::string> head = split(text.substr(lines[0].first, lines[0].second - lines[0].first), sep);
     const bool alias = head.size() >= 2 && head[1] == "Alias";
     const size_t skip = alias ? 2 : 1;
     for (size_t k = skip; k < head.size(); ++k) r.cols.push_back(head[k]);
-    std::vector<float> vals;
-    while (std::getline(f, line)) {
-        if (line.empty() || line == "\r") continue;
-        std::vector<std::string> tok = split(line, sep);
-        if (tok.size() != r.cols.size() + skip)
-            throw std::runtime_error("row " + (tok.empty() ? std::string("?") : tok[0]) + " of " + path +
-                                     " has the wrong number of values");
-        r.rows.push_back(tok[0]);
-        for (size_t k = skip; k < tok.size(); ++k) vals.push_back(std::strtof(tok[k].c_str(), nullptr));
+    const int64_t nrows = (int64_t)lines.size() - 1, ncols = (int64_t)r.cols.size();
+    r.m = Matrix<float>(nrows, ncols);
+    r.rows.assign((size_t)nrows, std::string());
+    int64_t bad = -1;  // the first row with the wrong number of values
+#pragma omp parallel for schedule(dynamic, 64) reduction(max : bad)
+    for (int64_t i = 0; i < nrows; ++i) {
+        const char* p = text.data() + lines[(size_t)i + 1].first;
+        const char* end = text.data() + lines[(size_t)i + 1].second;
+        int64_t field = 0, nv = 0;
+        float* out = r.m.data(i);
+        while (true) {
+            const char* q = (const char*)std::memchr(p, sep, (size_t)(end - p));
+            const char* fe = q ? q : end;
+            if (field == 0) {
+                r.rows[(size_t)i].assign(p, fe);
+            } else if (field >= (int64_t)skip) {
+                if (nv < ncols) out[nv] = parse_float(p, fe);
+                ++nv;
+            }
+            ++field;
+            if (!q) break;
+            p = q + 1;
+        }
+        if (nv != ncols) bad = std::max(bad, nrows - i);  // max of (nrows - i): the smallest i
     }
-    r.m = Matrix<float>((int64_t)r.rows.size(), (int64_t)r.cols.size());
-    if (!vals.empty()) std::memcpy(r.m.data(), vals.data(), vals.size() * sizeof(float));
+    if (bad >= 0) {
+        const int64_t i = nrows - bad;
+        throw std::runtime_error("row " + r.rows[(size_t)i] + " of " + path + " has the wrong number of values");
+    }
     return r;
 }
 
+// Text rows are formatted in parallel blocks (std::to_chars, 9 significant digits
+// as "%.9g": every float reads back exactly, also through a double) and written in
+// order.
 void write_matrix(const std::string& path, const Matrix<float>& m, const std::vector<std::string>& rows,
                   const std::vector<std::string>& cols) {
     if (ends_with(path, ".bin")) {
@@ -169,16 +221,40 @@ void write_matrix(const std::string& path, const Matrix<float>& m, const std::ve
     const char sep = ends_with(path, ".csv") ? ',' : '\t';
     std::FILE* f = std::fopen(path.c_str(), "w");
     if (!f) throw std::runtime_error("cannot write " + path);
-    std::fprintf(f, "Id%cAlias", sep);
-    for (int64_t j = 0; j < m.columns(); ++j)
-        std::fprintf(f, "%c%s", sep, j < (int64_t)cols.size() ? cols[(size_t)j].c_str() : std::to_string(j).c_str());
-    std::fprintf(f, "\n");
-    for (int64_t i = 0; i < m.rows(); ++i) {
-        std::fprintf(f, "%s%c---", i < (int64_t)rows.size() ? rows[(size_t)i].c_str() : std::to_string(i).c_str(), sep);
-        for (int64_t j = 0; j < m.columns(); ++j) std::fprintf(f, "%c%.9g", sep, (double)m.at(i, j));
-        std::fprintf(f, "\n");
+    std::string head = std::string("Id") + sep + "Alias";
+    for (int64_t j = 0; j < m.columns(); ++j) {
+        head += sep;
+        head += j < (int64_t)cols.size() ? cols[(size_t)j] : std::to_string(j);
     }
-    std::fclose(f);
+    head += '\n';
+    bool ok = std::fwrite(head.data(), 1, head.size(), f) == head.size();
+    const int64_t R = m.rows(), C = m.columns();
+    const int64_t per_block = std::max<int64_t>(1, (int64_t)(8 << 20) / std::max<int64_t>(1, C * 16));  // ~8 MB
+    const int64_t blocks = (R + per_block - 1) / per_block;
+#pragma omp parallel
+    {
+        std::string buf;
+#pragma omp for ordered schedule(static, 1)
+        for (int64_t b = 0; b < blocks; ++b) {
+            buf.clear();
+            char num[32];
+            for (int64_t i = b * per_block; i < std::min(R, (b + 1) * per_block); ++i) {
+                buf += i < (int64_t)rows.size() ? rows[(size_t)i] : std::to_string(i);
+                buf += sep;
+                buf += "---";
+                const float* row = m.data(i);
+                for (int64_t j = 0; j < C; ++j) {
+                    const auto res = std::to_chars(num, num + sizeof num, row[j], std::chars_format::general, 9);
+                    buf += sep;
+                    buf.append(num, res.ptr);
+                }
+                buf += '\n';
+            }
+#pragma omp ordered
+            if (std::fwrite(buf.data(), 1, buf.size(), f) != buf.size()) ok = false;
+        }
+    }
+    if (std::fclose(f) != 0 || !ok) throw std::runtime_error("cannot write " + path);
 }
 
 struct Args {

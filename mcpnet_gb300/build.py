@@ -92,8 +92,8 @@ def build(force: bool = False, verbose: bool = False) -> Path:
             raise RuntimeError(f"link failed\n{r.stdout}\n{r.stderr}")
     cli_src = APPS / "mcpgpu_cli.cpp"
     if cli_src.exists() and (force or _stale(CLI, [cli_src, LIB, *_headers()])):
-        cmd = ["g++", "-O2", "-std=c++17", f"-I{INCLUDE}", str(cli_src), "-o", str(CLI), f"-L{LIBDIR}", "-lmcpgpu",
-               "-Wl,-rpath,$ORIGIN"]
+        cmd = ["g++", "-O2", "-std=c++17", "-fopenmp", f"-I{INCLUDE}", str(cli_src), "-o", str(CLI), f"-L{LIBDIR}",
+               "-lmcpgpu", "-Wl,-rpath,$ORIGIN"]
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -44,6 +44,32 @@ def test_convert_round_trip(built_lib, tmp_path):
     assert r.returncode == 0 and np.array_equal(read_exp(tmp_path / "y.exp"), X)
 
 
+def test_text_io_round_trip_exact(built_lib, tmp_path):
+    """EXP / CSV text written in parallel blocks (9 significant digits) reads back to the
+    same float bits, through the program and through a double; CRLF lines, blank lines and
+    a leading '+' parse; a row with the wrong number of values is reported."""
+    rng = np.random.default_rng(3)
+    X = rng.standard_normal((301, 257)).astype(np.float32) * np.float32(1e3)
+    X[0, :6] = [0.0, -0.0, 1e-40, 3.4028235e38, -1.1754944e-38, np.float32(1) / 3]
+    with open(tmp_path / "x.bin", "wb") as f:
+        np.array(X.shape, dtype=np.int64).tofile(f)
+        X.tofile(f)
+    for ext in ("exp", "csv"):
+        r = run("convert", "-i", tmp_path / "x.bin", "-o", tmp_path / f"y.{ext}")
+        assert r.returncode == 0, r.stderr
+        r = run("convert", "-i", tmp_path / f"y.{ext}", "-o", tmp_path / f"z_{ext}.bin")
+        assert r.returncode == 0, r.stderr
+        assert np.array_equal(read_bin(tmp_path / f"z_{ext}.bin").view(np.uint32), X.view(np.uint32)), ext
+    assert np.array_equal(read_exp(tmp_path / "y.exp"), X)
+    (tmp_path / "w.exp").write_text("Id\tAlias\ta\tb\r\n\r\ng0\t---\t+1.5\t2e-3\r\ng1\t---\t-0\t7\n")
+    r = run("convert", "-i", tmp_path / "w.exp", "-o", tmp_path / "w.bin")
+    assert r.returncode == 0, r.stderr
+    assert np.array_equal(read_bin(tmp_path / "w.bin"), np.array([[1.5, 2e-3], [-0.0, 7]], np.float32))
+    (tmp_path / "bad.exp").write_text("Id\tAlias\ta\tb\ng0\t---\t1\t2\ng1\t---\t3\n")
+    r = run("convert", "-i", tmp_path / "bad.exp", "-o", tmp_path / "bad.bin")
+    assert r.returncode != 0 and "row g1" in r.stderr and "wrong number of values" in r.stderr
+
+
 def test_bad_usage_reports(built_lib, tmp_path):
     assert run("mi").returncode != 0
     r = run("frobnicate", "-i", tmp_path / "none.exp", "-o", tmp_path / "o.exp")
