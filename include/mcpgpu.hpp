@@ -303,6 +303,15 @@ inline std::vector<int64_t> train_counts(int64_t entries, bool tf) {
     return out;
 }
 
+// shuffle_truth (apps/pipeline/eval_mcpnet.cpp:214-224): iteration `seed`'s shuffled order of
+// `entries` labelled entries as mask positions (host only; seed 0 keeps the order).
+inline std::vector<uint32_t> shuffle_positions(int64_t entries, uint64_t seed) {
+    std::vector<uint32_t> out((size_t)(entries > 0 ? entries : 0));
+    const int rc = mcpg_shuffle_positions(out.data(), entries, seed);
+    if (rc != MCPG_OK) throw Error(rc, "shuffle_positions: bad entry count");
+    return out;
+}
+
 struct SplitAupr {
     double full = 0.0;
     std::vector<double> train, test;  // iterations x parts, row-major
