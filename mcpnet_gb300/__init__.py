@@ -284,6 +284,10 @@ class Handle:
 
     # -- host-buffer entry points --
     def bspline_mi(self, X, bins: int = 10, order: int = 3, precision: str = "fp32", return_H: bool = False):
+        """All-pairs B-spline MI (bits) of the genes (rows) of X, from host memory.  precision:
+        "fp32" (CUDA cores), "bf16f8" (BF16 hi*hi + E4M3 correction: the fastest form within
+        1e-4 nats of FP64), "bf16x3" / "fp16x3" (16-bit hi+lo splits), "bf16" / "fp16" (single
+        rounding).  With return_H, also the FP64 marginal entropies."""
         X = _f32(X)
         n, m = X.shape
         MI = np.empty((n, n), dtype=np.float32)
