@@ -319,7 +319,8 @@ int mi_prepare(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_t ldx
         pl.H = (double*)p;
     }
     if (precision == MCPG_MI_FP32) {
-        if (bins > 12) return fail(h, MCPG_ERR_UNSUPPORTED, "bspline_mi FP32: bins > 12 not supported");
+        if (bins < 2 || bins > 12)
+            return fail(h, MCPG_ERR_UNSUPPORTED, "bspline_mi FP32: bins must be 2..12 (got %d)", bins);
         const int64_t ldwt = round_up(n, 16) * bins;
         const int64_t m_pad = round_up(m, 16);
         void* p;
@@ -1003,6 +1004,7 @@ int mi_bwd_dev(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_t ldx
     if (ldx < m || ldg < n || lddx < m) return fail(h, MCPG_ERR_ARG, "bspline_mi_bwd: leading dimension too small");
     if (bins < 1 || bins > 12 || order < 1 || order > 8 || bins < order)
         return fail(h, MCPG_ERR_ARG, "bspline_mi_bwd: need 1 <= order <= bins <= 12, order <= 8");
+    if (bins < 2) return fail(h, MCPG_ERR_UNSUPPORTED, "bspline_mi_bwd: bins must be 2..12 (got %d)", bins);
     int rc;
     const int64_t ldwt = round_up(n, 16) * bins;
     const int64_t m_pad = round_up(m, 16);

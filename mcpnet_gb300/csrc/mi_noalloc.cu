@@ -17,10 +17,17 @@
 //    MCPG_ERR_SCRATCH_LIMIT before any device work;
 //  - the first call on each device looks up the array's device address
 //    (cudaGetSymbolAddress) with that device current; make that first call
-//    before any stream capture;
+//    before any stream capture.  The address is kept per device together with
+//    the identity of the device's CUDA context: after cudaDeviceReset (or any
+//    other teardown of the primary context) the module is loaded again, the
+//    array may sit elsewhere, and the next call looks the address up again --
+//    so the first call after a reset, too, belongs before any stream capture;
+//  - bins must be 2..12 (the compiled FP32 kernels); other values are rejected
+//    with MCPG_ERR_ARG before any device work;
 //  - every call shares the array and it keeps the last call's contents: the
 //    call clears the zero padding it relies on itself, but calls that overlap
 //    on the GPU (different streams, or other host threads) race on it.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -35,22 +42,59 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH
 
 constexpr int MAX_DEVICES = 64;
 std::mutex g_mu;
-void* g_addr[MAX_DEVICES] = {};
+struct CachedAddress {
+    void* ptr = nullptr;
+    unsigned long long ctx_id = 0;  // identity of the context the address belongs to (0: none yet)
+};
+CachedAddress g_addr[MAX_DEVICES];
 
-// Device address of the scratch array on the current device (looked up once).
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long*);
+
+// Identity of the calling thread's current context, 0 when there is none (or the
+// driver cannot tell).  Unique for the life of the process, unlike the CUcontext
+// handle, which a new context may reuse.
+unsigned long long current_context_id() {
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = (CtxGetCurrentFn)p;
+        p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = (CtxGetIdFn)p;
+    });
+    if (!get_current || !get_id) return 0;
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
+
+// Device address of the scratch array on the current device.  Looked up once per
+// device and context: a different (or no) current context means the device was
+// reset since, and the address is looked up again with the device current.
 cudaError_t scratch_address(void** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= MAX_DEVICES) return cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_addr[dev]) {
+    CachedAddress& c = g_addr[dev];
+    const unsigned long long id = current_context_id();
+    if (!c.ptr || id == 0 || id != c.ctx_id) {
         void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);  // makes the device's primary context current
         if (e != cudaSuccess) return e;
-        g_addr[dev] = p;
+        c.ptr = p;
+        c.ctx_id = current_context_id();
     }
-    *out = g_addr[dev];
+    *out = c.ptr;
     return cudaSuccess;
 }
 
@@ -61,7 +105,7 @@ inline int64_t round_up(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
 extern "C" int mcpg_bspline_mi_fp32_noalloc(const float* X, int64_t n, int64_t m, int64_t ldx, int bins, int order,
                                             float* MI, int64_t ldmi, double* H, void* stream) {
     if (!X || !MI || n < 1 || m < 1 || ldx < m || ldmi < n) return MCPG_ERR_ARG;
-    if (bins < 1 || bins > 12 || order < 1 || order > 8 || bins < order) return MCPG_ERR_ARG;
+    if (bins < 2 || bins > 12 || order < 1 || order > 8 || bins < order) return MCPG_ERR_ARG;
     const int64_t ldwt = round_up(n, 16) * bins;
     const int64_t m_pad = round_up(m, 16);
     const size_t wt_bytes = (size_t)round_up(m_pad * ldwt * (int64_t)sizeof(float), 256);
