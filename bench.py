@@ -136,12 +136,12 @@ class CpuMiSampler:
 
     def __init__(self, n: int, m: int, seed: int):
         from oracle import oracle as O
-        import mcpnet_gb300 as M
+        from synthgrn import synth_grn  # host-only generator: the GPU library is never loaded here
         self.n, self.m = n, m
         R = O.ref()
         self.kind = "reference" if R is not None else "port"
         self.impl = R if R is not None else O.port()
-        X = M.synth_grn(n, m, seed=seed)
+        X = synth_grn(n, m, seed=seed)
         self.W = self.impl.bspline_weights(X)
         self.threads = O.port().threads()
 
@@ -187,9 +187,10 @@ def reference_arm(args, ws, rank):
     print(json.dumps(line), flush=True)
 
 
-# (kernel, precision, genes, samples, bins, order) -> (DRAM bytes per launch, ncu summary)
+# (kernel, precision, genes, samples, bins, order) -> (DRAM bytes per launch, how it was measured)
 MEASURED_TRAFFIC = {
-    ("mi_tc", "bf16f8", 20000, 2000, 10, 3): (44.55e9 + 1.61e9, "profiles/mi_tc_traffic_20000x2000.md"),
+    ("mi_tc", "bf16f8", 20000, 2000, 10, 3): (
+        44.55e9 + 1.61e9, "ncu dram__bytes_read.sum + dram__bytes_write.sum, one full-size launch, one pass"),
 }
 
 

@@ -520,10 +520,12 @@ MCPG_API int mcpg_combo_eval(mcpg_handle* h, const float* mi, int64_t ldm, const
  * library holds until exit; problems whose table (ceil(m/16)*16 x
  * ceil(n/16)*16*bins floats, plus n doubles when H is null) does not fit return
  * MCPG_ERR_SCRATCH_LIMIT.  The first call on a device looks up the array's
- * address with that device current: make it before any stream capture.  All
+ * address with that device current: make it before any stream capture.  The
+ * address is kept per device and CUDA context, so after cudaDeviceReset the next
+ * call looks it up again (make that call, too, before any stream capture).  All
  * calls share the array and it keeps the last call's contents (the call clears
  * the padding it needs); calls that overlap on the GPU race on it.
- * bins <= 12. */
+ * 2 <= bins <= 12 (else MCPG_ERR_ARG, before any device work). */
 MCPG_API int mcpg_bspline_mi_fp32_noalloc(const float* X, int64_t n, int64_t m, int64_t ldx, int bins, int order,
                                           float* MI, int64_t ldmi, double* H, void* cuda_stream);
 
@@ -551,15 +553,6 @@ MCPG_API int mcpg_last_host_access(const mcpg_handle* h);
 /* ---- testing hook: make the next `count` device scratch allocations of this
  * handle fail with MCPG_ERR_OOM (exercises the error path without a GPU fault). */
 MCPG_API int mcpg_test_fail_allocs(mcpg_handle* h, int count);
-
-/* ---- seeded synthetic GRN expression (host only; no device work) ----
- * Random DAG over a random topological order, in-degree ~ Poisson(2) from
- * earlier genes, weights +-U(0.5,1.5); x_g = tanh(sum w x_parent) + N(0, 0.3^2),
- * roots ~ N(0,1); each gene min-max rescaled to [0,1].  X: n x m (ldx >= m).
- * edges (nullable, capacity max_edges pairs of int32 parent,child) receives the
- * ground-truth DAG; n_edges (nullable) gets the edge count. */
-MCPG_API int mcpg_synth_grn(int64_t n, int64_t m, uint64_t seed, float* X, int64_t ldx,
-                            int32_t* edges, int64_t max_edges, int64_t* n_edges);
 
 #ifdef __cplusplus
 }

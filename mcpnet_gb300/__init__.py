@@ -22,6 +22,7 @@ raise.
 from __future__ import annotations
 
 import ctypes as C
+import sys
 from pathlib import Path
 
 import numpy as np
@@ -79,7 +80,6 @@ ABI = [
     ("mcpg_ratio_bwd_dev", C.c_int, [_vp, _vp, _i64, _vp, _i64, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64]),
     ("mcpg_bspline_mi_bwd", C.c_int, [_vp, _vp, _i64, _i64, _i64, C.c_int, C.c_int, _vp, _i64, _vp, _i64]),
     ("mcpg_bspline_mi_bwd_dev", C.c_int, [_vp, _vp, _i64, _i64, _i64, C.c_int, C.c_int, _vp, _i64, _vp, _i64]),
-    ("mcpg_synth_grn", C.c_int, [_i64, _i64, C.c_uint64, _vp, _i64, _vp, _i64, C.POINTER(C.c_int64)]),
     ("mcpg_bspline_mi_fp32_noalloc", C.c_int, [_vp, _i64, _i64, _i64, C.c_int, C.c_int, _vp, _i64, _vp, _vp]),
     ("mcpg_aupr_auroc", C.c_int, [_vp, _vp, _i64, _vp, _i64, _vp, _vp]),
     ("mcpg_aupr_auroc_dev", C.c_int, [_vp, _vp, _i64, _vp, _i64, _vp, _vp]),
@@ -204,19 +204,14 @@ def _f32(a) -> np.ndarray:
 
 
 def synth_grn(n: int, m: int, seed: int = 20260001, with_edges: bool = False):
-    """Seeded synthetic GRN expression (n genes x m samples, float32 in [0, 1])."""
-    X = np.empty((n, m), dtype=np.float32)
-    ne = C.c_int64(0)
-    rc = lib().mcpg_synth_grn(n, m, seed, _ptr(X), m, None, 0, C.byref(ne))
-    if rc:
-        raise MCPGError(rc, "synth_grn failed")
-    if not with_edges:
-        return X
-    E = np.empty((max(ne.value, 1), 2), dtype=np.int32)
-    rc = lib().mcpg_synth_grn(n, 0, seed, None, 1, _ptr(E), ne.value, C.byref(ne))
-    if rc:
-        raise MCPGError(rc, "synth_grn failed")
-    return X, E[: ne.value]
+    """Seeded synthetic GRN expression (n genes x m samples, float32 in [0, 1]),
+    from the host-only generator library (synthgrn, libmcpsynth.so)."""
+    try:
+        from synthgrn import synth_grn as _synth
+    except ImportError:  # the package is used from outside the repository root
+        sys.path.insert(0, str(Path(__file__).resolve().parent.parent))
+        from synthgrn import synth_grn as _synth
+    return _synth(n, m, seed, with_edges)
 
 
 class Handle:

@@ -23,7 +23,8 @@ HERE = Path(__file__).resolve().parent
 PORT_LIB = HERE / "_build" / "libmcporacle.so"
 REF_LIB = HERE / "_ref" / "libmcpref.so"
 REF_FAST_LIB = HERE / "_ref" / "libmcpref_fastmath.so"
-REF_ROOT = Path(os.environ.get("MCPNET_REF_ROOT", "/root/reference"))
+# MCPNet source tree for the reference build; unset = no reference build (the restatement still builds)
+REF_ROOT = Path(os.environ["MCPNET_REF_ROOT"]) if os.environ.get("MCPNET_REF_ROOT") else None
 
 _i64, _vp = C.c_int64, C.c_void_p
 
@@ -32,7 +33,7 @@ def build(with_ref: bool | None = None) -> None:
     """make the oracle (and the reference build when the reference tree exists)."""
     subprocess.run(["make", "-s", "-C", str(HERE), "all"], check=True)
     if with_ref is None:
-        with_ref = (REF_ROOT / "include" / "mcp").is_dir()
+        with_ref = REF_ROOT is not None and (REF_ROOT / "include" / "mcp").is_dir()
     if with_ref:
         subprocess.run(["make", "-s", "-C", str(HERE), "ref", "ref-fast", f"REF_ROOT={REF_ROOT}"], check=True)
 

@@ -1,4 +1,6 @@
-// Seeded synthetic gene-regulatory-network expression data (host only).
+// Seeded synthetic gene-regulatory-network expression data (host only), built
+// as its own library (libmcpsynth.so) so that the CPU-only timing of the
+// reference path and the tests can make inputs without loading libmcpgpu.so.
 //
 // Stands in for MCPNet's GNW / DREAM inputs (absent from the reference
 // snapshot) with the generator the benchmark configurations name:
@@ -21,7 +23,7 @@
 #include <random>
 #include <vector>
 
-#include "../../include/mcpgpu.h"
+#include "../include/mcpsynth.h"
 
 namespace {
 
@@ -57,12 +59,12 @@ int poisson2(std::mt19937_64& rng) {
 
 }  // namespace
 
-extern "C" int mcpg_synth_grn(int64_t n, int64_t m, uint64_t seed, float* X, int64_t ldx, int32_t* edges,
+extern "C" int mcps_synth_grn(int64_t n, int64_t m, uint64_t seed, float* X, int64_t ldx, int32_t* edges,
                               int64_t max_edges, int64_t* n_edges) {
-    if (n < 0 || m < 0 || (n > 0 && m > 0 && (!X || ldx < m))) return MCPG_ERR_ARG;
-    if (n > INT32_MAX) return MCPG_ERR_ARG;
+    if (n < 0 || m < 0 || (n > 0 && m > 0 && (!X || ldx < m))) return MCPS_ERR_ARG;
+    if (n > INT32_MAX) return MCPS_ERR_ARG;
     if (n_edges) *n_edges = 0;
-    if (n == 0) return MCPG_OK;
+    if (n == 0) return MCPS_OK;
 
     std::mt19937_64 rng(seed);
     std::vector<int32_t> order((size_t)n);
@@ -104,7 +106,7 @@ extern "C" int mcpg_synth_grn(int64_t n, int64_t m, uint64_t seed, float* X, int
                 edges[2 * e + 1] = order[(size_t)t];
             }
     }
-    if (m == 0) return MCPG_OK;
+    if (m == 0) return MCPS_OK;
 
     // samples: columns are independent given the graph
     const uint64_t sseed = seed + 1;
@@ -141,5 +143,5 @@ extern "C" int mcpg_synth_grn(int64_t n, int64_t m, uint64_t seed, float* X, int
         const double span = mx - mn;
         for (int64_t s = 0; s < m; ++s) row[s] = span > 0 ? (float)(((double)row[s] - mn) / span) : 0.0f;
     }
-    return MCPG_OK;
+    return MCPS_OK;
 }

@@ -2,11 +2,11 @@
 
 Runs the reference's hot-path headers compiled from the MCPNet source tree
 (oracle/ref/ref_driver.cpp -> oracle/_ref/libmcpref.so; the tree is read from
-$MCPNET_REF_ROOT, default /root/reference) on seeded synthetic inputs and
+$MCPNET_REF_ROOT, which must be set) on seeded synthetic inputs and
 stores inputs and outputs together, so the fixtures need neither the
 reference nor this script at test time.
 
-    python tests/golden/make_golden.py
+    MCPNET_REF_ROOT=<MCPNet source tree> python tests/golden/make_golden.py
 
 Fixtures (all float32 unless noted):
   mi_*.npz       X, W (reference weight rows), MI32 (reference --single MI),
@@ -63,6 +63,8 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--only", choices=["core", "eval", "ap", "stouffer", "tf"], default=None)
     args = ap.parse_args()
+    if O.REF_ROOT is None:
+        raise SystemExit("set MCPNET_REF_ROOT to the MCPNet source tree")
     O.build(with_ref=True)
     R = O.ref()
     if R is None:

@@ -55,3 +55,20 @@ def test_reference_arm_under_torchrun_two_ranks(tmp_path):
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["value"] > 0 and d["n_gpus"] == 2
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["cpu_baseline"]["kind"] in ("port", "reference")
+
+
+def test_reference_arm_never_maps_the_gpu_library():
+    """The reference arm times the CPU path only: its process maps the oracle and
+    the host-only input generator, never libmcpgpu.so."""
+    code = (
+        "import sys; sys.path.insert(0, %r)\n"
+        "import bench\n"
+        "bench.main(['--impl', 'reference', '--genes', '200', '--samples', '100', '--steps', '1', '--warmup', '3',"
+        " '--ref-seconds', '0.05'])\n"
+        "maps = open('/proc/self/maps').read()\n"
+        "print('MAPS', 'libmcpgpu' in maps, 'libmcpsynth' in maps, 'mcpnet_gb300' in sys.modules)\n" % str(ROOT))
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, cwd=str(ROOT),
+                       env=dict(os.environ, OMP_NUM_THREADS="2"))
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = [l for l in r.stdout.splitlines() if l.startswith("MAPS")][0]
+    assert line == "MAPS False True False", line
