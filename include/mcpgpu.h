@@ -554,6 +554,15 @@ MCPG_API int mcpg_last_host_access(const mcpg_handle* h);
  * handle fail with MCPG_ERR_OOM (exercises the error path without a GPU fault). */
 MCPG_API int mcpg_test_fail_allocs(mcpg_handle* h, int count);
 
+/* ---- testing hook: the next tensor-core MI launch of this handle (precision
+ * BF16 / FP16 / BF16X3 / FP16X3 / BF16F8) gives every barrier wait a limit of
+ * wait_ns nanoseconds (1e3..2e9; the default limit is 2 s), and with starve != 0
+ * its TMA producers issue no loads, so the MMA issuer's first wait runs out with
+ * no load or MMA outstanding.  The kernel then raises its timeout flag, frees its
+ * tensor memory and returns; the call returns MCPG_ERR_DEVICE_TIMEOUT and the
+ * handle stays usable.  Exercises the bounded-wait path without a GPU fault. */
+MCPG_API int mcpg_test_tc_timeout(mcpg_handle* h, int64_t wait_ns, int starve);
+
 #ifdef __cplusplus
 }
 #endif

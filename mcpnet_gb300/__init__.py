@@ -46,6 +46,7 @@ ABI = [
     ("mcpg_synchronize", C.c_int, [_vp]),
     ("mcpg_kernel_launches", C.c_int64, [_vp]),
     ("mcpg_test_fail_allocs", C.c_int, [_vp, C.c_int]),
+    ("mcpg_test_tc_timeout", C.c_int, [_vp, _i64, C.c_int]),
     ("mcpg_profile", C.c_int, [_vp, C.c_int]),
     ("mcpg_profile_report", C.c_int64, [_vp, C.c_char_p, C.c_int64]),
     ("mcpg_bspline_mi", C.c_int, [_vp, _vp, _i64, _i64, _i64, C.c_int, C.c_int, C.c_int, _vp, _i64, _vp]),
@@ -276,6 +277,12 @@ class Handle:
 
     def fail_next_allocs(self, count: int):
         self._check(self._L.mcpg_test_fail_allocs(self._h, count), "test_fail_allocs")
+
+    def test_tc_timeout(self, wait_ns: int, starve: bool = True):
+        """Testing hook: the next tensor-core MI launch waits at most wait_ns per barrier
+        wait, and with starve its producers issue no loads (the call then fails with
+        ERR_DEVICE_TIMEOUT and the handle stays usable)."""
+        self._check(self._L.mcpg_test_tc_timeout(self._h, int(wait_ns), int(bool(starve))), "test_tc_timeout")
 
     # -- host-buffer entry points --
     def bspline_mi(self, X, bins: int = 10, order: int = 3, precision: str = "fp32", return_H: bool = False):

@@ -93,6 +93,8 @@ struct mcpg_handle {
     void* buf[NSLOTS] = {};
     size_t cap[NSLOTS] = {};
     int fail_allocs = 0;  // test hook: number of upcoming scratch allocations to fail
+    mcpg::TcWaitHook tc_hook;  // test hook: wait limit / starved producers of the next tensor-core MI launch
+    bool tc_hook_armed = false;
     // host MI: a second stream copies finished row slabs back while later slabs compute
     cudaStream_t copy_stream = nullptr;
     std::vector<cudaEvent_t> slab_events;
@@ -386,9 +388,12 @@ int mi_launch(mcpg_handle* h, const MiPlan& pl, int64_t g0, int64_t g1) {
     {
         PROF(h, "mi_tc");
         const bool f8 = pl.split == mcpg::TC_F8C;
+        const mcpg::TcWaitHook* hook = h->tc_hook_armed ? &h->tc_hook : nullptr;
+        h->tc_hook_armed = false;  // one launch only
         e = mcpg::launch_mi_tc((const uint16_t*)pl.w0, f8 ? nullptr : (const uint16_t*)pl.w1,
                                f8 ? (const uint8_t*)pl.w1 : nullptr, (const uint8_t*)pl.w2, pl.ld, pl.H, pl.n, pl.m,
-                               pl.bins, pl.fmt, pl.split, pl.MI, pl.ldmi, pl.flag, h->stream, &h->launches, g0, g1);
+                               pl.bins, pl.fmt, pl.split, pl.MI, pl.ldmi, pl.flag, h->stream, &h->launches, g0, g1,
+                               hook);
     }
     if (e == cudaErrorNotSupported)
         return fail(h, MCPG_ERR_UNSUPPORTED, "bspline_mi tensor-core path: unsupported shape or device");
@@ -2284,6 +2289,16 @@ int64_t mcpg_profile_report(mcpg_handle* h, char* buf, int64_t len) {
 int mcpg_test_fail_allocs(mcpg_handle* h, int count) {
     if (!h) return MCPG_ERR_ARG;
     h->fail_allocs = count;
+    return MCPG_OK;
+}
+
+int mcpg_test_tc_timeout(mcpg_handle* h, int64_t wait_ns, int starve) {
+    if (!h) return MCPG_ERR_ARG;
+    if (wait_ns < 1000 || wait_ns > (int64_t)mcpg::TC_WAIT_NS_DEFAULT)
+        return fail(h, MCPG_ERR_ARG, "test_tc_timeout: wait_ns must be 1e3..2e9 (got %lld)", (long long)wait_ns);
+    h->tc_hook.wait_ns = (unsigned long long)wait_ns;
+    h->tc_hook.starve = starve ? 1 : 0;
+    h->tc_hook_armed = true;
     return MCPG_OK;
 }
 

@@ -120,10 +120,20 @@ cudaError_t launch_mi_bwd_x(const float* X, int64_t n, int64_t m, int64_t ldx, i
 // Returns cudaErrorNotSupported when the shape/bins is outside the kernel's tiling.
 // Gene range as launch_mi_fp32 (gene0 a multiple of 12).
 enum TcMode : int { TC_SINGLE = 0, TC_SPLIT16 = 1, TC_F8C = 2 };
+// Limit of every mbarrier wait of the tensor-core MI kernels (the kernel gives up,
+// raises *timeout_flag, drains, frees its tensor memory and returns).
+constexpr unsigned long long TC_WAIT_NS_DEFAULT = 2000000000ull;
+// Test hook of one launch: wait_ns replaces the default limit; starve != 0 makes the
+// TMA producers issue no load at all, so the MMA issuer's first wait runs out with
+// no load or MMA outstanding (the timeout path, without a GPU fault).
+struct TcWaitHook {
+    unsigned long long wait_ns = TC_WAIT_NS_DEFAULT;
+    int starve = 0;
+};
 cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, const uint8_t* H8, const uint8_t* L8,
                          int64_t ldw, const double* H, int64_t n, int64_t m, int bins, int fmt, int mode, float* MI,
                          int64_t ldmi, int* timeout_flag, cudaStream_t stream, int64_t* launches, int64_t gene0 = 0,
-                         int64_t gene1 = -1);
+                         int64_t gene1 = -1, const TcWaitHook* hook = nullptr);
 
 // ---------------- gold-standard evaluation (eval.cu) ----------------
 enum TruthMode : int {

@@ -37,9 +37,10 @@
 // x 2,000 (1 MB per A tile) GI 8 144.4 ms, 16 134.5 ms, 32 133.3 ms, 64 162.7
 // ms; at 32,768 x 4,096 (2 MB per A tile) GI 8 902 ms, 16 972 ms, 32 987 ms.
 //
-// Every mbarrier wait is bounded (2 s of %globaltimer): on expiry the kernel
-// raises *err, stops issuing work, drains what it issued (bounded), frees its
-// tensor memory and returns.
+// Every mbarrier wait is bounded (2 s of %globaltimer by default; a test hook sets a
+// shorter limit and can starve the producers): on expiry the kernel raises *err,
+// stops issuing work, drains what it issued (bounded), frees its tensor memory and
+// returns.
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <math.h>
@@ -68,7 +69,6 @@ constexpr uint32_t A8_BYTES = MROWS * BK;      // 8 KB (8-bit correction operand
 constexpr uint32_t B8_BYTES = NCOLS * BK;      // 15 KB
 static_assert(2 * (A8_BYTES + B8_BYTES) == A_BYTES + B_BYTES, "correction slices fill a hi*hi stage");
 constexpr int PSTRIDE = GBN + 1;       // epilogue partials row stride (floats)
-constexpr unsigned long long WAIT_NS = 2000000000ull;
 
 // ---------------------------------------------------------------- PTX wrappers
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -201,6 +201,8 @@ struct TcArgs {
     uint32_t idesc;
     uint32_t idesc8;   // kind::f8f6f4 (TC_F8C)
     int* err;
+    unsigned long long wait_ns;  // limit of every mbarrier wait
+    int starve;                  // test hook: the producers issue no loads
 };
 
 __device__ __forceinline__ int j_min_for(int I) {
@@ -211,14 +213,15 @@ __device__ __forceinline__ int j_min_for(int I) {
 
 // Bounded wait that also gives up as soon as another role raised the CTA's
 // abort flag (so one timeout does not cascade into a long chain of timeouts).
-__device__ __forceinline__ bool mbar_wait_abortable(uint32_t bar, uint32_t parity, int* err, volatile int* abort_flag) {
+__device__ __forceinline__ bool mbar_wait_abortable(uint32_t bar, uint32_t parity, int* err, volatile int* abort_flag,
+                                                    unsigned long long wait_ns) {
     if (mbar_try(bar, parity)) return true;
     const unsigned long long t0 = gtimer();
     for (;;) {
         for (int i = 0; i < 64; ++i)
             if (mbar_try(bar, parity)) return true;
         if (*abort_flag) return false;
-        if (gtimer() - t0 > WAIT_NS) {
+        if (gtimer() - t0 > wait_ns) {
             atomicExch(err, 1);
             *abort_flag = 1;
             return false;
@@ -227,14 +230,14 @@ __device__ __forceinline__ bool mbar_wait_abortable(uint32_t bar, uint32_t parit
 }
 
 __device__ __forceinline__ bool mbar_wait_cluster_abortable(uint32_t bar, uint32_t parity, int* err,
-                                                            volatile int* abort_flag) {
+                                                            volatile int* abort_flag, unsigned long long wait_ns) {
     if (mbar_try_cluster(bar, parity)) return true;
     const unsigned long long t0 = gtimer();
     for (;;) {
         for (int i = 0; i < 64; ++i)
             if (mbar_try_cluster(bar, parity)) return true;
         if (*abort_flag) return false;
-        if (gtimer() - t0 > WAIT_NS) {
+        if (gtimer() - t0 > wait_ns) {
             atomicExch(err, 1);
             *abort_flag = 1;
             return false;
@@ -357,7 +360,7 @@ __global__ void __launch_bounds__(192, 1)
         if (lane == 0) {
             // ---------------- TMA producer ----------------
             int64_t g = 0;  // running k-slice counter across this CTA's tiles
-            bool ok = true;
+            bool ok = !args.starve;
             for (int64_t L = blockIdx.x; L < n_slots && ok; L += gridDim.x) {
                 int I, J;
                 if (!tile_of(L, args, I, J)) continue;
@@ -366,7 +369,7 @@ __global__ void __launch_bounds__(192, 1)
                     const int s = (int)(g % STAGES);
                     const int64_t u = g / STAGES;
                     if (u > 0 && !(ok = mbar_wait_abortable(empty0 + 8 * s, (uint32_t)((u - 1) & 1), args.err,
-                                                            abort_flag)))
+                                                            abort_flag, args.wait_ns)))
                         break;
                     const uint32_t st = base + s * STAGE_BYTES, fb = full0 + 8 * s;
                     const bool corr = F8C && q < QP;
@@ -396,7 +399,7 @@ __global__ void __launch_bounds__(192, 1)
             // drain: the last phase issued on each stage lands before the CTA exits
             for (int s = 0; s < STAGES && (int64_t)s < g; ++s) {
                 const int64_t last = (g - 1 - s) / STAGES;
-                mbar_wait_abortable(full0 + 8 * s, (uint32_t)(last & 1), args.err, abort_flag);
+                mbar_wait_abortable(full0 + 8 * s, (uint32_t)(last & 1), args.err, abort_flag, args.wait_ns);
             }
         }
         __syncwarp();
@@ -411,14 +414,14 @@ __global__ void __launch_bounds__(192, 1)
                 const int ab = (int)(t & 1);
                 const int64_t ua = t >> 1;
                 if (ua > 0 &&
-                    !(ok = mbar_wait_abortable(tempty0 + 8 * ab, (uint32_t)((ua - 1) & 1), args.err, abort_flag)))
+                    !(ok = mbar_wait_abortable(tempty0 + 8 * ab, (uint32_t)((ua - 1) & 1), args.err, abort_flag, args.wait_ns)))
                     break;
                 tc_fence_after();
                 const uint32_t dacc = tmem + (uint32_t)(ab * TMEM_COLS);
                 for (int q = 0; q < QT; ++q, ++g) {
                     const int s = (int)(g % STAGES);
                     if (!(ok = mbar_wait_abortable(full0 + 8 * s, (uint32_t)((g / STAGES) & 1), args.err,
-                                                   abort_flag)))
+                                                   abort_flag, args.wait_ns)))
                         break;
                     tc_fence_after();
                     const uint32_t st = base + s * STAGE_BYTES;
@@ -469,7 +472,7 @@ __global__ void __launch_bounds__(192, 1)
             int I, J;
             if (!tile_of(L, args, I, J)) continue;
             const int ab = (int)(t & 1);
-            const bool got = mbar_wait_abortable(tfull0 + 8 * ab, (uint32_t)((t >> 1) & 1), args.err, abort_flag);
+            const bool got = mbar_wait_abortable(tfull0 + 8 * ab, (uint32_t)((t >> 1) & 1), args.err, abort_flag, args.wait_ns);
             tc_fence_after();
             // uniform across the 128 epilogue threads (.sync.aligned loads below)
             asm volatile("bar.sync 1, 128;" ::: "memory");
@@ -634,7 +637,7 @@ __global__ void __launch_bounds__(192, 1)
         if (lane == 0) {
             // ---------------- TMA producer (both CTAs: own A tile, own half of B) ----------------
             int64_t g = 0;
-            bool ok = true;
+            bool ok = !args.starve;
             for (int64_t L = c0; L < n_slots && ok; L += nc) {
                 int IP, J;
                 if (!pair_tile_of(L, args, IP, J)) continue;
@@ -644,7 +647,7 @@ __global__ void __launch_bounds__(192, 1)
                     const int s = (int)(g % STAGES);
                     const int64_t u = g / STAGES;
                     if (u > 0 && !(ok = mbar_wait_abortable(empty0 + 8 * s, (uint32_t)((u - 1) & 1), args.err,
-                                                            abort_flag)))
+                                                            abort_flag, args.wait_ns)))
                         break;
                     const uint32_t st = base + s * STAGE_BYTES;
                     const uint32_t fb = map_to_rank(full0 + 8 * s, 0);
@@ -676,7 +679,7 @@ __global__ void __launch_bounds__(192, 1)
             // (the multicast commits reach both CTAs), so no load is still in flight
             for (int s = 0; s < STAGES && (int64_t)s < g; ++s) {
                 const int64_t last = (g - 1 - s) / STAGES;
-                mbar_wait_abortable(empty0 + 8 * s, (uint32_t)(last & 1), args.err, abort_flag);
+                mbar_wait_abortable(empty0 + 8 * s, (uint32_t)(last & 1), args.err, abort_flag, args.wait_ns);
             }
         }
         __syncwarp();
@@ -691,14 +694,14 @@ __global__ void __launch_bounds__(192, 1)
                 const int ab = (int)(t & 1);
                 const int64_t ua = t >> 1;
                 if (ua > 0 && !(ok = mbar_wait_cluster_abortable(tempty0 + 8 * ab, (uint32_t)((ua - 1) & 1),
-                                                                 args.err, abort_flag)))
+                                                                 args.err, abort_flag, args.wait_ns)))
                     break;
                 tc_fence_after();
                 const uint32_t dacc = tmem + (uint32_t)(ab * TMEM_COLS);
                 for (int q = 0; q < QT; ++q, ++g) {
                     const int s = (int)(g % STAGES);
                     if (!(ok = mbar_wait_abortable(full0 + 8 * s, (uint32_t)((g / STAGES) & 1), args.err,
-                                                   abort_flag)))
+                                                   abort_flag, args.wait_ns)))
                         break;
                     tc_fence_after();
                     const uint32_t st = base + s * STAGE_BYTES;
@@ -750,7 +753,7 @@ __global__ void __launch_bounds__(192, 1)
             int IP, J;
             if (!pair_tile_of(L, args, IP, J)) continue;
             const int ab = (int)(t & 1);
-            const bool got = mbar_wait_abortable(tfull0 + 8 * ab, (uint32_t)((t >> 1) & 1), args.err, abort_flag);
+            const bool got = mbar_wait_abortable(tfull0 + 8 * ab, (uint32_t)((t >> 1) & 1), args.err, abort_flag, args.wait_ns);
             tc_fence_after();
             asm volatile("bar.sync 1, 128;" ::: "memory");
             if (!got || *abort_flag) break;
@@ -901,7 +904,7 @@ static_assert((SUB1 == 1 || SUB1 == 2 || SUB1 == 4) && (SUB2 == 1 || SUB2 == 2 |
 cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, const uint8_t* H8, const uint8_t* L8,
                          int64_t ldw, const double* H, int64_t n, int64_t m, int bins, int fmt, int mode, float* MI,
                          int64_t ldmi, int* timeout_flag, cudaStream_t stream, int64_t* launches, int64_t gene0,
-                         int64_t gene1) {
+                         int64_t gene1, const TcWaitHook* hook) {
     if (bins != BINS || (ldw % BK) != 0) return cudaErrorNotSupported;
     if (mode != TC_SINGLE && mode != TC_SPLIT16 && mode != TC_F8C) return cudaErrorInvalidValue;
     if (mode == TC_F8C && fmt != 0) return cudaErrorInvalidValue;
@@ -945,6 +948,8 @@ cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, const uint8_t
     a.idesc = idesc_f16(fmt == 0 ? 1u : 0u, MROWS, NCOLS);
     a.idesc8 = idesc_f16(0u, MROWS, NCOLS);  // E4M3 x E4M3 (format code 0 in kind::f8f6f4)
     a.err = timeout_flag;
+    a.wait_ns = hook ? hook->wait_ns : TC_WAIT_NS_DEFAULT;
+    a.starve = hook ? hook->starve : 0;
     {
         const int64_t tile_bytes = (int64_t)MROWS * ldw * 2 * (mode == TC_SINGLE ? 1 : 2);
         int gi = 1;

@@ -251,32 +251,59 @@ void FN(orc_max_transpose)(const REAL* M, int64_t n, int64_t ldm, REAL* out, int
         }
 }
 
-/* dpi_kernel<IT,true,true> -- include/mcp/filter/dpi.hpp:42-69, followed by
- * mask<IT,true> -- include/mcp/filter/threshold.hpp:33-54, as driven by
- * apps/filter/dpi.cpp:236-287.  Returns the "removed" count (mask.processed). */
+/* dpi_kernel<IT,true,true>::operator()(x, z, row_x, row_z, count) --
+ * include/mcp/filter/dpi.hpp:56-68: delete (x, z) if x == z, or if some
+ * y not in {x, z} has row_x[y] >= i_xz and row_z[y] >= i_xz, with
+ * i_xz = (IT)(row_x[z] * tol_multiplier) and tol_multiplier = 1/(1 - tol) in
+ * double (dpi.hpp:47). */
+static int FN(dpi_delete)(const REAL* A, int64_t n, int64_t lda, double tm, int64_t x, int64_t z) {
+    if (x == z) return 1;
+    const REAL* rx = A + x * lda;
+    const REAL* rz = A + z * lda;
+    REAL ixz = (REAL)((double)rx[z] * tm);
+    int64_t y = 0;
+    for (; y < n && (y == x || y == z || rx[y] < ixz || rz[y] < ixz); ++y) {}
+    return y < n;
+}
+
+/* The dpi app's filter: dpi_kernel over every (x, z) -- as driven by
+ * apps/filter/dpi.cpp:236-287 -- followed by mask<IT,true> --
+ * include/mcp/filter/threshold.hpp:33-54.  Returns the "removed" count
+ * (mask.processed). */
 int64_t FN(orc_dpi)(const REAL* A, int64_t n, int64_t lda, double tol, REAL* out, int64_t ldo, uint8_t* mask) {
     double tm = 1.0 / (1.0 - tol);
     int64_t removed = 0;
 #pragma omp parallel for schedule(dynamic, 1) reduction(+:removed)
     for (int64_t x = 0; x < n; ++x) {
-        const REAL* rx = A + x * lda;
         for (int64_t z = 0; z < n; ++z) {
-            const REAL* rz = A + z * lda;
-            int del;
-            if (x == z) {
-                del = 1;
-            } else {
-                REAL ixz = (REAL)((double)rx[z] * tm);
-                int64_t y = 0;
-                for (; y < n && (y == x || y == z || rx[y] < ixz || rz[y] < ixz); ++y) {}
-                del = y < n;
-            }
+            int del = FN(dpi_delete)(A, n, lda, tm, x, z);
             if (mask) mask[x * n + z] = (uint8_t)del;
-            REAL in = rx[z];
+            REAL in = A[x * lda + z];
             REAL o = del ? (REAL)0 : in;
             out[x * ldo + z] = o;
             removed += (o != in);
         }
+    }
+    return removed;
+}
+
+/* orc_dpi restricted to the rows x = rows[0..nr) of the output: row r of out and
+ * mask (mask row stride n) is row rows[r] of the full filter; returns the removed
+ * count of these rows.  For sampled-row checks of matrices too large to filter
+ * whole on the CPU. */
+int64_t FN(orc_dpi_rows)(const REAL* A, int64_t n, int64_t lda, double tol, const int64_t* rows, int64_t nr,
+                         REAL* out, int64_t ldo, uint8_t* mask) {
+    double tm = 1.0 / (1.0 - tol);
+    int64_t removed = 0;
+#pragma omp parallel for schedule(dynamic, 64) reduction(+:removed)
+    for (int64_t q = 0; q < nr * n; ++q) {
+        const int64_t r = q / n, z = q - r * n, x = rows[r];
+        int del = FN(dpi_delete)(A, n, lda, tm, x, z);
+        if (mask) mask[r * n + z] = (uint8_t)del;
+        REAL in = A[x * lda + z];
+        REAL o = del ? (REAL)0 : in;
+        out[r * ldo + z] = o;
+        removed += (o != in);
     }
     return removed;
 }
@@ -340,6 +367,44 @@ int FN(orc_closure)(const REAL* A, int64_t n, int64_t lda, REAL* out, int64_t ld
     for (int64_t i = 0; i < n; ++i) memcpy(out + i * ldo, cur + i * n, sizeof(REAL) * (size_t)n);
     free(cur); free(nxt);
     return changed ? -1 : it;
+}
+
+/* Rows rows[0..nr) of the maximum-capacity closure of a SYMMETRIC matrix, by a
+ * widest-path search from each row (a bottleneck form of Dijkstra's algorithm),
+ * independent of orc_closure's repeated squaring.  For x = rows[r]:
+ * out[r][j] (j != x) = max over paths x -> j of the smallest entry on the path
+ * (the direct entry included); out[r][x] = max(A[x][x], max over j != x of
+ * out[r][j]), the value the squaring B <- max(B, B (x) B) leaves on the diagonal
+ * of a symmetric matrix.  Only min and max are taken, so every output is an
+ * input entry and the comparison with the squaring is exact.  O(n^2) per row. */
+void FN(orc_widest_rows)(const REAL* A, int64_t n, int64_t lda, const int64_t* rows, int64_t nr, REAL* out,
+                         int64_t ldo) {
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t r = 0; r < nr; ++r) {
+        const int64_t x = rows[r];
+        REAL* cap = out + r * ldo;
+        uint8_t* done = (uint8_t*)calloc((size_t)(n > 0 ? n : 1), 1);
+        for (int64_t j = 0; j < n; ++j) cap[j] = A[x * lda + j];
+        done[x] = 1;
+        for (int64_t it = 1; it < n; ++it) {
+            int64_t u = -1;
+            for (int64_t j = 0; j < n; ++j)
+                if (!done[j] && (u < 0 || cap[u] < cap[j])) u = j;
+            done[u] = 1;
+            const REAL cu = cap[u];
+            const REAL* au = A + u * lda;
+            for (int64_t v = 0; v < n; ++v) {
+                if (done[v]) continue;
+                const REAL c = (au[v] < cu) ? au[v] : cu;
+                if (cap[v] < c) cap[v] = c;
+            }
+        }
+        REAL d = A[x * lda + x];
+        for (int64_t j = 0; j < n; ++j)
+            if (j != x && d < cap[j]) d = cap[j];
+        cap[x] = d;
+        free(done);
+    }
 }
 
 /* ================= adjoints (no reference routine; oracle of this build's
@@ -464,6 +529,7 @@ void FN(orc_maxmin_bwd)(const REAL* A, int64_t lda, const REAL* B, int64_t ldb, 
     for (int64_t i = 0; i < rows; ++i)
         for (int64_t j = 0; j < cols; ++j) {
             const REAL g = dC[i * lddc + j];
+            if (!witness && g == 0) continue;  /* nothing to route and no witness asked for */
             int64_t ks = -1;
             /* no witness (and no gradient) where the product is -inf */
             for (int64_t q = 0; q < k && Cm[i * ldc + j] > (REAL)(-DBL_MAX); ++q) {

@@ -49,6 +49,8 @@ def _bind(L, sfx: str, prefix: str):
         "max_transpose": (None, [_vp, _i64, _i64, _vp, _i64]),
         "dpi": (C.c_int64, [_vp, _i64, _i64, C.c_double, _vp, _i64, _vp]),
         "closure": (C.c_int, [_vp, _i64, _i64, _vp, _i64, C.c_int]),
+        "dpi_rows": (C.c_int64, [_vp, _i64, _i64, C.c_double, _vp, _i64, _vp, _i64, _vp]),
+        "widest_rows": (None, [_vp, _i64, _i64, _vp, _i64, _vp, _i64]),
         "maxmin_masked": (None, [_vp, _i64, _vp, _i64, _i64, _i64, _i64, _vp, _vp, _i64]),
     }
     for name, (res, args) in sig.items():
@@ -338,6 +340,28 @@ class _Port(_TfCompositions, _EvalCompositions):
                                                             mask.ctypes.data)
         return out, mask, int(removed)
 
+    def dpi_rows(self, A, rows, tol=0.1):
+        """Rows `rows` of dpi(A, tol): (out rows, mask rows, removed count of those rows)."""
+        A = np.ascontiguousarray(A)
+        n = A.shape[0]
+        rows = np.ascontiguousarray(rows, dtype=np.int64)
+        out = np.empty((rows.size, n), dtype=A.dtype)
+        mask = np.empty((rows.size, n), dtype=np.uint8)
+        t = float(np.float32(tol)) if A.dtype == np.float32 else float(tol)
+        removed = getattr(self.L, f"orc_dpi_rows_{self._dt(A)}")(A.ctypes.data, n, n, t, rows.ctypes.data, rows.size,
+                                                                 out.ctypes.data, n, mask.ctypes.data)
+        return out, mask, int(removed)
+
+    def widest_rows(self, A, rows):
+        """Rows `rows` of the maximum-capacity closure of a symmetric A, by widest-path search."""
+        A = np.ascontiguousarray(A)
+        n = A.shape[0]
+        rows = np.ascontiguousarray(rows, dtype=np.int64)
+        out = np.empty((rows.size, n), dtype=A.dtype)
+        getattr(self.L, f"orc_widest_rows_{self._dt(A)}")(A.ctypes.data, n, n, rows.ctypes.data, rows.size,
+                                                          out.ctypes.data, n)
+        return out
+
     def maxmin_masked(self, A, B, mask):
         A = np.ascontiguousarray(A)
         B = A if B is None else np.ascontiguousarray(B)
@@ -369,15 +393,17 @@ class _Port(_TfCompositions, _EvalCompositions):
                                                      dX.ctypes.data, m)
         return dX
 
-    def maxmin_bwd(self, A, B, Cm, dC, dA, dB):
-        """Accumulates into dA, dB (may be the same array); returns the witnesses."""
+    def maxmin_bwd(self, A, B, Cm, dC, dA, dB, want_witness=True):
+        """Accumulates into dA, dB (may be the same array); returns the witnesses
+        (None with want_witness=False, which scans only the entries with a gradient)."""
         A, B, Cm, dC = (np.ascontiguousarray(x) for x in (A, B, Cm, dC))
         rows, k = A.shape
         cols = B.shape[0]
-        K = np.empty((rows, cols), dtype=np.int32)
+        K = np.empty((rows, cols), dtype=np.int32) if want_witness else None
         getattr(self.L, f"orc_maxmin_bwd_{self._dt(A)}")(A.ctypes.data, k, B.ctypes.data, k, rows, cols, k,
                                                          Cm.ctypes.data, cols, dC.ctypes.data, cols, dA.ctypes.data,
-                                                         dA.shape[1], dB.ctypes.data, dB.shape[1], K.ctypes.data)
+                                                         dA.shape[1], dB.ctypes.data, dB.shape[1],
+                                                         None if K is None else K.ctypes.data)
         return K
 
     def ratio_bwd(self, A, M, dR, dA, dM):

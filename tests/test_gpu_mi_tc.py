@@ -95,3 +95,34 @@ def test_one_sm_form_matches_pair_form(gpu, built_lib, tmp_path, prec):
     one = np.load(tmp_path / "one.npy")
     pair = gpu.bspline_mi(X, 10, 3, prec)
     assert np.abs(one - pair).max() <= 2e-6
+
+
+@pytest.mark.parametrize("prec", ["bf16f8", "bf16x3"])
+def test_bounded_wait_runs_out_and_the_handle_recovers(gpu, built_lib, prec):
+    """A device wait that runs out: the test hook gives the next tensor-core launch
+    a 5 ms barrier-wait limit and starves its TMA producers, so the MMA issuer's
+    first wait expires with no load or MMA in flight.  The call must return
+    ERR_DEVICE_TIMEOUT with a message, and the next normal call on the same handle
+    (which needs every SM's tensor memory again, so the starved launch must have
+    freed it) must give the same bits as before."""
+    import torch
+    n, m = 300, 640
+    X = torch.from_numpy(built_lib.synth_grn(n, m, seed=77)).cuda()
+    ref = torch.empty((n, n), dtype=torch.float32, device="cuda")
+    gpu.bspline_mi_dev(X, ref, 10, 3, prec)
+    gpu.synchronize()
+    out = torch.zeros((n, n), dtype=torch.float32, device="cuda")
+    gpu.test_tc_timeout(5_000_000, starve=True)
+    with pytest.raises(built_lib.MCPGError) as e:
+        gpu.bspline_mi_dev(X, out, 10, 3, prec)
+    assert e.value.status == built_lib.ERR_DEVICE_TIMEOUT
+    assert b"bounded barrier wait" in gpu._L.mcpg_last_error(gpu._h)
+    again = torch.empty((n, n), dtype=torch.float32, device="cuda")
+    gpu.bspline_mi_dev(X, again, 10, 3, prec)
+    gpu.synchronize()
+    assert torch.equal(again.view(torch.int32), ref.view(torch.int32))
+
+
+def test_timeout_hook_argument_check(gpu, built_lib):
+    assert gpu._L.mcpg_test_tc_timeout(gpu._h, 10, 1) == built_lib.ERR_ARG
+    assert gpu._L.mcpg_test_tc_timeout(None, 5_000_000, 1) == built_lib.ERR_ARG

@@ -353,3 +353,30 @@ def test_library_shuffle_equals_std_shuffle(built_lib, port, E):
 def test_library_shuffle_rejects_bad_counts(built_lib):
     with pytest.raises(built_lib.MCPGError):
         built_lib.shuffle_positions(-1, 1)
+
+
+@pytest.mark.parametrize("n", [1, 2, 7, 64, 150])
+def test_widest_path_rows_equal_the_squaring_closure(port, n):
+    """The widest-path rows (the sampled-row check of large closures) equal the
+    repeated-squaring closure exactly, with ties, negative entries and a nonzero
+    diagonal."""
+    rng = np.random.default_rng(n + 17)
+    A = (rng.integers(-3, 9, size=(n, n)) * 0.125).astype(np.float32)
+    A = np.maximum(A, A.T)
+    np.fill_diagonal(A, rng.integers(-2, 3, size=n) * 0.125)
+    C, _ = port.closure(A)
+    assert np.array_equal(port.widest_rows(A, np.arange(n)), C)
+
+
+def test_dpi_rows_equal_the_full_filter(port):
+    rng = np.random.default_rng(5)
+    A = (rng.integers(0, 6, size=(90, 90)) * 0.2).astype(np.float32)
+    A = np.maximum(A, A.T)
+    np.fill_diagonal(A, 0)
+    for tol in (0.0, 0.1):
+        out, mask, _ = port.dpi(A, tol)
+        rows = np.array([0, 5, 89, 44])
+        ro, rm, rr = port.dpi_rows(A, rows, tol)
+        assert np.array_equal(ro.view(np.uint32), out[rows].view(np.uint32))
+        assert np.array_equal(rm, mask[rows])
+        assert rr == int((out[rows] != A[rows]).sum())
