@@ -383,6 +383,29 @@ def gpu_arm(args, ws, rank, local):
         b.record(stream)
         b.synchronize()
         line["maxmin"]["mcp2_ms"] = a.elapsed_time(b)
+        # the DPI filter (tolerance 0.1) and the converged max-capacity closure on the same MI
+        Dm = torch.empty((n, n), dtype=torch.uint8, device=dev)
+        h.dpi_dev(A, C, 0.1, Dm)  # untimed: scratch
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        removed = h.dpi_dev(A, C, 0.1, Dm)
+        b.record(stream)
+        b.synchronize()
+        dpi_ms = a.elapsed_time(b)
+        line["maxmin"]["dpi"] = {"ms": dpi_ms, "tol": 0.1, "removed": removed,
+                                 "one_phase_equivalent_gops": 2.0 * 0.5 * n ** 3 / (dpi_ms / 1e3) / 1e9,
+                                 "note": "two phases: the tiled max-min over the first 512 intermediates, then an "
+                                         "early-exit scan of the outputs it left undecided"}
+        del Dm
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        iters = h.closure_dev(A, C, 64)
+        b.record(stream)
+        b.synchronize()
+        cl_ms = a.elapsed_time(b)
+        line["maxmin"]["closure"] = {"ms": cl_ms, "squarings": iters,
+                                     "frac_alu_peak_at_max_clock": 2.0 * 0.5 * n ** 3 * max(iters, 1) / (cl_ms / 1e3)
+                                     / (alu_peak * 1e9)}
         del M1, R, C
 
     # ---- end to end through the host C ABI ----

@@ -18,6 +18,18 @@ enum MaxminMode : int {
                      // MM_DPI; an output with no admissible k is NaN
     MM_WITNESS = 5,  // C = A (x) B and K[i][j] = first k attaining it (-1 where C is -inf)
     MM_GEMM = 6,     // C = A B^T in (+, x): the plus-times twin of the kernel (FP32 FFMA)
+    MM_DPI1 = 7,     // first phase of the two-phase DPI: k runs over [0, k_len) only; outputs it
+                     // decides are written (as MM_DPI), the others appended to `pending`
+};
+
+// An output pair of the two-phase DPI that the first k_len intermediates did not
+// decide: (x, z) and, when `flags` bit 1 is set, its mirror (z, x), with m the
+// max-min over the first phase's admissible intermediates.  flags bit 0: (x, z)
+// undecided; bit 1: (z, x) undecided.
+struct DpiPending {
+    int32_t x, z;
+    float m;
+    uint32_t flags;
 };
 
 struct MaxminParams {
@@ -36,6 +48,9 @@ struct MaxminParams {
     const int* excl_row;
     const int* excl_col;
     int32_t* K; int64_t ldk;      // MM_WITNESS output
+    // MM_DPI1: pending outputs (capacity pending_cap; *pending_n counts every append,
+    // so a count above the capacity means the list overflowed)
+    DpiPending* pending; int64_t pending_cap; unsigned long long* pending_n;
 };
 
 // symmetric != 0: A == B (same rows), rows == cols; only tiles on or above the
@@ -43,6 +58,13 @@ struct MaxminParams {
 cudaError_t launch_maxmin(const MaxminParams& p, int mode, int symmetric, cudaStream_t stream, int64_t* launches);
 cudaError_t launch_ratio(const float* A, int64_t lda, const float* M, int64_t ldm, int64_t rows, int64_t cols,
                          float* R, int64_t ldr, cudaStream_t stream, int64_t* launches);
+// Second phase of the two-phase DPI: for every pending pair, continue the max-min over
+// the intermediates y in [k0, n) (y not in {x, z}) until every undecided orientation is
+// deleted or the row ends, then write out / mask and add to *removed as MM_DPI does.
+// A: n x n (16-byte aligned rows, lda % 4 == 0), also the DPI input E.
+cudaError_t launch_dpi_pending(const float* A, int64_t lda, int64_t n, int64_t k0, const DpiPending* list,
+                               int64_t count, double tol_mult, float* out, int64_t ldo, uint8_t* mask,
+                               int64_t ldmask, unsigned long long* removed, cudaStream_t stream, int64_t* launches);
 cudaError_t launch_set_diagonal(float* A, int64_t rows, int64_t cols, int64_t lda, float value,
                                 cudaStream_t stream, int64_t* launches);
 cudaError_t launch_max_transpose(const float* M, int64_t n, int64_t ldm, float* out, int64_t ldo,

@@ -126,7 +126,8 @@ __global__ void __launch_bounds__(THREADS, MCPG_MM_MINB) maxmin_kernel(const Max
 
     // DPI: NaN is the neutral element of the NaN-ignoring max, so an output with
     // no admissible y stays NaN and compares false (the reference keeps it).
-    constexpr bool EXCL = (MODE == MM_DPI || MODE == MM_EXCL);
+    constexpr bool DPI1 = (MODE == MM_DPI1);
+    constexpr bool EXCL = (MODE == MM_DPI || MODE == MM_EXCL || DPI1);
     constexpr bool WIT = (MODE == MM_WITNESS);
     constexpr bool GEMM = (MODE == MM_GEMM);
     const float init = EXCL ? __int_as_float(0x7fc00000) : (GEMM ? 0.0f : -INFINITY);
@@ -283,6 +284,7 @@ __global__ void __launch_bounds__(THREADS, MCPG_MM_MINB) maxmin_kernel(const Max
     // ---------------- epilogue ----------------
     int any_changed = 0;
     unsigned long long removed = 0;
+    uint64_t pend0 = 0, pend1 = 0;  // MM_DPI1: outputs (and mirrors) the first phase left undecided
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
         const int64_t i = i0 + ty + 16 * q;
@@ -321,24 +323,32 @@ __global__ void __launch_bounds__(THREADS, MCPG_MM_MINB) maxmin_kernel(const Max
                     p.C[j * p.ldc + i] = v2;
                     any_changed |= (v2 != e2);
                 }
-            } else {  // MM_DPI
+            } else {  // MM_DPI; MM_DPI1 writes only what the first phase decides (deleted)
                 {
                     const float e = p.E[i * p.lde + j];
                     const float ixz = (float)((double)e * p.tol_mult);
                     const bool del = (i == j) || (m >= ixz);
-                    const float o = del ? 0.0f : e;
-                    p.C[i * p.ldc + j] = o;
-                    removed += (o != e);
-                    if (p.mask) p.mask[i * p.ldmask + j] = del ? 1 : 0;
+                    if (!DPI1 || del) {
+                        const float o = del ? 0.0f : e;
+                        p.C[i * p.ldc + j] = o;
+                        removed += (o != e);
+                        if (p.mask) p.mask[i * p.ldmask + j] = del ? 1 : 0;
+                    } else {
+                        pend0 |= 1ull << (q * TN + r);
+                    }
                 }
                 if (mirror) {
                     const float e = p.E[j * p.lde + i];
                     const float ixz = (float)((double)e * p.tol_mult);
                     const bool del = (m >= ixz);
-                    const float o = del ? 0.0f : e;
-                    p.C[j * p.ldc + i] = o;
-                    removed += (o != e);
-                    if (p.mask) p.mask[j * p.ldmask + i] = del ? 1 : 0;
+                    if (!DPI1 || del) {
+                        const float o = del ? 0.0f : e;
+                        p.C[j * p.ldc + i] = o;
+                        removed += (o != e);
+                        if (p.mask) p.mask[j * p.ldmask + i] = del ? 1 : 0;
+                    } else {
+                        pend1 |= 1ull << (q * TN + r);
+                    }
                 }
             }
         }
@@ -346,7 +356,40 @@ __global__ void __launch_bounds__(THREADS, MCPG_MM_MINB) maxmin_kernel(const Max
     if (MODE == MM_CLOSURE) {
         if (__syncthreads_or(any_changed) && tid == 0) atomicOr(p.changed, 1);
     }
-    if (MODE == MM_DPI && p.removed) {
+    if (DPI1) {
+        // append the undecided outputs: one atomic per warp, then each lane writes its own
+        const uint64_t any = pend0 | pend1;
+        const unsigned cnt = (unsigned)__popcll(any);
+        unsigned incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        unsigned long long base = 0;
+        if (lane == 31 && incl) base = atomicAdd(p.pending_n, (unsigned long long)incl);
+        base = __shfl_sync(0xffffffffu, base, 31);
+        if (any) {
+            unsigned long long idx = base + incl - cnt;
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+#pragma unroll
+                for (int r = 0; r < TN; ++r) {
+                    const uint64_t bit = 1ull << (q * TN + r);
+                    if (!(any & bit)) continue;
+                    if (idx < (unsigned long long)p.pending_cap) {
+                        DpiPending d;
+                        d.x = (int32_t)(i0 + ty + 16 * q);
+                        d.z = (int32_t)(j0 + tx + TXS * r);
+                        d.m = acc[q][r];
+                        d.flags = ((pend0 & bit) ? 1u : 0u) | ((pend1 & bit) ? 2u : 0u);
+                        p.pending[idx] = d;
+                    }
+                    ++idx;
+                }
+        }
+    }
+    if ((MODE == MM_DPI || DPI1) && p.removed) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) removed += __shfl_xor_sync(0xffffffffu, removed, o);
         if (lane == 0 && removed) atomicAdd(p.removed, removed);
@@ -476,6 +519,73 @@ __global__ void ratio_bwd_kernel(const float* A, int64_t lda, const float* M, in
     });
 }
 
+// Second phase of the two-phase DPI: one warp per pending pair continues
+// dpi_kernel's scan (dpi.hpp:56-68) over the intermediates y in [k0, n), 128 per
+// step (float4 per lane, rows x and z coalesced), and stops as soon as the running
+// max-min reaches every undecided orientation's threshold -- the reference's own
+// early exit, at warp granularity.  Excluded y (x and z) contribute NaN, which the
+// NaN-ignoring max drops, exactly as in the tiled kernel.
+__global__ void __launch_bounds__(256) dpi_pending_kernel(const float* __restrict__ A, int64_t lda, int64_t n,
+                                                          int64_t k0, const DpiPending* __restrict__ list,
+                                                          int64_t count, double tm, float* __restrict__ out,
+                                                          int64_t ldo, uint8_t* __restrict__ mask, int64_t ldmask,
+                                                          unsigned long long* removed) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const float qnan = __int_as_float(0x7fc00000);
+    unsigned long long cnt = 0;
+    for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < count; w += nw) {
+        const DpiPending d = list[w];
+        const int64_t x = d.x, z = d.z;
+        const float* rx = A + x * lda;
+        const float* rz = A + z * lda;
+        const float exz = rx[z], ezx = rz[x];
+        const float t0 = (float)((double)exz * tm), t1 = (float)((double)ezx * tm);
+        const bool u0 = (d.flags & 1u) != 0, u1 = (d.flags & 2u) != 0;
+        const float target = u0 ? (u1 ? fmaxf(t0, t1) : t0) : t1;
+        float mm = d.m;
+        for (int64_t y0 = k0; y0 < n; y0 += 128) {
+            const int64_t y = y0 + 4 * lane;
+            if (y + 3 < n) {
+                const float4 a = __ldg(reinterpret_cast<const float4*>(rx + y));
+                const float4 b = __ldg(reinterpret_cast<const float4*>(rz + y));
+                const float v0 = (y == x || y == z) ? qnan : fmin2(a.x, b.x);
+                const float v1 = (y + 1 == x || y + 1 == z) ? qnan : fmin2(a.y, b.y);
+                const float v2 = (y + 2 == x || y + 2 == z) ? qnan : fmin2(a.z, b.z);
+                const float v3 = (y + 3 == x || y + 3 == z) ? qnan : fmin2(a.w, b.w);
+                mm = fmax2(fmax2(mm, v0), fmax2(v1, fmax2(v2, v3)));
+            } else {
+                for (int64_t c = y; c < n && c < y + 4; ++c)
+                    if (c != x && c != z) mm = fmax2(mm, fmin2(rx[c], rz[c]));
+            }
+            if (__any_sync(0xffffffffu, mm >= target)) break;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mm = fmax2(mm, __shfl_xor_sync(0xffffffffu, mm, o));
+        if (lane == 0) {
+            if (u0) {
+                const bool del = mm >= t0;
+                const float o = del ? 0.0f : exz;
+                out[x * ldo + z] = o;
+                cnt += (o != exz);
+                if (mask) mask[x * ldmask + z] = del ? 1 : 0;
+            }
+            if (u1) {
+                const bool del = mm >= t1;
+                const float o = del ? 0.0f : ezx;
+                out[z * ldo + x] = o;
+                cnt += (o != ezx);
+                if (mask) mask[z * ldmask + x] = del ? 1 : 0;
+            }
+        }
+    }
+    if (removed) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+        if (lane == 0 && cnt) atomicAdd(removed, cnt);
+    }
+}
+
 // compute_combo (mcpnet_helper.hpp:507-573): combo_value_ff gives the
 // reference's double-precision result, mostly without the FP64 pipe.
 __global__ void __launch_bounds__(EW_TPB) combo_kernel(const float* __restrict__ mi, int64_t ldm,
@@ -508,6 +618,7 @@ cudaError_t launch_maxmin(const MaxminParams& p, int mode, int symmetric, cudaSt
         case MM_WITNESS:
             return s ? launch_one<MM_WITNESS, true>(p, stream) : launch_one<MM_WITNESS, false>(p, stream);
         case MM_GEMM: return launch_one<MM_GEMM, false>(p, stream);
+        case MM_DPI1: return s ? launch_one<MM_DPI1, true>(p, stream) : launch_one<MM_DPI1, false>(p, stream);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -517,6 +628,22 @@ cudaError_t launch_ratio(const float* A, int64_t lda, const float* M, int64_t ld
     if (rows <= 0 || cols <= 0) return cudaSuccess;
     if (launches) ++*launches;
     ratio_kernel_ew<<<ew_grid2d(rows, cols), 256, 0, stream>>>(A, lda, M, ldm, rows, cols, R, ldr);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dpi_pending(const float* A, int64_t lda, int64_t n, int64_t k0, const DpiPending* list,
+                               int64_t count, double tol_mult, float* out, int64_t ldo, uint8_t* mask,
+                               int64_t ldmask, unsigned long long* removed, cudaStream_t stream, int64_t* launches) {
+    if (count <= 0 || n <= 0) return cudaSuccess;
+    if ((lda % 4) != 0 || ((uintptr_t)A & 15u) || (k0 % 4) != 0) return cudaErrorInvalidValue;
+    if (launches) ++*launches;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t want = ceil_div(count, (int64_t)8);  // 8 warps per block
+    const int64_t grid = want < (int64_t)sms * 8 ? want : (int64_t)sms * 8;
+    dpi_pending_kernel<<<(unsigned)grid, 256, 0, stream>>>(A, lda, n, k0, list, count, tol_mult, out, ldo, mask,
+                                                           ldmask, removed);
     return cudaGetLastError();
 }
 
