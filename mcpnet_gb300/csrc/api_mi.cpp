@@ -13,8 +13,7 @@ struct MiPlan {
     int precision = 0, fmt = 0, split = 0, bins = 0;  // split: mcpg::TcMode
     int64_t n = 0, m = 0;
     const void* w0 = nullptr;  // FP32 sample-major or 16-bit hi weights
-    const void* w1 = nullptr;  // 16-bit lo weights, or the E4M3 H8 plane (split 2)
-    const void* w2 = nullptr;  // E4M3 L8 plane (split 2)
+    const void* w1 = nullptr;  // 16-bit lo weights, or the interleaved E4M3 H8|L8 plane (split 2)
     int64_t ld = 0;            // weight leading dimension
     double* H = nullptr;
     float* MI = nullptr;
@@ -64,23 +63,18 @@ int mi_prepare(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_t ldx
                                                                             : mcpg::TC_SINGLE;
     const int64_t ldw = round_up(m, 64);
     const int64_t rows = round_up(n * bins, 256) + 256;  // whole tiles stay in bounds
-    // S_W1: the 16-bit lo plane, or the two 8-bit planes H8 | L8 (the same bytes)
+    // S_W1: the 16-bit lo plane, or the interleaved 8-bit plane H8|L8 (rows of 2 * ldw bytes: the same bytes)
     void *hi, *lo = nullptr;
     if ((rc = scratch(h, S_W0, (size_t)(rows * ldw) * 2, &hi))) return rc;
     if (pl.split && (rc = scratch(h, S_W1, (size_t)(rows * ldw) * 2, &lo))) return rc;
-    uint8_t* l8 = pl.split == mcpg::TC_F8C ? (uint8_t*)lo + (size_t)(rows * ldw) : nullptr;
+    const bool f8 = pl.split == mcpg::TC_F8C;
     // rows beyond n*bins must be zero (they are read by the last tiles)
     const size_t done = (size_t)(n * bins * ldw), tail = (size_t)((rows - n * bins) * ldw);
     CK(h, cudaMemsetAsync((char*)hi + done * 2, 0, tail * 2, h->stream), "memset weights");
-    if (pl.split == mcpg::TC_SPLIT16)
-        CK(h, cudaMemsetAsync((char*)lo + done * 2, 0, tail * 2, h->stream), "memset weights");
-    if (l8) {
-        CK(h, cudaMemsetAsync((char*)lo + done, 0, tail, h->stream), "memset weights");
-        CK(h, cudaMemsetAsync(l8 + done, 0, tail, h->stream), "memset weights");
-    }
-    if (l8) {
+    if (pl.split) CK(h, cudaMemsetAsync((char*)lo + done * 2, 0, tail * 2, h->stream), "memset weights");
+    if (f8) {
         PROF(h, "bspline_weights_f8");
-        CK(h, mcpg::launch_bspline_weights_f8(X, n, m, ldx, bins, order, (uint16_t*)hi, (uint8_t*)lo, l8, ldw, pl.H,
+        CK(h, mcpg::launch_bspline_weights_f8(X, n, m, ldx, bins, order, (uint16_t*)hi, (uint8_t*)lo, ldw, pl.H,
                                                h->stream, &h->launches),
            "bspline weights kernel");
     } else {
@@ -92,7 +86,7 @@ int mi_prepare(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_t ldx
     void* flag;
     if ((rc = scratch(h, S_SMALL, 64, &flag))) return rc;
     CK(h, cudaMemsetAsync(flag, 0, sizeof(int), h->stream), "memset flag");
-    pl.w0 = hi; pl.w1 = lo; pl.w2 = l8; pl.ld = ldw; pl.flag = (int*)flag;
+    pl.w0 = hi; pl.w1 = lo; pl.ld = ldw; pl.flag = (int*)flag;
     return MCPG_OK;
 }
 
@@ -112,7 +106,7 @@ int mi_launch(mcpg_handle* h, const MiPlan& pl, int64_t g0, int64_t g1) {
         const mcpg::TcWaitHook* hook = h->tc_hook_armed ? &h->tc_hook : nullptr;
         h->tc_hook_armed = false;  // one launch only
         e = mcpg::launch_mi_tc((const uint16_t*)pl.w0, f8 ? nullptr : (const uint16_t*)pl.w1,
-                               f8 ? (const uint8_t*)pl.w1 : nullptr, (const uint8_t*)pl.w2, pl.ld, pl.H, pl.n, pl.m,
+                               f8 ? (const uint8_t*)pl.w1 : nullptr, pl.ld, pl.H, pl.n, pl.m,
                                pl.bins, pl.fmt, pl.split, pl.MI, pl.ldmi, pl.flag, h->stream, &h->launches, g0, g1,
                                hook);
     }

@@ -18,8 +18,11 @@
 //   OUT_T32   : Wt[s*ldwt + g*bins + a] (sample-major FP32, CUDA-core MI)
 //   OUT_BF16/OUT_FP16 : Whi/Wlo[(g*bins + a)*ldw + s] (gene-bin-major, K = samples
 //               contiguous, zero-padded to ldw; tcgen05 MI)
-//   OUT_BF16F8 : the same layout, three planes: Whi = bf16(w) * 2^8 (BF16), and the
-//               E4M3 correction operands H8 = e4m3(bf16(w) * 2^4), L8 = e4m3((w - bf16(w)) * 2^12).
+//   OUT_BF16F8 : Whi = bf16(w) * 2^8 (BF16, the layout above), and the E4M3 correction
+//               operands H8 = e4m3(bf16(w) * 2^4), L8 = e4m3((w - bf16(w)) * 2^12) in one
+//               interleaved plane HL8 of rows of 2 * ldw bytes: for every 64 samples of a
+//               row, their 64 H8 bytes then their 64 L8 bytes, so that one 128-byte TMA box
+//               row carries both correction operands of a 64-sample slice.
 //               The scales multiply to 2^16 in every product (hi*hi, H8*L8, L8*H8), so
 //               the three contractions accumulate 2^16 * P into one FP32 accumulator.
 #include <cuda_bf16.h>
@@ -226,14 +229,15 @@ __global__ void __launch_bounds__(WTHREADS) bspline_weights_kernel(const float* 
             float* W = static_cast<float*>(out0) + s * ldo + g * bins;
             for (int a = 0; a < bins; ++a) W[a] = w[a];
         } else if (OUT == OUT_BF16F8) {
+            const int64_t s8 = (s >> 6) * 128 + (s & 63);  // H8 byte of sample s in an HL8 row; L8 at +64
             for (int a = 0; a < bins; ++a) {
                 const int64_t o = (g * bins + a) * ldo + s;
                 const __nv_bfloat16 hi = __float2bfloat16_rn(w[a]);
                 const float hf = __bfloat162float(hi);
                 static_cast<__nv_bfloat16*>(out0)[o] = __float2bfloat16_rn(hf * 256.0f);
-                static_cast<__nv_fp8_storage_t*>(out1)[o] = __nv_cvt_float_to_fp8(hf * 16.0f, __NV_SATFINITE, __NV_E4M3);
-                static_cast<__nv_fp8_storage_t*>(out2)[o] =
-                    __nv_cvt_float_to_fp8(__fsub_rn(w[a], hf) * 4096.0f, __NV_SATFINITE, __NV_E4M3);
+                __nv_fp8_storage_t* hl = static_cast<__nv_fp8_storage_t*>(out1) + (g * bins + a) * 2 * ldo + s8;
+                hl[0] = __nv_cvt_float_to_fp8(hf * 16.0f, __NV_SATFINITE, __NV_E4M3);
+                hl[64] = __nv_cvt_float_to_fp8(__fsub_rn(w[a], hf) * 4096.0f, __NV_SATFINITE, __NV_E4M3);
             }
         } else {
             for (int a = 0; a < bins; ++a) {
@@ -256,8 +260,9 @@ __global__ void __launch_bounds__(WTHREADS) bspline_weights_kernel(const float* 
             for (int a = 0; a < bins; ++a) {
                 const int64_t o = (g * bins + a) * ldo + s;
                 static_cast<uint16_t*>(out0)[o] = 0;
-                static_cast<uint8_t*>(out1)[o] = 0;
-                static_cast<uint8_t*>(out2)[o] = 0;
+                uint8_t* hl = static_cast<uint8_t*>(out1) + (g * bins + a) * 2 * ldo + (s >> 6) * 128 + (s & 63);
+                hl[0] = 0;
+                hl[64] = 0;
             }
     }
     if (OUT == OUT_BF16 || OUT == OUT_FP16) {
@@ -526,18 +531,18 @@ cudaError_t launch_bspline_weights_16(const float* X, int64_t n, int64_t m, int6
 }
 
 cudaError_t launch_bspline_weights_f8(const float* X, int64_t n, int64_t m, int64_t ldx, int bins, int order,
-                                      uint16_t* Whi, uint8_t* H8, uint8_t* L8, int64_t ldw, double* H,
-                                      cudaStream_t stream, int64_t* launches) {
+                                      uint16_t* Whi, uint8_t* HL8, int64_t ldw, double* H, cudaStream_t stream,
+                                      int64_t* launches) {
     if (n <= 0) return cudaSuccess;
     Knots kv;
     host_knots(bins, order, kv);
     if (launches) ++*launches;
     if (bins == 10 && order == 3)
         bspline_weights_kernel<OUT_BF16F8, 10, 3><<<(unsigned)n, WTHREADS, 0, stream>>>(X, n, m, ldx, bins, order, kv,
-                                                                                    Whi, H8, L8, ldw, H);
+                                                                                    Whi, HL8, nullptr, ldw, H);
     else
         bspline_weights_kernel<OUT_BF16F8, 0, 0><<<(unsigned)n, WTHREADS, 0, stream>>>(X, n, m, ldx, bins, order, kv,
-                                                                                  Whi, H8, L8, ldw, H);
+                                                                                  Whi, HL8, nullptr, ldw, H);
     return cudaGetLastError();
 }
 

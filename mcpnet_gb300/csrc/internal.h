@@ -112,11 +112,12 @@ cudaError_t launch_bspline_weights_fp32(const float* X, int64_t n, int64_t m, in
 cudaError_t launch_bspline_weights_16(const float* X, int64_t n, int64_t m, int64_t ldx, int bins, int order,
                                       int fmt, uint16_t* Whi, uint16_t* Wlo, int64_t ldw, double* H,
                                       cudaStream_t stream, int64_t* launches);
-// The same layout in three planes for the FP8-corrected form: Whi = bf16(w) * 2^8,
-// H8 = e4m3(bf16(w) * 2^4), L8 = e4m3((w - bf16(w)) * 2^12) (every product scaled 2^16).
+// The FP8-corrected form: Whi = bf16(w) * 2^8 in the layout above, and the E4M3 planes
+// H8 = e4m3(bf16(w) * 2^4), L8 = e4m3((w - bf16(w)) * 2^12) (every product scaled 2^16)
+// interleaved in HL8: rows of 2 * ldw bytes, each 64 samples as 64 H8 bytes then 64 L8 bytes.
 cudaError_t launch_bspline_weights_f8(const float* X, int64_t n, int64_t m, int64_t ldx, int bins, int order,
-                                      uint16_t* Whi, uint8_t* H8, uint8_t* L8, int64_t ldw, double* H,
-                                      cudaStream_t stream, int64_t* launches);
+                                      uint16_t* Whi, uint8_t* HL8, int64_t ldw, double* H, cudaStream_t stream,
+                                      int64_t* launches);
 // FP32 MI from sample-major weights (CUDA cores), symmetric output.
 // Covers gene pairs (i, j >= i) with i in [gene0, gene1) (gene0 a multiple of 16;
 // gene1 = -1 for n): rows i < gene1 of MI are complete once every earlier range ran.
@@ -137,8 +138,8 @@ cudaError_t launch_mi_bwd_x(const float* X, int64_t n, int64_t m, int64_t ldx, i
                             int64_t g1, const float* gsum, const float* dWq, int64_t lddw, float* dX, int64_t lddx,
                             cudaStream_t stream, int64_t* launches);
 // Tensor-core MI (tcgen05).  mode TC_SINGLE: 16-bit weights Whi; TC_SPLIT16: adds
-// the 16-bit lo terms from Wlo; TC_F8C: BF16 Whi (x 2^8) plus the E4M3 correction
-// planes H8 / L8 (launch_bspline_weights_f8).
+// the 16-bit lo terms from Wlo; TC_F8C: BF16 Whi (x 2^8) plus the interleaved E4M3
+// correction plane HL8 (launch_bspline_weights_f8).
 // Returns cudaErrorNotSupported when the shape/bins is outside the kernel's tiling.
 // Gene range as launch_mi_fp32 (gene0 a multiple of 12).
 enum TcMode : int { TC_SINGLE = 0, TC_SPLIT16 = 1, TC_F8C = 2 };
@@ -152,8 +153,7 @@ struct TcWaitHook {
     unsigned long long wait_ns = TC_WAIT_NS_DEFAULT;
     int starve = 0;
 };
-cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, const uint8_t* H8, const uint8_t* L8,
-                         int64_t ldw, const double* H, int64_t n, int64_t m, int bins, int fmt, int mode, float* MI,
+cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, const uint8_t* HL8, int64_t ldw, const double* H, int64_t n, int64_t m, int bins, int fmt, int mode, float* MI,
                          int64_t ldmi, int* timeout_flag, cudaStream_t stream, int64_t* launches, int64_t gene0 = 0,
                          int64_t gene1 = -1, const TcWaitHook* hook = nullptr);
 

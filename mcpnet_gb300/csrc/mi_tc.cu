@@ -16,8 +16,13 @@
 // L8 = e4m3(4096 lo):  2^16 P = (256 Whi)(256 Whi)' + H8 L8' + L8 H8'.  A tile
 // first runs the correction over all samples (while the accumulator is small),
 // then the hi*hi term: per 64 samples 4 BF16 MMAs + 4 FP8 MMAs of equal duration,
-// against 12 for the BF16 split.  Its operands (8-bit: 64-byte rows, 64-byte
-// swizzle) fill the same 46 KB stages as the hi*hi slices, so the ring is 4 deep.
+// against 12 for the BF16 split.  H8 and L8 are stored interleaved (per 64 samples
+// of a row: 64 H8 bytes, then 64 L8 bytes), so a correction slice is one 128-byte
+// -wide TMA box per operand, 128-byte swizzled like the hi*hi slices and of the
+// same size: the MMA descriptors pick H8 at byte offsets 0 / 32 and L8 at 64 / 96
+// of the swizzled rows (two K = 32 steps each).  Every TMA instruction costs the
+// issuing thread a few hundred cycles, and four 64-byte boxes per slice had made
+// the correction pass the producer's bottleneck.
 //
 // CTA tile: A = 12 genes (120 of the 128 MMA rows), B = 24 genes (N = 240);
 // D = 128 x 240 FP32 in tensor memory (256 columns allocated).
@@ -65,9 +70,7 @@ constexpr int TMEM_COLS = 256;
 inline int64_t group_bytes(int64_t ldw) { return ldw <= 2048 ? (32ll << 20) : (16ll << 20); }
 constexpr uint32_t A_BYTES = MROWS * BK * 2;   // 16 KB
 constexpr uint32_t B_BYTES = NCOLS * BK * 2;   // 30 KB
-constexpr uint32_t A8_BYTES = MROWS * BK;      // 8 KB (8-bit correction operand)
-constexpr uint32_t B8_BYTES = NCOLS * BK;      // 15 KB
-static_assert(2 * (A8_BYTES + B8_BYTES) == A_BYTES + B_BYTES, "correction slices fill a hi*hi stage");
+constexpr uint32_t HL8_OFF = 64;               // byte offset of L8 within an interleaved 128-byte row
 constexpr int PSTRIDE = GBN + 1;       // epilogue partials row stride (floats)
 
 // ---------------------------------------------------------------- PTX wrappers
@@ -166,18 +169,6 @@ __device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
     d |= (uint64_t)(1024 >> 4) << 32;                  // SBO
     d |= (uint64_t)1 << 46;                            // version
     d |= (uint64_t)2 << 61;                            // SWIZZLE_128B
-    return d;
-}
-
-// Shared-memory matrix descriptor for the 8-bit operands: K-major, 64-byte swizzle,
-// rows of 64 bytes, 8-row groups 512 bytes apart (SBO).
-__device__ __forceinline__ uint64_t sdesc_sw64(uint32_t saddr) {
-    uint64_t d = 0;
-    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
-    d |= (uint64_t)1 << 16;
-    d |= (uint64_t)(512 >> 4) << 32;
-    d |= (uint64_t)1 << 46;
-    d |= (uint64_t)4 << 61;                            // SWIZZLE_64B
     return d;
 }
 
@@ -310,7 +301,7 @@ __device__ __forceinline__ void epilogue_tile(uint32_t trow, float* part, int ro
 //   warps 2-5          epilogue, 128 threads = 128 accumulator rows
 // Two TMEM accumulators (2 x 256 columns) let the epilogue of tile t overlap the
 // main loop of tile t+1.
-// map_lo / mapb_lo carry Wlo (TC_SPLIT16) or H8 (TC_F8C); map_l8 / mapb_l8 carry L8.
+// map_lo / mapb_lo carry Wlo (TC_SPLIT16) or the interleaved H8|L8 plane (TC_F8C); map_l8 / mapb_l8 are unused.
 template <int MODE, int STAGES, int SUB>
 __global__ void __launch_bounds__(192, 1)
     mi_tc_kernel(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CUtensorMap map_lo,
@@ -380,11 +371,9 @@ __global__ void __launch_bounds__(192, 1)
                         if (j >= ns) break;
                         const uint32_t sl = st + j * SLICE;
                         const int x = (kt0 + j) * BK;
-                        if (corr) {
-                            tma_load_2d(sl, &map_lo, x, rowA, fb);
-                            tma_load_2d(sl + A8_BYTES, &map_l8, x, rowA, fb);
-                            tma_load_2d(sl + A_BYTES, &mapb_lo, x, rowB, fb);
-                            tma_load_2d(sl + A_BYTES + B8_BYTES, &mapb_l8, x, rowB, fb);
+                        if (corr) {  // H8|L8 of 64 samples: one 128-byte box row per operand row
+                            tma_load_2d(sl, &map_lo, 2 * x, rowA, fb);
+                            tma_load_2d(sl + A_BYTES, &mapb_lo, 2 * x, rowB, fb);
                             continue;
                         }
                         tma_load_2d(sl, &map_hi, x, rowA, fb);
@@ -434,9 +423,9 @@ __global__ void __launch_bounds__(192, 1)
                         if (corr) {
 #pragma unroll
                             for (int k = 0; k < BK / 32; ++k) {
-                                const uint64_t ah = sdesc_sw64(sl + 32 * k), al = sdesc_sw64(sl + A8_BYTES + 32 * k);
-                                const uint64_t bh = sdesc_sw64(sl + A_BYTES + 32 * k);
-                                const uint64_t bl = sdesc_sw64(sl + A_BYTES + B8_BYTES + 32 * k);
+                                const uint64_t ah = sdesc_sw128(sl + 32 * k), al = sdesc_sw128(sl + HL8_OFF + 32 * k);
+                                const uint64_t bh = sdesc_sw128(sl + A_BYTES + 32 * k);
+                                const uint64_t bl = sdesc_sw128(sl + A_BYTES + HL8_OFF + 32 * k);
                                 mma_f8(dacc, ah, bl, args.idesc8, (q > 0 || j > 0 || k > 0) ? 1u : 0u);
                                 mma_f8(dacc, al, bh, args.idesc8, 1u);
                             }
@@ -507,8 +496,6 @@ __global__ void __launch_bounds__(192, 1)
 // accumulator-full barriers in both CTAs (multicast commits); accumulator-empty in
 // the leader (8 arrivals: both CTAs' epilogue warps).
 constexpr uint32_t BH_BYTES = (NCOLS / 2) * BK * 2;   // 15 KB: half a B tile, 16-bit
-constexpr uint32_t BH8_BYTES = (NCOLS / 2) * BK;      // 7.5 KB: half a B tile, 8-bit
-static_assert(2 * (A8_BYTES + BH8_BYTES) == A_BYTES + BH_BYTES, "correction slices fill a hi*hi stage");
 
 __device__ __forceinline__ uint32_t cluster_rank() {
     uint32_t r;
@@ -659,11 +646,9 @@ __global__ void __launch_bounds__(192, 1)
                         if (j >= ns) break;
                         const uint32_t sl = st + j * SLICE;
                         const int x = (kt0 + j) * BK;
-                        if (corr) {
-                            tma_load_2d_pair(sl, &map_lo, x, rowA, fb);
-                            tma_load_2d_pair(sl + A8_BYTES, &map_l8, x, rowA, fb);
-                            tma_load_2d_pair(sl + A_BYTES, &mapb_lo, x, rowB, fb);
-                            tma_load_2d_pair(sl + A_BYTES + BH8_BYTES, &mapb_l8, x, rowB, fb);
+                        if (corr) {  // H8|L8 of 64 samples: one 128-byte box row per operand row
+                            tma_load_2d_pair(sl, &map_lo, 2 * x, rowA, fb);
+                            tma_load_2d_pair(sl + A_BYTES, &mapb_lo, 2 * x, rowB, fb);
                             continue;
                         }
                         tma_load_2d_pair(sl, &map_hi, x, rowA, fb);
@@ -714,9 +699,9 @@ __global__ void __launch_bounds__(192, 1)
                         if (corr) {
 #pragma unroll
                             for (int k = 0; k < BK / 32; ++k) {
-                                const uint64_t ah = sdesc_sw64(sl + 32 * k), al = sdesc_sw64(sl + A8_BYTES + 32 * k);
-                                const uint64_t bh = sdesc_sw64(sl + A_BYTES + 32 * k);
-                                const uint64_t bl = sdesc_sw64(sl + A_BYTES + BH8_BYTES + 32 * k);
+                                const uint64_t ah = sdesc_sw128(sl + 32 * k), al = sdesc_sw128(sl + HL8_OFF + 32 * k);
+                                const uint64_t bh = sdesc_sw128(sl + A_BYTES + 32 * k);
+                                const uint64_t bl = sdesc_sw128(sl + A_BYTES + HL8_OFF + 32 * k);
                                 mma2_f8(dacc, ah, bl, args.idesc8, (q > 0 || j > 0 || k > 0) ? 1u : 0u);
                                 mma2_f8(dacc, al, bh, args.idesc8, 1u);
                             }
@@ -805,16 +790,17 @@ bool make_map(CUtensorMap* map, const uint16_t* base, int fmt, int64_t rows, int
     return r == CUDA_SUCCESS;
 }
 
-// 8-bit operand planes: 64-sample boxes of 64 bytes, 64-byte swizzle.
-bool make_map8(CUtensorMap* map, const uint8_t* base, int64_t rows, int64_t ldw, uint32_t box_rows) {
+// The interleaved 8-bit correction plane: rows of 2 * ldw bytes, boxes of 128 bytes
+// (64 samples of H8 and their 64 of L8) with a 128-byte swizzle.
+bool make_map_hl8(CUtensorMap* map, const uint8_t* base, int64_t rows, int64_t ldw, uint32_t box_rows) {
     EncodeTiledFn enc = encode_fn();
     if (!enc) return false;
-    cuuint64_t dims[2] = {(cuuint64_t)ldw, (cuuint64_t)rows};
-    cuuint64_t strides[1] = {(cuuint64_t)ldw};
-    cuuint32_t box[2] = {(cuuint32_t)BK, box_rows};
+    cuuint64_t dims[2] = {(cuuint64_t)(2 * ldw), (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)(2 * ldw)};
+    cuuint32_t box[2] = {(cuuint32_t)(2 * BK), box_rows};
     cuuint32_t estr[2] = {1, 1};
     CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, (void*)base, dims, strides, box, estr,
-                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r == CUDA_SUCCESS;
 }
@@ -899,10 +885,9 @@ static_assert((SUB1 == 1 || SUB1 == 2 || SUB1 == 4) && (SUB2 == 1 || SUB2 == 2 |
 
 }  // namespace
 
-// Whi/Wlo (16-bit) and H8/L8 (8-bit): rows >= ceil(n*bins/256)*256 + 256 rows of
-// ldw values, zero beyond row n*bins and beyond column m; ldw a multiple of 64.
-cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, const uint8_t* H8, const uint8_t* L8,
-                         int64_t ldw, const double* H, int64_t n, int64_t m, int bins, int fmt, int mode, float* MI,
+// Whi/Wlo (16-bit) and HL8 (8-bit, 2 * ldw bytes per row): rows >= ceil(n*bins/256)*256
+// + 256 rows of ldw samples, zero beyond row n*bins and beyond sample m; ldw a multiple of 64.
+cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, const uint8_t* HL8, int64_t ldw, const double* H, int64_t n, int64_t m, int bins, int fmt, int mode, float* MI,
                          int64_t ldmi, int* timeout_flag, cudaStream_t stream, int64_t* launches, int64_t gene0,
                          int64_t gene1, const TcWaitHook* hook) {
     if (bins != BINS || (ldw % BK) != 0) return cudaErrorNotSupported;
@@ -918,7 +903,7 @@ cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, const uint8_t
     if (major < 10) return cudaErrorNotSupported;
     const int64_t rows = ((n * bins + 255) / 256) * 256 + 256;
     if (mode == TC_SPLIT16 && !Wlo) return cudaErrorNotSupported;
-    if (mode == TC_F8C && (!H8 || !L8)) return cudaErrorNotSupported;
+    if (mode == TC_F8C && !HL8) return cudaErrorNotSupported;
     // A maps (128-row boxes) and B maps with b_rows-row boxes (240: whole B tile; 120: a pair's half)
     CUtensorMap ma_hi, ma_lo, mb_hi, mb_lo, ma_l8, mb_l8;
     auto make_maps = [&](uint32_t b_rows) -> bool {
@@ -929,8 +914,7 @@ cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, const uint8_t
         if (mode == TC_SPLIT16)
             return make_map(&ma_lo, Wlo, fmt, rows, ldw, MROWS) && make_map(&mb_lo, Wlo, fmt, rows, ldw, b_rows);
         if (mode == TC_F8C)
-            return make_map8(&ma_lo, H8, rows, ldw, MROWS) && make_map8(&mb_lo, H8, rows, ldw, b_rows) &&
-                   make_map8(&ma_l8, L8, rows, ldw, MROWS) && make_map8(&mb_l8, L8, rows, ldw, b_rows);
+            return make_map_hl8(&ma_lo, HL8, rows, ldw, MROWS) && make_map_hl8(&mb_lo, HL8, rows, ldw, b_rows);
         return true;
     };
     TcArgs a;
