@@ -65,6 +65,10 @@ constexpr int MROWS = 128;             // MMA M
 constexpr int NCOLS = GBN * BINS;      // MMA N = 240
 constexpr int BK = 64;                 // samples per stage (128 bytes of 16-bit)
 constexpr int TMEM_COLS = 256;
+// 2-SM form: warps 0 and 6 issue the TMA loads (alternate 64-sample slices), 1 the MMAs,
+// 2-5 the epilogue.  (The 1-SM form keeps one producer warp and 192 threads.)
+constexpr int PRODUCER_B_WARP = 6;
+constexpr int PAIR_THREADS = 224;
 // A-tile bytes of one rasterization group: 32 MB up to 2,048 samples, 16 MB beyond
 // (longer rows mean larger B tiles streaming past the group in L2).
 inline int64_t group_bytes(int64_t ldw) { return ldw <= 2048 ? (32ll << 20) : (16ll << 20); }
@@ -568,7 +572,7 @@ __device__ __forceinline__ bool pair_tile_of(int64_t L, const TcArgs& a, int& IP
 
 // TcArgs in pair units: TI = pair tiles (24 genes), I0 / TIr = the launch's pair range.
 template <int MODE, int STAGES, int SUB>
-__global__ void __launch_bounds__(192, 1)
+__global__ void __launch_bounds__(PAIR_THREADS, 1)
     mi_tc_pair_kernel(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CUtensorMap map_lo,
                       const __grid_constant__ CUtensorMap mapb_hi, const __grid_constant__ CUtensorMap mapb_lo,
                       const __grid_constant__ CUtensorMap map_l8, const __grid_constant__ CUtensorMap mapb_l8,
@@ -583,11 +587,16 @@ __global__ void __launch_bounds__(192, 1)
     const uint32_t raw = smem_u32(smem_raw);
     const uint32_t base = (raw + 1023u) & ~1023u;
     uint8_t* gbase = smem_raw + (base - raw);
+    // ring of SLOTS = STAGES x SUB slices: the MMA issuer waits once per stage (full, one
+    // arrival per slice), but every slice is released on its own (empty, one commit per
+    // slice), so a slot refills while the rest of the ring is consumed
+    constexpr int SLOTS = STAGES * SUB;
     float* part = reinterpret_cast<float*>(gbase + STAGES * STAGE_BYTES);
     const uint32_t bars = base + STAGES * STAGE_BYTES + PART_BYTES;
     const uint32_t full0 = bars, empty0 = bars + 8 * STAGES;
-    const uint32_t tfull0 = bars + 16 * STAGES, tempty0 = tfull0 + 16;
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(gbase + STAGES * STAGE_BYTES + PART_BYTES + 16 * STAGES + 32);
+    const uint32_t tfull0 = empty0 + 8 * SLOTS, tempty0 = tfull0 + 16;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(gbase + STAGES * STAGE_BYTES + PART_BYTES + 8 * STAGES +
+                                                      8 * SLOTS + 32);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -595,10 +604,8 @@ __global__ void __launch_bounds__(192, 1)
     const bool leader = rank == 0;
     const int64_t c0 = cluster_index(), nc = cluster_total();
     if (tid == 0) {
-        for (int s = 0; s < STAGES; ++s) {
-            mbar_init(full0 + 8 * s, 1);
-            mbar_init(empty0 + 8 * s, 1);
-        }
+        for (int s = 0; s < STAGES; ++s) mbar_init(full0 + 8 * s, SUB);  // one arrival per slice
+        for (int r = 0; r < SLOTS; ++r) mbar_init(empty0 + 8 * r, 1);
         for (int b = 0; b < 2; ++b) {
             mbar_init(tfull0 + 8 * b, 1);
             mbar_init(tempty0 + 8 * b, 8);
@@ -620,31 +627,41 @@ __global__ void __launch_bounds__(192, 1)
     const int QP = (KT + SUB - 1) / SUB;
     const int QT = F8C ? 2 * QP : QP;
 
-    if (warp == 0) {
+    if (warp == 0 || warp == PRODUCER_B_WARP) {
         if (lane == 0) {
-            // ---------------- TMA producer (both CTAs: own A tile, own half of B) ----------------
-            int64_t g = 0;
+            // ---------------- TMA producers (both CTAs: own A tile, own half of B) ----------------
+            // Two threads take alternate slices (a thread waits a few hundred cycles per TMA
+            // instruction and per barrier wait, so one thread alone falls behind 64-sample
+            // slices).  A slice missing at the end of a pass (KT not a multiple of SUB) is a
+            // bare arrival, so every stage takes SUB arrivals and every slot SUB commits a round.
+            const int pid = warp == 0 ? 0 : 1;
+            int64_t g = 0;  // stages issued by this CTA (both producers count all of them)
             bool ok = !args.starve;
             for (int64_t L = c0; L < n_slots && ok; L += nc) {
                 int IP, J;
                 if (!pair_tile_of(L, args, IP, J)) continue;
                 const int rowA = (2 * IP + (int)rank) * GA * BINS;
                 const int rowB = J * GBN * BINS + (int)rank * (NCOLS / 2);
-                for (int q = 0; q < QT; ++q, ++g) {
+                for (int q = 0; q < QT && ok; ++q, ++g) {
                     const int s = (int)(g % STAGES);
-                    const int64_t u = g / STAGES;
-                    if (u > 0 && !(ok = mbar_wait_abortable(empty0 + 8 * s, (uint32_t)((u - 1) & 1), args.err,
-                                                            abort_flag, args.wait_ns)))
-                        break;
-                    const uint32_t st = base + s * STAGE_BYTES;
                     const uint32_t fb = map_to_rank(full0 + 8 * s, 0);
                     const bool corr = F8C && q < QP;
                     const int kt0 = (q % QP) * SUB, ns = KT - kt0 < SUB ? KT - kt0 : SUB;
-                    if (leader) mbar_expect_tx(full0 + 8 * s, 2u * (uint32_t)ns * SLICE);
-#pragma unroll
+#pragma unroll 1
                     for (int j = 0; j < SUB; ++j) {
-                        if (j >= ns) break;
-                        const uint32_t sl = st + j * SLICE;
+                        const int64_t gs = g * SUB + j;  // slice slot sequence
+                        if ((int)(gs & 1) != pid) continue;
+                        const int r = (int)(gs % SLOTS);
+                        const int64_t u = gs / SLOTS;
+                        if (u > 0 && !(ok = mbar_wait_abortable(empty0 + 8 * r, (uint32_t)((u - 1) & 1), args.err,
+                                                                abort_flag, args.wait_ns)))
+                            break;
+                        if (j >= ns) {
+                            if (leader) mbar_arrive(full0 + 8 * s);
+                            continue;
+                        }
+                        if (leader) mbar_expect_tx(full0 + 8 * s, 2u * SLICE);  // this slice of both CTAs
+                        const uint32_t sl = base + (uint32_t)r * SLICE;
                         const int x = (kt0 + j) * BK;
                         if (corr) {  // H8|L8 of 64 samples: one 128-byte box row per operand row
                             tma_load_2d_pair(sl, &map_lo, 2 * x, rowA, fb);
@@ -660,11 +677,12 @@ __global__ void __launch_bounds__(192, 1)
                     }
                 }
             }
-            // drain: every stage this CTA filled has been consumed by the MMAs
-            // (the multicast commits reach both CTAs), so no load is still in flight
-            for (int s = 0; s < STAGES && (int64_t)s < g; ++s) {
-                const int64_t last = (g - 1 - s) / STAGES;
-                mbar_wait_abortable(empty0 + 8 * s, (uint32_t)(last & 1), args.err, abort_flag, args.wait_ns);
+            // drain: every slot filled has been consumed by the MMAs (the multicast commits
+            // reach both CTAs), so no load is still in flight
+            const int64_t G = g * SUB;
+            for (int r = 0; r < SLOTS && (int64_t)r < G; ++r) {
+                const int64_t last = (G - 1 - r) / SLOTS;
+                mbar_wait_abortable(empty0 + 8 * r, (uint32_t)(last & 1), args.err, abort_flag, args.wait_ns);
             }
         }
         __syncwarp();
@@ -689,38 +707,40 @@ __global__ void __launch_bounds__(192, 1)
                                                    abort_flag, args.wait_ns)))
                         break;
                     tc_fence_after();
-                    const uint32_t st = base + s * STAGE_BYTES;
                     const bool corr = F8C && q < QP;
                     const int kt0 = (q % QP) * SUB, ns = KT - kt0 < SUB ? KT - kt0 : SUB;
 #pragma unroll
                     for (int j = 0; j < SUB; ++j) {
-                        if (j >= ns) break;
-                        const uint32_t sl = st + j * SLICE;
-                        if (corr) {
+                        const int r = (int)((g * SUB + j) % SLOTS);
+                        const uint32_t sl = base + (uint32_t)r * SLICE;
+                        if (j < ns) {
+                            if (corr) {
 #pragma unroll
-                            for (int k = 0; k < BK / 32; ++k) {
-                                const uint64_t ah = sdesc_sw128(sl + 32 * k), al = sdesc_sw128(sl + HL8_OFF + 32 * k);
-                                const uint64_t bh = sdesc_sw128(sl + A_BYTES + 32 * k);
-                                const uint64_t bl = sdesc_sw128(sl + A_BYTES + HL8_OFF + 32 * k);
-                                mma2_f8(dacc, ah, bl, args.idesc8, (q > 0 || j > 0 || k > 0) ? 1u : 0u);
-                                mma2_f8(dacc, al, bh, args.idesc8, 1u);
-                            }
-                            continue;
-                        }
+                                for (int k = 0; k < BK / 32; ++k) {
+                                    const uint64_t ah = sdesc_sw128(sl + 32 * k);
+                                    const uint64_t al = sdesc_sw128(sl + HL8_OFF + 32 * k);
+                                    const uint64_t bh = sdesc_sw128(sl + A_BYTES + 32 * k);
+                                    const uint64_t bl = sdesc_sw128(sl + A_BYTES + HL8_OFF + 32 * k);
+                                    mma2_f8(dacc, ah, bl, args.idesc8, (q > 0 || j > 0 || k > 0) ? 1u : 0u);
+                                    mma2_f8(dacc, al, bh, args.idesc8, 1u);
+                                }
+                            } else {
 #pragma unroll
-                        for (int k = 0; k < BK / 16; ++k) {
-                            const uint64_t ahi = sdesc_sw128(sl + 32 * k);
-                            const uint64_t bhi = sdesc_sw128(sl + A_BYTES + 32 * k);
-                            mma2_f16(dacc, ahi, bhi, args.idesc, (F8C || q > 0 || j > 0 || k > 0) ? 1u : 0u);
-                            if (SPLIT) {
-                                const uint64_t alo = sdesc_sw128(sl + HALF + 32 * k);
-                                const uint64_t blo = sdesc_sw128(sl + HALF + A_BYTES + 32 * k);
-                                mma2_f16(dacc, ahi, blo, args.idesc, 1u);
-                                mma2_f16(dacc, alo, bhi, args.idesc, 1u);
+                                for (int k = 0; k < BK / 16; ++k) {
+                                    const uint64_t ahi = sdesc_sw128(sl + 32 * k);
+                                    const uint64_t bhi = sdesc_sw128(sl + A_BYTES + 32 * k);
+                                    mma2_f16(dacc, ahi, bhi, args.idesc, (F8C || q > 0 || j > 0 || k > 0) ? 1u : 0u);
+                                    if (SPLIT) {
+                                        const uint64_t alo = sdesc_sw128(sl + HALF + 32 * k);
+                                        const uint64_t blo = sdesc_sw128(sl + HALF + A_BYTES + 32 * k);
+                                        mma2_f16(dacc, ahi, blo, args.idesc, 1u);
+                                        mma2_f16(dacc, alo, bhi, args.idesc, 1u);
+                                    }
+                                }
                             }
                         }
+                        mma2_commit_both(empty0 + 8 * r);  // frees this slot once its MMAs have read it
                     }
-                    mma2_commit_both(empty0 + 8 * s);
                 }
                 if (!ok) break;
                 mma2_commit_both(tfull0 + 8 * ab);
@@ -813,7 +833,9 @@ cudaError_t launch_pair(const CUtensorMap& a0, const CUtensorMap& a1, const CUte
                         const CUtensorMap& a2, const CUtensorMap& b2, const TcArgs& a, int64_t n_slots,
                         cudaStream_t stream) {
     constexpr uint32_t stage_bytes = SUB * (MODE == TC_SPLIT16 ? 2u : 1u) * (A_BYTES + BH_BYTES);
-    const size_t smem = 1024 + STAGES * stage_bytes + MROWS * PSTRIDE * 4 + 16 * STAGES + 32 + 16;
+    // stages, epilogue partials, full (per stage) and empty (per slice) barriers, two accumulator
+    // barrier pairs, the tensor-memory slot and the abort flag
+    const size_t smem = 1024 + STAGES * stage_bytes + MROWS * PSTRIDE * 4 + 8 * STAGES + 8 * STAGES * SUB + 32 + 16;
     cudaError_t e = cudaFuncSetAttribute(mi_tc_pair_kernel<MODE, STAGES, SUB>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -823,7 +845,7 @@ cudaError_t launch_pair(const CUtensorMap& a0, const CUtensorMap& a1, const CUte
     attr[0].val.clusterDim.x = 2;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
-    cfg.blockDim = dim3(192, 1, 1);
+    cfg.blockDim = dim3(PAIR_THREADS, 1, 1);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = stream;
     cfg.attrs = attr;
