@@ -493,12 +493,15 @@ __global__ void __launch_bounds__(192, 1)
 // samples the stages carry 31 KB instead of 46 KB for the same MMA time, which
 // is what the L2 -> SM path sustains at the tensor pipe's rate.  Tiles are 24 x 24
 // genes (pair index IP over A, J over B; only J >= IP run).
-//   leader (rank 0): warp 0 TMA for its halves, warp 1 the MMA issuer, warps 2-5 epilogue
-//   peer   (rank 1): warp 0 TMA for its halves, warps 2-5 epilogue
-// Full barriers live in the leader (its expect_tx covers both CTAs' bytes; the
-// peer's loads signal it through the cta_group::2 TMA form); stage-empty and
-// accumulator-full barriers in both CTAs (multicast commits); accumulator-empty in
-// the leader (8 arrivals: both CTAs' epilogue warps).
+//   leader (rank 0): warps 0 and 6 TMA for its halves (alternate slices), warp 1 the
+//                    MMA issuer, warps 2-5 epilogue
+//   peer   (rank 1): warps 0 and 6 TMA for its halves, warps 2-5 epilogue
+// The ring holds STAGES x SUB slices.  Full barriers (one per stage, SUB arrivals) live
+// in the leader: each slice's expect_tx covers both CTAs' bytes, the peer's loads signal
+// it through the cta_group::2 TMA form, and the MMA issuer waits once per stage.  Slot
+// empty barriers (one per slice, a multicast commit after that slice's MMAs) and the
+// accumulator-full barriers sit in both CTAs; accumulator-empty in the leader (8
+// arrivals: both CTAs' epilogue warps).
 constexpr uint32_t BH_BYTES = (NCOLS / 2) * BK * 2;   // 15 KB: half a B tile, 16-bit
 
 __device__ __forceinline__ uint32_t cluster_rank() {
