@@ -75,7 +75,6 @@ inline int64_t group_bytes(int64_t ldw) { return ldw <= 2048 ? (32ll << 20) : (1
 constexpr uint32_t A_BYTES = MROWS * BK * 2;   // 16 KB
 constexpr uint32_t B_BYTES = NCOLS * BK * 2;   // 30 KB
 constexpr uint32_t HL8_OFF = 64;               // byte offset of L8 within an interleaved 128-byte row
-constexpr int PSTRIDE = GBN + 1;       // epilogue partials row stride (floats)
 
 // ---------------------------------------------------------------- PTX wrappers
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -261,8 +260,16 @@ __device__ __forceinline__ bool tile_of(int64_t L, const TcArgs& a, int& I, int&
 // H_i + H_j - H_ij in FP64 for the tile's pairs (i in [gi0, gi0 + 12),
 // j in [gj0, gj0 + 24), j >= i) and stores both mirror entries.  The (n*bins)^2
 // joint table never leaves tensor memory.
+// The ten rows (bins) of an A gene are summed inside the warp by a segmented
+// shuffle reduction (a fixed tree order); only per-gene sums pass through shared
+// memory: gsum[0][gene][jl] for the part that starts at the gene's first row, and
+// gsum[1][gene][jl] for the rest of a gene that crosses a 32-row warp boundary.
+constexpr int GSUM_FLOATS = 2 * GA * GBN;  // 2.3 KB
+
+__device__ __forceinline__ bool gene_crosses_warps(int g) { return (BINS * g) / 32 != (BINS * g + BINS - 1) / 32; }
+
 template <typename FreeAcc>
-__device__ __forceinline__ void epilogue_tile(uint32_t trow, float* part, int row, int etid, const TcArgs& args,
+__device__ __forceinline__ void epilogue_tile(uint32_t trow, float* gsum, int row, int etid, const TcArgs& args,
                                               int64_t gi0, int64_t gj0, FreeAcc free_acc) {
     float acc[GBN];
 #pragma unroll
@@ -283,16 +290,36 @@ __device__ __forceinline__ void epilogue_tile(uint32_t trow, float* part, int ro
     tc_fence_before();
     __syncwarp();
     free_acc();
+    const int lane = row & 31, gene = row / BINS;
+    const bool same1 = (lane + 1 < 32) && ((row + 1) / BINS == gene);
+    const bool same2 = (lane + 2 < 32) && ((row + 2) / BINS == gene);
+    const bool same4 = (lane + 4 < 32) && ((row + 4) / BINS == gene);
+    const bool same8 = (lane + 8 < 32) && ((row + 8) / BINS == gene);
 #pragma unroll
-    for (int q = 0; q < GBN; ++q) part[row * PSTRIDE + q] = acc[q];
+    for (int q = 0; q < GBN; ++q) {
+        float a = acc[q], u;
+        u = __shfl_down_sync(0xffffffffu, a, 1);
+        if (same1) a += u;
+        u = __shfl_down_sync(0xffffffffu, a, 2);
+        if (same2) a += u;
+        u = __shfl_down_sync(0xffffffffu, a, 4);
+        if (same4) a += u;
+        u = __shfl_down_sync(0xffffffffu, a, 8);
+        if (same8) a += u;
+        acc[q] = a;
+    }
+    if (gene < GA && (row % BINS == 0 || lane == 0)) {
+        float* dst = gsum + ((row % BINS == 0) ? 0 : GA * GBN) + gene * GBN;
+#pragma unroll
+        for (int q = 0; q < GBN; ++q) dst[q] = acc[q];
+    }
     asm volatile("bar.sync 1, 128;" ::: "memory");
     for (int p = etid; p < GA * GBN; p += 128) {
         const int il = p / GBN, jl = p - il * GBN;
         const int64_t i = gi0 + il, j = gj0 + jl;
         if (i >= args.n || j >= args.n || j < i) continue;
-        double sum = 0.0;
-#pragma unroll
-        for (int a = 0; a < BINS; ++a) sum += (double)part[(il * BINS + a) * PSTRIDE + jl];
+        double sum = (double)gsum[il * GBN + jl];
+        if (gene_crosses_warps(il)) sum += (double)gsum[GA * GBN + il * GBN + jl];
         const float val = (float)(args.H[i] + args.H[j] + sum);  // sum = -H_ij
         args.MI[i * args.ldmi + j] = val;
         args.MI[j * args.ldmi + i] = val;
@@ -320,7 +347,7 @@ __global__ void __launch_bounds__(192, 1)
     uint8_t* gbase = smem_raw + (base - raw);
     constexpr uint32_t SLICE = (SPLIT ? 2 : 1) * (A_BYTES + B_BYTES);  // one 64-sample slice
     constexpr uint32_t STAGE_BYTES = SUB * SLICE;
-    constexpr uint32_t PART_BYTES = MROWS * PSTRIDE * 4;
+    constexpr uint32_t PART_BYTES = GSUM_FLOATS * 4;  // per-gene bin sums of the epilogue
     float* part = reinterpret_cast<float*>(gbase + STAGES * STAGE_BYTES);
     const uint32_t bars = base + STAGES * STAGE_BYTES + PART_BYTES;
     const uint32_t full0 = bars, empty0 = bars + 8 * STAGES;
@@ -496,9 +523,14 @@ __global__ void __launch_bounds__(192, 1)
 //   leader (rank 0): warps 0 and 6 TMA for its halves (alternate slices), warp 1 the
 //                    MMA issuer, warps 2-5 epilogue
 //   peer   (rank 1): warps 0 and 6 TMA for its halves, warps 2-5 epilogue
-// The ring holds STAGES x SUB slices.  Full barriers (one per stage, SUB arrivals) live
-// in the leader: each slice's expect_tx covers both CTAs' bytes, the peer's loads signal
-// it through the cta_group::2 TMA form, and the MMA issuer waits once per stage.  Slot
+// The ring holds SLOTS slices; a stage is SUB consecutive slices (slot (stage*SUB + j)
+// mod SLOTS), so the ring length need not be a multiple of the stage.  Full barriers
+// (NF = ceil(SLOTS / SUB), one per stage in flight, SUB arrivals) live in the leader:
+// each slice's expect_tx covers both CTAs' bytes, the peer's loads signal it through
+// the cta_group::2 TMA form, and the MMA issuer waits once per stage.  A producer
+// refills a slot only after the MMAs of the slice SLOTS earlier committed, which is in
+// stage (g*SUB - SLOTS)/SUB >= g - NF, so a full barrier is never re-armed before the
+// issuer has passed its previous phase.  Slot
 // empty barriers (one per slice, a multicast commit after that slice's MMAs) and the
 // accumulator-full barriers sit in both CTAs; accumulator-empty in the leader (8
 // arrivals: both CTAs' epilogue warps).
@@ -574,7 +606,7 @@ __device__ __forceinline__ bool pair_tile_of(int64_t L, const TcArgs& a, int& IP
 }
 
 // TcArgs in pair units: TI = pair tiles (24 genes), I0 / TIr = the launch's pair range.
-template <int MODE, int STAGES, int SUB>
+template <int MODE, int SLOTS, int SUB>
 __global__ void __launch_bounds__(PAIR_THREADS, 1)
     mi_tc_pair_kernel(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CUtensorMap map_lo,
                       const __grid_constant__ CUtensorMap mapb_hi, const __grid_constant__ CUtensorMap mapb_lo,
@@ -584,22 +616,22 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1)
     constexpr bool F8C = MODE == TC_F8C;
     constexpr uint32_t HALF = A_BYTES + BH_BYTES;                 // 31 KB
     constexpr uint32_t SLICE = (SPLIT ? 2 : 1) * HALF;
-    constexpr uint32_t STAGE_BYTES = SUB * SLICE;
-    constexpr uint32_t PART_BYTES = MROWS * PSTRIDE * 4;
+    constexpr uint32_t RING_BYTES = SLOTS * SLICE;
+    constexpr uint32_t PART_BYTES = GSUM_FLOATS * 4;  // per-gene bin sums of the epilogue
+    // the MMA issuer waits once per stage (full, one arrival per slice), but every slice
+    // is released on its own (empty, one commit per slice), so a slot refills while the
+    // rest of the ring is consumed
+    constexpr int NF = (SLOTS + SUB - 1) / SUB;
+    static_assert(NF * SUB >= SLOTS && SLOTS >= SUB, "ring of at least one stage");
     extern __shared__ uint8_t smem_raw[];
     const uint32_t raw = smem_u32(smem_raw);
     const uint32_t base = (raw + 1023u) & ~1023u;
     uint8_t* gbase = smem_raw + (base - raw);
-    // ring of SLOTS = STAGES x SUB slices: the MMA issuer waits once per stage (full, one
-    // arrival per slice), but every slice is released on its own (empty, one commit per
-    // slice), so a slot refills while the rest of the ring is consumed
-    constexpr int SLOTS = STAGES * SUB;
-    float* part = reinterpret_cast<float*>(gbase + STAGES * STAGE_BYTES);
-    const uint32_t bars = base + STAGES * STAGE_BYTES + PART_BYTES;
-    const uint32_t full0 = bars, empty0 = bars + 8 * STAGES;
+    float* part = reinterpret_cast<float*>(gbase + RING_BYTES);
+    const uint32_t bars = base + RING_BYTES + PART_BYTES;
+    const uint32_t full0 = bars, empty0 = bars + 8 * NF;
     const uint32_t tfull0 = empty0 + 8 * SLOTS, tempty0 = tfull0 + 16;
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(gbase + STAGES * STAGE_BYTES + PART_BYTES + 8 * STAGES +
-                                                      8 * SLOTS + 32);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(gbase + RING_BYTES + PART_BYTES + 8 * NF + 8 * SLOTS + 32);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -607,7 +639,7 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1)
     const bool leader = rank == 0;
     const int64_t c0 = cluster_index(), nc = cluster_total();
     if (tid == 0) {
-        for (int s = 0; s < STAGES; ++s) mbar_init(full0 + 8 * s, SUB);  // one arrival per slice
+        for (int s = 0; s < NF; ++s) mbar_init(full0 + 8 * s, SUB);  // one arrival per slice
         for (int r = 0; r < SLOTS; ++r) mbar_init(empty0 + 8 * r, 1);
         for (int b = 0; b < 2; ++b) {
             mbar_init(tfull0 + 8 * b, 1);
@@ -646,7 +678,7 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1)
                 const int rowA = (2 * IP + (int)rank) * GA * BINS;
                 const int rowB = J * GBN * BINS + (int)rank * (NCOLS / 2);
                 for (int q = 0; q < QT && ok; ++q, ++g) {
-                    const int s = (int)(g % STAGES);
+                    const int s = (int)(g % NF);
                     const uint32_t fb = map_to_rank(full0 + 8 * s, 0);
                     const bool corr = F8C && q < QP;
                     const int kt0 = (q % QP) * SUB, ns = KT - kt0 < SUB ? KT - kt0 : SUB;
@@ -705,8 +737,8 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1)
                 tc_fence_after();
                 const uint32_t dacc = tmem + (uint32_t)(ab * TMEM_COLS);
                 for (int q = 0; q < QT; ++q, ++g) {
-                    const int s = (int)(g % STAGES);
-                    if (!(ok = mbar_wait_abortable(full0 + 8 * s, (uint32_t)((g / STAGES) & 1), args.err,
+                    const int s = (int)(g % NF);
+                    if (!(ok = mbar_wait_abortable(full0 + 8 * s, (uint32_t)((g / NF) & 1), args.err,
                                                    abort_flag, args.wait_ns)))
                         break;
                     tc_fence_after();
@@ -831,15 +863,16 @@ bool make_map_hl8(CUtensorMap* map, const uint8_t* base, int64_t rows, int64_t l
 // The 2-SM form: clusters of two CTAs, as many as fit at once (persistent).
 // Returns cudaErrorNotSupported when no cluster of two fits (the caller then
 // runs the 1-SM form).
-template <int MODE, int STAGES, int SUB>
+template <int MODE, int SLOTS, int SUB>
 cudaError_t launch_pair(const CUtensorMap& a0, const CUtensorMap& a1, const CUtensorMap& b0, const CUtensorMap& b1,
                         const CUtensorMap& a2, const CUtensorMap& b2, const TcArgs& a, int64_t n_slots,
                         cudaStream_t stream) {
-    constexpr uint32_t stage_bytes = SUB * (MODE == TC_SPLIT16 ? 2u : 1u) * (A_BYTES + BH_BYTES);
-    // stages, epilogue partials, full (per stage) and empty (per slice) barriers, two accumulator
-    // barrier pairs, the tensor-memory slot and the abort flag
-    const size_t smem = 1024 + STAGES * stage_bytes + MROWS * PSTRIDE * 4 + 8 * STAGES + 8 * STAGES * SUB + 32 + 16;
-    cudaError_t e = cudaFuncSetAttribute(mi_tc_pair_kernel<MODE, STAGES, SUB>,
+    constexpr uint32_t slice_bytes = (MODE == TC_SPLIT16 ? 2u : 1u) * (A_BYTES + BH_BYTES);
+    constexpr int NF = (SLOTS + SUB - 1) / SUB;
+    // ring, epilogue gene sums, full (per stage in flight) and empty (per slice) barriers,
+    // two accumulator barrier pairs, the tensor-memory slot and the abort flag
+    const size_t smem = 1024 + SLOTS * slice_bytes + GSUM_FLOATS * 4 + 8 * NF + 8 * SLOTS + 32 + 16;
+    cudaError_t e = cudaFuncSetAttribute(mi_tc_pair_kernel<MODE, SLOTS, SUB>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     cudaLaunchConfig_t cfg = {};
@@ -858,14 +891,14 @@ cudaError_t launch_pair(const CUtensorMap& a0, const CUtensorMap& a1, const CUte
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cfg.gridDim = dim3((unsigned)(sms & ~1), 1, 1);
     int clusters = 0;
-    e = cudaOccupancyMaxActiveClusters(&clusters, mi_tc_pair_kernel<MODE, STAGES, SUB>, &cfg);
+    e = cudaOccupancyMaxActiveClusters(&clusters, mi_tc_pair_kernel<MODE, SLOTS, SUB>, &cfg);
     if (e != cudaSuccess || clusters < 1) {
         cudaGetLastError();
         return cudaErrorNotSupported;
     }
     const int64_t nclu = n_slots < clusters ? n_slots : clusters;
     cfg.gridDim = dim3((unsigned)(2 * nclu), 1, 1);
-    e = cudaLaunchKernelEx(&cfg, mi_tc_pair_kernel<MODE, STAGES, SUB>, a0, a1, b0, b1, a2, b2, a, n_slots);
+    e = cudaLaunchKernelEx(&cfg, mi_tc_pair_kernel<MODE, SLOTS, SUB>, a0, a1, b0, b1, a2, b2, a, n_slots);
     if (e != cudaSuccess) return e;
     return cudaGetLastError();
 }
@@ -885,7 +918,7 @@ cudaError_t launch_mode(const CUtensorMap& a0, const CUtensorMap& a1, const CUte
                         const CUtensorMap& a2, const CUtensorMap& b2, const TcArgs& a, int64_t n_slots, int64_t grid,
                         cudaStream_t stream) {
     constexpr uint32_t stage_bytes = SUB * (MODE == TC_SPLIT16 ? 2u : 1u) * (A_BYTES + B_BYTES);
-    const size_t smem = 1024 + STAGES * stage_bytes + MROWS * PSTRIDE * 4 + 16 * STAGES + 32 + 16;
+    const size_t smem = 1024 + STAGES * stage_bytes + GSUM_FLOATS * 4 + 16 * STAGES + 32 + 16;
     cudaError_t e = cudaFuncSetAttribute(mi_tc_kernel<MODE, STAGES, SUB>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -898,15 +931,21 @@ cudaError_t launch_mode(const CUtensorMap& a0, const CUtensorMap& a1, const CUte
 // Measured at 20,000 x 2,000 (weights + MI, ms; FP8-corrected / single BF16):
 // 1-SM 1 slice x 4 stages 116.2 / 56.9, 2 x 2 123.6 / 61.6; 2-SM 1 x 6 117.9 /
 // 60.7, 2 x 3 112.0 / 54.1, 3 x 2 107.0 / 52.2 (BF16 split: 1-SM 139.4, 2-SM 131.6).
+// With per-slice release, two producers and the 2.3 KB epilogue (2-SM ring slots /
+// slices per stage): 6 / 3 89.8 / 46.4, 7 / 3 104.1 / 48.2, 7 / 2 105.7 / 50.2,
+// 7 / 1 115.4 / 55.3, 6 / 2 106.2 / 51.3; 1-SM 101.5 / 52.1.
 #ifndef MCPG_TC_SUB
 #define MCPG_TC_SUB 1
 #endif
 #ifndef MCPG_TC_PSUB
 #define MCPG_TC_PSUB 3
 #endif
-constexpr int SUB1 = MCPG_TC_SUB, SUB2 = MCPG_TC_PSUB;
-static_assert((SUB1 == 1 || SUB1 == 2 || SUB1 == 4) && (SUB2 == 1 || SUB2 == 2 || SUB2 == 3 || SUB2 == 6),
-              "slices per stage");
+#ifndef MCPG_TC_PSLOTS
+#define MCPG_TC_PSLOTS 6
+#endif
+constexpr int SUB1 = MCPG_TC_SUB, SUB2 = MCPG_TC_PSUB, SLOTS2 = MCPG_TC_PSLOTS;
+static_assert((SUB1 == 1 || SUB1 == 2 || SUB1 == 4) && (SUB2 >= 1 && SUB2 <= 6) && SLOTS2 >= SUB2 && SLOTS2 <= 7,
+              "slices per stage, ring slots");
 
 }  // namespace
 
@@ -982,9 +1021,9 @@ cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, const uint8_t
         if (mode == TC_SPLIT16)
             e = launch_pair<TC_SPLIT16, 3, 1>(ma_hi, ma_lo, mb_hi, mb_lo, ma_l8, mb_l8, p, pslots, stream);
         else if (mode == TC_F8C)
-            e = launch_pair<TC_F8C, 6 / SUB2, SUB2>(ma_hi, ma_lo, mb_hi, mb_lo, ma_l8, mb_l8, p, pslots, stream);
+            e = launch_pair<TC_F8C, SLOTS2, SUB2>(ma_hi, ma_lo, mb_hi, mb_lo, ma_l8, mb_l8, p, pslots, stream);
         else
-            e = launch_pair<TC_SINGLE, 6 / SUB2, SUB2>(ma_hi, ma_lo, mb_hi, mb_lo, ma_l8, mb_l8, p, pslots, stream);
+            e = launch_pair<TC_SINGLE, SLOTS2, SUB2>(ma_hi, ma_lo, mb_hi, mb_lo, ma_l8, mb_l8, p, pslots, stream);
         if (e != cudaErrorNotSupported) {
             if (launches) ++*launches;
             return e;
