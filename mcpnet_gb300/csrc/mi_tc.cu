@@ -65,10 +65,14 @@ constexpr int MROWS = 128;             // MMA M
 constexpr int NCOLS = GBN * BINS;      // MMA N = 240
 constexpr int BK = 64;                 // samples per stage (128 bytes of 16-bit)
 constexpr int TMEM_COLS = 256;
-// 2-SM form: warps 0 and 6 issue the TMA loads (alternate 64-sample slices), 1 the MMAs,
-// 2-5 the epilogue.  (The 1-SM form keeps one producer warp and 192 threads.)
-constexpr int PRODUCER_B_WARP = 6;
-constexpr int PAIR_THREADS = 224;
+// 2-SM form: warp 0 and warps 6.. issue the TMA loads (64-sample slices round robin),
+// 1 the MMAs, 2-5 the epilogue.  (The 1-SM form keeps one producer warp and 192 threads.)
+#ifndef MCPG_TC_PPROD
+#define MCPG_TC_PPROD 2
+#endif
+constexpr int NPROD = MCPG_TC_PPROD;
+static_assert(NPROD >= 1 && NPROD <= 3, "producer threads per CTA");
+constexpr int PAIR_THREADS = 32 * (6 + NPROD - 1);
 // A-tile bytes of one rasterization group: 32 MB up to 2,048 samples, 16 MB beyond
 // (longer rows mean larger B tiles streaming past the group in L2).
 inline int64_t group_bytes(int64_t ldw) { return ldw <= 2048 ? (32ll << 20) : (16ll << 20); }
@@ -151,14 +155,18 @@ __device__ __forceinline__ void mma_commit(uint32_t bar) {
 }
 
 // 32 lanes x 32 bits, 16 consecutive columns per thread.
+// tcgen05.ld writes its destination registers asynchronously, so the wait sits in the
+// same asm statement: the compiler sees the registers defined only once they hold the
+// data, and cannot move, spill or reuse them in between.
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
     uint32_t r[16];
     asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+        "tcgen05.wait::ld.sync.aligned;"
         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
           "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        : "r"(taddr)
+        : "memory");
 #pragma unroll
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
@@ -662,15 +670,15 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1)
     const int QP = (KT + SUB - 1) / SUB;
     const int QT = F8C ? 2 * QP : QP;
 
-    if (warp == 0 || warp == PRODUCER_B_WARP) {
+    if (warp == 0 || warp >= 6) {
         if (lane == 0) {
             // ---------------- TMA producers (both CTAs: own A tile, own half of B) ----------------
-            // Two threads take alternate slices (a thread waits a few hundred cycles per TMA
-            // instruction and per barrier wait, so one thread alone falls behind 64-sample
-            // slices).  A slice missing at the end of a pass (KT not a multiple of SUB) is a
+            // NPROD threads take the slices round robin (a thread waits a few hundred cycles
+            // per TMA instruction and per barrier wait, so one thread alone falls behind
+            // 64-sample slices; two are fastest, measured against one and three).  A slice missing at the end of a pass (KT not a multiple of SUB) is a
             // bare arrival, so every stage takes SUB arrivals and every slot SUB commits a round.
-            const int pid = warp == 0 ? 0 : 1;
-            int64_t g = 0;  // stages issued by this CTA (both producers count all of them)
+            const int pid = warp == 0 ? 0 : warp - 5;
+            int64_t g = 0;  // stages issued by this CTA (every producer counts all of them)
             bool ok = !args.starve;
             for (int64_t L = c0; L < n_slots && ok; L += nc) {
                 int IP, J;
@@ -685,7 +693,7 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1)
 #pragma unroll 1
                     for (int j = 0; j < SUB; ++j) {
                         const int64_t gs = g * SUB + j;  // slice slot sequence
-                        if ((int)(gs & 1) != pid) continue;
+                        if ((int)(gs % NPROD) != pid) continue;
                         const int r = (int)(gs % SLOTS);
                         const int64_t u = gs / SLOTS;
                         if (u > 0 && !(ok = mbar_wait_abortable(empty0 + 8 * r, (uint32_t)((u - 1) & 1), args.err,
