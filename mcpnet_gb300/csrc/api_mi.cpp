@@ -61,7 +61,7 @@ int mi_prepare(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_t ldx
     pl.split = (precision == MCPG_MI_BF16X3 || precision == MCPG_MI_FP16X3) ? mcpg::TC_SPLIT16
                : precision == MCPG_MI_BF16F8                                ? mcpg::TC_F8C
                                                                             : mcpg::TC_SINGLE;
-    const int64_t ldw = round_up(m, 64);
+    const int64_t ldw = mcpg::mi_tc_pitch(m);
     const int64_t rows = round_up(n * bins, 256) + 256;  // whole tiles stay in bounds
     // S_W1: the 16-bit lo plane, or the interleaved 8-bit plane H8|L8 (rows of 2 * ldw bytes: the same bytes)
     void *hi, *lo = nullptr;

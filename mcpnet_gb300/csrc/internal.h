@@ -153,6 +153,8 @@ struct TcWaitHook {
     unsigned long long wait_ns = TC_WAIT_NS_DEFAULT;
     int starve = 0;
 };
+// Row pitch (samples) of the tensor-core weight planes for m samples: a multiple of 64.
+int64_t mi_tc_pitch(int64_t m);
 cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, const uint8_t* HL8, int64_t ldw, const double* H, int64_t n, int64_t m, int bins, int fmt, int mode, float* MI,
                          int64_t ldmi, int* timeout_flag, cudaStream_t stream, int64_t* launches, int64_t gene0 = 0,
                          int64_t gene1 = -1, const TcWaitHook* hook = nullptr);

@@ -95,6 +95,16 @@ __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
 __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
 }
+// non-blocking: has the phase of this parity completed?
+__device__ __forceinline__ bool mbar_test(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
 __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
     uint32_t ok;
     asm volatile(
@@ -732,7 +742,16 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1)
     } else if (warp == 1) {
         if (lane == 0 && leader) {
             // ---------------- MMA issuer (leader only) ----------------
-            int64_t g = 0, t = 0;
+            // The tensor pipe runs only slightly behind this thread, so every pause here
+            // (a barrier wait costs ~100 cycles even when the phase is already complete)
+            // shows up as idle tensor cycles.  The next stage's full barrier is therefore
+            // tested without blocking before the current stage's last slice is issued; the
+            // blocking wait runs only when that test found the stage incomplete.  Barrier
+            // and slot indices advance incrementally (no 64-bit division per slice).
+            int64_t t = 0;
+            int fs = 0, rs = 0;    // full barrier of the current stage, slot of its first slice
+            uint32_t fph = 0;      // phase parity of that full barrier
+            bool ready = false;    // the current stage's full barrier was already seen complete
             bool ok = true;
             for (int64_t L = c0; L < n_slots && ok; L += nc) {
                 int IP, J;
@@ -744,18 +763,24 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1)
                     break;
                 tc_fence_after();
                 const uint32_t dacc = tmem + (uint32_t)(ab * TMEM_COLS);
-                for (int q = 0; q < QT; ++q, ++g) {
-                    const int s = (int)(g % NF);
-                    if (!(ok = mbar_wait_abortable(full0 + 8 * s, (uint32_t)((g / NF) & 1), args.err,
-                                                   abort_flag, args.wait_ns)))
+                for (int q = 0; q < QT; ++q) {
+                    if (!ready && !(ok = mbar_wait_abortable(full0 + 8 * fs, fph, args.err, abort_flag,
+                                                             args.wait_ns)))
                         break;
                     tc_fence_after();
+                    const int fs1 = fs + 1 == NF ? 0 : fs + 1;
+                    const uint32_t fph1 = fs + 1 == NF ? fph ^ 1u : fph;
+                    ready = false;
                     const bool corr = F8C && q < QP;
                     const int kt0 = (q % QP) * SUB, ns = KT - kt0 < SUB ? KT - kt0 : SUB;
 #pragma unroll
                     for (int j = 0; j < SUB; ++j) {
-                        const int r = (int)((g * SUB + j) % SLOTS);
+                        const int r = rs;
+                        rs = rs + 1 == SLOTS ? 0 : rs + 1;
                         const uint32_t sl = base + (uint32_t)r * SLICE;
+                        // the next stage of this tile: its barrier's previous phase (stage
+                        // g + 1 - NF) was waited for already, so the test sees its own phase
+                        if (j == SUB - 1 && q + 1 < QT) ready = mbar_test(full0 + 8 * fs1, fph1);
                         if (j < ns) {
                             if (corr) {
 #pragma unroll
@@ -784,6 +809,8 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1)
                         }
                         mma2_commit_both(empty0 + 8 * r);  // frees this slot once its MMAs have read it
                     }
+                    fs = fs1;
+                    fph = fph1;
                 }
                 if (!ok) break;
                 mma2_commit_both(tfull0 + 8 * ab);
@@ -957,6 +984,11 @@ static_assert((SUB1 == 1 || SUB1 == 2 || SUB1 == 4) && (SUB2 >= 1 && SUB2 <= 6) 
 
 }  // namespace
 
+#ifndef MCPG_TC_PITCH_PAD
+#define MCPG_TC_PITCH_PAD 0
+#endif
+int64_t mi_tc_pitch(int64_t m) { return (m + BK - 1) / BK * BK + MCPG_TC_PITCH_PAD; }
+
 // Whi/Wlo (16-bit) and HL8 (8-bit, 2 * ldw bytes per row): rows >= ceil(n*bins/256)*256
 // + 256 rows of ldw samples, zero beyond row n*bins and beyond sample m; ldw a multiple of 64.
 cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, const uint8_t* HL8, int64_t ldw, const double* H, int64_t n, int64_t m, int bins, int fmt, int mode, float* MI,
@@ -998,7 +1030,7 @@ cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, const uint8_t
     a.TJ = (int)((n + GBN - 1) / GBN);
     a.I0 = (int)(gene0 / GA);
     a.TIr = (int)((gene1 + GA - 1) / GA) - a.I0;
-    a.ktiles = (int)(ldw / BK);
+    a.ktiles = (int)((m + BK - 1) / BK);  // the row pitch ldw may exceed the samples
     // the FP8-corrected form accumulates 2^16 P (power-of-two scale: exact)
     a.inv_m = (1.0f / (float)m) * (mode == TC_F8C ? 1.0f / 65536.0f : 1.0f);
     a.idesc = idesc_f16(fmt == 0 ? 1u : 0u, MROWS, NCOLS);
