@@ -411,7 +411,8 @@ int maxmins_tf_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, const
     return MCPG_OK;
 }
 
-// dpi_tf_kernel (dpi.hpp:74-110) over all (x, z), then mask<float,true>.
+// dpi_tf_kernel (dpi.hpp:74-110) over all (x, z), then mask<float,true>: two phases on the
+// TF-first permutation where they apply, else the all-y and TF-y products and one apply pass.
 int dpi_tf_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, float tol, const float* tfs, float* out,
                int64_t ldo, uint8_t* mask, int64_t* removed) {
     if (n < 0) return fail(h, MCPG_ERR_ARG, "dpi_tf: negative size");
@@ -434,6 +435,71 @@ int dpi_tf_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, float tol
     }
     TfSet ts = tf_set(tfs, n);
     const int64_t t = (int64_t)ts.idx.size();
+    const float tm = (float)(1.0 / (1.0 - (double)tol));  // dpi_tf_kernel stores it as IT
+    // Two phases on B = P A P^T with the t TFs first (P: TFs ascending, then the rest).
+    // In that order the x, z exclusion is the diagonal again, a pair of one TF and one
+    // non-TF admits exactly the intermediates y < t, any other pair all y; the deletion
+    // test is an existential one, so the order of the y does not change it.  The first
+    // phase scans the first K1 = min(DPI_K0, t) intermediates, TFs only, which are
+    // admissible for every pair; the pending scan continues each undecided pair to its
+    // own end (t or n).  Outputs go back through P.  On pending-list overflow the
+    // product form below runs and rewrites every output.
+    if (n > 2 * DPI_K0 && t >= 128) {
+        std::vector<int> perm;
+        perm.reserve((size_t)n);
+        {
+            std::vector<uint8_t> is_tf((size_t)n, 0);
+            for (int i : ts.idx) is_tf[(size_t)i] = 1;
+            for (int64_t g = 0; g < n; ++g)
+                if (is_tf[(size_t)g]) perm.push_back((int)g);
+            for (int64_t g = 0; g < n; ++g)
+                if (!is_tf[(size_t)g]) perm.push_back((int)g);
+        }
+        void *pd, *bp, *pend, *cnt;
+        if ((rc = upload(h, S_TFIDX, perm.data(), (size_t)n * sizeof(int), &pd))) return rc;
+        if ((rc = scratch(h, S_M1, (size_t)(n * ldt) * sizeof(float), &bp))) return rc;
+        CK(h, mcpg::launch_gather(a, la, (const int*)pd, (const int*)pd, n, n, (float*)bp, ldt, h->stream,
+                                  &h->launches),
+           "gather kernel (TF-first order)");
+        const int64_t cap = std::max<int64_t>(int64_t(1) << 16, n * n / 32);
+        if ((rc = scratch(h, S_DPI_PEND, (size_t)cap * sizeof(mcpg::DpiPending), &pend))) return rc;
+        if ((rc = scratch(h, S_SMALL, 64, &cnt))) return rc;
+        unsigned long long* cnt_removed = (unsigned long long*)cnt;
+        CK(h, cudaMemsetAsync(cnt, 0, 2 * sizeof(unsigned long long), h->stream), "memset counters");
+        const int64_t k1 = std::min<int64_t>(DPI_K0, t & ~int64_t(3));
+        mcpg::MaxminParams p1{};
+        p1.A = (const float*)bp; p1.lda = ldt; p1.B = (const float*)bp; p1.ldb = ldt;
+        p1.rows = n; p1.cols = n; p1.k_len = k1;
+        p1.C = out; p1.ldc = ldo; p1.E = (const float*)bp; p1.lde = ldt;
+        p1.tm_float = 1; p1.tol_mult_f = tm; p1.perm = (const int*)pd;
+        p1.mask = mask; p1.ldmask = n;
+        p1.removed = cnt_removed;
+        p1.pending = (mcpg::DpiPending*)pend; p1.pending_cap = cap; p1.pending_n = cnt_removed + 1;
+        {
+            PROF(h, "maxmin");
+            CK(h, mcpg::launch_maxmin(p1, mcpg::MM_DPI1, 1, h->stream, &h->launches), "TF DPI kernel (first phase)");
+        }
+        unsigned long long np = 0;
+        CK(h, cudaMemcpyAsync(&np, cnt_removed + 1, sizeof np, cudaMemcpyDeviceToHost, h->stream), "read pending");
+        CK(h, cudaStreamSynchronize(h->stream), "stream synchronize");
+        if (np <= (unsigned long long)cap) {
+            mcpg::DpiPendingTf tf;
+            tf.tsplit = t; tf.perm = (const int*)pd; tf.tol_mult_f = tm; tf.tm_float = 1;
+            {
+                PROF(h, "dpi_pending");
+                CK(h, mcpg::launch_dpi_pending((const float*)bp, ldt, n, k1, p1.pending, (int64_t)np, 0.0, out, ldo,
+                                               mask, n, cnt_removed, h->stream, &h->launches, tf),
+                   "TF DPI kernel (second phase)");
+            }
+            if (removed) {
+                unsigned long long r = 0;
+                CK(h, cudaMemcpyAsync(&r, cnt_removed, sizeof r, cudaMemcpyDeviceToHost, h->stream), "read removed");
+                CK(h, cudaStreamSynchronize(h->stream), "stream synchronize");
+                *removed = (int64_t)r;
+            }
+            return MCPG_OK;
+        }
+    }
     // all-y value (y not in {x, z})
     void* call;
     if ((rc = scratch(h, S_M1, (size_t)(n * ldt) * sizeof(float), &call))) return rc;
@@ -473,7 +539,6 @@ int dpi_tf_dev(mcpg_handle* h, const float* A, int64_t n, int64_t lda, float tol
     if ((rc = upload(h, S_MASK + 0, flag.data(), (size_t)n, &fl))) return rc;
     if ((rc = scratch(h, S_SMALL, 64, &cnt))) return rc;
     CK(h, cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), h->stream), "memset counter");
-    const float tm = (float)(1.0 / (1.0 - (double)tol));  // dpi_tf_kernel stores it as IT
     {
         PROF(h, "dpi_tf_apply");
         CK(h, mcpg::launch_dpi_tf_apply(a, la, (const float*)call, ldt, ctf, ldt, (const uint8_t*)fl, n, tm, out, ldo,

@@ -41,6 +41,9 @@ struct MaxminParams {
     float* R; int64_t ldr;        // RATIO output
     int* changed;                 // CLOSURE flag (device)
     double tol_mult;              // DPI 1/(1 - tol)
+    // DPI threshold in float arithmetic when tm_float != 0: e * tol_mult_f rounded once
+    // (dpi_tf_kernel keeps its multiplier in the value type)
+    float tol_mult_f; int tm_float;
     uint8_t* mask; int64_t ldmask;  // DPI mask (nullable)
     unsigned long long* removed;  // DPI removed count (device, nullable)
     // MM_DPI / MM_EXCL: the excluded k of output (i, j) are excl_row[i] and
@@ -51,6 +54,9 @@ struct MaxminParams {
     // MM_DPI1: pending outputs (capacity pending_cap; *pending_n counts every append,
     // so a count above the capacity means the list overflowed)
     DpiPending* pending; int64_t pending_cap; unsigned long long* pending_n;
+    // MM_DPI / MM_DPI1 on a permuted input P A P^T: output (i, j) goes to
+    // C / mask [perm[i]][perm[j]] (device, nullable = identity)
+    const int* perm;
 };
 
 // symmetric != 0: A == B (same rows), rows == cols; only tiles on or above the
@@ -62,9 +68,19 @@ cudaError_t launch_ratio(const float* A, int64_t lda, const float* M, int64_t ld
 // the intermediates y in [k0, n) (y not in {x, z}) until every undecided orientation is
 // deleted or the row ends, then write out / mask and add to *removed as MM_DPI does.
 // A: n x n (16-byte aligned rows, lda % 4 == 0), also the DPI input E.
+// TF form (dpi_tf_kernel on the permuted input P A P^T, TFs first): tsplit >= 0 is the
+// TF count t; a pair with exactly one TF scans only y < t.  perm (nullable) maps the
+// permuted indices back for out / mask; tm_float selects the float threshold.
+struct DpiPendingTf {
+    int64_t tsplit = -1;
+    const int* perm = nullptr;
+    float tol_mult_f = 0.0f;
+    int tm_float = 0;
+};
 cudaError_t launch_dpi_pending(const float* A, int64_t lda, int64_t n, int64_t k0, const DpiPending* list,
                                int64_t count, double tol_mult, float* out, int64_t ldo, uint8_t* mask,
-                               int64_t ldmask, unsigned long long* removed, cudaStream_t stream, int64_t* launches);
+                               int64_t ldmask, unsigned long long* removed, cudaStream_t stream, int64_t* launches,
+                               const DpiPendingTf& tf = DpiPendingTf());
 cudaError_t launch_set_diagonal(float* A, int64_t rows, int64_t cols, int64_t lda, float value,
                                 cudaStream_t stream, int64_t* launches);
 cudaError_t launch_max_transpose(const float* M, int64_t n, int64_t ldm, float* out, int64_t ldo,

@@ -324,28 +324,29 @@ __global__ void __launch_bounds__(THREADS, MCPG_MM_MINB) maxmin_kernel(const Max
                     any_changed |= (v2 != e2);
                 }
             } else {  // MM_DPI; MM_DPI1 writes only what the first phase decides (deleted)
+                const int64_t oi = p.perm ? (int64_t)p.perm[i] : i, oj = p.perm ? (int64_t)p.perm[j] : j;
                 {
                     const float e = p.E[i * p.lde + j];
-                    const float ixz = (float)((double)e * p.tol_mult);
+                    const float ixz = p.tm_float ? __fmul_rn(e, p.tol_mult_f) : (float)((double)e * p.tol_mult);
                     const bool del = (i == j) || (m >= ixz);
                     if (!DPI1 || del) {
                         const float o = del ? 0.0f : e;
-                        p.C[i * p.ldc + j] = o;
+                        p.C[oi * p.ldc + oj] = o;
                         removed += (o != e);
-                        if (p.mask) p.mask[i * p.ldmask + j] = del ? 1 : 0;
+                        if (p.mask) p.mask[oi * p.ldmask + oj] = del ? 1 : 0;
                     } else {
                         pend0 |= 1ull << (q * TN + r);
                     }
                 }
                 if (mirror) {
                     const float e = p.E[j * p.lde + i];
-                    const float ixz = (float)((double)e * p.tol_mult);
+                    const float ixz = p.tm_float ? __fmul_rn(e, p.tol_mult_f) : (float)((double)e * p.tol_mult);
                     const bool del = (m >= ixz);
                     if (!DPI1 || del) {
                         const float o = del ? 0.0f : e;
-                        p.C[j * p.ldc + i] = o;
+                        p.C[oj * p.ldc + oi] = o;
                         removed += (o != e);
-                        if (p.mask) p.mask[j * p.ldmask + i] = del ? 1 : 0;
+                        if (p.mask) p.mask[oj * p.ldmask + oi] = del ? 1 : 0;
                     } else {
                         pend1 |= 1ull << (q * TN + r);
                     }
@@ -525,11 +526,13 @@ __global__ void ratio_bwd_kernel(const float* A, int64_t lda, const float* M, in
 // max-min reaches every undecided orientation's threshold -- the reference's own
 // early exit, at warp granularity.  Excluded y (x and z) contribute NaN, which the
 // NaN-ignoring max drops, exactly as in the tiled kernel.
+// TF form (dpi_tf_kernel, dpi.hpp:74-110, on P A P^T with the t TFs first): a pair
+// with exactly one TF admits only TF intermediates, i.e. y < t.
 __global__ void __launch_bounds__(256) dpi_pending_kernel(const float* __restrict__ A, int64_t lda, int64_t n,
                                                           int64_t k0, const DpiPending* __restrict__ list,
                                                           int64_t count, double tm, float* __restrict__ out,
                                                           int64_t ldo, uint8_t* __restrict__ mask, int64_t ldmask,
-                                                          unsigned long long* removed) {
+                                                          unsigned long long* removed, const DpiPendingTf tf) {
     const int lane = threadIdx.x & 31;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const float qnan = __int_as_float(0x7fc00000);
@@ -540,13 +543,15 @@ __global__ void __launch_bounds__(256) dpi_pending_kernel(const float* __restric
         const float* rx = A + x * lda;
         const float* rz = A + z * lda;
         const float exz = rx[z], ezx = rz[x];
-        const float t0 = (float)((double)exz * tm), t1 = (float)((double)ezx * tm);
+        const float t0 = tf.tm_float ? __fmul_rn(exz, tf.tol_mult_f) : (float)((double)exz * tm);
+        const float t1 = tf.tm_float ? __fmul_rn(ezx, tf.tol_mult_f) : (float)((double)ezx * tm);
+        const int64_t kend = (tf.tsplit >= 0 && ((x < tf.tsplit) != (z < tf.tsplit))) ? tf.tsplit : n;
         const bool u0 = (d.flags & 1u) != 0, u1 = (d.flags & 2u) != 0;
         const float target = u0 ? (u1 ? fmaxf(t0, t1) : t0) : t1;
         float mm = d.m;
-        for (int64_t y0 = k0; y0 < n; y0 += 128) {
+        for (int64_t y0 = k0; y0 < kend; y0 += 128) {
             const int64_t y = y0 + 4 * lane;
-            if (y + 3 < n) {
+            if (y + 3 < kend) {
                 const float4 a = __ldg(reinterpret_cast<const float4*>(rx + y));
                 const float4 b = __ldg(reinterpret_cast<const float4*>(rz + y));
                 const float v0 = (y == x || y == z) ? qnan : fmin2(a.x, b.x);
@@ -555,7 +560,7 @@ __global__ void __launch_bounds__(256) dpi_pending_kernel(const float* __restric
                 const float v3 = (y + 3 == x || y + 3 == z) ? qnan : fmin2(a.w, b.w);
                 mm = fmax2(fmax2(mm, v0), fmax2(v1, fmax2(v2, v3)));
             } else {
-                for (int64_t c = y; c < n && c < y + 4; ++c)
+                for (int64_t c = y; c < kend && c < y + 4; ++c)
                     if (c != x && c != z) mm = fmax2(mm, fmin2(rx[c], rz[c]));
             }
             if (__any_sync(0xffffffffu, mm >= target)) break;
@@ -563,19 +568,20 @@ __global__ void __launch_bounds__(256) dpi_pending_kernel(const float* __restric
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) mm = fmax2(mm, __shfl_xor_sync(0xffffffffu, mm, o));
         if (lane == 0) {
+            const int64_t ox = tf.perm ? (int64_t)tf.perm[x] : x, oz = tf.perm ? (int64_t)tf.perm[z] : z;
             if (u0) {
                 const bool del = mm >= t0;
                 const float o = del ? 0.0f : exz;
-                out[x * ldo + z] = o;
+                out[ox * ldo + oz] = o;
                 cnt += (o != exz);
-                if (mask) mask[x * ldmask + z] = del ? 1 : 0;
+                if (mask) mask[ox * ldmask + oz] = del ? 1 : 0;
             }
             if (u1) {
                 const bool del = mm >= t1;
                 const float o = del ? 0.0f : ezx;
-                out[z * ldo + x] = o;
+                out[oz * ldo + ox] = o;
                 cnt += (o != ezx);
-                if (mask) mask[z * ldmask + x] = del ? 1 : 0;
+                if (mask) mask[oz * ldmask + ox] = del ? 1 : 0;
             }
         }
     }
@@ -633,7 +639,8 @@ cudaError_t launch_ratio(const float* A, int64_t lda, const float* M, int64_t ld
 
 cudaError_t launch_dpi_pending(const float* A, int64_t lda, int64_t n, int64_t k0, const DpiPending* list,
                                int64_t count, double tol_mult, float* out, int64_t ldo, uint8_t* mask,
-                               int64_t ldmask, unsigned long long* removed, cudaStream_t stream, int64_t* launches) {
+                               int64_t ldmask, unsigned long long* removed, cudaStream_t stream, int64_t* launches,
+                               const DpiPendingTf& tf) {
     if (count <= 0 || n <= 0) return cudaSuccess;
     if ((lda % 4) != 0 || ((uintptr_t)A & 15u) || (k0 % 4) != 0) return cudaErrorInvalidValue;
     if (launches) ++*launches;
@@ -643,7 +650,7 @@ cudaError_t launch_dpi_pending(const float* A, int64_t lda, int64_t n, int64_t k
     const int64_t want = ceil_div(count, (int64_t)8);  // 8 warps per block
     const int64_t grid = want < (int64_t)sms * 8 ? want : (int64_t)sms * 8;
     dpi_pending_kernel<<<(unsigned)grid, 256, 0, stream>>>(A, lda, n, k0, list, count, tol_mult, out, ldo, mask,
-                                                           ldmask, removed);
+                                                           ldmask, removed, tf);
     return cudaGetLastError();
 }
 

@@ -309,33 +309,53 @@ int64_t FN(orc_dpi_rows)(const REAL* A, int64_t n, int64_t lda, double tol, cons
 }
 
 /* dpi_tf_kernel<IT,true> -- include/mcp/filter/dpi.hpp:74-110 (note its
- * multiplier is stored in IT, so i_xz is an IT product), then mask<IT,true>
- * as apps/filter/dpi.cpp:276-287.  tfs: the reference's TF vector (> 0 = TF). */
+ * multiplier is stored in IT, so i_xz is an IT product): is (x, z) deleted?
+ * tfs: the reference's TF vector (> 0 = TF). */
+static int FN(dpi_tf_delete)(const REAL* A, int64_t n, int64_t lda, REAL tm, const REAL* tfs, int64_t x, int64_t z) {
+    if (x == z) return 1;
+    const REAL* rx = A + x * lda;
+    const REAL* rz = A + z * lda;
+    REAL ixz = rx[z] * tm;
+    int tfxz = (tfs[x] > 0) ^ (tfs[z] > 0);
+    int64_t y = 0;
+    for (; y < n && (y == x || y == z || rx[y] < ixz || rz[y] < ixz || ((tfs[y] <= 0) && tfxz)); ++y) {}
+    return y < n;
+}
+
+/* dpi_tf_kernel over all (x, z), then mask<IT,true> as apps/filter/dpi.cpp:276-287. */
 int64_t FN(orc_dpi_tf)(const REAL* A, int64_t n, int64_t lda, REAL tol, const REAL* tfs, REAL* out, int64_t ldo,
                        uint8_t* mask) {
     const REAL tm = (REAL)(1.0 / (1.0 - (double)tol));
     int64_t removed = 0;
 #pragma omp parallel for schedule(dynamic, 1) reduction(+:removed)
     for (int64_t x = 0; x < n; ++x) {
-        const REAL* rx = A + x * lda;
         for (int64_t z = 0; z < n; ++z) {
-            const REAL* rz = A + z * lda;
-            int del;
-            if (x == z) {
-                del = 1;
-            } else {
-                REAL ixz = rx[z] * tm;
-                int tfxz = (tfs[x] > 0) ^ (tfs[z] > 0);
-                int64_t y = 0;
-                for (; y < n && (y == x || y == z || rx[y] < ixz || rz[y] < ixz || ((tfs[y] <= 0) && tfxz)); ++y) {}
-                del = y < n;
-            }
+            int del = FN(dpi_tf_delete)(A, n, lda, tm, tfs, x, z);
             if (mask) mask[x * n + z] = (uint8_t)del;
-            REAL in = rx[z];
+            REAL in = A[x * lda + z];
             REAL o = del ? (REAL)0 : in;
             out[x * ldo + z] = o;
             removed += (o != in);
         }
+    }
+    return removed;
+}
+
+/* orc_dpi_tf restricted to the rows x = rows[0..nr) of the output (row r of out and
+ * mask is row rows[r] of the full filter); returns the removed count of these rows. */
+int64_t FN(orc_dpi_tf_rows)(const REAL* A, int64_t n, int64_t lda, REAL tol, const REAL* tfs, const int64_t* rows,
+                            int64_t nr, REAL* out, int64_t ldo, uint8_t* mask) {
+    const REAL tm = (REAL)(1.0 / (1.0 - (double)tol));
+    int64_t removed = 0;
+#pragma omp parallel for schedule(dynamic, 64) reduction(+:removed)
+    for (int64_t q = 0; q < nr * n; ++q) {
+        const int64_t r = q / n, z = q - r * n, x = rows[r];
+        int del = FN(dpi_tf_delete)(A, n, lda, tm, tfs, x, z);
+        if (mask) mask[r * n + z] = (uint8_t)del;
+        REAL in = A[x * lda + z];
+        REAL o = del ? (REAL)0 : in;
+        out[r * ldo + z] = o;
+        removed += (o != in);
     }
     return removed;
 }

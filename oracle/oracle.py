@@ -73,6 +73,10 @@ def _bind(L, sfx: str, prefix: str):
     if f is not None:
         f.restype = C.c_int64
         f.argtypes = [_vp, _i64, _i64, C.c_float if sfx == "f32" else C.c_double, _vp, _vp, _i64, _vp]
+    f = getattr(L, f"{prefix}dpi_tf_rows_{sfx}", None)
+    if f is not None:
+        f.restype = C.c_int64
+        f.argtypes = [_vp, _i64, _i64, C.c_float if sfx == "f32" else C.c_double, _vp, _vp, _i64, _vp, _i64, _vp]
 
 
 class _TfCompositions:
@@ -381,6 +385,19 @@ class _Port(_TfCompositions, _EvalCompositions):
         mask = np.empty((n, n), dtype=np.uint8)
         removed = getattr(self.L, f"orc_dpi_tf_{self._dt(A)}")(A.ctypes.data, n, n, tol, tfs.ctypes.data,
                                                                out.ctypes.data, n, mask.ctypes.data)
+        return out, mask, int(removed)
+
+    def dpi_tf_rows(self, A, tfs, rows, tol=0.1):
+        """Rows `rows` of dpi_tf(A, tfs, tol): (out rows, mask rows, removed count of those rows)."""
+        A = np.ascontiguousarray(A)
+        tfs = np.ascontiguousarray(tfs, dtype=A.dtype)
+        n = A.shape[0]
+        rows = np.ascontiguousarray(rows, dtype=np.int64)
+        out = np.empty((rows.size, n), dtype=A.dtype)
+        mask = np.empty((rows.size, n), dtype=np.uint8)
+        removed = getattr(self.L, f"orc_dpi_tf_rows_{self._dt(A)}")(A.ctypes.data, n, n, tol, tfs.ctypes.data,
+                                                                    rows.ctypes.data, rows.size, out.ctypes.data, n,
+                                                                    mask.ctypes.data)
         return out, mask, int(removed)
 
     # -- adjoints (this build's definitions; see mcp_oracle_impl.h) --

@@ -93,8 +93,8 @@ def test_c2_plain_fp32_chain_at_2000(gpu, port, built_lib):
 
 
 def _chain_sampled_rows(gpu, port, built_lib, n, m, precision, k_rows):
-    """Runs MI -> diagonal 0 -> M1/M2/M3 + ratios -> DPI(0.1) -> closure on the GPU
-    and checks every output on sampled rows against the oracle, bit for bit."""
+    """Runs MI -> diagonal 0 -> M1/M2/M3 + ratios -> DPI(0.1) -> TF DPI(0.1) -> closure
+    on the GPU and checks every output on sampled rows against the oracle, bit for bit."""
     import torch
     X = built_lib.synth_grn(n, m, seed=SEED)
     f32 = dict(dtype=torch.float32, device="cuda")
@@ -132,6 +132,22 @@ def _chain_sampled_rows(gpu, port, built_lib, n, m, precision, k_rows):
     Do, mo, _ = port.dpi_rows(A, rows, 0.1)
     assert np.array_equal(bits(Dr), bits(Do)), "DPI output rows"
     assert np.array_equal(maskr, mo), "DPI mask rows"
+
+    # TF DPI (dpi_tf_kernel) with a seeded set of n/16 TFs: at these sizes it runs in two
+    # phases on the TF-first permutation of the matrix
+    rng = np.random.default_rng(n + 1)
+    tfs = np.full(n, -np.inf, dtype=np.float32)
+    tfs[rng.choice(n, n // 16, replace=False)] = np.inf
+    D = torch.empty((n, n), **f32)
+    mask = torch.empty((n, n), dtype=torch.uint8, device="cuda")
+    removed_tf = gpu.dpi_tf_dev(Ad, D, tfs, 0.1, mask)
+    Dr, maskr = D[ri].cpu().numpy(), mask[ri].cpu().numpy()
+    assert removed_tf == int((D != Ad).sum().item()), "TF DPI removed count = changed entries"
+    del D, mask
+    _free()
+    Do, mo, _ = port.dpi_tf_rows(A, tfs, rows, 0.1)
+    assert np.array_equal(bits(Dr), bits(Do)), "TF DPI output rows"
+    assert np.array_equal(maskr, mo), "TF DPI mask rows"
 
     Cl = torch.empty((n, n), **f32)
     iters = gpu.closure_dev(Ad, Cl, 64)

@@ -66,3 +66,59 @@ def test_tf_bad_transition(gpu, built_lib):
     tfs = np.array([np.inf, -np.inf, np.inf, -np.inf], np.float32)
     with pytest.raises(built_lib.MCPGError):
         gpu.mcp_tf(A, tfs, 2, 2)
+
+
+def _mi_like(built_lib, gpu, n, m, seed):
+    """An MI matrix (the DPI's real input) with diagonal 0."""
+    X = built_lib.synth_grn(n, m, seed=seed)
+    A = gpu.bspline_mi(X, 10, 3, "bf16f8")
+    np.fill_diagonal(A, 0)
+    return A
+
+
+@pytest.mark.parametrize("n,frac", [(1100, 0.15), (1601, 0.3), (2100, 0.6)])
+@pytest.mark.parametrize("tol", [0.0, 0.1, 0.5])
+def test_two_phase_tf_dpi_on_mi_matrices(gpu, port, built_lib, n, frac, tol):
+    """Above 1,024 genes with at least 128 TFs the TF DPI runs in two phases on the
+    TF-first permutation of the matrix (a tiled max-min over the first min(512, t)
+    intermediates, then an early-exit scan of each undecided pair to its own end):
+    the same outputs, mask and removed count as the reference's dpi_tf_kernel loop.
+    The TF counts put t below and above the first phase's 512 intermediates."""
+    rng = np.random.default_rng(n + int(frac * 100))
+    A = _mi_like(built_lib, gpu, n, 400, seed=n)
+    tfs = _tf_vector(rng, n, frac)
+    assert (tfs > 0).sum() >= 128
+    out, mask, removed = gpu.dpi_tf(A, tfs, tol, want_mask=True)
+    oo, om, orem = port.dpi_tf(A, tfs, tol)
+    assert np.array_equal(bits(out), bits(oo))
+    assert np.array_equal(mask, om)
+    assert removed == orem
+
+
+def test_two_phase_tf_dpi_ties_nonsymmetric_and_general_tf_values(gpu, port):
+    """Many ties, a non-symmetric input, and a TF vector of arbitrary values (a gene
+    is a TF when its value is > 0, as in the reference)."""
+    rng = np.random.default_rng(35)
+    n = 1300
+    A = (rng.integers(0, 7, size=(n, n)) * 0.125).astype(np.float32)
+    A = np.maximum(A, A.T)
+    np.fill_diagonal(A, 0)
+    tfs = (rng.random(n) - 0.7).astype(np.float32)  # ~30 % positive, none infinite
+    for M in (A, (rng.random((n, n)) ** 3).astype(np.float32)):
+        out, mask, removed = gpu.dpi_tf(M, tfs, 0.1, want_mask=True)
+        oo, om, orem = port.dpi_tf(M, tfs, 0.1)
+        assert np.array_equal(bits(out), bits(oo)) and np.array_equal(mask, om) and removed == orem
+
+
+def test_two_phase_tf_dpi_falls_back_when_most_outputs_stay_undecided(gpu, port):
+    """tol = 0.999: almost nothing is deleted, the pending list overflows, and the
+    product form rewrites every output."""
+    rng = np.random.default_rng(36)
+    n = 1200
+    A = rng.random((n, n)).astype(np.float32)
+    A = np.maximum(A, A.T)
+    np.fill_diagonal(A, 0)
+    tfs = _tf_vector(rng, n, 0.25)
+    out, mask, removed = gpu.dpi_tf(A, tfs, 0.999, want_mask=True)
+    oo, om, orem = port.dpi_tf(A, tfs, 0.999)
+    assert np.array_equal(bits(out), bits(oo)) and np.array_equal(mask, om) and removed == orem
