@@ -782,25 +782,29 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1)
                         // g + 1 - NF) was waited for already, so the test sees its own phase
                         if (j == SUB - 1 && q + 1 < QT) ready = mbar_test(full0 + 8 * fs1, fph1);
                         if (j < ns) {
+                            // every operand of the slice from one descriptor: the start-address
+                            // field is addr >> 4 and all shared addresses stay below 2^18, so
+                            // desc(sl + off) == desc(sl) + off / 16 with no carry
+                            const uint64_t d0 = sdesc_sw128(sl);
                             if (corr) {
 #pragma unroll
                                 for (int k = 0; k < BK / 32; ++k) {
-                                    const uint64_t ah = sdesc_sw128(sl + 32 * k);
-                                    const uint64_t al = sdesc_sw128(sl + HL8_OFF + 32 * k);
-                                    const uint64_t bh = sdesc_sw128(sl + A_BYTES + 32 * k);
-                                    const uint64_t bl = sdesc_sw128(sl + A_BYTES + HL8_OFF + 32 * k);
+                                    const uint64_t ah = d0 + (uint64_t)((32 * k) >> 4);
+                                    const uint64_t al = d0 + (uint64_t)((HL8_OFF + 32 * k) >> 4);
+                                    const uint64_t bh = d0 + (uint64_t)((A_BYTES + 32 * k) >> 4);
+                                    const uint64_t bl = d0 + (uint64_t)((A_BYTES + HL8_OFF + 32 * k) >> 4);
                                     mma2_f8(dacc, ah, bl, args.idesc8, (q > 0 || j > 0 || k > 0) ? 1u : 0u);
                                     mma2_f8(dacc, al, bh, args.idesc8, 1u);
                                 }
                             } else {
 #pragma unroll
                                 for (int k = 0; k < BK / 16; ++k) {
-                                    const uint64_t ahi = sdesc_sw128(sl + 32 * k);
-                                    const uint64_t bhi = sdesc_sw128(sl + A_BYTES + 32 * k);
+                                    const uint64_t ahi = d0 + (uint64_t)((32 * k) >> 4);
+                                    const uint64_t bhi = d0 + (uint64_t)((A_BYTES + 32 * k) >> 4);
                                     mma2_f16(dacc, ahi, bhi, args.idesc, (F8C || q > 0 || j > 0 || k > 0) ? 1u : 0u);
                                     if (SPLIT) {
-                                        const uint64_t alo = sdesc_sw128(sl + HALF + 32 * k);
-                                        const uint64_t blo = sdesc_sw128(sl + HALF + A_BYTES + 32 * k);
+                                        const uint64_t alo = d0 + (uint64_t)((HALF + 32 * k) >> 4);
+                                        const uint64_t blo = d0 + (uint64_t)((HALF + A_BYTES + 32 * k) >> 4);
                                         mma2_f16(dacc, ahi, blo, args.idesc, 1u);
                                         mma2_f16(dacc, alo, bhi, args.idesc, 1u);
                                     }
