@@ -190,7 +190,7 @@ def reference_arm(args, ws, rank):
 # (kernel, precision, genes, samples, bins, order) -> (DRAM bytes per launch, how it was measured)
 MEASURED_TRAFFIC = {
     ("mi_tc", "bf16f8", 20000, 2000, 10, 3): (
-        44.49e9 + 1.61e9, "ncu dram__bytes_read.sum + dram__bytes_write.sum, one full-size launch, one pass"),
+        44.33e9 + 1.61e9, "ncu dram__bytes_read.sum + dram__bytes_write.sum, one full-size launch, one pass"),
 }
 
 
@@ -459,11 +459,30 @@ def gpu_arm(args, ws, rank, local):
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": info["threads"], "kind": sampler.kind,
                                 "sample": sampler.describe(info)}
     h.close()
+
+    # ---- the large single-GPU configuration, once (N = 1 only; not part of `value`) ----
+    if ws == 1 and not args.no_large:
+        sub = argparse.Namespace(**vars(args))
+        sub.genes, sub.samples, sub.mi_method = 32768, 4096, "bspline"
+        sub.no_eval, sub.closure, sub.split_iters, sub.no_cpu = True, False, 0, True
+        sub.tfs = 2048
+        pl = pipeline_run(sub, local)
+        line["large_pipeline"] = {
+            "workload": "32768 genes x 4096 samples: B-spline MI (%s), diagonal 0, MCP2/3/4 (M1 shared, ratios "
+                        "fused), DPI(0.1), TF MCP2/3/4, TF products and TF DPI(0.1) with 2048 seeded TFs; "
+                        "each stage timed once with CUDA events" % args.precision,
+            "stage_s": pl["stage_s"], "wall_s": pl["wall_s"], "stages": pl["stages"], "clocks": pl["clocks"]}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
 
 def pipeline_arm(args, ws, rank, local):
+    line = pipeline_run(args, local)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def pipeline_run(args, local):
     """The whole MCPNet compute core once, stage by stage (the large single-GPU
     configuration: 32,768 genes x 4,096 samples by default): B-spline MI
     (tensor cores), diagonal reset, the three max-min products with the
@@ -471,8 +490,8 @@ def pipeline_arm(args, ws, rank, local):
     max-capacity closure, then the gold-standard evaluation (AUPR / AUROC of
     the MI and MCP2 networks against the synthetic GRN's edges, every other
     pair a negative) and the ensemble coefficient search over a 35-row
-    coefficient grid, plain and Stouffer-transformed.  Prints one JSON line with per-stage times and
-    roofline fractions, and the reference CPU path's time on the host cores
+    coefficient grid, plain and Stouffer-transformed.  Returns one JSON object with per-stage
+    times and roofline fractions, and the reference CPU path's time on the host cores
     extrapolated from timed row slabs."""
     import torch
     import mcpnet_gb300 as M
@@ -715,8 +734,7 @@ def pipeline_arm(args, ws, rank, local):
                                           f"({mm_row_s:.3f} s/row); DPI counted as one symmetric product "
                                           "(an upper bound: the reference's DPI scan exits early)"}
     h.close()
-    if rank == 0:
-        print(json.dumps(line), flush=True)
+    return line
 
 
 def main(argv=None):
@@ -745,6 +763,8 @@ def main(argv=None):
     ap.add_argument("--no-maxmin", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-large", action="store_true",
+                    help="skip the one-off 32,768 x 4,096 pipeline leg of the default run")
     ap.add_argument("--pipeline", action="store_true",
                     help="run the whole compute core once, stage by stage (defaults to 32768 x 4096)")
     ap.add_argument("--closure", action="store_true", help="with --pipeline: add the max-capacity closure")
