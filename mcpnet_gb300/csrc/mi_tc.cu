@@ -74,8 +74,13 @@ constexpr int NPROD = MCPG_TC_PPROD;
 static_assert(NPROD >= 1 && NPROD <= 3, "producer threads per CTA");
 constexpr int PAIR_THREADS = 32 * (6 + NPROD - 1);
 // A-tile bytes of one rasterization group: 32 MB up to 2,048 samples, 16 MB beyond
-// (longer rows mean larger B tiles streaming past the group in L2).
-inline int64_t group_bytes(int64_t ldw) { return ldw <= 2048 ? (32ll << 20) : (16ll << 20); }
+// (longer rows mean larger B tiles streaming past the group in L2), 8 MB beyond for the
+// FP8-corrected form.  Measured at 32,768 x 4,096 on the 2-SM kernel (ms): bf16f8
+// 4 MB 610, 8 MB 595-610, 16 MB 653-660, 32 MB 677, 64 MB 673; BF16x3 8 MB 755,
+// 16 MB 725, 32 MB 740, 64 MB 748.
+inline int64_t group_bytes(int64_t ldw, int mode) {
+    return ldw <= 2048 ? (32ll << 20) : mode == TC_F8C ? (8ll << 20) : (16ll << 20);
+}
 constexpr uint32_t A_BYTES = MROWS * BK * 2;   // 16 KB
 constexpr uint32_t B_BYTES = NCOLS * BK * 2;   // 30 KB
 constexpr uint32_t HL8_OFF = 64;               // byte offset of L8 within an interleaved 128-byte row
@@ -1045,7 +1050,7 @@ cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, const uint8_t
     {
         const int64_t tile_bytes = (int64_t)MROWS * ldw * 2 * (mode == TC_SINGLE ? 1 : 2);
         int gi = 1;
-        while (gi < 64 && (int64_t)(2 * gi) * tile_bytes <= group_bytes(ldw)) gi *= 2;
+        while (gi < 64 && (int64_t)(2 * gi) * tile_bytes <= group_bytes(ldw, mode)) gi *= 2;
 #ifdef MCPG_TC_GI
         gi = MCPG_TC_GI;  // fixed group size (tuning builds)
 #endif
