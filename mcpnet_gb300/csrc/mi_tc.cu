@@ -558,6 +558,12 @@ __global__ void __launch_bounds__(192, 1)
 // accumulator-full barriers sit in both CTAs; accumulator-empty in the leader (8
 // arrivals: both CTAs' epilogue warps).
 constexpr uint32_t BH_BYTES = (NCOLS / 2) * BK * 2;   // 15 KB: half a B tile, 16-bit
+#ifndef MCPG_TC_PAIR_A_ROWS
+#define MCPG_TC_PAIR_A_ROWS 120
+#endif
+constexpr uint32_t PAIR_A_ROWS = MCPG_TC_PAIR_A_ROWS;   // A rows a pair CTA loads (its 12 genes)
+static_assert(PAIR_A_ROWS == GA * BINS || PAIR_A_ROWS == MROWS, "pair A box");
+constexpr uint32_t PAIR_A_TX = PAIR_A_ROWS * BK * 2;  // bytes of one A box
 
 __device__ __forceinline__ uint32_t cluster_rank() {
     uint32_t r;
@@ -640,6 +646,7 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1)
     constexpr uint32_t HALF = A_BYTES + BH_BYTES;                 // 31 KB
     constexpr uint32_t SLICE = (SPLIT ? 2 : 1) * HALF;
     constexpr uint32_t RING_BYTES = SLOTS * SLICE;
+    constexpr uint32_t SLICE_TX = (SPLIT ? 2 : 1) * (PAIR_A_TX + BH_BYTES);  // bytes one CTA loads per slice
     constexpr uint32_t PART_BYTES = GSUM_FLOATS * 4;  // per-gene bin sums of the epilogue
     // the MMA issuer waits once per stage (full, one arrival per slice), but every slice
     // is released on its own (empty, one commit per slice), so a slot refills while the
@@ -718,7 +725,7 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1)
                             if (leader) mbar_arrive(full0 + 8 * s);
                             continue;
                         }
-                        if (leader) mbar_expect_tx(full0 + 8 * s, 2u * SLICE);  // this slice of both CTAs
+                        if (leader) mbar_expect_tx(full0 + 8 * s, 2u * SLICE_TX);  // this slice of both CTAs
                         const uint32_t sl = base + (uint32_t)r * SLICE;
                         const int x = (kt0 + j) * BK;
                         if (corr) {  // H8|L8 of 64 samples: one 128-byte box row per operand row
@@ -1017,17 +1024,19 @@ cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, const uint8_t
     const int64_t rows = ((n * bins + 255) / 256) * 256 + 256;
     if (mode == TC_SPLIT16 && !Wlo) return cudaErrorNotSupported;
     if (mode == TC_F8C && !HL8) return cudaErrorNotSupported;
-    // A maps (128-row boxes) and B maps with b_rows-row boxes (240: whole B tile; 120: a pair's half)
+    // A maps with a_rows-row boxes (128: the 1-SM tile; 120: a pair CTA's 12 genes, the MMA's
+    // last 8 rows then hold stale shared memory and the epilogue drops them) and B maps with
+    // b_rows-row boxes (240: whole B tile; 120: a pair's half)
     CUtensorMap ma_hi, ma_lo, mb_hi, mb_lo, ma_l8, mb_l8;
-    auto make_maps = [&](uint32_t b_rows) -> bool {
-        if (!make_map(&ma_hi, Whi, fmt, rows, ldw, MROWS) || !make_map(&mb_hi, Whi, fmt, rows, ldw, b_rows))
+    auto make_maps = [&](uint32_t a_rows, uint32_t b_rows) -> bool {
+        if (!make_map(&ma_hi, Whi, fmt, rows, ldw, a_rows) || !make_map(&mb_hi, Whi, fmt, rows, ldw, b_rows))
             return false;
         ma_lo = ma_l8 = ma_hi;
         mb_lo = mb_l8 = mb_hi;
         if (mode == TC_SPLIT16)
-            return make_map(&ma_lo, Wlo, fmt, rows, ldw, MROWS) && make_map(&mb_lo, Wlo, fmt, rows, ldw, b_rows);
+            return make_map(&ma_lo, Wlo, fmt, rows, ldw, a_rows) && make_map(&mb_lo, Wlo, fmt, rows, ldw, b_rows);
         if (mode == TC_F8C)
-            return make_map_hl8(&ma_lo, HL8, rows, ldw, MROWS) && make_map_hl8(&mb_lo, HL8, rows, ldw, b_rows);
+            return make_map_hl8(&ma_lo, HL8, rows, ldw, a_rows) && make_map_hl8(&mb_lo, HL8, rows, ldw, b_rows);
         return true;
     };
     TcArgs a;
@@ -1056,7 +1065,7 @@ cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, const uint8_t
 #endif
         a.GI = gi < 4 ? 4 : gi;
     }
-    if (pair_form_enabled() && gene0 % (2 * GA) == 0 && make_maps(NCOLS / 2)) {
+    if (pair_form_enabled() && gene0 % (2 * GA) == 0 && make_maps(PAIR_A_ROWS, NCOLS / 2)) {
         // pair units: 24-gene A tiles; same group bytes (a pair tile is two A tiles)
         TcArgs p = a;
         p.TI = (int)((n + 2 * GA - 1) / (2 * GA));
@@ -1078,7 +1087,7 @@ cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, const uint8_t
             return e;
         }
     }
-    if (!make_maps(NCOLS)) return cudaErrorNotSupported;
+    if (!make_maps(MROWS, NCOLS)) return cudaErrorNotSupported;
     const int groups = (a.TIr + a.GI - 1) / a.GI;
     const int64_t n_slots = (int64_t)groups * a.GI * a.TJ;
     int sms = 0;
