@@ -99,6 +99,12 @@ int mi_launch(mcpg_handle* h, const MiPlan& pl, int64_t g0, int64_t g1) {
            "MI FP32 kernel");
         return MCPG_OK;
     }
+    // a whole-matrix launch packs its tiles and needs the edge scratch
+    void* strad = nullptr;
+    if (g0 == 0 && g1 == pl.n) {
+        int rc = scratch(h, S_STRAD, (size_t)mcpg::mi_tc_strad_floats(pl.n, pl.bins) * sizeof(float), &strad);
+        if (rc) return rc;
+    }
     cudaError_t e;
     {
         PROF(h, "mi_tc");
@@ -108,7 +114,7 @@ int mi_launch(mcpg_handle* h, const MiPlan& pl, int64_t g0, int64_t g1) {
         e = mcpg::launch_mi_tc((const uint16_t*)pl.w0, f8 ? nullptr : (const uint16_t*)pl.w1,
                                f8 ? (const uint8_t*)pl.w1 : nullptr, pl.ld, pl.H, pl.n, pl.m,
                                pl.bins, pl.fmt, pl.split, pl.MI, pl.ldmi, pl.flag, h->stream, &h->launches, g0, g1,
-                               hook);
+                               hook, (float*)strad);
     }
     if (e == cudaErrorNotSupported)
         return fail(h, MCPG_ERR_UNSUPPORTED, "bspline_mi tensor-core path: unsupported shape or device");
@@ -325,9 +331,11 @@ int mcpg_bspline_mi(mcpg_handle* h, const float* X, int64_t n, int64_t m, int64_
     // Row slabs of 48-gene multiples: once slab k has run, rows < its end are
     // final (row i's j >= i entries come from its own slab, the j < i ones are
     // mirrors written by earlier slabs), so their copy to the host overlaps
-    // the next slabs' compute on a second stream.
+    // the next slabs' compute on a second stream.  The tensor-core forms run one
+    // whole-matrix launch instead (its packed tiles give the bits the device and
+    // in-place paths give; gene-range launches keep 12-gene tiles).
     if (!h->copy_stream) CK(h, cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking), "create stream");
-    const int64_t nslab = n >= 48 * 16 ? 16 : 1;
+    const int64_t nslab = (n >= 48 * 16 && precision == MCPG_MI_FP32) ? 16 : 1;
     while ((int64_t)h->slab_events.size() < nslab) {
         cudaEvent_t e;
         CK(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "create event");

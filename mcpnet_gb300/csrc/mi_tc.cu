@@ -220,6 +220,11 @@ struct TcArgs {
     int* err;
     unsigned long long wait_ns;  // limit of every mbarrier wait
     int starve;                  // test hook: the producers issue no loads
+    // 2-SM form: weight rows per CTA tile (120 = 12 whole genes; 128 = packed, genes may
+    // straddle two tiles) and, packed, the straddling genes' partial sums per tile edge b:
+    // strad[(b * n + j) * 2 + part] (part 0 from the tile below the edge, 1 above)
+    int tile_rows;
+    float* strad;
 };
 
 __device__ __forceinline__ int j_min_for(int I) {
@@ -280,20 +285,22 @@ __device__ __forceinline__ bool tile_of(int64_t L, const TcArgs& a, int& I, int&
 // One tile's epilogue (warps 2-5, one accumulator row per thread): reads the
 // 128 x 240 accumulator at trow with tcgen05.ld, sums p*log2(p) per (row, B gene)
 // in FP32, hands the accumulator back through free_acc(), then forms
-// H_i + H_j - H_ij in FP64 for the tile's pairs (i in [gi0, gi0 + 12),
-// j in [gj0, gj0 + 24), j >= i) and stores both mirror entries.  The (n*bins)^2
-// joint table never leaves tensor memory.
-// The ten rows (bins) of an A gene are summed inside the warp by a segmented
-// shuffle reduction (a fixed tree order); only per-gene sums pass through shared
-// memory: gsum[0][gene][jl] for the part that starts at the gene's first row, and
-// gsum[1][gene][jl] for the rest of a gene that crosses a 32-row warp boundary.
-constexpr int GSUM_FLOATS = 2 * GA * GBN;  // 2.3 KB
-
-__device__ __forceinline__ bool gene_crosses_warps(int g) { return (BINS * g) / 32 != (BINS * g + BINS - 1) / 32; }
+// H_i + H_j - H_ij in FP64 for the tile's pairs (j in [gj0, gj0 + 24), j >= i) and
+// stores both mirror entries.  The (n*bins)^2 joint table never leaves tensor memory.
+// The tile holds weight rows [rowA, rowA + valid) (tile index `tile`); its genes are
+// those rows' genes.  The rows (bins) of a gene are summed inside the warp by a
+// segmented shuffle reduction (a fixed tree order); only per-gene sums pass through
+// shared memory: gsum[0][gene][jl] for the segment that starts at the gene's first
+// row, gsum[1][gene][jl] for a segment that starts at a warp's first row (the rest of
+// a gene that crosses a 32-row warp boundary, or a gene that began in the tile below).
+// A gene cut by a tile edge (packed tiles only) stores its partial sum in args.strad
+// for mi_straddle_kernel, which completes those entries.
+constexpr int NGMAX = 14;  // genes a 128-row tile touches at most
+constexpr int GSUM_FLOATS = 2 * NGMAX * GBN;  // 2.7 KB
 
 template <typename FreeAcc>
 __device__ __forceinline__ void epilogue_tile(uint32_t trow, float* gsum, int row, int etid, const TcArgs& args,
-                                              int64_t gi0, int64_t gj0, FreeAcc free_acc) {
+                                              int rowA, int valid, int tile, int gj0, FreeAcc free_acc) {
     float acc[GBN];
 #pragma unroll
     for (int q = 0; q < GBN; ++q) acc[q] = 0.0f;
@@ -313,11 +320,14 @@ __device__ __forceinline__ void epilogue_tile(uint32_t trow, float* gsum, int ro
     tc_fence_before();
     __syncwarp();
     free_acc();
-    const int lane = row & 31, gene = row / BINS;
-    const bool same1 = (lane + 1 < 32) && ((row + 1) / BINS == gene);
-    const bool same2 = (lane + 2 < 32) && ((row + 2) / BINS == gene);
-    const bool same4 = (lane + 4 < 32) && ((row + 4) / BINS == gene);
-    const bool same8 = (lane + 8 < 32) && ((row + 8) / BINS == gene);
+    const int lane = row & 31;
+    const int g0 = rowA / BINS;  // weight rows and genes fit in 32 bits
+    const int R = rowA + row;
+    const int gl = R / BINS - g0, bin = R % BINS;
+    const bool same1 = (lane + 1 < 32) && (bin + 1 < BINS);
+    const bool same2 = (lane + 2 < 32) && (bin + 2 < BINS);
+    const bool same4 = (lane + 4 < 32) && (bin + 4 < BINS);
+    const bool same8 = (lane + 8 < 32) && (bin + 8 < BINS);
 #pragma unroll
     for (int q = 0; q < GBN; ++q) {
         float a = acc[q], u;
@@ -331,21 +341,51 @@ __device__ __forceinline__ void epilogue_tile(uint32_t trow, float* gsum, int ro
         if (same8) a += u;
         acc[q] = a;
     }
-    if (gene < GA && (row % BINS == 0 || lane == 0)) {
-        float* dst = gsum + ((row % BINS == 0) ? 0 : GA * GBN) + gene * GBN;
+    if (row < valid && (bin == 0 || lane == 0)) {
+        float* dst = gsum + (bin == 0 ? 0 : NGMAX * GBN) + gl * GBN;
 #pragma unroll
         for (int q = 0; q < GBN; ++q) dst[q] = acc[q];
     }
     asm volatile("bar.sync 1, 128;" ::: "memory");
-    for (int p = etid; p < GA * GBN; p += 128) {
+    const int g_last = (rowA + valid - 1) / BINS;
+    for (int p = etid; p < NGMAX * GBN; p += 128) {
         const int il = p / GBN, jl = p - il * GBN;
-        const int64_t i = gi0 + il, j = gj0 + jl;
-        if (i >= args.n || j >= args.n || j < i) continue;
-        double sum = (double)gsum[il * GBN + jl];
-        if (gene_crosses_warps(il)) sum += (double)gsum[GA * GBN + il * GBN + jl];
+        const int64_t i = g0 + il, j = gj0 + jl;
+        if (i > g_last || i >= args.n || j >= args.n || j < i) continue;
+        const int r0 = BINS * (g0 + il) - rowA, r1 = r0 + BINS;  // the gene's rows, tile-relative
+        const bool starts_here = r0 >= 0, ends_here = r1 <= valid;
+        const int lo = starts_here ? r0 : 0, hi = ends_here ? r1 : valid;
+        double sum = (double)gsum[(starts_here ? 0 : NGMAX * GBN) + il * GBN + jl];
+        if (lo / 32 != (hi - 1) / 32) sum += (double)gsum[NGMAX * GBN + il * GBN + jl];
+        if (!starts_here || !ends_here) {  // cut by a tile edge: at most 9 rows here, one segment
+            if (args.strad)
+                args.strad[((int64_t)(starts_here ? tile + 1 : tile) * args.n + j) * 2 + (starts_here ? 0 : 1)] =
+                    (float)sum;
+            continue;
+        }
         const float val = (float)(args.H[i] + args.H[j] + sum);  // sum = -H_ij
         args.MI[i * args.ldmi + j] = val;
         args.MI[j * args.ldmi + i] = val;
+    }
+}
+
+// Completes the entries of the genes a packed tile edge cuts: edge b (weight row
+// b * tile_rows) splits gene i = b * tile_rows / 10 unless the row is a gene start;
+// MI[i][j] = MI[j][i] = H_i + H_j + (lower part + upper part) for j >= i, the same
+// FP64 combine as the epilogue's.
+__global__ void mi_straddle_kernel(const double* __restrict__ H, const float* __restrict__ strad, int64_t n,
+                                   int tile_rows, int64_t b0, int64_t b1, float* __restrict__ MI, int64_t ldmi) {
+    for (int64_t b = b0 + blockIdx.y; b < b1; b += gridDim.y) {
+        const int64_t r = b * tile_rows;
+        if (r % BINS == 0) continue;
+        const int64_t i = r / BINS;
+        if (i >= n) continue;
+        for (int64_t j = i + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+            const float2 s = *reinterpret_cast<const float2*>(strad + (b * n + j) * 2);
+            const float val = (float)(H[i] + H[j] + ((double)s.x + (double)s.y));
+            MI[i * ldmi + j] = val;
+            MI[j * ldmi + i] = val;
+        }
     }
 }
 
@@ -521,7 +561,7 @@ __global__ void __launch_bounds__(192, 1)
             asm volatile("bar.sync 1, 128;" ::: "memory");
             if (!got || *abort_flag) break;
             const uint32_t trow = tmem + (uint32_t)(ab * TMEM_COLS) + ((uint32_t)((warp & 3) * 32) << 16);
-            epilogue_tile(trow, part, row, etid, args, (int64_t)I * GA, (int64_t)J * GBN, [&] {
+            epilogue_tile(trow, part, row, etid, args, I * GA * BINS, GA * BINS, I, J * GBN, [&] {
                 if (lane == 0) mbar_arrive(tempty0 + 8 * ab);
             });
             ++t;
@@ -558,12 +598,9 @@ __global__ void __launch_bounds__(192, 1)
 // accumulator-full barriers sit in both CTAs; accumulator-empty in the leader (8
 // arrivals: both CTAs' epilogue warps).
 constexpr uint32_t BH_BYTES = (NCOLS / 2) * BK * 2;   // 15 KB: half a B tile, 16-bit
-#ifndef MCPG_TC_PAIR_A_ROWS
-#define MCPG_TC_PAIR_A_ROWS 120
+#ifndef MCPG_TC_PACKED
+#define MCPG_TC_PACKED 1
 #endif
-constexpr uint32_t PAIR_A_ROWS = MCPG_TC_PAIR_A_ROWS;   // A rows a pair CTA loads (its 12 genes)
-static_assert(PAIR_A_ROWS == GA * BINS || PAIR_A_ROWS == MROWS, "pair A box");
-constexpr uint32_t PAIR_A_TX = PAIR_A_ROWS * BK * 2;  // bytes of one A box
 
 __device__ __forceinline__ uint32_t cluster_rank() {
     uint32_t r;
@@ -624,6 +661,12 @@ __device__ __forceinline__ void mma2_commit_both(uint32_t bar) {
         : "memory");
 }
 
+// first B tile with some j >= i for pair tile IP (2 * tile_rows weight rows)
+__device__ __forceinline__ int pair_j_min(int IP, int tile_rows) {
+    const int64_t v = (int64_t)2 * IP * tile_rows / BINS - (GBN - 1);
+    return v <= 0 ? 0 : (int)((v + GBN - 1) / GBN);
+}
+
 // Pair tile (IP, J): groups of a.GI pair tiles, B tiles outer (as tile_of).
 __device__ __forceinline__ bool pair_tile_of(int64_t L, const TcArgs& a, int& IP, int& J) {
     const int64_t per_group = (int64_t)a.GI * a.TJ;
@@ -631,7 +674,7 @@ __device__ __forceinline__ bool pair_tile_of(int64_t L, const TcArgs& a, int& IP
     const int r = (int)(L - (int64_t)g * per_group);
     J = r / a.GI;
     IP = a.I0 + g * a.GI + (r - J * a.GI);
-    return IP < a.I0 + a.TIr && IP < a.TI && J >= IP;
+    return IP < a.I0 + a.TIr && IP < a.TI && J >= pair_j_min(IP, a.tile_rows);
 }
 
 // TcArgs in pair units: TI = pair tiles (24 genes), I0 / TIr = the launch's pair range.
@@ -646,7 +689,7 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1)
     constexpr uint32_t HALF = A_BYTES + BH_BYTES;                 // 31 KB
     constexpr uint32_t SLICE = (SPLIT ? 2 : 1) * HALF;
     constexpr uint32_t RING_BYTES = SLOTS * SLICE;
-    constexpr uint32_t SLICE_TX = (SPLIT ? 2 : 1) * (PAIR_A_TX + BH_BYTES);  // bytes one CTA loads per slice
+    const uint32_t slice_tx = (SPLIT ? 2u : 1u) * ((uint32_t)args.tile_rows * BK * 2u + BH_BYTES);  // per CTA
     constexpr uint32_t PART_BYTES = GSUM_FLOATS * 4;  // per-gene bin sums of the epilogue
     // the MMA issuer waits once per stage (full, one arrival per slice), but every slice
     // is released on its own (empty, one commit per slice), so a slot refills while the
@@ -705,7 +748,7 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1)
             for (int64_t L = c0; L < n_slots && ok; L += nc) {
                 int IP, J;
                 if (!pair_tile_of(L, args, IP, J)) continue;
-                const int rowA = (2 * IP + (int)rank) * GA * BINS;
+                const int rowA = (2 * IP + (int)rank) * args.tile_rows;
                 const int rowB = J * GBN * BINS + (int)rank * (NCOLS / 2);
                 for (int q = 0; q < QT && ok; ++q, ++g) {
                     const int s = (int)(g % NF);
@@ -725,7 +768,7 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1)
                             if (leader) mbar_arrive(full0 + 8 * s);
                             continue;
                         }
-                        if (leader) mbar_expect_tx(full0 + 8 * s, 2u * SLICE_TX);  // this slice of both CTAs
+                        if (leader) mbar_expect_tx(full0 + 8 * s, 2u * slice_tx);  // this slice of both CTAs
                         const uint32_t sl = base + (uint32_t)r * SLICE;
                         const int x = (kt0 + j) * BK;
                         if (corr) {  // H8|L8 of 64 samples: one 128-byte box row per operand row
@@ -849,7 +892,8 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1)
             asm volatile("bar.sync 1, 128;" ::: "memory");
             if (!got || *abort_flag) break;
             const uint32_t trow = tmem + (uint32_t)(ab * TMEM_COLS) + ((uint32_t)((warp & 3) * 32) << 16);
-            epilogue_tile(trow, part, row, etid, args, (int64_t)(2 * IP + (int)rank) * GA, (int64_t)J * GBN, [&] {
+            const int tile = 2 * IP + (int)rank;
+            epilogue_tile(trow, part, row, etid, args, tile * args.tile_rows, args.tile_rows, tile, J * GBN, [&] {
                 if (lane == 0) mbar_arrive_remote(te_leader + 8 * ab);
             });
             ++t;
@@ -1004,12 +1048,16 @@ static_assert((SUB1 == 1 || SUB1 == 2 || SUB1 == 4) && (SUB2 >= 1 && SUB2 <= 6) 
 #define MCPG_TC_PITCH_PAD 0
 #endif
 int64_t mi_tc_pitch(int64_t m) { return (m + BK - 1) / BK * BK + MCPG_TC_PITCH_PAD; }
+int64_t mi_tc_strad_floats(int64_t n, int bins) {
+    const int64_t tiles = 2 * ((n * bins + 2 * MROWS - 1) / (2 * MROWS));
+    return (tiles + 1) * n * 2;
+}
 
 // Whi/Wlo (16-bit) and HL8 (8-bit, 2 * ldw bytes per row): rows >= ceil(n*bins/256)*256
 // + 256 rows of ldw samples, zero beyond row n*bins and beyond sample m; ldw a multiple of 64.
 cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, const uint8_t* HL8, int64_t ldw, const double* H, int64_t n, int64_t m, int bins, int fmt, int mode, float* MI,
                          int64_t ldmi, int* timeout_flag, cudaStream_t stream, int64_t* launches, int64_t gene0,
-                         int64_t gene1, const TcWaitHook* hook) {
+                         int64_t gene1, const TcWaitHook* hook, float* strad) {
     if (bins != BINS || (ldw % BK) != 0) return cudaErrorNotSupported;
     if (mode != TC_SINGLE && mode != TC_SPLIT16 && mode != TC_F8C) return cudaErrorInvalidValue;
     if (mode == TC_F8C && fmt != 0) return cudaErrorInvalidValue;
@@ -1056,6 +1104,8 @@ cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, const uint8_t
     a.err = timeout_flag;
     a.wait_ns = hook ? hook->wait_ns : TC_WAIT_NS_DEFAULT;
     a.starve = hook ? hook->starve : 0;
+    a.tile_rows = GA * BINS;
+    a.strad = nullptr;
     {
         const int64_t tile_bytes = (int64_t)MROWS * ldw * 2 * (mode == TC_SINGLE ? 1 : 2);
         int gi = 1;
@@ -1065,12 +1115,26 @@ cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, const uint8_t
 #endif
         a.GI = gi < 4 ? 4 : gi;
     }
-    if (pair_form_enabled() && gene0 % (2 * GA) == 0 && make_maps(PAIR_A_ROWS, NCOLS / 2)) {
-        // pair units: 24-gene A tiles; same group bytes (a pair tile is two A tiles)
+    // 2-SM form.  A whole-matrix launch packs its A tiles: 128 weight rows per CTA, so no
+    // MMA row idles, and a gene may straddle two tiles (mi_straddle_kernel completes its
+    // entries from strad).  A launch over a gene range keeps 12-gene tiles of 120 rows
+    // (the MMA's last 8 rows then read stale shared memory and the epilogue drops them).
+    const bool packed = MCPG_TC_PACKED && strad != nullptr && gene0 == 0 && gene1 == n;
+    const int tile_rows = packed ? MROWS : GA * BINS;
+    if (pair_form_enabled() && (packed || gene0 % (2 * GA) == 0) && make_maps((uint32_t)tile_rows, NCOLS / 2)) {
+        // pair units: two A tiles; same group bytes
         TcArgs p = a;
-        p.TI = (int)((n + 2 * GA - 1) / (2 * GA));
-        p.I0 = (int)(gene0 / (2 * GA));
-        p.TIr = (int)((gene1 + 2 * GA - 1) / (2 * GA)) - p.I0;
+        p.tile_rows = tile_rows;
+        p.strad = packed ? strad : nullptr;
+        if (packed) {
+            p.TI = (int)((n * bins + 2 * tile_rows - 1) / (2 * tile_rows));
+            p.I0 = 0;
+            p.TIr = p.TI;
+        } else {
+            p.TI = (int)((n + 2 * GA - 1) / (2 * GA));
+            p.I0 = (int)(gene0 / (2 * GA));
+            p.TIr = (int)((gene1 + 2 * GA - 1) / (2 * GA)) - p.I0;
+        }
         p.GI = a.GI / 2 < 2 ? 2 : a.GI / 2;
         p.idesc = idesc_f16(fmt == 0 ? 1u : 0u, 2 * MROWS, NCOLS);
         p.idesc8 = idesc_f16(0u, 2 * MROWS, NCOLS);
@@ -1084,7 +1148,13 @@ cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, const uint8_t
             e = launch_pair<TC_SINGLE, SLOTS2, SUB2>(ma_hi, ma_lo, mb_hi, mb_lo, ma_l8, mb_l8, p, pslots, stream);
         if (e != cudaErrorNotSupported) {
             if (launches) ++*launches;
-            return e;
+            if (e != cudaSuccess || !packed) return e;
+            // the tile edges inside the matrix: rows b * tile_rows, b in [1, 2 TI)
+            const int64_t nb = 2 * (int64_t)p.TI;
+            const dim3 fg((unsigned)std::min<int64_t>((n + 255) / 256, 16), (unsigned)std::min<int64_t>(nb, 2048));
+            mi_straddle_kernel<<<fg, 256, 0, stream>>>(H, strad, n, tile_rows, 1, nb, MI, ldmi);
+            if (launches) ++*launches;
+            return cudaGetLastError();
         }
     }
     if (!make_maps(MROWS, NCOLS)) return cudaErrorNotSupported;

@@ -25,9 +25,12 @@ def same_bits(a, b):
     return np.array_equal(np.asarray(a, np.float32).view(np.uint32), np.asarray(b, np.float32).view(np.uint32))
 
 
-@pytest.mark.parametrize("precision", ["bf16x3", "fp32"])
-def test_pageable_in_place_matches_device(gpu, built_lib, precision):
-    X = built_lib.synth_grn(600, 700, seed=31)
+@pytest.mark.parametrize("precision", ["bf16x3", "bf16f8", "fp32"])
+@pytest.mark.parametrize("n", [600, 1000])
+def test_pageable_in_place_matches_device(gpu, built_lib, precision, n):
+    """1,000 genes take the staged path's row slabs (FP32) or its whole-matrix launch
+    (tensor-core forms, whose packed tiles must give the device path's bits)."""
+    X = built_lib.synth_grn(n, 700, seed=31)
     want = device_mi(gpu, X, precision)
     gpu.set_host_access("auto")
     got = gpu.bspline_mi(X, precision=precision)   # pageable X, fresh (untouched) np.empty output
