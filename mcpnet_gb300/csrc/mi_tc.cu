@@ -210,7 +210,7 @@ struct TcArgs {
     float* MI;
     int64_t ldmi;
     int64_t n;
-    int TI, TJ;        // A tiles (12 genes), B tiles (24 genes)
+    int TI, TJ;        // A tiles (1-SM: 12 genes; 2-SM: pair tiles of 2 * tile_rows rows), B tiles (24 genes)
     int GI;            // A tiles per rasterization group
     int I0, TIr;       // this launch covers A tiles [I0, I0 + TIr)
     int ktiles;        // K / 64
@@ -577,12 +577,13 @@ __global__ void __launch_bounds__(192, 1)
 
 // ---------------------------------------------------------------- 2-SM form
 // A cluster of two CTAs (an SM pair) runs cta_group::2 MMAs of M = 256: each CTA
-// holds its own A tile (12 genes, 128 rows) and HALF of the B tile (12 of its 24
+// holds its own A tile (tile_rows weight rows: 128 packed, or 12 genes) and HALF of the B tile (12 of its 24
 // genes, 120 rows); the MMA reads both CTAs' shared memory and writes each CTA's
 // 128 x 240 accumulator into that CTA's tensor memory.  Per SM and per 64
 // samples the stages carry 31 KB instead of 46 KB for the same MMA time, which
-// is what the L2 -> SM path sustains at the tensor pipe's rate.  Tiles are 24 x 24
-// genes (pair index IP over A, J over B; only J >= IP run).
+// is what the L2 -> SM path sustains at the tensor pipe's rate.  Pair tile IP covers
+// weight rows [2 IP tile_rows, 2 (IP + 1) tile_rows) (24 genes, or 25.6 packed), B tile J
+// genes [24 J, 24 J + 24); only pairs with some j >= i run (pair_j_min).
 //   leader (rank 0): warps 0 and 6 TMA for its halves (alternate slices), warp 1 the
 //                    MMA issuer, warps 2-5 epilogue
 //   peer   (rank 1): warps 0 and 6 TMA for its halves, warps 2-5 epilogue
