@@ -99,10 +99,10 @@ int mi_launch(mcpg_handle* h, const MiPlan& pl, int64_t g0, int64_t g1) {
            "MI FP32 kernel");
         return MCPG_OK;
     }
-    // a whole-matrix launch packs its tiles and needs the edge scratch
-    void* strad = nullptr;
-    if (g0 == 0 && g1 == pl.n) {
-        int rc = scratch(h, S_STRAD, (size_t)mcpg::mi_tc_strad_floats(pl.n, pl.bins) * sizeof(float), &strad);
+    // the 2-SM form's tile counters and (whole-matrix launch) edge partial sums
+    void* work = nullptr;
+    {
+        int rc = scratch(h, S_STRAD, (size_t)mcpg::mi_tc_work_bytes(pl.n, pl.bins), &work);
         if (rc) return rc;
     }
     cudaError_t e;
@@ -114,7 +114,7 @@ int mi_launch(mcpg_handle* h, const MiPlan& pl, int64_t g0, int64_t g1) {
         e = mcpg::launch_mi_tc((const uint16_t*)pl.w0, f8 ? nullptr : (const uint16_t*)pl.w1,
                                f8 ? (const uint8_t*)pl.w1 : nullptr, pl.ld, pl.H, pl.n, pl.m,
                                pl.bins, pl.fmt, pl.split, pl.MI, pl.ldmi, pl.flag, h->stream, &h->launches, g0, g1,
-                               hook, (float*)strad);
+                               hook, work);
     }
     if (e == cudaErrorNotSupported)
         return fail(h, MCPG_ERR_UNSUPPORTED, "bspline_mi tensor-core path: unsupported shape or device");

@@ -173,10 +173,11 @@ struct TcWaitHook {
 int64_t mi_tc_pitch(int64_t m);
 cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, const uint8_t* HL8, int64_t ldw, const double* H, int64_t n, int64_t m, int bins, int fmt, int mode, float* MI,
                          int64_t ldmi, int* timeout_flag, cudaStream_t stream, int64_t* launches, int64_t gene0 = 0,
-                         int64_t gene1 = -1, const TcWaitHook* hook = nullptr, float* strad = nullptr);
-// Floats of the strad scratch launch_mi_tc takes for a whole-matrix launch of n genes
-// (the partial sums of genes its packed tiles cut).
-int64_t mi_tc_strad_floats(int64_t n, int bins);
+                         int64_t gene1 = -1, const TcWaitHook* hook = nullptr, void* work = nullptr);
+// Bytes of the work area launch_mi_tc's 2-SM form takes for n genes (its tile
+// counters and, for a whole-matrix launch, the partial sums of the genes its packed
+// tiles cut); without it the 1-SM form runs.
+int64_t mi_tc_work_bytes(int64_t n, int bins);
 
 // ---------------- gold-standard evaluation (eval.cu) ----------------
 enum TruthMode : int {

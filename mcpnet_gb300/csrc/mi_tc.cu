@@ -73,6 +73,8 @@ constexpr int TMEM_COLS = 256;
 constexpr int NPROD = MCPG_TC_PPROD;
 static_assert(NPROD >= 1 && NPROD <= 3, "producer threads per CTA");
 constexpr int PAIR_THREADS = 32 * (6 + NPROD - 1);
+constexpr int TQ = 4;                   // tile ring entries (2-SM form)
+constexpr int TQ_CONS = 2 * NPROD + 8;  // ring readers: producers but the scheduler, the MMA issuer, 8 epilogue warps
 // A-tile bytes of one rasterization group: 32 MB up to 2,048 samples, 16 MB beyond
 // (longer rows mean larger B tiles streaming past the group in L2), 8 MB beyond for the
 // FP8-corrected form.  Measured at 32,768 x 4,096 on the 2-SM kernel (ms): bf16f8
@@ -225,6 +227,13 @@ struct TcArgs {
     // strad[(b * n + j) * 2 + part] (part 0 from the tile below the edge, 1 above)
     int tile_rows;
     float* strad;
+    // K steps of the last 64-sample slice that hold samples < m (16- and 32-sample MMAs);
+    // the rest multiply the zero padding and are skipped
+    int klast16, klast32;
+    // 2-SM form: one tile counter per rasterization group (zeroed before the launch);
+    // a cluster takes its next tile from the current group's counter, so all clusters
+    // work on neighbouring tiles
+    unsigned long long* sched;
 };
 
 __device__ __forceinline__ int j_min_for(int I) {
@@ -608,16 +617,6 @@ __device__ __forceinline__ uint32_t cluster_rank() {
     asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
     return r;
 }
-__device__ __forceinline__ uint32_t cluster_index() {
-    uint32_t r;
-    asm volatile("mov.u32 %0, %%clusterid.x;" : "=r"(r));
-    return r;
-}
-__device__ __forceinline__ uint32_t cluster_total() {
-    uint32_t r;
-    asm volatile("mov.u32 %0, %%nclusterid.x;" : "=r"(r));
-    return r;
-}
 // shared::cluster address of this CTA's shared variable at saddr, in CTA `rank`
 __device__ __forceinline__ uint32_t map_to_rank(uint32_t saddr, uint32_t rank) {
     uint32_t d;
@@ -662,21 +661,33 @@ __device__ __forceinline__ void mma2_commit_both(uint32_t bar) {
         : "memory");
 }
 
+__device__ __forceinline__ void st_cluster_u32(uint32_t cluster_addr, uint32_t v) {
+    asm volatile("st.shared::cluster.u32 [%0], %1;" ::"r"(cluster_addr), "r"(v) : "memory");
+}
+
 // first B tile with some j >= i for pair tile IP (2 * tile_rows weight rows)
 __device__ __forceinline__ int pair_j_min(int IP, int tile_rows) {
     const int64_t v = (int64_t)2 * IP * tile_rows / BINS - (GBN - 1);
     return v <= 0 ? 0 : (int)((v + GBN - 1) / GBN);
 }
 
-// Pair tile (IP, J): groups of a.GI pair tiles, B tiles outer (as tile_of).
-__device__ __forceinline__ bool pair_tile_of(int64_t L, const TcArgs& a, int& IP, int& J) {
-    const int64_t per_group = (int64_t)a.GI * a.TJ;
-    const int g = (int)(L / per_group);
-    const int r = (int)(L - (int64_t)g * per_group);
-    J = r / a.GI;
-    IP = a.I0 + g * a.GI + (r - J * a.GI);
-    return IP < a.I0 + a.TIr && IP < a.TI && J >= pair_j_min(IP, a.tile_rows);
+// Rasterization group g of the 2-SM form: pair tiles [ip0, ip0 + gi), B tiles
+// [js, TJ) outer; slot v is (IP, J) = (ip0 + v % gi, js + v / gi), a tile with some
+// j >= i unless IP's own first B tile lies above J (near the diagonal only).
+struct PairGroup {
+    int ip0, gi, js;
+    int64_t slots;
+};
+__device__ __forceinline__ PairGroup pair_group(const TcArgs& a, int g) {
+    PairGroup G;
+    G.ip0 = a.I0 + g * a.GI;
+    const int end = min(a.I0 + a.TIr, a.TI);
+    G.gi = min(a.GI, end - G.ip0);
+    G.js = pair_j_min(G.ip0, a.tile_rows);
+    G.slots = G.gi > 0 && a.TJ > G.js ? (int64_t)G.gi * (a.TJ - G.js) : 0;
+    return G;
 }
+
 
 // TcArgs in pair units: TI = pair tiles (24 genes), I0 / TIr = the launch's pair range.
 template <int MODE, int SLOTS, int SUB>
@@ -705,15 +716,23 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1)
     const uint32_t bars = base + RING_BYTES + PART_BYTES;
     const uint32_t full0 = bars, empty0 = bars + 8 * NF;
     const uint32_t tfull0 = empty0 + 8 * SLOTS, tempty0 = tfull0 + 16;
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(gbase + RING_BYTES + PART_BYTES + 8 * NF + 8 * SLOTS + 32);
+    // tile ring: the leader's scheduler thread publishes each tile it takes from the
+    // launch's counter into both CTAs (qfull: one arrival); every other role of both
+    // CTAs reads it and arrives on the leader's qempty (TQ_CONS arrivals); -1 ends
+    const uint32_t qfull0 = tempty0 + 16, qempty0 = qfull0 + 8 * TQ, qtiles = qempty0 + 8 * TQ;
+    volatile int32_t* qt = reinterpret_cast<volatile int32_t*>(gbase + (qtiles - base));
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(gbase + (qtiles + 4 * TQ - base));
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const uint32_t rank = cluster_rank();
     const bool leader = rank == 0;
-    const int64_t c0 = cluster_index(), nc = cluster_total();
     if (tid == 0) {
         for (int s = 0; s < NF; ++s) mbar_init(full0 + 8 * s, SUB);  // one arrival per slice
+        for (int s = 0; s < TQ; ++s) {
+            mbar_init(qfull0 + 8 * s, 1);
+            mbar_init(qempty0 + 8 * s, TQ_CONS);
+        }
         for (int r = 0; r < SLOTS; ++r) mbar_init(empty0 + 8 * r, 1);
         for (int b = 0; b < 2; ++b) {
             mbar_init(tfull0 + 8 * b, 1);
@@ -735,6 +754,17 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1)
     const int KT = args.ktiles;
     const int QP = (KT + SUB - 1) / SUB;
     const int QT = F8C ? 2 * QP : QP;
+    // ring entry k of the tile sequence: wait until published, read it, release it
+    auto take_tile = [&](int64_t k, int32_t& L) -> bool {
+        const int s = (int)(k % TQ);
+        if (!mbar_wait_cluster_abortable(qfull0 + 8 * s, (uint32_t)((k / TQ) & 1), args.err, abort_flag,
+                                         args.wait_ns))
+            return false;
+        L = qt[s];
+        if (leader) mbar_arrive(qempty0 + 8 * s);
+        else mbar_arrive_remote(map_to_rank(qempty0 + 8 * s, 0));
+        return true;
+    };
 
     if (warp == 0 || warp >= 6) {
         if (lane == 0) {
@@ -744,11 +774,46 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1)
             // 64-sample slices; two are fastest, measured against one and three).  A slice missing at the end of a pass (KT not a multiple of SUB) is a
             // bare arrival, so every stage takes SUB arrivals and every slot SUB commits a round.
             const int pid = warp == 0 ? 0 : warp - 5;
+            const bool scheduler = leader && pid == 0;
+            const int ngroups = (args.TIr + args.GI - 1) / args.GI;
+            int sg = 0;  // the scheduler's current group, and its next slot in flight
+            unsigned long long pend = (scheduler && ngroups > 0) ? atomicAdd(args.sched, 1ull) : 0ull;
             int64_t g = 0;  // stages issued by this CTA (every producer counts all of them)
-            bool ok = !args.starve;
-            for (int64_t L = c0; L < n_slots && ok; L += nc) {
-                int IP, J;
-                if (!pair_tile_of(L, args, IP, J)) continue;
+            bool ok = true;
+            for (int64_t k = 0; ok; ++k) {
+                int32_t L = -1;
+                if (scheduler) {
+                    // the next tile with some j >= i as (IP << 16) | J, or -1 past the end;
+                    // published to both CTAs
+                    while (sg < ngroups) {
+                        const PairGroup G = pair_group(args, sg);
+                        const unsigned long long v = pend;
+                        if ((int64_t)v >= G.slots) {  // this group is taken: the next one
+                            if (++sg < ngroups) pend = atomicAdd(args.sched + sg, 1ull);
+                            continue;
+                        }
+                        pend = atomicAdd(args.sched + sg, 1ull);  // in flight while this tile loads
+                        const int J = G.js + (int)(v / (unsigned)G.gi), IP = G.ip0 + (int)(v % (unsigned)G.gi);
+                        if (J >= pair_j_min(IP, args.tile_rows)) {
+                            L = (IP << 16) | J;
+                            break;
+                        }
+                    }
+                    const int s = (int)(k % TQ);
+                    const int64_t u = k / TQ;
+                    if (u > 0 && !(ok = mbar_wait_cluster_abortable(qempty0 + 8 * s, (uint32_t)((u - 1) & 1), args.err,
+                                                                    abort_flag, args.wait_ns)))
+                        break;
+                    qt[s] = L;
+                    st_cluster_u32(map_to_rank(qtiles + 4 * s, 1), (uint32_t)L);
+                    mbar_arrive(qfull0 + 8 * s);
+                    mbar_arrive_remote(map_to_rank(qfull0 + 8 * s, 1));
+                } else if (!(ok = take_tile(k, L))) {
+                    break;
+                }
+                if (L < 0) break;
+                if (args.starve) continue;  // test hook: no loads, the MMA issuer's first wait runs out
+                const int IP = L >> 16, J = L & 0xFFFF;
                 const int rowA = (2 * IP + (int)rank) * args.tile_rows;
                 const int rowB = J * GBN * BINS + (int)rank * (NCOLS / 2);
                 for (int q = 0; q < QT && ok; ++q, ++g) {
@@ -809,9 +874,9 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1)
             uint32_t fph = 0;      // phase parity of that full barrier
             bool ready = false;    // the current stage's full barrier was already seen complete
             bool ok = true;
-            for (int64_t L = c0; L < n_slots && ok; L += nc) {
-                int IP, J;
-                if (!pair_tile_of(L, args, IP, J)) continue;
+            for (int64_t k = 0; ok; ++k) {
+                int32_t L;
+                if (!(ok = take_tile(k, L)) || L < 0) break;
                 const int ab = (int)(t & 1);
                 const int64_t ua = t >> 1;
                 if (ua > 0 && !(ok = mbar_wait_cluster_abortable(tempty0 + 8 * ab, (uint32_t)((ua - 1) & 1),
@@ -842,9 +907,12 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1)
                             // field is addr >> 4 and all shared addresses stay below 2^18, so
                             // desc(sl + off) == desc(sl) + off / 16 with no carry
                             const uint64_t d0 = sdesc_sw128(sl);
+                            const bool last = kt0 + j == KT - 1;
+                            const int k32 = last ? args.klast32 : BK / 32, k16 = last ? args.klast16 : BK / 16;
                             if (corr) {
 #pragma unroll
                                 for (int k = 0; k < BK / 32; ++k) {
+                                    if (k >= k32) break;
                                     const uint64_t ah = d0 + (uint64_t)((32 * k) >> 4);
                                     const uint64_t al = d0 + (uint64_t)((HL8_OFF + 32 * k) >> 4);
                                     const uint64_t bh = d0 + (uint64_t)((A_BYTES + 32 * k) >> 4);
@@ -855,6 +923,7 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1)
                             } else {
 #pragma unroll
                                 for (int k = 0; k < BK / 16; ++k) {
+                                    if (k >= k16) break;
                                     const uint64_t ahi = d0 + (uint64_t)((32 * k) >> 4);
                                     const uint64_t bhi = d0 + (uint64_t)((A_BYTES + 32 * k) >> 4);
                                     mma2_f16(dacc, ahi, bhi, args.idesc, (F8C || q > 0 || j > 0 || k > 0) ? 1u : 0u);
@@ -884,9 +953,18 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1)
         const int etid = tid - 64;
         const uint32_t te_leader = map_to_rank(tempty0, 0);
         int64_t t = 0;
-        for (int64_t L = c0; L < n_slots; L += nc) {
-            int IP, J;
-            if (!pair_tile_of(L, args, IP, J)) continue;
+        for (int64_t k = 0;; ++k) {
+            // one ring read per warp (its lane 0), shared with the warp
+            int32_t L = -1;
+            bool gotq = true;
+            if (lane == 0) gotq = take_tile(k, L);
+            L = __shfl_sync(0xffffffffu, L, 0);
+            gotq = __shfl_sync(0xffffffffu, gotq ? 1 : 0, 0) != 0;
+            if (!gotq || L < 0) {
+                asm volatile("bar.sync 1, 128;" ::: "memory");
+                break;
+            }
+            const int IP = L >> 16, J = L & 0xFFFF;
             const int ab = (int)(t & 1);
             const bool got = mbar_wait_abortable(tfull0 + 8 * ab, (uint32_t)((t >> 1) & 1), args.err, abort_flag, args.wait_ns);
             tc_fence_after();
@@ -966,8 +1044,9 @@ cudaError_t launch_pair(const CUtensorMap& a0, const CUtensorMap& a1, const CUte
     constexpr uint32_t slice_bytes = (MODE == TC_SPLIT16 ? 2u : 1u) * (A_BYTES + BH_BYTES);
     constexpr int NF = (SLOTS + SUB - 1) / SUB;
     // ring, epilogue gene sums, full (per stage in flight) and empty (per slice) barriers,
-    // two accumulator barrier pairs, the tensor-memory slot and the abort flag
-    const size_t smem = 1024 + SLOTS * slice_bytes + GSUM_FLOATS * 4 + 8 * NF + 8 * SLOTS + 32 + 16;
+    // two accumulator barrier pairs, the tile ring (barriers and entries), the
+    // tensor-memory slot and the abort flag
+    const size_t smem = 1024 + SLOTS * slice_bytes + GSUM_FLOATS * 4 + 8 * NF + 8 * SLOTS + 32 + 20 * TQ + 16;
     cudaError_t e = cudaFuncSetAttribute(mi_tc_pair_kernel<MODE, SLOTS, SUB>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -1049,16 +1128,22 @@ static_assert((SUB1 == 1 || SUB1 == 2 || SUB1 == 4) && (SUB2 >= 1 && SUB2 <= 6) 
 #define MCPG_TC_PITCH_PAD 0
 #endif
 int64_t mi_tc_pitch(int64_t m) { return (m + BK - 1) / BK * BK + MCPG_TC_PITCH_PAD; }
-int64_t mi_tc_strad_floats(int64_t n, int bins) {
+// work: the group tile counters (one per rasterization group, at most one per pair
+// tile), then the packed launch's edge partial sums
+static int64_t work_counter_bytes(int64_t n, int bins) {
+    const int64_t pair_tiles = (n * bins + 2 * GA * BINS - 1) / (2 * GA * BINS) + 1;
+    return (pair_tiles * 8 + 255) / 256 * 256;
+}
+int64_t mi_tc_work_bytes(int64_t n, int bins) {
     const int64_t tiles = 2 * ((n * bins + 2 * MROWS - 1) / (2 * MROWS));
-    return (tiles + 1) * n * 2;
+    return work_counter_bytes(n, bins) + (tiles + 1) * n * 2 * (int64_t)sizeof(float);
 }
 
 // Whi/Wlo (16-bit) and HL8 (8-bit, 2 * ldw bytes per row): rows >= ceil(n*bins/256)*256
 // + 256 rows of ldw samples, zero beyond row n*bins and beyond sample m; ldw a multiple of 64.
 cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, const uint8_t* HL8, int64_t ldw, const double* H, int64_t n, int64_t m, int bins, int fmt, int mode, float* MI,
                          int64_t ldmi, int* timeout_flag, cudaStream_t stream, int64_t* launches, int64_t gene0,
-                         int64_t gene1, const TcWaitHook* hook, float* strad) {
+                         int64_t gene1, const TcWaitHook* hook, void* work) {
     if (bins != BINS || (ldw % BK) != 0) return cudaErrorNotSupported;
     if (mode != TC_SINGLE && mode != TC_SPLIT16 && mode != TC_F8C) return cudaErrorInvalidValue;
     if (mode == TC_F8C && fmt != 0) return cudaErrorInvalidValue;
@@ -1107,6 +1192,16 @@ cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, const uint8_t
     a.starve = hook ? hook->starve : 0;
     a.tile_rows = GA * BINS;
     a.strad = nullptr;
+    a.sched = nullptr;
+    {
+        const int64_t tail_samples = m - (int64_t)(a.ktiles - 1) * BK;  // 1..64
+        a.klast16 = (int)((tail_samples + 15) / 16);
+        a.klast32 = (int)((tail_samples + 31) / 32);
+#if defined(MCPG_TC_NO_PAD_SKIP)
+        a.klast16 = BK / 16;  // tuning builds: issue the padding's MMAs too
+        a.klast32 = BK / 32;
+#endif
+    }
     {
         const int64_t tile_bytes = (int64_t)MROWS * ldw * 2 * (mode == TC_SINGLE ? 1 : 2);
         int gi = 1;
@@ -1120,13 +1215,16 @@ cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, const uint8_t
     // MMA row idles, and a gene may straddle two tiles (mi_straddle_kernel completes its
     // entries from strad).  A launch over a gene range keeps 12-gene tiles of 120 rows
     // (the MMA's last 8 rows then read stale shared memory and the epilogue drops them).
-    const bool packed = MCPG_TC_PACKED && strad != nullptr && gene0 == 0 && gene1 == n;
+    float* strad = work ? reinterpret_cast<float*>(static_cast<char*>(work) + work_counter_bytes(n, bins)) : nullptr;
+    const bool packed = MCPG_TC_PACKED && work != nullptr && gene0 == 0 && gene1 == n;
     const int tile_rows = packed ? MROWS : GA * BINS;
-    if (pair_form_enabled() && (packed || gene0 % (2 * GA) == 0) && make_maps((uint32_t)tile_rows, NCOLS / 2)) {
+    if (pair_form_enabled() && work && (packed || gene0 % (2 * GA) == 0) &&
+        make_maps((uint32_t)tile_rows, NCOLS / 2)) {
         // pair units: two A tiles; same group bytes
         TcArgs p = a;
         p.tile_rows = tile_rows;
         p.strad = packed ? strad : nullptr;
+        p.sched = static_cast<unsigned long long*>(work);  // filled in below, once GI is known
         if (packed) {
             p.TI = (int)((n * bins + 2 * tile_rows - 1) / (2 * tile_rows));
             p.I0 = 0;
@@ -1137,6 +1235,9 @@ cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, const uint8_t
             p.TIr = (int)((gene1 + 2 * GA - 1) / (2 * GA)) - p.I0;
         }
         p.GI = a.GI / 2 < 2 ? 2 : a.GI / 2;
+        const int64_t ngroups = (p.TIr + p.GI - 1) / p.GI;
+        if (ngroups * 8 > work_counter_bytes(n, bins)) return cudaErrorInvalidValue;
+        if (cudaMemsetAsync(p.sched, 0, (size_t)ngroups * 8, stream) != cudaSuccess) return cudaGetLastError();
         p.idesc = idesc_f16(fmt == 0 ? 1u : 0u, 2 * MROWS, NCOLS);
         p.idesc8 = idesc_f16(0u, 2 * MROWS, NCOLS);
         const int64_t pslots = (int64_t)((p.TIr + p.GI - 1) / p.GI) * p.GI * p.TJ;
