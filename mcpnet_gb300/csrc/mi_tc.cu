@@ -75,13 +75,14 @@ static_assert(NPROD >= 1 && NPROD <= 3, "producer threads per CTA");
 constexpr int PAIR_THREADS = 32 * (6 + NPROD - 1);
 constexpr int TQ = 4;                   // tile ring entries (2-SM form)
 constexpr int TQ_CONS = 2 * NPROD + 8;  // ring readers: producers but the scheduler, the MMA issuer, 8 epilogue warps
-// A-tile bytes of one rasterization group: 32 MB up to 2,048 samples, 16 MB beyond
-// (longer rows mean larger B tiles streaming past the group in L2), 8 MB beyond for the
-// FP8-corrected form.  Measured at 32,768 x 4,096 on the 2-SM kernel (ms): bf16f8
-// 4 MB 610, 8 MB 595-610, 16 MB 653-660, 32 MB 677, 64 MB 673; BF16x3 8 MB 755,
-// 16 MB 725, 32 MB 740, 64 MB 748.
+// A-tile bytes of one rasterization group: 32 MB, except 16 MB beyond 2,048 samples
+// for the 16-bit forms.  Measured on the 2-SM kernel with dynamic tile scheduling
+// (ms): 20,000 x 2,000 bf16f8 16 / 32 / 64 MB 89.5 / 87.1 / 91.7, BF16x3 112.2 /
+// 110.3 / 114.5; 32,768 x 4,096 bf16f8 8 / 16 / 32 / 64 MB 519 / 496 / 485 / 499.
+// (With a fixed tile sequence per cluster the optimum at 32,768 x 4,096 was 8 MB for
+// bf16f8 and 16 MB for BF16x3.)
 inline int64_t group_bytes(int64_t ldw, int mode) {
-    return ldw <= 2048 ? (32ll << 20) : mode == TC_F8C ? (8ll << 20) : (16ll << 20);
+    return (ldw <= 2048 || mode == TC_F8C) ? (32ll << 20) : (16ll << 20);
 }
 constexpr uint32_t A_BYTES = MROWS * BK * 2;   // 16 KB
 constexpr uint32_t B_BYTES = NCOLS * BK * 2;   // 30 KB
