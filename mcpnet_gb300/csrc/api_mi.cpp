@@ -99,7 +99,7 @@ int mi_launch(mcpg_handle* h, const MiPlan& pl, int64_t g0, int64_t g1) {
            "MI FP32 kernel");
         return MCPG_OK;
     }
-    // the 2-SM form's tile counters and (whole-matrix launch) edge partial sums
+    // the 2-SM form's tile counters
     void* work = nullptr;
     {
         int rc = scratch(h, S_STRAD, (size_t)mcpg::mi_tc_work_bytes(pl.n, pl.bins), &work);

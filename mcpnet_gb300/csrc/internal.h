@@ -175,8 +175,7 @@ cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, const uint8_t
                          int64_t ldmi, int* timeout_flag, cudaStream_t stream, int64_t* launches, int64_t gene0 = 0,
                          int64_t gene1 = -1, const TcWaitHook* hook = nullptr, void* work = nullptr);
 // Bytes of the work area launch_mi_tc's 2-SM form takes for n genes (its tile
-// counters and, for a whole-matrix launch, the partial sums of the genes its packed
-// tiles cut); without it the 1-SM form runs.
+// counters); without it the 1-SM form runs.
 int64_t mi_tc_work_bytes(int64_t n, int bins);
 
 // ---------------- gold-standard evaluation (eval.cu) ----------------

@@ -213,7 +213,7 @@ struct TcArgs {
     float* MI;
     int64_t ldmi;
     int64_t n;
-    int TI, TJ;        // A tiles (1-SM: 12 genes; 2-SM: pair tiles of 2 * tile_rows rows), B tiles (24 genes)
+    int TI, TJ;        // A tiles (1-SM: 12 genes; 2-SM: pair tiles of pair_rows rows), B tiles (24 genes)
     int GI;            // A tiles per rasterization group
     int I0, TIr;       // this launch covers A tiles [I0, I0 + TIr)
     int ktiles;        // K / 64
@@ -223,11 +223,11 @@ struct TcArgs {
     int* err;
     unsigned long long wait_ns;  // limit of every mbarrier wait
     int starve;                  // test hook: the producers issue no loads
-    // 2-SM form: weight rows per CTA tile (120 = 12 whole genes; 128 = packed, genes may
-    // straddle two tiles) and, packed, the straddling genes' partial sums per tile edge b:
-    // strad[(b * n + j) * 2 + part] (part 0 from the tile below the edge, 1 above)
-    int tile_rows;
-    float* strad;
+    // 2-SM form: weight rows of a pair tile (240: 24 genes, 120 per CTA; 250: 25 genes,
+    // rows [0, 128) for rank 0 and [128, 250) for rank 1, so gene 12 of the pair is cut
+    // at row 128 and rank 1 hands its two rows' sums to rank 0 through shared memory)
+    // and the first row of rank 1's tile
+    int pair_rows, rank1_row;
     // K steps of the last 64-sample slice that hold samples < m (16- and 32-sample MMAs);
     // the rest multiply the zero padding and are skipped
     int klast16, klast32;
@@ -303,14 +303,22 @@ __device__ __forceinline__ bool tile_of(int64_t L, const TcArgs& a, int& I, int&
 // shared memory: gsum[0][gene][jl] for the segment that starts at the gene's first
 // row, gsum[1][gene][jl] for a segment that starts at a warp's first row (the rest of
 // a gene that crosses a 32-row warp boundary, or a gene that began in the tile below).
-// A gene cut by a tile edge (packed tiles only) stores its partial sum in args.strad
-// for mi_straddle_kernel, which completes those entries.
+// In a 25-gene pair tile, gene 12 is cut at the ranks' boundary: rank 1 (role SEND)
+// stores its part of that gene's sums into rank 0's exchange buffer and arrives on
+// rank 0's barrier; rank 0 (role RECV) waits for it and writes the gene's entries.
 constexpr int NGMAX = 14;  // genes a 128-row tile touches at most
 constexpr int GSUM_FLOATS = 2 * NGMAX * GBN;  // 2.7 KB
+constexpr int XSLOTS = 4;  // exchange slots (tile parity mod 4: rank 1 runs at most two tiles ahead)
+struct Exchange {
+    int role = 0;                 // 0: none, 1: RECV (rank 0), 2: SEND (rank 1)
+    uint32_t buf0 = 0, bar0 = 0;  // this CTA's slot buffers (XSLOTS x GBN floats) and barriers (shared addresses)
+    int64_t use = 0;              // the tile's exchange number: slot use % XSLOTS, phase (use / XSLOTS) & 1
+};
 
 template <typename FreeAcc>
 __device__ __forceinline__ void epilogue_tile(uint32_t trow, float* gsum, int row, int etid, const TcArgs& args,
-                                              int rowA, int valid, int tile, int gj0, FreeAcc free_acc) {
+                                              int rowA, int valid, int gj0, const Exchange& xc,
+                                              volatile int* abort_flag, FreeAcc free_acc) {
     float acc[GBN];
 #pragma unroll
     for (int q = 0; q < GBN; ++q) acc[q] = 0.0f;
@@ -357,6 +365,27 @@ __device__ __forceinline__ void epilogue_tile(uint32_t trow, float* gsum, int ro
         for (int q = 0; q < GBN; ++q) dst[q] = acc[q];
     }
     asm volatile("bar.sync 1, 128;" ::: "memory");
+    // the addresses are formed only here, after the accumulator loads
+    const int xs = (int)(xc.use % XSLOTS);
+    const uint32_t xbuf = xc.buf0 + 4u * GBN * xs, xbar = xc.bar0 + 8u * xs;
+    if (xc.role == 2 && etid == 0) {
+        // this tile's first gene (the pair's cut gene): its rows here went to gsum[1][0]
+        uint32_t dbuf, dbar;
+        asm volatile("mapa.shared::cluster.u32 %0, %1, 0;" : "=r"(dbuf) : "r"(xbuf));
+        asm volatile("mapa.shared::cluster.u32 %0, %1, 0;" : "=r"(dbar) : "r"(xbar));
+#pragma unroll 1
+        for (int q = 0; q < GBN; ++q)
+            asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(dbuf + 4 * q), "f"(gsum[NGMAX * GBN + q]) : "memory");
+        asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(dbar) : "memory");
+    }
+    bool have_peer = true;
+    if (xc.role == 1) {
+        if (etid == 0 && !mbar_wait_cluster_abortable(xbar, (uint32_t)((xc.use / XSLOTS) & 1), args.err, abort_flag,
+                                                       args.wait_ns))
+            *abort_flag = 1;
+        asm volatile("bar.sync 1, 128;" ::: "memory");
+        have_peer = !*abort_flag;
+    }
     const int g_last = (rowA + valid - 1) / BINS;
     for (int p = etid; p < NGMAX * GBN; p += 128) {
         const int il = p / GBN, jl = p - il * GBN;
@@ -367,35 +396,16 @@ __device__ __forceinline__ void epilogue_tile(uint32_t trow, float* gsum, int ro
         const int lo = starts_here ? r0 : 0, hi = ends_here ? r1 : valid;
         double sum = (double)gsum[(starts_here ? 0 : NGMAX * GBN) + il * GBN + jl];
         if (lo / 32 != (hi - 1) / 32) sum += (double)gsum[NGMAX * GBN + il * GBN + jl];
-        if (!starts_here || !ends_here) {  // cut by a tile edge: at most 9 rows here, one segment
-            if (args.strad)
-                args.strad[((int64_t)(starts_here ? tile + 1 : tile) * args.n + j) * 2 + (starts_here ? 0 : 1)] =
-                    (float)sum;
-            continue;
+        if (!starts_here) continue;  // rank 1's part of the pair's cut gene: rank 0 writes it
+        if (!ends_here) {             // rank 0: the cut gene, plus rank 1's two rows
+            if (xc.role != 1 || !have_peer) continue;
+            float peer;
+            asm volatile("ld.shared.f32 %0, [%1];" : "=f"(peer) : "r"(xbuf + 4u * jl) : "memory");
+            sum += (double)peer;
         }
         const float val = (float)(args.H[i] + args.H[j] + sum);  // sum = -H_ij
         args.MI[i * args.ldmi + j] = val;
         args.MI[j * args.ldmi + i] = val;
-    }
-}
-
-// Completes the entries of the genes a packed tile edge cuts: edge b (weight row
-// b * tile_rows) splits gene i = b * tile_rows / 10 unless the row is a gene start;
-// MI[i][j] = MI[j][i] = H_i + H_j + (lower part + upper part) for j >= i, the same
-// FP64 combine as the epilogue's.
-__global__ void mi_straddle_kernel(const double* __restrict__ H, const float* __restrict__ strad, int64_t n,
-                                   int tile_rows, int64_t b0, int64_t b1, float* __restrict__ MI, int64_t ldmi) {
-    for (int64_t b = b0 + blockIdx.y; b < b1; b += gridDim.y) {
-        const int64_t r = b * tile_rows;
-        if (r % BINS == 0) continue;
-        const int64_t i = r / BINS;
-        if (i >= n) continue;
-        for (int64_t j = i + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
-            const float2 s = *reinterpret_cast<const float2*>(strad + (b * n + j) * 2);
-            const float val = (float)(H[i] + H[j] + ((double)s.x + (double)s.y));
-            MI[i * ldmi + j] = val;
-            MI[j * ldmi + i] = val;
-        }
     }
 }
 
@@ -571,7 +581,7 @@ __global__ void __launch_bounds__(192, 1)
             asm volatile("bar.sync 1, 128;" ::: "memory");
             if (!got || *abort_flag) break;
             const uint32_t trow = tmem + (uint32_t)(ab * TMEM_COLS) + ((uint32_t)((warp & 3) * 32) << 16);
-            epilogue_tile(trow, part, row, etid, args, I * GA * BINS, GA * BINS, I, J * GBN, [&] {
+            epilogue_tile(trow, part, row, etid, args, I * GA * BINS, GA * BINS, J * GBN, Exchange(), abort_flag, [&] {
                 if (lane == 0) mbar_arrive(tempty0 + 8 * ab);
             });
             ++t;
@@ -587,13 +597,13 @@ __global__ void __launch_bounds__(192, 1)
 
 // ---------------------------------------------------------------- 2-SM form
 // A cluster of two CTAs (an SM pair) runs cta_group::2 MMAs of M = 256: each CTA
-// holds its own A tile (tile_rows weight rows: 128 packed, or 12 genes) and HALF of the B tile (12 of its 24
+// holds its own A tile (128 or 122 weight rows of a 25-gene pair, or 12 genes) and HALF of the B tile (12 of its 24
 // genes, 120 rows); the MMA reads both CTAs' shared memory and writes each CTA's
 // 128 x 240 accumulator into that CTA's tensor memory.  Per SM and per 64
 // samples the stages carry 31 KB instead of 46 KB for the same MMA time, which
 // is what the L2 -> SM path sustains at the tensor pipe's rate.  Pair tile IP covers
-// weight rows [2 IP tile_rows, 2 (IP + 1) tile_rows) (24 genes, or 25.6 packed), B tile J
-// genes [24 J, 24 J + 24); only pairs with some j >= i run (pair_j_min).
+// weight rows [IP pair_rows, (IP + 1) pair_rows) (24 or 25 genes), B tile J genes
+// [24 J, 24 J + 24); only pairs with some j >= i run (pair_j_min).
 //   leader (rank 0): warps 0 and 6 TMA for its halves (alternate slices), warp 1 the
 //                    MMA issuer, warps 2-5 epilogue
 //   peer   (rank 1): warps 0 and 6 TMA for its halves, warps 2-5 epilogue
@@ -666,9 +676,9 @@ __device__ __forceinline__ void st_cluster_u32(uint32_t cluster_addr, uint32_t v
     asm volatile("st.shared::cluster.u32 [%0], %1;" ::"r"(cluster_addr), "r"(v) : "memory");
 }
 
-// first B tile with some j >= i for pair tile IP (2 * tile_rows weight rows)
-__device__ __forceinline__ int pair_j_min(int IP, int tile_rows) {
-    const int64_t v = (int64_t)2 * IP * tile_rows / BINS - (GBN - 1);
+// first B tile with some j >= i for pair tile IP (pair_rows weight rows, whole genes)
+__device__ __forceinline__ int pair_j_min(int IP, int pair_rows) {
+    const int64_t v = (int64_t)IP * pair_rows / BINS - (GBN - 1);
     return v <= 0 ? 0 : (int)((v + GBN - 1) / GBN);
 }
 
@@ -684,7 +694,7 @@ __device__ __forceinline__ PairGroup pair_group(const TcArgs& a, int g) {
     G.ip0 = a.I0 + g * a.GI;
     const int end = min(a.I0 + a.TIr, a.TI);
     G.gi = min(a.GI, end - G.ip0);
-    G.js = pair_j_min(G.ip0, a.tile_rows);
+    G.js = pair_j_min(G.ip0, a.pair_rows);
     G.slots = G.gi > 0 && a.TJ > G.js ? (int64_t)G.gi * (a.TJ - G.js) : 0;
     return G;
 }
@@ -702,8 +712,11 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1)
     constexpr uint32_t HALF = A_BYTES + BH_BYTES;                 // 31 KB
     constexpr uint32_t SLICE = (SPLIT ? 2 : 1) * HALF;
     constexpr uint32_t RING_BYTES = SLOTS * SLICE;
-    const uint32_t slice_tx = (SPLIT ? 2u : 1u) * ((uint32_t)args.tile_rows * BK * 2u + BH_BYTES);  // per CTA
-    constexpr uint32_t PART_BYTES = GSUM_FLOATS * 4;  // per-gene bin sums of the epilogue
+    // A box rows: 128 for 25-gene pair tiles (rank 1's last 6 rows are the next pair's), 120 for 24
+    const uint32_t a_box = args.rank1_row == GA * BINS ? GA * BINS : MROWS;
+    const uint32_t slice_tx = (SPLIT ? 2u : 1u) * (a_box * BK * 2u + BH_BYTES);  // per CTA
+    // per-gene bin sums of the epilogue, then the exchange slots of the pair's cut gene
+    constexpr uint32_t PART_BYTES = (GSUM_FLOATS + XSLOTS * GBN) * 4;
     // the MMA issuer waits once per stage (full, one arrival per slice), but every slice
     // is released on its own (empty, one commit per slice), so a slot refills while the
     // rest of the ring is consumed
@@ -722,7 +735,9 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1)
     // CTAs reads it and arrives on the leader's qempty (TQ_CONS arrivals); -1 ends
     const uint32_t qfull0 = tempty0 + 16, qempty0 = qfull0 + 8 * TQ, qtiles = qempty0 + 8 * TQ;
     volatile int32_t* qt = reinterpret_cast<volatile int32_t*>(gbase + (qtiles - base));
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(gbase + (qtiles + 4 * TQ - base));
+    const uint32_t xfull0 = qtiles + 4 * TQ;                      // exchange barriers (rank 0's used)
+    const uint32_t xbuf0 = base + RING_BYTES + GSUM_FLOATS * 4;   // exchange slots (XSLOTS x GBN floats)
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(gbase + (xfull0 + 8 * XSLOTS - base));
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -734,6 +749,7 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1)
             mbar_init(qfull0 + 8 * s, 1);
             mbar_init(qempty0 + 8 * s, TQ_CONS);
         }
+        for (int s = 0; s < XSLOTS; ++s) mbar_init(xfull0 + 8 * s, 1);  // rank 1's arrival
         for (int r = 0; r < SLOTS; ++r) mbar_init(empty0 + 8 * r, 1);
         for (int b = 0; b < 2; ++b) {
             mbar_init(tfull0 + 8 * b, 1);
@@ -795,7 +811,7 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1)
                         }
                         pend = atomicAdd(args.sched + sg, 1ull);  // in flight while this tile loads
                         const int J = G.js + (int)(v / (unsigned)G.gi), IP = G.ip0 + (int)(v % (unsigned)G.gi);
-                        if (J >= pair_j_min(IP, args.tile_rows)) {
+                        if (J >= pair_j_min(IP, args.pair_rows)) {
                             L = (IP << 16) | J;
                             break;
                         }
@@ -815,7 +831,7 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1)
                 if (L < 0) break;
                 if (args.starve) continue;  // test hook: no loads, the MMA issuer's first wait runs out
                 const int IP = L >> 16, J = L & 0xFFFF;
-                const int rowA = (2 * IP + (int)rank) * args.tile_rows;
+                const int rowA = IP * args.pair_rows + (int)rank * args.rank1_row;
                 const int rowB = J * GBN * BINS + (int)rank * (NCOLS / 2);
                 for (int q = 0; q < QT && ok; ++q, ++g) {
                     const int s = (int)(g % NF);
@@ -972,8 +988,16 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1)
             asm volatile("bar.sync 1, 128;" ::: "memory");
             if (!got || *abort_flag) break;
             const uint32_t trow = tmem + (uint32_t)(ab * TMEM_COLS) + ((uint32_t)((warp & 3) * 32) << 16);
-            const int tile = 2 * IP + (int)rank;
-            epilogue_tile(trow, part, row, etid, args, tile * args.tile_rows, args.tile_rows, tile, J * GBN, [&] {
+            Exchange xc;
+            if (args.rank1_row != GA * BINS) {  // 25-gene pair tile: gene 12 is cut at row 128
+                xc.role = leader ? 1 : 2;
+                xc.buf0 = xbuf0;
+                xc.bar0 = xfull0;
+                xc.use = t;
+            }
+            const int rowA = IP * args.pair_rows + (int)rank * args.rank1_row;
+            const int valid = rank ? args.pair_rows - args.rank1_row : args.rank1_row;
+            epilogue_tile(trow, part, row, etid, args, rowA, valid, J * GBN, xc, abort_flag, [&] {
                 if (lane == 0) mbar_arrive_remote(te_leader + 8 * ab);
             });
             ++t;
@@ -1047,7 +1071,8 @@ cudaError_t launch_pair(const CUtensorMap& a0, const CUtensorMap& a1, const CUte
     // ring, epilogue gene sums, full (per stage in flight) and empty (per slice) barriers,
     // two accumulator barrier pairs, the tile ring (barriers and entries), the
     // tensor-memory slot and the abort flag
-    const size_t smem = 1024 + SLOTS * slice_bytes + GSUM_FLOATS * 4 + 8 * NF + 8 * SLOTS + 32 + 20 * TQ + 16;
+    const size_t smem = 1024 + SLOTS * slice_bytes + (GSUM_FLOATS + XSLOTS * GBN) * 4 + 8 * NF + 8 * SLOTS + 32 +
+                        20 * TQ + 8 * XSLOTS + 16;
     cudaError_t e = cudaFuncSetAttribute(mi_tc_pair_kernel<MODE, SLOTS, SUB>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -1129,15 +1154,11 @@ static_assert((SUB1 == 1 || SUB1 == 2 || SUB1 == 4) && (SUB2 >= 1 && SUB2 <= 6) 
 #define MCPG_TC_PITCH_PAD 0
 #endif
 int64_t mi_tc_pitch(int64_t m) { return (m + BK - 1) / BK * BK + MCPG_TC_PITCH_PAD; }
-// work: the group tile counters (one per rasterization group, at most one per pair
-// tile), then the packed launch's edge partial sums
-static int64_t work_counter_bytes(int64_t n, int bins) {
+// work: the group tile counters of the 2-SM form (one per rasterization group, at most
+// one per pair tile)
+int64_t mi_tc_work_bytes(int64_t n, int bins) {
     const int64_t pair_tiles = (n * bins + 2 * GA * BINS - 1) / (2 * GA * BINS) + 1;
     return (pair_tiles * 8 + 255) / 256 * 256;
-}
-int64_t mi_tc_work_bytes(int64_t n, int bins) {
-    const int64_t tiles = 2 * ((n * bins + 2 * MROWS - 1) / (2 * MROWS));
-    return work_counter_bytes(n, bins) + (tiles + 1) * n * 2 * (int64_t)sizeof(float);
 }
 
 // Whi/Wlo (16-bit) and HL8 (8-bit, 2 * ldw bytes per row): rows >= ceil(n*bins/256)*256
@@ -1191,8 +1212,8 @@ cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, const uint8_t
     a.err = timeout_flag;
     a.wait_ns = hook ? hook->wait_ns : TC_WAIT_NS_DEFAULT;
     a.starve = hook ? hook->starve : 0;
-    a.tile_rows = GA * BINS;
-    a.strad = nullptr;
+    a.pair_rows = 2 * GA * BINS;
+    a.rank1_row = GA * BINS;
     a.sched = nullptr;
     {
         const int64_t tail_samples = m - (int64_t)(a.ktiles - 1) * BK;  // 1..64
@@ -1212,32 +1233,26 @@ cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, const uint8_t
 #endif
         a.GI = gi < 4 ? 4 : gi;
     }
-    // 2-SM form.  A whole-matrix launch packs its A tiles: 128 weight rows per CTA, so no
-    // MMA row idles, and a gene may straddle two tiles (mi_straddle_kernel completes its
-    // entries from strad).  A launch over a gene range keeps 12-gene tiles of 120 rows
-    // (the MMA's last 8 rows then read stale shared memory and the epilogue drops them).
-    float* strad = work ? reinterpret_cast<float*>(static_cast<char*>(work) + work_counter_bytes(n, bins)) : nullptr;
-    const bool packed = MCPG_TC_PACKED && work != nullptr && gene0 == 0 && gene1 == n;
-    const int tile_rows = packed ? MROWS : GA * BINS;
-    if (pair_form_enabled() && work && (packed || gene0 % (2 * GA) == 0) &&
-        make_maps((uint32_t)tile_rows, NCOLS / 2)) {
-        // pair units: two A tiles; same group bytes
+    // 2-SM form.  A whole-matrix launch takes pair tiles of 25 genes (250 weight rows:
+    // rank 0 rows [0, 128), rank 1 rows [128, 250), so only 6 of the 256 MMA rows idle and
+    // rank 1 hands its two rows of the pair's gene 12 to rank 0).  A launch over a gene
+    // range keeps 24-gene pair tiles of 120 rows per CTA (the MMA's last 8 rows then read
+    // stale shared memory and the epilogue drops them).
+    const bool wide = MCPG_TC_PACKED && gene0 == 0 && gene1 == n;
+    const int pair_rows = wide ? 25 * BINS : 2 * GA * BINS, rank1_row = wide ? MROWS : GA * BINS;
+    if (pair_form_enabled() && work && (wide || gene0 % (2 * GA) == 0) &&
+        make_maps((uint32_t)(wide ? MROWS : GA * BINS), NCOLS / 2)) {
         TcArgs p = a;
-        p.tile_rows = tile_rows;
-        p.strad = packed ? strad : nullptr;
-        p.sched = static_cast<unsigned long long*>(work);  // filled in below, once GI is known
-        if (packed) {
-            p.TI = (int)((n * bins + 2 * tile_rows - 1) / (2 * tile_rows));
-            p.I0 = 0;
-            p.TIr = p.TI;
-        } else {
-            p.TI = (int)((n + 2 * GA - 1) / (2 * GA));
-            p.I0 = (int)(gene0 / (2 * GA));
-            p.TIr = (int)((gene1 + 2 * GA - 1) / (2 * GA)) - p.I0;
-        }
+        p.pair_rows = pair_rows;
+        p.rank1_row = rank1_row;
+        p.sched = static_cast<unsigned long long*>(work);  // one counter per group, zeroed below
+        const int genes_per_pair = pair_rows / BINS;
+        p.TI = (int)((n + genes_per_pair - 1) / genes_per_pair);
+        p.I0 = (int)(gene0 / genes_per_pair);
+        p.TIr = (int)((gene1 + genes_per_pair - 1) / genes_per_pair) - p.I0;
         p.GI = a.GI / 2 < 2 ? 2 : a.GI / 2;
         const int64_t ngroups = (p.TIr + p.GI - 1) / p.GI;
-        if (ngroups * 8 > work_counter_bytes(n, bins)) return cudaErrorInvalidValue;
+        if (ngroups * 8 > mi_tc_work_bytes(n, bins)) return cudaErrorInvalidValue;
         if (cudaMemsetAsync(p.sched, 0, (size_t)ngroups * 8, stream) != cudaSuccess) return cudaGetLastError();
         p.idesc = idesc_f16(fmt == 0 ? 1u : 0u, 2 * MROWS, NCOLS);
         p.idesc8 = idesc_f16(0u, 2 * MROWS, NCOLS);
@@ -1251,13 +1266,7 @@ cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, const uint8_t
             e = launch_pair<TC_SINGLE, SLOTS2, SUB2>(ma_hi, ma_lo, mb_hi, mb_lo, ma_l8, mb_l8, p, pslots, stream);
         if (e != cudaErrorNotSupported) {
             if (launches) ++*launches;
-            if (e != cudaSuccess || !packed) return e;
-            // the tile edges inside the matrix: rows b * tile_rows, b in [1, 2 TI)
-            const int64_t nb = 2 * (int64_t)p.TI;
-            const dim3 fg((unsigned)std::min<int64_t>((n + 255) / 256, 16), (unsigned)std::min<int64_t>(nb, 2048));
-            mi_straddle_kernel<<<fg, 256, 0, stream>>>(H, strad, n, tile_rows, 1, nb, MI, ldmi);
-            if (launches) ++*launches;
-            return cudaGetLastError();
+            return e;
         }
     }
     if (!make_maps(MROWS, NCOLS)) return cudaErrorNotSupported;
