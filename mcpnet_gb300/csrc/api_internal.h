@@ -89,7 +89,7 @@ enum Slot {
     S_SP_CNT,    // split evaluation: subset counters
     S_SP_ST,     // split evaluation: Stouffer scores of every coefficient row at the entries
     S_DPI_PEND,  // two-phase DPI: outputs the first phase left undecided
-    S_STRAD,     // tensor-core MI: the 2-SM form's tile counters
+    S_TCWORK,    // tensor-core MI: the 2-SM form's tile counters
     NSLOTS
 };
 

@@ -102,7 +102,7 @@ int mi_launch(mcpg_handle* h, const MiPlan& pl, int64_t g0, int64_t g1) {
     // the 2-SM form's tile counters
     void* work = nullptr;
     {
-        int rc = scratch(h, S_STRAD, (size_t)mcpg::mi_tc_work_bytes(pl.n, pl.bins), &work);
+        int rc = scratch(h, S_TCWORK, (size_t)mcpg::mi_tc_work_bytes(pl.n, pl.bins), &work);
         if (rc) return rc;
     }
     cudaError_t e;
