@@ -1134,7 +1134,10 @@ cudaError_t launch_mode(const CUtensorMap& a0, const CUtensorMap& a1, const CUte
 // 60.7, 2 x 3 112.0 / 54.1, 3 x 2 107.0 / 52.2 (BF16 split: 1-SM 139.4, 2-SM 131.6).
 // With per-slice release, two producers and the 2.3 KB epilogue (2-SM ring slots /
 // slices per stage): 6 / 3 89.8 / 46.4, 7 / 3 104.1 / 48.2, 7 / 2 105.7 / 50.2,
-// 7 / 1 115.4 / 55.3, 6 / 2 106.2 / 51.3; 1-SM 101.5 / 52.1.
+// 7 / 1 115.4 / 55.3, 6 / 2 106.2 / 51.3; 1-SM 101.5 / 52.1.  The 7-slot ring lost then
+// because clusters drifted apart and L2 reuse collapsed (461 GB of DRAM reads per launch);
+// with dynamic tile scheduling it wins: bf16f8 6 / 7 slots 88.7 / 86.9 ms at 20,000 x
+// 2,000 and 488 / 457 ms at 32,768 x 4,096.
 #ifndef MCPG_TC_SUB
 #define MCPG_TC_SUB 1
 #endif
@@ -1142,7 +1145,7 @@ cudaError_t launch_mode(const CUtensorMap& a0, const CUtensorMap& a1, const CUte
 #define MCPG_TC_PSUB 3
 #endif
 #ifndef MCPG_TC_PSLOTS
-#define MCPG_TC_PSLOTS 6
+#define MCPG_TC_PSLOTS 7
 #endif
 constexpr int SUB1 = MCPG_TC_SUB, SUB2 = MCPG_TC_PSUB, SLOTS2 = MCPG_TC_PSLOTS;
 static_assert((SUB1 == 1 || SUB1 == 2 || SUB1 == 4) && (SUB2 >= 1 && SUB2 <= 6) && SLOTS2 >= SUB2 && SLOTS2 <= 7,
