@@ -24,7 +24,11 @@
 // issuing thread a few hundred cycles, and four 64-byte boxes per slice had made
 // the correction pass the producer's bottleneck.
 //
-// CTA tile: A = 12 genes (120 of the 128 MMA rows), B = 24 genes (N = 240);
+// The default is the 2-SM form (mi_tc_pair_kernel, below): clusters of two CTAs
+// running tcgen05.mma.cta_group::2 on 25-gene pair tiles, fed by a 7-slice ring and
+// scheduled dynamically from per-group tile counters.  The 1-SM form described here
+// runs when no cluster of two fits (or MCPG_TC_FORM=1sm).
+// 1-SM CTA tile: A = 12 genes (120 of the 128 MMA rows), B = 24 genes (N = 240);
 // D = 128 x 240 FP32 in tensor memory (256 columns allocated).
 //   warp 0 / one lane : TMA producer (cp.async.bulk.tensor, 128B swizzle, 64-sample slices)
 //   warp 1 / one lane : tcgen05.mma issuer (kind::f16 K=16 / kind::f8f6f4 K=32, M=128, N=240)
@@ -604,7 +608,8 @@ __global__ void __launch_bounds__(192, 1)
 // is what the L2 -> SM path sustains at the tensor pipe's rate.  Pair tile IP covers
 // weight rows [IP pair_rows, (IP + 1) pair_rows) (24 or 25 genes), B tile J genes
 // [24 J, 24 J + 24); only pairs with some j >= i run (pair_j_min).
-//   leader (rank 0): warps 0 and 6 TMA for its halves (alternate slices), warp 1 the
+//   leader (rank 0): warps 0 and 6 TMA for its halves (alternate slices; warp 0's lane 0
+//                    also takes the tiles and publishes them to both CTAs), warp 1 the
 //                    MMA issuer, warps 2-5 epilogue
 //   peer   (rank 1): warps 0 and 6 TMA for its halves, warps 2-5 epilogue
 // The ring holds SLOTS slices; a stage is SUB consecutive slices (slot (stage*SUB + j)
