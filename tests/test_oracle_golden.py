@@ -380,3 +380,34 @@ def test_dpi_rows_equal_the_full_filter(port):
         assert np.array_equal(ro.view(np.uint32), out[rows].view(np.uint32))
         assert np.array_equal(rm, mask[rows])
         assert rr == int((out[rows] != A[rows]).sum())
+
+
+@pytest.mark.parametrize("n,frac,tol", [(60, 0.3, 0.1), (75, 0.1, 0.0), (64, 0.9, 0.5)])
+def test_dpi_tf_on_tf_first_permutation(port, n, frac, tol):
+    """The GPU's two-phase TF DPI decides on B = P A P^T with the t TFs first: a pair of
+    one TF and one non-TF admits the intermediates y < t of B, any other pair all y; the
+    x, z exclusion is B's diagonal.  Restated here in numpy and compared with the oracle's
+    dpi_tf_kernel loop (dpi.hpp:74-110), which scans A's own order with its TF test."""
+    rng = np.random.default_rng(n)
+    A = (rng.integers(0, 9, size=(n, n)) * 0.125).astype(np.float32)  # ties
+    A = np.maximum(A, A.T)
+    np.fill_diagonal(A, 0)
+    tfs = np.where(rng.random(n) < frac, np.float32(np.inf), np.float32(-np.inf))
+    is_tf = tfs > 0
+    perm = np.concatenate([np.flatnonzero(is_tf), np.flatnonzero(~is_tf)])
+    t = int(is_tf.sum())
+    B = A[perm][:, perm]
+    tm = np.float32(1.0 / (1.0 - np.float64(np.float32(tol))))
+    mask = np.zeros((n, n), dtype=np.uint8)
+    for xp in range(n):
+        for zp in range(n):
+            x, z = perm[xp], perm[zp]
+            if xp == zp:
+                mask[x, z] = 1
+                continue
+            end = t if (xp < t) != (zp < t) else n
+            ys = np.array([y for y in range(end) if y != xp and y != zp], dtype=np.int64)
+            thr = np.float32(A[x, z] * tm)
+            mask[x, z] = 1 if ys.size and np.minimum(B[xp, ys], B[zp, ys]).max() >= thr else 0
+    _, om, _ = port.dpi_tf(A, tfs, tol)
+    assert np.array_equal(mask, om)
