@@ -624,8 +624,8 @@ __global__ void __launch_bounds__(192, 1)
 // accumulator-full barriers sit in both CTAs; accumulator-empty in the leader (8
 // arrivals: both CTAs' epilogue warps).
 constexpr uint32_t BH_BYTES = (NCOLS / 2) * BK * 2;   // 15 KB: half a B tile, 16-bit
-#ifndef MCPG_TC_PACKED
-#define MCPG_TC_PACKED 1
+#ifndef MCPG_TC_PAIR25
+#define MCPG_TC_PAIR25 1  // whole-matrix launches on 25-gene pair tiles (0: 24-gene pairs)
 #endif
 
 __device__ __forceinline__ uint32_t cluster_rank() {
@@ -1246,10 +1246,10 @@ cudaError_t launch_mi_tc(const uint16_t* Whi, const uint16_t* Wlo, const uint8_t
     // rank 1 hands its two rows of the pair's gene 12 to rank 0).  A launch over a gene
     // range keeps 24-gene pair tiles of 120 rows per CTA (the MMA's last 8 rows then read
     // stale shared memory and the epilogue drops them).
-    const bool wide = MCPG_TC_PACKED && gene0 == 0 && gene1 == n;
-    const int pair_rows = wide ? 25 * BINS : 2 * GA * BINS, rank1_row = wide ? MROWS : GA * BINS;
-    if (pair_form_enabled() && work && (wide || gene0 % (2 * GA) == 0) &&
-        make_maps((uint32_t)(wide ? MROWS : GA * BINS), NCOLS / 2)) {
+    const bool pair25 = MCPG_TC_PAIR25 && gene0 == 0 && gene1 == n;
+    const int pair_rows = pair25 ? 25 * BINS : 2 * GA * BINS, rank1_row = pair25 ? MROWS : GA * BINS;
+    if (pair_form_enabled() && work && (pair25 || gene0 % (2 * GA) == 0) &&
+        make_maps((uint32_t)(pair25 ? MROWS : GA * BINS), NCOLS / 2)) {
         TcArgs p = a;
         p.pair_rows = pair_rows;
         p.rank1_row = rank1_row;
